@@ -1,0 +1,210 @@
+// gb_internal.cuh -- shared definitions of the GB300 greedy sparse-recovery library.
+//
+// Layout in HBM (per solve workspace):
+//   dense A   column-major, leading dimension lda (a multiple of 4 floats when the library
+//             owns the copy, so every column starts 16-byte aligned for float4 streams)
+//   vectors   x, x_thres, grad, grad_prev, grad_prev_thres (n); y, resid, resid_update (m,
+//             padded to lda with zeros); bins, bins_prev (n int32); counters (num_bins int32)
+//   support   S = ascending list of indices with bin <= k_bin (rebuilt at each binning)
+//   state     one GbState struct: every scalar of the reference's host loop lives here,
+//             so an iteration never returns to the host
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include "../../include/gb_cs.h"
+
+#define GB_NSLOT 16     // reduction result slots
+#define GB_MAXRB 1024   // max blocks of a reducing kernel
+#define GB_NFLAG 8      // predicate flags
+#define GB_TILE 2048    // elements per block in the ordered compaction
+
+// predicate flags (GbState::flags)
+enum {
+  F_ALWAYS = 0,  // constant 1
+  F_DOBIN = 1,   // binning happens this iteration (minVal <= maxChange)
+  F_UCG = 2,     // CGIHT: unrestricted CG step this iteration
+  F_RCG = 3,     // CGIHT: restricted CG step this iteration
+  F_CG = 4,      // HTP: inner CG loop running
+  F_REMASK = 5   // CGIHT: support changed, re-restrict the search direction
+};
+
+// reduction slots
+enum {
+  R_RES = 0,   // ||resid||^2
+  R_XT = 1,    // ||x_thres||^2
+  R_GMAX = 2,  // max |grad| (or |grad_prev|)
+  R_AXT = 3,   // ||A x_thres||^2
+  R_XMAX = 4,  // max |x|
+  R_DOT1 = 5,
+  R_DOT2 = 6,
+  R_DOT3 = 7,
+  R_DOT4 = 8,
+  R_CG = 9     // HTP inner CG: ||A grad||^2
+};
+
+struct GbState {
+  // configuration
+  int m, n, k, lda, num_bins, maxiter, alg, restart, l0_thresh, d;
+  float tol;
+  // loop bookkeeping (GAGA/gaga/algorithms.cu:1285-1330)
+  int iter, active, fail, cycle, passes, pass_limit, status, stop_reason;
+  float err, err_start, resid_diff;
+  float prev[16], evol[16];
+  // support selection (GAGA/gaga/functions.cu:397-436)
+  int max_bin, k_bin, sum, k_bin_prev;
+  float alpha_bin, min_val, slope, max_value, max_change;
+  int s_cnt;
+  // CG scalars
+  float mu, cg_alpha, cg_beta;
+  int beta_to_zero, supp_change;
+  // HTP inner CG (GAGA/gaga/algorithms.cu:2531-2540,2617-2669)
+  int it_cg;
+  float err_cg, tol_cg, tol2, diff_cg, prev_cg[16], evol_cg[16];
+  // l0 decoding bookkeeping (GAGA/gaga/expander/parallel_l0.cu:36-60)
+  int found, l0_len, l0_offset;
+  float norm, norm0, l0_diff, l0_prev[64], l0_evol[64], l0_cyc[64];
+  // predicates and reduction results
+  int flags[GB_NFLAG];
+  double red[GB_NSLOT];
+  // CGIHT support-change detection
+  int changed;
+};
+
+// Operator description on the device.
+struct GbOp {
+  int kind;  // GB_OP_DENSE / GB_OP_DCT / GB_OP_SMV
+  int m, n, lda;
+  const float *A;
+  int vec4;  // dense: lda % 4 == 0 and A 16-byte aligned
+  // dct: n = 2^logn = 2^log1 * 2^log2
+  const int *rows;
+  int logn, log1, log2;
+  float2 *cbuf0, *cbuf1;  // complex work buffers (n)
+  float *freq;            // frequency image for A^T (zero except at rows)
+  // smv: column-grouped rows/vals (n*d) and a row-major (CSR) copy, columns ascending
+  const int *smv_rows;
+  const float *smv_vals;
+  int d;
+  const int *csr_ptr, *csr_col;
+  const float *csr_val;
+};
+
+struct GbWork {
+  GbState *st;            // device state
+  float *red_part;        // [GB_NSLOT][GB_MAXRB]
+  unsigned int *tickets;  // [GB_NSLOT]
+  float *x, *xt, *grad, *gp, *gpt;
+  float *y, *resid, *ru;
+  int *bins, *bins_prev, *counters;
+  int *S;        // support list (n)
+  int *tile_cnt; // per-tile counts for ordered compaction
+  float *part;   // dense A*v split-K partials
+  size_t part_cap;
+  float *upd;    // l0 updates (n)
+  float *rec;    // l0 residual record (maxiter + 1)
+  GbOp op;
+  int num_sms;
+  int red_blocks;  // grid of reducing kernels (fixed -> deterministic reductions)
+};
+
+void gb_set_error_message(const char *msg, const char *file, int line);
+
+#define GB_CUDA_TRY(call)                                               \
+  do {                                                                  \
+    cudaError_t e_ = (call);                                            \
+    if (e_ != cudaSuccess) {                                            \
+      gb_set_error_message(cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return e_ == cudaErrorMemoryAllocation ? GB_OOM : GB_CUDA_ERROR;  \
+    }                                                                   \
+  } while (0)
+
+#define GB_TRY(call)            \
+  do {                          \
+    gb_status s_ = (call);      \
+    if (s_ != GB_OK) return s_; \
+  } while (0)
+
+// ---------------------------------------------------------------- device helpers
+__device__ __forceinline__ bool gb_pred(const GbState *st, int flag) {
+  return st->active != 0 && st->flags[flag] != 0;
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Block reduction (OP 0 sum, 1 max); the result is valid in thread 0.
+template <int OP>
+__device__ __forceinline__ float block_reduce(float v, float *smem32) {
+  v = OP == 0 ? warp_sum(v) : warp_max(v);
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) smem32[wid] = v;
+  __syncthreads();
+  int nw = blockDim.x >> 5;
+  v = (threadIdx.x < nw) ? smem32[threadIdx.x] : 0.0f;
+  if (wid == 0) v = OP == 0 ? warp_sum(v) : warp_max(v);
+  return v;
+}
+
+// Grid reduction in a fixed order: every block publishes its partial, the last block to
+// arrive combines the partials (sums in double) and writes st->red[slot].  All threads
+// of every block must call it; the grid size must not exceed GB_MAXRB.
+template <int OP>
+__device__ void grid_reduce_publish(float v, int slot, GbState *st, float *parts, unsigned int *tickets) {
+  __shared__ float sm[32];
+  __shared__ int last;
+  float b = block_reduce<OP>(v, sm);
+  if (threadIdx.x == 0) {
+    parts[slot * GB_MAXRB + blockIdx.x] = b;
+    __threadfence();
+    unsigned int t = atomicAdd(&tickets[slot], 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last && threadIdx.x < 32) {
+    __threadfence();
+    double acc = 0.0;
+    float mx = 0.0f;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += 32) {
+      float p = __ldcg(&parts[slot * GB_MAXRB + i]);
+      if (OP == 0) acc += (double)p;
+      else mx = fmaxf(mx, p);
+    }
+    if (OP == 0) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    } else {
+      mx = warp_max(mx);
+    }
+    if (threadIdx.x == 0) {
+      st->red[slot] = OP == 0 ? acc : (double)mx;
+      tickets[slot] = 0u;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- host-side pieces
+// operators (gb_ops.cu)
+// out = A v (v must vanish outside S for the dense operator); with y, out = y - A v;
+// with slot >= 0, st->red[slot] = ||out||^2.  Runs only while flag `pf` is set.
+void enq_A(GbWork &w, cudaStream_t s, const float *v, float *out, const float *y, int slot, int pf);
+// g = A^T r
+void enq_AT(GbWork &w, cudaStream_t s, const float *r, float *g, int pf);
+// dense split-K partial buffer size (floats) for an n-column operator
+size_t gb_dense_part_floats(int m_pad, int n);
+
+// solver (gb_solver.cu)
+enum { GB_RUN_SOLVE = 0, GB_RUN_L0 = 1 };
+gb_status gb_run_solver(GbWork &w, int alg, const gb_options &o, int k, cudaStream_t s, float tol_abs);
+// support list S := { j : v_j != 0 } (used by the component operator entry point)
+void enq_support_of_nonzeros(GbWork &w, cudaStream_t s, const float *v, int n);

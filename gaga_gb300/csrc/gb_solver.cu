@@ -1,0 +1,933 @@
+// gb_solver.cu -- NIHT / HTP / CGIHT and parallel_l0 as one CUDA graph per solve.
+//
+// The reference runs each algorithm as a host loop that returns to the host several
+// times per iteration (cuBLAS v1 scalars, bin counters, flags).  Here every scalar of
+// that loop lives in a device-resident GbState; small single-thread "control" kernels
+// execute the reference's scalar logic; every other kernel is predicated on
+// GbState::active and a flag.  One iteration is captured into the body of a CUDA graph
+// WHILE node whose condition the last control kernel sets from the stopping rules, so
+// a whole solve is a single graph launch.
+#include <string.h>
+
+#include "gb_internal.cuh"
+
+// ------------------------------------------------------------------ control phases
+enum {
+  C_INIT0,        // after ||y||^2 : err, err_start
+  C_INIT_BINPREP, // after A^T y and max|x| : decide binning
+  C_BINPREP,      // new max|x| and slope when binning
+  C_INIT_DONE,    // after threshold : (CGIHT needs more) evaluate the loop condition
+  C_CGIHT_INIT,   // CGIHT prologue after r0 = y - A x
+  C_PUSH_RES,     // push sqrt(red[R_RES]) into prev[]
+  C_SD_MU,        // RestrictedSD step size and maxChange; binning decision
+  C_NIHT_STOP,
+  C_HTP_CGINIT,
+  C_HTP_CG1,
+  C_HTP_CG2,
+  C_HTP_CG3,
+  C_HTP_STOP,
+  C_RCG_BETA,
+  C_RCG_ALPHA,
+  C_UCG_BETA,
+  C_UCG_ALPHA,
+  C_CGIHT_BINDEC,
+  C_CGIHT_POST,
+  C_CGIHT_STOP,
+  C_L0_INIT,
+  C_L0_PRE,
+  C_L0_STOP
+};
+
+__device__ static float max_list(const float *a, int n) {
+  float m = a[0];
+  for (int j = 1; j < n; ++j)
+    if (a[j] > m) m = a[j];
+  return m;
+}
+
+__device__ static float sqrt_red(const GbState *st, int slot) { return (float)sqrt(st->red[slot]); }
+
+// stopping test of the reference loops, e.g. GAGA/gaga/algorithms.cu:1365
+__device__ static int keep_going(GbState *st) {
+  int go = (st->err > st->tol) & (st->iter < st->maxiter) & (st->err < (100.0f * st->err_start)) &
+           ((double)st->resid_diff > 0.01 * (double)st->tol) & (st->fail == 0) & (st->cycle != 0);
+  if (!go && st->stop_reason == 0) {
+    if (!(st->err > st->tol)) st->stop_reason = 1;
+    else if (!(st->iter < st->maxiter)) st->stop_reason = 2;
+    else if (!(st->err < 100.0f * st->err_start)) st->stop_reason = 3;
+    else if (!((double)st->resid_diff > 0.01 * (double)st->tol)) st->stop_reason = 4;
+    else if (st->cycle == 0) st->stop_reason = 5;
+    else st->stop_reason = 6;
+  }
+  return go;
+}
+
+// residual bookkeeping after each outer iteration (algorithms.cu:1398-1421)
+__device__ static void stop_update(GbState *st, int fail_after) {
+  for (int j = 0; j < 15; ++j) st->evol[j] = st->evol[j + 1];
+  st->evol[15] = st->prev[14] - st->prev[15];
+  st->resid_diff = max_list(st->evol, 16);
+  for (int j = 0; j < 15; ++j)
+    if ((st->prev[15] == st->prev[j]) && (st->iter > 4)) st->cycle = 0;
+  if (st->iter > fail_after) {
+    float root = 1.0f / 15.0f;
+    float rate = st->prev[15] / st->prev[0];
+    rate = powf(rate, root);
+    if (rate > 0.999f) st->fail = 1;
+  }
+}
+
+__device__ static void push16(float *a, float v) {
+  for (int j = 0; j < 15; ++j) a[j] = a[j + 1];
+  a[15] = v;
+}
+
+__device__ static void finish_iteration(GbState *st, int fail_after) {
+  stop_update(st, fail_after);
+  st->iter++;
+  st->passes++;
+  st->active = keep_going(st);
+  if (st->passes > st->pass_limit && st->active) {
+    st->active = 0;
+    st->status = GB_WATCHDOG;
+  }
+}
+
+// the binning decision shared by every algorithm: FindSupportSet's skip path
+// (GAGA/gaga/functions.cu:401-403) or a new binning with a new max (algorithms.cu:1380-1383)
+__device__ static void bin_decision(GbState *st) {
+  if (st->min_val <= st->max_change) {
+    st->flags[F_DOBIN] = 1;
+  } else {
+    st->flags[F_DOBIN] = 0;
+    st->min_val = st->min_val - st->max_change;
+  }
+}
+
+__global__ void k_ctrl(GbState *st, int phase, cudaGraphConditionalHandle h) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int live = st->active;
+  switch (phase) {
+    case C_INIT0:
+      st->err = sqrt_red(st, R_RES);
+      st->err_start = st->err;
+      break;
+    case C_INIT_BINPREP:
+      // max_value = MaxMagnitude(A^T y); slope = (num_bins-1)/max_value; HTP passes
+      // max_value as maxChange to force the first binning (algorithms.cu:1335-1354,2575)
+      st->max_value = (float)st->red[R_XMAX];
+      st->slope = ((float)(st->num_bins - 1) / st->max_value);
+      st->max_change = (st->alg == GB_ALG_HTP) ? st->max_value : 1.0f;
+      bin_decision(st);
+      break;
+    case C_BINPREP:
+      // if (minVal <= maxChange) { max_value = MaxMagnitude(d_vec,n); slope = ...; }
+      if (live && st->flags[F_DOBIN]) {
+        st->max_value = (float)st->red[R_XMAX];
+        st->slope = ((float)(st->num_bins - 1) / st->max_value);
+      }
+      break;
+    case C_INIT_DONE:
+      if (st->alg != GB_ALG_CGIHT) {
+        st->active = keep_going(st);
+        cudaGraphSetConditional(h, st->active ? 1u : 0u);
+      }
+      break;
+    case C_CGIHT_INIT:
+      st->err = sqrt_red(st, R_RES);
+      st->prev[15] = st->err;
+      for (int j = 0; j < 15; ++j) st->evol[j] = st->evol[j + 1];
+      st->evol[15] = st->prev[14] - st->prev[15];
+      st->beta_to_zero = 1;
+      st->supp_change = 1;
+      st->k_bin_prev = 0;
+      st->flags[F_UCG] = st->restart ? 0 : 1;
+      st->flags[F_RCG] = st->restart ? 1 : 0;
+      st->active = keep_going(st);
+      cudaGraphSetConditional(h, st->active ? 1u : 0u);
+      break;
+    case C_PUSH_RES:
+      if (!live) break;
+      push16(st->prev, sqrt_red(st, R_RES));
+      break;
+    case C_SD_MU: {
+      if (!live) break;
+      // RestrictedSD_S_gen (GAGA/gaga/functions.cu:715-744)
+      float err2 = sqrt_red(st, R_AXT);
+      float mu = sqrt_red(st, R_XT);
+      if (mu < 400.0f * err2) {
+        mu = mu / err2;
+        mu = mu * mu;
+      } else {
+        mu = 0.0f;
+      }
+      st->mu = mu;
+      st->max_change = 2.0f * mu * (float)st->red[R_GMAX];
+      bin_decision(st);
+      break;
+    }
+    case C_NIHT_STOP:
+      if (live) {
+        st->err = st->prev[15];
+        finish_iteration(st, 749);
+      }
+      cudaGraphSetConditional(h, st->active ? 1u : 0u);
+      break;
+    case C_HTP_CGINIT:
+      if (!live) {
+        st->flags[F_CG] = 0;
+        cudaGraphSetConditional(h, 0u);
+        break;
+      }
+      for (int j = 0; j < 16; ++j) { st->prev_cg[j] = 0.0f; st->evol_cg[j] = 1.0f; }
+      st->diff_cg = 1.0f;
+      st->prev_cg[15] = st->prev[15];
+      st->mu = (float)st->red[R_DOT1];
+      st->err_cg = (float)st->red[R_RES];
+      st->prev_cg[15] = st->err_cg;
+      st->it_cg = 0;
+      st->flags[F_CG] = (st->err_cg > st->tol_cg) & (st->it_cg < 15) & (st->diff_cg > st->tol2);
+      cudaGraphSetConditional(h, st->flags[F_CG] ? 1u : 0u);
+      break;
+    case C_HTP_CG1: {
+      // RestrictedCG_S_gen (GAGA/gaga/functions.cu:944-950)
+      float alpha = (float)st->red[R_CG];
+      if (st->mu < 1000.0f * alpha) alpha = st->mu / alpha;
+      else alpha = 0.0f;
+      st->cg_alpha = alpha;
+      break;
+    }
+    case C_HTP_CG2: {
+      float beta = st->mu;
+      st->mu = (float)st->red[R_DOT3];
+      if (st->mu < 1000.0f * beta) beta = st->mu / beta;
+      else beta = 0.0f;
+      st->cg_beta = beta;
+      break;
+    }
+    case C_HTP_CG3:
+      if (st->flags[F_CG] && live) {
+        push16(st->prev_cg, (float)st->red[R_RES]);
+        st->err_cg = st->prev_cg[15];
+        st->it_cg++;
+        for (int j = 0; j < 15; ++j) st->evol_cg[j] = st->evol_cg[j + 1];
+        st->evol_cg[15] = st->prev_cg[14] - st->prev_cg[15];
+        st->diff_cg = max_list(st->evol_cg, 16);
+        st->flags[F_CG] = (st->err_cg > st->tol_cg) & (st->it_cg < 15) & (st->diff_cg > st->tol2);
+      } else {
+        st->flags[F_CG] = 0;
+      }
+      cudaGraphSetConditional(h, (st->flags[F_CG] && live) ? 1u : 0u);
+      break;
+    case C_HTP_STOP:
+      if (live) {
+        st->err = sqrtf(st->err_cg);
+        push16(st->prev, st->err);
+        finish_iteration(st, 125);
+      }
+      cudaGraphSetConditional(h, st->active ? 1u : 0u);
+      break;
+    case C_RCG_BETA: {
+      if (!live || !st->flags[F_RCG]) break;
+      // RestrictedCGwithSupportEvolution (GAGA/gaga/functions.cu:1054-1064)
+      float beta;
+      if (st->beta_to_zero == 1) {
+        beta = 0.0f;
+        st->mu = (float)st->red[R_XT];
+      } else {
+        beta = st->mu;
+        st->mu = (float)st->red[R_XT];
+        if (st->mu < 1000.0f * beta) beta = st->mu / beta;
+        else beta = 0.0f;
+      }
+      st->cg_beta = beta;
+      break;
+    }
+    case C_RCG_ALPHA: {
+      if (!live || !st->flags[F_RCG]) break;
+      float alpha = (float)st->red[R_AXT];
+      if (st->mu < 1000.0f * alpha) alpha = st->mu / alpha;
+      else alpha = 0.0f;
+      st->cg_alpha = alpha;
+      st->max_change = 2.0f * alpha * (float)st->red[R_GMAX];
+      break;
+    }
+    case C_UCG_BETA:
+      if (!live || !st->flags[F_UCG]) break;
+      // UnrestrictedCG (GAGA/gaga/functions.cu:1169-1178)
+      if (st->beta_to_zero == 1) st->cg_beta = 0.0f;
+      else st->cg_beta = -((float)st->red[R_DOT1]) / (float)st->red[R_DOT2];
+      break;
+    case C_UCG_ALPHA:
+      if (!live || !st->flags[F_UCG]) break;
+      st->cg_alpha = ((float)st->red[R_DOT3]) / (float)st->red[R_DOT4];
+      st->mu = (float)st->red[R_XT];
+      st->max_change = 2.0f * st->cg_alpha * (float)st->red[R_GMAX];
+      break;
+    case C_CGIHT_BINDEC:
+      if (!live) break;
+      // CGIHT_S_gen (GAGA/gaga/algorithms.cu:3849-3899)
+      st->beta_to_zero = 0;
+      if (st->min_val <= st->max_change) {
+        st->flags[F_DOBIN] = 1;
+        st->k_bin_prev = st->k_bin;
+        st->changed = 0;
+      } else {
+        st->flags[F_DOBIN] = 0;
+        st->supp_change = 0;
+        st->min_val = st->min_val - st->max_change;
+      }
+      st->flags[F_REMASK] = 0;
+      break;
+    case C_CGIHT_POST:
+      if (!live || !st->flags[F_DOBIN]) break;
+      st->supp_change = st->changed ? 1 : 0;
+      if (st->supp_change) {
+        if (st->restart) st->beta_to_zero = 1;
+        else st->flags[F_REMASK] = 1;
+      }
+      break;
+    case C_CGIHT_STOP:
+      if (live) {
+        st->err = st->prev[15];
+        finish_iteration(st, 749);
+        if (st->restart) { st->flags[F_UCG] = 0; st->flags[F_RCG] = 1; }
+        else { st->flags[F_UCG] = st->supp_change ? 1 : 0; st->flags[F_RCG] = st->supp_change ? 0 : 1; }
+      }
+      cudaGraphSetConditional(h, st->active ? 1u : 0u);
+      break;
+    default:
+      break;
+  }
+}
+
+// ------------------------------------------------------------------ l0 control
+__global__ void k_ctrl_l0(GbState *st, int phase, float *rec, cudaGraphConditionalHandle h) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int L = st->l0_len;
+  switch (phase) {
+    case C_L0_INIT:
+      // parallel_l0 (GAGA/gaga/expander/parallel_l0.cu:31-60)
+      st->norm = sqrt_red(st, R_RES);
+      st->norm0 = st->norm;
+      if (rec) rec[0] = st->norm;
+      for (int i = 0; i < L; ++i) { st->l0_cyc[i] = 0.0f; st->l0_prev[i] = 0.0f; st->l0_evol[i] = 1.0f; }
+      st->l0_diff = 1.0f;
+      st->found = 1;
+      st->active = (st->iter < st->maxiter) & (st->norm > st->tol) & (st->norm < (100.0f * st->norm0)) &
+                   ((double)st->l0_diff > 0.000001) & (st->cycle != 0) & (st->found == 1);
+      cudaGraphSetConditional(h, st->active ? 1u : 0u);
+      break;
+    case C_L0_PRE:
+      if (!st->active) break;
+      st->l0_offset = st->iter % st->d;
+      st->found = 0;
+      break;
+    case C_L0_STOP:
+      if (st->active) {
+        st->norm = sqrt_red(st, R_RES);
+        for (int i = 0; i < L - 1; ++i) st->l0_prev[i] = st->l0_prev[i + 1];
+        st->l0_prev[L - 1] = st->norm;
+        for (int i = 0; i < L - 1; ++i) st->l0_evol[i] = st->l0_evol[i + 1];
+        st->l0_evol[L - 1] = st->l0_prev[L - 2] - st->l0_prev[L - 1];
+        st->l0_diff = max_list(st->l0_evol, L);
+        for (int i = 0; i < L - 1; ++i) st->l0_cyc[i] = st->l0_cyc[i + 1];
+        st->l0_cyc[L - 1] = st->norm;
+        int cycling = 0;
+        if (st->iter > L) {
+          cycling = 1;
+          for (int i = 3; i < L; i += 2) cycling = cycling * (st->l0_cyc[i] == st->l0_cyc[i - 2]);
+        }
+        st->cycle = cycling ? 0 : 1;
+        st->iter++;
+        st->passes++;
+        if (rec) rec[st->iter] = st->norm;
+        int go = (st->iter < st->maxiter) & (st->norm > st->tol) & (st->norm < (100.0f * st->norm0)) &
+                 ((double)st->l0_diff > 0.000001) & (cycling == 0) & (st->found == 1);
+        if (!go) {
+          if (!(st->norm > st->tol)) st->stop_reason = 1;
+          else if (!(st->iter < st->maxiter)) st->stop_reason = 2;
+          else if (!(st->norm < 100.0f * st->norm0)) st->stop_reason = 3;
+          else if (!((double)st->l0_diff > 0.000001)) st->stop_reason = 4;
+          else if (cycling) st->stop_reason = 5;
+          else st->stop_reason = 7;
+        }
+        st->active = go;
+        if (st->passes > st->pass_limit && st->active) {
+          st->active = 0;
+          st->status = GB_WATCHDOG;
+        }
+      }
+      cudaGraphSetConditional(h, st->active ? 1u : 0u);
+      break;
+  }
+}
+
+// ------------------------------------------------------------------ vector kernels
+// dst_i = src_i if bin_i <= k_bin else 0 (zero_vector_float + threshold_one,
+// GAGA/gaga/kernels.cu:64-71); optional ||dst||^2 and max|src|
+__global__ void k_mask(GbState *st, int pf, const float *__restrict__ src, float *__restrict__ dst,
+                       const int *__restrict__ bins, int n, int slot_sq, int slot_max, float *rp,
+                       unsigned int *tk) {
+  if (!gb_pred(st, pf)) return;
+  const int kb = st->k_bin;
+  float s2 = 0.0f, mx = 0.0f;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float v = src[i];
+    const float o = bins[i] <= kb ? v : 0.0f;
+    dst[i] = o;
+    s2 = fmaf(o, o, s2);
+    mx = fmaxf(mx, fabsf(v));
+  }
+  if (slot_sq >= 0) grid_reduce_publish<0>(s2, slot_sq, st, rp, tk);
+  if (slot_max >= 0) grid_reduce_publish<1>(mx, slot_max, st, rp, tk);
+}
+
+// v_i = 0 where bin_i > k_bin (threshold, GAGA/gaga/kernels.cu:74-81)
+__global__ void k_threshold(const GbState *st, int pf, float *__restrict__ v, const int *__restrict__ bins, int n) {
+  if (!gb_pred(st, pf)) return;
+  const int kb = st->k_bin;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    if (bins[i] > kb) v[i] = 0.0f;
+}
+
+// scalar selector for the fused updates
+enum { SC_MU = 0, SC_CG_ALPHA = 1, SC_NEG_CG_ALPHA = 2, SC_CG_BETA = 3, SC_ONE = 4 };
+__device__ __forceinline__ float pick(const GbState *st, int which) {
+  switch (which) {
+    case SC_MU: return st->mu;
+    case SC_CG_ALPHA: return st->cg_alpha;
+    case SC_NEG_CG_ALPHA: return -st->cg_alpha;
+    case SC_CG_BETA: return st->cg_beta;
+    default: return 1.0f;
+  }
+}
+
+// y += a * x (cublasSaxpy); optional max|y| and ||y||^2; optionally clears the bin counters
+__global__ void k_axpy(GbState *st, int pf, int which, const float *__restrict__ x, float *__restrict__ y, int n,
+                       int slot_max, int slot_sq, int *counters, int ncount, float *rp, unsigned int *tk) {
+  if (!gb_pred(st, pf)) return;
+  const float a = pick(st, which);
+  float mx = 0.0f, s2 = 0.0f;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float o = fmaf(a, x[i], y[i]);
+    y[i] = o;
+    mx = fmaxf(mx, fabsf(o));
+    s2 = fmaf(o, o, s2);
+  }
+  if (counters)
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ncount; i += gridDim.x * blockDim.x) counters[i] = 0;
+  if (slot_max >= 0) grid_reduce_publish<1>(mx, slot_max, st, rp, tk);
+  if (slot_sq >= 0) grid_reduce_publish<0>(s2, slot_sq, st, rp, tk);
+}
+
+// a = beta * a + b (cublasSscal then cublasSaxpy with 1)
+__global__ void k_scale_add(const GbState *st, int pf, int which, float *__restrict__ a, const float *__restrict__ b,
+                            int n) {
+  if (!gb_pred(st, pf)) return;
+  const float beta = pick(st, which);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float t = beta * a[i];
+    a[i] = fmaf(1.0f, b[i], t);
+  }
+}
+
+// two dot products in one pass: red[s1] = a.b, red[s2] = c.d
+__global__ void k_dot2(GbState *st, int pf, const float *__restrict__ a, const float *__restrict__ b, int s1, int n1,
+                       const float *__restrict__ c, const float *__restrict__ d, int s2, int n2, float *rp,
+                       unsigned int *tk) {
+  if (!gb_pred(st, pf)) return;
+  float p = 0.0f, q = 0.0f;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n1; i += gridDim.x * blockDim.x) p = fmaf(a[i], b[i], p);
+  if (c)
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += gridDim.x * blockDim.x) q = fmaf(c[i], d[i], q);
+  grid_reduce_publish<0>(p, s1, st, rp, tk);
+  if (c) grid_reduce_publish<0>(q, s2, st, rp, tk);
+}
+
+// dst = src; red[slot] = ||src||^2 ; optional max|src|
+__global__ void k_copy_norm(GbState *st, int pf, const float *__restrict__ src, float *__restrict__ dst, int n,
+                            int slot_sq, int slot_max, float *rp, unsigned int *tk) {
+  if (!gb_pred(st, pf)) return;
+  float s2 = 0.0f, mx = 0.0f;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float v = src[i];
+    if (dst) dst[i] = v;
+    s2 = fmaf(v, v, s2);
+    mx = fmaxf(mx, fabsf(v));
+  }
+  if (slot_sq >= 0) grid_reduce_publish<0>(s2, slot_sq, st, rp, tk);
+  if (slot_max >= 0) grid_reduce_publish<1>(mx, slot_max, st, rp, tk);
+}
+
+// ------------------------------------------------------------------ support selection
+// LinearBinning (GAGA/gaga/kernels.cu:135-146), bit-exact.  The double-precision test
+// (double)t > (double)intercept * 1e-6 equals t > F in float with F the double product
+// rounded toward -inf.  float -> int stores use round-toward-zero with saturation and
+// NaN -> 0, as the reference's compiled kernel does; `slope*intercept + 1.0f` is one
+// fused multiply-add there and here.
+__device__ __forceinline__ int lin_bin(float v, float slope, float intercept, float small_f, bool &counted) {
+  const float t = fabsf(v);
+  if (t > small_f) {
+    counted = true;
+    return __float2int_rz(fmaxf(0.0f, __fmul_rn(slope, __fsub_rn(intercept, t))));
+  }
+  counted = false;
+  return __float2int_rz(__fmaf_rn(slope, intercept, 1.0f));
+}
+
+__global__ void k_hist(const GbState *st, int pf, const float *__restrict__ v, int *__restrict__ bins,
+                       int *__restrict__ bins_prev, int *__restrict__ counters, int n) {
+  if (!gb_pred(st, pf)) return;
+  const float intercept = st->max_value;
+  const float slope = st->slope;
+  const float small_f = __double2float_rd((double)intercept * 0.000001);
+  const int max_bin = st->max_bin;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    bool counted;
+    const int b = lin_bin(v[i], slope, intercept, small_f, counted);
+    if (bins_prev) bins_prev[i] = bins[i];
+    bins[i] = b;
+    if (counted && b < max_bin) {
+      // warp-aggregated increment of equal bins
+      const unsigned act = __activemask();
+      const unsigned same = __match_any_sync(act, b);
+      const int leader = __ffs(same) - 1;
+      if ((int)(threadIdx.x & 31) == leader) atomicAdd(&counters[b], __popc(same));
+    }
+  }
+}
+
+// k-th largest bin: the reference copies the first MaxBin counters to the host and scans
+// (GAGA/gaga/functions.cu:412-433).  One block of 1024 threads does the same scan.
+__global__ void __launch_bounds__(1024) k_kbin(GbState *st, int pf, const int *__restrict__ counters, int k) {
+  if (!gb_pred(st, pf)) return;
+  __shared__ int scan[1024];
+  __shared__ int res_kbin, res_sum;
+  const int max_bin = st->max_bin;
+  const int C = (max_bin + 1023) / 1024;
+  const int t = threadIdx.x;
+  const int b0 = t * C, b1 = min(b0 + C, max_bin);
+  int csum = 0;
+  for (int b = b0; b < b1; ++b) csum += counters[b];
+  scan[t] = csum;
+  if (t == 0) { res_kbin = -2; res_sum = 0; }
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {  // inclusive Hillis-Steele scan
+    int v = t >= off ? scan[t - off] : 0;
+    __syncthreads();
+    scan[t] += v;
+    __syncthreads();
+  }
+  const int incl = scan[t], excl = incl - csum;
+  if (k > 0 && excl < k && incl >= k) {
+    int s = excl;
+    for (int b = b0; b < b1; ++b) {
+      s += counters[b];
+      if (s >= k) { res_kbin = b; res_sum = s; break; }
+    }
+  }
+  __syncthreads();
+  if (t == 0) {
+    int k_bin, sum;
+    if (k <= 0) { k_bin = -1; sum = 0; }
+    else if (res_kbin == -2) { k_bin = max_bin - 1; sum = scan[1023]; }
+    else { k_bin = res_kbin; sum = res_sum; }
+    const float intercept = st->max_value;
+    const float slope = st->slope;
+    if (sum < k) {
+      st->alpha_bin = st->alpha_bin * 0.5f;
+      st->max_bin = (int)((float)st->num_bins * (1.0f - st->alpha_bin));
+    }
+    st->min_val = intercept - (float)(k_bin + 1) / slope;
+    st->k_bin = k_bin;
+    st->sum = sum;
+  }
+}
+
+// threshold v (always) and, when binning, count the tile's support entries and detect
+// whether a previous support entry left the support (checkSupportEvolution,
+// GAGA/gaga/kernels.cu:178-193, without its block-local flag reset race)
+__global__ void __launch_bounds__(256) k_thresh_count(GbState *st, int pf, float *__restrict__ v,
+                                                      const int *__restrict__ bins, const int *__restrict__ bins_prev,
+                                                      int n, int *__restrict__ tile_cnt) {
+  if (!gb_pred(st, pf)) return;
+  const int kb = st->k_bin, kbp = st->k_bin_prev;
+  const bool count = st->flags[F_DOBIN] != 0;
+  const int base = blockIdx.x * GB_TILE;
+  int cnt = 0, changed = 0;
+  for (int q = threadIdx.x; q < GB_TILE; q += blockDim.x) {
+    const int i = base + q;
+    if (i < n) {
+      const int b = bins[i];
+      if (b > kb) {
+        if (v) v[i] = 0.0f;
+      } else {
+        cnt++;
+      }
+      if (bins_prev && count && bins_prev[i] <= kbp && b > kb) changed = 1;
+    }
+  }
+  if (!count) return;
+  __shared__ float sm[32];
+  const float tot = block_reduce<0>((float)cnt, sm);
+  if (threadIdx.x == 0) tile_cnt[blockIdx.x] = (int)tot;
+  if (bins_prev && __syncthreads_or(changed) && threadIdx.x == 0) atomicOr(&st->changed, 1);
+}
+
+// ordered compaction: S = ascending { i : bin_i <= k_bin }
+__global__ void __launch_bounds__(256) k_compact(GbState *st, int pf, const int *__restrict__ bins, int n,
+                                                 const int *__restrict__ tile_cnt, int *__restrict__ S) {
+  if (!gb_pred(st, pf)) return;
+  __shared__ float sm[32];
+  __shared__ int warp_base[8];
+  const int kb = st->k_bin;
+  // offset of this tile = sum of the previous tiles' counts
+  float off = 0.0f;
+  for (int t = threadIdx.x; t < (int)blockIdx.x; t += blockDim.x) off += (float)tile_cnt[t];
+  int offset = (int)block_reduce<0>(off, sm);
+  __shared__ int s_off;
+  if (threadIdx.x == 0) s_off = offset;
+  __syncthreads();
+  int running = s_off;
+  const int base = blockIdx.x * GB_TILE;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int q0 = 0; q0 < GB_TILE; q0 += blockDim.x) {
+    const int i = base + q0 + threadIdx.x;
+    const bool in = i < n && bins[i] <= kb;
+    const unsigned bal = __ballot_sync(0xffffffffu, in);
+    if (lane == 0) warp_base[wid] = __popc(bal);
+    __syncthreads();
+    int wb = 0, tot = 0;
+    for (int w2 = 0; w2 < 8; ++w2) {
+      if (w2 < wid) wb += warp_base[w2];
+      tot += warp_base[w2];
+    }
+    if (in) S[running + wb + __popc(bal & ((1u << lane) - 1u))] = i;
+    running += tot;
+    __syncthreads();
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) st->s_cnt = running;
+}
+
+// ------------------------------------------------------------------ l0 kernels
+// cuda_compute_scores_l0 (GAGA/gaga/expander/kernels.cu:353-388); the score stays a float
+// counter as in the reference
+__global__ void k_l0_scores(GbState *st, const float *__restrict__ res, float *__restrict__ x,
+                            float *__restrict__ upd, const int *__restrict__ rows, int n, int d) {
+  if (!st->active) return;
+  const int thresh = st->l0_thresh;
+  const int shift = st->l0_offset;
+  const float EPS = 0.000001f;
+  int found = 0;
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const size_t idx = (size_t)d * j;
+    float score = 0.0f;
+    const float omega = res[rows[idx + shift]];
+    float u = 0.0f;
+    if (fabsf(omega) > EPS) {
+      for (int i = 0; i < d; ++i) {
+        const float ri = res[rows[idx + i]];
+        if (fabsf(__fsub_rn(ri, omega)) <= EPS) score += 1.0f;
+        if (fabsf(ri) <= EPS) score -= 1.0f;
+      }
+      if (score > (float)thresh) {
+        found = 1;
+        x[j] = __fadd_rn(x[j], omega);
+        u = omega;
+      }
+    }
+    upd[j] = u;
+  }
+  if (__syncthreads_or(found) && threadIdx.x == 0) st->found = 1;
+}
+
+// cuda_update_residual (GAGA/gaga/expander/kernels.cu:3-14) as a row gather over the CSR
+// copy: each row applies its accepted updates in ascending column order; ||res||^2
+__global__ void k_l0_update(GbState *st, float *__restrict__ res, const int *__restrict__ ptr,
+                            const int *__restrict__ col, const float *__restrict__ upd, int m, float *rp,
+                            unsigned int *tk) {
+  if (!st->active) return;
+  float s2 = 0.0f;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    float r = res[i];
+    const int e1 = ptr[i + 1];
+    for (int e = ptr[i]; e < e1; ++e) {
+      const float u = upd[col[e]];
+      if (fabsf(u) > 0.0f) r = __fadd_rn(r, -u);
+    }
+    res[i] = r;
+    s2 = fmaf(r, r, s2);
+  }
+  grid_reduce_publish<0>(s2, R_RES, st, rp, tk);
+}
+
+// ------------------------------------------------------------------ state init
+__global__ void k_init_state(GbState *st, GbState init) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *st = init;
+}
+
+// ------------------------------------------------------------------ graph helpers
+namespace {
+
+// A conditional handle is created on the graph being captured on `parent`; the kernel
+// that sets its first value is captured next, then the WHILE node itself.
+gb_status make_handle(cudaStream_t parent, cudaGraphConditionalHandle *h) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g;
+  GB_CUDA_TRY(cudaStreamGetCaptureInfo(parent, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+  GB_CUDA_TRY(cudaGraphConditionalHandleCreate(h, g, 0, 0));
+  return GB_OK;
+}
+
+gb_status open_while(cudaStream_t parent, cudaStream_t body, cudaGraphConditionalHandle h) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g;
+  const cudaGraphNode_t *deps = nullptr;
+  size_t nd = 0;
+  GB_CUDA_TRY(cudaStreamGetCaptureInfo(parent, &cs, nullptr, &g, &deps, nullptr, &nd));
+  cudaGraphNodeParams p = {};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = h;
+  p.conditional.type = cudaGraphCondTypeWhile;
+  p.conditional.size = 1;
+  cudaGraphNode_t node;
+  GB_CUDA_TRY(cudaGraphAddNode(&node, g, deps, nullptr, nd, &p));
+  GB_CUDA_TRY(cudaStreamUpdateCaptureDependencies(parent, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  GB_CUDA_TRY(cudaStreamBeginCaptureToGraph(body, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                            cudaStreamCaptureModeRelaxed));
+  return GB_OK;
+}
+
+gb_status close_while(cudaStream_t body) {
+  cudaGraph_t g;
+  GB_CUDA_TRY(cudaStreamEndCapture(body, &g));
+  return GB_OK;
+}
+
+}  // namespace
+
+static void enq_mask(GbWork &w, cudaStream_t s, int pf, const float *src, float *dst, int slot_sq, int slot_max) {
+  k_mask<<<w.red_blocks, 256, 0, s>>>(w.st, pf, src, dst, w.bins, w.op.n, slot_sq, slot_max, w.red_part, w.tickets);
+}
+static void enq_axpy(GbWork &w, cudaStream_t s, int pf, int which, const float *x, float *y, int n, int slot_max,
+                     bool clear_counters, int num_bins) {
+  k_axpy<<<w.red_blocks, 256, 0, s>>>(w.st, pf, which, x, y, n, slot_max, -1, clear_counters ? w.counters : nullptr,
+                                      num_bins, w.red_part, w.tickets);
+}
+static void enq_ctrl(GbWork &w, cudaStream_t s, int phase, cudaGraphConditionalHandle h = 0) {
+  k_ctrl<<<1, 32, 0, s>>>(w.st, phase, h);
+}
+
+// FindSupportSet + Threshold: binning, k-th bin and ordered compaction predicated on
+// F_DOBIN; the threshold of x always runs
+static void enq_support(GbWork &w, cudaStream_t s, int k, bool save_prev) {
+  const int n = w.op.n;
+  k_hist<<<w.red_blocks, 256, 0, s>>>(w.st, F_DOBIN, w.x, w.bins, save_prev ? w.bins_prev : nullptr, w.counters, n);
+  k_kbin<<<1, 1024, 0, s>>>(w.st, F_DOBIN, w.counters, k);
+  const int tiles = (n + GB_TILE - 1) / GB_TILE;
+  k_thresh_count<<<tiles, 256, 0, s>>>(w.st, F_ALWAYS, w.x, w.bins, save_prev ? w.bins_prev : nullptr, n, w.tile_cnt);
+  k_compact<<<tiles, 256, 0, s>>>(w.st, F_DOBIN, w.bins, n, w.tile_cnt, w.S);
+}
+
+static gb_status build_graph(GbWork &w, int alg, int k, int num_bins, cudaStream_t s0, cudaStream_t s1,
+                             cudaStream_t s2, cudaGraph_t *graph) {
+  const int n = w.op.n, m = w.op.m;
+  GB_CUDA_TRY(cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal));
+  cudaGraphConditionalHandle h_outer = 0, h_inner = 0;
+  GB_TRY(make_handle(s0, &h_outer));
+  if (alg == GB_ALG_PARALLEL_L0) {
+    // res = y - A x with x = 0 (computeResidual, GAGA/gaga/expander/functions.cu:73-79)
+    enq_A(w, s0, w.x, w.resid, w.y, R_RES, F_ALWAYS);
+    k_ctrl_l0<<<1, 32, 0, s0>>>(w.st, C_L0_INIT, w.rec, h_outer);
+  } else {
+    // resid = y; err = ||y||  (algorithms.cu:1296-1300)
+    k_copy_norm<<<w.red_blocks, 256, 0, s0>>>(w.st, F_ALWAYS, w.y, w.resid, m, R_RES, -1, w.red_part, w.tickets);
+    enq_ctrl(w, s0, C_INIT0);
+    // x = A^T y ; max |x| ; FindSupportSet ; Threshold  (algorithms.cu:1335-1354)
+    enq_AT(w, s0, w.y, w.x, F_ALWAYS);
+    k_copy_norm<<<w.red_blocks, 256, 0, s0>>>(w.st, F_ALWAYS, w.x, nullptr, n, -1, R_XMAX, w.red_part, w.tickets);
+    enq_ctrl(w, s0, C_INIT_BINPREP);
+    k_axpy<<<w.red_blocks, 256, 0, s0>>>(w.st, F_ALWAYS, SC_ONE, w.x, w.x, 0, -1, -1, w.counters, num_bins,
+                                         w.red_part, w.tickets);
+    enq_support(w, s0, k, false);
+    if (alg == GB_ALG_CGIHT) {
+      // r0, grad_previous = A^T r0, grad_prev_thres (algorithms.cu:3776-3808)
+      enq_A(w, s0, w.x, w.resid, w.y, R_RES, F_ALWAYS);
+      enq_AT(w, s0, w.resid, w.gp, F_ALWAYS);
+      enq_mask(w, s0, F_ALWAYS, w.gp, w.gpt, -1, -1);
+      enq_ctrl(w, s0, C_CGIHT_INIT, h_outer);
+    } else {
+      enq_ctrl(w, s0, C_INIT_DONE, h_outer);
+    }
+  }
+  GB_TRY(open_while(s0, s1, h_outer));
+  // ---------------- loop body (one outer iteration) on s1
+  if (alg == GB_ALG_NIHT || alg == GB_ALG_HTP) {
+    // RestrictedSD (GAGA/gaga/functions.cu:659-745)
+    enq_A(w, s1, w.x, w.resid, w.y, R_RES, F_ALWAYS);
+    enq_ctrl(w, s1, C_PUSH_RES);
+    enq_AT(w, s1, w.resid, w.grad, F_ALWAYS);
+    enq_mask(w, s1, F_ALWAYS, w.grad, w.xt, R_XT, R_GMAX);
+    enq_A(w, s1, w.xt, w.ru, nullptr, R_AXT, F_ALWAYS);
+    enq_ctrl(w, s1, C_SD_MU);
+    enq_axpy(w, s1, F_ALWAYS, SC_MU, w.grad, w.x, n, R_XMAX, true, num_bins);
+    enq_ctrl(w, s1, C_BINPREP);
+    enq_support(w, s1, k, false);
+    if (alg == GB_ALG_NIHT) {
+      enq_ctrl(w, s1, C_NIHT_STOP, h_outer);
+    } else {
+      // CG projection on the support (GAGA/gaga/algorithms.cu:2588-2669)
+      enq_A(w, s1, w.x, w.resid, w.y, R_RES, F_ALWAYS);
+      enq_AT(w, s1, w.resid, w.grad, F_ALWAYS);
+      k_threshold<<<w.red_blocks, 256, 0, s1>>>(w.st, F_ALWAYS, w.grad, w.bins, n);
+      k_copy_norm<<<w.red_blocks, 256, 0, s1>>>(w.st, F_ALWAYS, w.grad, w.gp, n, R_DOT1, -1, w.red_part, w.tickets);
+      GB_TRY(make_handle(s1, &h_inner));
+      enq_ctrl(w, s1, C_HTP_CGINIT, h_inner);
+      GB_TRY(open_while(s1, s2, h_inner));
+      {
+        // RestrictedCG_S_gen (GAGA/gaga/functions.cu:922-1000)
+        enq_A(w, s2, w.grad, w.resid, nullptr, R_CG, F_CG);
+        enq_ctrl(w, s2, C_HTP_CG1);
+        enq_axpy(w, s2, F_CG, SC_CG_ALPHA, w.grad, w.x, n, -1, false, 0);
+        enq_AT(w, s2, w.resid, w.xt, F_CG);
+        k_threshold<<<w.red_blocks, 256, 0, s2>>>(w.st, F_CG, w.xt, w.bins, n);
+        k_axpy<<<w.red_blocks, 256, 0, s2>>>(w.st, F_CG, SC_NEG_CG_ALPHA, w.xt, w.gp, n, -1, R_DOT3, nullptr, 0,
+                                             w.red_part, w.tickets);
+        enq_ctrl(w, s2, C_HTP_CG2);
+        k_scale_add<<<w.red_blocks, 256, 0, s2>>>(w.st, F_CG, SC_CG_BETA, w.grad, w.gp, n);
+        enq_A(w, s2, w.x, w.resid, w.y, R_RES, F_CG);
+        enq_ctrl(w, s2, C_HTP_CG3, h_inner);
+      }
+      GB_TRY(close_while(s2));
+      enq_ctrl(w, s1, C_HTP_STOP, h_outer);
+    }
+  } else if (alg == GB_ALG_CGIHT) {
+    // RestrictedCGwithSupportEvolution (functions.cu:1004-1102) under F_RCG;
+    // UnrestrictedCG (functions.cu:1107-1220) under F_UCG
+    enq_A(w, s1, w.x, w.resid, w.y, R_RES, F_RCG);
+    enq_A(w, s1, w.x, w.ru, w.y, R_RES, F_UCG);
+    enq_ctrl(w, s1, C_PUSH_RES);
+    // RCG branch
+    enq_AT(w, s1, w.resid, w.grad, F_RCG);
+    enq_mask(w, s1, F_RCG, w.grad, w.xt, R_XT, -1);
+    enq_ctrl(w, s1, C_RCG_BETA);
+    k_scale_add<<<w.red_blocks, 256, 0, s1>>>(w.st, F_RCG, SC_CG_BETA, w.gp, w.grad, n);
+    enq_mask(w, s1, F_RCG, w.gp, w.gpt, -1, R_GMAX);
+    enq_A(w, s1, w.gpt, w.ru, nullptr, R_AXT, F_RCG);
+    enq_ctrl(w, s1, C_RCG_ALPHA);
+    // UCG branch
+    enq_AT(w, s1, w.ru, w.grad, F_UCG);
+    enq_mask(w, s1, F_UCG, w.grad, w.xt, R_XT, -1);
+    enq_A(w, s1, w.gpt, w.resid, nullptr, -1, F_UCG);
+    enq_A(w, s1, w.xt, w.ru, nullptr, -1, F_UCG);
+    k_dot2<<<w.red_blocks, 256, 0, s1>>>(w.st, F_UCG, w.resid, w.ru, R_DOT1, m, w.resid, w.resid, R_DOT2, m,
+                                         w.red_part, w.tickets);
+    enq_ctrl(w, s1, C_UCG_BETA);
+    k_scale_add<<<w.red_blocks, 256, 0, s1>>>(w.st, F_UCG, SC_CG_BETA, w.gp, w.grad, n);
+    enq_mask(w, s1, F_UCG, w.gp, w.gpt, -1, R_GMAX);
+    k_scale_add<<<w.red_blocks, 256, 0, s1>>>(w.st, F_UCG, SC_CG_BETA, w.resid, w.ru, m);
+    k_dot2<<<w.red_blocks, 256, 0, s1>>>(w.st, F_UCG, w.gpt, w.xt, R_DOT3, n, w.resid, w.resid, R_DOT4, m,
+                                         w.red_part, w.tickets);
+    enq_ctrl(w, s1, C_UCG_ALPHA);
+    // x += alpha * grad_previous; bins; support change (algorithms.cu:3849-3899)
+    enq_axpy(w, s1, F_ALWAYS, SC_CG_ALPHA, w.gp, w.x, n, R_XMAX, true, num_bins);
+    enq_ctrl(w, s1, C_CGIHT_BINDEC);
+    enq_ctrl(w, s1, C_BINPREP);
+    enq_support(w, s1, k, true);
+    enq_ctrl(w, s1, C_CGIHT_POST);
+    enq_mask(w, s1, F_REMASK, w.gp, w.gpt, -1, -1);
+    enq_ctrl(w, s1, C_CGIHT_STOP, h_outer);
+  } else {
+    // parallel_l0 loop (GAGA/gaga/expander/parallel_l0.cu:56-137)
+    k_ctrl_l0<<<1, 32, 0, s1>>>(w.st, C_L0_PRE, w.rec, 0);
+    int blocks = (n + 255) / 256;
+    if (blocks > w.num_sms * 16) blocks = w.num_sms * 16;
+    k_l0_scores<<<blocks, 256, 0, s1>>>(w.st, w.resid, w.x, w.upd, w.op.smv_rows, n, w.op.d);
+    k_l0_update<<<w.red_blocks, 256, 0, s1>>>(w.st, w.resid, w.op.csr_ptr, w.op.csr_col, w.upd, m, w.red_part,
+                                               w.tickets);
+    k_ctrl_l0<<<1, 32, 0, s1>>>(w.st, C_L0_STOP, w.rec, h_outer);
+  }
+  GB_TRY(close_while(s1));
+  GB_CUDA_TRY(cudaStreamEndCapture(s0, graph));
+  return GB_OK;
+}
+
+// Initial device state for a solve.
+static GbState initial_state(const GbWork &w, int alg, const gb_options &o, int k, float tol_abs) {
+  GbState st;
+  memset(&st, 0, sizeof(st));
+  st.m = w.op.m;
+  st.n = w.op.n;
+  st.k = k;
+  st.lda = w.op.lda;
+  st.num_bins = o.num_bins;
+  st.maxiter = o.maxiter;
+  st.alg = alg;
+  st.restart = o.restart_flag;
+  st.l0_thresh = o.l0_thresh;
+  st.d = w.op.d;
+  st.tol = tol_abs;
+  st.active = 1;
+  st.cycle = 1;
+  st.pass_limit = o.maxiter + 4;
+  st.resid_diff = 1.0f;
+  for (int j = 0; j < 16; ++j) { st.prev[j] = 0.0f; st.evol[j] = 1.0f; }
+  st.alpha_bin = 0.25f;
+  st.max_bin = (int)((float)o.num_bins * (1.0f - st.alpha_bin));
+  st.beta_to_zero = 1;
+  st.supp_change = 1;
+  st.tol_cg = tol_abs * tol_abs;
+  st.tol2 = 10.0f * st.tol_cg;
+  st.l0_len = 2 * w.op.d;
+  st.flags[F_ALWAYS] = 1;
+  return st;
+}
+
+// Runs one solve on the prepared workspace (x zero, y uploaded); results stay in GbState.
+gb_status gb_run_solver(GbWork &w, int alg, const gb_options &o, int k, cudaStream_t s, float tol_abs) {
+  if (alg == GB_ALG_PARALLEL_L0 && (w.op.d <= 0 || 2 * w.op.d > 64)) return GB_UNSUPPORTED;
+  GbState init = initial_state(w, alg, o, k, tol_abs);
+  k_init_state<<<1, 1, 0, s>>>(w.st, init);
+  GB_CUDA_TRY(cudaGetLastError());
+  cudaStream_t s0, s1, s2;
+  GB_CUDA_TRY(cudaStreamCreateWithFlags(&s0, cudaStreamNonBlocking));
+  GB_CUDA_TRY(cudaStreamCreateWithFlags(&s1, cudaStreamNonBlocking));
+  GB_CUDA_TRY(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  gb_status rc = build_graph(w, alg, k, o.num_bins, s0, s1, s2, &graph);
+  if (rc == GB_OK) {
+    cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+    if (e != cudaSuccess) {
+      gb_set_error_message(cudaGetErrorString(e), __FILE__, __LINE__);
+      rc = GB_CUDA_ERROR;
+    }
+  }
+  if (rc == GB_OK) {
+    cudaError_t e = cudaGraphLaunch(exec, s);
+    if (e != cudaSuccess) {
+      gb_set_error_message(cudaGetErrorString(e), __FILE__, __LINE__);
+      rc = GB_CUDA_ERROR;
+    }
+  }
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  cudaStreamDestroy(s0);
+  cudaStreamDestroy(s1);
+  cudaStreamDestroy(s2);
+  return rc;
+}
+
+// ------------------------------------------------------------------ component helpers
+__global__ void k_support_nonzero(GbState *st, const float *__restrict__ v, int n, int *__restrict__ S) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int c = 0;
+  for (int i = 0; i < n; ++i)
+    if (v[i] != 0.0f) S[c++] = i;
+  st->s_cnt = c;
+}
+
+void enq_support_of_nonzeros(GbWork &w, cudaStream_t s, const float *v, int n) {
+  k_support_nonzero<<<1, 1, 0, s>>>(w.st, v, n, w.S);
+}

@@ -1,0 +1,180 @@
+/*
+ * gb_cs.h -- C ABI of the GB300-native greedy sparse-recovery library (libgb_cs.so).
+ *
+ * The drop-in boundary for GAGA's recovery path.  GAGA exposes it as three MATLAB
+ * MEX gateways reached through gaga_cs.m:
+ *     gaga_gen  GAGA/gaga/gaga_gen.cu:41-848   dense Gaussian / Bernoulli matrices
+ *     gaga_dct  GAGA/gaga/gaga_dct.cu:40-831   row-subsampled orthonormal DCT
+ *     gaga_smv  GAGA/gaga/gaga_smv.cu:39-1198  sparse expander (d nonzeros per column)
+ * each with a "generate and solve" usage and a "solve given data" usage
+ * (GAGA/gaga/gaga_cs.m:7-64).  This header exports both usages as plain C calls on
+ * host or device pointers.  A MEX shim maps MATLAB arrays onto
+ * these calls one to one.  Names use the gb_cs_ prefix; the GAGA licence
+ * (GAGA/GAGA_license:5) reserves the gaga_* function names.
+ *
+ * Semantics kept from the reference:
+ *   - algorithms NIHT, HTP, CGIHT (restartFlag) on all operators; parallel_l0 on smv
+ *   - option names/meaning/defaults of gagaOptions.m, including tol compared with the
+ *     ABSOLUTE residual norm ||y - A x||_2 and the default tol of 10^(-4) evaluated
+ *     as C's XOR (= -10), which disables the residual test (GAGA/gaga/gaga_gen.cu:183)
+ *   - support selection by linear binning, bit-exact to the reference kernel
+ *   - outputs: x, iterations, convergence rate; norms / times / support counts in
+ *     generate mode; residual record for parallel_l0
+ * Additions: integer status codes, an explicit CUDA stream, host or device buffers,
+ * tol_is_relative (tol * ||y||), re-entrant calls (no globals on the solve path).
+ */
+#ifndef GB_CS_H
+#define GB_CS_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  GB_OK = 0,
+  GB_BAD_ARG = 1,      /* invalid algorithm / size / option (reference: printf + return) */
+  GB_OOM = 2,          /* device allocation failed */
+  GB_WATCHDOG = 3,     /* a device-side iteration bound was hit before the stopping rules */
+  GB_CUDA_ERROR = 4,   /* CUDA runtime error; text in gb_cs_last_error() */
+  GB_UNSUPPORTED = 5,  /* valid reference input outside this build (e.g. DCT length not 2^p) */
+  GB_NO_DEVICE = 6
+} gb_status;
+
+enum { GB_OP_DENSE = 0, GB_OP_DCT = 1, GB_OP_SMV = 2 };
+enum { GB_HOST = 0, GB_DEVICE = 1 };
+
+/* Reference algorithm numbers (GAGA/gaga/gaga_gen.cu:619-631, gaga_smv.cu:841-857). */
+enum { GB_ALG_NIHT = 0, GB_ALG_HTP = 1, GB_ALG_CGIHT = 6, GB_ALG_PARALLEL_L0 = 14 };
+
+/* Options: the gagaOptions name/value list (GAGA/gaga/gagaOptions.m:8-58) as a struct. */
+typedef struct {
+  float tol;            /* 'tol'            default 10^(-4) == -10 (reference XOR) */
+  int tol_is_relative;  /* extension: tol * ||y||_2 becomes the absolute tolerance */
+  int maxiter;          /* 'maxiter'        300 for HTP, 5000 otherwise */
+  int num_bins;         /* 'numBins'        max(n/20, 1000) */
+  int restart_flag;     /* 'restartFlag'    0 */
+  int l0_thresh;        /* 'l0_thresh'      1, clamped to [1, d] (gaga_smv.cu:310-313) */
+  int vec_distribution; /* 'vecDistribution' 0 uniform, 1 binary (default), 2 gaussian */
+  int matrix_ensemble;  /* 'matrixEnsemble' gen: 1 gaussian / 2 binary; smv: 1 ones/sqrt(d),
+                           2 +-1/sqrt(d), 3 expander ones (default; forced for l0) */
+  int k_fixed;          /* 'kFixed'         0 */
+  unsigned int seed;    /* 'seed'           0 here (the reference uses clock()) */
+  float noise;          /* 'noise'          0 */
+  int gpu_number;       /* 'gpuNumber'      0 */
+  int conv_rate_num;    /* 'convRateNum'    16 */
+  float alpha;          /* 'alpha'          0.25 (used by the timing variants only) */
+  int support_flag;     /* 'supportFlag'    0 (timing variants only) */
+  int timing;           /* 'timing'         0 (accepted; timing variants are not built) */
+} gb_options;
+
+/* A recovery problem in "given data" form. */
+typedef struct {
+  int kind;            /* GB_OP_DENSE / GB_OP_DCT / GB_OP_SMV */
+  int m, n, k;
+  const float *y;      /* m measurements */
+  const float *A;      /* dense: column-major m x n, leading dimension lda (0 -> m) */
+  int lda;
+  const int *rows;     /* dct: m sampled rows; smv: n*d row indices, grouped by column */
+  const int *cols;     /* smv: n*d column indices (each column's d entries contiguous) */
+  const float *vals;   /* smv: n*d values */
+  int d;               /* smv nonzeros per column (0: inferred from cols as the reference does) */
+  int index_base;      /* 0, or 1 for MATLAB indices (the reference shifts down on the device) */
+  int location;        /* GB_HOST or GB_DEVICE for every pointer above and x_out */
+  void *stream;        /* cudaStream_t, NULL for the legacy default stream */
+} gb_problem;
+
+typedef struct {
+  int iter;             /* iterations */
+  float conv_rate;      /* convRate */
+  float norms[3];       /* generate mode: relative l1, l2, linf error (results.cu:444-487) */
+  float times[3];       /* ms: algorithm, average iteration, total incl. generation */
+  int support[4];       /* generate mode: TP, FP, TN, FN */
+  int k_used;           /* generate mode: support size actually drawn */
+  float resid_prev[16]; /* residNorm_prev at exit */
+  int stop_reason;      /* 1 tol, 2 maxiter, 3 divergence, 4 stall, 5 cycle, 6 slow rate, 7 no candidates */
+  float *res_record;    /* parallel_l0: caller buffer of maxiter+1 floats or NULL (resRecord) */
+} gb_result;
+
+/* Support-selection state carried between FindSupportSet calls. */
+typedef struct {
+  int num_bins, max_bin, k_bin, sum;
+  float alpha, min_val;
+} gb_bin_state;
+
+const char *gb_cs_version(void);
+const char *gb_cs_last_error(void);
+
+/* Reference defaults for `alg` and signal length n (GAGA/gaga/gaga_gen.cu:176-197,
+ * gaga_smv.cu:239-258). */
+void gb_cs_default_options(gb_options *o, const char *alg, int n);
+
+/* Reference algorithm number for an algorithm string, or -1 (gaga_gen.cu:65, gaga_smv.cu:97-107). */
+int gb_cs_alg_id(const char *alg);
+
+/* "Solve given data": [x, iters, convRate] = gaga_gen(alg, y, A, k, opts)
+ * (GAGA/gaga/gaga_gen.cu:115-134,560-563,730-743), gaga_dct(alg, y, rows, k, m, n, opts)
+ * (gaga_dct.cu:88-127,540-544) and [x, iters, convRate, resRecord, timeRecord] =
+ * gaga_smv(alg, y, rows, cols, vals, k, opts) (gaga_smv.cu:131-195,675-688).
+ * x_out has n floats at p->location. */
+gb_status gb_cs_solve(const char *alg, const gb_problem *p, const gb_options *o, float *x_out,
+                      gb_result *r);
+
+/* "Generate and solve": [norms, times, iters, support, convRate, xout] =
+ * gaga_gen(alg, k, m, n, opts) (gaga_gen.cu:90-114,535-559), gaga_dct(alg, k, m, n, opts),
+ * gaga_smv(alg, k, m, n, d, opts).  The problem is drawn on the device from o->seed
+ * (Philox-4x32-10 instead of cuRAND).  x_out / x_true_out are host buffers of n floats
+ * (x_true_out may be NULL). */
+gb_status gb_cs_generate_and_solve(const char *alg, int kind, int k, int m, int n, int d,
+                                   const gb_options *o, float *x_out, float *x_true_out,
+                                   gb_result *r);
+
+/* ---- component entry points (device pointers; replace the reference's L1/L2 routines) ---- */
+
+/* LinearBinning (GAGA/gaga/kernels.cu:135-146): bins[i] for every i; counters[b]
+ * incremented for b < max_bin.  counters must hold num_bins ints and is NOT cleared. */
+gb_status gb_cs_linear_binning(const float *d_v, int n, int num_bins, int max_bin, float slope,
+                               float intercept, int *d_bins, int *d_counters, void *stream);
+
+/* FindSupportSet (GAGA/gaga/functions.cu:397-436) followed by Threshold
+ * (functions.cu:374-378) when threshold_v != 0.  `st` (host) is read and updated.
+ * d_counters may be NULL. */
+gb_status gb_cs_find_support_set(float *d_v, int n, int k, float slope, float intercept,
+                                 float max_change, gb_bin_state *st, int *d_bins,
+                                 int *d_counters, int threshold_v, void *stream);
+
+/* A_gen/AT_gen (GAGA/Matrices/gen_gpu.cu:141-171), A_dct/AT_dct (dct_gpu.cu:328-353),
+ * A_smv/AT_smv (smv_gpu.cu:108-135): out = A in (transpose 0) or A^T in (transpose 1).
+ * p->location must be GB_DEVICE; y/k are ignored. */
+gb_status gb_cs_operator_apply(const gb_problem *p, int transpose, const float *d_in, float *d_out);
+
+/* One parallel_l0 iteration body (cuda_compute_scores_l0 + cuda_update_residual,
+ * GAGA/gaga/expander/kernels.cu:3-14,353-388) on column-grouped 0-based rows.
+ * Returns the candidate flag in *found. */
+gb_status gb_cs_l0_step(float *d_res, float *d_x, float *d_updates, const int *d_rows, int m, int n,
+                        int d, int thresh, int shift, int *found, void *stream);
+
+/* ---- batched form (no reference counterpart: the reference solves one trial per call) ----
+ * Thousands of independent dense Gaussian trials, each with its own (n, m, k) and its own
+ * A drawn on the device from (seed, trial id), solved by NIHT or CGIHT in one persistent
+ * launch.  Per-trial outputs (host or device arrays of ntrials entries, any may be NULL):
+ * iterations, relative l2 error against the generated x, and a verdict flag
+ * (rel l2 <= 1e-3).  tol_rel is relative to ||y||. */
+typedef struct {
+  int ntrials;
+  const int *n, *m, *k;          /* host arrays */
+  const unsigned int *trial_id;  /* host array (NULL: 0..ntrials-1) */
+  unsigned int seed;
+  int alg;                       /* GB_ALG_NIHT or GB_ALG_CGIHT */
+  float tol_rel;
+  int maxiter;
+  int use_learned;               /* reserved, must be 0 */
+  void *stream;
+} gb_batch;
+
+gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float *rel_err_out,
+                            int *success_out, int *num_success);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

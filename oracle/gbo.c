@@ -1,0 +1,937 @@
+/*
+ * gbo.c -- CPU oracle (test infrastructure only; see gbo.h).
+ *
+ * Build: oracle/build.py (gcc -O2 -fopenmp -ffp-contract=off).  Floating-point
+ * contraction is disabled so that every multiply-add below is exactly the
+ * operation written; where the reference's nvcc build fuses a multiply-add
+ * (cuBLAS saxpy, `slope * intercept + 1.0f` in LinearBinning) an explicit fmaf
+ * is written instead.
+ */
+#include "gbo.h"
+
+#include <float.h>
+#include <limits.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ------------------------------------------------------------------ */
+/* Philox-4x32-10 (Salmon, Moraes, Dror, Shaw: "Parallel random numbers: as easy
+ * as 1, 2, 3", SC'11).  The reference uses cuRAND's default generator, which is
+ * not reproducible outside that closed library; problems are therefore generated
+ * from this counter-based generator and handed to every implementation. */
+void gbo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+  uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+  uint32_t k0 = key[0], k1 = key[1];
+  for (int r = 0; r < 10; ++r) {
+    uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+    uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+  }
+  out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+/* uniform on (0,1): 24 random bits, centred in their cell (exact in float) */
+float gbo_u01(uint32_t x) { return ((float)(x >> 8) + 0.5f) * (1.0f / 16777216.0f); }
+
+enum { ST_MATRIX = 1, ST_VALUES = 2, ST_SUPPORT = 3, ST_ROWS = 4, ST_SMV = 5, ST_SIGNS = 6 };
+static const uint32_t KEY_HI = 0x6A09E667u;
+
+static void draw4(uint32_t seed, uint32_t trial, uint32_t stream, uint64_t block, uint32_t out[4]) {
+  uint32_t ctr[4] = {(uint32_t)block, (uint32_t)(block >> 32), stream, trial};
+  uint32_t key[2] = {seed, KEY_HI};
+  gbo_philox4x32_10(ctr, key, out);
+}
+
+static float box_muller(uint32_t a, uint32_t b, int second) {
+  double u1 = gbo_u01(a), u2 = gbo_u01(b);
+  double r = sqrt(-2.0 * log(u1));
+  double t = 6.283185307179586 * u2;
+  return (float)(second ? r * sin(t) : r * cos(t));
+}
+
+/* element e of a gaussian stream: one Philox call gives 4 normals */
+static float gauss_at(uint32_t seed, uint32_t trial, uint32_t stream, uint64_t e) {
+  uint32_t o[4];
+  draw4(seed, trial, stream, e >> 2, o);
+  int lane = (int)(e & 3);
+  return lane < 2 ? box_muller(o[0], o[1], lane) : box_muller(o[2], o[3], lane - 2);
+}
+
+static float uniform_at(uint32_t seed, uint32_t trial, uint32_t stream, uint64_t e) {
+  uint32_t o[4];
+  draw4(seed, trial, stream, e >> 2, o);
+  return gbo_u01(o[e & 3]);
+}
+
+/* createMeasurements_gen (GAGA/gaga/createMeasurements_gen.cu:81-100): N(0,1) or
+ * +-1 entries, scaled by 1/sqrt(m) in float. */
+void gbo_gen_dense(int m, int n, int lda, int ens, uint32_t seed, uint32_t trial, float *A) {
+  float scale = sqrtf((float)m);
+  scale = 1.0f / scale;
+#pragma omp parallel for schedule(static)
+  for (int j = 0; j < n; ++j) {
+    for (int i = 0; i < m; ++i) {
+      uint64_t e = (uint64_t)j * (uint64_t)m + (uint64_t)i;
+      float v;
+      if (ens == 2) v = signbit(uniform_at(seed, trial, ST_MATRIX, e) - 0.5f) ? -1.0f : 1.0f;
+      else v = gauss_at(seed, trial, ST_MATRIX, e);
+      A[(size_t)j * lda + i] = v * scale;
+    }
+    for (int i = m; i < lda; ++i) A[(size_t)j * lda + i] = 0.0f;
+  }
+}
+
+/* createVector (GAGA/gaga/createVector.cu:207-300) with the value distributions of
+ * createProblem_gen (GAGA/gaga/createProblem_gen.cu:70-95 / sign_pattern). */
+int gbo_gen_vector(int n, int k, int vec_dist, uint32_t seed, uint32_t trial, float *x) {
+  float *vals = (float *)malloc(sizeof(float) * n);
+  float *keys = (float *)malloc(sizeof(float) * n);
+  int *bins = (int *)malloc(sizeof(int) * n);
+  int *cnt = (int *)calloc((size_t)n, sizeof(int));
+  for (int i = 0; i < n; ++i) {
+    float u = uniform_at(seed, trial, ST_VALUES, (uint64_t)i);
+    if (vec_dist == 1) vals[i] = signbit(u - 0.5f) ? -1.0f : 1.0f;
+    else if (vec_dist == 2) vals[i] = gauss_at(seed, trial, ST_VALUES, (uint64_t)i);
+    else vals[i] = u;
+    keys[i] = uniform_at(seed, trial, ST_SUPPORT, (uint64_t)i);
+  }
+  float max_value = gbo_max_magnitude(keys, n);
+  float slope = ((float)(n - 1) / max_value);
+  gbo_linear_binning(keys, n, n, n, slope, max_value, bins, cnt);
+  int k_bin = 0, sum = 0;
+  while ((sum < k) & (k_bin < n)) { sum += cnt[k_bin]; k_bin++; }
+  k_bin -= 1;
+  for (int i = 0; i < n; ++i) x[i] = (bins[i] <= k_bin) ? vals[i] : 0.0f;
+  free(vals); free(keys); free(bins); free(cnt);
+  return sum;
+}
+
+void gbo_gen_dct_rows(int n, int m, uint32_t seed, uint32_t trial, int *rows) {
+  int *idx = (int *)malloc(sizeof(int) * n);
+  for (int i = 0; i < n; ++i) idx[i] = i;
+  for (int j = n - 1; j > n - m; --j) {
+    float u = uniform_at(seed, trial, ST_ROWS, (uint64_t)j);
+    int kk = (int)((float)j * u);
+    int t = idx[j]; idx[j] = idx[kk]; idx[kk] = t;
+  }
+  for (int j = 0; j < m; ++j) rows[j] = idx[n - 1 - j];
+  free(idx);
+}
+
+void gbo_gen_smv(int m, int n, int d, int ens, uint32_t seed, uint32_t trial, int *rows, float *vals) {
+  float scale = 1.0f;
+  if (ens == 1 || ens == 2) { scale = sqrtf((float)d); scale = 1.0f / scale; }
+#pragma omp parallel for schedule(static)
+  for (int j = 0; j < n; ++j) {
+    int have = 0;
+    uint64_t draw = 0;
+    while (have < d) {
+      uint32_t o[4];
+      uint32_t ctr[4] = {(uint32_t)j, (uint32_t)draw, ST_SMV, trial};
+      uint32_t key[2] = {seed, KEY_HI};
+      gbo_philox4x32_10(ctr, key, o);
+      draw++;
+      for (int q = 0; q < 4 && have < d; ++q) {
+        int r = (int)((float)m * gbo_u01(o[q]));
+        if (r == m) r = m - 1;
+        int dup = 0;
+        for (int t = 0; t < have; ++t) dup |= (rows[(size_t)j * d + t] == r);
+        if (!dup) rows[(size_t)j * d + have++] = r;
+      }
+    }
+    for (int t = 0; t < d; ++t) {
+      float v = 1.0f;
+      if (ens == 2) v = signbit(uniform_at(seed, trial, ST_SIGNS, (uint64_t)j * d + t) - 0.5f) ? -1.0f : 1.0f;
+      vals[(size_t)j * d + t] = v * scale;
+    }
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* reductions: FP64 accumulation, FP32 result */
+static float dotf(const float *a, const float *b, int n) {
+  double s = 0.0;
+  for (int i = 0; i < n; ++i) s += (double)a[i] * (double)b[i];
+  return (float)s;
+}
+static float nrm2f(const float *a, int n) {
+  double s = 0.0;
+  for (int i = 0; i < n; ++i) s += (double)a[i] * (double)a[i];
+  return (float)sqrt(s);
+}
+/* cublasSaxpy: y = alpha*x + y, fused */
+static void saxpy(int n, float alpha, const float *x, float *y) {
+  for (int i = 0; i < n; ++i) y[i] = fmaf(alpha, x[i], y[i]);
+}
+static void sscal(int n, float alpha, float *x) {
+  for (int i = 0; i < n; ++i) x[i] = alpha * x[i];
+}
+
+/* MaxMagnitude (GAGA/gaga/functions.cu:382-393): |v| at the first index of max |v| */
+float gbo_max_magnitude(const float *v, int n) {
+  float best = -1.0f;
+  for (int i = 0; i < n; ++i) {
+    float a = fabsf(v[i]);
+    if (a > best) best = a;
+  }
+  return best < 0.0f ? 0.0f : best;
+}
+
+/* ------------------------------------------------------------------ */
+/* Operators */
+
+static void dense_A(const gbo_op *op, const float *x, float *y) {
+  int m = op->m, n = op->n, lda = op->lda;
+  int *nz = (int *)malloc(sizeof(int) * (n > 0 ? n : 1));
+  int cnt = 0;
+  for (int j = 0; j < n; ++j)
+    if (x[j] != 0.0f) nz[cnt++] = j;
+  /* gen_matvec_sparse (GAGA/Matrices/gen_gpu.cu:79-132) reads only the
+   * columns where x is nonzero */
+#pragma omp parallel for schedule(static)
+  for (int i0 = 0; i0 < m; i0 += 256) {
+    int i1 = i0 + 256 < m ? i0 + 256 : m;
+    float acc[256];
+    for (int i = i0; i < i1; ++i) acc[i - i0] = 0.0f;
+    for (int t = 0; t < cnt; ++t) {
+      int j = nz[t];
+      float xj = x[j];
+      const float *col = op->A + (size_t)j * lda;
+      for (int i = i0; i < i1; ++i) acc[i - i0] = acc[i - i0] + col[i] * xj;
+    }
+    for (int i = i0; i < i1; ++i) y[i] = acc[i - i0];
+  }
+  free(nz);
+}
+
+static void dense_AT(const gbo_op *op, const float *r, float *g) {
+  int m = op->m, n = op->n, lda = op->lda;
+#pragma omp parallel for schedule(static)
+  for (int j = 0; j < n; ++j) {
+    const float *col = op->A + (size_t)j * lda;
+    float s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int i = 0;
+    for (; i + 8 <= m; i += 8)
+      for (int q = 0; q < 8; ++q) s[q] = s[q] + col[i + q] * r[i + q];
+    for (; i < m; ++i) s[0] = s[0] + col[i] * r[i];
+    g[j] = ((s[0] + s[1]) + (s[2] + s[3])) + ((s[4] + s[5]) + (s[6] + s[7]));
+  }
+}
+
+/* iterative radix-2 complex FFT in double; sign -1 forward, +1 inverse (unnormalised) */
+static void fft_d(double *re, double *im, int N, int sign) {
+  for (int i = 1, j = 0; i < N; ++i) {
+    int bit = N >> 1;
+    for (; j & bit; bit >>= 1) j ^= bit;
+    j ^= bit;
+    if (i < j) {
+      double t = re[i]; re[i] = re[j]; re[j] = t;
+      t = im[i]; im[i] = im[j]; im[j] = t;
+    }
+  }
+  for (int len = 2; len <= N; len <<= 1) {
+    double ang = sign * 2.0 * M_PI / len;
+    int half = len >> 1;
+#pragma omp parallel for schedule(static) if (N >= (1 << 16))
+    for (int i = 0; i < N; i += len) {
+      for (int q = 0; q < half; ++q) {
+        double wr = cos(ang * q), wi = sin(ang * q);
+        double ur = re[i + q], ui = im[i + q];
+        double vr = re[i + q + half] * wr - im[i + q + half] * wi;
+        double vi = re[i + q + half] * wi + im[i + q + half] * wr;
+        re[i + q] = ur + vr; im[i + q] = ui + vi;
+        re[i + q + half] = ur - vr; im[i + q + half] = ui - vi;
+      }
+    }
+  }
+}
+
+/* Orthonormal DCT-II by Makhoul's reordering (as GAGA/Matrices/dct_gpu.cu:121-206,
+ * __split + C2C + __fft2dct), evaluated in FP64. */
+void gbo_dct2(int N, const float *x, float *out) {
+  double *re = (double *)malloc(sizeof(double) * N), *im = (double *)calloc((size_t)N, sizeof(double));
+  for (int m = 0; m < N / 2; ++m) { re[m] = x[2 * m]; re[N - 1 - m] = x[2 * m + 1]; }
+  fft_d(re, im, N, -1);
+  for (int k = 0; k < N; ++k) {
+    double f = k * M_PI / (2.0 * N);
+    double w = k == 0 ? sqrt(1.0 / N) : sqrt(2.0 / N);
+    out[k] = (float)(w * (re[k] * cos(f) + im[k] * sin(f)));
+  }
+  free(re); free(im);
+}
+
+/* Its transpose, DCT-III (as __dct2fft + inverse C2C + __gather, dct_gpu.cu:121-206,287-314) */
+void gbo_dct3(int N, const float *X, float *out) {
+  double *re = (double *)malloc(sizeof(double) * N), *im = (double *)malloc(sizeof(double) * N);
+  for (int k = 0; k < N; ++k) {
+    double f = k * M_PI / (2.0 * N);
+    double w = k == 0 ? sqrt(1.0 / N) : sqrt(2.0 / N);
+    re[k] = w * X[k] * cos(f);
+    im[k] = w * X[k] * sin(f);
+  }
+  fft_d(re, im, N, +1);
+  for (int m = 0; m < N / 2; ++m) { out[2 * m] = (float)re[m]; out[2 * m + 1] = (float)re[N - 1 - m]; }
+  free(re); free(im);
+}
+
+static void dct_A(const gbo_op *op, const float *x, float *y) {
+  float *full = (float *)malloc(sizeof(float) * op->n);
+  gbo_dct2(op->n, x, full);
+  for (int i = 0; i < op->m; ++i) y[i] = full[op->dct_rows[i]];
+  free(full);
+}
+
+static void dct_AT(const gbo_op *op, const float *r, float *g) {
+  float *full = (float *)calloc((size_t)op->n, sizeof(float));
+  for (int i = 0; i < op->m; ++i) full[op->dct_rows[i]] = r[i];
+  gbo_dct3(op->n, full, g);
+  free(full);
+}
+
+/* sparse_matvec / sparse_matvecT (GAGA/Matrices/smv_gpu.cu:29-47); nonzeros summed in
+ * storage order (the reference's atomicAdd order is unspecified) */
+static void smv_A(const gbo_op *op, const float *x, float *y) {
+  int d = op->d;
+  for (int i = 0; i < op->m; ++i) y[i] = 0.0f;
+  for (int j = 0; j < op->n; ++j) {
+    if (x[j] == 0.0f) continue;
+    for (int t = 0; t < d; ++t) {
+      float v = op->smv_vals[(size_t)j * d + t] * x[j];
+      if (v != 0.0f) y[op->smv_rows[(size_t)j * d + t]] += v;
+    }
+  }
+}
+
+static void smv_AT(const gbo_op *op, const float *r, float *g) {
+  int d = op->d;
+#pragma omp parallel for schedule(static)
+  for (int j = 0; j < op->n; ++j) {
+    float s = 0.0f;
+    for (int t = 0; t < d; ++t) s = s + op->smv_vals[(size_t)j * d + t] * r[op->smv_rows[(size_t)j * d + t]];
+    g[j] = s;
+  }
+}
+
+void gbo_A(const gbo_op *op, const float *x, float *y) {
+  if (op->kind == GBO_OP_DENSE) dense_A(op, x, y);
+  else if (op->kind == GBO_OP_DCT) dct_A(op, x, y);
+  else smv_A(op, x, y);
+}
+void gbo_AT(const gbo_op *op, const float *r, float *g) {
+  if (op->kind == GBO_OP_DENSE) dense_AT(op, r, g);
+  else if (op->kind == GBO_OP_DCT) dct_AT(op, r, g);
+  else smv_AT(op, r, g);
+}
+
+/* ------------------------------------------------------------------ */
+/* Support selection */
+
+/* float -> int32 conversion with round-toward-zero and saturation, NaN -> 0: the
+ * semantics of the GPU conversion the reference kernel performs when it stores a
+ * float expression into an int (cvt.rzi.s32.f32). */
+int gbo_f2i_rz(float v) {
+  if (v != v) return 0;
+  if (v >= 2147483648.0f) return INT_MAX;
+  if (v <= -2147483648.0f) return INT_MIN;
+  return (int)v;
+}
+
+/* LinearBinning (GAGA/gaga/kernels.cu:135-146).  The magnitude test is done in double
+ * (`intercept * .000001` is a double product); bins use FP32 `slope*(intercept-t)`
+ * clamped at 0; tiny entries get bin (int)(slope*intercept + 1.0f), which nvcc
+ * contracts to one fused multiply-add. */
+void gbo_linear_binning(const float *v, int n, int num_bins, int max_bin, float slope,
+                        float intercept, int *bins, int *counters) {
+  (void)num_bins;
+  double small = (double)intercept * 0.000001;
+  for (int i = 0; i < n; ++i) {
+    float t = fabsf(v[i]);
+    if ((double)t > small) {
+      float b = slope * (intercept - t);
+      int bi = gbo_f2i_rz(fmaxf(0.0f, b));
+      bins[i] = bi;
+      if (bi < max_bin) counters[bi] += 1;
+    } else {
+      bins[i] = gbo_f2i_rz(fmaf(slope, intercept, 1.0f));
+    }
+  }
+}
+
+/* FindSupportSet (GAGA/gaga/functions.cu:397-436) */
+int gbo_find_support_set(const float *v, int *bins, int *counters, float slope, float intercept,
+                         float max_change, gbo_bin_state *st, int n, int k) {
+  float min_val = st->min_val;
+  int max_bin = st->max_bin;
+  int k_bin = st->k_bin;
+  int sum = st->sum; /* the reference returns an uninitialised sum on this path */
+  if (min_val > max_change) {
+    min_val = min_val - max_change;
+  } else {
+    memset(counters, 0, sizeof(int) * st->num_bins);
+    gbo_linear_binning(v, n, st->num_bins, max_bin, slope, intercept, bins, counters);
+    k_bin = 0;
+    sum = 0;
+    while ((sum < k) & (k_bin < max_bin)) {
+      sum = sum + counters[k_bin];
+      k_bin++;
+    }
+    k_bin = k_bin - 1;
+    if (sum < k) {
+      st->alpha = st->alpha * 0.5f;
+      st->max_bin = (int)((float)st->num_bins * (1.0f - st->alpha));
+    }
+    min_val = intercept - (float)(k_bin + 1) / slope;
+  }
+  st->min_val = min_val;
+  st->k_bin = k_bin;
+  st->sum = sum;
+  return sum;
+}
+
+/* threshold (GAGA/gaga/kernels.cu:74-81) */
+void gbo_threshold(float *v, const int *bins, int k_bin, int n) {
+  for (int i = 0; i < n; ++i)
+    if (bins[i] > k_bin) v[i] = 0.0f;
+}
+
+/* zero_vector_float + threshold_one (GAGA/gaga/kernels.cu:64-71,100-105) */
+static void masked_copy(const float *src, float *dst, const int *bins, int k_bin, int n) {
+  for (int i = 0; i < n; ++i) dst[i] = (bins[i] <= k_bin) ? src[i] : 0.0f;
+}
+
+/* ------------------------------------------------------------------ */
+/* Solver workspace */
+typedef struct {
+  const gbo_op *op;
+  int m, n, k;
+  const float *y;
+  float *x, *xt, *grad, *gp, *gpt, *resid, *ru;
+  int *bins, *bins_prev, *counters;
+  float prev[16];
+} ws_t;
+
+static void push16(float *a, float v) {
+  for (int j = 0; j < 15; ++j) a[j] = a[j + 1];
+  a[15] = v;
+}
+
+static float max_list(const float *a, int n) {
+  float m = a[0];
+  for (int j = 1; j < n; ++j)
+    if (a[j] > m) m = a[j];
+  return m;
+}
+
+/* resid = y - A x, via copy + saxpy(-1) as the reference does */
+static void residual(ws_t *w, const float *x, float *resid, float *tmp) {
+  gbo_A(w->op, x, tmp);
+  for (int i = 0; i < w->m; ++i) resid[i] = fmaf(-1.0f, tmp[i], w->y[i]);
+}
+
+/* RestrictedSD_S_gen (GAGA/gaga/functions.cu:659-745) */
+static float restricted_sd(ws_t *w, int k_bin) {
+  int m = w->m, n = w->n;
+  residual(w, w->x, w->resid, w->ru);
+  push16(w->prev, nrm2f(w->resid, m));
+  gbo_AT(w->op, w->resid, w->grad);
+  masked_copy(w->grad, w->xt, w->bins, k_bin, n);
+  gbo_A(w->op, w->xt, w->ru);
+  float err = nrm2f(w->ru, m);
+  float mu = nrm2f(w->xt, n);
+  if (mu < 400.0f * err) {
+    mu = mu / err;
+    mu = mu * mu;
+  } else {
+    mu = 0.0f;
+  }
+  saxpy(n, mu, w->grad, w->x);
+  return 2.0f * mu * gbo_max_magnitude(w->grad, n);
+}
+
+/* RestrictedCG_S_gen (GAGA/gaga/functions.cu:922-1000); prevCG receives ||y-Ax||^2 */
+static void restricted_cg(ws_t *w, float *prevcg, float *mu, int k_bin) {
+  int m = w->m, n = w->n;
+  float alpha, beta;
+  gbo_A(w->op, w->grad, w->resid);
+  alpha = dotf(w->resid, w->resid, m);
+  if (*mu < 1000.0f * alpha) alpha = *mu / alpha;
+  else alpha = 0.0f;
+  saxpy(n, alpha, w->grad, w->x);
+  gbo_AT(w->op, w->resid, w->xt);
+  gbo_threshold(w->xt, w->bins, k_bin, n);
+  saxpy(n, -alpha, w->xt, w->gp);
+  beta = *mu;
+  *mu = dotf(w->gp, w->gp, n);
+  if (*mu < 1000.0f * beta) beta = *mu / beta;
+  else beta = 0.0f;
+  sscal(n, beta, w->grad);
+  saxpy(n, 1.0f, w->gp, w->grad);
+  for (int j = 0; j < 15; ++j) prevcg[j] = prevcg[j + 1];
+  residual(w, w->x, w->resid, w->ru);
+  prevcg[15] = dotf(w->resid, w->resid, m);
+}
+
+/* RestrictedCGwithSupportEvolution_S_gen (GAGA/gaga/functions.cu:1004-1102) */
+static float rcg_support_evolution(ws_t *w, float *mu, int beta_to_zero, int k_bin) {
+  int m = w->m, n = w->n;
+  float alpha, beta;
+  residual(w, w->x, w->resid, w->ru);
+  push16(w->prev, nrm2f(w->resid, m));
+  gbo_AT(w->op, w->resid, w->grad);
+  masked_copy(w->grad, w->xt, w->bins, k_bin, n);
+  if (beta_to_zero == 1) {
+    beta = 0.0f;
+    *mu = dotf(w->xt, w->xt, n);
+  } else {
+    beta = *mu;
+    *mu = dotf(w->xt, w->xt, n);
+    if (*mu < 1000.0f * beta) beta = *mu / beta;
+    else beta = 0.0f;
+  }
+  sscal(n, beta, w->gp);
+  saxpy(n, 1.0f, w->grad, w->gp);
+  masked_copy(w->gp, w->gpt, w->bins, k_bin, n);
+  gbo_A(w->op, w->gpt, w->ru);
+  alpha = dotf(w->ru, w->ru, m);
+  if (*mu < 1000.0f * alpha) alpha = *mu / alpha;
+  else alpha = 0.0f;
+  saxpy(n, alpha, w->gp, w->x);
+  return 2.0f * alpha * gbo_max_magnitude(w->gp, n);
+}
+
+/* UnrestrictedCG_S_gen (GAGA/gaga/functions.cu:1107-1220) */
+static float unrestricted_cg(ws_t *w, float *mu, int beta_to_zero, int k_bin) {
+  int m = w->m, n = w->n;
+  gbo_A(w->op, w->x, w->ru);
+  saxpy(m, -1.0f, w->y, w->ru);
+  sscal(m, -1.0f, w->ru);
+  push16(w->prev, nrm2f(w->ru, m));
+  gbo_AT(w->op, w->ru, w->grad);
+  masked_copy(w->grad, w->xt, w->bins, k_bin, n);
+  gbo_A(w->op, w->gpt, w->resid);
+  gbo_A(w->op, w->xt, w->ru);
+  float beta;
+  if (beta_to_zero == 1) {
+    beta = 0.0f;
+  } else {
+    float bn = dotf(w->resid, w->ru, m);
+    float bd = dotf(w->resid, w->resid, m);
+    beta = -bn / bd;
+  }
+  sscal(n, beta, w->gp);
+  saxpy(n, 1.0f, w->grad, w->gp);
+  masked_copy(w->gp, w->gpt, w->bins, k_bin, n);
+  sscal(m, beta, w->resid);
+  saxpy(m, 1.0f, w->ru, w->resid);
+  float an = dotf(w->gpt, w->xt, n);
+  float ad = dotf(w->resid, w->resid, m);
+  float alpha = an / ad;
+  saxpy(n, alpha, w->gp, w->x);
+  *mu = dotf(w->xt, w->xt, n);
+  return 2.0f * alpha * gbo_max_magnitude(w->gp, n);
+}
+
+/* The stopping bookkeeping shared by the loops (e.g. GAGA/gaga/algorithms.cu:1398-1421). */
+typedef struct {
+  float err, err_start, tol, resid_diff, evol[16];
+  int fail, cycle;
+} stop_t;
+
+static int keep_going(const stop_t *s, int iter, int maxiter) {
+  return (s->err > s->tol) & (iter < maxiter) & (s->err < (100.0f * s->err_start)) &
+         ((double)s->resid_diff > 0.01 * (double)s->tol) & (s->fail == 0) & (s->cycle != 0);
+}
+
+static void stop_update(stop_t *s, const float *prev, int iter, int fail_after) {
+  for (int j = 0; j < 15; ++j) s->evol[j] = s->evol[j + 1];
+  s->evol[15] = prev[14] - prev[15];
+  s->resid_diff = max_list(s->evol, 16);
+  for (int j = 0; j < 15; ++j)
+    if ((prev[15] == prev[j]) && (iter > 4)) s->cycle = 0;
+  if (iter > fail_after) {
+    float root = 1.0f / 15.0f;
+    float rate = prev[15] / prev[0];
+    rate = powf(rate, root);
+    if (rate > 0.999f) s->fail = 1;
+  }
+}
+
+int gbo_solve(const gbo_op *op, const float *y, int k, const gbo_opts *o, float *x, gbo_info *info) {
+#ifdef _OPENMP
+  int saved_threads = omp_get_max_threads();
+  if (o->threads > 0) omp_set_num_threads(o->threads);
+#endif
+  ws_t w;
+  memset(&w, 0, sizeof(w));
+  w.op = op; w.m = op->m; w.n = op->n; w.k = k; w.y = y; w.x = x;
+  int m = op->m, n = op->n;
+  w.xt = (float *)calloc((size_t)n, sizeof(float));
+  w.grad = (float *)calloc((size_t)n, sizeof(float));
+  w.gp = (float *)calloc((size_t)n, sizeof(float));
+  w.gpt = (float *)calloc((size_t)n, sizeof(float));
+  w.resid = (float *)calloc((size_t)m, sizeof(float));
+  w.ru = (float *)calloc((size_t)m, sizeof(float));
+  w.bins = (int *)calloc((size_t)n, sizeof(int));
+  w.bins_prev = (int *)calloc((size_t)n, sizeof(int));
+  w.counters = (int *)calloc((size_t)o->num_bins, sizeof(int));
+
+  gbo_bin_state bs;
+  bs.num_bins = o->num_bins;
+  bs.alpha = 0.25f;
+  bs.max_bin = (int)((float)o->num_bins * (1.0f - bs.alpha));
+  bs.min_val = 0.0f;
+  bs.k_bin = 0;
+  bs.sum = 0;
+  int iter = 0;
+  float mu = 0.0f;
+
+  stop_t s;
+  memcpy(w.resid, y, sizeof(float) * m);
+  s.err = nrm2f(w.resid, m);
+  s.err_start = s.err;
+  s.tol = o->tol;
+  s.resid_diff = 1.0f;
+  for (int j = 0; j < 16; ++j) { w.prev[j] = 0.0f; s.evol[j] = 1.0f; }
+  s.fail = 0;
+  s.cycle = 1;
+
+  /* Set the linear bins: x = H_k(A^T y) */
+  gbo_AT(op, y, x);
+  float max_value = gbo_max_magnitude(x, n);
+  float slope = ((float)(o->num_bins - 1) / max_value);
+  /* HTP (and NIHT_dct) pass max_value as maxChange to force binning; with
+   * minVal = 0 every algorithm bins here. */
+  gbo_find_support_set(x, w.bins, w.counters, slope, max_value,
+                       o->alg == GBO_HTP ? max_value : 1.0f, &bs, n, k);
+  gbo_threshold(x, w.bins, bs.k_bin, n);
+
+  if (o->alg == GBO_NIHT) {
+    /* NIHT_S_gen (GAGA/gaga/algorithms.cu:1274-1441) */
+    while (keep_going(&s, iter, o->maxiter)) {
+      float max_change = restricted_sd(&w, bs.k_bin);
+      if (bs.min_val <= max_change) {
+        max_value = gbo_max_magnitude(x, n);
+        slope = ((float)(o->num_bins - 1) / max_value);
+      }
+      gbo_find_support_set(x, w.bins, w.counters, slope, max_value, max_change, &bs, n, k);
+      gbo_threshold(x, w.bins, bs.k_bin, n);
+      s.err = w.prev[15];
+      stop_update(&s, w.prev, iter, 749);
+      iter++;
+    }
+  } else if (o->alg == GBO_HTP) {
+    /* HTP_S_gen (GAGA/gaga/algorithms.cu:2491-2716) */
+    float tol_cg = s.tol * s.tol;
+    float tol2 = 10.0f * tol_cg;
+    while (keep_going(&s, iter, o->maxiter)) {
+      float max_change = restricted_sd(&w, bs.k_bin);
+      if (bs.min_val <= max_change) {
+        max_value = gbo_max_magnitude(x, n);
+        slope = ((float)(o->num_bins - 1) / max_value);
+      }
+      gbo_find_support_set(x, w.bins, w.counters, slope, max_value, max_change, &bs, n, k);
+      gbo_threshold(x, w.bins, bs.k_bin, n);
+      float prevcg[16], evolcg[16];
+      for (int j = 0; j < 16; ++j) { prevcg[j] = 0.0f; evolcg[j] = 1.0f; }
+      float diffcg = 1.0f;
+      prevcg[15] = w.prev[15];
+      residual(&w, x, w.resid, w.ru);
+      gbo_AT(op, w.resid, w.grad);
+      gbo_threshold(w.grad, w.bins, bs.k_bin, n);
+      memcpy(w.gp, w.grad, sizeof(float) * n);
+      mu = dotf(w.gp, w.gp, n);
+      float errcg = dotf(w.resid, w.resid, m);
+      prevcg[15] = errcg;
+      int itcg = 0;
+      while ((errcg > tol_cg) & (itcg < 15) & (diffcg > tol2)) {
+        restricted_cg(&w, prevcg, &mu, bs.k_bin);
+        errcg = prevcg[15];
+        itcg++;
+        for (int j = 0; j < 15; ++j) evolcg[j] = evolcg[j + 1];
+        evolcg[15] = prevcg[14] - prevcg[15];
+        diffcg = max_list(evolcg, 16);
+      }
+      s.err = sqrtf(errcg);
+      push16(w.prev, s.err);
+      stop_update(&s, w.prev, iter, 125);
+      iter++;
+    }
+  } else if (o->alg == GBO_CGIHT) {
+    /* CGIHT_S_gen (GAGA/gaga/algorithms.cu:3689-3942) */
+    residual(&w, x, w.resid, w.ru);
+    s.err = nrm2f(w.resid, m);
+    w.prev[15] = s.err;
+    gbo_AT(op, w.resid, w.gp);
+    masked_copy(w.gp, w.gpt, w.bins, bs.k_bin, n);
+    for (int j = 0; j < 15; ++j) s.evol[j] = s.evol[j + 1];
+    s.evol[15] = w.prev[14] - w.prev[15];
+    int beta_to_zero = 1, supp_change = 1, k_bin_prev = 0;
+    while (keep_going(&s, iter, o->maxiter)) {
+      float max_change;
+      if (o->restart) max_change = rcg_support_evolution(&w, &mu, beta_to_zero, bs.k_bin);
+      else if (supp_change) max_change = unrestricted_cg(&w, &mu, beta_to_zero, bs.k_bin);
+      else max_change = rcg_support_evolution(&w, &mu, beta_to_zero, bs.k_bin);
+      beta_to_zero = 0;
+      if (bs.min_val <= max_change) {
+        max_value = gbo_max_magnitude(x, n);
+        slope = ((float)(o->num_bins - 1) / max_value);
+        memcpy(w.bins_prev, w.bins, sizeof(int) * n);
+        k_bin_prev = bs.k_bin;
+        gbo_find_support_set(x, w.bins, w.counters, slope, max_value, max_change, &bs, n, k);
+        /* checkSupportEvolution (GAGA/gaga/kernels.cu:178-193), race-free form */
+        int changed = 0;
+        for (int i = 0; i < n; ++i)
+          if (w.bins_prev[i] <= k_bin_prev && w.bins[i] > bs.k_bin) changed = 1;
+        supp_change = changed;
+        if (supp_change) {
+          if (o->restart) beta_to_zero = 1;
+          else masked_copy(w.gp, w.gpt, w.bins, bs.k_bin, n);
+        }
+      } else {
+        supp_change = 0;
+        bs.min_val = bs.min_val - max_change;
+      }
+      gbo_threshold(x, w.bins, bs.k_bin, n);
+      s.err = w.prev[15];
+      stop_update(&s, w.prev, iter, 749);
+      iter++;
+    }
+  }
+
+  if (info) {
+    info->iter = iter;
+    info->sum = bs.sum;
+    info->k_bin = bs.k_bin;
+    memcpy(info->resid_prev, w.prev, sizeof(w.prev));
+    /* given-data convRate (GAGA/gaga/gaga_gen.cu:733-741) */
+    int temp = iter < 16 ? iter : 16;
+    if (temp > 0) {
+      float root = 1.0f / (float)temp;
+      temp = 16 - temp;
+      info->conv_rate = powf(w.prev[15] / w.prev[temp], root);
+    } else {
+      info->conv_rate = 0.0f;
+    }
+  }
+  free(w.xt); free(w.grad); free(w.gp); free(w.gpt); free(w.resid); free(w.ru);
+  free(w.bins); free(w.bins_prev); free(w.counters);
+#ifdef _OPENMP
+  omp_set_num_threads(saved_threads);
+#endif
+  return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* Expander l0 decoding */
+
+/* cuda_compute_scores_l0 (GAGA/gaga/expander/kernels.cu:353-388); the score is
+ * kept as a float counter exactly as the reference kernel does. */
+void gbo_l0_scores(const float *res, float *x, float *updates, const int *rows, int n, int d,
+                   int thresh, int shift, int *found) {
+  const float EPS = 0.000001f;
+  for (int j = 0; j < n; ++j) {
+    int idx = d * j;
+    float score = 0.0f;
+    float omega = res[rows[idx + shift]];
+    updates[j] = 0.0f;
+    if (fabsf(omega) > EPS) {
+      for (int i = 0; i < d; ++i) {
+        if (fabsf(res[rows[idx + i]] - omega) <= EPS) score += 1.0f;
+        if (fabsf(res[rows[idx + i]]) <= EPS) score -= 1.0f;
+      }
+      if (score > (float)thresh) {
+        *found = 1;
+        x[j] = x[j] + omega;
+        updates[j] = omega;
+      }
+    }
+  }
+}
+
+/* cuda_update_residual (GAGA/gaga/expander/kernels.cu:3-14); updates applied in
+ * column order */
+void gbo_l0_update_residual(float *res, const int *rows, const float *updates, int n, int d) {
+  for (int j = 0; j < n; ++j) {
+    if (fabsf(updates[j]) > 0.0f) {
+      float u = -updates[j];
+      for (int i = 0; i < d; ++i) res[rows[j * d + i]] += u;
+    }
+  }
+}
+
+/* parallel_l0 (GAGA/gaga/expander/parallel_l0.cu:9-151) */
+int gbo_parallel_l0(const gbo_op *op, const float *y, const gbo_opts *o, float *x, float *res,
+                    float *res_record, gbo_info *info) {
+  int m = op->m, n = op->n, d = op->d;
+  float *ax = (float *)malloc(sizeof(float) * m);
+  float *upd = (float *)calloc((size_t)n, sizeof(float));
+  gbo_A(op, x, ax);
+  for (int i = 0; i < m; ++i) res[i] = fmaf(-1.0f, ax[i], y[i]);
+  float norm = nrm2f(res, m), norm0 = norm;
+  if (res_record) res_record[0] = norm;
+  int L = 2 * d;
+  float *cyc = (float *)calloc((size_t)L, sizeof(float));
+  float *prev = (float *)calloc((size_t)L, sizeof(float));
+  float *evol = (float *)malloc(sizeof(float) * L);
+  for (int i = 0; i < L; ++i) evol[i] = 1.0f;
+  float diff = 1.0f;
+  int iter = 0, cycling = 0, found = 1;
+  while ((iter < o->maxiter) & (norm > o->tol) & (norm < (100.0f * norm0)) & ((double)diff > 0.000001) &
+         (cycling == 0) & (found == 1)) {
+    int offset = iter % d;
+    found = 0;
+    gbo_l0_scores(res, x, upd, op->smv_rows, n, d, o->l0_thresh, offset, &found);
+    gbo_l0_update_residual(res, op->smv_rows, upd, n, d);
+    norm = nrm2f(res, m);
+    for (int i = 0; i < L - 1; ++i) prev[i] = prev[i + 1];
+    prev[L - 1] = norm;
+    for (int i = 0; i < L - 1; ++i) evol[i] = evol[i + 1];
+    evol[L - 1] = prev[L - 2] - prev[L - 1];
+    diff = max_list(evol, L);
+    for (int i = 0; i < L - 1; ++i) cyc[i] = cyc[i + 1];
+    cyc[L - 1] = norm;
+    if (iter > L) {
+      cycling = 1;
+      for (int i = 3; i < L; i += 2) cycling = cycling * (cyc[i] == cyc[i - 2]);
+    }
+    iter = iter + 1;
+    if (res_record) res_record[iter] = norm;
+  }
+  if (info) {
+    memset(info, 0, sizeof(*info));
+    info->iter = iter;
+    /* gaga_smv.cu:1013-1020: the last <=16 records become residNorm_prev */
+    if (res_record)
+      for (int j = 0; j < (iter < 16 ? iter : 16); ++j) info->resid_prev[15 - j] = res_record[iter - j];
+  }
+  free(ax); free(upd); free(cyc); free(prev); free(evol);
+  return 0;
+}
+
+/* serial_l0 (GAGA/gaga/expander/serial_l0.cu:16-161): Gauss-Seidel, the residual is
+ * updated as soon as a column is accepted.  res must hold y - A x on entry. */
+int gbo_serial_l0(const gbo_op *op, const float *y, const gbo_opts *o, float *x, float *res,
+                  float *res_record, gbo_info *info) {
+  (void)y;
+  int m = op->m, n = op->n, d = op->d;
+  const int *rows = op->smv_rows;
+  float ss = 0.0f;
+  for (int i = 0; i < m; ++i) ss = ss + res[i] * res[i];
+  float norm = sqrtf(ss), norm0 = norm;
+  if (res_record) res_record[0] = norm;
+  int L = 2 * d;
+  float *cyc = (float *)calloc((size_t)L, sizeof(float));
+  float *prev = (float *)calloc((size_t)L, sizeof(float));
+  float *evol = (float *)malloc(sizeof(float) * L);
+  for (int i = 0; i < L; ++i) evol[i] = 1.0f;
+  float diff = 1.0f;
+  const float EPS = 0.000001f;
+  int iter = 0, cycling = 0, nit = 0;
+  while ((iter < o->maxiter) && (norm > o->tol) && (norm < (100.0f * norm0)) && (cycling == 0) &&
+         ((double)diff > 0.000001)) {
+    int shift = iter % d;
+    for (int node = 0; node < n; ++node) {
+      int idx = d * node;
+      float omega = res[rows[idx + shift]];
+      int score = 0;
+      if (fabsf(omega) > EPS) {
+        for (int i = 0; i < d; ++i) {
+          if (fabsf(res[rows[idx + i]] - omega) <= EPS) score++;
+          if (fabsf(res[rows[idx + i]]) <= EPS) score--;
+        }
+        if (score > o->l0_thresh) {
+          x[node] = x[node] + omega;
+          for (int i = 0; i < d; ++i) res[rows[idx + i]] = res[rows[idx + i]] - omega;
+        }
+      }
+    }
+    ss = 0.0f;
+    for (int i = 0; i < m; ++i) ss = ss + res[i] * res[i];
+    norm = sqrtf(ss);
+    for (int i = 0; i < L - 1; ++i) prev[i] = prev[i + 1];
+    prev[L - 1] = norm;
+    for (int i = 0; i < L - 1; ++i) evol[i] = evol[i + 1];
+    evol[L - 1] = prev[L - 2] - prev[L - 1];
+    diff = evol[0];
+    for (int i = 0; i < L; ++i) diff = diff > evol[i] ? diff : evol[i];
+    for (int i = 0; i < L - 1; ++i) cyc[i] = cyc[i + 1];
+    cyc[L - 1] = norm;
+    if (iter > L) {
+      cycling = 1;
+      for (int i = 3; i < L; i += 2) cycling = cycling * (cyc[i] == cyc[i - 2]);
+    }
+    /* the reference writes resRecord[nIters] starting at 0 (overwriting the
+     * initial norm), serial_l0.cu:146-148 */
+    if (res_record) res_record[nit] = norm;
+    nit++;
+    iter = iter + 1;
+  }
+  if (info) {
+    memset(info, 0, sizeof(*info));
+    info->iter = iter;
+  }
+  free(cyc); free(prev); free(evol);
+  return 0;
+}
+
+/* ------------------------------------------------------------------ */
+void gbo_results(const float *x, const float *x_true, int n, int k, float norms[3], int supp[4]) {
+  int tp = 0, tn = 0;
+  double l1 = 0, l2 = 0, li = 0, e1 = 0, e2 = 0, ei = 0;
+  for (int i = 0; i < n; ++i) {
+    if (x_true[i] != 0.0f) { if (x[i] != 0.0f) tp++; }
+    else if (x[i] == 0.0f) tn++;
+    double a = fabs((double)x_true[i]), e = fabs((double)x_true[i] - (double)x[i]);
+    l1 += a; l2 += a * a; if (a > li) li = a;
+    e1 += e; e2 += e * e; if (e > ei) ei = e;
+  }
+  norms[0] = (float)(e1 / l1);
+  norms[1] = (float)(sqrt(e2) / sqrt(l2));
+  norms[2] = (float)(ei / li);
+  supp[0] = tp; supp[1] = k - tp; supp[2] = tn; supp[3] = n - k - tn;
+}
+
+/* ------------------------------------------------------------------ */
+int gbo_solve_dense_trials(int ntrials, const int *nn, const int *mm, const int *kk, uint32_t seed,
+                           const uint32_t *trial_ids, int alg, float tol_rel, int maxiter,
+                           int threads, int *iters, float *rel_err) {
+  int ok = 0;
+#ifdef _OPENMP
+  if (threads > 0) omp_set_num_threads(threads);
+#endif
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : ok)
+  for (int t = 0; t < ntrials; ++t) {
+    int n = nn[t], m = mm[t], k = kk[t];
+    uint32_t tid = trial_ids ? trial_ids[t] : (uint32_t)t;
+    float *A = (float *)malloc(sizeof(float) * (size_t)m * n);
+    float *xt = (float *)malloc(sizeof(float) * n);
+    float *x = (float *)calloc((size_t)n, sizeof(float));
+    float *y = (float *)malloc(sizeof(float) * m);
+    /* generation is serial inside a trial (the outer loop is parallel) */
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < m; ++i) A[(size_t)j * m + i] = gauss_at(seed, tid, ST_MATRIX, (uint64_t)j * m + i) *
+                                                          (1.0f / sqrtf((float)m));
+    int ksupp = gbo_gen_vector(n, k, 1, seed, tid, xt);
+    gbo_op op = {GBO_OP_DENSE, m, n, A, m, 0, 0, 0, 0};
+    gbo_A(&op, xt, y);
+    gbo_opts o = {alg, tol_rel * nrm2f(y, m), maxiter, n / 20 > 1000 ? n / 20 : 1000, 0, 1, 1};
+    gbo_info info;
+    gbo_solve(&op, y, ksupp, &o, x, &info);
+    float norms[3];
+    int supp[4];
+    gbo_results(x, xt, n, ksupp, norms, supp);
+    if (iters) iters[t] = info.iter;
+    if (rel_err) rel_err[t] = norms[1];
+    if (norms[1] <= 1e-3f) ok += 1;
+    free(A); free(xt); free(x); free(y);
+  }
+  return ok;
+}

@@ -1,0 +1,97 @@
+"""The oracle pinned against the golden fixtures (tests/golden, written by
+tests/golden/make_golden.py from the reference's own source run on the CPU, and from
+scipy's orthonormal DCT).  CPU only."""
+import os
+
+import numpy as np
+import pytest
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load(name):
+    return np.load(os.path.join(GOLD, name))
+
+
+def test_linear_binning_matches_reference(gbo):
+    z = load("linear_binning.npz")
+    assert len(z["names"]) >= 5
+    for name in z["names"]:
+        bins, cnt = gbo.linear_binning(z[f"{name}__v"], int(z[f"{name}__num_bins"]), int(z[f"{name}__max_bin"]),
+                                       float(z[f"{name}__slope"]), float(z[f"{name}__intercept"]))
+        assert np.array_equal(bins, z[f"{name}__bins"]), name
+        assert np.array_equal(cnt, z[f"{name}__counters"]), name
+
+
+def test_threshold_matches_reference(gbo):
+    z = load("threshold.npz")
+    v, bins = z["v"], z["bins"]
+    for kb in z["k_bins"]:
+        a = v.copy()
+        gbo.lib().gbo_threshold(a.ctypes.data, bins.ctypes.data, int(kb), len(a))
+        assert np.array_equal(a, z[f"threshold_{kb}"])
+        b = np.where(bins <= kb, v, np.float32(0))
+        assert np.array_equal(b, z[f"threshold_one_{kb}"])
+
+
+def test_support_evolution_matches_reference(gbo):
+    z = load("support_evolution.npz")
+    for i in range(int(z["count"])):
+        cur, prev = z[f"c{i}__cur"], z[f"c{i}__prev"]
+        kc, kp = int(z[f"c{i}__kcur"]), int(z[f"c{i}__kprev"])
+        changed = int(np.any((prev <= kp) & (cur > kc)))
+        assert changed == int(z[f"c{i}__flag"] > 0)
+
+
+def test_l0_step_matches_reference(gbo):
+    z = load("l0_step.npz")
+    for i in range(int(z["count"])):
+        g = lambda key: z[f"c{i}__{key}"]
+        n, d, shift = int(g("n")), int(g("d")), int(g("shift"))
+        x, upd, found = gbo.l0_scores(g("res"), np.zeros(n, np.float32), g("rows"), n, d, 1, shift)
+        assert found == int(g("found"))
+        assert np.array_equal(x, g("x_after"))
+        assert np.array_equal(upd, g("updates"))
+        res2 = gbo.l0_update_residual(g("res"), g("rows"), upd, n, d)
+        assert np.array_equal(res2, g("res_after"))
+
+
+def test_serial_l0_matches_reference(gbo):
+    z = load("serial_l0.npz")
+    for i in range(int(z["count"])):
+        g = lambda key: z[f"c{i}__{key}"]
+        m, n, d = int(g("m")), int(g("n")), int(g("d"))
+        op = gbo.Op.smv(m, n, d, g("rows"), np.ones(n * d, np.float32))
+        x, res, rec, info = gbo.serial_l0(op, g("y"), tol=1e-6, maxiter=int(g("maxiter")))
+        it = int(g("iter"))
+        assert info.iter == it
+        assert np.array_equal(x, g("x"))
+        assert np.array_equal(res, g("res"))
+        assert np.array_equal(rec[:it], g("rec")[:it])
+
+
+def test_dct_matches_scipy(gbo):
+    z = load("dct_scipy.npz")
+    for N in z["sizes"]:
+        x = z[f"N{N}__x"]
+        d2, d3 = gbo.dct2(x), gbo.dct3(x)
+        np.testing.assert_allclose(d2, z[f"N{N}__dct2"], rtol=0, atol=1e-5 * np.abs(z[f"N{N}__dct2"]).max())
+        np.testing.assert_allclose(d3, z[f"N{N}__dct3"], rtol=0, atol=1e-5 * np.abs(z[f"N{N}__dct3"]).max())
+
+
+def test_ref_library_matches_fixtures_when_present(gbo):
+    """Where the reference tree is present, its CPU build still reproduces the fixtures."""
+    R = gbo.ref_lib()
+    if R is None:
+        pytest.skip("reference tree not present")
+    import ctypes as C
+
+    z = load("linear_binning.npz")
+    name = z["names"][0]
+    v = z[f"{name}__v"].copy()
+    nb, mb = int(z[f"{name}__num_bins"]), int(z[f"{name}__max_bin"])
+    bins = np.zeros(len(v), np.int32)
+    cnt = np.zeros(nb, np.int32)
+    R.ref_linear_binning(v.ctypes.data, bins.ctypes.data, cnt.ctypes.data, nb, mb, len(v),
+                         C.c_float(float(z[f"{name}__slope"])), C.c_float(float(z[f"{name}__intercept"])))
+    assert np.array_equal(bins, z[f"{name}__bins"])
