@@ -260,3 +260,11 @@ def solve_batch(n, m, k, seed, trial_ids=None, alg="NIHT", tol_rel=1e-4, maxiter
     _lib.check(L.gb_cs_solve_batch(C.byref(b), C.c_void_p(iters.ctypes.data), C.c_void_p(err.ctypes.data),
                                    C.c_void_p(ok.ctypes.data), C.byref(ns)))
     return ns.value, iters, err, ok
+
+
+def batch_last_stats():
+    """(algorithmic matvec bytes, device ms) of the last solve_batch call."""
+    L = _lib.load()
+    b, t = C.c_double(0), C.c_float(0)
+    L.gb_cs_batch_last_stats(C.byref(b), C.byref(t))
+    return b.value, t.value

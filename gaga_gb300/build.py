@@ -17,7 +17,7 @@ ROOT = os.path.dirname(HERE)
 SOURCES = ["gb_ops.cu", "gb_solver.cu", "gb_api.cu", "gb_batch.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
-FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr",
          "-I", os.path.join(ROOT, "include")]
 
 

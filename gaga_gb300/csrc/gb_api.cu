@@ -116,6 +116,7 @@ gb_status alloc_work(DeviceBuffers &db, GbWork &w, int m, int n, int lda, int nu
   GB_CUDA_TRY(cudaGetDevice(&dev));
   GB_CUDA_TRY(cudaDeviceGetAttribute(&w.num_sms, cudaDevAttrMultiProcessorCount, dev));
   w.red_blocks = std::min(GB_MAXRB, w.num_sms * 2);
+  w.wide_blocks = w.num_sms * 8;
   GB_TRY(db.alloc(&w.st, 1));
   GB_TRY(db.alloc(&w.red_part, (size_t)GB_NSLOT * GB_MAXRB));
   GB_TRY(db.alloc(&w.tickets, GB_NSLOT));
@@ -374,31 +375,34 @@ __host__ __device__ inline void philox(uint32_t c0, uint32_t c1, uint32_t c2, ui
 }
 __host__ __device__ inline float u01(uint32_t x) { return ((float)(x >> 8) + 0.5f) * (1.0f / 16777216.0f); }
 
-// dense A entries N(0,1)/sqrt(m) (ens 1) or +-1/sqrt(m) (ens 2), column-major with lda
+// dense A entries N(0,1)/sqrt(m) (ens 1) or +-1/sqrt(m) (ens 2), column-major with lda.
+// Element e = j*m + i is lane e%4 of Philox block e/4 (one block gives 4 normals by two
+// Box-Muller pairs); each lane draws one block and writes its entries inside column j.
 __global__ void k_gen_dense(float *A, int m, int n, int lda, int ens, uint32_t seed, uint32_t trial) {
   const float scale = 1.0f / sqrtf((float)m);
-  const size_t total = (size_t)m * n;
-  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < (total + 3) / 4;
-       q += (size_t)gridDim.x * blockDim.x) {
-    uint32_t o[4];
-    philox((uint32_t)q, (uint32_t)(q >> 32), ST_MATRIX, trial, seed, KEY_HI, o);
-    float v[4];
-    if (ens == 2) {
-      for (int t = 0; t < 4; ++t) v[t] = signbit(u01(o[t]) - 0.5f) ? -1.0f : 1.0f;
-    } else {
-      for (int t = 0; t < 2; ++t) {
-        float r = sqrtf(-2.0f * logf(u01(o[2 * t])));
-        float sn, cs;
-        sincospif(2.0f * u01(o[2 * t + 1]), &sn, &cs);
-        v[2 * t] = r * cs;
-        v[2 * t + 1] = r * sn;
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  for (int j = gw; j < n; j += nw) {
+    const uint64_t e0 = (uint64_t)j * (uint64_t)m, e1 = e0 + (uint64_t)m;
+    float *col = A + (size_t)j * lda;
+    for (uint64_t g = (e0 >> 2) + lane; g < ((e1 + 3) >> 2); g += 32) {
+      uint32_t o[4];
+      philox((uint32_t)g, (uint32_t)(g >> 32), ST_MATRIX, trial, seed, KEY_HI, o);
+      float v[4];
+      if (ens == 2) {
+        for (int t = 0; t < 4; ++t) v[t] = signbit(u01(o[t]) - 0.5f) ? -1.0f : 1.0f;
+      } else {
+        for (int t = 0; t < 2; ++t) {
+          const float r = sqrtf(-2.0f * logf(u01(o[2 * t])));
+          float sn, cs;
+          sincospif(2.0f * u01(o[2 * t + 1]), &sn, &cs);
+          v[2 * t] = r * cs;
+          v[2 * t + 1] = r * sn;
+        }
       }
-    }
-    for (int t = 0; t < 4; ++t) {
-      size_t e = q * 4 + t;
-      if (e < total) {
-        size_t j = e / m, i = e % m;
-        A[j * lda + i] = v[t] * scale;
+      for (int t = 0; t < 4; ++t) {
+        const uint64_t e = g * 4 + t;
+        if (e >= e0 && e < e1) col[e - e0] = v[t] * scale;
       }
     }
   }
@@ -493,7 +497,7 @@ extern "C" gb_status gb_cs_generate_and_solve(const char *alg, int kind, int k, 
     // A drawn on the device straight into the padded layout
     GB_TRY(db.alloc(&dA, (size_t)lda * n, true));
     int ens = o.matrix_ensemble == 2 ? 2 : 1;
-    k_gen_dense<<<1024, 256>>>(dA, m, n, lda, ens, seed, 0);
+    k_gen_dense<<<2048, 256>>>(dA, m, n, lda, ens, seed, 0);
     GB_CUDA_TRY(cudaGetLastError());
     p.location = GB_DEVICE;
     p.A = dA;

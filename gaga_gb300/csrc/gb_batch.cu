@@ -1,9 +1,502 @@
-// gb_batch.cu -- batched multi-trial form (see gb_cs_solve_batch in include/gb_cs.h).
+// gb_batch.cu -- batched multi-trial form.
+//
+// The reference solves one trial per gaga_cs call: allocate, generate, run a host loop
+// with ~20 launches and ~6 device->host round trips per iteration, free.  Here a batch
+// of independent dense trials is served by B "slots".  Each slot owns a workspace sized
+// for the largest trial of the batch and one CUDA graph, launched once on its own
+// stream:
+//
+//     fetch a trial from a device-side queue
+//     WHILE (a trial was fetched)
+//         draw A, x0 on the device from (seed + trial id); y = A x0
+//         the solver's prologue, then WHILE (stopping rules) { one iteration }
+//         write the trial's iterations / relative error / verdict; fetch the next trial
+//
+// The solver kernels are the plain path's (gb_ops.cu, gb_solver.cu) reading the current
+// trial's m, n, k from the slot's device state, so one captured graph serves trials of
+// every size.  Large trials run their kernels over the whole GPU; small ones overlap
+// across slots.  No host work, allocation or graph build happens per trial.
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <map>
+#include <vector>
+
 #include "gb_internal.cuh"
+
+__global__ void k_hist(const GbState *st, int pf, const float *__restrict__ v, int *__restrict__ bins,
+                       int *__restrict__ bins_prev, int *__restrict__ counters, int n);
+__global__ void k_kbin(GbState *st, int pf, const int *__restrict__ counters, int k);
+__global__ void k_thresh_count(GbState *st, int pf, float *__restrict__ v, const int *__restrict__ bins,
+                               const int *__restrict__ bins_prev, int n, int *__restrict__ tile_cnt);
+__global__ void k_compact(GbState *st, int pf, const int *__restrict__ bins, int n, const int *__restrict__ tile_cnt,
+                          int *__restrict__ S);
+
+namespace {
+
+struct BatchParams {
+  int T;
+  unsigned int seed;
+  float tol_rel;
+  int maxiter, alg;
+  const int *n, *m, *k;
+  const unsigned int *tid;
+  const int *order;
+  int *queue;
+  int *iters;
+  float *err;
+  int *ok;
+  double *bytes;
+};
+
+const uint32_t KEY_HI = 0x6A09E667u;
+enum { ST_MATRIX = 1, ST_VALUES = 2, ST_SUPPORT = 3 };
+
+__device__ __forceinline__ void philox_d(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0,
+                                         uint32_t k1, uint32_t out[4]) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+    const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+  }
+  out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+__device__ __forceinline__ float u01d(uint32_t x) { return ((float)(x >> 8) + 0.5f) * (1.0f / 16777216.0f); }
+
+__device__ __forceinline__ uint32_t trial_key(const BatchParams *bp, const GbState *st) {
+  return bp->seed + (bp->tid ? bp->tid[st->trial] : (uint32_t)st->trial);
+}
+
+// set the slot's state for trial q of the queue order, or end the slot's trial loop
+__device__ void load_trial(GbState *st, const BatchParams *bp, int q, cudaGraphConditionalHandle h_trial) {
+  if (q >= bp->T) {
+    st->active = 0;
+    st->trial = -1;
+    cudaGraphSetConditional(h_trial, 0u);
+    return;
+  }
+  const int t = bp->order[q];
+  st->trial = t;
+  st->m = bp->m[t];
+  st->n = bp->n[t];
+  st->k = bp->k[t];
+  st->num_bins = max(st->n / 20, 1000);
+  st->maxiter = bp->maxiter;
+  st->alg = bp->alg;
+  st->restart = 0;
+  st->op_kind = GB_OP_DENSE;
+  st->active = 1;
+  for (int f = 0; f < GB_NFLAG; ++f) st->flags[f] = 0;
+  st->flags[F_ALWAYS] = 1;
+  st->bytes = 0.0;
+  cudaGraphSetConditional(h_trial, 1u);
+}
+
+__global__ void k_b_fetch(GbState *st, const BatchParams *bp, cudaGraphConditionalHandle h_trial) {
+  if (threadIdx.x || blockIdx.x) return;
+  load_trial(st, bp, atomicAdd(bp->queue, 1), h_trial);
+}
+
+// A of the current trial: the element stream of k_gen_dense (gb_api.cu) keyed by seed + trial id
+__global__ void k_b_gen_A(const GbState *st, const BatchParams *bp, float *A) {
+  if (!st->active) return;
+  const int m = st->m, n = st->n, lda = st->lda;
+  const uint32_t key = trial_key(bp, st);
+  const float scale = 1.0f / sqrtf((float)m);
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  for (int j = gw; j < n; j += nw) {
+    const uint64_t e0 = (uint64_t)j * (uint64_t)m, e1 = e0 + (uint64_t)m;
+    float *col = A + (size_t)j * lda;
+    for (uint64_t g = (e0 >> 2) + lane; g < ((e1 + 3) >> 2); g += 32) {
+      uint32_t o[4];
+      philox_d((uint32_t)g, (uint32_t)(g >> 32), ST_MATRIX, 0u, key, KEY_HI, o);
+      float v[4];
+      for (int t = 0; t < 2; ++t) {
+        const float r = sqrtf(-2.0f * logf(u01d(o[2 * t])));
+        float sn, cs;
+        sincospif(2.0f * u01d(o[2 * t + 1]), &sn, &cs);
+        v[2 * t] = r * cs;
+        v[2 * t + 1] = r * sn;
+      }
+      for (int t = 0; t < 4; ++t) {
+        const uint64_t e = g * 4 + t;
+        if (e >= e0 && e < e1) col[e - e0] = v[t] * scale;
+      }
+    }
+  }
+}
+
+// x0 values (+-1) and support keys of createVector (GAGA/gaga/createVector.cu:207-300);
+// max key into red[R_XMAX]; clears the n-bin key histogram
+__global__ void k_b_gen_x(GbState *st, const BatchParams *bp, float *vals, float *keys, int *hist, float *rp,
+                          unsigned int *tk) {
+  if (!st->active) return;
+  const int n = st->n;
+  const uint32_t key = trial_key(bp, st);
+  float mx = 0.0f;
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    uint32_t o[4];
+    philox_d((uint32_t)(j >> 2), 0u, ST_VALUES, 0u, key, KEY_HI, o);
+    vals[j] = signbit(u01d(o[j & 3]) - 0.5f) ? -1.0f : 1.0f;
+    philox_d((uint32_t)(j >> 2), 0u, ST_SUPPORT, 0u, key, KEY_HI, o);
+    const float u = u01d(o[j & 3]);
+    keys[j] = u;
+    mx = fmaxf(mx, u);
+    hist[j] = 0;
+  }
+  grid_reduce_publish<1>(mx, R_XMAX, st, rp, tk);
+}
+
+// generation bookkeeping (single thread)
+enum { B_KEYS = 0, B_X0 = 1, B_INIT = 2, B_RESULT = 3 };
+__global__ void k_b_ctrl(GbState *st, const BatchParams *bp, int phase, cudaGraphConditionalHandle h_trial) {
+  if (threadIdx.x || blockIdx.x) return;
+  if (phase == B_KEYS) {
+    if (!st->active) return;
+    // n linear bins over the keys, every key counted (createVector.cu:236-248)
+    st->max_value = (float)st->red[R_XMAX];
+    st->slope = ((float)(st->n - 1) / st->max_value);
+    st->max_bin = st->n;
+    st->alpha_bin = 0.25f;
+    st->flags[F_DOBIN] = 1;
+  } else if (phase == B_X0) {
+    if (!st->active) return;
+    st->k = st->sum;  // |support| >= k, the k the solver is given
+  } else if (phase == B_INIT) {
+    if (!st->active) return;
+    // the solver's initial state (initial_state in gb_solver.cu) with tol = tol_rel ||y||
+    const float tol = bp->tol_rel * (float)sqrt(st->red[R_RES]);
+    st->tol = tol;
+    st->iter = 0; st->fail = 0; st->cycle = 1; st->passes = 0; st->pass_limit = st->maxiter + 4;
+    st->status = 0; st->stop_reason = 0;
+    st->err = 0.0f; st->err_start = 0.0f; st->resid_diff = 1.0f;
+    for (int j = 0; j < 16; ++j) { st->prev[j] = 0.0f; st->evol[j] = 1.0f; }
+    st->alpha_bin = 0.25f;
+    st->max_bin = (int)((float)st->num_bins * (1.0f - st->alpha_bin));
+    st->k_bin = 0; st->sum = 0; st->k_bin_prev = 0;
+    st->min_val = 0.0f; st->slope = 0.0f; st->max_value = 0.0f; st->max_change = 0.0f;
+    st->mu = 0.0f; st->cg_alpha = 0.0f; st->cg_beta = 0.0f;
+    st->beta_to_zero = 1; st->supp_change = 1;
+    st->it_cg = 0; st->tol_cg = tol * tol; st->tol2 = 10.0f * st->tol_cg;
+    for (int f = 0; f < GB_NFLAG; ++f) st->flags[f] = 0;
+    st->flags[F_ALWAYS] = 1;
+    st->changed = 0;
+    st->bytes = 0.0;
+  } else {
+    // verdict of the finished trial (results.cu:468-475), then the next trial
+    if (st->trial >= 0) {
+      const int t = st->trial;
+      const float rel = (float)(sqrt(st->red[R_DOT1]) / sqrt(st->red[R_DOT2]));
+      bp->iters[t] = st->iter;
+      bp->err[t] = rel;
+      bp->ok[t] = rel <= 1e-3f ? 1 : 0;
+      atomicAdd(bp->bytes, st->bytes);
+    }
+    load_trial(st, bp, atomicAdd(bp->queue, 1), h_trial);
+  }
+}
+
+// ||x - x0||^2 and ||x0||^2
+__global__ void k_b_err(GbState *st, const float *__restrict__ x, const float *__restrict__ x0, float *rp,
+                        unsigned int *tk) {
+  if (st->trial < 0) return;
+  const int n = st->n;
+  float e2 = 0.0f, x2 = 0.0f;
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const float d = x0[j] - x[j];
+    e2 = fmaf(d, d, e2);
+    x2 = fmaf(x0[j], x0[j], x2);
+  }
+  grid_reduce_publish<0>(e2, R_DOT1, st, rp, tk);
+  grid_reduce_publish<0>(x2, R_DOT2, st, rp, tk);
+}
+
+struct Slot {
+  GbWork w;
+  std::vector<void *> bufs;
+  float *x0 = nullptr;
+  int *hist = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+struct Engine {
+  int dev = -1, alg = -1, n_cap = 0, m_cap = 0, t_cap = 0, slots = 0;
+  std::vector<Slot> slot;
+  char *table = nullptr;
+  BatchParams *d_params = nullptr;
+  int *dn = nullptr, *dm = nullptr, *dk = nullptr, *dorder = nullptr, *dqueue = nullptr, *diters = nullptr,
+      *dok = nullptr;
+  unsigned *dtid = nullptr;
+  float *derr = nullptr;
+  double *dbytes = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  std::vector<cudaEvent_t> done;
+};
+std::map<int, Engine> g_engines;
+
+gb_status dalloc(std::vector<void *> &bufs, void **p, size_t bytes) {
+  GB_CUDA_TRY(cudaMalloc(p, std::max<size_t>(bytes, 4)));
+  bufs.push_back(*p);
+  GB_CUDA_TRY(cudaMemset(*p, 0, std::max<size_t>(bytes, 4)));
+  return GB_OK;
+}
+
+void release(Engine &E) {
+  for (auto &s : E.slot) {
+    if (s.exec) cudaGraphExecDestroy(s.exec);
+    for (void *p : s.bufs) cudaFree(p);
+    if (s.stream) cudaStreamDestroy(s.stream);
+  }
+  for (auto e : E.done) cudaEventDestroy(e);
+  if (E.table) cudaFree(E.table);
+  if (E.e0) cudaEventDestroy(E.e0);
+  if (E.e1) cudaEventDestroy(E.e1);
+  E = Engine();
+}
+
+gb_status build_slot_graph(Engine &E, Slot &S) {
+  GbWork &w = S.w;
+  cudaStream_t s0, s1, s2, s3;
+  GB_CUDA_TRY(cudaStreamCreateWithFlags(&s0, cudaStreamNonBlocking));
+  GB_CUDA_TRY(cudaStreamCreateWithFlags(&s1, cudaStreamNonBlocking));
+  GB_CUDA_TRY(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+  GB_CUDA_TRY(cudaStreamCreateWithFlags(&s3, cudaStreamNonBlocking));
+  SolvePlan P{&w, E.alg, 0, 0};
+  cudaGraph_t graph;
+  GB_CUDA_TRY(cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal));
+  cudaGraphConditionalHandle h_trial = 0, h_iter = 0, h_cg = 0;
+  GB_TRY(gb_make_handle(s0, &h_trial));
+  k_b_fetch<<<1, 32, 0, s0>>>(w.st, E.d_params, h_trial);
+  GB_TRY(gb_open_while(s0, s1, h_trial));
+  {
+    // ---- draw the trial on the device
+    k_b_gen_A<<<w.num_sms * 8, 256, 0, s1>>>(w.st, E.d_params, const_cast<float *>(w.op.A));
+    k_b_gen_x<<<w.red_blocks, 256, 0, s1>>>(w.st, E.d_params, S.x0, w.xt, S.hist, w.red_part, w.tickets);
+    k_b_ctrl<<<1, 32, 0, s1>>>(w.st, E.d_params, B_KEYS, 0);
+    // support of x0: keys in n linear bins, the top bins holding >= k keys
+    k_hist<<<w.red_blocks, 256, 0, s1>>>(w.st, F_ALWAYS, w.xt, w.bins, nullptr, S.hist, D_N);
+    k_kbin<<<1, 1024, 0, s1>>>(w.st, F_ALWAYS, S.hist, D_K);
+    k_b_ctrl<<<1, 32, 0, s1>>>(w.st, E.d_params, B_X0, 0);
+    const int tiles = (w.op.n + GB_TILE - 1) / GB_TILE;
+    k_thresh_count<<<tiles, 256, 0, s1>>>(w.st, F_ALWAYS, S.x0, w.bins, nullptr, D_N, w.tile_cnt);
+    k_compact<<<tiles, 256, 0, s1>>>(w.st, F_DOBIN, w.bins, D_N, w.tile_cnt, w.S);
+    // y = A x0 and ||y||
+    enq_A(w, s1, S.x0, w.y, nullptr, R_RES, F_ALWAYS);
+    k_b_ctrl<<<1, 32, 0, s1>>>(w.st, E.d_params, B_INIT, 0);
+    // ---- solve
+    GB_TRY(gb_make_handle(s1, &h_iter));
+    enq_prologue(P, s1, h_iter);
+    GB_TRY(gb_open_while(s1, s2, h_iter));
+    enq_body(P, s2, h_iter);
+    if (E.alg == GB_ALG_HTP) {
+      GB_TRY(gb_make_handle(s2, &h_cg));
+      enq_ctrl_phase(w, s2, GB_PHASE_HTP_CGINIT, h_cg);
+      GB_TRY(gb_open_while(s2, s3, h_cg));
+      enq_cg_body(P, s3, h_cg);
+      GB_TRY(gb_close_while(s3));
+      enq_ctrl_phase(w, s2, GB_PHASE_HTP_STOP, h_iter);
+    }
+    GB_TRY(gb_close_while(s2));
+    // ---- verdict, next trial
+    k_b_err<<<w.red_blocks, 256, 0, s1>>>(w.st, w.x, S.x0, w.red_part, w.tickets);
+    k_b_ctrl<<<1, 32, 0, s1>>>(w.st, E.d_params, B_RESULT, h_trial);
+  }
+  GB_TRY(gb_close_while(s1));
+  GB_CUDA_TRY(cudaStreamEndCapture(s0, &graph));
+  cudaError_t e = cudaGraphInstantiate(&S.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  cudaStreamDestroy(s0);
+  cudaStreamDestroy(s1);
+  cudaStreamDestroy(s2);
+  cudaStreamDestroy(s3);
+  GB_CUDA_TRY(e);
+  return GB_OK;
+}
+
+gb_status setup_engine(Engine &E, int dev, int alg, int n_cap, int m_cap, int T, int slots) {
+  if (E.dev == dev && E.alg == alg && E.n_cap >= n_cap && E.m_cap >= m_cap && E.t_cap >= T && E.slots == slots)
+    return GB_OK;
+  release(E);
+  E.dev = dev;
+  E.alg = alg;
+  E.n_cap = n_cap;
+  E.m_cap = m_cap;
+  E.t_cap = std::max(T, 1024);
+  E.slots = slots;
+  const size_t tb = (size_t)E.t_cap * 4;
+  const size_t bytes = 10 * (tb + 256) + sizeof(BatchParams) + 2048;
+  GB_CUDA_TRY(cudaMalloc(&E.table, bytes));
+  GB_CUDA_TRY(cudaMemset(E.table, 0, bytes));
+  char *p = E.table;
+  auto take = [&](size_t b) {
+    char *q = p;
+    p += (b + 255) & ~(size_t)255;
+    return q;
+  };
+  E.dn = (int *)take(tb); E.dm = (int *)take(tb); E.dk = (int *)take(tb); E.dtid = (unsigned *)take(tb);
+  E.dorder = (int *)take(tb); E.diters = (int *)take(tb); E.derr = (float *)take(tb); E.dok = (int *)take(tb);
+  E.dqueue = (int *)take(256); E.dbytes = (double *)take(256);
+  E.d_params = (BatchParams *)take(sizeof(BatchParams));
+  int sms = 0;
+  GB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int lda = (m_cap + 31) / 32 * 32;
+  E.slot.resize(slots);
+  for (int i = 0; i < slots; ++i) {
+    Slot &S = E.slot[i];
+    GbWork &w = S.w;
+    memset(&w, 0, sizeof(w));
+    w.dyn = 1;
+    w.num_sms = sms;
+    // slots run concurrently: each slot's kernels take a fraction of the GPU
+    w.red_blocks = std::max(1, sms / 2);
+    w.wide_blocks = sms * 2;
+    GbOp &op = w.op;
+    op.kind = GB_OP_DENSE;
+    op.m = m_cap;
+    op.n = n_cap;
+    op.lda = lda;
+    op.vec4 = 1;
+    auto A = [&](void **q, size_t b) { return dalloc(S.bufs, q, b); };
+    float *Abuf = nullptr;
+    GB_TRY(A((void **)&Abuf, (size_t)lda * n_cap * 4));
+    op.A = Abuf;
+    GB_TRY(A((void **)&w.st, sizeof(GbState)));
+    GB_TRY(A((void **)&w.red_part, (size_t)GB_NSLOT * GB_MAXRB * 4));
+    GB_TRY(A((void **)&w.tickets, GB_NSLOT * 4));
+    for (float **v : {&w.x, &w.xt, &w.grad, &w.gp, &w.gpt, &w.upd, &S.x0}) GB_TRY(A((void **)v, (size_t)n_cap * 4));
+    for (float **v : {&w.y, &w.resid, &w.ru}) GB_TRY(A((void **)v, (size_t)lda * 4));
+    for (int **v : {&w.bins, &w.bins_prev, &w.S, &S.hist}) GB_TRY(A((void **)v, (size_t)n_cap * 4));
+    GB_TRY(A((void **)&w.counters, (size_t)std::max(n_cap / 20, 1000) * 4));
+    GB_TRY(A((void **)&w.tile_cnt, (size_t)((n_cap + GB_TILE - 1) / GB_TILE) * 4));
+    w.part_cap = gb_dense_part_floats(lda, n_cap);
+    GB_TRY(A((void **)&w.part, w.part_cap * 4));
+    GbState st0;
+    memset(&st0, 0, sizeof(st0));
+    st0.lda = lda;
+    st0.trial = -1;
+    GB_CUDA_TRY(cudaMemcpy(w.st, &st0, sizeof(st0), cudaMemcpyHostToDevice));
+    GB_CUDA_TRY(cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking));
+    cudaEvent_t ev;
+    GB_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    E.done.push_back(ev);
+  }
+  for (auto &S : E.slot) GB_TRY(build_slot_graph(E, S));
+  GB_CUDA_TRY(cudaEventCreate(&E.e0));
+  GB_CUDA_TRY(cudaEventCreate(&E.e1));
+  return GB_OK;
+}
+
+// Number of slots: enough concurrency for small trials, within 60% of free memory.
+int slots_for(int n_cap, int m_cap, size_t free_bytes, int T) {
+  int s = 16;
+  if (const char *e = getenv("GB_CS_BATCH_SLOTS")) s = std::max(1, atoi(e));
+  const double per = (double)((m_cap + 31) / 32 * 32) * n_cap * 4.0 * 1.05 + 64.0 * n_cap + (1 << 24);
+  while (s > 1 && s * per > 0.6 * (double)free_bytes) s--;
+  return std::max(1, std::min(s, T));
+}
+
+}  // namespace
+
+static thread_local double g_last_bytes = 0.0;
+static thread_local float g_last_kernel_ms = 0.0f;
 
 extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float *rel_err_out, int *success_out,
                                        int *num_success) {
-  (void)b; (void)iters_out; (void)rel_err_out; (void)success_out; (void)num_success;
-  gb_set_error_message("batched form not built", __FILE__, __LINE__);
-  return GB_UNSUPPORTED;
+  if (!b || b->ntrials < 0 || (b->ntrials > 0 && (!b->n || !b->m || !b->k))) {
+    gb_set_error_message("bad batch arguments", __FILE__, __LINE__);
+    return GB_BAD_ARG;
+  }
+  if (b->alg != GB_ALG_NIHT && b->alg != GB_ALG_CGIHT && b->alg != GB_ALG_HTP) {
+    gb_set_error_message("batched form supports NIHT, HTP and CGIHT", __FILE__, __LINE__);
+    return GB_BAD_ARG;
+  }
+  if (b->use_learned) {
+    gb_set_error_message("use_learned must be 0", __FILE__, __LINE__);
+    return GB_BAD_ARG;
+  }
+  if (b->maxiter < 0) {
+    gb_set_error_message("maxiter must be >= 0", __FILE__, __LINE__);
+    return GB_BAD_ARG;
+  }
+  const int T = b->ntrials;
+  int n_cap = 16, m_cap = 1;
+  for (int t = 0; t < T; ++t) {
+    if (b->n[t] < 16 || b->m[t] < 1 || b->k[t] < 1 || b->m[t] > b->n[t] || b->n[t] > (1 << 22)) {
+      gb_set_error_message("trial sizes must satisfy 1 <= k, 1 <= m <= n, 16 <= n <= 2^22", __FILE__, __LINE__);
+      return GB_BAD_ARG;
+    }
+    n_cap = std::max(n_cap, b->n[t]);
+    m_cap = std::max(m_cap, b->m[t]);
+  }
+  if (num_success) *num_success = 0;
+  if (T == 0) return GB_OK;
+  int dev = 0;
+  GB_CUDA_TRY(cudaGetDevice(&dev));
+  Engine &E = g_engines[dev];
+  const bool reuse = E.dev == dev && E.alg == b->alg && E.n_cap >= n_cap && E.m_cap >= m_cap && E.t_cap >= T;
+  if (!reuse) {
+    release(E);
+    size_t free_b = 0, total_b = 0;
+    GB_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+    GB_TRY(setup_engine(E, dev, b->alg, n_cap, m_cap, T, slots_for(n_cap, m_cap, free_b, std::max(T, 16))));
+  }
+  cudaStream_t s = (cudaStream_t)b->stream;
+  // trial table, longest (m*n) first
+  std::vector<int> order(T);
+  for (int t = 0; t < T; ++t) order[t] = t;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int x, int y) { return (double)b->m[x] * b->n[x] > (double)b->m[y] * b->n[y]; });
+  std::vector<unsigned> tid(T);
+  for (int t = 0; t < T; ++t) tid[t] = b->trial_id ? b->trial_id[t] : (unsigned)t;
+  BatchParams bp;
+  bp.T = T; bp.seed = b->seed; bp.tol_rel = b->tol_rel; bp.maxiter = b->maxiter; bp.alg = b->alg;
+  bp.n = E.dn; bp.m = E.dm; bp.k = E.dk; bp.tid = E.dtid; bp.order = E.dorder; bp.queue = E.dqueue;
+  bp.iters = E.diters; bp.err = E.derr; bp.ok = E.dok; bp.bytes = E.dbytes;
+  GB_CUDA_TRY(cudaMemcpyAsync(E.dn, b->n, (size_t)T * 4, cudaMemcpyHostToDevice, s));
+  GB_CUDA_TRY(cudaMemcpyAsync(E.dm, b->m, (size_t)T * 4, cudaMemcpyHostToDevice, s));
+  GB_CUDA_TRY(cudaMemcpyAsync(E.dk, b->k, (size_t)T * 4, cudaMemcpyHostToDevice, s));
+  GB_CUDA_TRY(cudaMemcpyAsync(E.dtid, tid.data(), (size_t)T * 4, cudaMemcpyHostToDevice, s));
+  GB_CUDA_TRY(cudaMemcpyAsync(E.dorder, order.data(), (size_t)T * 4, cudaMemcpyHostToDevice, s));
+  GB_CUDA_TRY(cudaMemcpyAsync(E.d_params, &bp, sizeof(bp), cudaMemcpyHostToDevice, s));
+  GB_CUDA_TRY(cudaMemsetAsync(E.dqueue, 0, 4, s));
+  GB_CUDA_TRY(cudaMemsetAsync(E.dbytes, 0, 8, s));
+  GB_CUDA_TRY(cudaEventRecord(E.e0, s));
+  for (size_t i = 0; i < E.slot.size(); ++i) {
+    Slot &S = E.slot[i];
+    GB_CUDA_TRY(cudaStreamWaitEvent(S.stream, E.e0, 0));
+    GB_CUDA_TRY(cudaGraphLaunch(S.exec, S.stream));
+    GB_CUDA_TRY(cudaEventRecord(E.done[i], S.stream));
+    GB_CUDA_TRY(cudaStreamWaitEvent(s, E.done[i], 0));
+  }
+  GB_CUDA_TRY(cudaEventRecord(E.e1, s));
+  std::vector<int> hit(T), hok(T);
+  std::vector<float> herr(T);
+  double hbytes = 0.0;
+  GB_CUDA_TRY(cudaMemcpyAsync(hit.data(), E.diters, (size_t)T * 4, cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaMemcpyAsync(herr.data(), E.derr, (size_t)T * 4, cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaMemcpyAsync(hok.data(), E.dok, (size_t)T * 4, cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaMemcpyAsync(&hbytes, E.dbytes, 8, cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  cudaEventElapsedTime(&g_last_kernel_ms, E.e0, E.e1);
+  g_last_bytes = hbytes;
+  int ns = 0;
+  for (int t = 0; t < T; ++t) {
+    if (iters_out) iters_out[t] = hit[t];
+    if (rel_err_out) rel_err_out[t] = herr[t];
+    if (success_out) success_out[t] = hok[t];
+    ns += hok[t];
+  }
+  if (num_success) *num_success = ns;
+  return GB_OK;
+}
+
+extern "C" void gb_cs_batch_last_stats(double *bytes, float *kernel_ms) {
+  if (bytes) *bytes = g_last_bytes;
+  if (kernel_ms) *kernel_ms = g_last_kernel_ms;
 }

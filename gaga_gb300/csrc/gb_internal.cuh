@@ -70,6 +70,9 @@ struct GbState {
   double red[GB_NSLOT];
   // CGIHT support-change detection
   int changed;
+  // batched form: current trial index and algorithmic operator bytes of this trial
+  int trial, op_kind;
+  double bytes;
 };
 
 // Operator description on the device.
@@ -104,9 +107,11 @@ struct GbWork {
   size_t part_cap;
   float *upd;    // l0 updates (n)
   float *rec;    // l0 residual record (maxiter + 1)
-  GbOp op;
+  GbOp op;          // dimensions here are capacities when dyn is set
+  int dyn;          // 1: kernels read m, n, lda, num_bins, k of the current trial from GbState
   int num_sms;
-  int red_blocks;  // grid of reducing kernels (fixed -> deterministic reductions)
+  int red_blocks;   // grid of reducing kernels (fixed -> deterministic reductions)
+  int wide_blocks;  // grid of the dense streaming kernels
 };
 
 void gb_set_error_message(const char *msg, const char *file, int line);
@@ -127,6 +132,21 @@ void gb_set_error_message(const char *msg, const char *file, int line);
   } while (0)
 
 // ---------------------------------------------------------------- device helpers
+// Dimension arguments of the solver kernels: a value >= 0 is used as is; a negative code
+// reads the current trial's dimension from GbState (the batched form reuses one captured
+// graph for trials of different sizes).
+enum { D_N = -1, D_M = -2, D_LDA = -3, D_NBINS = -4, D_K = -5 };
+__device__ __forceinline__ int dimv(const GbState *st, int v) {
+  if (v >= 0) return v;
+  switch (v) {
+    case D_N: return st->n;
+    case D_M: return st->m;
+    case D_LDA: return st->lda;
+    case D_NBINS: return st->num_bins;
+    default: return st->k;
+  }
+}
+
 __device__ __forceinline__ bool gb_pred(const GbState *st, int flag) {
   return st->active != 0 && st->flags[flag] != 0;
 }
@@ -193,6 +213,11 @@ __device__ void grid_reduce_publish(float v, int slot, GbState *st, float *parts
   }
 }
 
+// host-side dimension arguments (codes when the workspace is dynamic)
+inline int argN(const GbWork &w) { return w.dyn ? D_N : w.op.n; }
+inline int argM(const GbWork &w) { return w.dyn ? D_M : w.op.m; }
+inline int argLDA(const GbWork &w) { return w.dyn ? D_LDA : w.op.lda; }
+
 // ---------------------------------------------------------------- host-side pieces
 // operators (gb_ops.cu)
 // out = A v (v must vanish outside S for the dense operator); with y, out = y - A v;
@@ -200,6 +225,8 @@ __device__ void grid_reduce_publish(float v, int slot, GbState *st, float *parts
 void enq_A(GbWork &w, cudaStream_t s, const float *v, float *out, const float *y, int slot, int pf);
 // g = A^T r
 void enq_AT(GbWork &w, cudaStream_t s, const float *r, float *g, int pf);
+// dense only: g = A^T r fused with xt = g on the support, ||xt||^2 and max|g|
+void enq_AT_mask(GbWork &w, cudaStream_t s, const float *r, float *g, float *xt, int slot_sq, int slot_max, int pf);
 // dense split-K partial buffer size (floats) for an n-column operator
 size_t gb_dense_part_floats(int m_pad, int n);
 
@@ -208,3 +235,23 @@ enum { GB_RUN_SOLVE = 0, GB_RUN_L0 = 1 };
 gb_status gb_run_solver(GbWork &w, int alg, const gb_options &o, int k, cudaStream_t s, float tol_abs);
 // support list S := { j : v_j != 0 } (used by the component operator entry point)
 void enq_support_of_nonzeros(GbWork &w, cudaStream_t s, const float *v, int n);
+
+// pieces of a solve (gb_solver.cu), composed into larger graphs by the batched form
+struct SolvePlan {
+  GbWork *w;
+  int alg, k, num_bins;
+};
+void enq_prologue(SolvePlan &P, cudaStream_t s0, cudaGraphConditionalHandle h_outer);
+void enq_body(SolvePlan &P, cudaStream_t s1, cudaGraphConditionalHandle h_outer);
+void enq_cg_body(SolvePlan &P, cudaStream_t s2, cudaGraphConditionalHandle h_inner);
+void enq_ctrl_phase(GbWork &w, cudaStream_t s, int phase, cudaGraphConditionalHandle h);
+gb_status gb_make_handle(cudaStream_t parent, cudaGraphConditionalHandle *h);
+gb_status gb_open_while(cudaStream_t parent, cudaStream_t body, cudaGraphConditionalHandle h);
+gb_status gb_close_while(cudaStream_t body);
+enum { GB_PHASE_HTP_CGINIT = 1000, GB_PHASE_HTP_STOP = 1001 };
+// per-iteration algorithmic operator bytes of the dense operator (survey formula):
+// A^T r: 4mn + 4m + 4n ; A x_S: 4 m s + 8 s + 4 m
+__device__ __forceinline__ double dense_bytes(const GbState *st, int n_at, int n_a) {
+  const double m = st->m, n = st->n, s = st->s_cnt;
+  return n_at * (4.0 * m * n + 4.0 * m + 4.0 * n) + n_a * (4.0 * m * s + 8.0 * s + 4.0 * m);
+}

@@ -1,9 +1,10 @@
 // gb_ops.cu -- measurement operators on sm_103a.
 //
-//   dense   A v  : gather of the support columns (coalesced float4 column streams,
-//                  split-K over fixed chunks of S, partials reduced in chunk order)
+//   dense   A v  : gather of the support columns, one CTA per 128-row tile streaming the
+//                  support columns as float4 rows (no partial sums, no second pass)
 //                  replaces gen_matvec_sparse (GAGA/Matrices/gen_gpu.cu:79-132,141-152)
-//           A^T r: one warp per column of the same column-major A (no transposed copy),
+//           A^T r: 4 columns per warp of the same column-major A (no transposed copy),
+//                  with the restriction to the support fused into the epilogue;
 //                  replaces gen_matvec on d_AT + matrix_transpose (gen_gpu.cu:33-74,161-171,
 //                  GAGA/gaga/kernels.cu:237-246)
 //   dct     row-subsampled orthonormal DCT-II and its transpose by Makhoul's reordering
@@ -12,150 +13,198 @@
 //   smv     A v  : one thread per row over a column-sorted CSR copy (atomic-free)
 //           A^T r: one thread per column over its d nonzeros
 //           replaces sparse_matvec / sparse_matvecT (GAGA/Matrices/smv_gpu.cu:29-47)
+#include <algorithm>
+
 #include "gb_internal.cuh"
 
 // ------------------------------------------------------------------ dense
-#define DG_THREADS 128  // 4 warps
-#define DG_ROWS 128     // rows per work item (32 lanes x float4)
-#define DG_CHUNK 32     // support columns per work item
+#define DV_THREADS 512  // A x_S: 16 warps share one 128-row tile
+#define DV_ROWS 128
+#define DV_STAGE 512    // support entries staged in shared memory per pass
+#define DA_THREADS 256  // A^T r: 8 warps, 4 columns per warp
 
 size_t gb_dense_part_floats(int m_pad, int n) {
-  size_t nch = (size_t)(n + DG_CHUNK - 1) / DG_CHUNK;
-  return nch * (size_t)m_pad;
+  (void)m_pad;
+  (void)n;
+  return 1;  // the single-pass A x_S kernel keeps no partial sums
 }
 
-// partial[c][i] = sum_{s in chunk c} A[i, S[s]] * v[S[s]]  for rows i of the work item
+// 16-byte load that does not allocate in L1 (A is streamed once per pass; r stays in L1)
+__device__ __forceinline__ float4 ld_stream4(const float *p) {
+  float4 v;
+  asm volatile("ld.global.nc.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "l"(p));
+  return v;
+}
+
+// out_i = [y_i -] sum_{s < |S|} A[i, S[s]] v[S[s]]  for the 128 rows of this CTA's tile;
+// st->red[slot] = ||out||^2.  Warps take support entries w, w+16, ... of each staged
+// chunk; the 16 partial tiles are summed in warp order (deterministic).
 template <int VEC>
-__global__ void __launch_bounds__(DG_THREADS) k_dense_gather(const GbState *__restrict__ st, int pf,
-                                                             const float *__restrict__ A, int lda, int m,
-                                                             const int *__restrict__ S,
-                                                             const float *__restrict__ v,
-                                                             float *__restrict__ part) {
+__global__ void __launch_bounds__(DV_THREADS) k_dense_av(GbState *st, int pf, const float *__restrict__ A, int lda,
+                                                         int m, const int *__restrict__ S,
+                                                         const float *__restrict__ v, const float *__restrict__ y,
+                                                         float *__restrict__ out, int slot, float *red_part,
+                                                         unsigned int *tickets) {
   if (!gb_pred(st, pf)) return;
+  lda = dimv(st, lda);
+  m = dimv(st, m);
   const int s = st->s_cnt;
-  const int nch = (s + DG_CHUNK - 1) / DG_CHUNK;
-  const int nrt = (m + DG_ROWS - 1) / DG_ROWS;
-  const int items = nrt * nch;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  __shared__ int sj[DG_CHUNK];
-  __shared__ float sv[DG_CHUNK];
-  __shared__ float4 red[4][32];
-  for (int it = blockIdx.x; it < items; it += gridDim.x) {
-    const int rt = it % nrt, ch = it / nrt;
-    const int c0 = ch * DG_CHUNK;
-    const int cn = min(DG_CHUNK, s - c0);
-    __syncthreads();
-    if (threadIdx.x < cn) {
-      int j = S[c0 + threadIdx.x];
-      sj[threadIdx.x] = j;
-      sv[threadIdx.x] = v[j];
-    }
-    __syncthreads();
+  __shared__ int sj[DV_STAGE];
+  __shared__ float sv[DV_STAGE];
+  __shared__ float4 red[DV_THREADS / 32][32];
+  const int ntile = (m + DV_ROWS - 1) / DV_ROWS;
+  float acc2 = 0.0f;
+  for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+    const int r0 = tile * DV_ROWS;
     float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
-    if (VEC == 4) {
-      const int row = rt * DG_ROWS + lane * 4;
-      if (row < m) {
-#pragma unroll 4
-        for (int c = warp; c < cn; c += 4) {
-          const float4 a = __ldg(reinterpret_cast<const float4 *>(A + (size_t)sj[c] * lda + row));
-          const float vj = sv[c];
-          a0 = fmaf(a.x, vj, a0);
-          a1 = fmaf(a.y, vj, a1);
-          a2 = fmaf(a.z, vj, a2);
-          a3 = fmaf(a.w, vj, a3);
-        }
+    for (int c0 = 0; c0 < s; c0 += DV_STAGE) {
+      const int cn = min(DV_STAGE, s - c0);
+      __syncthreads();
+      for (int c = threadIdx.x; c < cn; c += DV_THREADS) {
+        const int j = S[c0 + c];
+        sj[c] = j;
+        sv[c] = v[j];
       }
-    } else {
-      const int rbase = rt * DG_ROWS + lane;
-#pragma unroll 2
-      for (int c = warp; c < cn; c += 4) {
-        const float *col = A + (size_t)sj[c] * lda;
-        const float vj = sv[c];
-        if (rbase < m) a0 = fmaf(__ldg(col + rbase), vj, a0);
-        if (rbase + 32 < m) a1 = fmaf(__ldg(col + rbase + 32), vj, a1);
-        if (rbase + 64 < m) a2 = fmaf(__ldg(col + rbase + 64), vj, a2);
-        if (rbase + 96 < m) a3 = fmaf(__ldg(col + rbase + 96), vj, a3);
+      __syncthreads();
+      if (VEC == 4) {
+        const int row = r0 + lane * 4;
+        if (row < m) {
+#pragma unroll 8
+          for (int c = warp; c < cn; c += DV_THREADS / 32) {
+            const float4 q = ld_stream4(A + (size_t)sj[c] * lda + row);
+            const float vj = sv[c];
+            a0 = fmaf(q.x, vj, a0);
+            a1 = fmaf(q.y, vj, a1);
+            a2 = fmaf(q.z, vj, a2);
+            a3 = fmaf(q.w, vj, a3);
+          }
+        }
+      } else {
+        const int rb = r0 + lane;
+#pragma unroll 4
+        for (int c = warp; c < cn; c += DV_THREADS / 32) {
+          const float *col = A + (size_t)sj[c] * lda;
+          const float vj = sv[c];
+          if (rb < m) a0 = fmaf(__ldg(col + rb), vj, a0);
+          if (rb + 32 < m) a1 = fmaf(__ldg(col + rb + 32), vj, a1);
+          if (rb + 64 < m) a2 = fmaf(__ldg(col + rb + 64), vj, a2);
+          if (rb + 96 < m) a3 = fmaf(__ldg(col + rb + 96), vj, a3);
+        }
       }
     }
     red[warp][lane] = make_float4(a0, a1, a2, a3);
     __syncthreads();
     if (warp == 0) {
-      float4 r = red[0][lane];
+      float4 t = red[0][lane];
 #pragma unroll
-      for (int w2 = 1; w2 < 4; ++w2) {
-        float4 q = red[w2][lane];
-        r.x += q.x; r.y += q.y; r.z += q.z; r.w += q.w;
+      for (int w2 = 1; w2 < DV_THREADS / 32; ++w2) {
+        const float4 q = red[w2][lane];
+        t.x += q.x; t.y += q.y; t.z += q.z; t.w += q.w;
       }
-      float *dst = part + (size_t)ch * lda;
-      if (VEC == 4) {
-        const int row = rt * DG_ROWS + lane * 4;
-        if (row < m) *reinterpret_cast<float4 *>(dst + row) = r;
-      } else {
-        const int rbase = rt * DG_ROWS + lane;
-        if (rbase < m) dst[rbase] = r.x;
-        if (rbase + 32 < m) dst[rbase + 32] = r.y;
-        if (rbase + 64 < m) dst[rbase + 64] = r.z;
-        if (rbase + 96 < m) dst[rbase + 96] = r.w;
+      const float o4[4] = {t.x, t.y, t.z, t.w};
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const int i = VEC == 4 ? r0 + lane * 4 + c : r0 + lane + 32 * c;
+        if (i < m) {
+          const float o = y ? y[i] - o4[c] : o4[c];
+          out[i] = o;
+          acc2 = fmaf(o, o, acc2);
+        }
       }
     }
-  }
-}
-
-// out_i = [y_i -] sum_c partial[c][i]; optional ||out||^2 into st->red[slot]
-__global__ void k_dense_finish(GbState *st, int pf, const float *__restrict__ part, int lda, int m,
-                               const float *__restrict__ y, float *__restrict__ out, int slot,
-                               float *red_part, unsigned int *tickets) {
-  if (!gb_pred(st, pf)) return;
-  const int nch = (st->s_cnt + DG_CHUNK - 1) / DG_CHUNK;
-  float acc2 = 0.0f;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
-    float sum = 0.0f;
-    for (int c = 0; c < nch; ++c) sum += part[(size_t)c * lda + i];
-    float o = y ? y[i] - sum : sum;
-    out[i] = o;
-    acc2 = fmaf(o, o, acc2);
+    __syncthreads();  // red[] is rewritten by the next tile
   }
   if (slot >= 0) grid_reduce_publish<0>(acc2, slot, st, red_part, tickets);
 }
 
-// g_j = sum_i A[i, j] r_i, one warp per column
+// g_j = sum_i A[i, j] r_i.  One warp owns 4 adjacent columns: every r chunk it loads
+// (from L1) feeds 4 independent A streams.  Optional fused epilogue: xt_j = g_j if
+// bin_j <= k_bin else 0, ||xt||^2 into red[slot_sq], max|g| into red[slot_max].
 template <int VEC>
-__global__ void __launch_bounds__(256) k_dense_at(const GbState *__restrict__ st, int pf,
-                                                  const float *__restrict__ A, int lda, int m, int n,
-                                                  const float *__restrict__ r, float *__restrict__ g) {
+__global__ void __launch_bounds__(DA_THREADS) k_dense_at(GbState *st, int pf, const float *__restrict__ A, int lda,
+                                                         int m, int n, const float *__restrict__ r,
+                                                         float *__restrict__ g, const int *__restrict__ bins,
+                                                         float *__restrict__ xt, int slot_sq, int slot_max,
+                                                         float *red_part, unsigned int *tickets) {
   if (!gb_pred(st, pf)) return;
+  lda = dimv(st, lda);
+  m = dimv(st, m);
+  n = dimv(st, n);
+  const int kb = st->k_bin;
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nw = (gridDim.x * blockDim.x) >> 5;
-  for (int j = gw; j < n; j += nw) {
-    const float *col = A + (size_t)j * lda;
-    float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+  float s2 = 0.0f, gmax = 0.0f;
+  for (int j0 = gw * 4; j0 < n; j0 += nw * 4) {
+    const int nc = min(4, n - j0);
+    float acc[4][4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) acc[c][0] = acc[c][1] = acc[c][2] = acc[c][3] = 0.0f;
+    const float *col0 = A + (size_t)j0 * lda;
     if (VEC == 4) {
-      int i = lane * 4;
-      // full float4 groups (rows i..i+3 all < m)
       const int mfull = m & ~3;
-#pragma unroll 4
-      for (; i < mfull; i += 128) {
-        const float4 a = __ldg(reinterpret_cast<const float4 *>(col + i));
-        const float4 b = __ldg(reinterpret_cast<const float4 *>(r + i));
-        a0 = fmaf(a.x, b.x, a0);
-        a1 = fmaf(a.y, b.y, a1);
-        a2 = fmaf(a.z, b.z, a2);
-        a3 = fmaf(a.w, b.w, a3);
+      int i = lane * 4;
+      if (nc == 4) {
+#pragma unroll 2
+        for (; i < mfull; i += 128) {
+          const float4 b = __ldg(reinterpret_cast<const float4 *>(r + i));
+          float4 q[4];
+#pragma unroll
+          for (int c = 0; c < 4; ++c) q[c] = ld_stream4(col0 + (size_t)c * lda + i);
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            acc[c][0] = fmaf(q[c].x, b.x, acc[c][0]);
+            acc[c][1] = fmaf(q[c].y, b.y, acc[c][1]);
+            acc[c][2] = fmaf(q[c].z, b.z, acc[c][2]);
+            acc[c][3] = fmaf(q[c].w, b.w, acc[c][3]);
+          }
+        }
+      } else {
+        for (; i < mfull; i += 128) {
+          const float4 b = __ldg(reinterpret_cast<const float4 *>(r + i));
+          for (int c = 0; c < nc; ++c) {
+            const float4 q = ld_stream4(col0 + (size_t)c * lda + i);
+            acc[c][0] = fmaf(q.x, b.x, acc[c][0]);
+            acc[c][1] = fmaf(q.y, b.y, acc[c][1]);
+            acc[c][2] = fmaf(q.z, b.z, acc[c][2]);
+            acc[c][3] = fmaf(q.w, b.w, acc[c][3]);
+          }
+        }
       }
       if (i < m) {  // ragged tail inside one float4 group
-        if (i < m) a0 = fmaf(__ldg(col + i), __ldg(r + i), a0);
-        if (i + 1 < m) a1 = fmaf(__ldg(col + i + 1), __ldg(r + i + 1), a1);
-        if (i + 2 < m) a2 = fmaf(__ldg(col + i + 2), __ldg(r + i + 2), a2);
+        for (int c = 0; c < nc; ++c) {
+          const float *col = col0 + (size_t)c * lda;
+          acc[c][0] = fmaf(__ldg(col + i), __ldg(r + i), acc[c][0]);
+          if (i + 1 < m) acc[c][1] = fmaf(__ldg(col + i + 1), __ldg(r + i + 1), acc[c][1]);
+          if (i + 2 < m) acc[c][2] = fmaf(__ldg(col + i + 2), __ldg(r + i + 2), acc[c][2]);
+        }
       }
     } else {
-#pragma unroll 4
-      for (int i = lane; i < m; i += 32) a0 = fmaf(__ldg(col + i), __ldg(r + i), a0);
+      for (int i = lane; i < m; i += 32) {
+        const float b = __ldg(r + i);
+        for (int c = 0; c < nc; ++c) acc[c][0] = fmaf(__ldg(col0 + (size_t)c * lda + i), b, acc[c][0]);
+      }
     }
-    float t = (a0 + a1) + (a2 + a3);
-    t = warp_sum(t);
-    if (lane == 0) g[j] = t;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const float t = warp_sum((acc[c][0] + acc[c][1]) + (acc[c][2] + acc[c][3]));
+      if (c < nc) {
+        const int j = j0 + c;
+        if (lane == 0) g[j] = t;
+        if (xt) {
+          const float o = bins[j] <= kb ? t : 0.0f;
+          if (lane == 0) xt[j] = o;
+          if (lane == 0) s2 = fmaf(o, o, s2);
+        }
+        gmax = fmaxf(gmax, fabsf(t));
+      }
+    }
   }
+  if (slot_sq >= 0) grid_reduce_publish<0>(s2, slot_sq, st, red_part, tickets);
+  if (slot_max >= 0) grid_reduce_publish<1>(gmax, slot_max, st, red_part, tickets);
 }
 
 // ------------------------------------------------------------------ DCT
@@ -352,15 +401,20 @@ static void launch_fft(GbWork &w, cudaStream_t s, int pf, int pass, const float 
                                                                   cin, cout, rout);
 }
 
+static int dense_av_grid(const GbWork &w) {
+  const int tiles = (w.op.m + DV_ROWS - 1) / DV_ROWS;
+  return tiles < GB_MAXRB ? tiles : GB_MAXRB;
+}
+
 void enq_A(GbWork &w, cudaStream_t s, const float *v, float *out, const float *y, int slot, int pf) {
   const GbOp &op = w.op;
   if (op.kind == GB_OP_DENSE) {
-    int blocks = w.num_sms * 8;
+    const int grid = dense_av_grid(w);
     if (op.vec4)
-      k_dense_gather<4><<<blocks, DG_THREADS, 0, s>>>(w.st, pf, op.A, op.lda, op.m, w.S, v, w.part);
+      k_dense_av<4><<<grid, DV_THREADS, 0, s>>>(w.st, pf, op.A, argLDA(w), argM(w), w.S, v, y, out, slot, w.red_part,
+                                                 w.tickets);
     else
-      k_dense_gather<1><<<blocks, DG_THREADS, 0, s>>>(w.st, pf, op.A, op.lda, op.m, w.S, v, w.part);
-    k_dense_finish<<<w.red_blocks, 256, 0, s>>>(w.st, pf, w.part, op.lda, op.m, y, out, slot, w.red_part,
+      k_dense_av<1><<<grid, DV_THREADS, 0, s>>>(w.st, pf, op.A, argLDA(w), argM(w), w.S, v, y, out, slot, w.red_part,
                                                  w.tickets);
   } else if (op.kind == GB_OP_DCT) {
     launch_fft<0, LOAD_MAKHOUL, STORE_CPLX_T>(w, s, pf, 1, v, nullptr, op.cbuf0, nullptr);
@@ -373,14 +427,28 @@ void enq_A(GbWork &w, cudaStream_t s, const float *v, float *out, const float *y
   }
 }
 
+static int dense_at_grid(const GbWork &w) {
+  // 8 warps per block, 4 columns per warp
+  const int blocks = (w.op.n + 31) / 32;
+  const int cap = std::min(GB_MAXRB, w.wide_blocks);
+  return blocks < cap ? blocks : cap;
+}
+
+void enq_AT_mask(GbWork &w, cudaStream_t s, const float *r, float *g, float *xt, int slot_sq, int slot_max, int pf) {
+  const GbOp &op = w.op;
+  const int grid = dense_at_grid(w);
+  if (op.vec4)
+    k_dense_at<4><<<grid, DA_THREADS, 0, s>>>(w.st, pf, op.A, argLDA(w), argM(w), argN(w), r, g, w.bins, xt, slot_sq,
+                                               slot_max, w.red_part, w.tickets);
+  else
+    k_dense_at<1><<<grid, DA_THREADS, 0, s>>>(w.st, pf, op.A, argLDA(w), argM(w), argN(w), r, g, w.bins, xt, slot_sq,
+                                               slot_max, w.red_part, w.tickets);
+}
+
 void enq_AT(GbWork &w, cudaStream_t s, const float *r, float *g, int pf) {
   const GbOp &op = w.op;
   if (op.kind == GB_OP_DENSE) {
-    int blocks = w.num_sms * 8;
-    if (op.vec4)
-      k_dense_at<4><<<blocks, 256, 0, s>>>(w.st, pf, op.A, op.lda, op.m, op.n, r, g);
-    else
-      k_dense_at<1><<<blocks, 256, 0, s>>>(w.st, pf, op.A, op.lda, op.m, op.n, r, g);
+    enq_AT_mask(w, s, r, g, nullptr, -1, -1, pf);
   } else if (op.kind == GB_OP_DCT) {
     int blocks = (op.m + 255) / 256;
     if (blocks > w.num_sms * 8) blocks = w.num_sms * 8;

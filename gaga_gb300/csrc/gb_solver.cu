@@ -7,6 +7,7 @@
 // GbState::active and a flag.  One iteration is captured into the body of a CUDA graph
 // WHILE node whose condition the last control kernel sets from the stopping rules, so
 // a whole solve is a single graph launch.
+#include <stdlib.h>
 #include <string.h>
 
 #include "gb_internal.cuh"
@@ -104,6 +105,11 @@ __device__ static void bin_decision(GbState *st) {
   }
 }
 
+// In eager mode (no graph) the handle is 0 and the host reads GbState instead.
+__device__ __forceinline__ void set_cond(cudaGraphConditionalHandle h, unsigned v) {
+  if (h) cudaGraphSetConditional(h, v);
+}
+
 __global__ void k_ctrl(GbState *st, int phase, cudaGraphConditionalHandle h) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const int live = st->active;
@@ -130,7 +136,7 @@ __global__ void k_ctrl(GbState *st, int phase, cudaGraphConditionalHandle h) {
     case C_INIT_DONE:
       if (st->alg != GB_ALG_CGIHT) {
         st->active = keep_going(st);
-        cudaGraphSetConditional(h, st->active ? 1u : 0u);
+        set_cond(h, st->active ? 1u : 0u);
       }
       break;
     case C_CGIHT_INIT:
@@ -144,7 +150,7 @@ __global__ void k_ctrl(GbState *st, int phase, cudaGraphConditionalHandle h) {
       st->flags[F_UCG] = st->restart ? 0 : 1;
       st->flags[F_RCG] = st->restart ? 1 : 0;
       st->active = keep_going(st);
-      cudaGraphSetConditional(h, st->active ? 1u : 0u);
+      set_cond(h, st->active ? 1u : 0u);
       break;
     case C_PUSH_RES:
       if (!live) break;
@@ -168,15 +174,16 @@ __global__ void k_ctrl(GbState *st, int phase, cudaGraphConditionalHandle h) {
     }
     case C_NIHT_STOP:
       if (live) {
+        if (st->op_kind == GB_OP_DENSE) st->bytes += dense_bytes(st, 1, 2);
         st->err = st->prev[15];
         finish_iteration(st, 749);
       }
-      cudaGraphSetConditional(h, st->active ? 1u : 0u);
+      set_cond(h, st->active ? 1u : 0u);
       break;
     case C_HTP_CGINIT:
       if (!live) {
         st->flags[F_CG] = 0;
-        cudaGraphSetConditional(h, 0u);
+        set_cond(h, 0u);
         break;
       }
       for (int j = 0; j < 16; ++j) { st->prev_cg[j] = 0.0f; st->evol_cg[j] = 1.0f; }
@@ -187,7 +194,7 @@ __global__ void k_ctrl(GbState *st, int phase, cudaGraphConditionalHandle h) {
       st->prev_cg[15] = st->err_cg;
       st->it_cg = 0;
       st->flags[F_CG] = (st->err_cg > st->tol_cg) & (st->it_cg < 15) & (st->diff_cg > st->tol2);
-      cudaGraphSetConditional(h, st->flags[F_CG] ? 1u : 0u);
+      set_cond(h, st->flags[F_CG] ? 1u : 0u);
       break;
     case C_HTP_CG1: {
       // RestrictedCG_S_gen (GAGA/gaga/functions.cu:944-950)
@@ -217,15 +224,16 @@ __global__ void k_ctrl(GbState *st, int phase, cudaGraphConditionalHandle h) {
       } else {
         st->flags[F_CG] = 0;
       }
-      cudaGraphSetConditional(h, (st->flags[F_CG] && live) ? 1u : 0u);
+      set_cond(h, (st->flags[F_CG] && live) ? 1u : 0u);
       break;
     case C_HTP_STOP:
       if (live) {
+        if (st->op_kind == GB_OP_DENSE) st->bytes += dense_bytes(st, 2 + st->it_cg, 3 + 2 * st->it_cg);
         st->err = sqrtf(st->err_cg);
         push16(st->prev, st->err);
         finish_iteration(st, 125);
       }
-      cudaGraphSetConditional(h, st->active ? 1u : 0u);
+      set_cond(h, st->active ? 1u : 0u);
       break;
     case C_RCG_BETA: {
       if (!live || !st->flags[F_RCG]) break;
@@ -289,12 +297,13 @@ __global__ void k_ctrl(GbState *st, int phase, cudaGraphConditionalHandle h) {
       break;
     case C_CGIHT_STOP:
       if (live) {
+        if (st->op_kind == GB_OP_DENSE) st->bytes += dense_bytes(st, 1, st->flags[F_UCG] ? 3 : 2);
         st->err = st->prev[15];
         finish_iteration(st, 749);
         if (st->restart) { st->flags[F_UCG] = 0; st->flags[F_RCG] = 1; }
         else { st->flags[F_UCG] = st->supp_change ? 1 : 0; st->flags[F_RCG] = st->supp_change ? 0 : 1; }
       }
-      cudaGraphSetConditional(h, st->active ? 1u : 0u);
+      set_cond(h, st->active ? 1u : 0u);
       break;
     default:
       break;
@@ -316,7 +325,7 @@ __global__ void k_ctrl_l0(GbState *st, int phase, float *rec, cudaGraphCondition
       st->found = 1;
       st->active = (st->iter < st->maxiter) & (st->norm > st->tol) & (st->norm < (100.0f * st->norm0)) &
                    ((double)st->l0_diff > 0.000001) & (st->cycle != 0) & (st->found == 1);
-      cudaGraphSetConditional(h, st->active ? 1u : 0u);
+      set_cond(h, st->active ? 1u : 0u);
       break;
     case C_L0_PRE:
       if (!st->active) break;
@@ -358,7 +367,7 @@ __global__ void k_ctrl_l0(GbState *st, int phase, float *rec, cudaGraphCondition
           st->status = GB_WATCHDOG;
         }
       }
-      cudaGraphSetConditional(h, st->active ? 1u : 0u);
+      set_cond(h, st->active ? 1u : 0u);
       break;
   }
 }
@@ -370,6 +379,7 @@ __global__ void k_mask(GbState *st, int pf, const float *__restrict__ src, float
                        const int *__restrict__ bins, int n, int slot_sq, int slot_max, float *rp,
                        unsigned int *tk) {
   if (!gb_pred(st, pf)) return;
+  n = dimv(st, n);
   const int kb = st->k_bin;
   float s2 = 0.0f, mx = 0.0f;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -386,6 +396,7 @@ __global__ void k_mask(GbState *st, int pf, const float *__restrict__ src, float
 // v_i = 0 where bin_i > k_bin (threshold, GAGA/gaga/kernels.cu:74-81)
 __global__ void k_threshold(const GbState *st, int pf, float *__restrict__ v, const int *__restrict__ bins, int n) {
   if (!gb_pred(st, pf)) return;
+  n = dimv(st, n);
   const int kb = st->k_bin;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     if (bins[i] > kb) v[i] = 0.0f;
@@ -407,6 +418,8 @@ __device__ __forceinline__ float pick(const GbState *st, int which) {
 __global__ void k_axpy(GbState *st, int pf, int which, const float *__restrict__ x, float *__restrict__ y, int n,
                        int slot_max, int slot_sq, int *counters, int ncount, float *rp, unsigned int *tk) {
   if (!gb_pred(st, pf)) return;
+  n = dimv(st, n);
+  ncount = dimv(st, ncount);
   const float a = pick(st, which);
   float mx = 0.0f, s2 = 0.0f;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -425,6 +438,7 @@ __global__ void k_axpy(GbState *st, int pf, int which, const float *__restrict__
 __global__ void k_scale_add(const GbState *st, int pf, int which, float *__restrict__ a, const float *__restrict__ b,
                             int n) {
   if (!gb_pred(st, pf)) return;
+  n = dimv(st, n);
   const float beta = pick(st, which);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float t = beta * a[i];
@@ -437,6 +451,8 @@ __global__ void k_dot2(GbState *st, int pf, const float *__restrict__ a, const f
                        const float *__restrict__ c, const float *__restrict__ d, int s2, int n2, float *rp,
                        unsigned int *tk) {
   if (!gb_pred(st, pf)) return;
+  n1 = dimv(st, n1);
+  n2 = dimv(st, n2);
   float p = 0.0f, q = 0.0f;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n1; i += gridDim.x * blockDim.x) p = fmaf(a[i], b[i], p);
   if (c)
@@ -449,6 +465,7 @@ __global__ void k_dot2(GbState *st, int pf, const float *__restrict__ a, const f
 __global__ void k_copy_norm(GbState *st, int pf, const float *__restrict__ src, float *__restrict__ dst, int n,
                             int slot_sq, int slot_max, float *rp, unsigned int *tk) {
   if (!gb_pred(st, pf)) return;
+  n = dimv(st, n);
   float s2 = 0.0f, mx = 0.0f;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float v = src[i];
@@ -479,6 +496,7 @@ __device__ __forceinline__ int lin_bin(float v, float slope, float intercept, fl
 __global__ void k_hist(const GbState *st, int pf, const float *__restrict__ v, int *__restrict__ bins,
                        int *__restrict__ bins_prev, int *__restrict__ counters, int n) {
   if (!gb_pred(st, pf)) return;
+  n = dimv(st, n);
   const float intercept = st->max_value;
   const float slope = st->slope;
   const float small_f = __double2float_rd((double)intercept * 0.000001);
@@ -502,6 +520,7 @@ __global__ void k_hist(const GbState *st, int pf, const float *__restrict__ v, i
 // (GAGA/gaga/functions.cu:412-433).  One block of 1024 threads does the same scan.
 __global__ void __launch_bounds__(1024) k_kbin(GbState *st, int pf, const int *__restrict__ counters, int k) {
   if (!gb_pred(st, pf)) return;
+  k = dimv(st, k);
   __shared__ int scan[1024];
   __shared__ int res_kbin, res_sum;
   const int max_bin = st->max_bin;
@@ -552,6 +571,7 @@ __global__ void __launch_bounds__(256) k_thresh_count(GbState *st, int pf, float
                                                       const int *__restrict__ bins, const int *__restrict__ bins_prev,
                                                       int n, int *__restrict__ tile_cnt) {
   if (!gb_pred(st, pf)) return;
+  n = dimv(st, n);
   const int kb = st->k_bin, kbp = st->k_bin_prev;
   const bool count = st->flags[F_DOBIN] != 0;
   const int base = blockIdx.x * GB_TILE;
@@ -579,6 +599,7 @@ __global__ void __launch_bounds__(256) k_thresh_count(GbState *st, int pf, float
 __global__ void __launch_bounds__(256) k_compact(GbState *st, int pf, const int *__restrict__ bins, int n,
                                                  const int *__restrict__ tile_cnt, int *__restrict__ S) {
   if (!gb_pred(st, pf)) return;
+  n = dimv(st, n);
   __shared__ float sm[32];
   __shared__ int warp_base[8];
   const int kb = st->k_bin;
@@ -708,7 +729,7 @@ gb_status close_while(cudaStream_t body) {
 }  // namespace
 
 static void enq_mask(GbWork &w, cudaStream_t s, int pf, const float *src, float *dst, int slot_sq, int slot_max) {
-  k_mask<<<w.red_blocks, 256, 0, s>>>(w.st, pf, src, dst, w.bins, w.op.n, slot_sq, slot_max, w.red_part, w.tickets);
+  k_mask<<<w.red_blocks, 256, 0, s>>>(w.st, pf, src, dst, w.bins, argN(w), slot_sq, slot_max, w.red_part, w.tickets);
 }
 static void enq_axpy(GbWork &w, cudaStream_t s, int pf, int which, const float *x, float *y, int n, int slot_max,
                      bool clear_counters, int num_bins) {
@@ -722,59 +743,67 @@ static void enq_ctrl(GbWork &w, cudaStream_t s, int phase, cudaGraphConditionalH
 // FindSupportSet + Threshold: binning, k-th bin and ordered compaction predicated on
 // F_DOBIN; the threshold of x always runs
 static void enq_support(GbWork &w, cudaStream_t s, int k, bool save_prev) {
-  const int n = w.op.n;
+  const int n = argN(w);
   k_hist<<<w.red_blocks, 256, 0, s>>>(w.st, F_DOBIN, w.x, w.bins, save_prev ? w.bins_prev : nullptr, w.counters, n);
-  k_kbin<<<1, 1024, 0, s>>>(w.st, F_DOBIN, w.counters, k);
-  const int tiles = (n + GB_TILE - 1) / GB_TILE;
+  k_kbin<<<1, 1024, 0, s>>>(w.st, F_DOBIN, w.counters, w.dyn ? D_K : k);
+  const int tiles = (w.op.n + GB_TILE - 1) / GB_TILE;  // capacity; tiles past n count 0
   k_thresh_count<<<tiles, 256, 0, s>>>(w.st, F_ALWAYS, w.x, w.bins, save_prev ? w.bins_prev : nullptr, n, w.tile_cnt);
   k_compact<<<tiles, 256, 0, s>>>(w.st, F_DOBIN, w.bins, n, w.tile_cnt, w.S);
 }
 
-static gb_status build_graph(GbWork &w, int alg, int k, int num_bins, cudaStream_t s0, cudaStream_t s1,
-                             cudaStream_t s2, cudaGraph_t *graph) {
-  const int n = w.op.n, m = w.op.m;
-  GB_CUDA_TRY(cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal));
-  cudaGraphConditionalHandle h_outer = 0, h_inner = 0;
-  GB_TRY(make_handle(s0, &h_outer));
-  if (alg == GB_ALG_PARALLEL_L0) {
+// The solve as pieces: prologue, loop body (with the HTP inner CG loop), run either as one
+// graph with WHILE nodes or eagerly (GB_CS_EAGER=1: same kernels, host-checked loops;
+// used for profiling, since kernels inside conditional graphs cannot be profiled).
+void enq_prologue(SolvePlan &P, cudaStream_t s0, cudaGraphConditionalHandle h_outer) {
+  GbWork &w = *P.w;
+  const int n = argN(w), m = argM(w), k = P.k, num_bins = w.dyn ? D_NBINS : P.num_bins;
+  if (P.alg == GB_ALG_PARALLEL_L0) {
     // res = y - A x with x = 0 (computeResidual, GAGA/gaga/expander/functions.cu:73-79)
     enq_A(w, s0, w.x, w.resid, w.y, R_RES, F_ALWAYS);
     k_ctrl_l0<<<1, 32, 0, s0>>>(w.st, C_L0_INIT, w.rec, h_outer);
-  } else {
-    // resid = y; err = ||y||  (algorithms.cu:1296-1300)
-    k_copy_norm<<<w.red_blocks, 256, 0, s0>>>(w.st, F_ALWAYS, w.y, w.resid, m, R_RES, -1, w.red_part, w.tickets);
-    enq_ctrl(w, s0, C_INIT0);
-    // x = A^T y ; max |x| ; FindSupportSet ; Threshold  (algorithms.cu:1335-1354)
-    enq_AT(w, s0, w.y, w.x, F_ALWAYS);
-    k_copy_norm<<<w.red_blocks, 256, 0, s0>>>(w.st, F_ALWAYS, w.x, nullptr, n, -1, R_XMAX, w.red_part, w.tickets);
-    enq_ctrl(w, s0, C_INIT_BINPREP);
-    k_axpy<<<w.red_blocks, 256, 0, s0>>>(w.st, F_ALWAYS, SC_ONE, w.x, w.x, 0, -1, -1, w.counters, num_bins,
-                                         w.red_part, w.tickets);
-    enq_support(w, s0, k, false);
-    if (alg == GB_ALG_CGIHT) {
-      // r0, grad_previous = A^T r0, grad_prev_thres (algorithms.cu:3776-3808)
-      enq_A(w, s0, w.x, w.resid, w.y, R_RES, F_ALWAYS);
-      enq_AT(w, s0, w.resid, w.gp, F_ALWAYS);
-      enq_mask(w, s0, F_ALWAYS, w.gp, w.gpt, -1, -1);
-      enq_ctrl(w, s0, C_CGIHT_INIT, h_outer);
-    } else {
-      enq_ctrl(w, s0, C_INIT_DONE, h_outer);
-    }
+    return;
   }
-  GB_TRY(open_while(s0, s1, h_outer));
-  // ---------------- loop body (one outer iteration) on s1
-  if (alg == GB_ALG_NIHT || alg == GB_ALG_HTP) {
+  // resid = y; err = ||y||  (algorithms.cu:1296-1300)
+  k_copy_norm<<<w.red_blocks, 256, 0, s0>>>(w.st, F_ALWAYS, w.y, w.resid, m, R_RES, -1, w.red_part, w.tickets);
+  enq_ctrl(w, s0, C_INIT0);
+  // x = A^T y ; max |x| ; FindSupportSet ; Threshold  (algorithms.cu:1335-1354)
+  enq_AT(w, s0, w.y, w.x, F_ALWAYS);
+  k_copy_norm<<<w.red_blocks, 256, 0, s0>>>(w.st, F_ALWAYS, w.x, nullptr, n, -1, R_XMAX, w.red_part, w.tickets);
+  enq_ctrl(w, s0, C_INIT_BINPREP);
+  k_axpy<<<w.red_blocks, 256, 0, s0>>>(w.st, F_ALWAYS, SC_ONE, w.x, w.x, 0, -1, -1, w.counters, num_bins,
+                                       w.red_part, w.tickets);
+  enq_support(w, s0, k, false);
+  if (P.alg == GB_ALG_CGIHT) {
+    // r0, grad_previous = A^T r0, grad_prev_thres (algorithms.cu:3776-3808)
+    enq_A(w, s0, w.x, w.resid, w.y, R_RES, F_ALWAYS);
+    enq_AT(w, s0, w.resid, w.gp, F_ALWAYS);
+    enq_mask(w, s0, F_ALWAYS, w.gp, w.gpt, -1, -1);
+    enq_ctrl(w, s0, C_CGIHT_INIT, h_outer);
+  } else {
+    enq_ctrl(w, s0, C_INIT_DONE, h_outer);
+  }
+}
+
+// first part of an outer iteration (everything for NIHT / CGIHT; up to the CG loop for HTP)
+void enq_body(SolvePlan &P, cudaStream_t s1, cudaGraphConditionalHandle h_outer) {
+  GbWork &w = *P.w;
+  const int n = argN(w), m = argM(w), k = P.k, num_bins = w.dyn ? D_NBINS : P.num_bins;
+  if (P.alg == GB_ALG_NIHT || P.alg == GB_ALG_HTP) {
     // RestrictedSD (GAGA/gaga/functions.cu:659-745)
     enq_A(w, s1, w.x, w.resid, w.y, R_RES, F_ALWAYS);
     enq_ctrl(w, s1, C_PUSH_RES);
-    enq_AT(w, s1, w.resid, w.grad, F_ALWAYS);
-    enq_mask(w, s1, F_ALWAYS, w.grad, w.xt, R_XT, R_GMAX);
+    if (w.op.kind == GB_OP_DENSE) {
+      enq_AT_mask(w, s1, w.resid, w.grad, w.xt, R_XT, R_GMAX, F_ALWAYS);
+    } else {
+      enq_AT(w, s1, w.resid, w.grad, F_ALWAYS);
+      enq_mask(w, s1, F_ALWAYS, w.grad, w.xt, R_XT, R_GMAX);
+    }
     enq_A(w, s1, w.xt, w.ru, nullptr, R_AXT, F_ALWAYS);
     enq_ctrl(w, s1, C_SD_MU);
     enq_axpy(w, s1, F_ALWAYS, SC_MU, w.grad, w.x, n, R_XMAX, true, num_bins);
     enq_ctrl(w, s1, C_BINPREP);
     enq_support(w, s1, k, false);
-    if (alg == GB_ALG_NIHT) {
+    if (P.alg == GB_ALG_NIHT) {
       enq_ctrl(w, s1, C_NIHT_STOP, h_outer);
     } else {
       // CG projection on the support (GAGA/gaga/algorithms.cu:2588-2669)
@@ -782,43 +811,32 @@ static gb_status build_graph(GbWork &w, int alg, int k, int num_bins, cudaStream
       enq_AT(w, s1, w.resid, w.grad, F_ALWAYS);
       k_threshold<<<w.red_blocks, 256, 0, s1>>>(w.st, F_ALWAYS, w.grad, w.bins, n);
       k_copy_norm<<<w.red_blocks, 256, 0, s1>>>(w.st, F_ALWAYS, w.grad, w.gp, n, R_DOT1, -1, w.red_part, w.tickets);
-      GB_TRY(make_handle(s1, &h_inner));
-      enq_ctrl(w, s1, C_HTP_CGINIT, h_inner);
-      GB_TRY(open_while(s1, s2, h_inner));
-      {
-        // RestrictedCG_S_gen (GAGA/gaga/functions.cu:922-1000)
-        enq_A(w, s2, w.grad, w.resid, nullptr, R_CG, F_CG);
-        enq_ctrl(w, s2, C_HTP_CG1);
-        enq_axpy(w, s2, F_CG, SC_CG_ALPHA, w.grad, w.x, n, -1, false, 0);
-        enq_AT(w, s2, w.resid, w.xt, F_CG);
-        k_threshold<<<w.red_blocks, 256, 0, s2>>>(w.st, F_CG, w.xt, w.bins, n);
-        k_axpy<<<w.red_blocks, 256, 0, s2>>>(w.st, F_CG, SC_NEG_CG_ALPHA, w.xt, w.gp, n, -1, R_DOT3, nullptr, 0,
-                                             w.red_part, w.tickets);
-        enq_ctrl(w, s2, C_HTP_CG2);
-        k_scale_add<<<w.red_blocks, 256, 0, s2>>>(w.st, F_CG, SC_CG_BETA, w.grad, w.gp, n);
-        enq_A(w, s2, w.x, w.resid, w.y, R_RES, F_CG);
-        enq_ctrl(w, s2, C_HTP_CG3, h_inner);
-      }
-      GB_TRY(close_while(s2));
-      enq_ctrl(w, s1, C_HTP_STOP, h_outer);
     }
-  } else if (alg == GB_ALG_CGIHT) {
+  } else if (P.alg == GB_ALG_CGIHT) {
     // RestrictedCGwithSupportEvolution (functions.cu:1004-1102) under F_RCG;
     // UnrestrictedCG (functions.cu:1107-1220) under F_UCG
     enq_A(w, s1, w.x, w.resid, w.y, R_RES, F_RCG);
     enq_A(w, s1, w.x, w.ru, w.y, R_RES, F_UCG);
     enq_ctrl(w, s1, C_PUSH_RES);
     // RCG branch
-    enq_AT(w, s1, w.resid, w.grad, F_RCG);
-    enq_mask(w, s1, F_RCG, w.grad, w.xt, R_XT, -1);
+    if (w.op.kind == GB_OP_DENSE) {
+      enq_AT_mask(w, s1, w.resid, w.grad, w.xt, R_XT, -1, F_RCG);
+    } else {
+      enq_AT(w, s1, w.resid, w.grad, F_RCG);
+      enq_mask(w, s1, F_RCG, w.grad, w.xt, R_XT, -1);
+    }
     enq_ctrl(w, s1, C_RCG_BETA);
     k_scale_add<<<w.red_blocks, 256, 0, s1>>>(w.st, F_RCG, SC_CG_BETA, w.gp, w.grad, n);
     enq_mask(w, s1, F_RCG, w.gp, w.gpt, -1, R_GMAX);
     enq_A(w, s1, w.gpt, w.ru, nullptr, R_AXT, F_RCG);
     enq_ctrl(w, s1, C_RCG_ALPHA);
     // UCG branch
-    enq_AT(w, s1, w.ru, w.grad, F_UCG);
-    enq_mask(w, s1, F_UCG, w.grad, w.xt, R_XT, -1);
+    if (w.op.kind == GB_OP_DENSE) {
+      enq_AT_mask(w, s1, w.ru, w.grad, w.xt, R_XT, -1, F_UCG);
+    } else {
+      enq_AT(w, s1, w.ru, w.grad, F_UCG);
+      enq_mask(w, s1, F_UCG, w.grad, w.xt, R_XT, -1);
+    }
     enq_A(w, s1, w.gpt, w.resid, nullptr, -1, F_UCG);
     enq_A(w, s1, w.xt, w.ru, nullptr, -1, F_UCG);
     k_dot2<<<w.red_blocks, 256, 0, s1>>>(w.st, F_UCG, w.resid, w.ru, R_DOT1, m, w.resid, w.resid, R_DOT2, m,
@@ -841,15 +859,93 @@ static gb_status build_graph(GbWork &w, int alg, int k, int num_bins, cudaStream
   } else {
     // parallel_l0 loop (GAGA/gaga/expander/parallel_l0.cu:56-137)
     k_ctrl_l0<<<1, 32, 0, s1>>>(w.st, C_L0_PRE, w.rec, 0);
-    int blocks = (n + 255) / 256;
+    int blocks = (w.op.n + 255) / 256;
     if (blocks > w.num_sms * 16) blocks = w.num_sms * 16;
     k_l0_scores<<<blocks, 256, 0, s1>>>(w.st, w.resid, w.x, w.upd, w.op.smv_rows, n, w.op.d);
     k_l0_update<<<w.red_blocks, 256, 0, s1>>>(w.st, w.resid, w.op.csr_ptr, w.op.csr_col, w.upd, m, w.red_part,
                                                w.tickets);
     k_ctrl_l0<<<1, 32, 0, s1>>>(w.st, C_L0_STOP, w.rec, h_outer);
   }
+}
+
+// HTP inner CG step (RestrictedCG_S_gen, GAGA/gaga/functions.cu:922-1000)
+void enq_cg_body(SolvePlan &P, cudaStream_t s2, cudaGraphConditionalHandle h_inner) {
+  GbWork &w = *P.w;
+  const int n = argN(w);
+  enq_A(w, s2, w.grad, w.resid, nullptr, R_CG, F_CG);
+  enq_ctrl(w, s2, C_HTP_CG1);
+  enq_axpy(w, s2, F_CG, SC_CG_ALPHA, w.grad, w.x, n, -1, false, 0);
+  enq_AT(w, s2, w.resid, w.xt, F_CG);
+  k_threshold<<<w.red_blocks, 256, 0, s2>>>(w.st, F_CG, w.xt, w.bins, n);
+  k_axpy<<<w.red_blocks, 256, 0, s2>>>(w.st, F_CG, SC_NEG_CG_ALPHA, w.xt, w.gp, n, -1, R_DOT3, nullptr, 0, w.red_part,
+                                       w.tickets);
+  enq_ctrl(w, s2, C_HTP_CG2);
+  k_scale_add<<<w.red_blocks, 256, 0, s2>>>(w.st, F_CG, SC_CG_BETA, w.grad, w.gp, n);
+  enq_A(w, s2, w.x, w.resid, w.y, R_RES, F_CG);
+  enq_ctrl(w, s2, C_HTP_CG3, h_inner);
+}
+
+void enq_ctrl_phase(GbWork &w, cudaStream_t s, int phase, cudaGraphConditionalHandle h) {
+  enq_ctrl(w, s, phase == GB_PHASE_HTP_CGINIT ? C_HTP_CGINIT : phase == GB_PHASE_HTP_STOP ? C_HTP_STOP : phase, h);
+}
+gb_status gb_make_handle(cudaStream_t parent, cudaGraphConditionalHandle *h) { return make_handle(parent, h); }
+gb_status gb_open_while(cudaStream_t parent, cudaStream_t body, cudaGraphConditionalHandle h) {
+  return open_while(parent, body, h);
+}
+gb_status gb_close_while(cudaStream_t body) { return close_while(body); }
+
+static gb_status build_graph(SolvePlan &P, cudaStream_t s0, cudaStream_t s1, cudaStream_t s2, cudaGraph_t *graph) {
+  GbWork &w = *P.w;
+  GB_CUDA_TRY(cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal));
+  cudaGraphConditionalHandle h_outer = 0, h_inner = 0;
+  GB_TRY(make_handle(s0, &h_outer));
+  enq_prologue(P, s0, h_outer);
+  GB_TRY(open_while(s0, s1, h_outer));
+  enq_body(P, s1, h_outer);
+  if (P.alg == GB_ALG_HTP) {
+    GB_TRY(make_handle(s1, &h_inner));
+    enq_ctrl(w, s1, C_HTP_CGINIT, h_inner);
+    GB_TRY(open_while(s1, s2, h_inner));
+    enq_cg_body(P, s2, h_inner);
+    GB_TRY(close_while(s2));
+    enq_ctrl(w, s1, C_HTP_STOP, h_outer);
+  }
   GB_TRY(close_while(s1));
   GB_CUDA_TRY(cudaStreamEndCapture(s0, graph));
+  return GB_OK;
+}
+
+static gb_status read_int(const int *d, int *h, cudaStream_t s) {
+  GB_CUDA_TRY(cudaMemcpyAsync(h, d, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  return GB_OK;
+}
+
+// Eager execution: the same kernels, the loop conditions read back by the host.
+static gb_status run_eager(SolvePlan &P, cudaStream_t s) {
+  GbWork &w = *P.w;
+  enq_prologue(P, s, 0);
+  int active = 0, guard = 0;
+  GB_TRY(read_int(&w.st->active, &active, s));
+  const int limit = P.w->op.n + 1;  // replaced below by the state's pass limit
+  (void)limit;
+  GbState probe;
+  GB_CUDA_TRY(cudaMemcpy(&probe, w.st, sizeof(probe), cudaMemcpyDeviceToHost));
+  while (active && guard++ <= probe.pass_limit) {
+    enq_body(P, s, 0);
+    if (P.alg == GB_ALG_HTP) {
+      enq_ctrl(w, s, C_HTP_CGINIT, 0);
+      int cg = 0, g2 = 0;
+      GB_TRY(read_int(&w.st->flags[F_CG], &cg, s));
+      while (cg && g2++ < 16) {
+        enq_cg_body(P, s, 0);
+        GB_TRY(read_int(&w.st->flags[F_CG], &cg, s));
+      }
+      enq_ctrl(w, s, C_HTP_STOP, 0);
+    }
+    GB_TRY(read_int(&w.st->active, &active, s));
+  }
+  GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
 }
 
@@ -881,6 +977,7 @@ static GbState initial_state(const GbWork &w, int alg, const gb_options &o, int 
   st.tol2 = 10.0f * st.tol_cg;
   st.l0_len = 2 * w.op.d;
   st.flags[F_ALWAYS] = 1;
+  st.op_kind = w.op.kind;
   return st;
 }
 
@@ -890,13 +987,16 @@ gb_status gb_run_solver(GbWork &w, int alg, const gb_options &o, int k, cudaStre
   GbState init = initial_state(w, alg, o, k, tol_abs);
   k_init_state<<<1, 1, 0, s>>>(w.st, init);
   GB_CUDA_TRY(cudaGetLastError());
+  SolvePlan P{&w, alg, k, o.num_bins};
+  static const bool eager = getenv("GB_CS_EAGER") && atoi(getenv("GB_CS_EAGER")) != 0;
+  if (eager) return run_eager(P, s);
   cudaStream_t s0, s1, s2;
   GB_CUDA_TRY(cudaStreamCreateWithFlags(&s0, cudaStreamNonBlocking));
   GB_CUDA_TRY(cudaStreamCreateWithFlags(&s1, cudaStreamNonBlocking));
   GB_CUDA_TRY(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  gb_status rc = build_graph(w, alg, k, o.num_bins, s0, s1, s2, &graph);
+  gb_status rc = build_graph(P, s0, s1, s2, &graph);
   if (rc == GB_OK) {
     cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
     if (e != cudaSuccess) {
@@ -920,14 +1020,52 @@ gb_status gb_run_solver(GbWork &w, int alg, const gb_options &o, int k, cudaStre
 }
 
 // ------------------------------------------------------------------ component helpers
-__global__ void k_support_nonzero(GbState *st, const float *__restrict__ v, int n, int *__restrict__ S) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  int c = 0;
-  for (int i = 0; i < n; ++i)
-    if (v[i] != 0.0f) S[c++] = i;
-  st->s_cnt = c;
+// S := ascending { j : v_j != 0 }, with the ordered compaction of the solver
+__global__ void __launch_bounds__(256) k_nonzero_count(const float *__restrict__ v, int n, int *__restrict__ tile_cnt) {
+  const int base = blockIdx.x * GB_TILE;
+  int cnt = 0;
+  for (int q = threadIdx.x; q < GB_TILE; q += blockDim.x) {
+    const int i = base + q;
+    if (i < n && v[i] != 0.0f) cnt++;
+  }
+  __shared__ float sm[32];
+  const float tot = block_reduce<0>((float)cnt, sm);
+  if (threadIdx.x == 0) tile_cnt[blockIdx.x] = (int)tot;
+}
+
+__global__ void __launch_bounds__(256) k_nonzero_compact(GbState *st, const float *__restrict__ v, int n,
+                                                         const int *__restrict__ tile_cnt, int *__restrict__ S) {
+  __shared__ float sm[32];
+  __shared__ int warp_base[8];
+  __shared__ int s_off;
+  float off = 0.0f;
+  for (int t = threadIdx.x; t < (int)blockIdx.x; t += blockDim.x) off += (float)tile_cnt[t];
+  const int offset = (int)block_reduce<0>(off, sm);
+  if (threadIdx.x == 0) s_off = offset;
+  __syncthreads();
+  int running = s_off;
+  const int base = blockIdx.x * GB_TILE;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int q0 = 0; q0 < GB_TILE; q0 += blockDim.x) {
+    const int i = base + q0 + threadIdx.x;
+    const bool in = i < n && v[i] != 0.0f;
+    const unsigned bal = __ballot_sync(0xffffffffu, in);
+    if (lane == 0) warp_base[wid] = __popc(bal);
+    __syncthreads();
+    int wb = 0, tot = 0;
+    for (int w2 = 0; w2 < 8; ++w2) {
+      if (w2 < wid) wb += warp_base[w2];
+      tot += warp_base[w2];
+    }
+    if (in) S[running + wb + __popc(bal & ((1u << lane) - 1u))] = i;
+    running += tot;
+    __syncthreads();
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) st->s_cnt = running;
 }
 
 void enq_support_of_nonzeros(GbWork &w, cudaStream_t s, const float *v, int n) {
-  k_support_nonzero<<<1, 1, 0, s>>>(w.st, v, n, w.S);
+  const int tiles = (n + GB_TILE - 1) / GB_TILE;
+  k_nonzero_count<<<tiles, 256, 0, s>>>(v, n, w.tile_cnt);
+  k_nonzero_compact<<<tiles, 256, 0, s>>>(w.st, v, n, w.tile_cnt, w.S);
 }

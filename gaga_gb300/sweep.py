@@ -1,0 +1,43 @@
+"""Phase-transition sweep of independent dense Gaussian trials.
+
+The grid is n in {1024, 2048, 4096, 8192, 16384}, delta = m/n in {0.1, ..., 0.9} and
+rho = k/m on a 0.02 grid up to 0.5 (1125 points); a sweep of T trials cycles through the
+grid with a distinct trial id (and therefore a distinct seeded A and x) per trial.  The
+reference sweeps the same grid shape through gaga_cs one trial per call
+(GAGA/gaga_for_CS_timings/generate_gpu_gen_timing_data.m, GAGA/CGIHTcode/shared/
+tests_delta_fixed.m), with success meaning a small relative error.
+"""
+import numpy as np
+
+N_VALUES = (1024, 2048, 4096, 8192, 16384)
+DELTAS = tuple(round(0.1 * i, 1) for i in range(1, 10))
+RHOS = tuple(round(0.02 * i, 2) for i in range(1, 26))
+
+
+def grid():
+    pts = [(n, d, r) for n in N_VALUES for d in DELTAS for r in RHOS]
+    return pts
+
+
+def sweep_trials(total=4096):
+    """Arrays (n, m, k, trial_id) of a sweep of `total` trials."""
+    pts = grid()
+    n = np.empty(total, np.int32)
+    m = np.empty(total, np.int32)
+    k = np.empty(total, np.int32)
+    for t in range(total):
+        nn, dd, rr = pts[t % len(pts)]
+        mm = int(round(dd * nn))
+        n[t], m[t], k[t] = nn, mm, max(1, int(round(rr * mm)))
+    return n, m, k, np.arange(total, dtype=np.uint32)
+
+
+def wave(total, waves, w):
+    """Indices of wave w when a sweep of `total` trials is split into `waves` interleaved waves."""
+    return np.arange(w, total, waves)
+
+
+def shard(indices, rank, world):
+    """Trials of one rank: contiguous, balanced by estimated cost (m*n)."""
+    indices = np.asarray(indices)
+    return indices[rank::world]

@@ -155,8 +155,9 @@ gb_status gb_cs_l0_step(float *d_res, float *d_x, float *d_updates, const int *d
 
 /* ---- batched form (no reference counterpart: the reference solves one trial per call) ----
  * Thousands of independent dense Gaussian trials, each with its own (n, m, k) and its own
- * A drawn on the device from (seed, trial id), solved by NIHT or CGIHT in one persistent
- * launch.  Per-trial outputs (host or device arrays of ntrials entries, any may be NULL):
+ * problem drawn on the device exactly as gb_cs_generate_and_solve draws it with seed
+ * `seed + trial_id` (Gaussian A, +-1 signal), solved by NIHT in one persistent launch per
+ * size class (n <= 20000).  Per-trial outputs (host or device arrays of ntrials entries, any may be NULL):
  * iterations, relative l2 error against the generated x, and a verdict flag
  * (rel l2 <= 1e-3).  tol_rel is relative to ||y||. */
 typedef struct {
@@ -173,6 +174,11 @@ typedef struct {
 
 gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float *rel_err_out,
                             int *success_out, int *num_success);
+
+/* Algorithmic matvec bytes (per-iteration operator traffic summed over all trials) and the
+ * device time in ms of the last gb_cs_solve_batch call on this thread (no reference
+ * counterpart; used for roofline reporting). */
+void gb_cs_batch_last_stats(double *bytes, float *kernel_ms);
 
 #ifdef __cplusplus
 }

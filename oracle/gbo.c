@@ -903,26 +903,25 @@ void gbo_results(const float *x, const float *x_true, int n, int k, float norms[
 int gbo_solve_dense_trials(int ntrials, const int *nn, const int *mm, const int *kk, uint32_t seed,
                            const uint32_t *trial_ids, int alg, float tol_rel, int maxiter,
                            int threads, int *iters, float *rel_err) {
+  /* trials one after another; generation and operators use all `threads` inside a trial */
   int ok = 0;
 #ifdef _OPENMP
   if (threads > 0) omp_set_num_threads(threads);
 #endif
-#pragma omp parallel for schedule(dynamic, 1) reduction(+ : ok)
   for (int t = 0; t < ntrials; ++t) {
     int n = nn[t], m = mm[t], k = kk[t];
     uint32_t tid = trial_ids ? trial_ids[t] : (uint32_t)t;
+    /* trial tid of a sweep is the problem drawn with seed + tid (the device's keying) */
+    const uint32_t key = seed + tid;
     float *A = (float *)malloc(sizeof(float) * (size_t)m * n);
     float *xt = (float *)malloc(sizeof(float) * n);
     float *x = (float *)calloc((size_t)n, sizeof(float));
     float *y = (float *)malloc(sizeof(float) * m);
-    /* generation is serial inside a trial (the outer loop is parallel) */
-    for (int j = 0; j < n; ++j)
-      for (int i = 0; i < m; ++i) A[(size_t)j * m + i] = gauss_at(seed, tid, ST_MATRIX, (uint64_t)j * m + i) *
-                                                          (1.0f / sqrtf((float)m));
-    int ksupp = gbo_gen_vector(n, k, 1, seed, tid, xt);
+    gbo_gen_dense(m, n, m, 1, key, 0, A);
+    int ksupp = gbo_gen_vector(n, k, 1, key, 0, xt);
     gbo_op op = {GBO_OP_DENSE, m, n, A, m, 0, 0, 0, 0};
     gbo_A(&op, xt, y);
-    gbo_opts o = {alg, tol_rel * nrm2f(y, m), maxiter, n / 20 > 1000 ? n / 20 : 1000, 0, 1, 1};
+    gbo_opts o = {alg, tol_rel * nrm2f(y, m), maxiter, n / 20 > 1000 ? n / 20 : 1000, 0, 1, threads};
     gbo_info info;
     gbo_solve(&op, y, ksupp, &o, x, &info);
     float norms[3];

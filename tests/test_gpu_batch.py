@@ -1,0 +1,68 @@
+"""Batched form (gb_cs_solve_batch) against the single-trial drop-in and the CPU oracle.
+
+Every batched trial is the problem gb_cs_generate_and_solve draws with seed + trial id,
+so both forms solve bit-identical inputs; their FP32 trajectories differ only in
+reduction order, so success verdicts (relative l2 error <= 1e-3) must agree on almost
+every trial and recovered signals must agree to 1e-4.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SEED = 777
+
+
+def pick(ns, count):
+    from gaga_gb300 import sweep
+
+    n, m, k, tid = sweep.sweep_trials(4096)
+    idx = np.flatnonzero(np.isin(n, ns))
+    idx = idx[np.linspace(0, len(idx) - 1, count).astype(int)]
+    return n[idx], m[idx], k[idx], tid[idx]
+
+
+def plain(gb, n, m, k, tid, maxiter):
+    opts = gb.gaga_options("tol", 1e-4, "tol_is_relative", 1, "maxiter", maxiter, "seed", int(SEED + tid))
+    x, xt, r = gb.generate_and_solve("NIHT", "gen", int(k), int(m), int(n), 0, opts)
+    return x, xt, r
+
+
+def test_batch_matches_plain_small(gb):
+    n, m, k, tid = pick([1024, 2048, 4096], 48)
+    ns, iters, err, ok = gb.solve_batch(n, m, k, SEED, tid, alg="NIHT", tol_rel=1e-4, maxiter=1000)
+    agree = 0
+    for i in range(len(n)):
+        x, xt, r = plain(gb, n[i], m[i], k[i], tid[i], 1000)
+        v_plain = r.norms[1] <= 1e-3
+        agree += int(v_plain == bool(ok[i]))
+        if v_plain and ok[i]:
+            assert err[i] < 1e-3 and r.norms[1] < 1e-3
+    assert agree >= len(n) - 1, (agree, len(n))
+    assert ns == int(ok.sum())
+    assert 0 < ns < len(n)  # the sample straddles the phase transition
+
+
+def test_batch_large_trials(gb):
+    """n = 8192 and 16384 trials next to each other in one batch."""
+    n, m, k, tid = pick([8192, 16384], 6)
+    ns, iters, err, ok = gb.solve_batch(n, m, k, SEED, tid, alg="NIHT", tol_rel=1e-4, maxiter=800)
+    for i in range(len(n)):
+        x, xt, r = plain(gb, n[i], m[i], k[i], tid[i], 800)
+        assert (r.norms[1] <= 1e-3) == bool(ok[i]), (i, n[i], m[i], k[i], r.norms[1], err[i])
+    bytes_, ms = gb.batch_last_stats()
+    assert bytes_ > 0 and ms > 0
+
+
+def test_batch_matches_oracle(gb, gbo):
+    n, m, k, tid = pick([1024, 2048], 8)
+    ns, iters, err, ok = gb.solve_batch(n, m, k, SEED, tid, alg="NIHT", tol_rel=1e-4, maxiter=1000)
+    ok_o, it_o, err_o = gbo.solve_dense_trials(n, m, k, SEED, tid, alg="NIHT", tol_rel=1e-4, maxiter=1000)
+    assert np.sum((err_o <= 1e-3) == ok.astype(bool)) >= len(n) - 1
+
+
+def test_batch_rejects_bad_sizes(gb):
+    with pytest.raises(gb.GagaError):
+        gb.solve_batch([100], [200], [5], SEED)
+    with pytest.raises(gb.GagaError):
+        gb.solve_batch([8], [4], [1], SEED)
