@@ -135,7 +135,9 @@ gb_status alloc_work(DeviceBuffers &db, GbWork &w, int m, int n, int lda, int nu
   GB_TRY(db.alloc(&w.S, n));
   GB_TRY(db.alloc(&w.tile_cnt, (n + GB_TILE - 1) / GB_TILE));
   GB_TRY(db.alloc(&w.rec, (size_t)maxiter + 2));
-  w.part_cap = gb_dense_part_floats(lda, n);
+  gb_dense_av_shape(m, w.num_sms, &w.av_ntile, &w.av_nsplit);
+  w.part_cap = gb_dense_part_floats_av(w.av_ntile, w.av_nsplit);
+  GB_TRY(db.alloc(&w.av_tickets, w.av_ntile));
   return GB_OK;
 }
 

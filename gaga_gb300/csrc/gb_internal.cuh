@@ -103,8 +103,10 @@ struct GbWork {
   int *bins, *bins_prev, *counters;
   int *S;        // support list (n)
   int *tile_cnt; // per-tile counts for ordered compaction
-  float *part;   // dense A*v split-K partials
+  float *part;   // dense A x_S partial tiles (av_ntile * av_nsplit * 128 floats)
   size_t part_cap;
+  unsigned int *av_tickets;  // per row tile arrival counters
+  int av_ntile, av_nsplit;   // A x_S launch shape
   float *upd;    // l0 updates (n)
   float *rec;    // l0 residual record (maxiter + 1)
   GbOp op;          // dimensions here are capacities when dyn is set
@@ -227,8 +229,9 @@ void enq_A(GbWork &w, cudaStream_t s, const float *v, float *out, const float *y
 void enq_AT(GbWork &w, cudaStream_t s, const float *r, float *g, int pf);
 // dense only: g = A^T r fused with xt = g on the support, ||xt||^2 and max|g|
 void enq_AT_mask(GbWork &w, cudaStream_t s, const float *r, float *g, float *xt, int slot_sq, int slot_max, int pf);
-// dense split-K partial buffer size (floats) for an n-column operator
-size_t gb_dense_part_floats(int m_pad, int n);
+// dense A x_S launch shape for (capacity) m and its partial buffer size in floats
+void gb_dense_av_shape(int m, int num_sms, int *ntile, int *nsplit);
+size_t gb_dense_part_floats_av(int ntile, int nsplit);
 
 // solver (gb_solver.cu)
 enum { GB_RUN_SOLVE = 0, GB_RUN_L0 = 1 };

@@ -21,13 +21,9 @@
 #define DV_THREADS 512  // A x_S: 16 warps share one 128-row tile
 #define DV_ROWS 128
 #define DV_STAGE 512    // support entries staged in shared memory per pass
+#define DV_MIN_SPLIT 512  // support columns per CTA before the support is split further
 #define DA_THREADS 256  // A^T r: 8 warps, 4 columns per warp
 
-size_t gb_dense_part_floats(int m_pad, int n) {
-  (void)m_pad;
-  (void)n;
-  return 1;  // the single-pass A x_S kernel keeps no partial sums
-}
 
 // 16-byte load that does not allocate in L1 (A is streamed once per pass; r stays in L1)
 __device__ __forceinline__ float4 ld_stream4(const float *p) {
@@ -38,14 +34,17 @@ __device__ __forceinline__ float4 ld_stream4(const float *p) {
   return v;
 }
 
-// out_i = [y_i -] sum_{s < |S|} A[i, S[s]] v[S[s]]  for the 128 rows of this CTA's tile;
-// st->red[slot] = ||out||^2.  Warps take support entries w, w+16, ... of each staged
-// chunk; the 16 partial tiles are summed in warp order (deterministic).
+// out_i = [y_i -] sum_{s < |S|} A[i, S[s]] v[S[s]]; st->red[slot] = ||out||^2.
+// CTA b works on row tile b % ntile (128 rows, float4 per lane) and on split b / ntile of
+// the support; its 16 warps take entries w, w+16, ... of each staged chunk.  With more
+// than one split, each CTA publishes its partial tile and the last CTA of the tile to
+// arrive adds the partials in split order (deterministic, no second kernel).
 template <int VEC>
 __global__ void __launch_bounds__(DV_THREADS) k_dense_av(GbState *st, int pf, const float *__restrict__ A, int lda,
-                                                         int m, const int *__restrict__ S,
+                                                         int m, int ntile_cap, int nsplit, const int *__restrict__ S,
                                                          const float *__restrict__ v, const float *__restrict__ y,
-                                                         float *__restrict__ out, int slot, float *red_part,
+                                                         float *__restrict__ out, float *__restrict__ part,
+                                                         unsigned int *__restrict__ tile_tk, int slot, float *red_part,
                                                          unsigned int *tickets) {
   if (!gb_pred(st, pf)) return;
   lda = dimv(st, lda);
@@ -55,13 +54,19 @@ __global__ void __launch_bounds__(DV_THREADS) k_dense_av(GbState *st, int pf, co
   __shared__ int sj[DV_STAGE];
   __shared__ float sv[DV_STAGE];
   __shared__ float4 red[DV_THREADS / 32][32];
+  __shared__ int is_last;
   const int ntile = (m + DV_ROWS - 1) / DV_ROWS;
+  const int tile = blockIdx.x % ntile_cap, split = blockIdx.x / ntile_cap;
+  // splits actually used: at least DV_MIN_SPLIT support columns per CTA
+  nsplit = max(1, min(nsplit, (s + DV_MIN_SPLIT - 1) / DV_MIN_SPLIT));
   float acc2 = 0.0f;
-  for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+  if (tile < ntile && split < nsplit) {
     const int r0 = tile * DV_ROWS;
+    const int chunk = ((s + nsplit - 1) / nsplit + 15) & ~15;
+    const int s_lo = min(s, split * chunk), s_hi = min(s, s_lo + chunk);
     float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
-    for (int c0 = 0; c0 < s; c0 += DV_STAGE) {
-      const int cn = min(DV_STAGE, s - c0);
+    for (int c0 = s_lo; c0 < s_hi; c0 += DV_STAGE) {
+      const int cn = min(DV_STAGE, s_hi - c0);
       __syncthreads();
       for (int c = threadIdx.x; c < cn; c += DV_THREADS) {
         const int j = S[c0 + c];
@@ -97,13 +102,39 @@ __global__ void __launch_bounds__(DV_THREADS) k_dense_av(GbState *st, int pf, co
     }
     red[warp][lane] = make_float4(a0, a1, a2, a3);
     __syncthreads();
+    float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
     if (warp == 0) {
-      float4 t = red[0][lane];
+      t = red[0][lane];
 #pragma unroll
       for (int w2 = 1; w2 < DV_THREADS / 32; ++w2) {
         const float4 q = red[w2][lane];
         t.x += q.x; t.y += q.y; t.z += q.z; t.w += q.w;
       }
+    }
+    if (nsplit > 1) {
+      if (warp == 0) reinterpret_cast<float4 *>(part)[((size_t)tile * nsplit + split) * 32 + lane] = t;
+      __threadfence();
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        const unsigned int tk = atomicAdd(&tile_tk[tile], 1u);
+        is_last = (tk == (unsigned)nsplit - 1);
+      }
+      __syncthreads();
+      if (is_last && warp == 0) {
+        __threadfence();
+        const float4 *pp = reinterpret_cast<const float4 *>(part) + (size_t)tile * nsplit * 32 + lane;
+        t = __ldcg(pp);
+        for (int q = 1; q < nsplit; ++q) {
+          const float4 u = __ldcg(pp + q * 32);
+          t.x += u.x; t.y += u.y; t.z += u.z; t.w += u.w;
+        }
+        if (lane == 0) tile_tk[tile] = 0u;
+      }
+    } else if (threadIdx.x == 0) {
+      is_last = 1;
+    }
+    __syncthreads();
+    if (is_last && warp == 0) {
       const float o4[4] = {t.x, t.y, t.z, t.w};
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
@@ -115,14 +146,15 @@ __global__ void __launch_bounds__(DV_THREADS) k_dense_av(GbState *st, int pf, co
         }
       }
     }
-    __syncthreads();  // red[] is rewritten by the next tile
   }
   if (slot >= 0) grid_reduce_publish<0>(acc2, slot, st, red_part, tickets);
 }
 
-// g_j = sum_i A[i, j] r_i.  One warp owns 4 adjacent columns: every r chunk it loads
-// (from L1) feeds 4 independent A streams.  Optional fused epilogue: xt_j = g_j if
-// bin_j <= k_bin else 0, ||xt||^2 into red[slot_sq], max|g| into red[slot_max].
+// g_j = sum_i A[i, j] r_i.  A CTA owns 4 adjacent columns; its 8 warps split the rows,
+// each lane streaming 4 columns against one r chunk (16 independent 16-byte loads in
+// flight per lane with the unroll).  Warp partials are summed in warp order.  Optional
+// fused epilogue: xt_j = g_j if bin_j <= k_bin else 0, ||xt||^2 into red[slot_sq],
+// max|g| into red[slot_max].
 template <int VEC>
 __global__ void __launch_bounds__(DA_THREADS) k_dense_at(GbState *st, int pf, const float *__restrict__ A, int lda,
                                                          int m, int n, const float *__restrict__ r,
@@ -134,11 +166,11 @@ __global__ void __launch_bounds__(DA_THREADS) k_dense_at(GbState *st, int pf, co
   m = dimv(st, m);
   n = dimv(st, n);
   const int kb = st->k_bin;
-  const int lane = threadIdx.x & 31;
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nw = (gridDim.x * blockDim.x) >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int NWARP = DA_THREADS / 32;
+  __shared__ float wpart[NWARP][4];
   float s2 = 0.0f, gmax = 0.0f;
-  for (int j0 = gw * 4; j0 < n; j0 += nw * 4) {
+  for (int j0 = blockIdx.x * 4; j0 < n; j0 += gridDim.x * 4) {
     const int nc = min(4, n - j0);
     float acc[4][4];
 #pragma unroll
@@ -146,10 +178,10 @@ __global__ void __launch_bounds__(DA_THREADS) k_dense_at(GbState *st, int pf, co
     const float *col0 = A + (size_t)j0 * lda;
     if (VEC == 4) {
       const int mfull = m & ~3;
-      int i = lane * 4;
+      int i = (warp * 32 + lane) * 4;
       if (nc == 4) {
-#pragma unroll 2
-        for (; i < mfull; i += 128) {
+#pragma unroll 4
+        for (; i < mfull; i += DA_THREADS * 4) {
           const float4 b = __ldg(reinterpret_cast<const float4 *>(r + i));
           float4 q[4];
 #pragma unroll
@@ -163,7 +195,7 @@ __global__ void __launch_bounds__(DA_THREADS) k_dense_at(GbState *st, int pf, co
           }
         }
       } else {
-        for (; i < mfull; i += 128) {
+        for (; i < mfull; i += DA_THREADS * 4) {
           const float4 b = __ldg(reinterpret_cast<const float4 *>(r + i));
           for (int c = 0; c < nc; ++c) {
             const float4 q = ld_stream4(col0 + (size_t)c * lda + i);
@@ -183,7 +215,7 @@ __global__ void __launch_bounds__(DA_THREADS) k_dense_at(GbState *st, int pf, co
         }
       }
     } else {
-      for (int i = lane; i < m; i += 32) {
+      for (int i = warp * 32 + lane; i < m; i += DA_THREADS) {
         const float b = __ldg(r + i);
         for (int c = 0; c < nc; ++c) acc[c][0] = fmaf(__ldg(col0 + (size_t)c * lda + i), b, acc[c][0]);
       }
@@ -191,17 +223,24 @@ __global__ void __launch_bounds__(DA_THREADS) k_dense_at(GbState *st, int pf, co
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
       const float t = warp_sum((acc[c][0] + acc[c][1]) + (acc[c][2] + acc[c][3]));
-      if (c < nc) {
-        const int j = j0 + c;
-        if (lane == 0) g[j] = t;
-        if (xt) {
-          const float o = bins[j] <= kb ? t : 0.0f;
-          if (lane == 0) xt[j] = o;
-          if (lane == 0) s2 = fmaf(o, o, s2);
-        }
-        gmax = fmaxf(gmax, fabsf(t));
-      }
+      if (lane == 0) wpart[warp][c] = t;
     }
+    __syncthreads();
+    if (threadIdx.x < nc) {
+      const int c = threadIdx.x;
+      float t = wpart[0][c];
+#pragma unroll
+      for (int w2 = 1; w2 < NWARP; ++w2) t += wpart[w2][c];
+      const int j = j0 + c;
+      g[j] = t;
+      if (xt) {
+        const float o = bins[j] <= kb ? t : 0.0f;
+        xt[j] = o;
+        s2 = fmaf(o, o, s2);
+      }
+      gmax = fmaxf(gmax, fabsf(t));
+    }
+    __syncthreads();
   }
   if (slot_sq >= 0) grid_reduce_publish<0>(s2, slot_sq, st, red_part, tickets);
   if (slot_max >= 0) grid_reduce_publish<1>(gmax, slot_max, st, red_part, tickets);
@@ -401,21 +440,28 @@ static void launch_fft(GbWork &w, cudaStream_t s, int pf, int pass, const float 
                                                                   cin, cout, rout);
 }
 
-static int dense_av_grid(const GbWork &w) {
-  const int tiles = (w.op.m + DV_ROWS - 1) / DV_ROWS;
-  return tiles < GB_MAXRB ? tiles : GB_MAXRB;
+// A x_S launch shape: row tiles of the (capacity) m times support splits, <= GB_MAXRB CTAs
+void gb_dense_av_shape(int m, int num_sms, int *ntile, int *nsplit) {
+  int t = (m + DV_ROWS - 1) / DV_ROWS;
+  if (t > GB_MAXRB) t = GB_MAXRB;
+  int sp = (4 * num_sms + t - 1) / t;
+  sp = std::max(1, std::min(sp, std::min(16, GB_MAXRB / t)));
+  *ntile = t;
+  *nsplit = sp;
 }
+
+size_t gb_dense_part_floats_av(int ntile, int nsplit) { return (size_t)ntile * nsplit * DV_ROWS; }
 
 void enq_A(GbWork &w, cudaStream_t s, const float *v, float *out, const float *y, int slot, int pf) {
   const GbOp &op = w.op;
   if (op.kind == GB_OP_DENSE) {
-    const int grid = dense_av_grid(w);
+    const int grid = w.av_ntile * w.av_nsplit;
     if (op.vec4)
-      k_dense_av<4><<<grid, DV_THREADS, 0, s>>>(w.st, pf, op.A, argLDA(w), argM(w), w.S, v, y, out, slot, w.red_part,
-                                                 w.tickets);
+      k_dense_av<4><<<grid, DV_THREADS, 0, s>>>(w.st, pf, op.A, argLDA(w), argM(w), w.av_ntile, w.av_nsplit, w.S, v,
+                                                 y, out, w.part, w.av_tickets, slot, w.red_part, w.tickets);
     else
-      k_dense_av<1><<<grid, DV_THREADS, 0, s>>>(w.st, pf, op.A, argLDA(w), argM(w), w.S, v, y, out, slot, w.red_part,
-                                                 w.tickets);
+      k_dense_av<1><<<grid, DV_THREADS, 0, s>>>(w.st, pf, op.A, argLDA(w), argM(w), w.av_ntile, w.av_nsplit, w.S, v,
+                                                 y, out, w.part, w.av_tickets, slot, w.red_part, w.tickets);
   } else if (op.kind == GB_OP_DCT) {
     launch_fft<0, LOAD_MAKHOUL, STORE_CPLX_T>(w, s, pf, 1, v, nullptr, op.cbuf0, nullptr);
     launch_fft<0, LOAD_CPLX, STORE_CPLX_NAT>(w, s, pf, 2, nullptr, op.cbuf0, op.cbuf1, nullptr);
@@ -428,8 +474,8 @@ void enq_A(GbWork &w, cudaStream_t s, const float *v, float *out, const float *y
 }
 
 static int dense_at_grid(const GbWork &w) {
-  // 8 warps per block, 4 columns per warp
-  const int blocks = (w.op.n + 31) / 32;
+  // one CTA per group of 4 columns (grid-stride beyond the cap)
+  const int blocks = (w.op.n + 3) / 4;
   const int cap = std::min(GB_MAXRB, w.wide_blocks);
   return blocks < cap ? blocks : cap;
 }
