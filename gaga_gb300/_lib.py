@@ -20,7 +20,8 @@ GB_ALG_NIHT, GB_ALG_HTP, GB_ALG_CGIHT, GB_ALG_PARALLEL_L0 = 0, 1, 6, 14
 # every symbol include/gb_cs.h declares
 EXPORTS = ["gb_cs_version", "gb_cs_last_error", "gb_cs_default_options", "gb_cs_alg_id", "gb_cs_solve",
            "gb_cs_generate_and_solve", "gb_cs_linear_binning", "gb_cs_find_support_set",
-           "gb_cs_operator_apply", "gb_cs_l0_step", "gb_cs_solve_batch", "gb_cs_batch_last_stats"]
+           "gb_cs_operator_apply", "gb_cs_l0_step", "gb_cs_solve_batch", "gb_cs_batch_last_stats",
+           "gb_cs_dense_apply_noalloc"]
 
 
 class Options(C.Structure):
@@ -89,6 +90,8 @@ def load():
     L.gb_cs_solve_batch.restype = i
     L.gb_cs_batch_last_stats.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_float)]
     L.gb_cs_batch_last_stats.restype = None
+    L.gb_cs_dense_apply_noalloc.argtypes = [vp, i, i, i, i, vp, vp, vp]
+    L.gb_cs_dense_apply_noalloc.restype = i
     _lib = L
     return L
 

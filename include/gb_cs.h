@@ -147,6 +147,18 @@ gb_status gb_cs_find_support_set(float *d_v, int n, int k, float slope, float in
  * p->location must be GB_DEVICE; y/k are ignored. */
 gb_status gb_cs_operator_apply(const gb_problem *p, int transpose, const float *d_in, float *d_out);
 
+/* Dense operator apply that allocates nothing (no counterpart in the reference): out = A in
+ * (transpose 0, in has n entries, out m) or A^T in (transpose 1), A column-major m x n with
+ * leading dimension lda, every pointer on the device; asynchronous on `stream`.  For
+ * callers that cannot allocate device memory during the call: code inside a CUDA stream
+ * capture, services that budget every allocation up front, embedders with their own
+ * allocator.  Its scratch is one fixed 1 MiB device array per GPU held until the process
+ * exits; m and n must be <= 65536 (GB_BAD_ARG otherwise).  The first call on a device
+ * resolves the array's address and must happen outside a stream capture.  All calls share
+ * the array: calls that overlap on the GPU race and must be serialised by the caller. */
+gb_status gb_cs_dense_apply_noalloc(const float *d_A, int lda, int m, int n, int transpose,
+                                    const float *d_in, float *d_out, void *stream);
+
 /* One parallel_l0 iteration body (cuda_compute_scores_l0 + cuda_update_residual,
  * GAGA/gaga/expander/kernels.cu:3-14,353-388) on column-grouped 0-based rows.
  * Returns the candidate flag in *found. */
