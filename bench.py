@@ -172,8 +172,10 @@ def bench_ours(args):
         return ns, wall, kms, nbytes, len(n), iters
 
     # warm-up waves
+    from gaga_gb300 import sweep
+
     for s in range(args.warmup):
-        solve_wave(rank + world * s)
+        solve_wave(sweep.rank_wave(rank, world, s))
     sampler = ClockSampler(local)
     if world > 1:
         torch.distributed.barrier()
@@ -184,7 +186,7 @@ def bench_ours(args):
     tot_wall = tot_kms = tot_bytes = 0.0
     launches = 0
     for s in range(args.steps):
-        w = rank + world * (args.warmup + s)
+        w = sweep.rank_wave(rank, world, args.warmup + s)
         ns, wall, kms, nbytes, cnt, _ = solve_wave(w)
         tot_ok += ns
         tot_trials += cnt
@@ -215,15 +217,18 @@ def bench_ours(args):
             "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded Philox Gaussian trials drawn on device)",
             "config": {"workload": "dense phase-transition sweep (4096 trials, n 1024-16384, delta 0.1-0.9, "
                                    "rho 0.02-0.5), NIHT tol 1e-4*||y||, one 256-trial wave per step per GPU",
-                       "form": "tuned: batched persistent cluster kernel",
+                       "form": "tuned: batched slot graphs (device trial queue, device generation)",
                        "trials_per_step": int(tot_trials // max(1, args.steps)), "l2": "working set >> L2 (A up to "
                                                                                          "966 MB per trial)"},
             "recovered": int(tot_ok), "trials": int(tot_trials),
             "e2e": {"value": e2e, "unit": "trials/s", "h2d_bytes_per_step": 16 * 256, "d2h_bytes_per_step": 12 * 256},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "kernel": "k_batch",
-                         "peak_source": peak_kind},
+            "batched_matvec_bytes_per_s": {"achieved": achieved, "unit": "GB/s", "frac": achieved / peak,
+                                           "what": "algorithmic dense operator bytes of all trials / device time of "
+                                                   "the whole batched form (generation and control included)"},
             "gpu_launches": launches, "clocks": clocks}
+    mv = matvec_roofline(peak, peak_kind)
+    line["roofline"] = mv["at"]
+    line["matvec"] = mv
     if args.plain_trials > 0 and world == 1:
         line["plain"] = bench_plain(args)
         line["tuned_vs_plain"] = value / line["plain"]["value"] if line["plain"]["value"] else None
@@ -232,6 +237,51 @@ def bench_ours(args):
     print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def matvec_roofline(peak, peak_kind, m=14746, n=16384, k=5000, reps=20):
+    """Dense A^T r (k_dense_at, the dominant kernel) and A x_S (k_dense_av) on the sweep's
+    largest trial shape, timed with CUDA events on the stream they run on."""
+    import ctypes as C
+
+    import torch
+
+    import gaga_gb300 as gb
+
+    L = gb._lib.load()
+    g = torch.Generator(device="cuda").manual_seed(1)
+    lda = (m + 31) // 32 * 32  # the library's own layout: 128-byte aligned columns
+    A = torch.randn(n * lda, device="cuda", generator=g) / np.sqrt(m)  # column-major
+    r = torch.randn(m, device="cuda", generator=g)
+    x = torch.zeros(n, device="cuda")
+    x[torch.randperm(n, device="cuda", generator=g)[:k]] = 1.0
+    g_out, y_out = torch.empty(n, device="cuda"), torch.empty(m, device="cuda")
+    s = torch.cuda.Stream()
+    res = {}
+    for name, tr, vin, vout, nbytes in (("at", 1, r, g_out, 4.0 * m * n + 4 * m + 4 * n),
+                                        ("av", 0, x, y_out, 4.0 * m * k + 8 * k + 4 * m)):
+        with torch.cuda.stream(s):
+            for _ in range(3):
+                L.gb_cs_dense_apply_noalloc(A.data_ptr(), lda, m, n, tr, vin.data_ptr(), vout.data_ptr(),
+                                            C.c_void_p(s.cuda_stream))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.synchronize()
+            e0.record(s)
+            for _ in range(reps):
+                L.gb_cs_dense_apply_noalloc(A.data_ptr(), lda, m, n, tr, vin.data_ptr(), vout.data_ptr(),
+                                            C.c_void_p(s.cuda_stream))
+            e1.record(s)
+        e1.synchronize()
+        t = e0.elapsed_time(e1) / 1e3 / reps
+        ach = nbytes / t / 1e9
+        res[name] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                     "traffic": None, "kernel": "k_dense_at" if name == "at" else "k_dense_av (+ support compaction)",
+                     "shape": "m=%d n=%d lda=%d%s, A %.0f MB > L2" % (m, n, lda, "" if name == "at" else
+                                                                      " |S|=%d" % k, 4.0 * m * n / 1e6),
+                     "us_per_launch": t * 1e6, "peak_source": peak_kind}
+    del A
+    torch.cuda.empty_cache()
+    return res
 
 
 def bench_plain(args):

@@ -38,6 +38,11 @@ def wave(total, waves, w):
 
 
 def shard(indices, rank, world):
-    """Trials of one rank: contiguous, balanced by estimated cost (m*n)."""
+    """Trials of one rank: every world-th index starting at rank."""
     indices = np.asarray(indices)
     return indices[rank::world]
+
+
+def rank_wave(rank, world, step):
+    """Wave solved by `rank` at global step `step` (weak scaling: every rank its own wave)."""
+    return rank + world * step
