@@ -268,3 +268,55 @@ def batch_last_stats():
     b, t = C.c_double(0), C.c_float(0)
     L.gb_cs_batch_last_stats(C.byref(b), C.byref(t))
     return b.value, t.value
+
+
+def solve_shared_batch(m, n, k, seed, tol_rel=1e-4, maxiter=5000, outputs=False, stream=None):
+    """Shared-matrix batched form (gb_cs_solve_shared_batch): len(k) NIHT trials with one
+    dense Gaussian A, operator work as BF16 tensor-core GEMMs, FP64 debias.
+
+    Returns (num_success, iters, rel_err, ok) and, with outputs=True, also the generated
+    A (m x n column-major, as an (n, m) CUDA tensor), Y (T x m) and X0 (T x n) on the device.
+    """
+    L = _lib.load()
+    k = np.ascontiguousarray(k, dtype=np.int32)
+    T = len(k)
+    A = Y = X0 = None
+    if outputs:
+        import torch
+        A = torch.empty((n, m), dtype=torch.float32, device="cuda")
+        Y = torch.empty((T, m), dtype=torch.float32, device="cuda")
+        X0 = torch.empty((T, n), dtype=torch.float32, device="cuda")
+    b = _lib.SharedBatch(T, int(m), int(n), k.ctypes.data, int(seed) & 0xFFFFFFFF, float(tol_rel), int(maxiter),
+                         None if A is None else A.data_ptr(), None if Y is None else Y.data_ptr(),
+                         None if X0 is None else X0.data_ptr(), stream)
+    iters = np.zeros(T, dtype=np.int32)
+    err = np.zeros(T, dtype=np.float32)
+    ok = np.zeros(T, dtype=np.int32)
+    ns = C.c_int(0)
+    _lib.check(L.gb_cs_solve_shared_batch(C.byref(b), C.c_void_p(iters.ctypes.data), C.c_void_p(err.ctypes.data),
+                                          C.c_void_p(ok.ctypes.data), C.byref(ns)))
+    if outputs:
+        return ns.value, iters, err, ok, A, Y, X0
+    return ns.value, iters, err, ok
+
+
+def shared_last_stats():
+    """(GEMM FLOPs, device ms) of the last solve_shared_batch call."""
+    L = _lib.load()
+    fl, t = C.c_double(0), C.c_float(0)
+    L.gb_cs_shared_last_stats(C.byref(fl), C.byref(t))
+    return fl.value, t.value
+
+
+def gemm_bf16_tn(A, B, Y=None, want_bf16=False):
+    """Ct = [Y -] (A B^T)^T for BF16 CUDA tensors A (M x K), B (N x K); returns (Ct, Cb)."""
+    import torch
+    L = _lib.load()
+    M, K = A.shape
+    N = B.shape[0]
+    Ct = torch.empty((N, M), dtype=torch.float32, device=A.device)
+    Cb = torch.empty((N, M), dtype=torch.bfloat16, device=A.device) if want_bf16 else None
+    _lib.check(L.gb_cs_gemm_bf16_tn(A.data_ptr(), B.data_ptr(), Ct.data_ptr(), M, N, K,
+                                    None if Y is None else Y.data_ptr(), None if Cb is None else Cb.data_ptr(),
+                                    torch.cuda.current_stream().cuda_stream))
+    return Ct, Cb

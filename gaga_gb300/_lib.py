@@ -21,7 +21,8 @@ GB_ALG_NIHT, GB_ALG_HTP, GB_ALG_CGIHT, GB_ALG_PARALLEL_L0 = 0, 1, 6, 14
 EXPORTS = ["gb_cs_version", "gb_cs_last_error", "gb_cs_default_options", "gb_cs_alg_id", "gb_cs_solve",
            "gb_cs_generate_and_solve", "gb_cs_linear_binning", "gb_cs_find_support_set",
            "gb_cs_operator_apply", "gb_cs_l0_step", "gb_cs_solve_batch", "gb_cs_batch_last_stats",
-           "gb_cs_dense_apply_noalloc"]
+           "gb_cs_dense_apply_noalloc", "gb_cs_solve_shared_batch", "gb_cs_shared_last_stats",
+           "gb_cs_gemm_bf16_tn"]
 
 
 class Options(C.Structure):
@@ -54,6 +55,12 @@ class Batch(C.Structure):
     _fields_ = [("ntrials", C.c_int), ("n", C.c_void_p), ("m", C.c_void_p), ("k", C.c_void_p),
                 ("trial_id", C.c_void_p), ("seed", C.c_uint), ("alg", C.c_int), ("tol_rel", C.c_float),
                 ("maxiter", C.c_int), ("use_learned", C.c_int), ("stream", C.c_void_p)]
+
+
+class SharedBatch(C.Structure):
+    _fields_ = [("ntrials", C.c_int), ("m", C.c_int), ("n", C.c_int), ("k", C.c_void_p), ("seed", C.c_uint),
+                ("tol_rel", C.c_float), ("maxiter", C.c_int), ("d_A_out", C.c_void_p), ("d_Y_out", C.c_void_p),
+                ("d_X0_out", C.c_void_p), ("stream", C.c_void_p)]
 
 
 _lib = None
@@ -92,6 +99,12 @@ def load():
     L.gb_cs_batch_last_stats.restype = None
     L.gb_cs_dense_apply_noalloc.argtypes = [vp, i, i, i, i, vp, vp, vp]
     L.gb_cs_dense_apply_noalloc.restype = i
+    L.gb_cs_solve_shared_batch.argtypes = [C.POINTER(SharedBatch), vp, vp, vp, C.POINTER(C.c_int)]
+    L.gb_cs_solve_shared_batch.restype = i
+    L.gb_cs_shared_last_stats.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_float)]
+    L.gb_cs_shared_last_stats.restype = None
+    L.gb_cs_gemm_bf16_tn.argtypes = [vp, vp, vp, i, i, i, vp, vp, vp]
+    L.gb_cs_gemm_bf16_tn.restype = i
     _lib = L
     return L
 

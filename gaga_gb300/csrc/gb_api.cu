@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "gb_internal.cuh"
+#include "gb_philox.cuh"
 
 gb_status gb_ops_init_attributes();
 
@@ -356,58 +357,19 @@ extern "C" gb_status gb_cs_solve(const char *alg, const gb_problem *p, const gb_
 }
 
 // ------------------------------------------------------------------ problem generation
-// Philox-4x32-10 counter generator shared with the problem description (streams keyed by
-// (seed, trial, stream id)); the reference's cuRAND streams are not reproducible.
+// problem generation: Philox-4x32-10 streams (gb_philox.cuh)
 namespace {
-enum { ST_MATRIX = 1, ST_VALUES = 2, ST_SUPPORT = 3, ST_ROWS = 4, ST_SMV = 5, ST_SIGNS = 6, ST_NOISE = 7 };
-const uint32_t KEY_HI = 0x6A09E667u;
+using gbgen::KEY_HI;
+using gbgen::philox;
+using gbgen::u01;
+enum { ST_MATRIX = gbgen::ST_MATRIX, ST_VALUES = gbgen::ST_VALUES, ST_SUPPORT = gbgen::ST_SUPPORT,
+       ST_ROWS = gbgen::ST_ROWS, ST_SMV = gbgen::ST_SMV, ST_SIGNS = gbgen::ST_SIGNS, ST_NOISE = gbgen::ST_NOISE };
 
-__host__ __device__ inline void philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1,
-                                       uint32_t out[4]) {
-  for (int r = 0; r < 10; ++r) {
-    uint64_t p0 = (uint64_t)0xD2511F53u * c0;
-    uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
-    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
-    uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
-    uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
-    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
-    k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
-  }
-  out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
-}
-__host__ __device__ inline float u01(uint32_t x) { return ((float)(x >> 8) + 0.5f) * (1.0f / 16777216.0f); }
-
-// dense A entries N(0,1)/sqrt(m) (ens 1) or +-1/sqrt(m) (ens 2), column-major with lda.
-// Element e = j*m + i is lane e%4 of Philox block e/4 (one block gives 4 normals by two
-// Box-Muller pairs); each lane draws one block and writes its entries inside column j.
+// dense A, column-major with lda: one warp per column (gbgen::gen_dense_column)
 __global__ void k_gen_dense(float *A, int m, int n, int lda, int ens, uint32_t seed, uint32_t trial) {
-  const float scale = 1.0f / sqrtf((float)m);
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-  for (int j = gw; j < n; j += nw) {
-    const uint64_t e0 = (uint64_t)j * (uint64_t)m, e1 = e0 + (uint64_t)m;
-    float *col = A + (size_t)j * lda;
-    for (uint64_t g = (e0 >> 2) + lane; g < ((e1 + 3) >> 2); g += 32) {
-      uint32_t o[4];
-      philox((uint32_t)g, (uint32_t)(g >> 32), ST_MATRIX, trial, seed, KEY_HI, o);
-      float v[4];
-      if (ens == 2) {
-        for (int t = 0; t < 4; ++t) v[t] = signbit(u01(o[t]) - 0.5f) ? -1.0f : 1.0f;
-      } else {
-        for (int t = 0; t < 2; ++t) {
-          const float r = sqrtf(-2.0f * logf(u01(o[2 * t])));
-          float sn, cs;
-          sincospif(2.0f * u01(o[2 * t + 1]), &sn, &cs);
-          v[2 * t] = r * cs;
-          v[2 * t + 1] = r * sn;
-        }
-      }
-      for (int t = 0; t < 4; ++t) {
-        const uint64_t e = g * 4 + t;
-        if (e >= e0 && e < e1) col[e - e0] = v[t] * scale;
-      }
-    }
-  }
+  for (int j = gw; j < n; j += nw) gbgen::gen_dense_column(A + (size_t)j * lda, j, m, seed, trial, ens, lane, 32);
 }
 
 float h_uniform(uint32_t seed, uint32_t trial, uint32_t stream, uint64_t e) {

@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "gb_internal.cuh"
+#include "gb_philox.cuh"
 
 __global__ void k_hist(const GbState *st, int pf, const float *__restrict__ v, int *__restrict__ bins,
                        int *__restrict__ bins_prev, int *__restrict__ counters, int n);
@@ -50,22 +51,13 @@ struct BatchParams {
   double *bytes;
 };
 
-const uint32_t KEY_HI = 0x6A09E667u;
-enum { ST_MATRIX = 1, ST_VALUES = 2, ST_SUPPORT = 3 };
-
+using gbgen::KEY_HI;
+enum { ST_MATRIX = gbgen::ST_MATRIX, ST_VALUES = gbgen::ST_VALUES, ST_SUPPORT = gbgen::ST_SUPPORT };
 __device__ __forceinline__ void philox_d(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0,
                                          uint32_t k1, uint32_t out[4]) {
-#pragma unroll
-  for (int r = 0; r < 10; ++r) {
-    const uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
-    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
-    const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
-    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
-    k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
-  }
-  out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+  gbgen::philox(c0, c1, c2, c3, k0, k1, out);
 }
-__device__ __forceinline__ float u01d(uint32_t x) { return ((float)(x >> 8) + 0.5f) * (1.0f / 16777216.0f); }
+__device__ __forceinline__ float u01d(uint32_t x) { return gbgen::u01(x); }
 
 __device__ __forceinline__ uint32_t trial_key(const BatchParams *bp, const GbState *st) {
   return bp->seed + (bp->tid ? bp->tid[st->trial] : (uint32_t)st->trial);
@@ -106,29 +98,9 @@ __global__ void k_b_gen_A(const GbState *st, const BatchParams *bp, float *A) {
   if (!st->active) return;
   const int m = st->m, n = st->n, lda = st->lda;
   const uint32_t key = trial_key(bp, st);
-  const float scale = 1.0f / sqrtf((float)m);
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-  for (int j = gw; j < n; j += nw) {
-    const uint64_t e0 = (uint64_t)j * (uint64_t)m, e1 = e0 + (uint64_t)m;
-    float *col = A + (size_t)j * lda;
-    for (uint64_t g = (e0 >> 2) + lane; g < ((e1 + 3) >> 2); g += 32) {
-      uint32_t o[4];
-      philox_d((uint32_t)g, (uint32_t)(g >> 32), ST_MATRIX, 0u, key, KEY_HI, o);
-      float v[4];
-      for (int t = 0; t < 2; ++t) {
-        const float r = sqrtf(-2.0f * logf(u01d(o[2 * t])));
-        float sn, cs;
-        sincospif(2.0f * u01d(o[2 * t + 1]), &sn, &cs);
-        v[2 * t] = r * cs;
-        v[2 * t + 1] = r * sn;
-      }
-      for (int t = 0; t < 4; ++t) {
-        const uint64_t e = g * 4 + t;
-        if (e >= e0 && e < e1) col[e - e0] = v[t] * scale;
-      }
-    }
-  }
+  for (int j = gw; j < n; j += nw) gbgen::gen_dense_column(A + (size_t)j * lda, j, m, key, 0u, 1, lane, 32);
 }
 
 // x0 values (+-1) and support keys of createVector (GAGA/gaga/createVector.cu:207-300);

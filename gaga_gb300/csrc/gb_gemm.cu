@@ -1,0 +1,161 @@
+// gb_gemm.cu -- BF16 "TN" GEMM with FP32 accumulation for the shared-matrix batched form.
+//
+//     Ct[N x M] = [Y -] (A[M x K] . B[N x K]^T)^T
+//
+// A and B are K-major (row-major with K contiguous), the output is written transposed
+// (one contiguous vector of M values per column n = per trial), optionally as Y - A B^T
+// and optionally also as BF16.  In the shared-matrix form A is the measurement matrix
+// (or its transpose) and B holds one trial's vector per row.
+//
+// This file holds the warp-level tensor-core kernel (mma.sync m16n8k16, 3-stage cp.async
+// pipeline, 128x128x32 CTA tile).  It is the correctness baseline that the tcgen05 kernel
+// (gb_gemm_tc.cu) is validated against.
+#include <cuda_bf16.h>
+
+#include "gb_internal.cuh"
+
+#define GT_M 128
+#define GT_N 128
+#define GT_K 32
+#define GT_STAGES 3
+#define GT_LD (GT_K + 8)  // padded row (halves) to avoid ldmatrix bank conflicts
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N));
+}
+
+__device__ __forceinline__ void ldmatrix_x4(unsigned &r0, unsigned &r1, unsigned &r2, unsigned &r3, const void *p) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "r"(s));
+}
+
+__device__ __forceinline__ void mma_bf16(float *d, const unsigned *a, const unsigned *b) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// M % 128 == 0, N % 128 == 0, K % 32 == 0 (the caller pads)
+__global__ void __launch_bounds__(256) k_gemm_tn_mma(const __nv_bfloat16 *__restrict__ A,
+                                                     const __nv_bfloat16 *__restrict__ B, float *__restrict__ Ct,
+                                                     int M, int N, int K, int lda, int ldb,
+                                                     const float *__restrict__ Y, __nv_bfloat16 *__restrict__ Cb) {
+  extern __shared__ __align__(16) __nv_bfloat16 gsm[];
+  __nv_bfloat16 *As = gsm;                                  // [stage][128][GT_LD]
+  __nv_bfloat16 *Bs = gsm + GT_STAGES * GT_M * GT_LD;       // [stage][128][GT_LD]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int wm = warp >> 2, wn = warp & 3;  // 2 x 4 warps, warp tile 64 x 32
+  const int m0 = blockIdx.x * GT_M, n0 = blockIdx.y * GT_N;
+  const int nk = K / GT_K;
+  float acc[4][4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j][0] = acc[i][j][1] = acc[i][j][2] = acc[i][j][3] = 0.0f;
+
+  auto load_stage = [&](int st, int kt) {
+    const int k0 = kt * GT_K;
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      const int q = tid + c * 256;  // 512 chunks of 16 bytes per operand
+      const int row = q >> 2, col = (q & 3) * 8;
+      cp_async16(As + (st * GT_M + row) * GT_LD + col, A + (size_t)(m0 + row) * lda + k0 + col);
+      cp_async16(Bs + (st * GT_N + row) * GT_LD + col, B + (size_t)(n0 + row) * ldb + k0 + col);
+    }
+  };
+
+  for (int s = 0; s < GT_STAGES - 1; ++s) {
+    if (s < nk) load_stage(s, s);
+    cp_async_commit();
+  }
+  for (int kt = 0; kt < nk; ++kt) {
+    cp_async_wait<GT_STAGES - 2>();
+    __syncthreads();
+    const int nxt = kt + GT_STAGES - 1;
+    if (nxt < nk) load_stage(nxt % GT_STAGES, nxt);
+    cp_async_commit();
+    const int st = kt % GT_STAGES;
+    const __nv_bfloat16 *as = As + st * GT_M * GT_LD;
+    const __nv_bfloat16 *bs = Bs + st * GT_N * GT_LD;
+#pragma unroll
+    for (int kk = 0; kk < GT_K; kk += 16) {
+      unsigned af[4][4], bf[4][2];
+#pragma unroll
+      for (int mi = 0; mi < 4; ++mi) {
+        const int r = wm * 64 + mi * 16 + (lane & 15);
+        const int c = kk + (lane >> 4) * 8;
+        ldmatrix_x4(af[mi][0], af[mi][1], af[mi][2], af[mi][3], as + r * GT_LD + c);
+      }
+#pragma unroll
+      for (int nj = 0; nj < 2; ++nj) {
+        const int r = wn * 32 + nj * 16 + (lane & 7) + ((lane >> 4) << 3);
+        const int c = kk + ((lane >> 3) & 1) * 8;
+        unsigned r0, r1, r2, r3;
+        ldmatrix_x4(r0, r1, r2, r3, bs + r * GT_LD + c);
+        bf[2 * nj][0] = r0;
+        bf[2 * nj][1] = r1;
+        bf[2 * nj + 1][0] = r2;
+        bf[2 * nj + 1][1] = r3;
+      }
+#pragma unroll
+      for (int mi = 0; mi < 4; ++mi)
+#pragma unroll
+        for (int ni = 0; ni < 4; ++ni) mma_bf16(acc[mi][ni], af[mi], bf[ni]);
+    }
+  }
+  cp_async_wait<0>();
+  // epilogue: element (row, col) of C goes to Ct[col * M + row]
+  const int g = lane >> 2, tq = lane & 3;
+#pragma unroll
+  for (int mi = 0; mi < 4; ++mi)
+#pragma unroll
+    for (int ni = 0; ni < 4; ++ni)
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int row = m0 + wm * 64 + mi * 16 + g + (e >> 1) * 8;
+        const int col = n0 + wn * 32 + ni * 8 + tq * 2 + (e & 1);
+        const size_t o = (size_t)col * M + row;
+        const float v = Y ? Y[o] - acc[mi][ni][e] : acc[mi][ni][e];
+        Ct[o] = v;
+        if (Cb) Cb[o] = __float2bfloat16_rn(v);
+      }
+}
+
+gb_status gb_gemm_tn(const void *A, const void *B, float *Ct, int M, int N, int K, int lda, int ldb, const float *Y,
+                     void *Cb, cudaStream_t s) {
+  if (M % GT_M || N % GT_N || K % GT_K || M <= 0 || N <= 0 || K <= 0 || lda < K || ldb < K || lda % 8 || ldb % 8) {
+    gb_set_error_message("GEMM sizes must be multiples of 128 (M, N) and 32 (K); strides multiples of 8", __FILE__,
+                         __LINE__);
+    return GB_BAD_ARG;
+  }
+  const int smem = GT_STAGES * (GT_M + GT_N) * GT_LD * 2;
+  static bool attr = false;
+  if (!attr) {
+    GB_CUDA_TRY(cudaFuncSetAttribute(k_gemm_tn_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    attr = true;
+  }
+  dim3 grid(M / GT_M, N / GT_N);
+  k_gemm_tn_mma<<<grid, 256, smem, s>>>((const __nv_bfloat16 *)A, (const __nv_bfloat16 *)B, Ct, M, N, K, lda, ldb,
+                                        Y, (__nv_bfloat16 *)Cb);
+  GB_CUDA_TRY(cudaGetLastError());
+  return GB_OK;
+}
+
+extern "C" gb_status gb_cs_gemm_bf16_tn(const void *d_A, const void *d_B, float *d_Ct, int M, int N, int K,
+                                        const float *d_Y, void *d_Cb, void *stream) {
+  if (!d_A || !d_B || !d_Ct) {
+    gb_set_error_message("gb_cs_gemm_bf16_tn: null buffer", __FILE__, __LINE__);
+    return GB_BAD_ARG;
+  }
+  return gb_gemm_tn(d_A, d_B, d_Ct, M, N, K, K, K, d_Y, d_Cb, (cudaStream_t)stream);
+}

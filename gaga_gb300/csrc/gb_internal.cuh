@@ -233,6 +233,10 @@ void enq_AT_mask(GbWork &w, cudaStream_t s, const float *r, float *g, float *xt,
 void gb_dense_av_shape(int m, int num_sms, int *ntile, int *nsplit);
 size_t gb_dense_part_floats_av(int ntile, int nsplit);
 
+// BF16 TN GEMM (gb_gemm.cu): Ct[N x M] = [Y -] (A[M x K] B[N x K]^T)^T, row strides lda, ldb
+gb_status gb_gemm_tn(const void *A, const void *B, float *Ct, int M, int N, int K, int lda, int ldb, const float *Y,
+                     void *Cb, cudaStream_t s);
+
 // solver (gb_solver.cu)
 enum { GB_RUN_SOLVE = 0, GB_RUN_L0 = 1 };
 gb_status gb_run_solver(GbWork &w, int alg, const gb_options &o, int k, cudaStream_t s, float tol_abs);

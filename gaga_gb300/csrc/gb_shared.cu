@@ -1,0 +1,695 @@
+// gb_shared.cu -- batched form for trials that share one dense A (BF16 tensor-core GEMMs).
+//
+// T trials y_t = A x0_t with the same Gaussian A run NIHT in lockstep.  The operator
+// applications of all trials become three GEMMs per iteration (gb_gemm.cu):
+//
+//   R  = Y - [A_hi | A_lo | A_hi] . [X_hi ; X_hi ; X_lo]   residual, ~FP32 accurate:
+//        A and X are split into BF16 high and low parts, the A_lo X_lo term is dropped
+//   G  = A_hi^T . bf16(R)                                  gradients
+//   Q  = A_hi . bf16(x_thres)                              step-size products
+//
+// with FP32 accumulation.  Everything else of an iteration -- the reference's scalar
+// logic (gb_ctrl.cuh), the restriction to the support, the update, LinearBinning and the
+// k-th bin -- runs in one CTA per trial.  The loop is a CUDA graph WHILE node that runs
+// while any trial is active.  Trials that stop with ||y - A x|| <= tol are then debiased:
+// least squares on their final support by conjugate gradients on the normal equations in
+// FP64 with the FP32 A.  The verdict is the relative l2 error against the planted x0.
+//
+// The shared A is drawn from `seed` exactly as gb_cs_generate_and_solve draws it; trial
+// t's x0 uses the key seed + 1 + t.
+#include <cuda_bf16.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "gb_ctrl.cuh"
+#include "gb_philox.cuh"
+
+#define SH_THREADS 256
+#define SH_NBINS_MAX 1640  // num_bins = max(n/20, 1000) <= 1638 for n <= 32768
+
+namespace {
+
+struct ShDev {
+  int m, n, T, Tp, maxiter;
+  float tol_rel;
+  unsigned int seed;
+  const int *kreq;
+  float *A32;               // m x n column-major (lda = m)
+  __nv_bfloat16 *Acat;      // m x 3n row-major: [A_hi | A_lo | A_hi]
+  __nv_bfloat16 *AThi;      // n x m row-major (A column-major) in BF16
+  float *X0, *X, *G, *Y, *R, *Q;
+  __nv_bfloat16 *Xcat, *XTbf, *Rbf;  // Tp x 3n, Tp x n, Tp x m
+  int *bins;
+  GbState *st;
+  double *scr;              // debias scratch, Tp x (3n + 2m)
+  int *iters;
+  float *err;
+  int *ok;
+};
+
+// ------------------------------------------------------------------ operands
+__global__ void k_sh_genA(float *A32, int m, int n, uint32_t seed) {
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  for (int j = gw; j < n; j += nw) gbgen::gen_dense_column(A32 + (size_t)j * m, j, m, seed, 0u, 1, lane, 32);
+}
+
+// BF16 operands: AThi (column-major A in BF16) and Acat rows [hi | lo | hi] through a
+// 32x32 shared-memory transpose
+__global__ void k_sh_split(const float *__restrict__ A32, __nv_bfloat16 *__restrict__ Acat,
+                           __nv_bfloat16 *__restrict__ AThi, int m, int n) {
+  __shared__ float tile[32][33];
+  const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    const int j = j0 + r, i = i0 + threadIdx.x;
+    const float v = A32[(size_t)j * m + i];
+    tile[r][threadIdx.x] = v;
+    AThi[(size_t)j * m + i] = __float2bfloat16_rn(v);
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    const int i = i0 + r, j = j0 + threadIdx.x;
+    const float v = tile[threadIdx.x][r];
+    const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+    const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
+    const size_t row = (size_t)i * 3 * n;
+    Acat[row + j] = hi;
+    Acat[row + n + j] = lo;
+    Acat[row + 2 * n + j] = hi;
+  }
+}
+
+// ------------------------------------------------------------------ CTA helpers
+__device__ float cta_sum(float v, float *sm) {
+  v = warp_sum(v);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+  __syncthreads();
+  float t = 0.0f;
+  for (int w = 0; w < SH_THREADS / 32; ++w) t += sm[w];
+  return t;
+}
+__device__ float cta_max(float v, float *sm) {
+  v = warp_max(v);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+  __syncthreads();
+  float t = 0.0f;
+  for (int w = 0; w < SH_THREADS / 32; ++w) t = fmaxf(t, sm[w]);
+  return t;
+}
+__device__ double cta_sumd(double v, double *sm) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int w = 0; w < SH_THREADS / 32; ++w) t += sm[w];
+  return t;
+}
+
+// first bin whose cumulative count reaches k (the host scan of FindSupportSet,
+// GAGA/gaga/functions.cu:414-420); results for every thread
+__device__ void cta_kbin(const int *hist, int max_bin, int k, int *k_bin, int *sum, int *scan) {
+  __shared__ int res[2];
+  const int t = threadIdx.x;
+  const int per = (max_bin + SH_THREADS - 1) / SH_THREADS;
+  const int b0 = t * per, b1 = min(b0 + per, max_bin);
+  int c = 0;
+  for (int b = b0; b < b1; ++b) c += hist[b];
+  scan[t] = c;
+  if (t == 0) { res[0] = -2; res[1] = 0; }
+  __syncthreads();
+  for (int off = 1; off < SH_THREADS; off <<= 1) {
+    const int v = t >= off ? scan[t - off] : 0;
+    __syncthreads();
+    scan[t] += v;
+    __syncthreads();
+  }
+  const int incl = scan[t], excl = incl - c;
+  if (k > 0 && excl < k && incl >= k) {
+    int a = excl;
+    for (int b = b0; b < b1; ++b) {
+      a += hist[b];
+      if (a >= k) { res[0] = b; res[1] = a; break; }
+    }
+  }
+  __syncthreads();
+  if (k <= 0) { *k_bin = -1; *sum = 0; }
+  else if (res[0] == -2) { *k_bin = max_bin - 1; *sum = scan[SH_THREADS - 1]; }
+  else { *k_bin = res[0]; *sum = res[1]; }
+  __syncthreads();
+}
+
+// FindSupportSet on x (GAGA/gaga/functions.cu:397-436) when binning this iteration, then
+// Threshold (functions.cu:374-378); refreshes the BF16 high/low parts of x
+__device__ void cta_support(GbState *st, float *x, int *bins, int n, __nv_bfloat16 *xcat, int *hist, int *scan) {
+  if (st->flags[F_DOBIN]) {
+    const int max_bin = st->max_bin;
+    for (int b = threadIdx.x; b < max_bin; b += SH_THREADS) hist[b] = 0;
+    __syncthreads();
+    const float intercept = st->max_value, slope = st->slope;
+    const float small_f = __double2float_rd((double)intercept * 0.000001);
+    for (int j = threadIdx.x; j < n; j += SH_THREADS) {
+      bool counted;
+      const int b = lin_bin(x[j], slope, intercept, small_f, counted);
+      bins[j] = b;
+      if (counted && b < max_bin) atomicAdd(&hist[b], 1);
+    }
+    __syncthreads();
+    int k_bin, sum;
+    cta_kbin(hist, max_bin, st->k, &k_bin, &sum, scan);
+    if (threadIdx.x == 0) {
+      if (sum < st->k) {
+        st->alpha_bin = st->alpha_bin * 0.5f;
+        st->max_bin = (int)((float)st->num_bins * (1.0f - st->alpha_bin));
+      }
+      st->min_val = intercept - (float)(k_bin + 1) / slope;
+      st->k_bin = k_bin;
+      st->sum = sum;
+    }
+    __syncthreads();
+  }
+  const int kb = st->k_bin;
+  for (int j = threadIdx.x; j < n; j += SH_THREADS) {
+    float v = x[j];
+    if (bins[j] > kb) {
+      v = 0.0f;
+      x[j] = 0.0f;
+    }
+    const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+    const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
+    xcat[j] = hi;
+    xcat[n + j] = hi;
+    xcat[2 * n + j] = lo;
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------------ problem per trial
+// x0 with createVector's binned support (GAGA/gaga/createVector.cu:207-300), key seed+1+t
+__global__ void __launch_bounds__(SH_THREADS) k_sh_genx(ShDev d) {
+  extern __shared__ int shist[];  // n counters
+  __shared__ float sm[32];
+  __shared__ int scan[SH_THREADS];
+  const int t = blockIdx.x, n = d.n;
+  float *x0 = d.X0 + (size_t)t * n;
+  int *bins = d.bins + (size_t)t * n;
+  if (t >= d.T) {
+    for (int j = threadIdx.x; j < n; j += SH_THREADS) x0[j] = 0.0f;
+    return;
+  }
+  const uint32_t key = d.seed + 1u + (uint32_t)t;
+  float mx = 0.0f;
+  for (int j = threadIdx.x; j < n; j += SH_THREADS) {
+    const float u = gbgen::uniform_at(key, 0u, gbgen::ST_VALUES, (uint64_t)j);
+    x0[j] = signbit(u - 0.5f) ? -1.0f : 1.0f;
+    mx = fmaxf(mx, gbgen::uniform_at(key, 0u, gbgen::ST_SUPPORT, (uint64_t)j));
+    shist[j] = 0;
+  }
+  const float keymax = cta_max(mx, sm);
+  const float slope = ((float)(n - 1) / keymax);
+  const float small_f = __double2float_rd((double)keymax * 0.000001);
+  for (int j = threadIdx.x; j < n; j += SH_THREADS) {
+    bool counted;
+    int b = lin_bin(gbgen::uniform_at(key, 0u, gbgen::ST_SUPPORT, (uint64_t)j), slope, keymax, small_f, counted);
+    if (!counted) b = n;  // keys below the cutoff never enter the support
+    bins[j] = b;
+    if (counted && b < n) atomicAdd(&shist[b], 1);
+  }
+  __syncthreads();
+  int k_bin, sum;
+  cta_kbin(shist, n, d.kreq[t], &k_bin, &sum, scan);
+  for (int j = threadIdx.x; j < n; j += SH_THREADS)
+    if (bins[j] > k_bin) x0[j] = 0.0f;
+  if (threadIdx.x == 0) d.st[t].k = sum;
+}
+
+// y_t = A x0_t in FP32, summed over the support in ascending column order; ||y||; initial
+// solver state (initial_state in gb_solver.cu) with tol = tol_rel ||y||
+__global__ void __launch_bounds__(SH_THREADS) k_sh_y(ShDev d) {
+  extern __shared__ int ssup[];  // support list (n) then values
+  __shared__ double smd[32];
+  __shared__ int cnt_s;
+  const int t = blockIdx.x, n = d.n, m = d.m;
+  const float *x0 = d.X0 + (size_t)t * n;
+  float *y = d.Y + (size_t)t * m;
+  __nv_bfloat16 *ybf = d.Rbf + (size_t)t * m;
+  GbState *st = d.st + t;
+  if (t >= d.T) {
+    for (int i = threadIdx.x; i < m; i += SH_THREADS) { y[i] = 0.0f; ybf[i] = __float2bfloat16_rn(0.0f); }
+    if (threadIdx.x == 0) { memset(st, 0, sizeof(GbState)); st->active = 0; }
+    return;
+  }
+  if (threadIdx.x == 0) cnt_s = 0;
+  __syncthreads();
+  // ordered support list: one warp-ballot pass per 256 columns
+  __shared__ int wcnt[SH_THREADS / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int j0 = 0; j0 < n; j0 += SH_THREADS) {
+    const int j = j0 + threadIdx.x;
+    const bool in = j < n && x0[j] != 0.0f;
+    const unsigned bal = __ballot_sync(0xffffffffu, in);
+    if (lane == 0) wcnt[w] = __popc(bal);
+    __syncthreads();
+    int wb = 0, tot = 0;
+    for (int q = 0; q < SH_THREADS / 32; ++q) {
+      if (q < w) wb += wcnt[q];
+      tot += wcnt[q];
+    }
+    if (in) ssup[cnt_s + wb + __popc(bal & ((1u << lane) - 1u))] = j;
+    __syncthreads();
+    if (threadIdx.x == 0) cnt_s += tot;
+    __syncthreads();
+  }
+  const int s = cnt_s;
+  double y2 = 0.0;
+  for (int i = threadIdx.x; i < m; i += SH_THREADS) {
+    float acc = 0.0f;
+    for (int c = 0; c < s; ++c) {
+      const int j = ssup[c];
+      acc = acc + d.A32[(size_t)j * m + i] * x0[j];
+    }
+    y[i] = acc;
+    ybf[i] = __float2bfloat16_rn(acc);
+    y2 += (double)acc * (double)acc;
+  }
+  const double ys = cta_sumd(y2, smd);
+  if (threadIdx.x == 0) {
+    const int ks = st->k;
+    memset(st, 0, sizeof(GbState));
+    st->m = m; st->n = n; st->k = ks; st->lda = m;
+    st->num_bins = max(n / 20, 1000);
+    st->maxiter = d.maxiter;
+    st->alg = GB_ALG_NIHT;
+    st->tol = d.tol_rel * (float)sqrt(ys);
+    st->active = 1; st->cycle = 1; st->pass_limit = d.maxiter + 4;
+    st->resid_diff = 1.0f;
+    for (int j = 0; j < 16; ++j) { st->prev[j] = 0.0f; st->evol[j] = 1.0f; }
+    st->alpha_bin = 0.25f;
+    st->max_bin = (int)((float)st->num_bins * (1.0f - st->alpha_bin));
+    st->beta_to_zero = 1; st->supp_change = 1;
+    st->flags[F_ALWAYS] = 1;
+    st->op_kind = GB_OP_DENSE;
+    st->trial = t;
+    st->red[R_RES] = ys;
+  }
+}
+
+// ------------------------------------------------------------------ NIHT in lockstep
+// x = H_k(A^T y) (algorithms.cu:1335-1354) from G = A_hi^T bf16(y)
+__global__ void __launch_bounds__(SH_THREADS) k_sh_init(ShDev d) {
+  __shared__ float sm[32];
+  __shared__ int hist[SH_NBINS_MAX];
+  __shared__ int scan[SH_THREADS];
+  const int t = blockIdx.x, n = d.n;
+  GbState *st = d.st + t;
+  if (t >= d.T) return;
+  float *x = d.X + (size_t)t * n;
+  const float *g = d.G + (size_t)t * n;
+  if (threadIdx.x == 0) ctrl_phase(st, C_INIT0, 0);
+  float mx = 0.0f;
+  for (int j = threadIdx.x; j < n; j += SH_THREADS) {
+    const float v = g[j];
+    x[j] = v;
+    mx = fmaxf(mx, fabsf(v));
+  }
+  mx = cta_max(mx, sm);
+  if (threadIdx.x == 0) {
+    st->red[R_XMAX] = mx;
+    ctrl_phase(st, C_INIT_BINPREP, 0);
+  }
+  __syncthreads();
+  cta_support(st, x, d.bins + (size_t)t * n, n, d.Xcat + (size_t)t * 3 * n, hist, scan);
+  if (threadIdx.x == 0) ctrl_phase(st, C_INIT_DONE, 0);
+}
+
+// ||r||^2, then x_thres = g restricted to the support, ||x_thres||^2, max|g|
+__global__ void __launch_bounds__(SH_THREADS) k_sh_mask(ShDev d) {
+  __shared__ float sm[32];
+  const int t = blockIdx.x, n = d.n, m = d.m;
+  GbState *st = d.st + t;
+  if (t >= d.T || !st->active) return;
+  const float *r = d.R + (size_t)t * m;
+  float r2 = 0.0f;
+  for (int i = threadIdx.x; i < m; i += SH_THREADS) r2 = fmaf(r[i], r[i], r2);
+  r2 = cta_sum(r2, sm);
+  if (threadIdx.x == 0) {
+    st->red[R_RES] = r2;
+    ctrl_phase(st, C_PUSH_RES, 0);
+  }
+  const float *g = d.G + (size_t)t * n;
+  const int *bins = d.bins + (size_t)t * n;
+  __nv_bfloat16 *xt = d.XTbf + (size_t)t * n;
+  const int kb = st->k_bin;
+  float s2 = 0.0f, gm = 0.0f;
+  for (int j = threadIdx.x; j < n; j += SH_THREADS) {
+    const float v = g[j];
+    const float o = bins[j] <= kb ? v : 0.0f;
+    xt[j] = __float2bfloat16_rn(o);
+    s2 = fmaf(o, o, s2);
+    gm = fmaxf(gm, fabsf(v));
+  }
+  s2 = cta_sum(s2, sm);
+  gm = cta_max(gm, sm);
+  if (threadIdx.x == 0) {
+    st->red[R_XT] = s2;
+    st->red[R_GMAX] = gm;
+  }
+}
+
+// step size (RestrictedSD), x += mu g, FindSupportSet + Threshold, stopping rules
+__global__ void __launch_bounds__(SH_THREADS) k_sh_step(ShDev d) {
+  __shared__ float sm[32];
+  __shared__ int hist[SH_NBINS_MAX];
+  __shared__ int scan[SH_THREADS];
+  const int t = blockIdx.x, n = d.n, m = d.m;
+  GbState *st = d.st + t;
+  if (t >= d.T || !st->active) return;
+  const float *q = d.Q + (size_t)t * m;
+  float q2 = 0.0f;
+  for (int i = threadIdx.x; i < m; i += SH_THREADS) q2 = fmaf(q[i], q[i], q2);
+  q2 = cta_sum(q2, sm);
+  if (threadIdx.x == 0) {
+    st->red[R_AXT] = q2;
+    ctrl_phase(st, C_SD_MU, 0);
+  }
+  __syncthreads();
+  const float mu = st->mu;
+  float *x = d.X + (size_t)t * n;
+  const float *g = d.G + (size_t)t * n;
+  float mx = 0.0f;
+  for (int j = threadIdx.x; j < n; j += SH_THREADS) {
+    const float o = fmaf(mu, g[j], x[j]);
+    x[j] = o;
+    mx = fmaxf(mx, fabsf(o));
+  }
+  mx = cta_max(mx, sm);
+  if (threadIdx.x == 0) {
+    st->red[R_XMAX] = mx;
+    ctrl_phase(st, C_BINPREP, 0);
+  }
+  __syncthreads();
+  cta_support(st, x, d.bins + (size_t)t * n, n, d.Xcat + (size_t)t * 3 * n, hist, scan);
+  if (threadIdx.x == 0) {
+    ctrl_phase(st, C_NIHT_STOP, 0);
+  }
+}
+
+// loop condition: any trial still active; bounded by maxiter + 4 passes
+__global__ void k_sh_any(ShDev d, int *passes, cudaGraphConditionalHandle h) {
+  __shared__ int any;
+  if (threadIdx.x == 0) any = 0;
+  __syncthreads();
+  int a = 0;
+  for (int t = threadIdx.x; t < d.T; t += blockDim.x) a |= d.st[t].active;
+  if (a) atomicOr(&any, 1);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int p = ++passes[0];
+    cudaGraphSetConditional(h, (any && p <= d.maxiter + 4) ? 1u : 0u);
+  }
+}
+
+// ------------------------------------------------------------------ debias and verdict
+// Least squares on the final support of a trial that reached ||y - A x|| <= tol: CG on
+// the normal equations in FP64 (A in FP32), from the NIHT solution; then the relative l2
+// error against x0 (GAGA/gaga/results.cu:468-475).
+__global__ void __launch_bounds__(SH_THREADS) k_sh_final(ShDev d, int debias) {
+  extern __shared__ int ssup[];
+  __shared__ double smd[32];
+  __shared__ int cnt_s;
+  const int t = blockIdx.x, n = d.n, m = d.m;
+  if (t >= d.T) return;
+  GbState *st = d.st + t;
+  float *x = d.X + (size_t)t * n;
+  const float *x0 = d.X0 + (size_t)t * n;
+  const float *y = d.Y + (size_t)t * m;
+  const bool converged = st->stop_reason == 1;
+  if (debias && converged) {
+    if (threadIdx.x == 0) cnt_s = 0;
+    __syncthreads();
+    __shared__ int wcnt[SH_THREADS / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int j0 = 0; j0 < n; j0 += SH_THREADS) {
+      const int j = j0 + threadIdx.x;
+      const bool in = j < n && x[j] != 0.0f;
+      const unsigned bal = __ballot_sync(0xffffffffu, in);
+      if (lane == 0) wcnt[w] = __popc(bal);
+      __syncthreads();
+      int wb = 0, tot = 0;
+      for (int q = 0; q < SH_THREADS / 32; ++q) {
+        if (q < w) wb += wcnt[q];
+        tot += wcnt[q];
+      }
+      if (in) ssup[cnt_s + wb + __popc(bal & ((1u << lane) - 1u))] = j;
+      __syncthreads();
+      if (threadIdx.x == 0) cnt_s += tot;
+      __syncthreads();
+    }
+    const int s = cnt_s;
+    double *z = d.scr + (size_t)t * (3 * (size_t)n + 2 * (size_t)m);
+    double *p = z + n, *g = p + n, *r = g + n, *q = r + m;
+    const float *A = d.A32;
+    for (int c = threadIdx.x; c < s; c += SH_THREADS) z[c] = x[ssup[c]];
+    __syncthreads();
+    // r = y - A_S z
+    for (int i = threadIdx.x; i < m; i += SH_THREADS) {
+      double a = 0.0;
+      for (int c = 0; c < s; ++c) a += (double)A[(size_t)ssup[c] * m + i] * z[c];
+      r[i] = (double)y[i] - a;
+    }
+    __syncthreads();
+    auto atr = [&](double *out) {  // out = A_S^T r, one warp per support column
+      for (int c = w; c < s; c += SH_THREADS / 32) {
+        const float *col = A + (size_t)ssup[c] * m;
+        double a = 0.0;
+        for (int i = lane; i < m; i += 32) a += (double)col[i] * r[i];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (lane == 0) out[c] = a;
+      }
+      __syncthreads();
+    };
+    atr(g);
+    double gg = 0.0;
+    for (int c = threadIdx.x; c < s; c += SH_THREADS) {
+      p[c] = g[c];
+      gg += g[c] * g[c];
+    }
+    gg = cta_sumd(gg, smd);
+    const double gg0 = gg;
+    for (int it = 0; it < 30 && gg > 1e-24 * gg0 && gg > 0.0; ++it) {
+      double qq = 0.0;
+      for (int i = threadIdx.x; i < m; i += SH_THREADS) {
+        double a = 0.0;
+        for (int c = 0; c < s; ++c) a += (double)A[(size_t)ssup[c] * m + i] * p[c];
+        q[i] = a;
+        qq += a * a;
+      }
+      qq = cta_sumd(qq, smd);
+      if (!(qq > 0.0)) break;
+      const double alpha = gg / qq;
+      for (int c = threadIdx.x; c < s; c += SH_THREADS) z[c] += alpha * p[c];
+      for (int i = threadIdx.x; i < m; i += SH_THREADS) r[i] -= alpha * q[i];
+      __syncthreads();
+      atr(g);
+      double gn = 0.0;
+      for (int c = threadIdx.x; c < s; c += SH_THREADS) gn += g[c] * g[c];
+      gn = cta_sumd(gn, smd);
+      const double beta = gn / gg;
+      for (int c = threadIdx.x; c < s; c += SH_THREADS) p[c] = g[c] + beta * p[c];
+      gg = gn;
+      __syncthreads();
+    }
+    for (int c = threadIdx.x; c < s; c += SH_THREADS) x[ssup[c]] = (float)z[c];
+    __syncthreads();
+  }
+  double e2 = 0.0, x2 = 0.0;
+  for (int j = threadIdx.x; j < n; j += SH_THREADS) {
+    const double df = (double)x0[j] - (double)x[j];
+    e2 += df * df;
+    x2 += (double)x0[j] * (double)x0[j];
+  }
+  e2 = cta_sumd(e2, smd);
+  x2 = cta_sumd(x2, smd);
+  if (threadIdx.x == 0) {
+    const float rel = (float)(sqrt(e2) / sqrt(x2));
+    d.iters[t] = st->iter;
+    d.err[t] = rel;
+    d.ok[t] = rel <= 1e-3f ? 1 : 0;
+  }
+}
+
+struct Buf {
+  std::vector<void *> p;
+  ~Buf() {
+    for (void *q : p) cudaFree(q);
+  }
+  template <class T>
+  gb_status get(T **out, size_t count) {
+    void *q = nullptr;
+    GB_CUDA_TRY(cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T)));
+    p.push_back(q);
+    *out = (T *)q;
+    return GB_OK;
+  }
+};
+
+}  // namespace
+
+static thread_local float g_sh_ms = 0.0f;
+static thread_local double g_sh_gemm_flops = 0.0;
+
+extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *iters_out, float *rel_err_out,
+                                              int *success_out, int *num_success) {
+  if (!b || !b->k || b->ntrials < 1 || b->m < 128 || b->n < 128 || b->m % 128 || b->n % 128 || b->m > b->n ||
+      b->n > 32768 || b->maxiter < 0) {
+    gb_set_error_message("shared batch: m, n multiples of 128 with 128 <= m <= n <= 32768, ntrials >= 1", __FILE__,
+                         __LINE__);
+    return GB_BAD_ARG;
+  }
+  const int m = b->m, n = b->n, T = b->ntrials, Tp = (T + 127) / 128 * 128;
+  for (int t = 0; t < T; ++t)
+    if (b->k[t] < 1 || b->k[t] > m) {
+      gb_set_error_message("shared batch: every k must satisfy 1 <= k <= m", __FILE__, __LINE__);
+      return GB_BAD_ARG;
+    }
+  cudaStream_t s = (cudaStream_t)b->stream;
+  Buf buf;
+  ShDev d;
+  memset(&d, 0, sizeof(d));
+  d.m = m; d.n = n; d.T = T; d.Tp = Tp; d.maxiter = b->maxiter; d.tol_rel = b->tol_rel; d.seed = b->seed;
+  int *dk;
+  GB_TRY(buf.get(&dk, T));
+  GB_CUDA_TRY(cudaMemcpyAsync(dk, b->k, sizeof(int) * T, cudaMemcpyHostToDevice, s));
+  d.kreq = dk;
+  GB_TRY(buf.get(&d.A32, (size_t)m * n));
+  GB_TRY(buf.get(&d.Acat, (size_t)m * 3 * n));
+  GB_TRY(buf.get(&d.AThi, (size_t)n * m));
+  for (float **v : {&d.X0, &d.X, &d.G}) GB_TRY(buf.get(v, (size_t)Tp * n));
+  for (float **v : {&d.Y, &d.R, &d.Q}) GB_TRY(buf.get(v, (size_t)Tp * m));
+  GB_TRY(buf.get(&d.Xcat, (size_t)Tp * 3 * n));
+  GB_TRY(buf.get(&d.XTbf, (size_t)Tp * n));
+  GB_TRY(buf.get(&d.Rbf, (size_t)Tp * m));
+  GB_TRY(buf.get(&d.bins, (size_t)Tp * n));
+  GB_TRY(buf.get(&d.st, (size_t)Tp));
+  GB_TRY(buf.get(&d.scr, (size_t)Tp * (3 * (size_t)n + 2 * (size_t)m)));
+  GB_TRY(buf.get(&d.iters, T));
+  GB_TRY(buf.get(&d.err, T));
+  GB_TRY(buf.get(&d.ok, T));
+  int *passes;
+  GB_TRY(buf.get(&passes, 1));
+  GB_CUDA_TRY(cudaMemsetAsync(passes, 0, sizeof(int), s));
+  GB_CUDA_TRY(cudaMemsetAsync(d.st, 0, sizeof(GbState) * Tp, s));
+  const int smem_n = n * (int)sizeof(int);
+  GB_CUDA_TRY(cudaFuncSetAttribute(k_sh_genx, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_n));
+  GB_CUDA_TRY(cudaFuncSetAttribute(k_sh_y, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_n));
+  GB_CUDA_TRY(cudaFuncSetAttribute(k_sh_final, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_n));
+  cudaEvent_t e0, e1;
+  GB_CUDA_TRY(cudaEventCreate(&e0));
+  GB_CUDA_TRY(cudaEventCreate(&e1));
+  GB_CUDA_TRY(cudaEventRecord(e0, s));
+  // ---- problem and operands
+  k_sh_genA<<<2048, 256, 0, s>>>(d.A32, m, n, b->seed);
+  k_sh_split<<<dim3(m / 32, n / 32), dim3(32, 8), 0, s>>>(d.A32, d.Acat, d.AThi, m, n);
+  k_sh_genx<<<Tp, SH_THREADS, smem_n, s>>>(d);
+  k_sh_y<<<Tp, SH_THREADS, smem_n, s>>>(d);
+  // ---- x = H_k(A^T y): G = A_hi^T bf16(y) (Rbf holds bf16(y) here)
+  GB_TRY(gb_gemm_tn(d.AThi, d.Rbf, d.G, n, Tp, m, m, m, nullptr, nullptr, s));
+  k_sh_init<<<Tp, SH_THREADS, 0, s>>>(d);
+  GB_CUDA_TRY(cudaGetLastError());
+  // ---- NIHT iterations in lockstep: one graph, WHILE any trial is active
+  cudaStream_t c0, c1;
+  GB_CUDA_TRY(cudaStreamCreateWithFlags(&c0, cudaStreamNonBlocking));
+  GB_CUDA_TRY(cudaStreamCreateWithFlags(&c1, cudaStreamNonBlocking));
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  gb_status rc = GB_OK;
+  {
+    cudaError_t e = cudaStreamBeginCapture(c0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+      gb_set_error_message(cudaGetErrorString(e), __FILE__, __LINE__);
+      rc = GB_CUDA_ERROR;
+    }
+    cudaGraphConditionalHandle h = 0;
+    if (rc == GB_OK) rc = gb_make_handle(c0, &h);
+    if (rc == GB_OK) {
+      k_sh_any<<<1, 1024, 0, c0>>>(d, passes, h);
+      rc = gb_open_while(c0, c1, h);
+    }
+    if (rc == GB_OK) {
+      rc = gb_gemm_tn(d.Acat, d.Xcat, d.R, m, Tp, 3 * n, 3 * n, 3 * n, d.Y, d.Rbf, c1);  // R = Y - A X
+      if (rc == GB_OK) rc = gb_gemm_tn(d.AThi, d.Rbf, d.G, n, Tp, m, m, m, nullptr, nullptr, c1);  // G = A^T R
+      k_sh_mask<<<Tp, SH_THREADS, 0, c1>>>(d);
+      if (rc == GB_OK) rc = gb_gemm_tn(d.Acat, d.XTbf, d.Q, m, Tp, n, 3 * n, n, nullptr, nullptr, c1);  // Q = A x_thres
+      k_sh_step<<<Tp, SH_THREADS, 0, c1>>>(d);
+      k_sh_any<<<1, 1024, 0, c1>>>(d, passes, h);
+      gb_status rc2 = gb_close_while(c1);
+      if (rc == GB_OK) rc = rc2;
+    }
+    cudaGraph_t g2 = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(c0, &g2);
+    if (rc == GB_OK && e2 != cudaSuccess) {
+      gb_set_error_message(cudaGetErrorString(e2), __FILE__, __LINE__);
+      rc = GB_CUDA_ERROR;
+    }
+    graph = g2;
+  }
+  if (rc == GB_OK) {
+    cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+    if (e == cudaSuccess) e = cudaGraphLaunch(exec, s);
+    if (e != cudaSuccess) {
+      gb_set_error_message(cudaGetErrorString(e), __FILE__, __LINE__);
+      rc = GB_CUDA_ERROR;
+    }
+  }
+  if (rc == GB_OK) {
+    k_sh_final<<<Tp, SH_THREADS, smem_n, s>>>(d, 1);
+    cudaEventRecord(e1, s);
+    if (b->d_A_out) cudaMemcpyAsync(b->d_A_out, d.A32, sizeof(float) * (size_t)m * n, cudaMemcpyDeviceToDevice, s);
+    if (b->d_Y_out) cudaMemcpyAsync(b->d_Y_out, d.Y, sizeof(float) * (size_t)T * m, cudaMemcpyDeviceToDevice, s);
+    if (b->d_X0_out) cudaMemcpyAsync(b->d_X0_out, d.X0, sizeof(float) * (size_t)T * n, cudaMemcpyDeviceToDevice, s);
+    std::vector<int> hit(T), hok(T);
+    std::vector<float> herr(T);
+    int hpass = 0;
+    cudaMemcpyAsync(hit.data(), d.iters, sizeof(int) * T, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(herr.data(), d.err, sizeof(float) * T, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(hok.data(), d.ok, sizeof(int) * T, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&hpass, passes, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+      gb_set_error_message(cudaGetErrorString(e), __FILE__, __LINE__);
+      rc = GB_CUDA_ERROR;
+    } else {
+      cudaEventElapsedTime(&g_sh_ms, e0, e1);
+      // per lockstep pass: GEMMs of 2*m*3n*Tp + 2*n*m*Tp + 2*m*n*Tp flops
+      g_sh_gemm_flops = (double)(hpass > 0 ? hpass - 1 : 0) * 2.0 * m * (double)n * Tp * 5.0 +
+                        2.0 * n * (double)m * Tp;
+      int ns = 0;
+      for (int t = 0; t < T; ++t) {
+        if (iters_out) iters_out[t] = hit[t];
+        if (rel_err_out) rel_err_out[t] = herr[t];
+        if (success_out) success_out[t] = hok[t];
+        ns += hok[t];
+      }
+      if (num_success) *num_success = ns;
+    }
+  }
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  cudaStreamDestroy(c0);
+  cudaStreamDestroy(c1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
+}
+
+extern "C" void gb_cs_shared_last_stats(double *gemm_flops, float *ms) {
+  if (gemm_flops) *gemm_flops = g_sh_gemm_flops;
+  if (ms) *ms = g_sh_ms;
+}

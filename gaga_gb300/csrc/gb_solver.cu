@@ -12,302 +12,11 @@
 
 #include "gb_internal.cuh"
 
-// ------------------------------------------------------------------ control phases
-enum {
-  C_INIT0,        // after ||y||^2 : err, err_start
-  C_INIT_BINPREP, // after A^T y and max|x| : decide binning
-  C_BINPREP,      // new max|x| and slope when binning
-  C_INIT_DONE,    // after threshold : (CGIHT needs more) evaluate the loop condition
-  C_CGIHT_INIT,   // CGIHT prologue after r0 = y - A x
-  C_PUSH_RES,     // push sqrt(red[R_RES]) into prev[]
-  C_SD_MU,        // RestrictedSD step size and maxChange; binning decision
-  C_NIHT_STOP,
-  C_HTP_CGINIT,
-  C_HTP_CG1,
-  C_HTP_CG2,
-  C_HTP_CG3,
-  C_HTP_STOP,
-  C_RCG_BETA,
-  C_RCG_ALPHA,
-  C_UCG_BETA,
-  C_UCG_ALPHA,
-  C_CGIHT_BINDEC,
-  C_CGIHT_POST,
-  C_CGIHT_STOP,
-  C_L0_INIT,
-  C_L0_PRE,
-  C_L0_STOP
-};
-
-__device__ static float max_list(const float *a, int n) {
-  float m = a[0];
-  for (int j = 1; j < n; ++j)
-    if (a[j] > m) m = a[j];
-  return m;
-}
-
-__device__ static float sqrt_red(const GbState *st, int slot) { return (float)sqrt(st->red[slot]); }
-
-// stopping test of the reference loops, e.g. GAGA/gaga/algorithms.cu:1365
-__device__ static int keep_going(GbState *st) {
-  int go = (st->err > st->tol) & (st->iter < st->maxiter) & (st->err < (100.0f * st->err_start)) &
-           ((double)st->resid_diff > 0.01 * (double)st->tol) & (st->fail == 0) & (st->cycle != 0);
-  if (!go && st->stop_reason == 0) {
-    if (!(st->err > st->tol)) st->stop_reason = 1;
-    else if (!(st->iter < st->maxiter)) st->stop_reason = 2;
-    else if (!(st->err < 100.0f * st->err_start)) st->stop_reason = 3;
-    else if (!((double)st->resid_diff > 0.01 * (double)st->tol)) st->stop_reason = 4;
-    else if (st->cycle == 0) st->stop_reason = 5;
-    else st->stop_reason = 6;
-  }
-  return go;
-}
-
-// residual bookkeeping after each outer iteration (algorithms.cu:1398-1421)
-__device__ static void stop_update(GbState *st, int fail_after) {
-  for (int j = 0; j < 15; ++j) st->evol[j] = st->evol[j + 1];
-  st->evol[15] = st->prev[14] - st->prev[15];
-  st->resid_diff = max_list(st->evol, 16);
-  for (int j = 0; j < 15; ++j)
-    if ((st->prev[15] == st->prev[j]) && (st->iter > 4)) st->cycle = 0;
-  if (st->iter > fail_after) {
-    float root = 1.0f / 15.0f;
-    float rate = st->prev[15] / st->prev[0];
-    rate = powf(rate, root);
-    if (rate > 0.999f) st->fail = 1;
-  }
-}
-
-__device__ static void push16(float *a, float v) {
-  for (int j = 0; j < 15; ++j) a[j] = a[j + 1];
-  a[15] = v;
-}
-
-__device__ static void finish_iteration(GbState *st, int fail_after) {
-  stop_update(st, fail_after);
-  st->iter++;
-  st->passes++;
-  st->active = keep_going(st);
-  if (st->passes > st->pass_limit && st->active) {
-    st->active = 0;
-    st->status = GB_WATCHDOG;
-  }
-}
-
-// the binning decision shared by every algorithm: FindSupportSet's skip path
-// (GAGA/gaga/functions.cu:401-403) or a new binning with a new max (algorithms.cu:1380-1383)
-__device__ static void bin_decision(GbState *st) {
-  if (st->min_val <= st->max_change) {
-    st->flags[F_DOBIN] = 1;
-  } else {
-    st->flags[F_DOBIN] = 0;
-    st->min_val = st->min_val - st->max_change;
-  }
-}
-
-// In eager mode (no graph) the handle is 0 and the host reads GbState instead.
-__device__ __forceinline__ void set_cond(cudaGraphConditionalHandle h, unsigned v) {
-  if (h) cudaGraphSetConditional(h, v);
-}
+#include "gb_ctrl.cuh"
 
 __global__ void k_ctrl(GbState *st, int phase, cudaGraphConditionalHandle h) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  const int live = st->active;
-  switch (phase) {
-    case C_INIT0:
-      st->err = sqrt_red(st, R_RES);
-      st->err_start = st->err;
-      break;
-    case C_INIT_BINPREP:
-      // max_value = MaxMagnitude(A^T y); slope = (num_bins-1)/max_value; HTP passes
-      // max_value as maxChange to force the first binning (algorithms.cu:1335-1354,2575)
-      st->max_value = (float)st->red[R_XMAX];
-      st->slope = ((float)(st->num_bins - 1) / st->max_value);
-      st->max_change = (st->alg == GB_ALG_HTP) ? st->max_value : 1.0f;
-      bin_decision(st);
-      break;
-    case C_BINPREP:
-      // if (minVal <= maxChange) { max_value = MaxMagnitude(d_vec,n); slope = ...; }
-      if (live && st->flags[F_DOBIN]) {
-        st->max_value = (float)st->red[R_XMAX];
-        st->slope = ((float)(st->num_bins - 1) / st->max_value);
-      }
-      break;
-    case C_INIT_DONE:
-      if (st->alg != GB_ALG_CGIHT) {
-        st->active = keep_going(st);
-        set_cond(h, st->active ? 1u : 0u);
-      }
-      break;
-    case C_CGIHT_INIT:
-      st->err = sqrt_red(st, R_RES);
-      st->prev[15] = st->err;
-      for (int j = 0; j < 15; ++j) st->evol[j] = st->evol[j + 1];
-      st->evol[15] = st->prev[14] - st->prev[15];
-      st->beta_to_zero = 1;
-      st->supp_change = 1;
-      st->k_bin_prev = 0;
-      st->flags[F_UCG] = st->restart ? 0 : 1;
-      st->flags[F_RCG] = st->restart ? 1 : 0;
-      st->active = keep_going(st);
-      set_cond(h, st->active ? 1u : 0u);
-      break;
-    case C_PUSH_RES:
-      if (!live) break;
-      push16(st->prev, sqrt_red(st, R_RES));
-      break;
-    case C_SD_MU: {
-      if (!live) break;
-      // RestrictedSD_S_gen (GAGA/gaga/functions.cu:715-744)
-      float err2 = sqrt_red(st, R_AXT);
-      float mu = sqrt_red(st, R_XT);
-      if (mu < 400.0f * err2) {
-        mu = mu / err2;
-        mu = mu * mu;
-      } else {
-        mu = 0.0f;
-      }
-      st->mu = mu;
-      st->max_change = 2.0f * mu * (float)st->red[R_GMAX];
-      bin_decision(st);
-      break;
-    }
-    case C_NIHT_STOP:
-      if (live) {
-        if (st->op_kind == GB_OP_DENSE) st->bytes += dense_bytes(st, 1, 2);
-        st->err = st->prev[15];
-        finish_iteration(st, 749);
-      }
-      set_cond(h, st->active ? 1u : 0u);
-      break;
-    case C_HTP_CGINIT:
-      if (!live) {
-        st->flags[F_CG] = 0;
-        set_cond(h, 0u);
-        break;
-      }
-      for (int j = 0; j < 16; ++j) { st->prev_cg[j] = 0.0f; st->evol_cg[j] = 1.0f; }
-      st->diff_cg = 1.0f;
-      st->prev_cg[15] = st->prev[15];
-      st->mu = (float)st->red[R_DOT1];
-      st->err_cg = (float)st->red[R_RES];
-      st->prev_cg[15] = st->err_cg;
-      st->it_cg = 0;
-      st->flags[F_CG] = (st->err_cg > st->tol_cg) & (st->it_cg < 15) & (st->diff_cg > st->tol2);
-      set_cond(h, st->flags[F_CG] ? 1u : 0u);
-      break;
-    case C_HTP_CG1: {
-      // RestrictedCG_S_gen (GAGA/gaga/functions.cu:944-950)
-      float alpha = (float)st->red[R_CG];
-      if (st->mu < 1000.0f * alpha) alpha = st->mu / alpha;
-      else alpha = 0.0f;
-      st->cg_alpha = alpha;
-      break;
-    }
-    case C_HTP_CG2: {
-      float beta = st->mu;
-      st->mu = (float)st->red[R_DOT3];
-      if (st->mu < 1000.0f * beta) beta = st->mu / beta;
-      else beta = 0.0f;
-      st->cg_beta = beta;
-      break;
-    }
-    case C_HTP_CG3:
-      if (st->flags[F_CG] && live) {
-        push16(st->prev_cg, (float)st->red[R_RES]);
-        st->err_cg = st->prev_cg[15];
-        st->it_cg++;
-        for (int j = 0; j < 15; ++j) st->evol_cg[j] = st->evol_cg[j + 1];
-        st->evol_cg[15] = st->prev_cg[14] - st->prev_cg[15];
-        st->diff_cg = max_list(st->evol_cg, 16);
-        st->flags[F_CG] = (st->err_cg > st->tol_cg) & (st->it_cg < 15) & (st->diff_cg > st->tol2);
-      } else {
-        st->flags[F_CG] = 0;
-      }
-      set_cond(h, (st->flags[F_CG] && live) ? 1u : 0u);
-      break;
-    case C_HTP_STOP:
-      if (live) {
-        if (st->op_kind == GB_OP_DENSE) st->bytes += dense_bytes(st, 2 + st->it_cg, 3 + 2 * st->it_cg);
-        st->err = sqrtf(st->err_cg);
-        push16(st->prev, st->err);
-        finish_iteration(st, 125);
-      }
-      set_cond(h, st->active ? 1u : 0u);
-      break;
-    case C_RCG_BETA: {
-      if (!live || !st->flags[F_RCG]) break;
-      // RestrictedCGwithSupportEvolution (GAGA/gaga/functions.cu:1054-1064)
-      float beta;
-      if (st->beta_to_zero == 1) {
-        beta = 0.0f;
-        st->mu = (float)st->red[R_XT];
-      } else {
-        beta = st->mu;
-        st->mu = (float)st->red[R_XT];
-        if (st->mu < 1000.0f * beta) beta = st->mu / beta;
-        else beta = 0.0f;
-      }
-      st->cg_beta = beta;
-      break;
-    }
-    case C_RCG_ALPHA: {
-      if (!live || !st->flags[F_RCG]) break;
-      float alpha = (float)st->red[R_AXT];
-      if (st->mu < 1000.0f * alpha) alpha = st->mu / alpha;
-      else alpha = 0.0f;
-      st->cg_alpha = alpha;
-      st->max_change = 2.0f * alpha * (float)st->red[R_GMAX];
-      break;
-    }
-    case C_UCG_BETA:
-      if (!live || !st->flags[F_UCG]) break;
-      // UnrestrictedCG (GAGA/gaga/functions.cu:1169-1178)
-      if (st->beta_to_zero == 1) st->cg_beta = 0.0f;
-      else st->cg_beta = -((float)st->red[R_DOT1]) / (float)st->red[R_DOT2];
-      break;
-    case C_UCG_ALPHA:
-      if (!live || !st->flags[F_UCG]) break;
-      st->cg_alpha = ((float)st->red[R_DOT3]) / (float)st->red[R_DOT4];
-      st->mu = (float)st->red[R_XT];
-      st->max_change = 2.0f * st->cg_alpha * (float)st->red[R_GMAX];
-      break;
-    case C_CGIHT_BINDEC:
-      if (!live) break;
-      // CGIHT_S_gen (GAGA/gaga/algorithms.cu:3849-3899)
-      st->beta_to_zero = 0;
-      if (st->min_val <= st->max_change) {
-        st->flags[F_DOBIN] = 1;
-        st->k_bin_prev = st->k_bin;
-        st->changed = 0;
-      } else {
-        st->flags[F_DOBIN] = 0;
-        st->supp_change = 0;
-        st->min_val = st->min_val - st->max_change;
-      }
-      st->flags[F_REMASK] = 0;
-      break;
-    case C_CGIHT_POST:
-      if (!live || !st->flags[F_DOBIN]) break;
-      st->supp_change = st->changed ? 1 : 0;
-      if (st->supp_change) {
-        if (st->restart) st->beta_to_zero = 1;
-        else st->flags[F_REMASK] = 1;
-      }
-      break;
-    case C_CGIHT_STOP:
-      if (live) {
-        if (st->op_kind == GB_OP_DENSE) st->bytes += dense_bytes(st, 1, st->flags[F_UCG] ? 3 : 2);
-        st->err = st->prev[15];
-        finish_iteration(st, 749);
-        if (st->restart) { st->flags[F_UCG] = 0; st->flags[F_RCG] = 1; }
-        else { st->flags[F_UCG] = st->supp_change ? 1 : 0; st->flags[F_RCG] = st->supp_change ? 0 : 1; }
-      }
-      set_cond(h, st->active ? 1u : 0u);
-      break;
-    default:
-      break;
-  }
+  ctrl_phase(st, phase, h);
 }
 
 // ------------------------------------------------------------------ l0 control
@@ -478,21 +187,6 @@ __global__ void k_copy_norm(GbState *st, int pf, const float *__restrict__ src, 
 }
 
 // ------------------------------------------------------------------ support selection
-// LinearBinning (GAGA/gaga/kernels.cu:135-146), bit-exact.  The double-precision test
-// (double)t > (double)intercept * 1e-6 equals t > F in float with F the double product
-// rounded toward -inf.  float -> int stores use round-toward-zero with saturation and
-// NaN -> 0, as the reference's compiled kernel does; `slope*intercept + 1.0f` is one
-// fused multiply-add there and here.
-__device__ __forceinline__ int lin_bin(float v, float slope, float intercept, float small_f, bool &counted) {
-  const float t = fabsf(v);
-  if (t > small_f) {
-    counted = true;
-    return __float2int_rz(fmaxf(0.0f, __fmul_rn(slope, __fsub_rn(intercept, t))));
-  }
-  counted = false;
-  return __float2int_rz(__fmaf_rn(slope, intercept, 1.0f));
-}
-
 __global__ void k_hist(const GbState *st, int pf, const float *__restrict__ v, int *__restrict__ bins,
                        int *__restrict__ bins_prev, int *__restrict__ counters, int n) {
   if (!gb_pred(st, pf)) return;

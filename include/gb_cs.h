@@ -192,6 +192,40 @@ gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float *rel_err_ou
  * counterpart; used for roofline reporting). */
 void gb_cs_batch_last_stats(double *bytes, float *kernel_ms);
 
+/* ---- shared-matrix batched form (no reference counterpart) ----
+ * ntrials NIHT trials y_t = A x0_t that share one dense Gaussian A (drawn from `seed` as
+ * gb_cs_generate_and_solve draws it; trial t's +-1 signal x0_t with k[t] nonzeros uses the
+ * key seed + 1 + t).  The operator applications of all trials run as BF16 tensor-core
+ * GEMMs with FP32 accumulation; the residual keeps ~FP32 accuracy by splitting A and x
+ * into BF16 high and low parts; trials that stop with ||y - A x|| <= tol_rel ||y|| are
+ * debiased by least squares on their support in FP64.  m, n multiples of 128 with
+ * 128 <= m <= n <= 32768.  Per-trial outputs as for gb_cs_solve_batch (host arrays).
+ * d_A_out (m*n, column-major), d_Y_out (ntrials*m), d_X0_out (ntrials*n) are optional
+ * device copies of the generated problem. */
+typedef struct {
+  int ntrials, m, n;
+  const int *k;                  /* host array of ntrials sparsities */
+  unsigned int seed;
+  float tol_rel;
+  int maxiter;
+  float *d_A_out, *d_Y_out, *d_X0_out;
+  void *stream;
+} gb_shared_batch;
+
+gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *iters_out, float *rel_err_out,
+                                   int *success_out, int *num_success);
+
+/* GEMM FLOPs issued and device time in ms of the last gb_cs_solve_shared_batch call on this
+ * thread (no reference counterpart; used for roofline reporting). */
+void gb_cs_shared_last_stats(double *gemm_flops, float *kernel_ms);
+
+/* BF16 tensor-core GEMM with FP32 accumulation (no reference counterpart; the building
+ * block of the shared-matrix form):  Ct[N x M] = [Y -] (A[M x K] . B[N x K]^T)^T with A, B
+ * row-major BF16 (K contiguous), Ct and Y FP32 with M contiguous per column, d_Cb an
+ * optional BF16 copy of Ct.  M, N multiples of 128, K a multiple of 32. */
+gb_status gb_cs_gemm_bf16_tn(const void *d_A, const void *d_B, float *d_Ct, int M, int N, int K,
+                             const float *d_Y, void *d_Cb, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,113 @@
+"""Shared-matrix batched form (gb_cs_solve_shared_batch) and its BF16 GEMM.
+
+The GEMM is checked against an FP64 product of the same BF16-rounded operands.  The
+shared-matrix solve draws its A and signals on the device; the test reads them back and
+checks them against the oracle's generators, then solves every trial again with the
+single-trial FP32 drop-in (gb_cs_solve on the same A and y) and compares verdicts
+(relative l2 error <= 1e-3).  The BF16 operator changes the iterates, not the problem,
+so verdicts agree except at the edge of the phase transition.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SEED = 4242
+
+
+def _bf16_round(a):
+    """Round-to-nearest-even FP32 -> BF16 -> FP32 in numpy."""
+    u = np.ascontiguousarray(a, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) >> 16 << 16
+    return u.astype(np.uint32).view(np.float32)
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 128, 32), (256, 384, 160), (512, 128, 1024)])
+def test_gemm_bf16_tn(gb, M, N, K):
+    import torch
+
+    rng = np.random.default_rng(M + N + K)
+    A = _bf16_round(rng.standard_normal((M, K)).astype(np.float32))
+    B = _bf16_round(rng.standard_normal((N, K)).astype(np.float32))
+    Y = rng.standard_normal((N, M)).astype(np.float32)
+    dA = torch.from_numpy(A).to(torch.bfloat16).cuda()
+    dB = torch.from_numpy(B).to(torch.bfloat16).cuda()
+    assert np.array_equal(dA.float().cpu().numpy(), A)
+    ref = (A.astype(np.float64) @ B.astype(np.float64).T).T  # (N, M)
+    Ct, _ = gb.gemm_bf16_tn(dA, dB)
+    torch.cuda.synchronize()
+    got = Ct.cpu().numpy()
+    # FP32 accumulation of K products: |error| <= ~K * eps32 * sum|a b|
+    bound = K * 2.0 ** -23 * (np.abs(A).astype(np.float64) @ np.abs(B).astype(np.float64).T).T
+    assert np.all(np.abs(got - ref) <= bound + 1e-6)
+    Ct2, Cb = gb.gemm_bf16_tn(dA, dB, Y=torch.from_numpy(Y).cuda(), want_bf16=True)
+    torch.cuda.synchronize()
+    got2 = Ct2.cpu().numpy()
+    assert np.all(np.abs(got2 - (Y - ref)) <= bound + 1e-5)
+    assert np.array_equal(Cb.float().cpu().numpy(), _bf16_round(got2))
+
+
+def test_gemm_rejects_bad_shapes(gb):
+    import torch
+
+    a = torch.zeros((100, 64), dtype=torch.bfloat16, device="cuda")
+    b = torch.zeros((128, 64), dtype=torch.bfloat16, device="cuda")
+    with pytest.raises(gb.GagaError):
+        gb.gemm_bf16_tn(a, b)
+
+
+def _shared_case(gb, gbo, m, n, ks, maxiter):
+    import torch
+
+    ns, iters, err, ok, A, Y, X0 = gb.solve_shared_batch(m, n, ks, SEED, tol_rel=1e-4, maxiter=maxiter,
+                                                          outputs=True)
+    torch.cuda.synchronize()
+    # the generated problem is the oracle's: A from SEED (trial 0), x0_t from SEED + 1 + t
+    A_o = gbo.gen_dense(m, n, SEED, 0, 1).reshape(n, m)
+    np.testing.assert_allclose(A.cpu().numpy(), A_o, rtol=1e-5, atol=1e-6)
+    X0h = X0.cpu().numpy()
+    for t in (0, len(ks) // 2, len(ks) - 1):
+        x_o, _ = gbo.gen_vector(n, int(ks[t]), 1, SEED + 1 + t, 0)
+        assert np.array_equal(X0h[t], x_o), t
+    return ns, iters, err, ok, A, Y, X0h
+
+
+def test_shared_batch_matches_plain(gb, gbo):
+    import torch
+
+    m, n = 512, 1024
+    ks = np.round(np.linspace(0.04, 0.42, 96) * m).astype(np.int32)
+    ns, iters, err, ok, A, Y, X0 = _shared_case(gb, gbo, m, n, ks, 1000)
+    assert ns == int(ok.sum())
+    agree = 0
+    for t in range(len(ks)):
+        k_t = int(np.count_nonzero(X0[t]))
+        opts = gb.gaga_options("tol", 1e-4, "tol_is_relative", 1, "maxiter", 1000)
+        x, it, _ = gb.gaga_cs("NIHT", "gen", Y[t].contiguous(), A.t(), k_t, opts)
+        x = x.cpu().numpy()
+        rel = np.linalg.norm(x - X0[t]) / np.linalg.norm(X0[t])
+        agree += int((rel <= 1e-3) == bool(ok[t]))
+        if ok[t]:
+            assert err[t] <= 1e-3
+    assert 0 < ns < len(ks)  # the sample straddles the phase transition
+    assert agree >= len(ks) - 1, (agree, len(ks))
+
+
+def test_shared_batch_debias_accuracy(gb, gbo):
+    """Trials well inside the recovery region come back exact to FP32 level after debias."""
+    m, n = 1024, 2048
+    ks = np.full(40, 60, dtype=np.int32)
+    ns, iters, err, ok, A, Y, X0 = _shared_case(gb, gbo, m, n, ks, 500)
+    assert ns == len(ks)
+    assert float(np.max(err)) < 1e-5
+    fl, ms = gb.shared_last_stats()
+    assert fl > 0 and ms > 0
+
+
+def test_shared_batch_rejects_bad_sizes(gb):
+    with pytest.raises(gb.GagaError):
+        gb.solve_shared_batch(500, 1024, [10], SEED)
+    with pytest.raises(gb.GagaError):
+        gb.solve_shared_batch(1024, 512, [10], SEED)
+    with pytest.raises(gb.GagaError):
+        gb.solve_shared_batch(512, 1024, [0], SEED)
