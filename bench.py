@@ -1,17 +1,23 @@
 """Benchmark: trials recovered per second on the dense phase-transition sweep.
 
-Workload: the sweep of independent dense Gaussian trials (n in {1024,...,16384},
-delta in {0.1,...,0.9}, rho on a 0.02 grid up to 0.5; gaga_gb300/sweep.py), NIHT with
-||y - A x|| <= 1e-4 ||y||, maxiter 5000; a trial is recovered when its relative l2
-error is <= 1e-3.  A step is one wave of the sweep (the 4096-trial sweep split into 16
-interleaved waves of 256 trials).  Each trial's A and x are drawn on the device from
-(seed + trial id) inside the timed region; every trial's A is a separate matrix.
+Workload: 4096 dense Gaussian NIHT trials with ||y - A x|| <= 1e-4 ||y||, maxiter 5000;
+a trial is recovered when its relative l2 error is <= 1e-3 (gaga_gb300/sweep.py):
+  - 3072 independent trials (n in {1024,...,16384}, delta in {0.1,...,0.9}, rho on a
+    0.02 grid up to 0.5), each with its own A and x drawn on the device from
+    (seed + trial id): the batched slot-graph form (gb_cs_solve_batch);
+  - 1024 trials sharing one A (n = 8192, m = 4096, rho cycling the same grid): the
+    shared-matrix form (gb_cs_solve_shared_batch; BF16 tensor-core GEMMs, split-BF16
+    residual, least-squares debias).
+A step is one quarter of the sweep: 768 independent trials plus 256 shared-matrix trials.
+Problem generation runs inside the timed region.
 
-  value : recovered trials / device time of the batched (tuned) form's kernels
-  e2e   : recovered trials / wall time of gb_cs_solve_batch called with host arrays
-          (trial table in, per-trial iterations/errors/verdicts out)
-  plain : the single-trial drop-in (gb_cs_generate_and_solve per trial) on a sample of
-          the same wave, for the tuned-vs-plain ratio
+  value : recovered trials / device time of both forms' kernels
+  e2e   : recovered trials / wall time of the two calls made with host arrays (trial
+          tables in, per-trial iterations/errors/verdicts out)
+  plain : the single-trial FP32 drop-in on samples of both parts (gb_cs_generate_and_solve
+          for independent trials, gb_cs_solve on the shared A for shared trials), scaled
+          to the 3072 + 1024 mix, for the tuned-vs-plain ratio; the verdicts of the same
+          trials give the agreement between the two forms
   cpu_baseline / --impl reference : the CPU oracle (oracle/gbo.c, OpenMP inside each
           trial) on a bounded sample of the wave
 
@@ -31,7 +37,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "trials recovered/s (rel err<=1e-3), tuned vs plain on 1 GB300; matvec % HBM peak"
-TOTAL, WAVES, SEED, TOL_REL, MAXITER = 4096, 16, 20240607, 1e-4, 5000
+TOTAL, SHARED, PARTS, SEED, TOL_REL, MAXITER = 4096, 1024, 4, 20240607, 1e-4, 5000
+SHARED_SEED = SEED + 1000003  # keys of the shared subset stay clear of the independent trials' seed + id
 
 
 def dist_env():
@@ -98,11 +105,21 @@ class ClockSampler:
 
 
 def wave_arrays(w):
+    """Independent trials of step w: one of PARTS interleaved waves of the 3072."""
     from gaga_gb300 import sweep
 
-    n, m, k, tid = sweep.sweep_trials(TOTAL)
-    idx = sweep.wave(TOTAL, WAVES, w % WAVES)
+    n, m, k, tid = sweep.sweep_trials(TOTAL - SHARED)
+    idx = sweep.wave(TOTAL - SHARED, PARTS, w % PARTS)
     return n[idx], m[idx], k[idx], tid[idx]
+
+
+def shared_part(w):
+    """Shared-matrix trials of step w: (k array, first trial index)."""
+    from gaga_gb300 import sweep
+
+    ks = sweep.shared_subset(SHARED)
+    q = w % PARTS
+    return np.ascontiguousarray(ks[q::PARTS]), q * (SHARED // PARTS)
 
 
 def cpu_sample(w, count):
@@ -162,81 +179,151 @@ def bench_ours(args):
     torch.cuda.set_device(local)
     gb._lib.load()
     peak, peak_kind = peaks()
+    tpeak, tpeak_kind = tensor_peak()
 
-    def solve_wave(w):
+    def solve_step(w):
+        """One quarter of the sweep: independent trials, then the shared-matrix trials."""
         n, m, k, tid = wave_arrays(w)
         t0 = time.perf_counter()
         ns, iters, err, ok = gb.solve_batch(n, m, k, SEED, tid, alg="NIHT", tol_rel=TOL_REL, maxiter=MAXITER)
-        wall = time.perf_counter() - t0
+        t1 = time.perf_counter()
         nbytes, kms = gb.batch_last_stats()
-        return ns, wall, kms, nbytes, len(n), iters
+        ks, first = shared_part(w)
+        ns2, it2, err2, ok2 = gb.solve_shared_batch(gb.sweep.SHARED_M, gb.sweep.SHARED_N, ks, SHARED_SEED,
+                                                    tol_rel=TOL_REL, maxiter=MAXITER, first_trial=first)
+        t2 = time.perf_counter()
+        flops, kms2 = gb.shared_last_stats()
+        return dict(ok=ns + ns2, trials=len(n) + len(ks), wall=t2 - t0, kms=kms + kms2, bytes=nbytes, flops=flops,
+                    kms_batch=kms, kms_shared=kms2, ok_batch=ns, ok_shared=ns2, n_batch=len(n), n_shared=len(ks),
+                    verdict_batch=ok, verdict_shared=ok2, wall_batch=t1 - t0, wall_shared=t2 - t1,
+                    h2d=12 * len(n) + 4 * len(ks), d2h=12 * (len(n) + len(ks)))
 
-    # warm-up waves
     from gaga_gb300 import sweep
 
     for s in range(args.warmup):
-        solve_wave(sweep.rank_wave(rank, world, s))
+        solve_step(sweep.rank_wave(rank, world, s))
     sampler = ClockSampler(local)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     sampler.start()
-    t_start = time.perf_counter()
-    tot_ok = tot_trials = 0
-    tot_wall = tot_kms = tot_bytes = 0.0
+    acc = {}
+    first_step = None
     launches = 0
     for s in range(args.steps):
         w = sweep.rank_wave(rank, world, args.warmup + s)
-        ns, wall, kms, nbytes, cnt, _ = solve_wave(w)
-        tot_ok += ns
-        tot_trials += cnt
-        tot_wall += wall
-        tot_kms += kms
-        tot_bytes += nbytes
-        # one persistent launch per cluster-size class present in the wave
-        launches += len({1 if nn <= 2048 else 2 if nn <= 4096 else 4 if nn <= 8192 else 8 for nn in wave_arrays(w)[0]})
+        r = solve_step(w)
+        if first_step is None:
+            first_step = (w, r)
+        for key in ("ok", "trials", "wall", "kms", "bytes", "flops", "kms_batch", "kms_shared", "ok_batch", "ok_shared",
+                    "n_batch", "n_shared", "wall_batch", "wall_shared", "h2d", "d2h"):
+            acc[key] = acc.get(key, 0) + r[key]
+        # host-issued launches: one graph per slot stream of the batched form; the shared
+        # form's 6 setup kernels, its graph and its verdict kernel
+        launches += gb.batch_slot_count() + 8
     torch.cuda.synchronize()
-    elapsed = time.perf_counter() - t_start
     clocks = sampler.stop()
     if world > 1:
-        t = torch.tensor([elapsed, tot_kms, tot_wall], dtype=torch.float64, device="cuda")
+        t = torch.tensor([acc["kms"], acc["wall"]], dtype=torch.float64, device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        c = torch.tensor([tot_ok, tot_trials, tot_bytes], dtype=torch.float64, device="cuda")
+        c = torch.tensor([acc["ok"], acc["trials"], acc["bytes"]], dtype=torch.float64, device="cuda")
         torch.distributed.all_reduce(c)
-        elapsed, tot_kms, tot_wall = t.tolist()
-        tot_ok, tot_trials, tot_bytes = c.tolist()
+        acc["kms"], acc["wall"] = t.tolist()
+        acc["ok"], acc["trials"], acc["bytes"] = c.tolist()
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
         return
-    value = tot_ok / (tot_kms / 1e3)
-    e2e = tot_ok / tot_wall
-    achieved = tot_bytes / (tot_kms / 1e3) / 1e9 / max(1, world)
+    value = acc["ok"] / (acc["kms"] / 1e3)
+    e2e = acc["ok"] / acc["wall"]
+    achieved = acc["bytes"] / (acc["kms_batch"] / 1e3) / 1e9 / max(1, world)
+    gemm_tf = acc["flops"] / (acc["kms_shared"] / 1e3) / 1e12
     line = {"metric": METRIC, "value": value, "unit": "trials/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": tot_kms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded Philox Gaussian trials drawn on device)",
-            "config": {"workload": "dense phase-transition sweep (4096 trials, n 1024-16384, delta 0.1-0.9, "
-                                   "rho 0.02-0.5), NIHT tol 1e-4*||y||, one 256-trial wave per step per GPU",
-                       "form": "tuned: batched slot graphs (device trial queue, device generation)",
-                       "trials_per_step": int(tot_trials // max(1, args.steps)), "l2": "working set >> L2 (A up to "
-                                                                                         "966 MB per trial)"},
-            "recovered": int(tot_ok), "trials": int(tot_trials),
-            "e2e": {"value": e2e, "unit": "trials/s", "h2d_bytes_per_step": 16 * 256, "d2h_bytes_per_step": 12 * 256},
+            "warmup": args.warmup, "ms_per_step": acc["kms"] / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32 (shared-matrix part: bf16 GEMM, fp32 accumulate)",
+            "data": "synthetic (seeded Philox Gaussian trials drawn on device)",
+            "config": {"workload": "dense phase-transition sweep: 4096 NIHT trials = 3072 independent (n 1024-16384, "
+                                   "delta 0.1-0.9, rho 0.02-0.5) + 1024 sharing one A (n 8192, m 4096, rho 0.02-0.5); "
+                                   "tol 1e-4*||y||; one quarter of the sweep per step per GPU",
+                       "form": "tuned: batched slot graphs (device trial queue, device generation) + shared-matrix "
+                               "BF16 tensor-core GEMM form",
+                       "trials_per_step": int(acc["trials"] // max(1, args.steps)),
+                       "l2": "working set >> L2 (A up to 966 MB per trial; shared form 600 MB of BF16 operands)"},
+            "recovered": int(acc["ok"]), "trials": int(acc["trials"]),
+            "parts": {"independent": {"trials": int(acc["n_batch"]), "recovered": int(acc["ok_batch"]),
+                                      "kernel_ms": acc["kms_batch"],
+                                      "recovered_per_s": acc["ok_batch"] / (acc["kms_batch"] / 1e3)},
+                      "shared_matrix": {"trials": int(acc["n_shared"]), "recovered": int(acc["ok_shared"]),
+                                        "kernel_ms": acc["kms_shared"],
+                                        "recovered_per_s": acc["ok_shared"] / (acc["kms_shared"] / 1e3),
+                                        "gemm_tflops": gemm_tf,
+                                        "gemm_frac": gemm_tf / tpeak if tpeak else None}},
+            "e2e": {"value": e2e, "unit": "trials/s", "h2d_bytes_per_step": int(acc["h2d"] // args.steps),
+                    "d2h_bytes_per_step": int(acc["d2h"] // args.steps)},
             "batched_matvec_bytes_per_s": {"achieved": achieved, "unit": "GB/s", "frac": achieved / peak,
-                                           "what": "algorithmic dense operator bytes of all trials / device time of "
-                                                   "the whole batched form (generation and control included)"},
-            "gpu_launches": launches, "clocks": clocks}
+                                           "what": "algorithmic dense operator bytes of the independent trials / "
+                                                   "device time of the whole batched form (generation and control "
+                                                   "included)"},
+            "gpu_launches": launches,
+            "gpu_launches_note": "host-issued launches (kernels and graphs); the graphs run the solver kernels in "
+                                 "device-side WHILE loops",
+            "clocks": clocks}
     mv = matvec_roofline(peak, peak_kind)
     line["roofline"] = mv["at"]
     line["matvec"] = mv
+    line["gemm"] = gemm_roofline(tpeak, tpeak_kind)
     if args.plain_trials > 0 and world == 1:
-        line["plain"] = bench_plain(args)
+        line["plain"] = bench_plain(args, first_step)
         line["tuned_vs_plain"] = value / line["plain"]["value"] if line["plain"]["value"] else None
     if not args.no_cpu and world == 1:
         line["cpu_baseline"] = run_cpu(args.warmup, args.cpu_trials)
     print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def tensor_peak():
+    """Dense BF16 tensor peak (TFLOP/s) for a kernel timed inside a long run."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        for key in ("bf16_tflops_sustained", "bf16_tflops"):
+            if d.get(key):
+                return float(d[key]), "measured (%s)" % key
+    except (OSError, ValueError):
+        pass
+    return 1700.0, "fallback (sustained bf16 on an earlier GB300)"
+
+
+def gemm_roofline(tpeak, tpeak_kind, M=4096, N=1024, K=3 * 8192, reps=10):
+    """The shared-matrix form's residual GEMM (k_gemm_tn_mma, [A_hi|A_lo|A_hi] . X^T) on its
+    full 1024-trial shape, timed with CUDA events on its stream."""
+    import torch
+
+    import gaga_gb300 as gb
+
+    g = torch.Generator(device="cuda").manual_seed(2)
+    A = torch.randn(M, K, device="cuda", generator=g).to(torch.bfloat16)
+    B = torch.randn(N, K, device="cuda", generator=g).to(torch.bfloat16)
+    Y = torch.randn(N, M, device="cuda", generator=g)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        for _ in range(3):
+            gb.gemm_bf16_tn(A, B, Y=Y, want_bf16=True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(reps):
+            gb.gemm_bf16_tn(A, B, Y=Y, want_bf16=True)
+        e1.record(s)
+    e1.synchronize()
+    t = e0.elapsed_time(e1) / 1e3 / reps
+    ach = 2.0 * M * N * K / t / 1e12
+    del A, B, Y
+    torch.cuda.empty_cache()
+    return {"bound": "tensor", "achieved": ach, "peak": tpeak, "unit": "TFLOP/s", "frac": ach / tpeak,
+            "kernel": "k_gemm_tn_mma", "shape": "M=%d N=%d K=%d (bf16 in, fp32 accumulate, Y - AB^T epilogue)" % (
+                M, N, K), "us_per_launch": t * 1e6, "peak_source": tpeak_kind}
 
 
 def matvec_roofline(peak, peak_kind, m=14746, n=16384, k=5000, reps=20):
@@ -284,22 +371,64 @@ def matvec_roofline(peak, peak_kind, m=14746, n=16384, k=5000, reps=20):
     return res
 
 
-def bench_plain(args):
-    """Single-trial drop-in on a sample of one wave: gb_cs_generate_and_solve per trial."""
+def bench_plain(args, first_step):
+    """Single-trial FP32 drop-in on samples of the first timed step's trials: independent
+    trials by gb_cs_generate_and_solve (same seeds, so the same problems), shared-matrix
+    trials by gb_cs_solve on the shared A and the trial's y.  The rate is scaled to the
+    3072 + 1024 mix; verdicts are compared with the tuned form's on the same trials."""
+    import torch
+
     import gaga_gb300 as gb
 
-    n, m, k, tid = wave_arrays(args.warmup)
-    step = max(1, len(n) // args.plain_trials)
-    sel = np.arange(0, len(n), step)[: args.plain_trials]
-    ok = 0
+    w, r = first_step
+    n, m, k, tid = wave_arrays(w)
+    cnt = args.plain_trials
+    sel = np.linspace(0, len(n) - 1, cnt).astype(int)
+    ok = agree = 0
     t0 = time.perf_counter()
     for i in sel:
         opts = gb.gaga_options("tol", TOL_REL, "tol_is_relative", 1, "maxiter", MAXITER, "seed", int(SEED + tid[i]))
-        x, xt, r = gb.generate_and_solve("NIHT", "gen", int(k[i]), int(m[i]), int(n[i]), 0, opts)
-        ok += int(r.norms[1] <= 1e-3)
-    dt = time.perf_counter() - t0
-    return {"value": ok / dt, "unit": "trials/s", "trials": int(len(sel)), "recovered": ok, "seconds": dt,
-            "sample": "every %d-th trial of wave %d" % (step, args.warmup)}
+        x, xt, res = gb.generate_and_solve("NIHT", "gen", int(k[i]), int(m[i]), int(n[i]), 0, opts)
+        v = res.norms[1] <= 1e-3
+        ok += int(v)
+        agree += int(v == bool(r["verdict_batch"][i]))
+    t_ind = (time.perf_counter() - t0) / len(sel)
+    ok_ind = ok / len(sel)
+    agree_ind = agree
+    # shared-matrix trials: regenerate the step's problems (same keys) to get A and y
+    ks, first = shared_part(w)
+    _, _, _, ok2, A, Y, X0 = gb.solve_shared_batch(gb.sweep.SHARED_M, gb.sweep.SHARED_N, ks, SHARED_SEED,
+                                                   tol_rel=TOL_REL, maxiter=MAXITER, first_trial=first, outputs=True)
+    torch.cuda.synchronize()
+    X0h = X0.cpu().numpy()
+    sel2 = np.linspace(0, len(ks) - 1, max(4, cnt // 2)).astype(int)
+    ok = agree = 0
+    tt = 0.0
+    for t in sel2:
+        kt = int(np.count_nonzero(X0h[t]))
+        opts = gb.gaga_options("tol", TOL_REL, "tol_is_relative", 1, "maxiter", MAXITER)
+        yt = Y[t].contiguous()
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        x, it, _ = gb.gaga_cs("NIHT", "gen", yt, A.t(), kt, opts)
+        torch.cuda.synchronize()
+        tt += time.perf_counter() - a
+        v = np.linalg.norm(x.cpu().numpy() - X0h[t]) / np.linalg.norm(X0h[t]) <= 1e-3
+        ok += int(v)
+        agree += int(v == bool(ok2[t]))
+    t_sh = tt / len(sel2)
+    ok_sh = ok / len(sel2)
+    n_ind, n_sh = TOTAL - SHARED, SHARED
+    est_time = n_ind * t_ind + n_sh * t_sh
+    est_ok = n_ind * ok_ind + n_sh * ok_sh
+    return {"value": est_ok / est_time, "unit": "trials/s",
+            "independent": {"trials": int(len(sel)), "s_per_trial": t_ind, "recovered_frac": ok_ind,
+                            "verdict_agreement": agree_ind / len(sel)},
+            "shared_matrix": {"trials": int(len(sel2)), "s_per_trial": t_sh, "recovered_frac": ok_sh,
+                              "verdict_agreement": agree / len(sel2)},
+            "verdict_agreement": (agree_ind + agree) / (len(sel) + len(sel2)),
+            "sample": "%d independent + %d shared-matrix trials of step %d, evenly spaced; rate = estimated "
+                      "recovered / estimated time of the 3072 + 1024 sweep" % (len(sel), len(sel2), w)}
 
 
 def main():

@@ -17,7 +17,7 @@ import ctypes as C
 
 import numpy as np
 
-from . import _lib
+from . import _lib, sweep
 from ._lib import GagaError
 
 __all__ = ["gaga_cs", "gaga_options", "GagaError", "solve_batch", "version"]
@@ -262,6 +262,13 @@ def solve_batch(n, m, k, seed, trial_ids=None, alg="NIHT", tol_rel=1e-4, maxiter
     return ns.value, iters, err, ok
 
 
+def batch_slot_count():
+    """Slot streams (one graph launch each) the batched form uses per call."""
+    import os
+
+    return int(os.environ.get("GB_CS_BATCH_SLOTS", "16"))
+
+
 def batch_last_stats():
     """(algorithmic matvec bytes, device ms) of the last solve_batch call."""
     L = _lib.load()
@@ -270,9 +277,11 @@ def batch_last_stats():
     return b.value, t.value
 
 
-def solve_shared_batch(m, n, k, seed, tol_rel=1e-4, maxiter=5000, outputs=False, stream=None):
+def solve_shared_batch(m, n, k, seed, tol_rel=1e-4, maxiter=5000, precision=3, outputs=False, first_trial=0,
+                       stream=None):
     """Shared-matrix batched form (gb_cs_solve_shared_batch): len(k) NIHT trials with one
-    dense Gaussian A, operator work as BF16 tensor-core GEMMs, FP64 debias.
+    dense Gaussian A, operator work as BF16 tensor-core GEMMs, least-squares debias.
+    precision: bit 0 splits A^T r, bit 1 splits A x_thres into BF16 high/low parts.
 
     Returns (num_success, iters, rel_err, ok) and, with outputs=True, also the generated
     A (m x n column-major, as an (n, m) CUDA tensor), Y (T x m) and X0 (T x n) on the device.
@@ -286,8 +295,9 @@ def solve_shared_batch(m, n, k, seed, tol_rel=1e-4, maxiter=5000, outputs=False,
         A = torch.empty((n, m), dtype=torch.float32, device="cuda")
         Y = torch.empty((T, m), dtype=torch.float32, device="cuda")
         X0 = torch.empty((T, n), dtype=torch.float32, device="cuda")
-    b = _lib.SharedBatch(T, int(m), int(n), k.ctypes.data, int(seed) & 0xFFFFFFFF, float(tol_rel), int(maxiter),
-                         None if A is None else A.data_ptr(), None if Y is None else Y.data_ptr(),
+    b = _lib.SharedBatch(T, int(m), int(n), k.ctypes.data, int(seed) & 0xFFFFFFFF, int(first_trial) & 0xFFFFFFFF,
+                         float(tol_rel), int(maxiter),
+                         int(precision), None if A is None else A.data_ptr(), None if Y is None else Y.data_ptr(),
                          None if X0 is None else X0.data_ptr(), stream)
     iters = np.zeros(T, dtype=np.int32)
     err = np.zeros(T, dtype=np.float32)

@@ -59,7 +59,8 @@ class Batch(C.Structure):
 
 class SharedBatch(C.Structure):
     _fields_ = [("ntrials", C.c_int), ("m", C.c_int), ("n", C.c_int), ("k", C.c_void_p), ("seed", C.c_uint),
-                ("tol_rel", C.c_float), ("maxiter", C.c_int), ("d_A_out", C.c_void_p), ("d_Y_out", C.c_void_p),
+                ("first_trial", C.c_uint),
+                ("tol_rel", C.c_float), ("maxiter", C.c_int), ("precision", C.c_int), ("d_A_out", C.c_void_p), ("d_Y_out", C.c_void_p),
                 ("d_X0_out", C.c_void_p), ("stream", C.c_void_p)]
 
 

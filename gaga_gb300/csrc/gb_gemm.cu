@@ -45,18 +45,39 @@ __device__ __forceinline__ void mma_bf16(float *d, const unsigned *a, const unsi
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
-// M % 128 == 0, N % 128 == 0, K % 32 == 0 (the caller pads)
-__global__ void __launch_bounds__(256) k_gemm_tn_mma(const __nv_bfloat16 *__restrict__ A,
-                                                     const __nv_bfloat16 *__restrict__ B, float *__restrict__ Ct,
-                                                     int M, int N, int K, int lda, int ldb,
-                                                     const float *__restrict__ Y, __nv_bfloat16 *__restrict__ Cb) {
+// M % 128 == 0, N % 128 == 0, K % 32 == 0 (the caller pads).
+// Grid: x = M/128 row tiles; y = (N/128 column tiles) x s_max K splits.  With a column map
+// the live column count is read on the device, tiles past it exit at once, and the K
+// split S is chosen from the live tile count so that about two CTAs per SM run; partial
+// tiles then go to a workspace and the last CTA of a tile to arrive sums them in split
+// order (deterministic) and runs the epilogue.
+__global__ void __launch_bounds__(256) k_gemm_tn_mma(GbGemm g, GbGemmWs ws, int s_max) {
   extern __shared__ __align__(16) __nv_bfloat16 gsm[];
   __nv_bfloat16 *As = gsm;                                  // [stage][128][GT_LD]
   __nv_bfloat16 *Bs = gsm + GT_STAGES * GT_M * GT_LD;       // [stage][128][GT_LD]
+  const __nv_bfloat16 *__restrict__ A = (const __nv_bfloat16 *)g.A;
+  const __nv_bfloat16 *__restrict__ B = (const __nv_bfloat16 *)g.B;
+  const int M = g.M, lda = g.lda, ldb = g.ldb;
+  const int *__restrict__ nmap = g.nmap;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int wm = warp >> 2, wn = warp & 3;  // 2 x 4 warps, warp tile 64 x 32
-  const int m0 = blockIdx.x * GT_M, n0 = blockIdx.y * GT_N;
-  const int nk = K / GT_K;
+  const int mt = blockIdx.x, mtiles = gridDim.x;
+  const int nti = blockIdx.y / s_max, sp = blockIdx.y % s_max;
+  const int m0 = mt * GT_M, n0 = nti * GT_N;
+  const int nk = g.K / GT_K;
+  // with a column map, tile columns c < *ncount are B rows / Ct columns nmap[c]
+  const int cnt = g.ncount ? *g.ncount : g.N;
+  if (n0 >= cnt) return;
+  int S = 1;
+  if (s_max > 1) {
+    const int tiles = mtiles * ((cnt + GT_N - 1) / GT_N);
+    S = max(1, min(min(s_max, nk), (2 * ws.num_sms) / tiles));
+    if (S * tiles > ws.part_tiles) S = 1;
+  }
+  if (sp >= S) return;
+  const int kb = (int)((long long)sp * nk / S), ke = (int)((long long)(sp + 1) * nk / S);
+  const int br0 = nmap ? nmap[min(n0 + (tid >> 2), cnt - 1)] : n0 + (tid >> 2);
+  const int br1 = nmap ? nmap[min(n0 + (tid >> 2) + 64, cnt - 1)] : n0 + (tid >> 2) + 64;
   float acc[4][4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
@@ -70,21 +91,22 @@ __global__ void __launch_bounds__(256) k_gemm_tn_mma(const __nv_bfloat16 *__rest
       const int q = tid + c * 256;  // 512 chunks of 16 bytes per operand
       const int row = q >> 2, col = (q & 3) * 8;
       cp_async16(As + (st * GT_M + row) * GT_LD + col, A + (size_t)(m0 + row) * lda + k0 + col);
-      cp_async16(Bs + (st * GT_N + row) * GT_LD + col, B + (size_t)(n0 + row) * ldb + k0 + col);
+      cp_async16(Bs + (st * GT_N + row) * GT_LD + col, B + (size_t)(c ? br1 : br0) * ldb + k0 + col);
     }
   };
 
+  const int nkl = ke - kb;
   for (int s = 0; s < GT_STAGES - 1; ++s) {
-    if (s < nk) load_stage(s, s);
+    if (s < nkl) load_stage(s, kb + s);
     cp_async_commit();
   }
-  for (int kt = 0; kt < nk; ++kt) {
+  for (int it = 0; it < nkl; ++it) {
     cp_async_wait<GT_STAGES - 2>();
     __syncthreads();
-    const int nxt = kt + GT_STAGES - 1;
-    if (nxt < nk) load_stage(nxt % GT_STAGES, nxt);
+    const int nxt = it + GT_STAGES - 1;
+    if (nxt < nkl) load_stage(nxt % GT_STAGES, kb + nxt);
     cp_async_commit();
-    const int st = kt % GT_STAGES;
+    const int st = it % GT_STAGES;
     const __nv_bfloat16 *as = As + st * GT_M * GT_LD;
     const __nv_bfloat16 *bs = Bs + st * GT_N * GT_LD;
 #pragma unroll
@@ -114,29 +136,81 @@ __global__ void __launch_bounds__(256) k_gemm_tn_mma(const __nv_bfloat16 *__rest
     }
   }
   cp_async_wait<0>();
+  if (S > 1) {
+    // publish this split's partial tile (fragment-major: element e of thread tid at e*256+tid)
+    __shared__ int last;
+    float *mine = ws.part + ((size_t)(nti * S + sp) * mtiles + mt) * (GT_M * GT_N);
+#pragma unroll
+    for (int mi = 0; mi < 4; ++mi)
+#pragma unroll
+      for (int ni = 0; ni < 4; ++ni)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) __stcg(mine + ((mi * 4 + ni) * 4 + e) * 256 + tid, acc[mi][ni][e]);
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) last = atomicAdd(&ws.tickets[nti * mtiles + mt], 1u) == (unsigned)(S - 1);
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+#pragma unroll
+    for (int mi = 0; mi < 4; ++mi)
+#pragma unroll
+      for (int ni = 0; ni < 4; ++ni)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) acc[mi][ni][e] = 0.0f;
+    for (int s2 = 0; s2 < S; ++s2) {
+      const float *src = ws.part + ((size_t)(nti * S + s2) * mtiles + mt) * (GT_M * GT_N);
+#pragma unroll
+      for (int mi = 0; mi < 4; ++mi)
+#pragma unroll
+        for (int ni = 0; ni < 4; ++ni)
+#pragma unroll
+          for (int e = 0; e < 4; ++e) acc[mi][ni][e] += __ldcg(src + ((mi * 4 + ni) * 4 + e) * 256 + tid);
+    }
+    if (tid == 0) ws.tickets[nti * mtiles + mt] = 0u;
+  }
   // epilogue: element (row, col) of C goes to Ct[col * M + row]
-  const int g = lane >> 2, tq = lane & 3;
+  const int gq = lane >> 2, tq = lane & 3;
+  __nv_bfloat16 *Cb = (__nv_bfloat16 *)g.Cb;
 #pragma unroll
   for (int mi = 0; mi < 4; ++mi)
 #pragma unroll
     for (int ni = 0; ni < 4; ++ni)
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
-        const int row = m0 + wm * 64 + mi * 16 + g + (e >> 1) * 8;
-        const int col = n0 + wn * 32 + ni * 8 + tq * 2 + (e & 1);
+        const int row = m0 + wm * 64 + mi * 16 + gq + (e >> 1) * 8;
+        int col = n0 + wn * 32 + ni * 8 + tq * 2 + (e & 1);
+        if (col >= cnt) continue;
+        if (nmap) col = nmap[col];
         const size_t o = (size_t)col * M + row;
-        const float v = Y ? Y[o] - acc[mi][ni][e] : acc[mi][ni][e];
-        Ct[o] = v;
-        if (Cb) Cb[o] = __float2bfloat16_rn(v);
+        const float v = g.Y ? g.Y[o] - acc[mi][ni][e] : acc[mi][ni][e];
+        g.Ct[o] = v;
+        if (Cb) {
+          const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+          if (g.cb_split) {  // column of 3M: [hi ; hi ; lo]
+            const size_t q = (size_t)col * 3 * M + row;
+            Cb[q] = hi;
+            Cb[q + M] = hi;
+            Cb[q + 2 * (size_t)M] = __float2bfloat16_rn(v - __bfloat162float(hi));
+          } else {
+            Cb[o] = hi;
+          }
+        }
       }
 }
 
-gb_status gb_gemm_tn(const void *A, const void *B, float *Ct, int M, int N, int K, int lda, int ldb, const float *Y,
-                     void *Cb, cudaStream_t s) {
-  if (M % GT_M || N % GT_N || K % GT_K || M <= 0 || N <= 0 || K <= 0 || lda < K || ldb < K || lda % 8 || ldb % 8) {
+gb_status gb_gemm(const GbGemm &g, cudaStream_t s) {
+  if (g.M % GT_M || g.N % GT_N || g.K % GT_K || g.M <= 0 || g.N <= 0 || g.K <= 0 || g.lda < g.K || g.ldb < g.K ||
+      g.lda % 8 || g.ldb % 8) {
     gb_set_error_message("GEMM sizes must be multiples of 128 (M, N) and 32 (K); strides multiples of 8", __FILE__,
                          __LINE__);
     return GB_BAD_ARG;
+  }
+  GbGemmWs ws = {};
+  int s_max = 1;
+  if (g.ws && g.ws->part && g.ws->tickets && (g.M / GT_M) * (g.N / GT_N) <= g.ws->ticket_count) {
+    ws = *g.ws;
+    s_max = GB_GEMM_SPLIT_MAX;
   }
   const int smem = GT_STAGES * (GT_M + GT_N) * GT_LD * 2;
   static bool attr = false;
@@ -144,9 +218,8 @@ gb_status gb_gemm_tn(const void *A, const void *B, float *Ct, int M, int N, int 
     GB_CUDA_TRY(cudaFuncSetAttribute(k_gemm_tn_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     attr = true;
   }
-  dim3 grid(M / GT_M, N / GT_N);
-  k_gemm_tn_mma<<<grid, 256, smem, s>>>((const __nv_bfloat16 *)A, (const __nv_bfloat16 *)B, Ct, M, N, K, lda, ldb,
-                                        Y, (__nv_bfloat16 *)Cb);
+  dim3 grid(g.M / GT_M, (g.N / GT_N) * s_max);
+  k_gemm_tn_mma<<<grid, 256, smem, s>>>(g, ws, s_max);
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
 }
@@ -157,5 +230,7 @@ extern "C" gb_status gb_cs_gemm_bf16_tn(const void *d_A, const void *d_B, float 
     gb_set_error_message("gb_cs_gemm_bf16_tn: null buffer", __FILE__, __LINE__);
     return GB_BAD_ARG;
   }
-  return gb_gemm_tn(d_A, d_B, d_Ct, M, N, K, K, K, d_Y, d_Cb, (cudaStream_t)stream);
+  GbGemm g = {};
+  g.A = d_A; g.B = d_B; g.Ct = d_Ct; g.M = M; g.N = N; g.K = K; g.lda = K; g.ldb = K; g.Y = d_Y; g.Cb = d_Cb;
+  return gb_gemm(g, (cudaStream_t)stream);
 }

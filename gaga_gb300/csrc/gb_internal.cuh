@@ -233,9 +233,29 @@ void enq_AT_mask(GbWork &w, cudaStream_t s, const float *r, float *g, float *xt,
 void gb_dense_av_shape(int m, int num_sms, int *ntile, int *nsplit);
 size_t gb_dense_part_floats_av(int ntile, int nsplit);
 
-// BF16 TN GEMM (gb_gemm.cu): Ct[N x M] = [Y -] (A[M x K] B[N x K]^T)^T, row strides lda, ldb
-gb_status gb_gemm_tn(const void *A, const void *B, float *Ct, int M, int N, int K, int lda, int ldb, const float *Y,
-                     void *Cb, cudaStream_t s);
+// BF16 TN GEMM with FP32 accumulation (gb_gemm.cu):
+//   Ct[N x M] = [Y -] (A[M x K] . B[N x K]^T)^T,  A, B row-major with row strides lda, ldb,
+// optional BF16 copy Cb of Ct, or with cb_split its split [hi ; hi ; lo] (3M per column).
+// With a device column map only columns c < *ncount are computed and column c stands for
+// B row / Ct column nmap[c] (the batched form passes its list of active trials).  With a
+// workspace, K is split over CTAs when the live tiles would leave SMs idle.
+#define GB_GEMM_SPLIT_MAX 8
+struct GbGemmWs {
+  float *part;            // partial 128 x 128 tiles
+  unsigned int *tickets;  // one per output tile, zero between launches
+  int part_tiles, ticket_count, num_sms;
+};
+struct GbGemm {
+  const void *A, *B;
+  float *Ct;
+  int M, N, K, lda, ldb;
+  const float *Y;
+  void *Cb;
+  int cb_split;
+  const int *nmap, *ncount;
+  const GbGemmWs *ws;
+};
+gb_status gb_gemm(const GbGemm &g, cudaStream_t s);
 
 // solver (gb_solver.cu)
 enum { GB_RUN_SOLVE = 0, GB_RUN_L0 = 1 };

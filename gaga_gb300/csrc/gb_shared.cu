@@ -12,11 +12,13 @@
 // logic (gb_ctrl.cuh), the restriction to the support, the update, LinearBinning and the
 // k-th bin -- runs in one CTA per trial.  The loop is a CUDA graph WHILE node that runs
 // while any trial is active.  Trials that stop with ||y - A x|| <= tol are then debiased:
-// least squares on their final support by conjugate gradients on the normal equations in
-// FP64 with the FP32 A.  The verdict is the relative l2 error against the planted x0.
+// least squares on their final support by conjugate gradients on the normal equations,
+// again as split-precision GEMMs over all trials, with the CG scalars in FP64 (FP64
+// arithmetic is a small fraction of the FP32 rate on this part, so no product runs in
+// it).  The verdict is the relative l2 error against the planted x0.
 //
 // The shared A is drawn from `seed` exactly as gb_cs_generate_and_solve draws it; trial
-// t's x0 uses the key seed + 1 + t.
+// t's x0 uses the key seed + 1 + first_trial + t.
 #include <cuda_bf16.h>
 #include <stdlib.h>
 #include <string.h>
@@ -28,23 +30,29 @@
 #include "gb_philox.cuh"
 
 #define SH_THREADS 256
+#define SH_CG_MAX 20       // debias iterations
 #define SH_NBINS_MAX 1640  // num_bins = max(n/20, 1000) <= 1638 for n <= 32768
 
 namespace {
 
 struct ShDev {
   int m, n, T, Tp, maxiter;
+  int kg, kq;               // K of the A^T r and A x_thres products (m or 3m, n or 3n)
+  double *flops;            // algorithmic GEMM flops of all trials
+  int prec;                 // bit 0: split A^T r; bit 1: split A x_thres (else BF16 operands)
   float tol_rel;
-  unsigned int seed;
+  unsigned int seed, first;
   const int *kreq;
   float *A32;               // m x n column-major (lda = m)
   __nv_bfloat16 *Acat;      // m x 3n row-major: [A_hi | A_lo | A_hi]
-  __nv_bfloat16 *AThi;      // n x m row-major (A column-major) in BF16
+  __nv_bfloat16 *ATcat;     // n x 3m row-major: [A_hi^T | A_lo^T | A_hi^T]
   float *X0, *X, *G, *Y, *R, *Q;
-  __nv_bfloat16 *Xcat, *XTbf, *Rbf;  // Tp x 3n, Tp x n, Tp x m
+  __nv_bfloat16 *Xcat, *XTbf, *Rbf;  // Tp x 3n, Tp x 3n (x_thres, split or not), Tp x m
   int *bins;
   GbState *st;
-  double *scr;              // debias scratch, Tp x (3n + 2m)
+  float *P;                 // debias search directions, Tp x n
+  __nv_bfloat16 *Rcat;      // debias residual split, Tp x 3m
+  int *act, *act_cnt;       // trials still iterating (ascending) and their count
   int *iters;
   float *err;
   int *ok;
@@ -57,17 +65,21 @@ __global__ void k_sh_genA(float *A32, int m, int n, uint32_t seed) {
   for (int j = gw; j < n; j += nw) gbgen::gen_dense_column(A32 + (size_t)j * m, j, m, seed, 0u, 1, lane, 32);
 }
 
-// BF16 operands: AThi (column-major A in BF16) and Acat rows [hi | lo | hi] through a
-// 32x32 shared-memory transpose
+// BF16 operands: rows [hi | lo | hi] of A (Acat, through a 32x32 shared-memory transpose)
+// and of A^T (ATcat, straight from the column-major A)
 __global__ void k_sh_split(const float *__restrict__ A32, __nv_bfloat16 *__restrict__ Acat,
-                           __nv_bfloat16 *__restrict__ AThi, int m, int n) {
+                           __nv_bfloat16 *__restrict__ ATcat, int m, int n) {
   __shared__ float tile[32][33];
   const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
   for (int r = threadIdx.y; r < 32; r += 8) {
     const int j = j0 + r, i = i0 + threadIdx.x;
     const float v = A32[(size_t)j * m + i];
     tile[r][threadIdx.x] = v;
-    AThi[(size_t)j * m + i] = __float2bfloat16_rn(v);
+    const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+    const size_t row = (size_t)j * 3 * m;
+    ATcat[row + i] = hi;
+    ATcat[row + m + i] = __float2bfloat16_rn(v - __bfloat162float(hi));
+    ATcat[row + 2 * m + i] = hi;
   }
   __syncthreads();
   for (int r = threadIdx.y; r < 32; r += 8) {
@@ -203,7 +215,7 @@ __global__ void __launch_bounds__(SH_THREADS) k_sh_genx(ShDev d) {
     for (int j = threadIdx.x; j < n; j += SH_THREADS) x0[j] = 0.0f;
     return;
   }
-  const uint32_t key = d.seed + 1u + (uint32_t)t;
+  const uint32_t key = d.seed + 1u + d.first + (uint32_t)t;
   float mx = 0.0f;
   for (int j = threadIdx.x; j < n; j += SH_THREADS) {
     const float u = gbgen::uniform_at(key, 0u, gbgen::ST_VALUES, (uint64_t)j);
@@ -241,7 +253,11 @@ __global__ void __launch_bounds__(SH_THREADS) k_sh_y(ShDev d) {
   __nv_bfloat16 *ybf = d.Rbf + (size_t)t * m;
   GbState *st = d.st + t;
   if (t >= d.T) {
-    for (int i = threadIdx.x; i < m; i += SH_THREADS) { y[i] = 0.0f; ybf[i] = __float2bfloat16_rn(0.0f); }
+    for (int i = threadIdx.x; i < m; i += SH_THREADS) {
+      y[i] = 0.0f;
+      ybf[i] = __float2bfloat16_rn(0.0f);
+      for (int c = 0; c < 3; ++c) d.Rcat[(size_t)t * 3 * m + c * m + i] = __float2bfloat16_rn(0.0f);
+    }
     if (threadIdx.x == 0) { memset(st, 0, sizeof(GbState)); st->active = 0; }
     return;
   }
@@ -275,7 +291,12 @@ __global__ void __launch_bounds__(SH_THREADS) k_sh_y(ShDev d) {
       acc = acc + d.A32[(size_t)j * m + i] * x0[j];
     }
     y[i] = acc;
-    ybf[i] = __float2bfloat16_rn(acc);
+    const __nv_bfloat16 hi = __float2bfloat16_rn(acc);
+    ybf[i] = hi;
+    __nv_bfloat16 *yc = d.Rcat + (size_t)t * 3 * m;
+    yc[i] = hi;
+    yc[m + i] = hi;
+    yc[2 * m + i] = __float2bfloat16_rn(acc - __bfloat162float(hi));
     y2 += (double)acc * (double)acc;
   }
   const double ys = cta_sumd(y2, smd);
@@ -344,13 +365,20 @@ __global__ void __launch_bounds__(SH_THREADS) k_sh_mask(ShDev d) {
   }
   const float *g = d.G + (size_t)t * n;
   const int *bins = d.bins + (size_t)t * n;
-  __nv_bfloat16 *xt = d.XTbf + (size_t)t * n;
   const int kb = st->k_bin;
   float s2 = 0.0f, gm = 0.0f;
   for (int j = threadIdx.x; j < n; j += SH_THREADS) {
     const float v = g[j];
     const float o = bins[j] <= kb ? v : 0.0f;
-    xt[j] = __float2bfloat16_rn(o);
+    const __nv_bfloat16 hi = __float2bfloat16_rn(o);
+    if (d.prec & 2) {
+      __nv_bfloat16 *xt = d.XTbf + (size_t)t * 3 * n;
+      xt[j] = hi;
+      xt[n + j] = hi;
+      xt[2 * n + j] = __float2bfloat16_rn(o - __bfloat162float(hi));
+    } else {
+      d.XTbf[(size_t)t * n + j] = hi;
+    }
     s2 = fmaf(o, o, s2);
     gm = fmaxf(gm, fabsf(v));
   }
@@ -400,115 +428,160 @@ __global__ void __launch_bounds__(SH_THREADS) k_sh_step(ShDev d) {
   }
 }
 
-// loop condition: any trial still active; bounded by maxiter + 4 passes
-__global__ void k_sh_any(ShDev d, int *passes, cudaGraphConditionalHandle h) {
-  __shared__ int any;
-  if (threadIdx.x == 0) any = 0;
+// Ordered list of the trials still iterating (NIHT: active; debias: F_CG) for the GEMMs'
+// column maps, and the loop condition: any trial left (NIHT also bounded by maxiter + 4
+// passes).  One block of 1024 threads, each owning a contiguous run of trials.
+__global__ void __launch_bounds__(1024) k_sh_list(ShDev d, int which, int *passes, cudaGraphConditionalHandle h) {
+  __shared__ int wsum[32];
+  const int T = d.T, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int per = (T + 1023) / 1024, b0 = min(tid * per, T), b1 = min(b0 + per, T);
+  auto on = [&](int t) { return which == 0 ? d.st[t].active != 0 : d.st[t].flags[F_CG] != 0; };
+  int c = 0;
+  for (int t = b0; t < b1; ++t) c += on(t) ? 1 : 0;
+  int incl = c;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  if (lane == 31) wsum[w] = incl;
   __syncthreads();
-  int a = 0;
-  for (int t = threadIdx.x; t < d.T; t += blockDim.x) a |= d.st[t].active;
-  if (a) atomicOr(&any, 1);
+  if (w == 0) {
+    int v = wsum[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += u;
+    }
+    wsum[lane] = v;  // inclusive warp totals
+  }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    const int p = ++passes[0];
-    cudaGraphSetConditional(h, (any && p <= d.maxiter + 4) ? 1u : 0u);
+  int pos = incl - c + (w > 0 ? wsum[w - 1] : 0);
+  for (int t = b0; t < b1; ++t)
+    if (on(t)) d.act[pos++] = t;
+  if (tid == 0) {
+    const int total = wsum[31];
+    *d.act_cnt = total;
+    unsigned go = total > 0 ? 1u : 0u;
+    if (which == 0) {
+      const int p = ++passes[0];
+      if (p > d.maxiter + 4) go = 0u;
+    }
+    if (h) cudaGraphSetConditional(h, go);
   }
 }
 
 // ------------------------------------------------------------------ debias and verdict
-// Least squares on the final support of a trial that reached ||y - A x|| <= tol: CG on
-// the normal equations in FP64 (A in FP32), from the NIHT solution; then the relative l2
-// error against x0 (GAGA/gaga/results.cu:468-475).
-__global__ void __launch_bounds__(SH_THREADS) k_sh_final(ShDev d, int debias) {
-  extern __shared__ int ssup[];
+// Least squares on the final support of every trial that reached ||y - A x|| <= tol:
+// conjugate gradients on the normal equations A_S^T A_S z = A_S^T y started from the NIHT
+// solution (CGNR).  The products of all trials run in lockstep as split-precision GEMMs
+//   q = [A_hi | A_lo | A_hi] . [p_hi ; p_hi ; p_lo]      g = [A_hi^T | A_lo^T | A_hi^T] . [r_hi ; r_hi ; r_lo]
+// (FP32 accumulation, ~2^-17 relative error); the scalars are kept in FP64 and r is
+// updated recursively in FP32.  A trial leaves the loop when ||A_S^T r||^2 <= 1e-12 of its
+// starting value or after SH_CG_MAX iterations.
+
+// trials that reached the residual tolerance enter the debias
+__global__ void k_cg_flags(ShDev d) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= d.T) return;
+  GbState *st = d.st + t;
+  st->flags[F_CG] = st->stop_reason == 1 ? 1 : 0;
+  st->it_cg = 0;
+}
+
+// r = y - A x from the last residual GEMM; split r for the A^T product
+__global__ void __launch_bounds__(SH_THREADS) k_cg_start(ShDev d) {
+  const int t = blockIdx.x, m = d.m;
+  GbState *st = d.st + t;
+  const bool on = t < d.T && st->flags[F_CG];
+  const float *r = d.R + (size_t)t * m;
+  __nv_bfloat16 *rc = d.Rcat + (size_t)t * 3 * m;
+  for (int i = threadIdx.x; i < m; i += SH_THREADS) {
+    const float v = on ? r[i] : 0.0f;
+    const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+    rc[i] = hi;
+    rc[m + i] = hi;
+    rc[2 * m + i] = __float2bfloat16_rn(v - __bfloat162float(hi));
+  }
+}
+
+// g = P_S A^T r ; gamma = ||g||^2 ; p = g + beta p ; convergence test ; split p
+__global__ void __launch_bounds__(SH_THREADS) k_cg_dir(ShDev d) {
   __shared__ double smd[32];
-  __shared__ int cnt_s;
+  const int t = blockIdx.x, n = d.n;
+  if (t >= d.T) return;
+  GbState *st = d.st + t;
+  if (!st->flags[F_CG]) return;
+  const float *g = d.G + (size_t)t * n;
+  const int *bins = d.bins + (size_t)t * n;
+  const int kb = st->k_bin;
+  double gg = 0.0;
+  for (int j = threadIdx.x; j < n; j += SH_THREADS) {
+    const double v = bins[j] <= kb ? (double)g[j] : 0.0;
+    gg += v * v;
+  }
+  gg = cta_sumd(gg, smd);
+  const int it = st->it_cg;
+  const double gamma_prev = st->red[R_DOT1];
+  if (it == 0) st->red[R_DOT2] = gg;  // every thread reads the same values before this
+  const double gamma0 = it == 0 ? gg : st->red[R_DOT2];
+  const bool go = it < SH_CG_MAX && gg > 1e-12 * gamma0 && gg > 0.0;
+  const float beta = it == 0 ? 0.0f : (float)(gg / gamma_prev);
+  float *p = d.P + (size_t)t * n;
+  __nv_bfloat16 *pc = d.Xcat + (size_t)t * 3 * n;
+  if (go) {
+    for (int j = threadIdx.x; j < n; j += SH_THREADS) {
+      const float v = bins[j] <= kb ? fmaf(beta, it == 0 ? 0.0f : p[j], g[j]) : 0.0f;
+      p[j] = v;
+      const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+      pc[j] = hi;
+      pc[n + j] = hi;
+      pc[2 * n + j] = __float2bfloat16_rn(v - __bfloat162float(hi));
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    st->red[R_DOT1] = gg;
+    st->flags[F_CG] = go ? 1 : 0;
+  }
+}
+
+// alpha = gamma / ||q||^2 ; x += alpha p ; r -= alpha q ; split r
+__global__ void __launch_bounds__(SH_THREADS) k_cg_step(ShDev d) {
+  __shared__ double smd[32];
   const int t = blockIdx.x, n = d.n, m = d.m;
   if (t >= d.T) return;
   GbState *st = d.st + t;
+  if (!st->flags[F_CG]) return;
+  const float *q = d.Q + (size_t)t * m;
+  double qq = 0.0;
+  for (int i = threadIdx.x; i < m; i += SH_THREADS) qq += (double)q[i] * (double)q[i];
+  qq = cta_sumd(qq, smd);
+  const float alpha = qq > 0.0 ? (float)(st->red[R_DOT1] / qq) : 0.0f;
   float *x = d.X + (size_t)t * n;
-  const float *x0 = d.X0 + (size_t)t * n;
-  const float *y = d.Y + (size_t)t * m;
-  const bool converged = st->stop_reason == 1;
-  if (debias && converged) {
-    if (threadIdx.x == 0) cnt_s = 0;
-    __syncthreads();
-    __shared__ int wcnt[SH_THREADS / 32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int j0 = 0; j0 < n; j0 += SH_THREADS) {
-      const int j = j0 + threadIdx.x;
-      const bool in = j < n && x[j] != 0.0f;
-      const unsigned bal = __ballot_sync(0xffffffffu, in);
-      if (lane == 0) wcnt[w] = __popc(bal);
-      __syncthreads();
-      int wb = 0, tot = 0;
-      for (int q = 0; q < SH_THREADS / 32; ++q) {
-        if (q < w) wb += wcnt[q];
-        tot += wcnt[q];
-      }
-      if (in) ssup[cnt_s + wb + __popc(bal & ((1u << lane) - 1u))] = j;
-      __syncthreads();
-      if (threadIdx.x == 0) cnt_s += tot;
-      __syncthreads();
-    }
-    const int s = cnt_s;
-    double *z = d.scr + (size_t)t * (3 * (size_t)n + 2 * (size_t)m);
-    double *p = z + n, *g = p + n, *r = g + n, *q = r + m;
-    const float *A = d.A32;
-    for (int c = threadIdx.x; c < s; c += SH_THREADS) z[c] = x[ssup[c]];
-    __syncthreads();
-    // r = y - A_S z
-    for (int i = threadIdx.x; i < m; i += SH_THREADS) {
-      double a = 0.0;
-      for (int c = 0; c < s; ++c) a += (double)A[(size_t)ssup[c] * m + i] * z[c];
-      r[i] = (double)y[i] - a;
-    }
-    __syncthreads();
-    auto atr = [&](double *out) {  // out = A_S^T r, one warp per support column
-      for (int c = w; c < s; c += SH_THREADS / 32) {
-        const float *col = A + (size_t)ssup[c] * m;
-        double a = 0.0;
-        for (int i = lane; i < m; i += 32) a += (double)col[i] * r[i];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-        if (lane == 0) out[c] = a;
-      }
-      __syncthreads();
-    };
-    atr(g);
-    double gg = 0.0;
-    for (int c = threadIdx.x; c < s; c += SH_THREADS) {
-      p[c] = g[c];
-      gg += g[c] * g[c];
-    }
-    gg = cta_sumd(gg, smd);
-    const double gg0 = gg;
-    for (int it = 0; it < 30 && gg > 1e-24 * gg0 && gg > 0.0; ++it) {
-      double qq = 0.0;
-      for (int i = threadIdx.x; i < m; i += SH_THREADS) {
-        double a = 0.0;
-        for (int c = 0; c < s; ++c) a += (double)A[(size_t)ssup[c] * m + i] * p[c];
-        q[i] = a;
-        qq += a * a;
-      }
-      qq = cta_sumd(qq, smd);
-      if (!(qq > 0.0)) break;
-      const double alpha = gg / qq;
-      for (int c = threadIdx.x; c < s; c += SH_THREADS) z[c] += alpha * p[c];
-      for (int i = threadIdx.x; i < m; i += SH_THREADS) r[i] -= alpha * q[i];
-      __syncthreads();
-      atr(g);
-      double gn = 0.0;
-      for (int c = threadIdx.x; c < s; c += SH_THREADS) gn += g[c] * g[c];
-      gn = cta_sumd(gn, smd);
-      const double beta = gn / gg;
-      for (int c = threadIdx.x; c < s; c += SH_THREADS) p[c] = g[c] + beta * p[c];
-      gg = gn;
-      __syncthreads();
-    }
-    for (int c = threadIdx.x; c < s; c += SH_THREADS) x[ssup[c]] = (float)z[c];
-    __syncthreads();
+  const float *p = d.P + (size_t)t * n;
+  for (int j = threadIdx.x; j < n; j += SH_THREADS) x[j] = fmaf(alpha, p[j], x[j]);
+  float *r = d.R + (size_t)t * m;
+  __nv_bfloat16 *rc = d.Rcat + (size_t)t * 3 * m;
+  for (int i = threadIdx.x; i < m; i += SH_THREADS) {
+    const float v = fmaf(-alpha, q[i], r[i]);
+    r[i] = v;
+    const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+    rc[i] = hi;
+    rc[m + i] = hi;
+    rc[2 * m + i] = __float2bfloat16_rn(v - __bfloat162float(hi));
   }
+  __syncthreads();
+  if (threadIdx.x == 0) st->it_cg++;
+}
+
+// relative l2 error against x0 (GAGA/gaga/results.cu:468-475) and the verdict
+__global__ void __launch_bounds__(SH_THREADS) k_sh_verdict(ShDev d) {
+  __shared__ double smd[32];
+  const int t = blockIdx.x, n = d.n;
+  if (t >= d.T) return;
+  const float *x = d.X + (size_t)t * n;
+  const float *x0 = d.X0 + (size_t)t * n;
   double e2 = 0.0, x2 = 0.0;
   for (int j = threadIdx.x; j < n; j += SH_THREADS) {
     const double df = (double)x0[j] - (double)x[j];
@@ -519,9 +592,15 @@ __global__ void __launch_bounds__(SH_THREADS) k_sh_final(ShDev d, int debias) {
   x2 = cta_sumd(x2, smd);
   if (threadIdx.x == 0) {
     const float rel = (float)(sqrt(e2) / sqrt(x2));
+    const GbState *st = d.st + t;
     d.iters[t] = st->iter;
     d.err[t] = rel;
     d.ok[t] = rel <= 1e-3f ? 1 : 0;
+    // GEMM flops this trial used: the initial A^T y, each NIHT iteration, and the debias
+    const double mn3 = 3.0 * d.m * (double)d.n;
+    double f = 2.0 * d.n * (double)d.kg + st->iter * 2.0 * (mn3 + (double)d.n * d.kg + (double)d.m * d.kq);
+    if (st->stop_reason == 1) f += (2.0 + st->it_cg) * 2.0 * mn3 * 2.0;
+    atomicAdd(d.flops, f);
   }
 }
 
@@ -548,7 +627,7 @@ static thread_local double g_sh_gemm_flops = 0.0;
 extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *iters_out, float *rel_err_out,
                                               int *success_out, int *num_success) {
   if (!b || !b->k || b->ntrials < 1 || b->m < 128 || b->n < 128 || b->m % 128 || b->n % 128 || b->m > b->n ||
-      b->n > 32768 || b->maxiter < 0) {
+      b->n > 32768 || b->maxiter < 0 || b->precision < 0 || b->precision > 3) {
     gb_set_error_message("shared batch: m, n multiples of 128 with 128 <= m <= n <= 32768, ntrials >= 1", __FILE__,
                          __LINE__);
     return GB_BAD_ARG;
@@ -564,43 +643,77 @@ extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *ite
   ShDev d;
   memset(&d, 0, sizeof(d));
   d.m = m; d.n = n; d.T = T; d.Tp = Tp; d.maxiter = b->maxiter; d.tol_rel = b->tol_rel; d.seed = b->seed;
+  d.prec = b->precision;
+  d.first = b->first_trial;
+  const int kg = (d.prec & 1) ? 3 * m : m, kq = (d.prec & 2) ? 3 * n : n;  // K of A^T r and A x_thres
+  d.kg = kg;
+  d.kq = kq;
   int *dk;
   GB_TRY(buf.get(&dk, T));
   GB_CUDA_TRY(cudaMemcpyAsync(dk, b->k, sizeof(int) * T, cudaMemcpyHostToDevice, s));
   d.kreq = dk;
   GB_TRY(buf.get(&d.A32, (size_t)m * n));
   GB_TRY(buf.get(&d.Acat, (size_t)m * 3 * n));
-  GB_TRY(buf.get(&d.AThi, (size_t)n * m));
+  GB_TRY(buf.get(&d.ATcat, (size_t)n * 3 * m));
   for (float **v : {&d.X0, &d.X, &d.G}) GB_TRY(buf.get(v, (size_t)Tp * n));
   for (float **v : {&d.Y, &d.R, &d.Q}) GB_TRY(buf.get(v, (size_t)Tp * m));
   GB_TRY(buf.get(&d.Xcat, (size_t)Tp * 3 * n));
-  GB_TRY(buf.get(&d.XTbf, (size_t)Tp * n));
+  GB_TRY(buf.get(&d.XTbf, (size_t)Tp * 3 * n));
   GB_TRY(buf.get(&d.Rbf, (size_t)Tp * m));
   GB_TRY(buf.get(&d.bins, (size_t)Tp * n));
   GB_TRY(buf.get(&d.st, (size_t)Tp));
-  GB_TRY(buf.get(&d.scr, (size_t)Tp * (3 * (size_t)n + 2 * (size_t)m)));
+  GB_TRY(buf.get(&d.P, (size_t)Tp * n));
+  GB_TRY(buf.get(&d.Rcat, (size_t)Tp * 3 * m));
   GB_TRY(buf.get(&d.iters, T));
   GB_TRY(buf.get(&d.err, T));
   GB_TRY(buf.get(&d.ok, T));
   int *passes;
   GB_TRY(buf.get(&passes, 1));
+  GB_TRY(buf.get(&d.act, Tp));
+  GB_TRY(buf.get(&d.act_cnt, 1));
+  GB_TRY(buf.get(&d.flops, 1));
+  GB_CUDA_TRY(cudaMemsetAsync(d.flops, 0, sizeof(double), s));
+  // split-K workspace of the GEMMs over the active trials (they run one after another)
+  int dev = 0, sms = 0;
+  GB_CUDA_TRY(cudaGetDevice(&dev));
+  GB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  GbGemmWs ws = {};
+  ws.num_sms = sms;
+  ws.part_tiles = 2 * sms;
+  ws.ticket_count = (n / 128) * (Tp / 128);
+  GB_TRY(buf.get(&ws.part, (size_t)ws.part_tiles * 128 * 128));
+  GB_TRY(buf.get(&ws.tickets, ws.ticket_count));
+  GB_CUDA_TRY(cudaMemsetAsync(ws.tickets, 0, sizeof(unsigned) * ws.ticket_count, s));
+  // Ct[Tp x M] = [Y -] A . B^T over all trials, or over the listed ones (mapped)
+  auto gemm = [&](const void *A, const void *B, float *C, int M, int K, int lda, int ldb, const float *Y, void *Cb,
+                  int split, bool mapped, cudaStream_t st) {
+    GbGemm g = {};
+    g.A = A; g.B = B; g.Ct = C; g.M = M; g.N = Tp; g.K = K; g.lda = lda; g.ldb = ldb; g.Y = Y; g.Cb = Cb;
+    g.cb_split = split;
+    if (mapped) {
+      g.nmap = d.act;
+      g.ncount = d.act_cnt;
+      g.ws = &ws;
+    }
+    return gb_gemm(g, st);
+  };
   GB_CUDA_TRY(cudaMemsetAsync(passes, 0, sizeof(int), s));
   GB_CUDA_TRY(cudaMemsetAsync(d.st, 0, sizeof(GbState) * Tp, s));
   const int smem_n = n * (int)sizeof(int);
   GB_CUDA_TRY(cudaFuncSetAttribute(k_sh_genx, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_n));
   GB_CUDA_TRY(cudaFuncSetAttribute(k_sh_y, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_n));
-  GB_CUDA_TRY(cudaFuncSetAttribute(k_sh_final, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_n));
   cudaEvent_t e0, e1;
   GB_CUDA_TRY(cudaEventCreate(&e0));
   GB_CUDA_TRY(cudaEventCreate(&e1));
   GB_CUDA_TRY(cudaEventRecord(e0, s));
   // ---- problem and operands
   k_sh_genA<<<2048, 256, 0, s>>>(d.A32, m, n, b->seed);
-  k_sh_split<<<dim3(m / 32, n / 32), dim3(32, 8), 0, s>>>(d.A32, d.Acat, d.AThi, m, n);
+  k_sh_split<<<dim3(m / 32, n / 32), dim3(32, 8), 0, s>>>(d.A32, d.Acat, d.ATcat, m, n);
   k_sh_genx<<<Tp, SH_THREADS, smem_n, s>>>(d);
   k_sh_y<<<Tp, SH_THREADS, smem_n, s>>>(d);
   // ---- x = H_k(A^T y): G = A_hi^T bf16(y) (Rbf holds bf16(y) here)
-  GB_TRY(gb_gemm_tn(d.AThi, d.Rbf, d.G, n, Tp, m, m, m, nullptr, nullptr, s));
+  GB_TRY(gemm(d.ATcat, (d.prec & 1) ? (const void *)d.Rcat : d.Rbf, d.G, n, kg, 3 * m, kg, nullptr, nullptr, 0, false,
+              s));
   k_sh_init<<<Tp, SH_THREADS, 0, s>>>(d);
   GB_CUDA_TRY(cudaGetLastError());
   // ---- NIHT iterations in lockstep: one graph, WHILE any trial is active
@@ -619,16 +732,48 @@ extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *ite
     cudaGraphConditionalHandle h = 0;
     if (rc == GB_OK) rc = gb_make_handle(c0, &h);
     if (rc == GB_OK) {
-      k_sh_any<<<1, 1024, 0, c0>>>(d, passes, h);
+      k_sh_list<<<1, 1024, 0, c0>>>(d, 0, passes, h);
       rc = gb_open_while(c0, c1, h);
     }
     if (rc == GB_OK) {
-      rc = gb_gemm_tn(d.Acat, d.Xcat, d.R, m, Tp, 3 * n, 3 * n, 3 * n, d.Y, d.Rbf, c1);  // R = Y - A X
-      if (rc == GB_OK) rc = gb_gemm_tn(d.AThi, d.Rbf, d.G, n, Tp, m, m, m, nullptr, nullptr, c1);  // G = A^T R
+      // R = Y - A X (and its BF16 form for the next product), G = A^T R, Q = A x_thres;
+      // each over the active trials only
+      const int split_r = (d.prec & 1) != 0;
+      void *rb = split_r ? (void *)d.Rcat : (void *)d.Rbf;
+      rc = gemm(d.Acat, d.Xcat, d.R, m, 3 * n, 3 * n, 3 * n, d.Y, rb, split_r, true, c1);
+      if (rc == GB_OK) rc = gemm(d.ATcat, rb, d.G, n, kg, 3 * m, kg, nullptr, nullptr, 0, true, c1);
       k_sh_mask<<<Tp, SH_THREADS, 0, c1>>>(d);
-      if (rc == GB_OK) rc = gb_gemm_tn(d.Acat, d.XTbf, d.Q, m, Tp, n, 3 * n, n, nullptr, nullptr, c1);  // Q = A x_thres
+      if (rc == GB_OK) rc = gemm(d.Acat, d.XTbf, d.Q, m, kq, 3 * n, kq, nullptr, nullptr, 0, true, c1);
       k_sh_step<<<Tp, SH_THREADS, 0, c1>>>(d);
-      k_sh_any<<<1, 1024, 0, c1>>>(d, passes, h);
+      k_sh_list<<<1, 1024, 0, c1>>>(d, 0, passes, h);
+      gb_status rc2 = gb_close_while(c1);
+      if (rc == GB_OK) rc = rc2;
+    }
+    // debias of the converged trials: r = y - A x, g = A^T r, then CG in lockstep while
+    // any of them iterates
+    cudaGraphConditionalHandle h2 = 0;
+    if (rc == GB_OK) {
+      k_cg_flags<<<(Tp + 255) / 256, 256, 0, c0>>>(d);
+      k_sh_list<<<1, 1024, 0, c0>>>(d, 1, passes, 0);
+      rc = gemm(d.Acat, d.Xcat, d.R, m, 3 * n, 3 * n, 3 * n, d.Y, nullptr, 0, true, c0);
+    }
+    if (rc == GB_OK) {
+      k_cg_start<<<Tp, SH_THREADS, 0, c0>>>(d);
+      rc = gemm(d.ATcat, d.Rcat, d.G, n, 3 * m, 3 * m, 3 * m, nullptr, nullptr, 0, true, c0);
+    }
+    if (rc == GB_OK) rc = gb_make_handle(c0, &h2);
+    if (rc == GB_OK) {
+      k_cg_dir<<<Tp, SH_THREADS, 0, c0>>>(d);
+      k_sh_list<<<1, 1024, 0, c0>>>(d, 1, passes, h2);
+      rc = gb_open_while(c0, c1, h2);
+    }
+    if (rc == GB_OK) {
+      rc = gemm(d.Acat, d.Xcat, d.Q, m, 3 * n, 3 * n, 3 * n, nullptr, nullptr, 0, true, c1);  // q = A p
+      k_cg_step<<<Tp, SH_THREADS, 0, c1>>>(d);
+      if (rc == GB_OK)
+        rc = gemm(d.ATcat, d.Rcat, d.G, n, 3 * m, 3 * m, 3 * m, nullptr, nullptr, 0, true, c1);
+      k_cg_dir<<<Tp, SH_THREADS, 0, c1>>>(d);
+      k_sh_list<<<1, 1024, 0, c1>>>(d, 1, passes, h2);
       gb_status rc2 = gb_close_while(c1);
       if (rc == GB_OK) rc = rc2;
     }
@@ -649,27 +794,25 @@ extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *ite
     }
   }
   if (rc == GB_OK) {
-    k_sh_final<<<Tp, SH_THREADS, smem_n, s>>>(d, 1);
+    k_sh_verdict<<<Tp, SH_THREADS, 0, s>>>(d);
     cudaEventRecord(e1, s);
     if (b->d_A_out) cudaMemcpyAsync(b->d_A_out, d.A32, sizeof(float) * (size_t)m * n, cudaMemcpyDeviceToDevice, s);
     if (b->d_Y_out) cudaMemcpyAsync(b->d_Y_out, d.Y, sizeof(float) * (size_t)T * m, cudaMemcpyDeviceToDevice, s);
     if (b->d_X0_out) cudaMemcpyAsync(b->d_X0_out, d.X0, sizeof(float) * (size_t)T * n, cudaMemcpyDeviceToDevice, s);
     std::vector<int> hit(T), hok(T);
     std::vector<float> herr(T);
-    int hpass = 0;
+    double hflops = 0.0;
     cudaMemcpyAsync(hit.data(), d.iters, sizeof(int) * T, cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(herr.data(), d.err, sizeof(float) * T, cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(hok.data(), d.ok, sizeof(int) * T, cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(&hpass, passes, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&hflops, d.flops, sizeof(double), cudaMemcpyDeviceToHost, s);
     cudaError_t e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
       gb_set_error_message(cudaGetErrorString(e), __FILE__, __LINE__);
       rc = GB_CUDA_ERROR;
     } else {
       cudaEventElapsedTime(&g_sh_ms, e0, e1);
-      // per lockstep pass: GEMMs of 2*m*3n*Tp + 2*n*m*Tp + 2*m*n*Tp flops
-      g_sh_gemm_flops = (double)(hpass > 0 ? hpass - 1 : 0) * 2.0 * m * (double)n * Tp * 5.0 +
-                        2.0 * n * (double)m * Tp;
+      g_sh_gemm_flops = hflops;
       int ns = 0;
       for (int t = 0; t < T; ++t) {
         if (iters_out) iters_out[t] = hit[t];

@@ -46,3 +46,13 @@ def shard(indices, rank, world):
 def rank_wave(rank, world, step):
     """Wave solved by `rank` at global step `step` (weak scaling: every rank its own wave)."""
     return rank + world * step
+
+
+# The shared-matrix subset of the sweep: trials that share one dense Gaussian A with
+# n = 8192 and delta = 0.5 (m = 4096), rho cycling through the sweep's 0.02 grid.
+SHARED_N, SHARED_M = 8192, 4096
+
+
+def shared_subset(total=1024):
+    """k of each trial of a shared-matrix subset of `total` trials."""
+    return np.array([max(1, int(round(RHOS[t % len(RHOS)] * SHARED_M))) for t in range(total)], dtype=np.int32)

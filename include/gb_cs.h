@@ -195,10 +195,11 @@ void gb_cs_batch_last_stats(double *bytes, float *kernel_ms);
 /* ---- shared-matrix batched form (no reference counterpart) ----
  * ntrials NIHT trials y_t = A x0_t that share one dense Gaussian A (drawn from `seed` as
  * gb_cs_generate_and_solve draws it; trial t's +-1 signal x0_t with k[t] nonzeros uses the
- * key seed + 1 + t).  The operator applications of all trials run as BF16 tensor-core
+ * key seed + 1 + first_trial + t).  The operator applications of all trials run as BF16 tensor-core
  * GEMMs with FP32 accumulation; the residual keeps ~FP32 accuracy by splitting A and x
  * into BF16 high and low parts; trials that stop with ||y - A x|| <= tol_rel ||y|| are
- * debiased by least squares on their support in FP64.  m, n multiples of 128 with
+ * debiased by least squares on their support (CG on the normal equations, FP64 scalars,
+ * split-precision GEMM products).  m, n multiples of 128 with
  * 128 <= m <= n <= 32768.  Per-trial outputs as for gb_cs_solve_batch (host arrays).
  * d_A_out (m*n, column-major), d_Y_out (ntrials*m), d_X0_out (ntrials*n) are optional
  * device copies of the generated problem. */
@@ -206,8 +207,10 @@ typedef struct {
   int ntrials, m, n;
   const int *k;                  /* host array of ntrials sparsities */
   unsigned int seed;
+  unsigned int first_trial;      /* trial t's signal uses the key seed + 1 + first_trial + t */
   float tol_rel;
   int maxiter;
+  int precision;                 /* bit 0: split-BF16 A^T r, bit 1: split-BF16 A x_thres (0: plain BF16) */
   float *d_A_out, *d_Y_out, *d_X0_out;
   void *stream;
 } gb_shared_batch;
