@@ -345,9 +345,14 @@ def matvec_roofline(peak, peak_kind, m=14746, n=16384, k=5000, reps=20):
     g_out, y_out = torch.empty(n, device="cuda"), torch.empty(m, device="cuda")
     s = torch.cuda.Stream()
     res = {}
+    # A x_S is timed on a fixed support (transpose 2: the support scan of the first call is
+    # reused), so the events bracket the k_dense_av launches alone
     for name, tr, vin, vout, nbytes in (("at", 1, r, g_out, 4.0 * m * n + 4 * m + 4 * n),
-                                        ("av", 0, x, y_out, 4.0 * m * k + 8 * k + 4 * m)):
+                                        ("av", 2, x, y_out, 4.0 * m * k + 8 * k + 4 * m)):
         with torch.cuda.stream(s):
+            if tr == 2:
+                L.gb_cs_dense_apply_noalloc(A.data_ptr(), lda, m, n, 0, vin.data_ptr(), vout.data_ptr(),
+                                            C.c_void_p(s.cuda_stream))
             for _ in range(3):
                 L.gb_cs_dense_apply_noalloc(A.data_ptr(), lda, m, n, tr, vin.data_ptr(), vout.data_ptr(),
                                             C.c_void_p(s.cuda_stream))
@@ -362,13 +367,28 @@ def matvec_roofline(peak, peak_kind, m=14746, n=16384, k=5000, reps=20):
         t = e0.elapsed_time(e1) / 1e3 / reps
         ach = nbytes / t / 1e9
         res[name] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                     "traffic": None, "kernel": "k_dense_at" if name == "at" else "k_dense_av (+ support compaction)",
+                     "traffic": None, "kernel": "k_dense_at" if name == "at" else "k_dense_av",
                      "shape": "m=%d n=%d lda=%d%s, A %.0f MB > L2" % (m, n, lda, "" if name == "at" else
                                                                       " |S|=%d" % k, 4.0 * m * n / 1e6),
                      "us_per_launch": t * 1e6, "peak_source": peak_kind}
     del A
     torch.cuda.empty_cache()
+    tr = ncu_traffic()
+    for name, key in (("at", "k_dense_at m=14746 n=16384 lda=14752"), ("av", "k_dense_av m=14746 n=16384 lda=14752 |S|=5000")):
+        if key in tr and (m, n, k) == (14746, 16384, 5000):
+            res[name]["traffic"] = tr[key]["read"] + tr[key]["write"]
+            res[name]["traffic_source"] = "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, same shape " \
+                                          "(profiles/dram_traffic.json)"
     return res
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of the dense kernels from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "dram_traffic.json")) as f:
+            return json.load(f)["per_launch_dram_bytes"]
+    except (OSError, ValueError, KeyError):
+        return {}
 
 
 def bench_plain(args, first_step):
@@ -431,6 +451,28 @@ def bench_plain(args, first_step):
                       "recovered / estimated time of the 3072 + 1024 sweep" % (len(sel), len(sel2), w)}
 
 
+def bench_only(args):
+    import torch
+
+    import gaga_gb300 as gb
+
+    gb._lib.load()
+    torch.cuda.set_device(0)
+    if args.only == "matvec":
+        out = matvec_roofline(*peaks())
+    elif args.only == "gemm":
+        out = gemm_roofline(*tensor_peak())
+    else:
+        w = args.warmup
+        n, m, k, tid = wave_arrays(w)
+        ns, iters, err, ok = gb.solve_batch(n, m, k, SEED, tid, alg="NIHT", tol_rel=TOL_REL, maxiter=MAXITER)
+        ks, first = shared_part(w)
+        _, _, _, ok2 = gb.solve_shared_batch(gb.sweep.SHARED_M, gb.sweep.SHARED_N, ks, SHARED_SEED, tol_rel=TOL_REL,
+                                             maxiter=MAXITER, first_trial=first)
+        out = bench_plain(args, (w, {"verdict_batch": ok, "verdict_shared": ok2}))
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -440,10 +482,14 @@ def main():
     ap.add_argument("--plain-trials", type=int, default=32)
     ap.add_argument("--cpu-trials", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--only", choices=["matvec", "gemm", "plain"],
+                    help="run one measurement alone and print its JSON (for profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
-    if args.impl == "reference":
+    if args.only:
+        bench_only(args)
+    elif args.impl == "reference":
         bench_reference(args)
     else:
         bench_ours(args)

@@ -34,6 +34,7 @@ namespace {
 
 const int kMaxDevices = 64;
 unsigned char *g_scratch_ptr[kMaxDevices] = {nullptr};
+int g_support_n[kMaxDevices] = {0};  // n of the support list the last transpose == 0 call built
 std::mutex g_scratch_mu;
 
 // device address of the scratch array for the current device (looked up once)
@@ -60,7 +61,7 @@ size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 extern "C" gb_status gb_cs_dense_apply_noalloc(const float *d_A, int lda, int m, int n, int transpose,
                                                const float *d_in, float *d_out, void *stream) {
-  if (!d_A || !d_in || !d_out || m < 1 || n < 1) {
+  if (!d_A || !d_in || !d_out || m < 1 || n < 1 || transpose < 0 || transpose > 2) {
     gb_set_error_message("gb_cs_dense_apply_noalloc: null buffer or empty size", __FILE__, __LINE__);
     return GB_BAD_ARG;
   }
@@ -118,6 +119,22 @@ extern "C" gb_status gb_cs_dense_apply_noalloc(const float *d_A, int lda, int m,
   init.lda = lda;
   init.active = 1;
   init.flags[F_ALWAYS] = 1;
+  if (transpose == 2) {
+    // A x on the support list of the previous transpose == 0 call: the state and the
+    // list are still in the scratch array, and the tile tickets are zero after any
+    // completed launch
+    {
+      std::lock_guard<std::mutex> lock(g_scratch_mu);
+      if (g_support_n[dev] != n) {
+        gb_set_error_message("gb_cs_dense_apply_noalloc: transpose == 2 needs a previous transpose == 0 call "
+                             "with the same n on this device", __FILE__, __LINE__);
+        return GB_BAD_ARG;
+      }
+    }
+    enq_A(w, s, d_in, d_out, nullptr, -1, F_ALWAYS);
+    GB_CUDA_TRY(cudaGetLastError());
+    return GB_OK;
+  }
   GB_CUDA_TRY(cudaMemsetAsync(w.av_tickets, 0, tickets_bytes, s));
   k_init_state<<<1, 1, 0, s>>>(w.st, init);
   if (transpose) {
@@ -125,6 +142,8 @@ extern "C" gb_status gb_cs_dense_apply_noalloc(const float *d_A, int lda, int m,
   } else {
     enq_support_of_nonzeros(w, s, d_in, n);
     enq_A(w, s, d_in, d_out, nullptr, -1, F_ALWAYS);
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    g_support_n[dev] = n;
   }
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;

@@ -14,6 +14,7 @@
 //           A^T r: one thread per column over its d nonzeros
 //           replaces sparse_matvec / sparse_matvecT (GAGA/Matrices/smv_gpu.cu:29-47)
 #include <algorithm>
+#include <cmath>
 
 #include "gb_internal.cuh"
 
@@ -22,7 +23,9 @@
 #define DV_ROWS 128
 #define DV_STAGE 512    // support entries staged in shared memory per pass
 #define DV_MIN_SPLIT 512  // support columns per CTA before the support is split further
+#define DV_BLOCKS_PER_SM 4  // 4 x 512 threads resident per SM (<= 32 registers per thread)
 #define DA_THREADS 256  // A^T r: 8 warps, 4 columns per warp
+#define DA_BLOCKS_PER_SM 3  // resident A^T r CTAs per SM (<= 85 registers per thread)
 
 
 // 16-byte load that does not allocate in L1 (A is streamed once per pass; r stays in L1)
@@ -40,7 +43,7 @@ __device__ __forceinline__ float4 ld_stream4(const float *p) {
 // than one split, each CTA publishes its partial tile and the last CTA of the tile to
 // arrive adds the partials in split order (deterministic, no second kernel).
 template <int VEC>
-__global__ void __launch_bounds__(DV_THREADS) k_dense_av(GbState *st, int pf, const float *__restrict__ A, int lda,
+__global__ void __launch_bounds__(DV_THREADS, DV_BLOCKS_PER_SM) k_dense_av(GbState *st, int pf, const float *__restrict__ A, int lda,
                                                          int m, int ntile_cap, int nsplit, const int *__restrict__ S,
                                                          const float *__restrict__ v, const float *__restrict__ y,
                                                          float *__restrict__ out, float *__restrict__ part,
@@ -156,7 +159,7 @@ __global__ void __launch_bounds__(DV_THREADS) k_dense_av(GbState *st, int pf, co
 // fused epilogue: xt_j = g_j if bin_j <= k_bin else 0, ||xt||^2 into red[slot_sq],
 // max|g| into red[slot_max].
 template <int VEC>
-__global__ void __launch_bounds__(DA_THREADS) k_dense_at(GbState *st, int pf, const float *__restrict__ A, int lda,
+__global__ void __launch_bounds__(DA_THREADS, DA_BLOCKS_PER_SM) k_dense_at(GbState *st, int pf, const float *__restrict__ A, int lda,
                                                          int m, int n, const float *__restrict__ r,
                                                          float *__restrict__ g, const int *__restrict__ bins,
                                                          float *__restrict__ xt, int slot_sq, int slot_max,
@@ -440,14 +443,25 @@ static void launch_fft(GbWork &w, cudaStream_t s, int pf, int pass, const float 
                                                                   cin, cout, rout);
 }
 
-// A x_S launch shape: row tiles of the (capacity) m times support splits, <= GB_MAXRB CTAs
+// A x_S launch shape: row tiles of the (capacity) m times support splits, <= GB_MAXRB CTAs.
+// The split count is the smallest that best fills whole waves of the resident CTA slots
+// (DV_BLOCKS_PER_SM per SM): a grid of 1.5 waves leaves half the GPU idle in its tail.
 void gb_dense_av_shape(int m, int num_sms, int *ntile, int *nsplit) {
   int t = (m + DV_ROWS - 1) / DV_ROWS;
   if (t > GB_MAXRB) t = GB_MAXRB;
-  int sp = (4 * num_sms + t - 1) / t;
-  sp = std::max(1, std::min(sp, std::min(16, GB_MAXRB / t)));
+  const double slots = (double)DV_BLOCKS_PER_SM * num_sms;
+  int best = 1;
+  double best_fill = -1.0;
+  for (int sp = 1; sp <= 16 && t * sp <= GB_MAXRB; ++sp) {
+    const double x = t * sp / slots;
+    const double fill = x < 1.0 ? x : x / std::ceil(x);
+    if (fill > best_fill + 1e-3) {
+      best_fill = fill;
+      best = sp;
+    }
+  }
   *ntile = t;
-  *nsplit = sp;
+  *nsplit = best;
 }
 
 size_t gb_dense_part_floats_av(int ntile, int nsplit) { return (size_t)ntile * nsplit * DV_ROWS; }
@@ -474,9 +488,10 @@ void enq_A(GbWork &w, cudaStream_t s, const float *v, float *out, const float *y
 }
 
 static int dense_at_grid(const GbWork &w) {
-  // one CTA per group of 4 columns (grid-stride beyond the cap)
+  // one CTA per group of 4 columns, grid-stride beyond one wave of resident CTAs (a grid
+  // of a fraction of a wave more leaves SMs idle in its tail)
   const int blocks = (w.op.n + 3) / 4;
-  const int cap = std::min(GB_MAXRB, w.wide_blocks);
+  const int cap = std::min(std::min(GB_MAXRB, w.wide_blocks), DA_BLOCKS_PER_SM * w.num_sms);
   return blocks < cap ? blocks : cap;
 }
 

@@ -155,7 +155,10 @@ gb_status gb_cs_operator_apply(const gb_problem *p, int transpose, const float *
  * allocator.  Its scratch is one fixed 1 MiB device array per GPU held until the process
  * exits; m and n must be <= 65536 (GB_BAD_ARG otherwise).  The first call on a device
  * resolves the array's address and must happen outside a stream capture.  All calls share
- * the array: calls that overlap on the GPU race and must be serialised by the caller. */
+ * the array: calls that overlap on the GPU race and must be serialised by the caller.
+ * transpose 2 is A in on the support (nonzero pattern) found by the previous transpose 0
+ * call with the same n on this device, skipping the support scan: repeated applications
+ * with a fixed support, as in a CG solve on the support. */
 gb_status gb_cs_dense_apply_noalloc(const float *d_A, int lda, int m, int n, int transpose,
                                     const float *d_in, float *d_out, void *stream);
 

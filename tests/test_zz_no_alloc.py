@@ -53,3 +53,29 @@ def test_noalloc_rejects_sizes_beyond_the_scratch(gb):
     fake = C.c_void_p(256)
     assert L.gb_cs_dense_apply_noalloc(fake, big, big, 8, 0, fake, fake, None) == gb._lib.GB_BAD_ARG
     assert b"65536" in L.gb_cs_last_error()
+
+
+def test_noalloc_fixed_support_mode(gb, gbo):
+    """transpose 2 reuses the support of the previous transpose 0 call (same n)."""
+    torch = _torch()
+    L = gb._lib.load()
+    rng = np.random.default_rng(22)
+    m, n = 640, 2048
+    A = gbo.gen_dense(m, n, seed=77)
+    dA = torch.tensor(A, device="cuda")
+    x = rng.standard_normal(n).astype(np.float32)
+    x[rng.random(n) < 0.7] = 0.0
+    x2 = (x * 3.0 - np.sign(x)).astype(np.float32)  # same support, new values
+    out = torch.zeros(m, device="cuda")
+    assert L.gb_cs_dense_apply_noalloc(dA.data_ptr(), m, m, n, 0, torch.tensor(x, device="cuda").data_ptr(),
+                                       out.data_ptr(), None) == 0
+    dx2 = torch.tensor(x2, device="cuda")
+    assert L.gb_cs_dense_apply_noalloc(dA.data_ptr(), m, m, n, 2, dx2.data_ptr(), out.data_ptr(), None) == 0
+    torch.cuda.synchronize()
+    want = A.reshape(n, m).T.astype(np.float64) @ x2.astype(np.float64)
+    np.testing.assert_allclose(out.cpu().numpy(), want, rtol=0, atol=2e-5 * np.abs(want).max())
+    # a different n has no support list to reuse
+    assert L.gb_cs_dense_apply_noalloc(dA.data_ptr(), m, m, n // 2, 2, dx2.data_ptr(), out.data_ptr(),
+                                       None) == gb._lib.GB_BAD_ARG
+    assert L.gb_cs_dense_apply_noalloc(dA.data_ptr(), m, m, n, 3, dx2.data_ptr(), out.data_ptr(),
+                                       None) == gb._lib.GB_BAD_ARG
