@@ -297,8 +297,8 @@ def tensor_peak():
 
 
 def gemm_roofline(tpeak, tpeak_kind, M=4096, N=1024, K=3 * 8192, reps=10):
-    """The shared-matrix form's residual GEMM (k_gemm_tn_mma, [A_hi|A_lo|A_hi] . X^T) on its
-    full 1024-trial shape, timed with CUDA events on its stream."""
+    """The shared-matrix form's residual GEMM ([A_hi|A_lo|A_hi] . X^T, the tcgen05 kernel
+    unless GB_CS_GEMM=mma) on its full 1024-trial shape, timed with CUDA events on its stream."""
     import torch
 
     import gaga_gb300 as gb
@@ -321,8 +321,9 @@ def gemm_roofline(tpeak, tpeak_kind, M=4096, N=1024, K=3 * 8192, reps=10):
     ach = 2.0 * M * N * K / t / 1e12
     del A, B, Y
     torch.cuda.empty_cache()
+    kern = "k_gemm_tn_mma (mma.sync)" if os.environ.get("GB_CS_GEMM") == "mma" else "k_gemm_tn_tc (tcgen05 + TMA)"
     return {"bound": "tensor", "achieved": ach, "peak": tpeak, "unit": "TFLOP/s", "frac": ach / tpeak,
-            "kernel": "k_gemm_tn_mma", "shape": "M=%d N=%d K=%d (bf16 in, fp32 accumulate, Y - AB^T epilogue)" % (
+            "kernel": kern, "shape": "M=%d N=%d K=%d (bf16 in, fp32 accumulate, Y - AB^T epilogue)" % (
                 M, N, K), "us_per_launch": t * 1e6, "peak_source": tpeak_kind}
 
 

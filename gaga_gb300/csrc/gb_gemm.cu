@@ -8,9 +8,13 @@
 // (or its transpose) and B holds one trial's vector per row.
 //
 // This file holds the warp-level tensor-core kernel (mma.sync m16n8k16, 3-stage cp.async
-// pipeline, 128x128x32 CTA tile).  It is the correctness baseline that the tcgen05 kernel
-// (gb_gemm_tc.cu) is validated against.
+// pipeline, 128x128x32 CTA tile) and the dispatch.  The mma.sync kernel is the baseline the
+// tcgen05 kernel (gb_gemm_tc.cu) is validated against; gb_gemm runs the tcgen05 kernel
+// whenever the shape allows (N % 256, K % 64) unless GB_CS_GEMM=mma.
 #include <cuda_bf16.h>
+
+#include <stdlib.h>
+#include <string.h>
 
 #include "gb_internal.cuh"
 
@@ -199,6 +203,11 @@ __global__ void __launch_bounds__(256) k_gemm_tn_mma(GbGemm g, GbGemmWs ws, int 
       }
 }
 
+int gb_gemm_use_tc() {
+  const char *e = getenv("GB_CS_GEMM");
+  return !(e && strcmp(e, "mma") == 0);
+}
+
 gb_status gb_gemm(const GbGemm &g, cudaStream_t s) {
   if (g.M % GT_M || g.N % GT_N || g.K % GT_K || g.M <= 0 || g.N <= 0 || g.K <= 0 || g.lda < g.K || g.ldb < g.K ||
       g.lda % 8 || g.ldb % 8) {
@@ -206,6 +215,10 @@ gb_status gb_gemm(const GbGemm &g, cudaStream_t s) {
                          __LINE__);
     return GB_BAD_ARG;
   }
+  const bool aligned = ((uintptr_t)g.A & 15) == 0 && ((uintptr_t)g.B & 15) == 0;
+  if (gb_gemm_use_tc() && g.N % 256 == 0 && g.K % 64 == 0 && aligned &&
+      (!g.nmap || (g.ws && g.ws->gather)))
+    return gb_gemm_tc(g, s);
   GbGemmWs ws = {};
   int s_max = 1;
   if (g.ws && g.ws->part && g.ws->tickets && (g.M / GT_M) * (g.N / GT_N) <= g.ws->ticket_count) {

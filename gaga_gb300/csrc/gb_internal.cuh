@@ -241,9 +241,11 @@ size_t gb_dense_part_floats_av(int ntile, int nsplit);
 // workspace, K is split over CTAs when the live tiles would leave SMs idle.
 #define GB_GEMM_SPLIT_MAX 8
 struct GbGemmWs {
-  float *part;            // partial 128 x 128 tiles
+  float *part;            // partial tiles, part_tiles units of 128 x 128 floats
   unsigned int *tickets;  // one per output tile, zero between launches
   int part_tiles, ticket_count, num_sms;
+  void *gather;           // tcgen05 path with a column map: the live B rows, contiguous
+  size_t gather_elems;
 };
 struct GbGemm {
   const void *A, *B;
@@ -256,6 +258,11 @@ struct GbGemm {
   const GbGemmWs *ws;
 };
 gb_status gb_gemm(const GbGemm &g, cudaStream_t s);
+// tcgen05 + TMA kernel (gb_gemm_tc.cu): M % 128, N % 256, K % 64; and its error word
+gb_status gb_gemm_tc(const GbGemm &g, cudaStream_t s);
+gb_status gb_gemm_tc_check();
+// which kernel gb_gemm uses: 1 tcgen05 (default), 0 the mma.sync kernel (GB_CS_GEMM=mma)
+int gb_gemm_use_tc();
 
 // solver (gb_solver.cu)
 enum { GB_RUN_SOLVE = 0, GB_RUN_L0 = 1 };

@@ -632,7 +632,7 @@ extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *ite
                          __LINE__);
     return GB_BAD_ARG;
   }
-  const int m = b->m, n = b->n, T = b->ntrials, Tp = (T + 127) / 128 * 128;
+  const int m = b->m, n = b->n, T = b->ntrials, Tp = (T + 255) / 256 * 256;  // tcgen05 N tile
   for (int t = 0; t < T; ++t)
     if (b->k[t] < 1 || b->k[t] > m) {
       gb_set_error_message("shared batch: every k must satisfy 1 <= k <= m", __FILE__, __LINE__);
@@ -683,6 +683,12 @@ extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *ite
   ws.ticket_count = (n / 128) * (Tp / 128);
   GB_TRY(buf.get(&ws.part, (size_t)ws.part_tiles * 128 * 128));
   GB_TRY(buf.get(&ws.tickets, ws.ticket_count));
+  ws.gather_elems = (size_t)Tp * 3 * std::max(m, n);  // widest B operand: Tp x 3n
+  {
+    __nv_bfloat16 *gbuf = nullptr;
+    GB_TRY(buf.get(&gbuf, ws.gather_elems));
+    ws.gather = gbuf;
+  }
   GB_CUDA_TRY(cudaMemsetAsync(ws.tickets, 0, sizeof(unsigned) * ws.ticket_count, s));
   // Ct[Tp x M] = [Y -] A . B^T over all trials, or over the listed ones (mapped)
   auto gemm = [&](const void *A, const void *B, float *C, int M, int K, int lda, int ldb, const float *Y, void *Cb,
@@ -810,6 +816,8 @@ extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *ite
     if (e != cudaSuccess) {
       gb_set_error_message(cudaGetErrorString(e), __FILE__, __LINE__);
       rc = GB_CUDA_ERROR;
+    } else if ((rc = gb_gemm_tc_check()) != GB_OK) {
+      // a tcgen05 GEMM gave up on a wait: results are not valid
     } else {
       cudaEventElapsedTime(&g_sh_ms, e0, e1);
       g_sh_gemm_flops = hflops;

@@ -47,6 +47,37 @@ def test_gemm_bf16_tn(gb, M, N, K):
     assert np.array_equal(Cb.float().cpu().numpy(), _bf16_round(got2))
 
 
+@pytest.mark.parametrize("M,N,K", [(128, 256, 64), (384, 512, 1024), (1024, 256, 24576)])
+def test_gemm_tcgen05(gb, M, N, K):
+    """N % 256 == 0 and K % 64 == 0 run the tcgen05 + TMA kernel: check it against an FP64
+    product of the same BF16 operands and against the mma.sync kernel (GB_CS_GEMM=mma)."""
+    import os
+
+    import torch
+
+    rng = np.random.default_rng(M * 7 + N + K)
+    A = _bf16_round(rng.standard_normal((M, K)).astype(np.float32))
+    B = _bf16_round(rng.standard_normal((N, K)).astype(np.float32))
+    Y = rng.standard_normal((N, M)).astype(np.float32)
+    dA = torch.from_numpy(A).to(torch.bfloat16).cuda()
+    dB = torch.from_numpy(B).to(torch.bfloat16).cuda()
+    dY = torch.from_numpy(Y).cuda()
+    ref = (A.astype(np.float64) @ B.astype(np.float64).T).T
+    bound = K * 2.0 ** -23 * (np.abs(A).astype(np.float64) @ np.abs(B).astype(np.float64).T).T + 1e-5
+    Ct, Cb = gb.gemm_bf16_tn(dA, dB, Y=dY, want_bf16=True)
+    torch.cuda.synchronize()
+    got = Ct.cpu().numpy()
+    assert np.all(np.abs(got - (Y - ref)) <= bound), float(np.max(np.abs(got - (Y - ref)) - bound))
+    assert np.array_equal(Cb.float().cpu().numpy(), _bf16_round(got))
+    os.environ["GB_CS_GEMM"] = "mma"
+    try:
+        Ct2, _ = gb.gemm_bf16_tn(dA, dB, Y=dY)
+        torch.cuda.synchronize()
+    finally:
+        del os.environ["GB_CS_GEMM"]
+    assert np.all(np.abs(got - Ct2.cpu().numpy()) <= 2 * bound)
+
+
 def test_gemm_rejects_bad_shapes(gb):
     import torch
 
