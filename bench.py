@@ -18,6 +18,8 @@ Problem generation runs inside the timed region.
           for independent trials, gb_cs_solve on the shared A for shared trials), scaled
           to the 3072 + 1024 mix, for the tuned-vs-plain ratio; the verdicts of the same
           trials give the agreement between the two forms
+  learned_warm_start : the trained MLP warm start for CGIHT against zero-initialised CGIHT
+          on 2048 fresh trials of its workload (n = 8192, delta 0.1-0.6, rho 0.05-0.45)
   cpu_baseline / --impl reference : the CPU oracle (oracle/gbo.c, OpenMP inside each
           trial) on a bounded sample of the wave
 
@@ -275,11 +277,25 @@ def bench_ours(args):
     if args.plain_trials > 0 and world == 1:
         line["plain"] = bench_plain(args, first_step)
         line["tuned_vs_plain"] = value / line["plain"]["value"] if line["plain"]["value"] else None
+    if args.learned_trials > 0 and world == 1:
+        line["learned_warm_start"] = bench_learned(args)
     if not args.no_cpu and world == 1:
         line["cpu_baseline"] = run_cpu(args.warmup, args.cpu_trials)
     print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def bench_learned(args):
+    """The learned warm start on its own workload: fresh dense Gaussian CGIHT trials with
+    n = 8192, delta in [0.1, 0.6], rho in [0.05, 0.45], warm-started from the trained MLP
+    (with the plain fallback) against zero-initialised CGIHT, both through the batched form."""
+    from gaga_gb300 import learned
+
+    res = learned.evaluate(learned.load_weights(), count=args.learned_trials)
+    res["workload"] = "%d fresh CGIHT trials, n=8192, delta U[0.1,0.6], rho U[0.05,0.45], tol 1e-4*||y||" % (
+        args.learned_trials)
+    return res
 
 
 def tensor_peak():
@@ -463,6 +479,8 @@ def bench_only(args):
         out = matvec_roofline(*peaks())
     elif args.only == "gemm":
         out = gemm_roofline(*tensor_peak())
+    elif args.only == "learned":
+        out = bench_learned(args)
     else:
         w = args.warmup
         n, m, k, tid = wave_arrays(w)
@@ -481,9 +499,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--plain-trials", type=int, default=32)
-    ap.add_argument("--cpu-trials", type=int, default=8)
+    ap.add_argument("--cpu-trials", type=int, default=32)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--only", choices=["matvec", "gemm", "plain"],
+    ap.add_argument("--learned-trials", type=int, default=2048)
+    ap.add_argument("--only", choices=["matvec", "gemm", "plain", "learned"],
                     help="run one measurement alone and print its JSON (for profiling)")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -25,7 +25,7 @@ __all__ = ["gaga_cs", "gaga_options", "GagaError", "solve_batch", "version"]
 _OPTION_NAMES = {"tol", "maxiter", "vecDistribution", "matrixEnsemble", "seed", "numBins", "threadsPerBlockn",
                  "threadsPerBlockm", "threadsPerBlocknp", "threadsPerBlockBin", "convRateNum", "kFixed", "noise",
                  "gpuNumber", "timing", "alpha", "supportFlag", "restartFlag", "projFracTol", "l0_thresh",
-                 "band_percentage", "debug_mode", "tol_is_relative"}
+                 "band_percentage", "debug_mode", "tol_is_relative", "learnedWarmStart"}
 
 
 def version():
@@ -88,6 +88,9 @@ def _options(alg, n, opts, ens):
             o.support_flag = int(v)
         elif name == "timing":
             o.timing = 1 if v in ("on", 1, True) else 0
+        elif name == "learnedWarmStart":
+            # extension: a CUDA tensor of gb_cs_mlp_num_params() FP32 MLP parameters (CGIHT)
+            o.learned_params = None if v is None else v.data_ptr()
         # threadsPerBlock*, projFracTol, band_percentage, debug_mode: accepted, no effect
     return o
 
@@ -244,15 +247,19 @@ def generate_and_solve(alg, ens, k, m, n, d=0, opts=None):
     return x, xt, r
 
 
-def solve_batch(n, m, k, seed, trial_ids=None, alg="NIHT", tol_rel=1e-4, maxiter=5000, stream=None):
-    """Batched multi-trial dense form (gb_cs_solve_batch)."""
+def solve_batch(n, m, k, seed, trial_ids=None, alg="NIHT", tol_rel=1e-4, maxiter=5000, stream=None,
+                learned_params=None):
+    """Batched multi-trial dense form (gb_cs_solve_batch); learned_params (a CUDA tensor of
+    MLP parameters, CGIHT only) turns on the learned warm start."""
     L = _lib.load()
     n = np.ascontiguousarray(n, dtype=np.int32)
     m = np.ascontiguousarray(m, dtype=np.int32)
     k = np.ascontiguousarray(k, dtype=np.int32)
     tids = None if trial_ids is None else np.ascontiguousarray(trial_ids, dtype=np.uint32)
     b = _lib.Batch(len(n), n.ctypes.data, m.ctypes.data, k.ctypes.data, None if tids is None else tids.ctypes.data,
-                   int(seed) & 0xFFFFFFFF, {"NIHT": 0, "CGIHT": 6}[alg], float(tol_rel), int(maxiter), 0, stream)
+                   int(seed) & 0xFFFFFFFF, {"NIHT": 0, "HTP": 1, "CGIHT": 6}[alg], float(tol_rel), int(maxiter),
+                   0 if learned_params is None else 1,
+                   None if learned_params is None else learned_params.data_ptr(), stream)
     iters = np.zeros(len(n), dtype=np.int32)
     err = np.zeros(len(n), dtype=np.float32)
     ok = np.zeros(len(n), dtype=np.int32)

@@ -22,7 +22,8 @@ EXPORTS = ["gb_cs_version", "gb_cs_last_error", "gb_cs_default_options", "gb_cs_
            "gb_cs_generate_and_solve", "gb_cs_linear_binning", "gb_cs_find_support_set",
            "gb_cs_operator_apply", "gb_cs_l0_step", "gb_cs_solve_batch", "gb_cs_batch_last_stats",
            "gb_cs_dense_apply_noalloc", "gb_cs_solve_shared_batch", "gb_cs_shared_last_stats",
-           "gb_cs_gemm_bf16_tn"]
+           "gb_cs_gemm_bf16_tn", "gb_cs_mlp_num_params", "gb_cs_mlp_features", "gb_cs_mlp_forward",
+           "gb_cs_mlp_grad", "gb_cs_mlp_train"]
 
 
 class Options(C.Structure):
@@ -30,7 +31,7 @@ class Options(C.Structure):
                 ("restart_flag", C.c_int), ("l0_thresh", C.c_int), ("vec_distribution", C.c_int),
                 ("matrix_ensemble", C.c_int), ("k_fixed", C.c_int), ("seed", C.c_uint), ("noise", C.c_float),
                 ("gpu_number", C.c_int), ("conv_rate_num", C.c_int), ("alpha", C.c_float),
-                ("support_flag", C.c_int), ("timing", C.c_int)]
+                ("support_flag", C.c_int), ("timing", C.c_int), ("learned_params", C.c_void_p)]
 
 
 class Problem(C.Structure):
@@ -43,7 +44,7 @@ class Problem(C.Structure):
 class Result(C.Structure):
     _fields_ = [("iter", C.c_int), ("conv_rate", C.c_float), ("norms", C.c_float * 3), ("times", C.c_float * 3),
                 ("support", C.c_int * 4), ("k_used", C.c_int), ("resid_prev", C.c_float * 16),
-                ("stop_reason", C.c_int), ("res_record", C.c_void_p)]
+                ("stop_reason", C.c_int), ("res_record", C.c_void_p), ("warm_start", C.c_int)]
 
 
 class BinState(C.Structure):
@@ -54,7 +55,8 @@ class BinState(C.Structure):
 class Batch(C.Structure):
     _fields_ = [("ntrials", C.c_int), ("n", C.c_void_p), ("m", C.c_void_p), ("k", C.c_void_p),
                 ("trial_id", C.c_void_p), ("seed", C.c_uint), ("alg", C.c_int), ("tol_rel", C.c_float),
-                ("maxiter", C.c_int), ("use_learned", C.c_int), ("stream", C.c_void_p)]
+                ("maxiter", C.c_int), ("use_learned", C.c_int), ("learned_params", C.c_void_p),
+                ("stream", C.c_void_p)]
 
 
 class SharedBatch(C.Structure):
@@ -106,6 +108,16 @@ def load():
     L.gb_cs_shared_last_stats.restype = None
     L.gb_cs_gemm_bf16_tn.argtypes = [vp, vp, vp, i, i, i, vp, vp, vp]
     L.gb_cs_gemm_bf16_tn.restype = i
+    L.gb_cs_mlp_num_params.argtypes = []
+    L.gb_cs_mlp_num_params.restype = i
+    L.gb_cs_mlp_features.argtypes = [vp, i, i, i, vp, vp]
+    L.gb_cs_mlp_features.restype = i
+    L.gb_cs_mlp_forward.argtypes = [vp, vp, i, vp, vp]
+    L.gb_cs_mlp_forward.restype = i
+    L.gb_cs_mlp_grad.argtypes = [vp, vp, vp, i, vp, vp, vp]
+    L.gb_cs_mlp_grad.restype = i
+    L.gb_cs_mlp_train.argtypes = [vp, vp, vp, i, i, i, f, C.c_uint, vp, vp]
+    L.gb_cs_mlp_train.restype = i
     _lib = L
     return L
 

@@ -14,7 +14,8 @@ BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libgb_cs.so")
 ROOT = os.path.dirname(HERE)
-SOURCES = ["gb_ops.cu", "gb_solver.cu", "gb_api.cu", "gb_batch.cu", "gb_noalloc.cu", "gb_gemm.cu", "gb_gemm_tc.cu", "gb_shared.cu"]
+SOURCES = ["gb_ops.cu", "gb_solver.cu", "gb_api.cu", "gb_batch.cu", "gb_noalloc.cu", "gb_gemm.cu", "gb_gemm_tc.cu",
+           "gb_shared.cu", "gb_learned.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr",
@@ -24,6 +25,7 @@ FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", 
 def _deps():
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
     files.append(os.path.join(ROOT, "include", "gb_cs.h"))
+    files.append(os.path.abspath(__file__))  # the source list and flags
     return files
 
 

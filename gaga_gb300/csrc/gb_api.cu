@@ -305,6 +305,11 @@ extern "C" gb_status gb_cs_solve(const char *alg, const gb_problem *p, const gb_
   if (alg_id == GB_ALG_PARALLEL_L0) {
     if (o.l0_thresh < 1 || o.l0_thresh > w.op.d) o.l0_thresh = 1;  // gaga_smv.cu:313
   }
+  if (o.learned_params && alg_id == GB_ALG_CGIHT) {
+    w.ml_params = o.learned_params;
+    GB_TRY(db.alloc(&w.ml_counts, gb_ml_rank_bins()));
+    GB_TRY(db.alloc(&w.ml_cum, gb_ml_rank_bins()));
+  }
   float tol_abs = o.tol;
   if (o.tol_is_relative) {
     std::vector<float> yh(p->m);
@@ -319,8 +324,22 @@ extern "C" gb_status gb_cs_solve(const char *alg, const gb_problem *p, const gb_
   GB_CUDA_TRY(cudaEventCreate(&e1));
   GB_CUDA_TRY(cudaEventRecord(e0, s));
   GB_TRY(gb_run_solver(w, alg_id, o, p->k, s, tol_abs));
-  GB_CUDA_TRY(cudaEventRecord(e1, s));
   GbState st;
+  int warm = 0, warm_iters = 0;
+  if (w.ml_params) {
+    GB_CUDA_TRY(cudaMemcpyAsync(&st, w.st, sizeof(st), cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    warm = 1;
+    if (st.fell_back) {
+      // the warm start did not reduce the residual: plain zero-initialised CGIHT decides
+      warm = 2;
+      warm_iters = st.iter;
+      w.ml_params = nullptr;
+      GB_CUDA_TRY(cudaMemsetAsync(w.x, 0, sizeof(float) * p->n, s));
+      GB_TRY(gb_run_solver(w, alg_id, o, p->k, s, tol_abs));
+    }
+  }
+  GB_CUDA_TRY(cudaEventRecord(e1, s));
   GB_CUDA_TRY(cudaMemcpyAsync(&st, w.st, sizeof(st), cudaMemcpyDeviceToHost, s));
   GB_CUDA_TRY(cudaMemcpyAsync(x_out, w.x, sizeof(float) * p->n,
                               p->location == GB_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
@@ -338,8 +357,9 @@ extern "C" gb_status gb_cs_solve(const char *alg, const gb_problem *p, const gb_
     float *user_rec = r->res_record;
     memset(r, 0, sizeof(*r));
     r->res_record = user_rec;
-    r->iter = st.iter;
+    r->iter = st.iter + warm_iters;
     r->stop_reason = st.stop_reason;
+    r->warm_start = warm;
     r->times[0] = ms;
     r->times[1] = st.iter > 0 ? ms / st.iter : 0.0f;
     r->times[2] = ms;

@@ -49,6 +49,8 @@ struct BatchParams {
   float *err;
   int *ok;
   double *bytes;
+  int learned;  // learned warm start (CGIHT)
+  int *fb;      // per trial: the warm start was abandoned (solve again from zero)
 };
 
 using gbgen::KEY_HI;
@@ -159,6 +161,9 @@ __global__ void k_b_ctrl(GbState *st, const BatchParams *bp, int phase, cudaGrap
     st->flags[F_ALWAYS] = 1;
     st->changed = 0;
     st->bytes = 0.0;
+    st->learned = bp->learned;
+    st->fell_back = 0;
+    st->err_warm0 = 0.0f;
   } else {
     // verdict of the finished trial (results.cu:468-475), then the next trial
     if (st->trial >= 0) {
@@ -167,6 +172,7 @@ __global__ void k_b_ctrl(GbState *st, const BatchParams *bp, int phase, cudaGrap
       bp->iters[t] = st->iter;
       bp->err[t] = rel;
       bp->ok[t] = rel <= 1e-3f ? 1 : 0;
+      if (bp->fb) bp->fb[t] = st->fell_back;
       atomicAdd(bp->bytes, st->bytes);
     }
     load_trial(st, bp, atomicAdd(bp->queue, 1), h_trial);
@@ -198,7 +204,9 @@ struct Slot {
 };
 
 struct Engine {
-  int dev = -1, alg = -1, n_cap = 0, m_cap = 0, t_cap = 0, slots = 0;
+  int dev = -1, alg = -1, n_cap = 0, m_cap = 0, t_cap = 0, slots = 0, learned = 0;
+  float *ml_params = nullptr;  // the warm-start MLP parameters (copied in by every call)
+  int *dfb = nullptr;
   std::vector<Slot> slot;
   char *table = nullptr;
   BatchParams *d_params = nullptr;
@@ -210,7 +218,7 @@ struct Engine {
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   std::vector<cudaEvent_t> done;
 };
-std::map<int, Engine> g_engines;
+std::map<int, Engine> g_engines;  // key: device * 2 + learned
 
 gb_status dalloc(std::vector<void *> &bufs, void **p, size_t bytes) {
   GB_CUDA_TRY(cudaMalloc(p, std::max<size_t>(bytes, 4)));
@@ -291,10 +299,12 @@ gb_status build_slot_graph(Engine &E, Slot &S) {
   return GB_OK;
 }
 
-gb_status setup_engine(Engine &E, int dev, int alg, int n_cap, int m_cap, int T, int slots) {
-  if (E.dev == dev && E.alg == alg && E.n_cap >= n_cap && E.m_cap >= m_cap && E.t_cap >= T && E.slots == slots)
+gb_status setup_engine(Engine &E, int dev, int alg, int n_cap, int m_cap, int T, int slots, int learned) {
+  if (E.dev == dev && E.alg == alg && E.n_cap >= n_cap && E.m_cap >= m_cap && E.t_cap >= T && E.slots == slots &&
+      E.learned == learned)
     return GB_OK;
   release(E);
+  E.learned = learned;
   E.dev = dev;
   E.alg = alg;
   E.n_cap = n_cap;
@@ -302,7 +312,7 @@ gb_status setup_engine(Engine &E, int dev, int alg, int n_cap, int m_cap, int T,
   E.t_cap = std::max(T, 1024);
   E.slots = slots;
   const size_t tb = (size_t)E.t_cap * 4;
-  const size_t bytes = 10 * (tb + 256) + sizeof(BatchParams) + 2048;
+  const size_t bytes = 11 * (tb + 256) + sizeof(BatchParams) + 2048 + (size_t)gb_ml_num_params() * 4 + 256;
   GB_CUDA_TRY(cudaMalloc(&E.table, bytes));
   GB_CUDA_TRY(cudaMemset(E.table, 0, bytes));
   char *p = E.table;
@@ -314,6 +324,8 @@ gb_status setup_engine(Engine &E, int dev, int alg, int n_cap, int m_cap, int T,
   E.dn = (int *)take(tb); E.dm = (int *)take(tb); E.dk = (int *)take(tb); E.dtid = (unsigned *)take(tb);
   E.dorder = (int *)take(tb); E.diters = (int *)take(tb); E.derr = (float *)take(tb); E.dok = (int *)take(tb);
   E.dqueue = (int *)take(256); E.dbytes = (double *)take(256);
+  E.dfb = (int *)take(tb);
+  E.ml_params = (float *)take((size_t)gb_ml_num_params() * 4);
   E.d_params = (BatchParams *)take(sizeof(BatchParams));
   int sms = 0;
   GB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -350,6 +362,11 @@ gb_status setup_engine(Engine &E, int dev, int alg, int n_cap, int m_cap, int T,
     w.part_cap = gb_dense_part_floats_av(w.av_ntile, w.av_nsplit);
     GB_TRY(A((void **)&w.part, w.part_cap * 4));
     GB_TRY(A((void **)&w.av_tickets, (size_t)w.av_ntile * 4));
+    if (learned) {
+      w.ml_params = E.ml_params;
+      GB_TRY(A((void **)&w.ml_counts, (size_t)gb_ml_rank_bins() * 4));
+      GB_TRY(A((void **)&w.ml_cum, (size_t)gb_ml_rank_bins() * 4));
+    }
     GbState st0;
     memset(&st0, 0, sizeof(st0));
     st0.lda = lda;
@@ -390,8 +407,8 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
     gb_set_error_message("batched form supports NIHT, HTP and CGIHT", __FILE__, __LINE__);
     return GB_BAD_ARG;
   }
-  if (b->use_learned) {
-    gb_set_error_message("use_learned must be 0", __FILE__, __LINE__);
+  if (b->use_learned && (b->alg != GB_ALG_CGIHT || !b->learned_params)) {
+    gb_set_error_message("use_learned needs CGIHT and learned_params", __FILE__, __LINE__);
     return GB_BAD_ARG;
   }
   if (b->maxiter < 0) {
@@ -412,13 +429,15 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
   if (T == 0) return GB_OK;
   int dev = 0;
   GB_CUDA_TRY(cudaGetDevice(&dev));
-  Engine &E = g_engines[dev];
+  const int learned = b->use_learned ? 1 : 0;
+  Engine &E = g_engines[dev * 2 + learned];
   const bool reuse = E.dev == dev && E.alg == b->alg && E.n_cap >= n_cap && E.m_cap >= m_cap && E.t_cap >= T;
   if (!reuse) {
     release(E);
     size_t free_b = 0, total_b = 0;
     GB_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
-    GB_TRY(setup_engine(E, dev, b->alg, n_cap, m_cap, T, slots_for(n_cap, m_cap, free_b, std::max(T, 16))));
+    GB_TRY(setup_engine(E, dev, b->alg, n_cap, m_cap, T, slots_for(n_cap, m_cap, free_b, std::max(T, 16)),
+                        learned));
   }
   cudaStream_t s = (cudaStream_t)b->stream;
   // trial table, longest (m*n) first
@@ -432,6 +451,11 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
   bp.T = T; bp.seed = b->seed; bp.tol_rel = b->tol_rel; bp.maxiter = b->maxiter; bp.alg = b->alg;
   bp.n = E.dn; bp.m = E.dm; bp.k = E.dk; bp.tid = E.dtid; bp.order = E.dorder; bp.queue = E.dqueue;
   bp.iters = E.diters; bp.err = E.derr; bp.ok = E.dok; bp.bytes = E.dbytes;
+  bp.learned = learned;
+  bp.fb = learned ? E.dfb : nullptr;
+  if (learned)
+    GB_CUDA_TRY(cudaMemcpyAsync(E.ml_params, b->learned_params, sizeof(float) * gb_ml_num_params(),
+                                cudaMemcpyDeviceToDevice, s));
   GB_CUDA_TRY(cudaMemcpyAsync(E.dn, b->n, (size_t)T * 4, cudaMemcpyHostToDevice, s));
   GB_CUDA_TRY(cudaMemcpyAsync(E.dm, b->m, (size_t)T * 4, cudaMemcpyHostToDevice, s));
   GB_CUDA_TRY(cudaMemcpyAsync(E.dk, b->k, (size_t)T * 4, cudaMemcpyHostToDevice, s));
@@ -449,9 +473,10 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
     GB_CUDA_TRY(cudaStreamWaitEvent(s, E.done[i], 0));
   }
   GB_CUDA_TRY(cudaEventRecord(E.e1, s));
-  std::vector<int> hit(T), hok(T);
+  std::vector<int> hit(T), hok(T), hfb(T, 0);
   std::vector<float> herr(T);
   double hbytes = 0.0;
+  if (learned) GB_CUDA_TRY(cudaMemcpyAsync(hfb.data(), E.dfb, (size_t)T * 4, cudaMemcpyDeviceToHost, s));
   GB_CUDA_TRY(cudaMemcpyAsync(hit.data(), E.diters, (size_t)T * 4, cudaMemcpyDeviceToHost, s));
   GB_CUDA_TRY(cudaMemcpyAsync(herr.data(), E.derr, (size_t)T * 4, cudaMemcpyDeviceToHost, s));
   GB_CUDA_TRY(cudaMemcpyAsync(hok.data(), E.dok, (size_t)T * 4, cudaMemcpyDeviceToHost, s));
@@ -459,6 +484,43 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
   GB_CUDA_TRY(cudaStreamSynchronize(s));
   cudaEventElapsedTime(&g_last_kernel_ms, E.e0, E.e1);
   g_last_bytes = hbytes;
+  if (learned) {
+    // trials whose warm start was abandoned: plain zero-initialised CGIHT decides
+    std::vector<int> sn, sm, sk, idx;
+    std::vector<unsigned> stid;
+    for (int t = 0; t < T; ++t)
+      if (hfb[t]) {
+        idx.push_back(t);
+        sn.push_back(b->n[t]);
+        sm.push_back(b->m[t]);
+        sk.push_back(b->k[t]);
+        stid.push_back(tid[t]);
+      }
+    if (!idx.empty()) {
+      const float ms1 = g_last_kernel_ms;
+      const double by1 = g_last_bytes;
+      gb_batch pb = *b;
+      pb.ntrials = (int)idx.size();
+      pb.n = sn.data();
+      pb.m = sm.data();
+      pb.k = sk.data();
+      pb.trial_id = stid.data();
+      pb.use_learned = 0;
+      pb.learned_params = nullptr;
+      const int F = (int)idx.size();
+      std::vector<int> pit(F), pok(F);
+      std::vector<float> perr(F);
+      GB_TRY(gb_cs_solve_batch(&pb, pit.data(), perr.data(), pok.data(), nullptr));
+      for (int q = 0; q < F; ++q) {
+        const int t = idx[q];
+        hit[t] += pit[q];
+        herr[t] = perr[q];
+        hok[t] = pok[q];
+      }
+      g_last_kernel_ms += ms1;
+      g_last_bytes += by1;
+    }
+  }
   int ns = 0;
   for (int t = 0; t < T; ++t) {
     if (iters_out) iters_out[t] = hit[t];

@@ -151,6 +151,7 @@ __device__ __forceinline__ void ctrl_phase(GbState *st, int phase, cudaGraphCond
       break;
     case C_CGIHT_INIT:
       st->err = sqrt_red(st, R_RES);
+      st->err_warm0 = st->err;
       st->prev[15] = st->err;
       for (int j = 0; j < 15; ++j) st->evol[j] = st->evol[j + 1];
       st->evol[15] = st->prev[14] - st->prev[15];
@@ -310,6 +311,13 @@ __device__ __forceinline__ void ctrl_phase(GbState *st, int phase, cudaGraphCond
         if (st->op_kind == GB_OP_DENSE) st->bytes += dense_bytes(st, 1, st->flags[F_UCG] ? 3 : 2);
         st->err = st->prev[15];
         finish_iteration(st, 749);
+        // learned warm start: give up when the residual has not dropped below the warm
+        // start's within 10 iterations (the caller then solves from zero)
+        if (st->learned && st->iter == 10 && st->active && !(st->err < st->err_warm0)) {
+          st->active = 0;
+          st->fell_back = 1;
+          st->stop_reason = 8;
+        }
         if (st->restart) { st->flags[F_UCG] = 0; st->flags[F_RCG] = 1; }
         else { st->flags[F_UCG] = st->supp_change ? 1 : 0; st->flags[F_RCG] = st->supp_change ? 0 : 1; }
       }

@@ -73,6 +73,9 @@ struct GbState {
   // batched form: current trial index and algorithmic operator bytes of this trial
   int trial, op_kind;
   double bytes;
+  // learned warm start (CGIHT): on, gave up after 10 iterations, residual at the warm x0
+  int learned, fell_back;
+  float err_warm0;
 };
 
 // Operator description on the device.
@@ -111,6 +114,8 @@ struct GbWork {
   float *rec;    // l0 residual record (maxiter + 1)
   GbOp op;          // dimensions here are capacities when dyn is set
   int dyn;          // 1: kernels read m, n, lda, num_bins, k of the current trial from GbState
+  const float *ml_params;    // learned warm start: MLP parameters (null: plain start)
+  int *ml_counts, *ml_cum;   // its rank histogram (4096 bins) and prefix
   int num_sms;
   int red_blocks;   // grid of reducing kernels (fixed -> deterministic reductions)
   int wide_blocks;  // grid of the dense streaming kernels
@@ -263,6 +268,11 @@ gb_status gb_gemm_tc(const GbGemm &g, cudaStream_t s);
 gb_status gb_gemm_tc_check();
 // which kernel gb_gemm uses: 1 tcgen05 (default), 0 the mma.sync kernel (GB_CS_GEMM=mma)
 int gb_gemm_use_tc();
+
+// learned warm start (gb_learned.cu): x = g . net(features) for g = A^T y held in x
+void enq_learned_warm(GbWork &w, cudaStream_t s, int pf);
+int gb_ml_num_params();
+int gb_ml_rank_bins();
 
 // solver (gb_solver.cu)
 enum { GB_RUN_SOLVE = 0, GB_RUN_L0 = 1 };

@@ -463,6 +463,12 @@ void enq_prologue(SolvePlan &P, cudaStream_t s0, cudaGraphConditionalHandle h_ou
   // x = A^T y ; max |x| ; FindSupportSet ; Threshold  (algorithms.cu:1335-1354)
   enq_AT(w, s0, w.y, w.x, F_ALWAYS);
   k_copy_norm<<<w.red_blocks, 256, 0, s0>>>(w.st, F_ALWAYS, w.x, nullptr, n, -1, R_XMAX, w.red_part, w.tickets);
+  if (P.alg == GB_ALG_CGIHT && w.ml_params) {
+    // learned warm start: x = g . net(features of g); the support selection below keeps
+    // the k largest |x| (GAGA/gaga/algorithms.cu:3776 starts from H_k(A^T y) instead)
+    enq_learned_warm(w, s0, F_ALWAYS);
+    k_copy_norm<<<w.red_blocks, 256, 0, s0>>>(w.st, F_ALWAYS, w.x, nullptr, n, -1, R_XMAX, w.red_part, w.tickets);
+  }
   enq_ctrl(w, s0, C_INIT_BINPREP);
   k_axpy<<<w.red_blocks, 256, 0, s0>>>(w.st, F_ALWAYS, SC_ONE, w.x, w.x, 0, -1, -1, w.counters, num_bins,
                                        w.red_part, w.tickets);
@@ -672,6 +678,7 @@ static GbState initial_state(const GbWork &w, int alg, const gb_options &o, int 
   st.l0_len = 2 * w.op.d;
   st.flags[F_ALWAYS] = 1;
   st.op_kind = w.op.kind;
+  st.learned = (w.ml_params && alg == GB_ALG_CGIHT) ? 1 : 0;
   return st;
 }
 

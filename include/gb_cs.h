@@ -65,6 +65,8 @@ typedef struct {
   float alpha;          /* 'alpha'          0.25 (used by the timing variants only) */
   int support_flag;     /* 'supportFlag'    0 (timing variants only) */
   int timing;           /* 'timing'         0 (accepted; timing variants are not built) */
+  const float *learned_params; /* extension: CGIHT only, device pointer to the warm-start
+                           MLP's gb_cs_mlp_num_params() FP32 parameters; NULL = plain start */
 } gb_options;
 
 /* A recovery problem in "given data" form. */
@@ -93,6 +95,8 @@ typedef struct {
   float resid_prev[16]; /* residNorm_prev at exit */
   int stop_reason;      /* 1 tol, 2 maxiter, 3 divergence, 4 stall, 5 cycle, 6 slow rate, 7 no candidates */
   float *res_record;    /* parallel_l0: caller buffer of maxiter+1 floats or NULL (resRecord) */
+  int warm_start;       /* learned warm start: 0 not used, 1 used, 2 abandoned after 10
+                           iterations and solved again from zero (iter counts both runs) */
 } gb_result;
 
 /* Support-selection state carried between FindSupportSet calls. */
@@ -183,7 +187,9 @@ typedef struct {
   int alg;                       /* GB_ALG_NIHT or GB_ALG_CGIHT */
   float tol_rel;
   int maxiter;
-  int use_learned;               /* reserved, must be 0 */
+  int use_learned;               /* CGIHT only: learned warm start, falling back to a plain
+                                    solve for trials whose residual does not drop in 10 iterations */
+  const float *learned_params;   /* device pointer to the MLP parameters when use_learned */
   void *stream;
 } gb_batch;
 
@@ -220,6 +226,25 @@ typedef struct {
 
 gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *iters_out, float *rel_err_out,
                                    int *success_out, int *num_success);
+
+/* ---- learned warm start (no reference counterpart) ----
+ * A per-coordinate MLP 4 -> 64 -> 64 -> 1 (GELU; weights rounded to BF16 at use, FP32
+ * accumulation) maps the features of coordinate i of a problem, g = A^T y:
+ *   |g_i| / max|g|, rank fraction of |g_i| (0 = largest), delta = m/n, rho = k/m
+ * to w_i ~ x_i / g_i of the final solution; CGIHT then starts from H_k(w . g).
+ * Parameters are FP32 on the device in the order W1[64][4] b1[64] W2[64][64] b2[64] W3[64] b3. */
+int gb_cs_mlp_num_params(void);
+/* features (n x 4 row-major, device) of g (device, n); synchronous */
+gb_status gb_cs_mlp_features(const float *d_g, int n, int m, int k, float *d_feat, void *stream);
+/* network outputs for ns feature rows */
+gb_status gb_cs_mlp_forward(const float *d_params, const float *d_feat, int ns, float *d_out, void *stream);
+/* gradient of the mean squared error against d_tgt over all ns rows (and the loss); synchronous */
+gb_status gb_cs_mlp_grad(const float *d_params, const float *d_feat, const float *d_tgt, int ns, float *d_grad,
+                         float *d_loss, void *stream);
+/* Adam training in place (minibatches of `batch` rows, `epochs` shuffled passes); the mean
+ * minibatch loss of each epoch goes to h_epoch_loss (host, epochs floats) if not NULL */
+gb_status gb_cs_mlp_train(float *d_params, const float *d_feat, const float *d_tgt, int ns, int batch, int epochs,
+                          float lr, unsigned int seed, float *h_epoch_loss, void *stream);
 
 /* GEMM FLOPs issued and device time in ms of the last gb_cs_solve_shared_batch call on this
  * thread (no reference counterpart; used for roofline reporting). */

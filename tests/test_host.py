@@ -25,6 +25,20 @@ def test_library_exports_every_declared_symbol(gb):
     assert sorted(gb._lib.EXPORTS) == syms
 
 
+def test_library_links_every_translation_unit(gb):
+    """Every symbol the library needs is defined in it or versioned in the C/C++ runtime (a
+    translation unit left out of the build shows up as an unversioned undefined symbol)."""
+    import shutil
+    import subprocess
+
+    nm = shutil.which("nm")
+    if nm is None:
+        pytest.skip("nm not available")
+    out = subprocess.run([nm, "-D", "--undefined-only", gb._lib.LIB_PATH], capture_output=True, text=True).stdout
+    missing = [ln.split()[-1] for ln in out.splitlines() if ln.split() and ln.split()[0] == "U" and "@" not in ln]
+    assert not missing, missing
+
+
 def test_default_options_mirror_reference(gb):
     L = gb._lib.load()
     o = gb._lib.Options()
