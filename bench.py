@@ -14,10 +14,10 @@ Problem generation runs inside the timed region.
   value : recovered trials / device time of both forms' kernels
   e2e   : recovered trials / wall time of the two calls made with host arrays (trial
           tables in, per-trial iterations/errors/verdicts out)
-  plain : the single-trial FP32 drop-in on samples of both parts (gb_cs_generate_and_solve
-          for independent trials, gb_cs_solve on the shared A for shared trials), scaled
-          to the 3072 + 1024 mix, for the tuned-vs-plain ratio; the verdicts of the same
-          trials give the agreement between the two forms
+  plain : the single-trial FP32 drop-in on the first timed step's trials (all 768 + 256 by
+          default; gb_cs_generate_and_solve for independent trials, gb_cs_solve on the shared A
+          for shared trials), scaled to the 3072 + 1024 mix, for the tuned-vs-plain ratio; the
+          verdicts of the same trials give the agreement between the two forms
   learned_warm_start : the trained MLP warm start for CGIHT against zero-initialised CGIHT
           on 2048 fresh trials of its workload (n = 8192, delta 0.1-0.6, rho 0.05-0.45)
   cpu_baseline / --impl reference : the CPU oracle (oracle/gbo.c, OpenMP inside each
@@ -420,7 +420,7 @@ def bench_plain(args, first_step):
     w, r = first_step
     n, m, k, tid = wave_arrays(w)
     cnt = args.plain_trials
-    sel = np.linspace(0, len(n) - 1, cnt).astype(int)
+    sel = np.linspace(0, len(n) - 1, min(cnt, len(n))).astype(int)
     ok = agree = 0
     t0 = time.perf_counter()
     for i in sel:
@@ -438,7 +438,7 @@ def bench_plain(args, first_step):
                                                    tol_rel=TOL_REL, maxiter=MAXITER, first_trial=first, outputs=True)
     torch.cuda.synchronize()
     X0h = X0.cpu().numpy()
-    sel2 = np.linspace(0, len(ks) - 1, max(4, cnt // 2)).astype(int)
+    sel2 = np.linspace(0, len(ks) - 1, min(len(ks), max(4, cnt // 3))).astype(int)
     ok = agree = 0
     tt = 0.0
     for t in sel2:
@@ -498,7 +498,9 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--plain-trials", type=int, default=32)
+    ap.add_argument("--plain-trials", type=int, default=768,
+                    help="independent trials of the first timed step solved by the plain form (768 = all); a third "
+                         "as many shared-matrix trials")
     ap.add_argument("--cpu-trials", type=int, default=32)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--learned-trials", type=int, default=2048)

@@ -17,7 +17,7 @@ import ctypes as C
 
 import numpy as np
 
-from . import _lib, sweep
+from . import _lib, learned, sweep
 from ._lib import GagaError
 
 __all__ = ["gaga_cs", "gaga_options", "GagaError", "solve_batch", "version"]
