@@ -1,0 +1,90 @@
+"""Parity at the full workload sizes through properties that do not depend on size.
+
+  DCT      n = 2^20, m = 2^18 rows, k = m/10, Gaussian values: CGIHT and HTP recover the
+           planted signal (relative l2 <= 1e-3) and every significant entry of its support, and the returned
+           x meets the residual tolerance under the oracle's FP64 operator; with noise of
+           1e-3 relative l2 the error stays at the noise level.
+  expander n = 2^18, m = 2^16, d = 7: NIHT and CGIHT recover the planted signal on the
+           1/sqrt(d) matrix; parallel_l0 on the unit-valued matrix with a +-1 signal
+           (integer residuals) equals the oracle bit for bit: x, iterations, residual record.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _support_matches(x, x0):
+    """Every significant entry of x0 (above 1% of its rms on the support; all of them for
+    +-1 signals) is among the |supp(x0)| largest |x|."""
+    s0 = np.flatnonzero(x0)
+    top = np.argsort(-np.abs(x), kind="stable")[: len(s0)]
+    rms = np.linalg.norm(x0) / np.sqrt(len(s0))
+    big = np.flatnonzero(np.abs(x0) > 1e-2 * rms)
+    return np.all(np.isin(big, top))
+
+
+@pytest.mark.parametrize("alg", ["CGIHT", "HTP"])
+def test_dct_full_size(gb, gbo, alg):
+    n, m = 2 ** 20, 2 ** 18
+    k = m // 10
+    rows = gbo.gen_dct_rows(n, m, seed=21)
+    x0, ks = gbo.gen_vector(n, k, 2, seed=21)
+    op = gbo.Op.dct(n, rows)
+    y = gbo.A(op, x0)
+    tol = 1e-4 * float(np.linalg.norm(y))
+    x, iters, conv = gb.gaga_cs(alg, "dct", y, rows, ks, m, n, gb.gaga_options("tol", tol), index_base=0)
+    assert np.linalg.norm(x - x0) / np.linalg.norm(x0) < 1e-3
+    assert _support_matches(x, x0)
+    r = y - gbo.A(op, x)
+    assert np.linalg.norm(r) <= 1.01 * tol
+    assert 0 < iters < 300
+
+
+def test_dct_full_size_noise(gb, gbo):
+    n, m = 2 ** 20, 2 ** 18
+    k = m // 10
+    rows = gbo.gen_dct_rows(n, m, seed=22)
+    x0, ks = gbo.gen_vector(n, k, 2, seed=22)
+    op = gbo.Op.dct(n, rows)
+    y = gbo.A(op, x0)
+    e = np.random.default_rng(22).standard_normal(m)
+    y = (y + e * (1e-3 * np.linalg.norm(y) / np.linalg.norm(e))).astype(np.float32)
+    tol = 1e-4 * float(np.linalg.norm(y))  # below the noise: the stall rules end the solve
+    x, iters, conv = gb.gaga_cs("CGIHT", "dct", y, rows, ks, m, n, gb.gaga_options("tol", tol), index_base=0)
+    assert np.linalg.norm(x - x0) / np.linalg.norm(x0) < 1e-2
+    assert _support_matches(x, x0)
+    assert iters < 5000
+
+
+@pytest.mark.parametrize("alg", ["NIHT", "CGIHT"])
+def test_expander_full_size(gb, gbo, alg):
+    n, m, d = 2 ** 18, 2 ** 16, 7
+    k = m // 20
+    rows, vals = gbo.gen_smv(m, n, d, 1, seed=31)
+    x0, ks = gbo.gen_vector(n, k, 1, seed=31)
+    op = gbo.Op.smv(m, n, d, rows, vals)
+    y = gbo.A(op, x0)
+    tol = 1e-4 * float(np.linalg.norm(y))
+    cols = np.repeat(np.arange(n, dtype=np.int32), d)
+    x, iters, conv, rec, trec = gb.gaga_cs(alg, "smv", y, rows, cols, vals, ks, gb.gaga_options("tol", tol),
+                                           index_base=0)
+    assert np.linalg.norm(x - x0) / np.linalg.norm(x0) < 1e-3
+    assert _support_matches(x, x0)
+
+
+def test_expander_full_size_parallel_l0_bit_exact(gb, gbo):
+    n, m, d = 2 ** 18, 2 ** 16, 7
+    k = m // 20
+    rows, vals = gbo.gen_smv(m, n, d, 3, seed=32)
+    x0, ks = gbo.gen_vector(n, k, 1, seed=32)
+    op = gbo.Op.smv(m, n, d, rows, vals)
+    y = gbo.A(op, x0)
+    cols = np.repeat(np.arange(n, dtype=np.int32), d)
+    opts = gb.gaga_options("tol", 1e-6, "maxiter", 300)
+    x, iters, conv, rec, trec = gb.gaga_cs("parallel_l0", "smv", y, rows, cols, vals, ks, opts, index_base=0)
+    xo, reso, reco, info = gbo.parallel_l0(op, y, tol=1e-6, maxiter=300)
+    assert iters == info.iter
+    assert np.array_equal(x, xo)
+    assert np.array_equal(rec[: iters + 1], reco[: iters + 1])
+    assert np.array_equal(x, x0)
