@@ -183,11 +183,19 @@ def bench_ours(args):
     peak, peak_kind = peaks()
     tpeak, tpeak_kind = tensor_peak()
 
+    # schedule of the batched form, measured on a probe of the first step (untimed)
+    from gaga_gb300 import autotune
+
+    n0, m0, k0, t0_ = wave_arrays(sweep_rank_first(rank, world))
+    sched = autotune.tune_batch(n0, m0, k0, SEED, t0_, alg="NIHT", tol_rel=TOL_REL, maxiter=MAXITER,
+                                use_cache=not args.retune)
+
     def solve_step(w):
         """One quarter of the sweep: independent trials, then the shared-matrix trials."""
         n, m, k, tid = wave_arrays(w)
         t0 = time.perf_counter()
-        ns, iters, err, ok = gb.solve_batch(n, m, k, SEED, tid, alg="NIHT", tol_rel=TOL_REL, maxiter=MAXITER)
+        ns, iters, err, ok = gb.solve_batch(n, m, k, SEED, tid, alg="NIHT", tol_rel=TOL_REL, maxiter=MAXITER,
+                                            slots=sched["slots"], sm_share=sched["sm_share"])
         t1 = time.perf_counter()
         nbytes, kms = gb.batch_last_stats()
         ks, first = shared_part(w)
@@ -222,7 +230,7 @@ def bench_ours(args):
             acc[key] = acc.get(key, 0) + r[key]
         # host-issued launches: one graph per slot stream of the batched form; the shared
         # form's 6 setup kernels, its graph and its verdict kernel
-        launches += gb.batch_slot_count() + 8
+        launches += sched["slots"] + 8
     torch.cuda.synchronize()
     clocks = sampler.stop()
     if world > 1:
@@ -249,6 +257,10 @@ def bench_ours(args):
                                    "tol 1e-4*||y||; one quarter of the sweep per step per GPU",
                        "form": "tuned: batched slot graphs (device trial queue, device generation) + shared-matrix "
                                "BF16 tensor-core GEMM form",
+                       "schedule": {"slots": sched["slots"], "sm_share": sched["sm_share"],
+                                    "picked_by": "autotune over %d candidates on %d probe trials%s" % (
+                                        len(sched["candidates"]), sched["probe_trials"],
+                                        " (cached)" if sched.get("cached") else "")},
                        "trials_per_step": int(acc["trials"] // max(1, args.steps)),
                        "l2": "working set >> L2 (A up to 966 MB per trial; shared form 600 MB of BF16 operands)"},
             "recovered": int(acc["ok"]), "trials": int(acc["trials"]),
@@ -296,6 +308,12 @@ def bench_learned(args):
     res["workload"] = "%d fresh CGIHT trials, n=8192, delta U[0.1,0.6], rho U[0.05,0.45], tol 1e-4*||y||" % (
         args.learned_trials)
     return res
+
+
+def sweep_rank_first(rank, world):
+    from gaga_gb300 import sweep
+
+    return sweep.rank_wave(rank, world, 0)
 
 
 def tensor_peak():
@@ -504,6 +522,7 @@ def main():
     ap.add_argument("--cpu-trials", type=int, default=32)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--learned-trials", type=int, default=2048)
+    ap.add_argument("--retune", action="store_true", help="ignore the autotuner's cache")
     ap.add_argument("--only", choices=["matvec", "gemm", "plain", "learned"],
                     help="run one measurement alone and print its JSON (for profiling)")
     args = ap.parse_args()

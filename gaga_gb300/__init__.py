@@ -17,7 +17,7 @@ import ctypes as C
 
 import numpy as np
 
-from . import _lib, learned, sweep
+from . import _lib, autotune, learned, sweep
 from ._lib import GagaError
 
 __all__ = ["gaga_cs", "gaga_options", "GagaError", "solve_batch", "version"]
@@ -248,9 +248,10 @@ def generate_and_solve(alg, ens, k, m, n, d=0, opts=None):
 
 
 def solve_batch(n, m, k, seed, trial_ids=None, alg="NIHT", tol_rel=1e-4, maxiter=5000, stream=None,
-                learned_params=None):
+                learned_params=None, slots=0, sm_share=0):
     """Batched multi-trial dense form (gb_cs_solve_batch); learned_params (a CUDA tensor of
-    MLP parameters, CGIHT only) turns on the learned warm start."""
+    MLP parameters, CGIHT only) turns on the learned warm start; slots / sm_share set the
+    schedule (0: automatic; gaga_gb300.autotune picks them by measurement)."""
     L = _lib.load()
     n = np.ascontiguousarray(n, dtype=np.int32)
     m = np.ascontiguousarray(m, dtype=np.int32)
@@ -259,7 +260,7 @@ def solve_batch(n, m, k, seed, trial_ids=None, alg="NIHT", tol_rel=1e-4, maxiter
     b = _lib.Batch(len(n), n.ctypes.data, m.ctypes.data, k.ctypes.data, None if tids is None else tids.ctypes.data,
                    int(seed) & 0xFFFFFFFF, {"NIHT": 0, "HTP": 1, "CGIHT": 6}[alg], float(tol_rel), int(maxiter),
                    0 if learned_params is None else 1,
-                   None if learned_params is None else learned_params.data_ptr(), stream)
+                   None if learned_params is None else learned_params.data_ptr(), int(slots), int(sm_share), stream)
     iters = np.zeros(len(n), dtype=np.int32)
     err = np.zeros(len(n), dtype=np.float32)
     ok = np.zeros(len(n), dtype=np.int32)

@@ -1,0 +1,83 @@
+"""Autotuner for the batched form's schedule.
+
+The batched form (gb_cs_solve_batch) runs `slots` trials at a time, each slot's kernels
+shaped for `sm_share` SMs (the dense A^T r grid is 4 CTAs per shared SM, the reductions one
+CTA per shared SM, and the A x_S row tiles x support splits fill whole waves of that many
+SMs).  Which pair is fastest depends on the GPU and on the mix of trial sizes, so it is
+measured: every candidate solves the same probe subset of the workload (every `stride`-th
+trial, all trial sizes represented), the second run of each is timed on the device, and the
+fastest candidate wins.  Results are cached per GPU, algorithm and trial-size mix in a JSON
+file (GB_CS_TUNE_CACHE, default ~/.cache/gaga_gb300/autotune.json).
+"""
+import json
+import os
+
+import numpy as np
+
+SLOTS = (8, 12, 16, 24)
+SHARE_FRACTIONS = (0.25, 0.5, 1.0)
+
+
+def _cache_path():
+    return os.environ.get("GB_CS_TUNE_CACHE",
+                          os.path.join(os.path.expanduser("~"), ".cache", "gaga_gb300", "autotune.json"))
+
+
+def _key(alg, n, m):
+    import torch
+
+    name = torch.cuda.get_device_name()
+    sizes = sorted(set(zip(np.asarray(n).tolist(), np.asarray(m).tolist())))
+    h = hash(tuple(sizes)) & 0xFFFFFFFF
+    return "%s|%s|%d sizes|%08x" % (name, alg, len(sizes), h)
+
+
+def tune_batch(n, m, k, seed, trial_ids=None, alg="NIHT", tol_rel=1e-4, maxiter=5000, stride=4, use_cache=True,
+               slots=SLOTS, fractions=SHARE_FRACTIONS, log=None):
+    """Pick (slots, sm_share) for solving trials like (n, m, k); returns a dict with the
+    choice and the measured device milliseconds of every candidate on the probe."""
+    import torch
+
+    import gaga_gb300 as gb
+
+    n, m, k = (np.asarray(a, dtype=np.int32) for a in (n, m, k))
+    tid = np.arange(len(n), dtype=np.uint32) if trial_ids is None else np.asarray(trial_ids, dtype=np.uint32)
+    key = _key(alg, n, m)
+    path = _cache_path()
+    cache = {}
+    if use_cache and os.path.exists(path):
+        try:
+            with open(path) as f:
+                cache = json.load(f)
+        except (OSError, ValueError):
+            cache = {}
+        if key in cache:
+            return dict(cache[key], cached=True)
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    # the probe: every stride-th trial in descending size order, so every size class appears
+    order = np.argsort(-(n.astype(np.int64) * m), kind="stable")
+    probe = np.sort(order[::stride])
+    pn, pm, pk, pt = n[probe], m[probe], k[probe], tid[probe]
+    table = []
+    for s in slots:
+        for fr in fractions:
+            share = max(1, int(round(sms * fr)))
+            for rep in range(2):  # the first run builds the engine and its graphs
+                ns, it, err, ok = gb.solve_batch(pn, pm, pk, seed, pt, alg=alg, tol_rel=tol_rel, maxiter=maxiter,
+                                                 slots=s, sm_share=share)
+            _, ms = gb.batch_last_stats()
+            table.append({"slots": s, "sm_share": share, "ms": ms, "recovered": int(ns)})
+            if log:
+                log(json.dumps(table[-1]))
+    best = min(table, key=lambda r: r["ms"])
+    res = {"slots": best["slots"], "sm_share": best["sm_share"], "probe_trials": int(len(probe)),
+           "candidates": table, "key": key}
+    if use_cache:
+        cache[key] = res
+        try:
+            os.makedirs(os.path.dirname(path), exist_ok=True)
+            with open(path, "w") as f:
+                json.dump(cache, f, indent=1)
+        except OSError:
+            pass
+    return dict(res, cached=False)

@@ -204,7 +204,7 @@ struct Slot {
 };
 
 struct Engine {
-  int dev = -1, alg = -1, n_cap = 0, m_cap = 0, t_cap = 0, slots = 0, learned = 0;
+  int dev = -1, alg = -1, n_cap = 0, m_cap = 0, t_cap = 0, slots = 0, learned = 0, sm_share = 0;
   float *ml_params = nullptr;  // the warm-start MLP parameters (copied in by every call)
   int *dfb = nullptr;
   std::vector<Slot> slot;
@@ -299,12 +299,14 @@ gb_status build_slot_graph(Engine &E, Slot &S) {
   return GB_OK;
 }
 
-gb_status setup_engine(Engine &E, int dev, int alg, int n_cap, int m_cap, int T, int slots, int learned) {
+gb_status setup_engine(Engine &E, int dev, int alg, int n_cap, int m_cap, int T, int slots, int learned,
+                       int sm_share) {
   if (E.dev == dev && E.alg == alg && E.n_cap >= n_cap && E.m_cap >= m_cap && E.t_cap >= T && E.slots == slots &&
-      E.learned == learned)
+      E.learned == learned && E.sm_share == sm_share)
     return GB_OK;
   release(E);
   E.learned = learned;
+  E.sm_share = sm_share;
   E.dev = dev;
   E.alg = alg;
   E.n_cap = n_cap;
@@ -337,9 +339,9 @@ gb_status setup_engine(Engine &E, int dev, int alg, int n_cap, int m_cap, int T,
     memset(&w, 0, sizeof(w));
     w.dyn = 1;
     w.num_sms = sms;
-    // slots run concurrently: each slot's kernels take a fraction of the GPU
-    w.red_blocks = std::max(1, sms / 2);
-    w.wide_blocks = sms * 2;
+    // slots run concurrently: each slot's kernels are shaped for sm_share SMs
+    w.red_blocks = std::max(1, std::min(GB_MAXRB, sm_share));
+    w.wide_blocks = sm_share * 4;
     GbOp &op = w.op;
     op.kind = GB_OP_DENSE;
     op.m = m_cap;
@@ -358,7 +360,7 @@ gb_status setup_engine(Engine &E, int dev, int alg, int n_cap, int m_cap, int T,
     for (int **v : {&w.bins, &w.bins_prev, &w.S, &S.hist}) GB_TRY(A((void **)v, (size_t)n_cap * 4));
     GB_TRY(A((void **)&w.counters, (size_t)std::max(n_cap / 20, 1000) * 4));
     GB_TRY(A((void **)&w.tile_cnt, (size_t)((n_cap + GB_TILE - 1) / GB_TILE) * 4));
-    gb_dense_av_shape(m_cap, sms / 2, &w.av_ntile, &w.av_nsplit);
+    gb_dense_av_shape(m_cap, sm_share, &w.av_ntile, &w.av_nsplit);
     w.part_cap = gb_dense_part_floats_av(w.av_ntile, w.av_nsplit);
     GB_TRY(A((void **)&w.part, w.part_cap * 4));
     GB_TRY(A((void **)&w.av_tickets, (size_t)w.av_ntile * 4));
@@ -383,9 +385,10 @@ gb_status setup_engine(Engine &E, int dev, int alg, int n_cap, int m_cap, int T,
   return GB_OK;
 }
 
-// Number of slots: enough concurrency for small trials, within 60% of free memory.
-int slots_for(int n_cap, int m_cap, size_t free_bytes, int T) {
-  int s = 16;
+// Number of slots: the requested count (default 16: enough concurrency for small trials),
+// within 60% of free memory.
+int slots_for(int n_cap, int m_cap, size_t free_bytes, int T, int requested) {
+  int s = requested > 0 ? requested : 16;
   if (const char *e = getenv("GB_CS_BATCH_SLOTS")) s = std::max(1, atoi(e));
   const double per = (double)((m_cap + 31) / 32 * 32) * n_cap * 4.0 * 1.05 + 64.0 * n_cap + (1 << 24);
   while (s > 1 && s * per > 0.6 * (double)free_bytes) s--;
@@ -431,13 +434,17 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
   GB_CUDA_TRY(cudaGetDevice(&dev));
   const int learned = b->use_learned ? 1 : 0;
   Engine &E = g_engines[dev * 2 + learned];
-  const bool reuse = E.dev == dev && E.alg == b->alg && E.n_cap >= n_cap && E.m_cap >= m_cap && E.t_cap >= T;
+  int sms = 0;
+  GB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int sm_share = b->sm_share > 0 ? std::min(b->sm_share, sms) : std::max(1, sms / 2);
+  const bool reuse = E.dev == dev && E.alg == b->alg && E.n_cap >= n_cap && E.m_cap >= m_cap && E.t_cap >= T &&
+                     E.sm_share == sm_share && (b->slots <= 0 || E.slots == b->slots);
   if (!reuse) {
     release(E);
     size_t free_b = 0, total_b = 0;
     GB_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
-    GB_TRY(setup_engine(E, dev, b->alg, n_cap, m_cap, T, slots_for(n_cap, m_cap, free_b, std::max(T, 16)),
-                        learned));
+    GB_TRY(setup_engine(E, dev, b->alg, n_cap, m_cap, T,
+                        slots_for(n_cap, m_cap, free_b, std::max(T, 16), b->slots), learned, sm_share));
   }
   cudaStream_t s = (cudaStream_t)b->stream;
   // trial table, longest (m*n) first

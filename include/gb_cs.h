@@ -190,6 +190,8 @@ typedef struct {
   int use_learned;               /* CGIHT only: learned warm start, falling back to a plain
                                     solve for trials whose residual does not drop in 10 iterations */
   const float *learned_params;   /* device pointer to the MLP parameters when use_learned */
+  int slots;                     /* schedule: concurrent trial slots (0: 16, fewer if memory is short) */
+  int sm_share;                  /* schedule: SMs each slot's kernels are shaped for (0: half the GPU) */
   void *stream;
 } gb_batch;
 

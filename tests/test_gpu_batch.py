@@ -66,3 +66,26 @@ def test_batch_rejects_bad_sizes(gb):
         gb.solve_batch([100], [200], [5], SEED)
     with pytest.raises(gb.GagaError):
         gb.solve_batch([8], [4], [1], SEED)
+
+
+def test_batch_schedule_and_autotune(gb, tmp_path, monkeypatch):
+    """Explicit schedules give the same verdicts on problems away from the phase transition,
+    and the autotuner returns one of its measured candidates."""
+    from gaga_gb300 import autotune
+
+    monkeypatch.setenv("GB_CS_TUNE_CACHE", str(tmp_path / "tune.json"))
+    n = np.array([1024, 2048, 4096] * 8, dtype=np.int32)
+    m = (n // 2).astype(np.int32)
+    k = (m // 20).astype(np.int32)  # rho = 0.05: deep inside the recovery region
+    tid = np.arange(len(n), dtype=np.uint32)
+    ref = gb.solve_batch(n, m, k, SEED, tid, alg="NIHT", maxiter=1000)
+    for slots, share in ((4, 38), (12, 152)):
+        got = gb.solve_batch(n, m, k, SEED, tid, alg="NIHT", maxiter=1000, slots=slots, sm_share=share)
+        assert got[0] == ref[0] == len(n)
+    res = autotune.tune_batch(n, m, k, SEED, tid, alg="NIHT", maxiter=1000, stride=2, slots=(4, 8),
+                              fractions=(0.5, 1.0))
+    assert (res["slots"], res["sm_share"]) in {(c["slots"], c["sm_share"]) for c in res["candidates"]}
+    assert len(res["candidates"]) == 4 and not res["cached"]
+    again = autotune.tune_batch(n, m, k, SEED, tid, alg="NIHT", maxiter=1000, stride=2, slots=(4, 8),
+                                fractions=(0.5, 1.0))
+    assert again["cached"] and again["slots"] == res["slots"]
