@@ -15,7 +15,7 @@ STATUS_NAMES = {0: "GB_OK", 1: "GB_BAD_ARG", 2: "GB_OOM", 3: "GB_WATCHDOG", 4: "
                 5: "GB_UNSUPPORTED", 6: "GB_NO_DEVICE"}
 GB_OP_DENSE, GB_OP_DCT, GB_OP_SMV = 0, 1, 2
 GB_HOST, GB_DEVICE = 0, 1
-GB_ALG_NIHT, GB_ALG_HTP, GB_ALG_CGIHT, GB_ALG_PARALLEL_L0 = 0, 1, 6, 14
+GB_ALG_NIHT, GB_ALG_HTP, GB_ALG_IHT, GB_ALG_HT_SD, GB_ALG_HT_CG, GB_ALG_CGIHT, GB_ALG_PARALLEL_L0 = 0, 1, 2, 3, 4, 6, 14
 
 # every symbol include/gb_cs.h declares
 EXPORTS = ["gb_cs_version", "gb_cs_last_error", "gb_cs_default_options", "gb_cs_alg_id", "gb_cs_solve",

@@ -47,7 +47,14 @@ enum {
   C_CGIHT_STOP,
   C_L0_INIT,
   C_L0_PRE,
-  C_L0_STOP
+  C_L0_STOP,
+  C_IHT_INIT,     // IHT: bins keep the scale of A^T y; first loop test
+  C_IHT_PREP,     // IHT: maxChange = 2 mu max|grad|; binning decision
+  C_IHT_STOP,     // IHT: residual history and stopping rules (no cycle test)
+  C_HTSD_MU,      // ThresholdSD: RestrictedSD step size, support kept
+  C_HTSD_STOP,    // ThresholdSD: stopping rules
+  C_HTCG_INIT,    // ThresholdCG: CG start on the thresholded support
+  C_HTCG_STOP     // ThresholdCG: squared-residual history and stopping rules
 };
 
 static __device__ float max_list(const float *a, int n) {
@@ -116,6 +123,46 @@ static __device__ void bin_decision(GbState *st) {
   }
 }
 
+// IHT loop test (GAGA/gaga/algorithms.cu:416): NIHT's rules without the cycle test
+static __device__ int iht_going(GbState *st) {
+  const int go = (st->err > st->tol) & (st->iter < st->maxiter) & (st->err < (100.0f * st->err_start)) &
+                 ((double)st->resid_diff > 0.01 * (double)st->tol) & (st->fail == 0);
+  if (!go && st->stop_reason == 0) {
+    if (!(st->err > st->tol)) st->stop_reason = 1;
+    else if (!(st->iter < st->maxiter)) st->stop_reason = 2;
+    else if (!(st->err < 100.0f * st->err_start)) st->stop_reason = 3;
+    else if (!((double)st->resid_diff > 0.01 * (double)st->tol)) st->stop_reason = 4;
+    else st->stop_reason = 6;
+  }
+  return go;
+}
+
+// ThresholdSD / ThresholdCG loop tests (algorithms.cu:861, 1937): tolerance, maxiter and a
+// stall threshold (0.1 tol on norms for SD, 10 tol^2 on squared norms for CG)
+static __device__ int ht_going(GbState *st, float err_tol, float stall_tol) {
+  const int go = (st->err > err_tol) & (st->iter < st->maxiter) & (st->resid_diff > stall_tol);
+  if (!go && st->stop_reason == 0) {
+    if (!(st->err > err_tol)) st->stop_reason = 1;
+    else if (!(st->iter < st->maxiter)) st->stop_reason = 2;
+    else st->stop_reason = 4;
+  }
+  return go;
+}
+
+static __device__ void evolve16(GbState *st) {
+  for (int j = 0; j < 15; ++j) st->evol[j] = st->evol[j + 1];
+  st->evol[15] = st->prev[14] - st->prev[15];
+  st->resid_diff = max_list(st->evol, 16);
+}
+
+static __device__ void pass_watchdog(GbState *st) {
+  st->passes++;
+  if (st->passes > st->pass_limit && st->active) {
+    st->active = 0;
+    st->status = GB_WATCHDOG;
+  }
+}
+
 // In eager mode (no graph) the handle is 0 and the host reads GbState instead.
 __device__ __forceinline__ void set_cond(cudaGraphConditionalHandle h, unsigned v) {
   if (h) cudaGraphSetConditional(h, v);
@@ -144,10 +191,89 @@ __device__ __forceinline__ void ctrl_phase(GbState *st, int phase, cudaGraphCond
       }
       break;
     case C_INIT_DONE:
-      if (st->alg != GB_ALG_CGIHT) {
+      if (st->alg == GB_ALG_HT_SD) {
+        st->active = ht_going(st, st->tol, (float)(0.1 * (double)st->tol));
+        set_cond(h, st->active ? 1u : 0u);
+      } else if (st->alg != GB_ALG_CGIHT) {
         st->active = keep_going(st);
         set_cond(h, st->active ? 1u : 0u);
       }
+      break;
+    case C_IHT_INIT:
+      // max_value = MaxMagnitude(A^T y); slope; x = 0 (algorithms.cu:399-405)
+      st->max_value = (float)st->red[R_XMAX];
+      st->slope = ((float)(st->num_bins - 1) / st->max_value);
+      st->max_change = 1.0f;
+      st->active = iht_going(st);
+      set_cond(h, st->active ? 1u : 0u);
+      break;
+    case C_IHT_PREP:
+      if (!live) break;
+      st->max_change = 2.0f * st->mu * (float)st->red[R_GMAX];
+      bin_decision(st);
+      break;
+    case C_IHT_STOP:
+      if (live) {
+        st->err = sqrt_red(st, R_RES);
+        push16(st->prev, st->err);
+        evolve16(st);
+        if (st->iter > 749) {
+          float rate = st->prev[15] / st->prev[0];
+          rate = powf(rate, 1.0f / 15.0f);
+          if (rate > 0.999f) st->fail = 1;
+        }
+        st->iter++;
+        st->active = iht_going(st);
+        pass_watchdog(st);
+      }
+      set_cond(h, st->active ? 1u : 0u);
+      break;
+    case C_HTSD_MU: {
+      if (!live) break;
+      // RestrictedSD_S_gen step size (functions.cu:715-744); the support stays fixed
+      float err2 = sqrt_red(st, R_AXT);
+      float mu = sqrt_red(st, R_XT);
+      if (mu < 400.0f * err2) {
+        mu = mu / err2;
+        mu = mu * mu;
+      } else {
+        mu = 0.0f;
+      }
+      st->mu = mu;
+      st->flags[F_DOBIN] = 0;
+      break;
+    }
+    case C_HTSD_STOP:
+      if (live) {
+        st->err = st->prev[15];
+        evolve16(st);
+        st->iter++;
+        st->active = ht_going(st, st->tol, (float)(0.1 * (double)st->tol));
+        pass_watchdog(st);
+      }
+      set_cond(h, st->active ? 1u : 0u);
+      break;
+    case C_HTCG_INIT:
+      // mu = <grad_prev, grad_prev>; err = ||y - A x||^2 into residNorm_prev[15]
+      // (algorithms.cu:1900-1911)
+      st->mu = (float)st->red[R_DOT1];
+      st->err = (float)st->red[R_RES];
+      st->prev[15] = st->err;
+      st->active = ht_going(st, st->tol_cg, st->tol2);
+      st->flags[F_CG] = st->active;
+      set_cond(h, st->active ? 1u : 0u);
+      break;
+    case C_HTCG_STOP:
+      if (live) {
+        push16(st->prev, (float)st->red[R_RES]);
+        st->err = st->prev[15];
+        evolve16(st);
+        st->iter++;
+        st->active = ht_going(st, st->tol_cg, st->tol2);
+        pass_watchdog(st);
+        st->flags[F_CG] = st->active;
+      }
+      set_cond(h, st->active ? 1u : 0u);
       break;
     case C_CGIHT_INIT:
       st->err = sqrt_red(st, R_RES);

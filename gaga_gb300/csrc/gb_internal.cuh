@@ -287,7 +287,7 @@ struct SolvePlan {
 };
 void enq_prologue(SolvePlan &P, cudaStream_t s0, cudaGraphConditionalHandle h_outer);
 void enq_body(SolvePlan &P, cudaStream_t s1, cudaGraphConditionalHandle h_outer);
-void enq_cg_body(SolvePlan &P, cudaStream_t s2, cudaGraphConditionalHandle h_inner);
+void enq_cg_body(SolvePlan &P, cudaStream_t s2, cudaGraphConditionalHandle h_inner, int stop_phase = -1);
 void enq_ctrl_phase(GbWork &w, cudaStream_t s, int phase, cudaGraphConditionalHandle h);
 gb_status gb_make_handle(cudaStream_t parent, cudaGraphConditionalHandle *h);
 gb_status gb_open_while(cudaStream_t parent, cudaStream_t body, cudaGraphConditionalHandle h);

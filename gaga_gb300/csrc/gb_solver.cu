@@ -460,6 +460,15 @@ void enq_prologue(SolvePlan &P, cudaStream_t s0, cudaGraphConditionalHandle h_ou
   // resid = y; err = ||y||  (algorithms.cu:1296-1300)
   k_copy_norm<<<w.red_blocks, 256, 0, s0>>>(w.st, F_ALWAYS, w.y, w.resid, m, R_RES, -1, w.red_part, w.tickets);
   enq_ctrl(w, s0, C_INIT0);
+  if (P.alg == GB_ALG_IHT) {
+    // IHT (algorithms.cu:347-405): x = 0; the bins take the scale of A^T y
+    cudaMemsetAsync(w.x, 0, sizeof(float) * w.op.n, s0);
+    enq_AT(w, s0, w.resid, w.grad, F_ALWAYS);
+    k_copy_norm<<<w.red_blocks, 256, 0, s0>>>(w.st, F_ALWAYS, w.grad, nullptr, n, -1, R_XMAX, w.red_part,
+                                              w.tickets);
+    enq_ctrl(w, s0, C_IHT_INIT, h_outer);
+    return;
+  }
   // x = A^T y ; max |x| ; FindSupportSet ; Threshold  (algorithms.cu:1335-1354)
   enq_AT(w, s0, w.y, w.x, F_ALWAYS);
   k_copy_norm<<<w.red_blocks, 256, 0, s0>>>(w.st, F_ALWAYS, w.x, nullptr, n, -1, R_XMAX, w.red_part, w.tickets);
@@ -473,7 +482,14 @@ void enq_prologue(SolvePlan &P, cudaStream_t s0, cudaGraphConditionalHandle h_ou
   k_axpy<<<w.red_blocks, 256, 0, s0>>>(w.st, F_ALWAYS, SC_ONE, w.x, w.x, 0, -1, -1, w.counters, num_bins,
                                        w.red_part, w.tickets);
   enq_support(w, s0, k, false);
-  if (P.alg == GB_ALG_CGIHT) {
+  if (P.alg == GB_ALG_HT_CG) {
+    // r = y - A x; grad = grad_previous = (A^T r) on the support (algorithms.cu:1870-1911)
+    enq_A(w, s0, w.x, w.resid, w.y, R_RES, F_ALWAYS);
+    enq_AT(w, s0, w.resid, w.grad, F_ALWAYS);
+    k_threshold<<<w.red_blocks, 256, 0, s0>>>(w.st, F_ALWAYS, w.grad, w.bins, n);
+    k_copy_norm<<<w.red_blocks, 256, 0, s0>>>(w.st, F_ALWAYS, w.grad, w.gp, n, R_DOT1, -1, w.red_part, w.tickets);
+    enq_ctrl(w, s0, C_HTCG_INIT, h_outer);
+  } else if (P.alg == GB_ALG_CGIHT) {
     // r0, grad_previous = A^T r0, grad_prev_thres (algorithms.cu:3776-3808)
     enq_A(w, s0, w.x, w.resid, w.y, R_RES, F_ALWAYS);
     enq_AT(w, s0, w.resid, w.gp, F_ALWAYS);
@@ -488,6 +504,40 @@ void enq_prologue(SolvePlan &P, cudaStream_t s0, cudaGraphConditionalHandle h_ou
 void enq_body(SolvePlan &P, cudaStream_t s1, cudaGraphConditionalHandle h_outer) {
   GbWork &w = *P.w;
   const int n = argN(w), m = argM(w), k = P.k, num_bins = w.dyn ? D_NBINS : P.num_bins;
+  if (P.alg == GB_ALG_IHT) {
+    // IHT_S_gen loop (GAGA/gaga/algorithms.cu:416-466), fixed step mu
+    enq_AT(w, s1, w.resid, w.grad, F_ALWAYS);
+    k_copy_norm<<<w.red_blocks, 256, 0, s1>>>(w.st, F_ALWAYS, w.grad, nullptr, n, -1, R_GMAX, w.red_part,
+                                              w.tickets);
+    enq_ctrl(w, s1, C_IHT_PREP);
+    enq_axpy(w, s1, F_ALWAYS, SC_MU, w.grad, w.x, n, -1, true, num_bins);
+    enq_support(w, s1, k, false);
+    enq_A(w, s1, w.x, w.resid, w.y, R_RES, F_ALWAYS);
+    enq_ctrl(w, s1, C_IHT_STOP, h_outer);
+    return;
+  }
+  if (P.alg == GB_ALG_HT_SD) {
+    // HT_SD_S_gen loop (algorithms.cu:861-890): RestrictedSD on the fixed support
+    enq_A(w, s1, w.x, w.resid, w.y, R_RES, F_ALWAYS);
+    enq_ctrl(w, s1, C_PUSH_RES);
+    if (w.op.kind == GB_OP_DENSE) {
+      enq_AT_mask(w, s1, w.resid, w.grad, w.xt, R_XT, R_GMAX, F_ALWAYS);
+    } else {
+      enq_AT(w, s1, w.resid, w.grad, F_ALWAYS);
+      enq_mask(w, s1, F_ALWAYS, w.grad, w.xt, R_XT, R_GMAX);
+    }
+    enq_A(w, s1, w.xt, w.ru, nullptr, R_AXT, F_ALWAYS);
+    enq_ctrl(w, s1, C_HTSD_MU);
+    enq_axpy(w, s1, F_ALWAYS, SC_MU, w.grad, w.x, n, -1, false, 0);
+    k_threshold<<<w.red_blocks, 256, 0, s1>>>(w.st, F_ALWAYS, w.x, w.bins, n);
+    enq_ctrl(w, s1, C_HTSD_STOP, h_outer);
+    return;
+  }
+  if (P.alg == GB_ALG_HT_CG) {
+    // HT_CG_S_gen loop (algorithms.cu:1937-1960): RestrictedCG steps on the fixed support
+    enq_cg_body(P, s1, h_outer, C_HTCG_STOP);
+    return;
+  }
   if (P.alg == GB_ALG_NIHT || P.alg == GB_ALG_HTP) {
     // RestrictedSD (GAGA/gaga/functions.cu:659-745)
     enq_A(w, s1, w.x, w.resid, w.y, R_RES, F_ALWAYS);
@@ -569,7 +619,7 @@ void enq_body(SolvePlan &P, cudaStream_t s1, cudaGraphConditionalHandle h_outer)
 }
 
 // HTP inner CG step (RestrictedCG_S_gen, GAGA/gaga/functions.cu:922-1000)
-void enq_cg_body(SolvePlan &P, cudaStream_t s2, cudaGraphConditionalHandle h_inner) {
+void enq_cg_body(SolvePlan &P, cudaStream_t s2, cudaGraphConditionalHandle h_inner, int stop_phase) {
   GbWork &w = *P.w;
   const int n = argN(w);
   enq_A(w, s2, w.grad, w.resid, nullptr, R_CG, F_CG);
@@ -582,7 +632,7 @@ void enq_cg_body(SolvePlan &P, cudaStream_t s2, cudaGraphConditionalHandle h_inn
   enq_ctrl(w, s2, C_HTP_CG2);
   k_scale_add<<<w.red_blocks, 256, 0, s2>>>(w.st, F_CG, SC_CG_BETA, w.grad, w.gp, n);
   enq_A(w, s2, w.x, w.resid, w.y, R_RES, F_CG);
-  enq_ctrl(w, s2, C_HTP_CG3, h_inner);
+  enq_ctrl(w, s2, stop_phase < 0 ? C_HTP_CG3 : stop_phase, h_inner);
 }
 
 void enq_ctrl_phase(GbWork &w, cudaStream_t s, int phase, cudaGraphConditionalHandle h) {
@@ -669,8 +719,10 @@ static GbState initial_state(const GbWork &w, int alg, const gb_options &o, int 
   st.pass_limit = o.maxiter + 4;
   st.resid_diff = 1.0f;
   for (int j = 0; j < 16; ++j) { st.prev[j] = 0.0f; st.evol[j] = 1.0f; }
-  st.alpha_bin = 0.25f;
+  // ThresholdSD / ThresholdCG start with alpha = 0 (MaxBin = num_bins, algorithms.cu:800-802)
+  st.alpha_bin = (alg == GB_ALG_HT_SD || alg == GB_ALG_HT_CG) ? 0.0f : 0.25f;
   st.max_bin = (int)((float)o.num_bins * (1.0f - st.alpha_bin));
+  if (alg == GB_ALG_IHT) st.mu = 0.65f;  // gaga_gen.cu:640 (case 2)
   st.beta_to_zero = 1;
   st.supp_change = 1;
   st.tol_cg = tol_abs * tol_abs;

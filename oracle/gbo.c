@@ -585,7 +585,9 @@ int gbo_solve(const gbo_op *op, const float *y, int k, const gbo_opts *o, float 
 
   gbo_bin_state bs;
   bs.num_bins = o->num_bins;
-  bs.alpha = 0.25f;
+  /* ThresholdSD / ThresholdCG start with alpha = 0, i.e. MaxBin = num_bins
+   * (GAGA/gaga/algorithms.cu:800-802,1838-1840) */
+  bs.alpha = (o->alg == GBO_HT_SD || o->alg == GBO_HT_CG) ? 0.0f : 0.25f;
   bs.max_bin = (int)((float)o->num_bins * (1.0f - bs.alpha));
   bs.min_val = 0.0f;
   bs.k_bin = 0;
@@ -603,17 +605,80 @@ int gbo_solve(const gbo_op *op, const float *y, int k, const gbo_opts *o, float 
   s.fail = 0;
   s.cycle = 1;
 
+  float max_value, slope;
+  if (o->alg == GBO_IHT) {
+    /* IHT_S_gen (GAGA/gaga/algorithms.cu:347-478): x starts at 0; the bins keep the scale
+     * of A^T y for the whole solve; fixed step mu = 0.65 (gaga_gen.cu, case 2) */
+    const float mu_iht = 0.65f;
+    memset(x, 0, sizeof(float) * n);
+    gbo_AT(op, w.resid, w.grad);
+    max_value = gbo_max_magnitude(w.grad, n);
+    slope = ((float)(o->num_bins - 1) / max_value);
+    while ((s.err > s.tol) & (iter < o->maxiter) & (s.err < (100.0f * s.err_start)) &
+           ((double)s.resid_diff > 0.01 * (double)s.tol) & (s.fail == 0)) {
+      gbo_AT(op, w.resid, w.grad);
+      float max_change = 2.0f * mu_iht * gbo_max_magnitude(w.grad, n);
+      saxpy(n, mu_iht, w.grad, x);
+      gbo_find_support_set(x, w.bins, w.counters, slope, max_value, max_change, &bs, n, k);
+      gbo_threshold(x, w.bins, bs.k_bin, n);
+      residual(&w, x, w.resid, w.ru);
+      s.err = nrm2f(w.resid, m);
+      push16(w.prev, s.err);
+      for (int j = 0; j < 15; ++j) s.evol[j] = s.evol[j + 1];
+      s.evol[15] = w.prev[14] - w.prev[15];
+      s.resid_diff = max_list(s.evol, 16);
+      if (iter > 749) {
+        float rate = powf(w.prev[15] / w.prev[0], 1.0f / 15.0f);
+        if (rate > 0.999f) s.fail = 1;
+      }
+      iter++;
+    }
+    goto done;
+  }
+
   /* Set the linear bins: x = H_k(A^T y) */
   gbo_AT(op, y, x);
-  float max_value = gbo_max_magnitude(x, n);
-  float slope = ((float)(o->num_bins - 1) / max_value);
+  max_value = gbo_max_magnitude(x, n);
+  slope = ((float)(o->num_bins - 1) / max_value);
   /* HTP (and NIHT_dct) pass max_value as maxChange to force binning; with
    * minVal = 0 every algorithm bins here. */
   gbo_find_support_set(x, w.bins, w.counters, slope, max_value,
                        o->alg == GBO_HTP ? max_value : 1.0f, &bs, n, k);
   gbo_threshold(x, w.bins, bs.k_bin, n);
 
-  if (o->alg == GBO_NIHT) {
+  if (o->alg == GBO_HT_SD) {
+    /* HT_SD_S_gen (GAGA/gaga/algorithms.cu:785-906): steepest descent on the fixed support */
+    const float tol2 = (float)(0.1 * (double)s.tol);
+    while ((s.err > s.tol) & (iter < o->maxiter) & (s.resid_diff > tol2)) {
+      restricted_sd(&w, bs.k_bin);
+      gbo_threshold(x, w.bins, bs.k_bin, n);
+      s.err = w.prev[15];
+      for (int j = 0; j < 15; ++j) s.evol[j] = s.evol[j + 1];
+      s.evol[15] = w.prev[14] - w.prev[15];
+      s.resid_diff = max_list(s.evol, 16);
+      iter++;
+    }
+  } else if (o->alg == GBO_HT_CG) {
+    /* HT_CG_S_gen (GAGA/gaga/algorithms.cu:1826-1990): CG on the fixed support, the
+     * residual history in squared norms */
+    const float tol_cg = s.tol * s.tol;
+    const float tol2 = 10.0f * tol_cg;
+    residual(&w, x, w.resid, w.ru);
+    gbo_AT(op, w.resid, w.grad);
+    gbo_threshold(w.grad, w.bins, bs.k_bin, n);
+    memcpy(w.gp, w.grad, sizeof(float) * n);
+    mu = dotf(w.gp, w.gp, n);
+    s.err = dotf(w.resid, w.resid, m);
+    w.prev[15] = s.err;
+    while ((s.err > tol_cg) & (iter < o->maxiter) & (s.resid_diff > tol2)) {
+      restricted_cg(&w, w.prev, &mu, bs.k_bin);
+      s.err = w.prev[15];
+      for (int j = 0; j < 15; ++j) s.evol[j] = s.evol[j + 1];
+      s.evol[15] = w.prev[14] - w.prev[15];
+      s.resid_diff = max_list(s.evol, 16);
+      iter++;
+    }
+  } else if (o->alg == GBO_NIHT) {
     /* NIHT_S_gen (GAGA/gaga/algorithms.cu:1274-1441) */
     while (keep_going(&s, iter, o->maxiter)) {
       float max_change = restricted_sd(&w, bs.k_bin);
@@ -706,6 +771,7 @@ int gbo_solve(const gbo_op *op, const float *y, int k, const gbo_opts *o, float 
     }
   }
 
+done:
   if (info) {
     info->iter = iter;
     info->sum = bs.sum;

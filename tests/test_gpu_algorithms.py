@@ -1,0 +1,84 @@
+"""IHT, ThresholdSD and ThresholdCG on the GPU against the CPU oracle, on the dense, DCT
+and expander operators.
+
+The oracle restates IHT_S_*, HT_SD_S_* and HT_CG_S_* (GAGA/gaga/algorithms.cu:347-478,
+785-906, 1826-1990).  Each case compares the success verdict (relative l2 <= 1e-3 to the
+planted signal), the solution against the oracle's, and the iteration count.  ThresholdSD /
+ThresholdCG fix the support after one hard threshold of A^T y, so a case with a larger k
+(a wrong support) checks that both sides reach the same least-squares fit on it.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ALGS = ["IHT", "ThresholdSD", "ThresholdCG"]
+
+
+def _dense(gbo, k, seed):
+    n, m = 4096, 1024
+    A = gbo.gen_dense(m, n, seed)
+    x0, ks = gbo.gen_vector(n, k, 1, seed)
+    op = gbo.Op.dense(A, m, n)
+    return op, x0, ks, ("gen", (A.reshape(n, m).T.copy(),))
+
+
+def _dct(gbo, k, seed):
+    n = 2 ** 14
+    m = n // 4
+    rows = gbo.gen_dct_rows(n, m, seed=seed)
+    x0, ks = gbo.gen_vector(n, k, 2, seed=seed)
+    return gbo.Op.dct(n, rows), x0, ks, ("dct", (rows,))
+
+
+def _smv(gbo, k, seed):
+    n, m, d = 2 ** 14, 2 ** 12, 7
+    rows, vals = gbo.gen_smv(m, n, d, 1, seed=seed)
+    x0, ks = gbo.gen_vector(n, k, 1, seed=seed)
+    return gbo.Op.smv(m, n, d, rows, vals), x0, ks, ("smv", (rows, vals, d))
+
+
+def _solve_gpu(gb, alg, op, y, ks, tol, spec):
+    kind, extra = spec
+    opts = gb.gaga_options("tol", tol)
+    if kind == "gen":
+        x, it, conv = gb.gaga_cs(alg, "gen", y, extra[0], ks, opts)
+    elif kind == "dct":
+        x, it, conv = gb.gaga_cs(alg, "dct", y, extra[0], ks, op.m, op.n, opts, index_base=0)
+    else:
+        rows, vals, d = extra
+        cols = np.repeat(np.arange(op.n, dtype=np.int32), d)
+        x, it, conv, rec, trec = gb.gaga_cs(alg, "smv", y, rows, cols, vals, ks, opts, index_base=0)
+    return np.asarray(x), it
+
+
+CASES = [("dense", _dense, 20), ("dense", _dense, 102), ("dct", _dct, 100), ("dct", _dct, 400),
+         ("smv", _smv, 60), ("smv", _smv, 200)]
+
+
+@pytest.mark.parametrize("alg", ALGS)
+@pytest.mark.parametrize("name,make,k", CASES)
+def test_algorithm_matches_oracle(gb, gbo, alg, name, make, k):
+    op, x0, ks, spec = make(gbo, k, seed=40 + k)
+    y = gbo.A(op, x0)
+    tol = 1e-5 * float(np.linalg.norm(y))
+    x, it = _solve_gpu(gb, alg, op, y, ks, tol, spec)
+    xo, info = gbo.solve(alg, op, y, ks, tol)
+    ok_gpu = np.linalg.norm(x - x0) / np.linalg.norm(x0) <= 1e-3
+    ok_ora = np.linalg.norm(xo - x0) / np.linalg.norm(x0) <= 1e-3
+    assert ok_gpu == ok_ora, (alg, name, k, it, info.iter)
+    if ok_ora:
+        assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-4
+        assert abs(it - info.iter) <= 3, (it, info.iter)
+    elif alg != "IHT":
+        # same one-shot support, same least-squares fit on it
+        assert np.array_equal(x != 0, xo != 0)
+        assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-3
+
+
+@pytest.mark.parametrize("alg", ALGS)
+def test_generate_and_solve_new_algorithms(gb, alg):
+    """The generate-and-solve usage accepts the algorithm strings (gaga_gen.cu:621-631)."""
+    opts = gb.gaga_options("tol", 1e-5, "tol_is_relative", 1, "seed", 3)
+    norms, times, iters, supp, conv, x = gb.gaga_cs(alg, "gen", 20, 1024, 4096, opts)
+    assert norms[1] < 1e-3 and iters > 0

@@ -95,3 +95,16 @@ def test_ref_library_matches_fixtures_when_present(gbo):
     R.ref_linear_binning(v.ctypes.data, bins.ctypes.data, cnt.ctypes.data, nb, mb, len(v),
                          C.c_float(float(z[f"{name}__slope"])), C.c_float(float(z[f"{name}__intercept"])))
     assert np.array_equal(bins, z[f"{name}__bins"])
+
+
+@pytest.mark.parametrize("alg", ["IHT", "ThresholdSD", "ThresholdCG"])
+def test_oracle_remaining_algorithms_recover_easy_problem(gbo, alg):
+    """IHT, ThresholdSD and ThresholdCG restated from the reference recover a problem well
+    inside their recovery region (one-step thresholding needs a small rho)."""
+    n, m, k = 4096, 1024, 20
+    A = gbo.gen_dense(m, n, 12)
+    x0, ks = gbo.gen_vector(n, k, 1, 12)
+    op = gbo.Op.dense(A, m, n)
+    y = gbo.A(op, x0)
+    x, info = gbo.solve(alg, op, y, ks, 1e-5 * float(np.linalg.norm(y)))
+    assert np.linalg.norm(x - x0) / np.linalg.norm(x0) < 1e-3, (alg, info.iter)
