@@ -25,7 +25,7 @@ __all__ = ["gaga_cs", "gaga_options", "GagaError", "solve_batch", "version"]
 _OPTION_NAMES = {"tol", "maxiter", "vecDistribution", "matrixEnsemble", "seed", "numBins", "threadsPerBlockn",
                  "threadsPerBlockm", "threadsPerBlocknp", "threadsPerBlockBin", "convRateNum", "kFixed", "noise",
                  "gpuNumber", "timing", "alpha", "supportFlag", "restartFlag", "projFracTol", "l0_thresh",
-                 "band_percentage", "debug_mode", "tol_is_relative", "learnedWarmStart"}
+                 "band_percentage", "debug_mode", "tol_is_relative", "learnedWarmStart", "resultsDir"}
 
 
 def version():
@@ -88,6 +88,10 @@ def _options(alg, n, opts, ens):
             o.support_flag = int(v)
         elif name == "timing":
             o.timing = 1 if v in ("on", 1, True) else 0
+        elif name == "resultsDir":
+            # extension: append the reference's result line to the dated file in this directory
+            o._results_dir = None if v is None else str(v).encode()
+            o.results_dir = o._results_dir
         elif name == "learnedWarmStart":
             # extension: a CUDA tensor of gb_cs_mlp_num_params() FP32 MLP parameters (CGIHT)
             o.learned_params = None if v is None else v.data_ptr()

@@ -23,7 +23,7 @@ EXPORTS = ["gb_cs_version", "gb_cs_last_error", "gb_cs_default_options", "gb_cs_
            "gb_cs_operator_apply", "gb_cs_l0_step", "gb_cs_solve_batch", "gb_cs_batch_last_stats",
            "gb_cs_dense_apply_noalloc", "gb_cs_solve_shared_batch", "gb_cs_shared_last_stats",
            "gb_cs_gemm_bf16_tn", "gb_cs_mlp_num_params", "gb_cs_mlp_features", "gb_cs_mlp_forward",
-           "gb_cs_mlp_grad", "gb_cs_mlp_train"]
+           "gb_cs_mlp_grad", "gb_cs_mlp_train", "gb_cs_write_result"]
 
 
 class Options(C.Structure):
@@ -31,7 +31,8 @@ class Options(C.Structure):
                 ("restart_flag", C.c_int), ("l0_thresh", C.c_int), ("vec_distribution", C.c_int),
                 ("matrix_ensemble", C.c_int), ("k_fixed", C.c_int), ("seed", C.c_uint), ("noise", C.c_float),
                 ("gpu_number", C.c_int), ("conv_rate_num", C.c_int), ("alpha", C.c_float),
-                ("support_flag", C.c_int), ("timing", C.c_int), ("learned_params", C.c_void_p)]
+                ("support_flag", C.c_int), ("timing", C.c_int), ("learned_params", C.c_void_p),
+                ("results_dir", C.c_char_p)]
 
 
 class Problem(C.Structure):
@@ -118,6 +119,9 @@ def load():
     L.gb_cs_mlp_grad.restype = i
     L.gb_cs_mlp_train.argtypes = [vp, vp, vp, i, i, i, f, C.c_uint, vp, vp]
     L.gb_cs_mlp_train.restype = i
+    L.gb_cs_write_result.argtypes = [C.c_char_p, C.c_char_p, i, i, i, i, i, C.POINTER(Options), C.POINTER(Result),
+                                     C.c_char_p, i]
+    L.gb_cs_write_result.restype = i
     _lib = L
     return L
 

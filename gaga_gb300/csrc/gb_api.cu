@@ -8,6 +8,7 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 #include <algorithm>
 #include <string>
@@ -589,6 +590,9 @@ extern "C" gb_status gb_cs_generate_and_solve(const char *alg, int kind, int k, 
   cudaEventDestroy(t1);
   cudaEventDestroy(t2);
   if (x_true_out) memcpy(x_true_out, xt.data(), sizeof(float) * n);
+  gb_result local_r;
+  memset(&local_r, 0, sizeof(local_r));
+  if (!r && o.results_dir) r = &local_r;
   if (r) {
     float *user_rec = r->res_record;
     memset(r, 0, sizeof(*r));
@@ -633,6 +637,69 @@ extern "C" gb_status gb_cs_generate_and_solve(const char *alg, int kind, int k, 
     r->times[2] = ms_tot;
   }
   if (st.status == GB_WATCHDOG) return bad("device iteration bound reached", GB_WATCHDOG);
+  if (o.results_dir) {
+    gb_options ow = o;
+    ow.seed = seed;  // the seed of the drawn problem (kFixed may have advanced it)
+    GB_TRY(gb_cs_write_result(o.results_dir, alg, kind, k, m, n, d, &ow, r, nullptr, 0));
+  }
+  return GB_OK;
+}
+
+// ------------------------------------------------------------------ results file
+extern "C" gb_status gb_cs_write_result(const char *dir, const char *alg, int kind, int k, int m, int n, int d,
+                                        const gb_options *o, const gb_result *r, char *path_out, int path_len) {
+  if (!alg || !o || !r || kind < GB_OP_DENSE || kind > GB_OP_SMV) return bad("bad arguments to gb_cs_write_result");
+  time_t raw;
+  time(&raw);
+  struct tm tmv;
+  localtime_r(&raw, &tmv);
+  const char *tag = kind == GB_OP_DENSE ? "gen" : kind == GB_OP_DCT ? "dct" : "smv";
+  char fname[160];
+  if (o->noise > 0.0f)
+    snprintf(fname, sizeof(fname), "gpu_data_%s%d%02d%02d_noise%0.3f.txt", tag, tmv.tm_year + 1900, tmv.tm_mon + 1,
+             tmv.tm_mday, o->noise);
+  else
+    snprintf(fname, sizeof(fname), "gpu_data_%s%d%02d%02d.txt", tag, tmv.tm_year + 1900, tmv.tm_mon + 1,
+             tmv.tm_mday);
+  std::string path = (dir && *dir) ? std::string(dir) + "/" + fname : std::string(fname);
+  FILE *f = fopen(path.c_str(), "a+");
+  if (!f) return bad("results file did not open");
+  const float *e = r->norms, *t = r->times;
+  const int *s = r->support;
+  if (kind == GB_OP_DENSE) {
+    // File_output_gen (GAGA/gaga/functions.cu:64-74)
+    const int ens = o->matrix_ensemble == 2 ? 2 : 1;
+    fprintf(f, "%s_S_gen output: ", alg);
+    fprintf(f, "k %d, m %d, n %d, vecDistribution %d matrixEnsemble %d ", k, m, n, o->vec_distribution, ens);
+  } else if (kind == GB_OP_DCT) {
+    // File_output (functions.cu:34-44)
+    fprintf(f, "%s_S_dct output: ", alg);
+    fprintf(f, "k %d, m %d, n %d, vecDistribution %d ", k, m, n, o->vec_distribution);
+  } else {
+    // File_output_smv (functions.cu:47-61)
+    const int ens = o->matrix_ensemble ? o->matrix_ensemble : 3;
+    fprintf(f, "%s_S_smv output: ", alg);
+    fprintf(f, "k %d, m %d, n %d, vecDistribution %d nonzeros_per_column %d matrixEnsemble %d ", k, m, n,
+            o->vec_distribution, d, ens);
+  }
+  fprintf(f, "errorl1 %0.7e errorl2 %0.7e errorlinf %0.7e ", e[0], e[1], e[2]);
+  fprintf(f, "timeALG %0.7e timeIter %0.7e timeTotal %0.7e ", t[0], t[1], t[2]);
+  fprintf(f, "iterations %d ", r->iter);
+  fprintf(f, "converge_rate %0.7e ", r->conv_rate);
+  fprintf(f, "TruePos %d FalsePos %d TrueNeg %d FalseNeg %d ", s[0], s[1], s[2], s[3]);
+  if (kind == GB_OP_SMV) {
+    fprintf(f, "seed %u ", o->seed);
+    fprintf(f, "band_percentage %1.2f ", 0.0f);
+    fprintf(f, "noise_level %2.4f ", o->noise);
+    fprintf(f, "\n");
+  } else {
+    fprintf(f, "seed %u \n", o->seed);
+  }
+  fclose(f);
+  if (path_out && path_len > 0) {
+    strncpy(path_out, path.c_str(), (size_t)path_len - 1);
+    path_out[path_len - 1] = 0;
+  }
   return GB_OK;
 }
 

@@ -69,6 +69,9 @@ typedef struct {
   int timing;           /* 'timing'         0 (accepted; timing variants are not built) */
   const float *learned_params; /* extension: CGIHT only, device pointer to the warm-start
                            MLP's gb_cs_mlp_num_params() FP32 parameters; NULL = plain start */
+  const char *results_dir;  /* extension: generate-and-solve appends the reference's result
+                           line to the dated file in this directory ("" = current directory,
+                           as the reference always does); NULL = no file */
 } gb_options;
 
 /* A recovery problem in "given data" form. */
@@ -133,6 +136,15 @@ gb_status gb_cs_solve(const char *alg, const gb_problem *p, const gb_options *o,
 gb_status gb_cs_generate_and_solve(const char *alg, int kind, int k, int m, int n, int d,
                                    const gb_options *o, float *x_out, float *x_true_out,
                                    gb_result *r);
+
+/* Append the result line of one generate-and-solve run to the reference's dated results file
+ * in `dir` (NULL or "" = current directory): gpu_data_{gen,dct,smv}YYYYMMDD.txt, with
+ * _noise%0.3f before .txt when o->noise > 0 (GAGA/gaga/results.cu:173,343,516,686,863,1032),
+ * the line as File_output / File_output_smv / File_output_gen write it
+ * (GAGA/gaga/functions.cu:34-80).  d is the expander's nonzeros per column (smv only).
+ * The file's path is copied to path_out (path_len bytes) when not NULL. */
+gb_status gb_cs_write_result(const char *dir, const char *alg, int kind, int k, int m, int n, int d,
+                             const gb_options *o, const gb_result *r, char *path_out, int path_len);
 
 /* ---- component entry points (device pointers; replace the reference's L1/L2 routines) ---- */
 

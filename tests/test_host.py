@@ -123,3 +123,43 @@ def test_generators_are_deterministic(gbo):
     r, v = gbo.gen_smv(128, 500, 7, 3, seed=1)
     cols = r.reshape(500, 7)
     assert all(len(set(c.tolist())) == 7 for c in cols)
+
+
+def test_result_file_lines_match_reference_format(gb, tmp_path):
+    """gb_cs_write_result appends File_output_gen / File_output / File_output_smv lines
+    (GAGA/gaga/functions.cu:34-80) to the dated gpu_data_* files."""
+    L = gb._lib.load()
+    o = gb._lib.Options()
+    L.gb_cs_default_options(C.byref(o), b"NIHT", 4096)
+    o.seed = 17
+    r = gb._lib.Result()
+    r.norms[0], r.norms[1], r.norms[2] = 1.5e-5, 2.25e-5, 3.0e-5
+    r.times[0], r.times[1], r.times[2] = 12.5, 0.5, 40.0
+    r.iter, r.conv_rate = 25, 0.75
+    for j, v in enumerate((102, 0, 3994, 0)):
+        r.support[j] = v
+    buf = C.create_string_buffer(512)
+    assert L.gb_cs_write_result(str(tmp_path).encode(), b"NIHT", 0, 102, 1024, 4096, 0, C.byref(o), C.byref(r), buf,
+                                512) == 0
+    path = buf.value.decode()
+    assert re.search(r"gpu_data_gen\d{8}\.txt$", path)
+    tail = ("errorl1 %0.7e errorl2 %0.7e errorlinf %0.7e timeALG %0.7e timeIter %0.7e timeTotal %0.7e "
+            "iterations %d converge_rate %0.7e TruePos %d FalsePos %d TrueNeg %d FalseNeg %d " % (
+                np.float32(1.5e-5), np.float32(2.25e-5), np.float32(3.0e-5), 12.5, 0.5, 40.0, 25, 0.75, 102, 0,
+                3994, 0))
+    want = "NIHT_S_gen output: k 102, m 1024, n 4096, vecDistribution 1 matrixEnsemble 1 " + tail + "seed 17 \n"
+    assert open(path).read() == want
+    # DCT and expander lines, and the noise file name
+    o.noise = 0.01
+    assert L.gb_cs_write_result(str(tmp_path).encode(), b"CGIHT", 2, 10, 100, 400, 7, C.byref(o), C.byref(r), buf,
+                                512) == 0
+    path = buf.value.decode()
+    assert path.endswith("_noise0.010.txt") and "gpu_data_smv" in path
+    line = open(path).read()
+    assert line.startswith("CGIHT_S_smv output: k 10, m 100, n 400, vecDistribution 1 nonzeros_per_column 7 "
+                           "matrixEnsemble 3 errorl1")
+    assert line.endswith("seed 17 band_percentage 0.00 noise_level 0.0100 \n")
+    o.noise = 0.0
+    assert L.gb_cs_write_result(str(tmp_path).encode(), b"HTP", 1, 10, 100, 512, 0, C.byref(o), C.byref(r), buf,
+                                512) == 0
+    assert open(buf.value.decode()).read().startswith("HTP_S_dct output: k 10, m 100, n 512, vecDistribution 1 error")
