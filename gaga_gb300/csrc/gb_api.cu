@@ -42,6 +42,7 @@ extern "C" int gb_cs_alg_id(const char *alg) {
   if (!strcmp(alg, "IHT")) return GB_ALG_IHT;
   if (!strcmp(alg, "ThresholdSD")) return GB_ALG_HT_SD;
   if (!strcmp(alg, "ThresholdCG")) return GB_ALG_HT_CG;
+  if (!strcmp(alg, "CSMPSP")) return GB_ALG_CSMPSP;
   if (!strcmp(alg, "CGIHT")) return GB_ALG_CGIHT;
   if (!strcmp(alg, "parallel_l0")) return GB_ALG_PARALLEL_L0;
   return -1;
@@ -293,7 +294,7 @@ extern "C" gb_status gb_cs_solve(const char *alg, const gb_problem *p, const gb_
                                  gb_result *r) {
   if (!p || !x_out) return bad("null argument");
   const int alg_id = gb_cs_alg_id(alg);
-  if (alg_id < 0) return bad("algorithm must be one of NIHT, HTP, IHT, ThresholdSD, ThresholdCG, CGIHT, parallel_l0");
+  if (alg_id < 0) return bad("algorithm must be one of NIHT, HTP, IHT, ThresholdSD, ThresholdCG, CSMPSP, CGIHT, parallel_l0");
   if (alg_id == GB_ALG_PARALLEL_L0 && p->kind != GB_OP_SMV) return bad("parallel_l0 requires the smv operator");
   gb_options o;
   if (opts) o = *opts;
@@ -449,7 +450,7 @@ extern "C" gb_status gb_cs_generate_and_solve(const char *alg, int kind, int k, 
                                               gb_result *r) {
   if (!x_out) return bad("null argument");
   const int alg_id = gb_cs_alg_id(alg);
-  if (alg_id < 0) return bad("algorithm must be one of NIHT, HTP, IHT, ThresholdSD, ThresholdCG, CGIHT, parallel_l0");
+  if (alg_id < 0) return bad("algorithm must be one of NIHT, HTP, IHT, ThresholdSD, ThresholdCG, CSMPSP, CGIHT, parallel_l0");
   if (alg_id == GB_ALG_PARALLEL_L0 && kind != GB_OP_SMV) return bad("parallel_l0 requires the smv operator");
   if (k < 1 || m < 1 || n < 1 || (kind == GB_OP_SMV && d < 1)) return bad("k, m, n (and d) must be positive");
   gb_options o;

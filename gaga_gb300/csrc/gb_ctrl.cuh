@@ -54,7 +54,13 @@ enum {
   C_HTSD_MU,      // ThresholdSD: RestrictedSD step size, support kept
   C_HTSD_STOP,    // ThresholdSD: stopping rules
   C_HTCG_INIT,    // ThresholdCG: CG start on the thresholded support
-  C_HTCG_STOP     // ThresholdCG: squared-residual history and stopping rules
+  C_HTCG_STOP,    // ThresholdCG: squared-residual history and stopping rules
+  C_CSMPSP_INIT_DONE,  // CSMPSP: after the first CG projection (counts as an iteration)
+  C_CSMPSP_GBIN,  // CSMPSP: bins of the gradient (forced binning, k-th bin to k_bin_prev)
+  C_CSMPSP_JOIN,  // CSMPSP: back to the support of x before joining
+  C_CSMPSP_CG3,   // CSMPSP: CG projection step bookkeeping (stall test disabled)
+  C_CSMPSP_XBIN,  // CSMPSP: forced binning of x after the projection
+  C_CSMPSP_STOP   // CSMPSP: residual history and stopping rules (fail after 125)
 };
 
 static __device__ float max_list(const float *a, int n) {
@@ -180,7 +186,7 @@ __device__ __forceinline__ void ctrl_phase(GbState *st, int phase, cudaGraphCond
       // max_value as maxChange to force the first binning (algorithms.cu:1335-1354,2575)
       st->max_value = (float)st->red[R_XMAX];
       st->slope = ((float)(st->num_bins - 1) / st->max_value);
-      st->max_change = (st->alg == GB_ALG_HTP) ? st->max_value : 1.0f;
+      st->max_change = (st->alg == GB_ALG_HTP || st->alg == GB_ALG_CSMPSP) ? st->max_value : 1.0f;
       bin_decision(st);
       break;
     case C_BINPREP:
@@ -250,6 +256,56 @@ __device__ __forceinline__ void ctrl_phase(GbState *st, int phase, cudaGraphCond
         st->iter++;
         st->active = ht_going(st, st->tol, (float)(0.1 * (double)st->tol));
         pass_watchdog(st);
+      }
+      set_cond(h, st->active ? 1u : 0u);
+      break;
+    case C_CSMPSP_INIT_DONE:
+      // err = sqrt(errCG); residNorm_prev[15] = err; iter++ (algorithms.cu:3491-3495)
+      st->err = sqrtf(st->err_cg);
+      st->prev[15] = st->err;
+      st->iter = 1;
+      st->active = keep_going(st);
+      set_cond(h, st->active ? 1u : 0u);
+      break;
+    case C_CSMPSP_GBIN:
+      if (!live) break;
+      // max_value = MaxMagnitude(grad); minVal = 0; FindSupportSet(grad, ..., max_value)
+      // into d_bin_grad / k_bin_grad (algorithms.cu:3519-3526)
+      st->max_value = (float)st->red[R_XMAX];
+      st->min_val = 0.0f;
+      st->slope = ((float)(st->num_bins - 1) / st->max_value);
+      st->flags[F_DOBIN] = 1;
+      st->flags[F_KBIN_ALT] = 1;
+      break;
+    case C_CSMPSP_JOIN:
+      st->flags[F_KBIN_ALT] = 0;
+      break;
+    case C_CSMPSP_CG3:
+      if (st->flags[F_CG] && live) {
+        push16(st->prev_cg, (float)st->red[R_RES]);
+        st->err_cg = st->prev_cg[15];
+        st->it_cg++;
+        for (int j = 0; j < 15; ++j) st->evol_cg[j] = st->evol_cg[j + 1];
+        st->evol_cg[15] = st->prev_cg[14] - st->prev_cg[15];
+        st->diff_cg = 10.0f;  // the reference disables the stall test here (algorithms.cu:3577)
+        st->flags[F_CG] = (st->err_cg > st->tol_cg) & (st->it_cg < 15) & (st->diff_cg > st->tol2);
+      } else {
+        st->flags[F_CG] = 0;
+      }
+      set_cond(h, (st->flags[F_CG] && live) ? 1u : 0u);
+      break;
+    case C_CSMPSP_XBIN:
+      if (!live) break;
+      st->max_value = (float)st->red[R_XMAX];
+      st->min_val = 0.0f;
+      st->slope = ((float)(st->num_bins - 1) / st->max_value);
+      st->flags[F_DOBIN] = 1;
+      break;
+    case C_CSMPSP_STOP:
+      if (live) {
+        st->err = sqrt_red(st, R_RES);
+        push16(st->prev, st->err);
+        finish_iteration(st, 125);
       }
       set_cond(h, st->active ? 1u : 0u);
       break;

@@ -27,7 +27,8 @@ enum {
   F_UCG = 2,     // CGIHT: unrestricted CG step this iteration
   F_RCG = 3,     // CGIHT: restricted CG step this iteration
   F_CG = 4,      // HTP: inner CG loop running
-  F_REMASK = 5   // CGIHT: support changed, re-restrict the search direction
+  F_REMASK = 5,  // CGIHT: support changed, re-restrict the search direction
+  F_KBIN_ALT = 6 // CSMPSP: the k-th bin scan is for the gradient (k_bin_prev), not x
 };
 
 // reduction slots
@@ -53,7 +54,7 @@ struct GbState {
   float err, err_start, resid_diff;
   float prev[16], evol[16];
   // support selection (GAGA/gaga/functions.cu:397-436)
-  int max_bin, k_bin, sum, k_bin_prev;
+  int max_bin, k_bin, sum, k_bin_prev;  // k_bin_prev: CGIHT's previous k_bin, CSMPSP's gradient k_bin
   float alpha_bin, min_val, slope, max_value, max_change;
   int s_cnt;
   // CG scalars

@@ -253,9 +253,20 @@ __global__ void __launch_bounds__(1024) k_kbin(GbState *st, int pf, const int *_
       st->max_bin = (int)((float)st->num_bins * (1.0f - st->alpha_bin));
     }
     st->min_val = intercept - (float)(k_bin + 1) / slope;
-    st->k_bin = k_bin;
+    if (st->flags[F_KBIN_ALT]) st->k_bin_prev = k_bin;
+    else st->k_bin = k_bin;
     st->sum = sum;
   }
+}
+
+// joinSupports (GAGA/gaga/kernels.cu:162-172): entries in the gradient's top bins join the
+// support of x (their bin becomes k_bin)
+__global__ void k_join(const GbState *st, int *__restrict__ bins, const int *__restrict__ bins_grad, int n) {
+  if (!gb_pred(st, F_ALWAYS)) return;
+  n = dimv(st, n);
+  const int kb = st->k_bin, kbg = st->k_bin_prev;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    if (bins_grad[i] <= kbg && bins[i] > kb) bins[i] = kb;
 }
 
 // threshold v (always) and, when binning, count the tile's support entries and detect
@@ -445,6 +456,48 @@ static void enq_support(GbWork &w, cudaStream_t s, int k, bool save_prev) {
   k_compact<<<tiles, 256, 0, s>>>(w.st, F_DOBIN, w.bins, n, w.tile_cnt, w.S);
 }
 
+// CG start on the current support (HTP's projection, ThresholdCG, CSMPSP): r = y - A x,
+// grad = grad_previous = (A^T r) restricted to the support; ||r||^2 and ||grad||^2
+static void enq_cg_start(GbWork &w, cudaStream_t s) {
+  const int n = argN(w);
+  enq_A(w, s, w.x, w.resid, w.y, R_RES, F_ALWAYS);
+  enq_AT(w, s, w.resid, w.grad, F_ALWAYS);
+  k_threshold<<<w.red_blocks, 256, 0, s>>>(w.st, F_ALWAYS, w.grad, w.bins, n);
+  k_copy_norm<<<w.red_blocks, 256, 0, s>>>(w.st, F_ALWAYS, w.grad, w.gp, n, R_DOT1, -1, w.red_part, w.tickets);
+}
+
+// CSMPSP loop, first part (GAGA/gaga/algorithms.cu:3513-3541): top-k of the gradient joins
+// the support of x; then the CG start on the joined support
+static void enq_csmpsp_join(SolvePlan &P, cudaStream_t s) {
+  GbWork &w = *P.w;
+  const int n = argN(w);
+  enq_AT(w, s, w.resid, w.grad, F_ALWAYS);
+  k_copy_norm<<<w.red_blocks, 256, 0, s>>>(w.st, F_ALWAYS, w.grad, nullptr, n, -1, R_XMAX, w.red_part, w.tickets);
+  enq_ctrl(w, s, C_CSMPSP_GBIN);
+  cudaMemsetAsync(w.counters, 0, sizeof(int) * P.num_bins, s);
+  k_hist<<<w.red_blocks, 256, 0, s>>>(w.st, F_DOBIN, w.grad, w.bins_prev, nullptr, w.counters, n);
+  k_kbin<<<1, 1024, 0, s>>>(w.st, F_DOBIN, w.counters, P.k);
+  enq_ctrl(w, s, C_CSMPSP_JOIN);
+  k_join<<<w.red_blocks, 256, 0, s>>>(w.st, w.bins, w.bins_prev, n);
+  const int tiles = (w.op.n + GB_TILE - 1) / GB_TILE;
+  k_thresh_count<<<tiles, 256, 0, s>>>(w.st, F_ALWAYS, w.x, w.bins, nullptr, n, w.tile_cnt);
+  k_compact<<<tiles, 256, 0, s>>>(w.st, F_DOBIN, w.bins, n, w.tile_cnt, w.S);
+  enq_cg_start(w, s);
+}
+
+// CSMPSP loop, last part (algorithms.cu:3580-3620): forced binning of x to its k largest,
+// the residual and the stopping rules
+static void enq_csmpsp_rebin(SolvePlan &P, cudaStream_t s, cudaGraphConditionalHandle h_outer) {
+  GbWork &w = *P.w;
+  const int n = argN(w);
+  k_copy_norm<<<w.red_blocks, 256, 0, s>>>(w.st, F_ALWAYS, w.x, nullptr, n, -1, R_XMAX, w.red_part, w.tickets);
+  enq_ctrl(w, s, C_CSMPSP_XBIN);
+  cudaMemsetAsync(w.counters, 0, sizeof(int) * P.num_bins, s);
+  enq_support(w, s, P.k, false);
+  enq_A(w, s, w.x, w.resid, w.y, R_RES, F_ALWAYS);
+  enq_ctrl(w, s, C_CSMPSP_STOP, h_outer);
+}
+
 // The solve as pieces: prologue, loop body (with the HTP inner CG loop), run either as one
 // graph with WHILE nodes or eagerly (GB_CS_EAGER=1: same kernels, host-checked loops;
 // used for profiling, since kernels inside conditional graphs cannot be profiled).
@@ -484,11 +537,11 @@ void enq_prologue(SolvePlan &P, cudaStream_t s0, cudaGraphConditionalHandle h_ou
   enq_support(w, s0, k, false);
   if (P.alg == GB_ALG_HT_CG) {
     // r = y - A x; grad = grad_previous = (A^T r) on the support (algorithms.cu:1870-1911)
-    enq_A(w, s0, w.x, w.resid, w.y, R_RES, F_ALWAYS);
-    enq_AT(w, s0, w.resid, w.grad, F_ALWAYS);
-    k_threshold<<<w.red_blocks, 256, 0, s0>>>(w.st, F_ALWAYS, w.grad, w.bins, n);
-    k_copy_norm<<<w.red_blocks, 256, 0, s0>>>(w.st, F_ALWAYS, w.grad, w.gp, n, R_DOT1, -1, w.red_part, w.tickets);
+    enq_cg_start(w, s0);
     enq_ctrl(w, s0, C_HTCG_INIT, h_outer);
+  } else if (P.alg == GB_ALG_CSMPSP) {
+    // the first CG projection on the support of x follows (algorithms.cu:3462-3476)
+    enq_cg_start(w, s0);
   } else if (P.alg == GB_ALG_CGIHT) {
     // r0, grad_previous = A^T r0, grad_prev_thres (algorithms.cu:3776-3808)
     enq_A(w, s0, w.x, w.resid, w.y, R_RES, F_ALWAYS);
@@ -650,6 +703,27 @@ static gb_status build_graph(SolvePlan &P, cudaStream_t s0, cudaStream_t s1, cud
   cudaGraphConditionalHandle h_outer = 0, h_inner = 0;
   GB_TRY(make_handle(s0, &h_outer));
   enq_prologue(P, s0, h_outer);
+  if (P.alg == GB_ALG_CSMPSP) {
+    // first projection, then WHILE(outer) { join; WHILE(CG) { step }; rebin; stop }
+    cudaGraphConditionalHandle h_first = 0;
+    GB_TRY(make_handle(s0, &h_first));
+    enq_ctrl(w, s0, C_HTP_CGINIT, h_first);
+    GB_TRY(open_while(s0, s2, h_first));
+    enq_cg_body(P, s2, h_first, C_HTP_CG3);
+    GB_TRY(close_while(s2));
+    enq_ctrl(w, s0, C_CSMPSP_INIT_DONE, h_outer);
+    GB_TRY(open_while(s0, s1, h_outer));
+    enq_csmpsp_join(P, s1);
+    GB_TRY(make_handle(s1, &h_inner));
+    enq_ctrl(w, s1, C_HTP_CGINIT, h_inner);
+    GB_TRY(open_while(s1, s2, h_inner));
+    enq_cg_body(P, s2, h_inner, C_CSMPSP_CG3);
+    GB_TRY(close_while(s2));
+    enq_csmpsp_rebin(P, s1, h_outer);
+    GB_TRY(close_while(s1));
+    GB_CUDA_TRY(cudaStreamEndCapture(s0, graph));
+    return GB_OK;
+  }
   GB_TRY(open_while(s0, s1, h_outer));
   enq_body(P, s1, h_outer);
   if (P.alg == GB_ALG_HTP) {
@@ -672,9 +746,36 @@ static gb_status read_int(const int *d, int *h, cudaStream_t s) {
 }
 
 // Eager execution: the same kernels, the loop conditions read back by the host.
+static gb_status run_cg_eager(SolvePlan &P, cudaStream_t s, int stop_phase) {
+  GbWork &w = *P.w;
+  enq_ctrl(w, s, C_HTP_CGINIT, 0);
+  int cg = 0, g2 = 0;
+  GB_TRY(read_int(&w.st->flags[F_CG], &cg, s));
+  while (cg && g2++ < 16) {
+    enq_cg_body(P, s, 0, stop_phase);
+    GB_TRY(read_int(&w.st->flags[F_CG], &cg, s));
+  }
+  return GB_OK;
+}
+
 static gb_status run_eager(SolvePlan &P, cudaStream_t s) {
   GbWork &w = *P.w;
   enq_prologue(P, s, 0);
+  if (P.alg == GB_ALG_CSMPSP) {
+    GB_TRY(run_cg_eager(P, s, C_HTP_CG3));
+    enq_ctrl(w, s, C_CSMPSP_INIT_DONE, 0);
+    GbState probe;
+    GB_CUDA_TRY(cudaMemcpy(&probe, w.st, sizeof(probe), cudaMemcpyDeviceToHost));
+    int active = probe.active, guard = 0;
+    while (active && guard++ <= probe.pass_limit) {
+      enq_csmpsp_join(P, s);
+      GB_TRY(run_cg_eager(P, s, C_CSMPSP_CG3));
+      enq_csmpsp_rebin(P, s, 0);
+      GB_TRY(read_int(&w.st->active, &active, s));
+    }
+    GB_CUDA_TRY(cudaGetLastError());
+    return GB_OK;
+  }
   int active = 0, guard = 0;
   GB_TRY(read_int(&w.st->active, &active, s));
   const int limit = P.w->op.n + 1;  // replaced below by the state's pass limit

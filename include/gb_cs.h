@@ -44,9 +44,9 @@ enum { GB_OP_DENSE = 0, GB_OP_DCT = 1, GB_OP_SMV = 2 };
 enum { GB_HOST = 0, GB_DEVICE = 1 };
 
 /* Reference algorithm numbers (GAGA/gaga/gaga_gen.cu:619-631, gaga_smv.cu:841-857):
- * "NIHT", "HTP", "IHT", "ThresholdSD", "ThresholdCG", "CGIHT", "parallel_l0". */
-enum { GB_ALG_NIHT = 0, GB_ALG_HTP = 1, GB_ALG_IHT = 2, GB_ALG_HT_SD = 3, GB_ALG_HT_CG = 4, GB_ALG_CGIHT = 6,
-       GB_ALG_PARALLEL_L0 = 14 };
+ * "NIHT", "HTP", "IHT", "ThresholdSD", "ThresholdCG", "CSMPSP", "CGIHT", "parallel_l0". */
+enum { GB_ALG_NIHT = 0, GB_ALG_HTP = 1, GB_ALG_IHT = 2, GB_ALG_HT_SD = 3, GB_ALG_HT_CG = 4, GB_ALG_CSMPSP = 5,
+       GB_ALG_CGIHT = 6, GB_ALG_PARALLEL_L0 = 14 };
 
 /* Options: the gagaOptions name/value list (GAGA/gaga/gagaOptions.m:8-58) as a struct. */
 typedef struct {

@@ -643,10 +643,69 @@ int gbo_solve(const gbo_op *op, const float *y, int k, const gbo_opts *o, float 
   /* HTP (and NIHT_dct) pass max_value as maxChange to force binning; with
    * minVal = 0 every algorithm bins here. */
   gbo_find_support_set(x, w.bins, w.counters, slope, max_value,
-                       o->alg == GBO_HTP ? max_value : 1.0f, &bs, n, k);
+                       (o->alg == GBO_HTP || o->alg == GBO_CSMPSP) ? max_value : 1.0f, &bs, n, k);
   gbo_threshold(x, w.bins, bs.k_bin, n);
 
-  if (o->alg == GBO_HT_SD) {
+  if (o->alg == GBO_CSMPSP) {
+    /* CSMPSP_S_gen (GAGA/gaga/algorithms.cu:3372-3688) */
+    const float tol_cg = s.tol * s.tol;
+    const float tol2 = 10.0f * tol_cg;
+    float prevcg[16], evolcg[16], errcg, diffcg;
+    int itcg;
+    /* one CG projection on the support of x (stall test on the CG history when `stall`) */
+#define CSMPSP_PROJECT(stall)                                                  \
+    do {                                                                       \
+      itcg = 0;                                                                \
+      for (int j = 0; j < 16; ++j) { prevcg[j] = 0.0f; evolcg[j] = 1.0f; }    \
+      diffcg = 1.0f;                                                           \
+      prevcg[15] = w.prev[15];                                                 \
+      residual(&w, x, w.resid, w.ru);                                          \
+      gbo_AT(op, w.resid, w.grad);                                             \
+      gbo_threshold(w.grad, w.bins, bs.k_bin, n);                              \
+      memcpy(w.gp, w.grad, sizeof(float) * n);                                 \
+      mu = dotf(w.gp, w.gp, n);                                                \
+      errcg = dotf(w.resid, w.resid, m);                                       \
+      prevcg[15] = errcg;                                                      \
+      while ((errcg > tol_cg) & (itcg < 15) & (diffcg > tol2)) {               \
+        restricted_cg(&w, prevcg, &mu, bs.k_bin);                              \
+        errcg = prevcg[15];                                                    \
+        itcg++;                                                                \
+        for (int j = 0; j < 15; ++j) evolcg[j] = evolcg[j + 1];                \
+        evolcg[15] = prevcg[14] - prevcg[15];                                  \
+        diffcg = (stall) ? max_list(evolcg, 16) : 10.0f;                       \
+      }                                                                        \
+    } while (0)
+    CSMPSP_PROJECT(1);
+    s.err = sqrtf(errcg);
+    w.prev[15] = s.err;
+    iter++;  /* the initial projection counts as an iteration */
+    int *bins_grad = w.bins_prev;
+    while (keep_going(&s, iter, o->maxiter)) {
+      gbo_AT(op, w.resid, w.grad);
+      max_value = gbo_max_magnitude(w.grad, n);
+      bs.min_val = 0.0f;
+      slope = ((float)(o->num_bins - 1) / max_value);
+      int k_bin_x = bs.k_bin;
+      gbo_find_support_set(w.grad, bins_grad, w.counters, slope, max_value, max_value, &bs, n, k);
+      int k_bin_grad = bs.k_bin;
+      bs.k_bin = k_bin_x;
+      /* joinSupports (GAGA/gaga/kernels.cu:162-172) */
+      for (int i = 0; i < n; ++i)
+        if (bins_grad[i] <= k_bin_grad && w.bins[i] > bs.k_bin) w.bins[i] = bs.k_bin;
+      CSMPSP_PROJECT(0);
+      max_value = gbo_max_magnitude(x, n);
+      bs.min_val = 0.0f;
+      slope = ((float)(o->num_bins - 1) / max_value);
+      gbo_find_support_set(x, w.bins, w.counters, slope, max_value, max_value, &bs, n, k);
+      gbo_threshold(x, w.bins, bs.k_bin, n);
+      residual(&w, x, w.resid, w.ru);
+      s.err = nrm2f(w.resid, m);
+      push16(w.prev, s.err);
+      stop_update(&s, w.prev, iter, 125);
+      iter++;
+    }
+#undef CSMPSP_PROJECT
+  } else if (o->alg == GBO_HT_SD) {
     /* HT_SD_S_gen (GAGA/gaga/algorithms.cu:785-906): steepest descent on the fixed support */
     const float tol2 = (float)(0.1 * (double)s.tol);
     while ((s.err > s.tol) & (iter < o->maxiter) & (s.resid_diff > tol2)) {

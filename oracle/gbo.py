@@ -6,9 +6,10 @@ import numpy as np
 
 from . import build as _build
 
-NIHT, HTP, IHT, HT_SD, HT_CG, CGIHT, PARALLEL_L0, SERIAL_L0 = 0, 1, 2, 3, 4, 6, 14, 15
+NIHT, HTP, IHT, HT_SD, HT_CG, CSMPSP, CGIHT, PARALLEL_L0, SERIAL_L0 = 0, 1, 2, 3, 4, 5, 6, 14, 15
 OP_DENSE, OP_DCT, OP_SMV = 0, 1, 2
-ALG_IDS = {"NIHT": NIHT, "HTP": HTP, "IHT": IHT, "ThresholdSD": HT_SD, "ThresholdCG": HT_CG, "CGIHT": CGIHT,
+ALG_IDS = {"NIHT": NIHT, "HTP": HTP, "IHT": IHT, "ThresholdSD": HT_SD, "ThresholdCG": HT_CG, "CSMPSP": CSMPSP,
+           "CGIHT": CGIHT,
            "parallel_l0": PARALLEL_L0, "serial_l0": SERIAL_L0}
 
 _lib = None
