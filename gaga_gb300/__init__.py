@@ -88,6 +88,8 @@ def _options(alg, n, opts, ens):
             o.support_flag = int(v)
         elif name == "timing":
             o.timing = 1 if v in ("on", 1, True) else 0
+        elif name == "projFracTol":
+            o.proj_frac_tol = float(v)
         elif name == "resultsDir":
             # extension: append the reference's result line to the dated file in this directory
             o._results_dir = None if v is None else str(v).encode()
@@ -95,7 +97,7 @@ def _options(alg, n, opts, ens):
         elif name == "learnedWarmStart":
             # extension: a CUDA tensor of gb_cs_mlp_num_params() FP32 MLP parameters (CGIHT)
             o.learned_params = None if v is None else v.data_ptr()
-        # threadsPerBlock*, projFracTol, band_percentage, debug_mode: accepted, no effect
+        # threadsPerBlock*, band_percentage, debug_mode: accepted, no effect
     return o
 
 

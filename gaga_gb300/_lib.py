@@ -15,7 +15,8 @@ STATUS_NAMES = {0: "GB_OK", 1: "GB_BAD_ARG", 2: "GB_OOM", 3: "GB_WATCHDOG", 4: "
                 5: "GB_UNSUPPORTED", 6: "GB_NO_DEVICE"}
 GB_OP_DENSE, GB_OP_DCT, GB_OP_SMV = 0, 1, 2
 GB_HOST, GB_DEVICE = 0, 1
-GB_ALG_NIHT, GB_ALG_HTP, GB_ALG_IHT, GB_ALG_HT_SD, GB_ALG_HT_CG, GB_ALG_CGIHT, GB_ALG_PARALLEL_L0 = 0, 1, 2, 3, 4, 6, 14
+GB_ALG_NIHT, GB_ALG_HTP, GB_ALG_IHT, GB_ALG_HT_SD, GB_ALG_HT_CG, GB_ALG_CSMPSP, GB_ALG_CGIHT = 0, 1, 2, 3, 4, 5, 6
+GB_ALG_FIHT, GB_ALG_ALPS, GB_ALG_CGIHT_PROJ, GB_ALG_PARALLEL_L0 = 7, 8, 9, 14
 
 # every symbol include/gb_cs.h declares
 EXPORTS = ["gb_cs_version", "gb_cs_last_error", "gb_cs_default_options", "gb_cs_alg_id", "gb_cs_solve",
@@ -32,7 +33,7 @@ class Options(C.Structure):
                 ("matrix_ensemble", C.c_int), ("k_fixed", C.c_int), ("seed", C.c_uint), ("noise", C.c_float),
                 ("gpu_number", C.c_int), ("conv_rate_num", C.c_int), ("alpha", C.c_float),
                 ("support_flag", C.c_int), ("timing", C.c_int), ("learned_params", C.c_void_p),
-                ("results_dir", C.c_char_p)]
+                ("results_dir", C.c_char_p), ("proj_frac_tol", C.c_float)]
 
 
 class Problem(C.Structure):

@@ -43,6 +43,9 @@ extern "C" int gb_cs_alg_id(const char *alg) {
   if (!strcmp(alg, "ThresholdSD")) return GB_ALG_HT_SD;
   if (!strcmp(alg, "ThresholdCG")) return GB_ALG_HT_CG;
   if (!strcmp(alg, "CSMPSP")) return GB_ALG_CSMPSP;
+  if (!strcmp(alg, "FIHT")) return GB_ALG_FIHT;
+  if (!strcmp(alg, "ALPS")) return GB_ALG_ALPS;
+  if (!strcmp(alg, "CGIHTprojected")) return GB_ALG_CGIHT_PROJ;
   if (!strcmp(alg, "CGIHT")) return GB_ALG_CGIHT;
   if (!strcmp(alg, "parallel_l0")) return GB_ALG_PARALLEL_L0;
   return -1;
@@ -66,6 +69,7 @@ extern "C" void gb_cs_default_options(gb_options *o, const char *alg, int n) {
   o->alpha = 0.25f;
   o->support_flag = 0;
   o->timing = 0;
+  o->proj_frac_tol = 3.0f;
 }
 
 // ------------------------------------------------------------------ workspace
@@ -135,6 +139,8 @@ gb_status alloc_work(DeviceBuffers &db, GbWork &w, int m, int n, int lda, int nu
   GB_TRY(db.alloc(&w.y, lda));
   GB_TRY(db.alloc(&w.resid, lda));
   GB_TRY(db.alloc(&w.ru, lda));
+  GB_TRY(db.alloc(&w.am1, lda));
+  GB_TRY(db.alloc(&w.am2, lda));
   GB_TRY(db.alloc(&w.bins, n));
   GB_TRY(db.alloc(&w.bins_prev, n));
   GB_TRY(db.alloc(&w.counters, std::max(num_bins, 1)));
@@ -294,7 +300,8 @@ extern "C" gb_status gb_cs_solve(const char *alg, const gb_problem *p, const gb_
                                  gb_result *r) {
   if (!p || !x_out) return bad("null argument");
   const int alg_id = gb_cs_alg_id(alg);
-  if (alg_id < 0) return bad("algorithm must be one of NIHT, HTP, IHT, ThresholdSD, ThresholdCG, CSMPSP, CGIHT, parallel_l0");
+  if (alg_id < 0) return bad("algorithm must be one of NIHT, HTP, IHT, ThresholdSD, ThresholdCG, CSMPSP, CGIHT, FIHT, ALPS, "
+                         "CGIHTprojected, parallel_l0");
   if (alg_id == GB_ALG_PARALLEL_L0 && p->kind != GB_OP_SMV) return bad("parallel_l0 requires the smv operator");
   gb_options o;
   if (opts) o = *opts;
@@ -450,7 +457,8 @@ extern "C" gb_status gb_cs_generate_and_solve(const char *alg, int kind, int k, 
                                               gb_result *r) {
   if (!x_out) return bad("null argument");
   const int alg_id = gb_cs_alg_id(alg);
-  if (alg_id < 0) return bad("algorithm must be one of NIHT, HTP, IHT, ThresholdSD, ThresholdCG, CSMPSP, CGIHT, parallel_l0");
+  if (alg_id < 0) return bad("algorithm must be one of NIHT, HTP, IHT, ThresholdSD, ThresholdCG, CSMPSP, CGIHT, FIHT, ALPS, "
+                         "CGIHTprojected, parallel_l0");
   if (alg_id == GB_ALG_PARALLEL_L0 && kind != GB_OP_SMV) return bad("parallel_l0 requires the smv operator");
   if (k < 1 || m < 1 || n < 1 || (kind == GB_OP_SMV && d < 1)) return bad("k, m, n (and d) must be positive");
   gb_options o;

@@ -60,7 +60,20 @@ enum {
   C_CSMPSP_JOIN,  // CSMPSP: back to the support of x before joining
   C_CSMPSP_CG3,   // CSMPSP: CG projection step bookkeeping (stall test disabled)
   C_CSMPSP_XBIN,  // CSMPSP: forced binning of x after the projection
-  C_CSMPSP_STOP   // CSMPSP: residual history and stopping rules (fail after 125)
+  C_CSMPSP_STOP,  // CSMPSP: residual history and stopping rules (fail after 125)
+  C_FH_INIT1,     // FIHT/ALPS/CGIHTprojected: residNorm_prev[15] = ||y - A x||
+  C_FH_BIN,       // FIHT/ALPS: forced binning of x (minVal = 0, maxChange = 1)
+  C_FH_INIT2,     // FIHT/ALPS: after the extra first iteration; first loop test
+  C_FH_TAU,       // FIHT/ALPS: extrapolation weight tau
+  C_FH_MU,        // FIHT/ALPS: step mu = <v,v>/<Av,Av> (1 when guarded out)
+  C_ALPS_LBIN,    // ALPS: local binning of the gradient outside supp(v), outer state kept
+  C_ALPS_LRESTORE,// ALPS: outer bin state back
+  C_FH_STOP,      // FIHT/ALPS/CGIHTprojected: residual history, stopping rules
+  C_CP_INIT2,     // CGIHTprojected: first loop test
+  C_CP_MU,        // CGIHTprojected: step mu for the active branch
+  C_CP_BIN,       // CGIHTprojected: forced binning in the steepest-descent branch
+  C_CP_BETA,      // CGIHTprojected: CG direction weight
+  C_CP_PROJ       // CGIHTprojected: projection fraction -> next branch
 };
 
 static __device__ float max_list(const float *a, int n) {
@@ -186,7 +199,8 @@ __device__ __forceinline__ void ctrl_phase(GbState *st, int phase, cudaGraphCond
       // max_value as maxChange to force the first binning (algorithms.cu:1335-1354,2575)
       st->max_value = (float)st->red[R_XMAX];
       st->slope = ((float)(st->num_bins - 1) / st->max_value);
-      st->max_change = (st->alg == GB_ALG_HTP || st->alg == GB_ALG_CSMPSP) ? st->max_value : 1.0f;
+      st->max_change =
+          (st->alg == GB_ALG_HTP || st->alg == GB_ALG_CSMPSP || st->alg == GB_ALG_CGIHT_PROJ) ? st->max_value : 1.0f;
       bin_decision(st);
       break;
     case C_BINPREP:
@@ -306,6 +320,123 @@ __device__ __forceinline__ void ctrl_phase(GbState *st, int phase, cudaGraphCond
         st->err = sqrt_red(st, R_RES);
         push16(st->prev, st->err);
         finish_iteration(st, 125);
+      }
+      set_cond(h, st->active ? 1u : 0u);
+      break;
+    case C_FH_INIT1:
+      st->err = sqrt_red(st, R_RES);
+      st->prev[15] = st->err;
+      break;
+    case C_FH_BIN:
+      if (!live) break;
+      st->min_val = 0.0f;
+      st->max_change = 1.0f;
+      st->max_value = (float)st->red[R_XMAX];
+      st->slope = ((float)(st->num_bins - 1) / st->max_value);
+      st->flags[F_DOBIN] = 1;
+      break;
+    case C_FH_INIT2:
+      st->err = sqrt_red(st, R_RES);
+      push16(st->prev, st->err);
+      evolve16(st);
+      st->active = keep_going(st);
+      set_cond(h, st->active ? 1u : 0u);
+      break;
+    case C_FH_TAU: {
+      if (!live) break;
+      // RestrictedFIHT/ALPS (GAGA/gaga/functions.cu:1680-1686)
+      float tau = (float)st->red[R_DOT1], tmp = (float)st->red[R_DOT2];
+      if (fabsf(tau) < 400.0f * fabsf(tmp)) tau = tau / tmp;
+      else tau = 0.0f;
+      st->cg_beta = tau;
+      break;
+    }
+    case C_FH_MU: {
+      if (!live) break;
+      float mu = (float)st->red[R_XT], tmp = (float)st->red[R_AXT];
+      if (mu < 400.0f * tmp) mu = mu / tmp;
+      else mu = 1.0f;
+      st->mu = mu;
+      break;
+    }
+    case C_ALPS_LBIN:
+      if (!live) break;
+      // FindSupportSet on v with the bin state passed by value (functions.cu:1803-1807)
+      st->sv_alpha = st->alpha_bin;
+      st->sv_max_bin = st->max_bin;
+      st->sv_min_val = st->min_val;
+      st->sv_k_bin = st->k_bin;
+      st->min_val = 0.0f;
+      st->max_value = (float)st->red[R_XMAX];
+      st->slope = ((float)(st->num_bins - 1) / st->max_value);
+      st->flags[F_DOBIN] = 1;
+      break;
+    case C_ALPS_LRESTORE:
+      if (!live) break;
+      st->alpha_bin = st->sv_alpha;
+      st->max_bin = st->sv_max_bin;
+      st->min_val = st->sv_min_val;
+      st->k_bin = st->sv_k_bin;
+      break;
+    case C_FH_STOP:
+      if (live) {
+        st->err = sqrt_red(st, R_RES);
+        push16(st->prev, st->err);
+        finish_iteration(st, 749);
+      }
+      set_cond(h, st->active ? 1u : 0u);
+      break;
+    case C_CP_INIT2:
+      for (int j = 0; j < 15; ++j) st->evol[j] = st->evol[j + 1];
+      st->evol[15] = st->prev[14] - st->prev[15];
+      st->flags[F_UCG] = 1;  // steepest-descent branch first
+      st->flags[F_RCG] = 0;
+      st->active = keep_going(st);
+      set_cond(h, st->active ? 1u : 0u);
+      break;
+    case C_CP_MU: {
+      if (!live) break;
+      // mu = <v,v> / <Ap,Ap> (SD: Ap = A v), 1 when guarded out (algorithms.cu:4578-4582)
+      float mu = (float)st->red[R_DOT1], tmp = (float)st->red[R_DOT2];
+      if (mu < 400.0f * tmp) mu = mu / tmp;
+      else mu = 1.0f;
+      st->mu = mu;
+      break;
+    }
+    case C_CP_BIN:
+      if (!live) break;
+      st->flags[F_DOBIN] = st->flags[F_UCG];
+      if (st->flags[F_UCG]) {
+        st->min_val = 0.0f;
+        st->max_change = 1.0f;
+        st->max_value = (float)st->red[R_XMAX];
+        st->slope = ((float)(st->num_bins - 1) / st->max_value);
+      }
+      break;
+    case C_CP_BETA: {
+      if (!live || !st->flags[F_RCG]) break;
+      float beta = (float)st->red[R_DOT3], tmp = (float)st->red[R_DOT4];
+      if (beta < 400.0f * tmp) beta = beta / tmp;
+      else beta = 0.0f;
+      st->cg_beta = beta;
+      break;
+    }
+    case C_CP_PROJ:
+      if (live) {
+        // proj_frac = ||grad - p|| / ||v|| decides the next branch (algorithms.cu:4637-4648)
+        float pf = (float)sqrt(st->red[R_DOT1]), tmp = (float)sqrt(st->red[R_XT]);
+        int supp;
+        if (pf < 1000.0f * tmp) {
+          pf = pf / tmp;
+          supp = pf > st->proj_frac_tol ? 1 : 0;
+        } else {
+          supp = 1;
+        }
+        st->flags[F_UCG] = supp;
+        st->flags[F_RCG] = !supp;
+        st->err = sqrt_red(st, R_RES);
+        push16(st->prev, st->err);
+        finish_iteration(st, 749);
       }
       set_cond(h, st->active ? 1u : 0u);
       break;

@@ -77,6 +77,9 @@ struct GbState {
   // learned warm start (CGIHT): on, gave up after 10 iterations, residual at the warm x0
   int learned, fell_back;
   float err_warm0;
+  // CGIHTprojected projFracTol; ALPS: the outer bin state kept across its local binning
+  float proj_frac_tol, sv_alpha, sv_min_val;
+  int sv_max_bin, sv_k_bin;
 };
 
 // Operator description on the device.
@@ -104,6 +107,7 @@ struct GbWork {
   unsigned int *tickets;  // [GB_NSLOT]
   float *x, *xt, *grad, *gp, *gpt;
   float *y, *resid, *ru;
+  float *am1, *am2;  // FIHT / ALPS / CGIHTprojected: A x_prev, A v (or A p)
   int *bins, *bins_prev, *counters;
   int *S;        // support list (n)
   int *tile_cnt; // per-tile counts for ordered compaction

@@ -112,13 +112,14 @@ __global__ void k_threshold(const GbState *st, int pf, float *__restrict__ v, co
 }
 
 // scalar selector for the fused updates
-enum { SC_MU = 0, SC_CG_ALPHA = 1, SC_NEG_CG_ALPHA = 2, SC_CG_BETA = 3, SC_ONE = 4 };
+enum { SC_MU = 0, SC_CG_ALPHA = 1, SC_NEG_CG_ALPHA = 2, SC_CG_BETA = 3, SC_ONE = 4, SC_NEG_ONE = 5 };
 __device__ __forceinline__ float pick(const GbState *st, int which) {
   switch (which) {
     case SC_MU: return st->mu;
     case SC_CG_ALPHA: return st->cg_alpha;
     case SC_NEG_CG_ALPHA: return -st->cg_alpha;
     case SC_CG_BETA: return st->cg_beta;
+    case SC_NEG_ONE: return -1.0f;
     default: return 1.0f;
   }
 }
@@ -141,6 +142,38 @@ __global__ void k_axpy(GbState *st, int pf, int which, const float *__restrict__
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ncount; i += gridDim.x * blockDim.x) counters[i] = 0;
   if (slot_max >= 0) grid_reduce_publish<1>(mx, slot_max, st, rp, tk);
   if (slot_sq >= 0) grid_reduce_publish<0>(s2, slot_sq, st, rp, tk);
+}
+
+// out = a + c b (cublasSaxpy form: one fused multiply-add), or out = a without b; the
+// optional reductions give sum(out * dv) and sum(out^2).  out may alias a or b.
+__global__ void k_lin(GbState *st, int pf, float *out, const float *a, int which, const float *b, int n,
+                      const float *dv, int slot_dot, int slot_sq, float *rp, unsigned int *tk) {
+  if (!gb_pred(st, pf)) return;
+  n = dimv(st, n);
+  const float c = pick(st, which);
+  float d = 0.0f, q = 0.0f;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float o = b ? fmaf(c, b[i], a[i]) : a[i];
+    out[i] = o;
+    if (dv) d = fmaf(o, dv[i], d);
+    q = fmaf(o, o, q);
+  }
+  if (slot_dot >= 0) grid_reduce_publish<0>(d, slot_dot, st, rp, tk);
+  if (slot_sq >= 0) grid_reduce_publish<0>(q, slot_sq, st, rp, tk);
+}
+
+// The reference's flag thresholds (GAGA/gaga/kernels.cu:32-61): mode 0 out = flag != 0 ? in : 0
+// (a copy then threshold_two), mode 1 out = flag == 0 ? in : 0 (zero then threshold_three),
+// mode 2 out = flag != 0 ? in : out (threshold_four)
+__global__ void k_flagmask(const GbState *st, int pf, float *out, const float *in, const float *flag, int mode, int n) {
+  if (!gb_pred(st, pf)) return;
+  n = dimv(st, n);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const bool f = flag[i] != 0.0f;
+    if (mode == 0) out[i] = f ? in[i] : 0.0f;
+    else if (mode == 1) out[i] = f ? 0.0f : in[i];
+    else if (f) out[i] = in[i];
+  }
 }
 
 // a = beta * a + b (cublasSscal then cublasSaxpy with 1)
@@ -498,6 +531,111 @@ static void enq_csmpsp_rebin(SolvePlan &P, cudaStream_t s, cudaGraphConditionalH
   enq_ctrl(w, s, C_CSMPSP_STOP, h_outer);
 }
 
+static void lin(GbWork &w, cudaStream_t s, int pf, float *out, const float *a, int which, const float *b, int n,
+                const float *dv = nullptr, int slot_dot = -1, int slot_sq = -1) {
+  k_lin<<<w.red_blocks, 256, 0, s>>>(w.st, pf, out, a, which, b, n, dv, slot_dot, slot_sq, w.red_part, w.tickets);
+}
+
+// forced binning of x (minVal = 0, maxChange = 1) and Threshold, as FIHT / ALPS do after
+// every change of x (GAGA/gaga/algorithms.cu:5475-5481)
+static void enq_fh_bin(SolvePlan &P, cudaStream_t s) {
+  GbWork &w = *P.w;
+  const int n = argN(w);
+  k_copy_norm<<<w.red_blocks, 256, 0, s>>>(w.st, F_ALWAYS, w.x, nullptr, n, -1, R_XMAX, w.red_part, w.tickets);
+  enq_ctrl(w, s, C_FH_BIN);
+  cudaMemsetAsync(w.counters, 0, sizeof(int) * P.num_bins, s);
+  enq_support(w, s, P.k, false);
+}
+
+// grad = A^T r and v = grad on the support with ||v||^2 in red[slot]
+static void enq_grad_masked(GbWork &w, cudaStream_t s, int pf, const float *r, float *v, int slot) {
+  if (w.op.kind == GB_OP_DENSE) {
+    enq_AT_mask(w, s, r, w.grad, v, slot, -1, pf);
+  } else {
+    enq_AT(w, s, r, w.grad, pf);
+    enq_mask(w, s, pf, w.grad, v, slot, -1);
+  }
+}
+
+// FIHT / ALPS loop (GAGA/gaga/algorithms.cu:5523-5560, 6356-6393; functions.cu:1668-1843)
+static void enq_fiht_body(SolvePlan &P, cudaStream_t s, cudaGraphConditionalHandle h_outer) {
+  GbWork &w = *P.w;
+  const int n = argN(w), m = argM(w);
+  float *xp = w.gp, *ex = w.gpt, *vt = w.xt, *Apv = w.am1, *Aex = w.am2;
+  // extrapolated point v = x + tau (x_prev - x), A v, the residual at v and the gradient
+  lin(w, s, F_ALWAYS, Apv, Apv, SC_NEG_ONE, w.ru, m, w.resid, R_DOT1, R_DOT2);
+  enq_ctrl(w, s, C_FH_TAU);
+  lin(w, s, F_ALWAYS, xp, xp, SC_NEG_ONE, w.x, n);
+  lin(w, s, F_ALWAYS, ex, w.x, SC_CG_BETA, xp, n);
+  lin(w, s, F_ALWAYS, Aex, w.ru, SC_CG_BETA, Apv, m);
+  lin(w, s, F_ALWAYS, w.resid, w.y, SC_NEG_ONE, Aex, m);
+  enq_AT(w, s, w.resid, w.grad, F_ALWAYS);
+  lin(w, s, F_ALWAYS, xp, w.x, SC_ONE, nullptr, n);
+  lin(w, s, F_ALWAYS, Apv, w.ru, SC_ONE, nullptr, m);
+  if (P.alg == GB_ALG_FIHT) {
+    k_flagmask<<<w.red_blocks, 256, 0, s>>>(w.st, F_ALWAYS, vt, w.grad, ex, 0, n);
+  } else {
+    // ALPS: the k largest of the gradient outside supp(v), then the gradient on supp(v)
+    k_flagmask<<<w.red_blocks, 256, 0, s>>>(w.st, F_ALWAYS, vt, w.grad, ex, 1, n);
+    k_copy_norm<<<w.red_blocks, 256, 0, s>>>(w.st, F_ALWAYS, vt, nullptr, n, -1, R_XMAX, w.red_part, w.tickets);
+    enq_ctrl(w, s, C_ALPS_LBIN);
+    cudaMemsetAsync(w.counters, 0, sizeof(int) * P.num_bins, s);
+    k_hist<<<w.red_blocks, 256, 0, s>>>(w.st, F_DOBIN, vt, w.bins, nullptr, w.counters, n);
+    k_kbin<<<1, 1024, 0, s>>>(w.st, F_DOBIN, w.counters, P.k);
+    k_threshold<<<w.red_blocks, 256, 0, s>>>(w.st, F_ALWAYS, vt, w.bins, n);
+    enq_ctrl(w, s, C_ALPS_LRESTORE);
+    k_flagmask<<<w.red_blocks, 256, 0, s>>>(w.st, F_ALWAYS, vt, w.grad, ex, 2, n);
+  }
+  if (w.op.kind == GB_OP_DENSE) enq_support_of_nonzeros(w, s, vt, n);
+  enq_A(w, s, vt, Aex, nullptr, R_AXT, F_ALWAYS);
+  k_copy_norm<<<w.red_blocks, 256, 0, s>>>(w.st, F_ALWAYS, vt, nullptr, n, R_XT, -1, w.red_part, w.tickets);
+  enq_ctrl(w, s, C_FH_MU);
+  lin(w, s, F_ALWAYS, w.x, ex, SC_MU, w.grad, n);
+  enq_fh_bin(P, s);
+  enq_A(w, s, w.x, w.ru, nullptr, -1, F_ALWAYS);
+  lin(w, s, F_ALWAYS, w.resid, w.y, SC_NEG_ONE, w.ru, m);
+  // steepest descent restricted to the support
+  enq_grad_masked(w, s, F_ALWAYS, w.resid, vt, R_XT);
+  enq_A(w, s, vt, Aex, nullptr, R_AXT, F_ALWAYS);
+  enq_ctrl(w, s, C_FH_MU);
+  lin(w, s, F_ALWAYS, w.x, w.x, SC_MU, vt, n);
+  lin(w, s, F_ALWAYS, w.ru, w.ru, SC_MU, Aex, m);
+  lin(w, s, F_ALWAYS, w.resid, w.y, SC_NEG_ONE, w.ru, m, nullptr, -1, R_RES);
+  enq_ctrl(w, s, C_FH_STOP, h_outer);
+}
+
+// CGIHTprojected loop (GAGA/gaga/algorithms.cu:4572-4660): steepest descent with a new
+// support (F_UCG) or a CG step on the previous one (F_RCG), chosen by the projection fraction
+static void enq_cgproj_body(SolvePlan &P, cudaStream_t s, cudaGraphConditionalHandle h_outer) {
+  GbWork &w = *P.w;
+  const int n = argN(w), m = argM(w);
+  float *vt = w.xt, *p = w.gp, *gpt = w.gpt, *Ap = w.am2, *diff = w.upd;
+  k_dot2<<<w.red_blocks, 256, 0, s>>>(w.st, F_UCG, vt, vt, R_DOT1, n, w.ru, w.ru, R_DOT2, m, w.red_part, w.tickets);
+  k_dot2<<<w.red_blocks, 256, 0, s>>>(w.st, F_RCG, vt, vt, R_DOT1, n, Ap, Ap, R_DOT2, m, w.red_part, w.tickets);
+  enq_ctrl(w, s, C_CP_MU);
+  lin(w, s, F_UCG, w.x, w.x, SC_MU, w.grad, n);
+  lin(w, s, F_RCG, w.x, w.x, SC_MU, p, n);
+  k_copy_norm<<<w.red_blocks, 256, 0, s>>>(w.st, F_UCG, w.x, nullptr, n, -1, R_XMAX, w.red_part, w.tickets);
+  enq_ctrl(w, s, C_CP_BIN);
+  cudaMemsetAsync(w.counters, 0, sizeof(int) * P.num_bins, s);
+  enq_support(w, s, P.k, false);
+  enq_A(w, s, w.x, w.ru, nullptr, -1, F_ALWAYS);
+  lin(w, s, F_ALWAYS, w.resid, w.y, SC_NEG_ONE, w.ru, m);
+  lin(w, s, F_RCG, gpt, vt, SC_ONE, nullptr, n);
+  enq_grad_masked(w, s, F_ALWAYS, w.resid, vt, -1);
+  enq_A(w, s, vt, w.ru, nullptr, -1, F_ALWAYS);
+  lin(w, s, F_UCG, p, vt, SC_ONE, nullptr, n);
+  lin(w, s, F_UCG, Ap, w.ru, SC_ONE, nullptr, m);
+  k_dot2<<<w.red_blocks, 256, 0, s>>>(w.st, F_RCG, vt, vt, R_DOT3, n, gpt, gpt, R_DOT4, n, w.red_part, w.tickets);
+  enq_ctrl(w, s, C_CP_BETA);
+  k_scale_add<<<w.red_blocks, 256, 0, s>>>(w.st, F_RCG, SC_CG_BETA, p, vt, n);
+  k_scale_add<<<w.red_blocks, 256, 0, s>>>(w.st, F_RCG, SC_CG_BETA, Ap, w.ru, m);
+  lin(w, s, F_ALWAYS, diff, w.grad, SC_NEG_ONE, p, n, nullptr, -1, R_DOT1);
+  k_copy_norm<<<w.red_blocks, 256, 0, s>>>(w.st, F_ALWAYS, vt, nullptr, n, R_XT, -1, w.red_part, w.tickets);
+  k_copy_norm<<<w.red_blocks, 256, 0, s>>>(w.st, F_ALWAYS, w.resid, nullptr, m, R_RES, -1, w.red_part, w.tickets);
+  enq_ctrl(w, s, C_CP_PROJ, h_outer);
+}
+
 // The solve as pieces: prologue, loop body (with the HTP inner CG loop), run either as one
 // graph with WHILE nodes or eagerly (GB_CS_EAGER=1: same kernels, host-checked loops;
 // used for profiling, since kernels inside conditional graphs cannot be profiled).
@@ -542,6 +680,27 @@ void enq_prologue(SolvePlan &P, cudaStream_t s0, cudaGraphConditionalHandle h_ou
   } else if (P.alg == GB_ALG_CSMPSP) {
     // the first CG projection on the support of x follows (algorithms.cu:3462-3476)
     enq_cg_start(w, s0);
+  } else if (P.alg == GB_ALG_FIHT || P.alg == GB_ALG_ALPS) {
+    // one more iteration: x_prev = x, x = H_k(x + A^T (y - A x)) (algorithms.cu:5484-5515)
+    enq_A(w, s0, w.x, w.ru, nullptr, -1, F_ALWAYS);
+    lin(w, s0, F_ALWAYS, w.resid, w.resid, SC_NEG_ONE, w.ru, m, nullptr, -1, R_RES);
+    enq_ctrl(w, s0, C_FH_INIT1);
+    enq_AT(w, s0, w.resid, w.grad, F_ALWAYS);
+    lin(w, s0, F_ALWAYS, w.gp, w.x, SC_ONE, nullptr, n);
+    lin(w, s0, F_ALWAYS, w.am1, w.ru, SC_ONE, nullptr, m);
+    lin(w, s0, F_ALWAYS, w.x, w.x, SC_ONE, w.grad, n);
+    enq_fh_bin(P, s0);
+    enq_A(w, s0, w.x, w.ru, nullptr, -1, F_ALWAYS);
+    lin(w, s0, F_ALWAYS, w.resid, w.y, SC_NEG_ONE, w.ru, m, nullptr, -1, R_RES);
+    enq_ctrl(w, s0, C_FH_INIT2, h_outer);
+  } else if (P.alg == GB_ALG_CGIHT_PROJ) {
+    // r = y - A x; v = (A^T r) on the support; A v (algorithms.cu:4532-4556)
+    enq_A(w, s0, w.x, w.ru, nullptr, -1, F_ALWAYS);
+    lin(w, s0, F_ALWAYS, w.resid, w.resid, SC_NEG_ONE, w.ru, m, nullptr, -1, R_RES);
+    enq_ctrl(w, s0, C_FH_INIT1);
+    enq_grad_masked(w, s0, F_ALWAYS, w.resid, w.xt, -1);
+    enq_A(w, s0, w.xt, w.ru, nullptr, -1, F_ALWAYS);
+    enq_ctrl(w, s0, C_CP_INIT2, h_outer);
   } else if (P.alg == GB_ALG_CGIHT) {
     // r0, grad_previous = A^T r0, grad_prev_thres (algorithms.cu:3776-3808)
     enq_A(w, s0, w.x, w.resid, w.y, R_RES, F_ALWAYS);
@@ -589,6 +748,14 @@ void enq_body(SolvePlan &P, cudaStream_t s1, cudaGraphConditionalHandle h_outer)
   if (P.alg == GB_ALG_HT_CG) {
     // HT_CG_S_gen loop (algorithms.cu:1937-1960): RestrictedCG steps on the fixed support
     enq_cg_body(P, s1, h_outer, C_HTCG_STOP);
+    return;
+  }
+  if (P.alg == GB_ALG_FIHT || P.alg == GB_ALG_ALPS) {
+    enq_fiht_body(P, s1, h_outer);
+    return;
+  }
+  if (P.alg == GB_ALG_CGIHT_PROJ) {
+    enq_cgproj_body(P, s1, h_outer);
     return;
   }
   if (P.alg == GB_ALG_NIHT || P.alg == GB_ALG_HTP) {
@@ -824,6 +991,7 @@ static GbState initial_state(const GbWork &w, int alg, const gb_options &o, int 
   st.alpha_bin = (alg == GB_ALG_HT_SD || alg == GB_ALG_HT_CG) ? 0.0f : 0.25f;
   st.max_bin = (int)((float)o.num_bins * (1.0f - st.alpha_bin));
   if (alg == GB_ALG_IHT) st.mu = 0.65f;  // gaga_gen.cu:640 (case 2)
+  st.proj_frac_tol = o.proj_frac_tol;
   st.beta_to_zero = 1;
   st.supp_change = 1;
   st.tol_cg = tol_abs * tol_abs;

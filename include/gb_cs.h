@@ -44,9 +44,10 @@ enum { GB_OP_DENSE = 0, GB_OP_DCT = 1, GB_OP_SMV = 2 };
 enum { GB_HOST = 0, GB_DEVICE = 1 };
 
 /* Reference algorithm numbers (GAGA/gaga/gaga_gen.cu:619-631, gaga_smv.cu:841-857):
- * "NIHT", "HTP", "IHT", "ThresholdSD", "ThresholdCG", "CSMPSP", "CGIHT", "parallel_l0". */
+ * "NIHT", "HTP", "IHT", "ThresholdSD", "ThresholdCG", "CSMPSP", "CGIHT", "FIHT", "ALPS",
+ * "CGIHTprojected", "parallel_l0". */
 enum { GB_ALG_NIHT = 0, GB_ALG_HTP = 1, GB_ALG_IHT = 2, GB_ALG_HT_SD = 3, GB_ALG_HT_CG = 4, GB_ALG_CSMPSP = 5,
-       GB_ALG_CGIHT = 6, GB_ALG_PARALLEL_L0 = 14 };
+       GB_ALG_CGIHT = 6, GB_ALG_FIHT = 7, GB_ALG_ALPS = 8, GB_ALG_CGIHT_PROJ = 9, GB_ALG_PARALLEL_L0 = 14 };
 
 /* Options: the gagaOptions name/value list (GAGA/gaga/gagaOptions.m:8-58) as a struct. */
 typedef struct {
@@ -72,6 +73,7 @@ typedef struct {
   const char *results_dir;  /* extension: generate-and-solve appends the reference's result
                            line to the dated file in this directory ("" = current directory,
                            as the reference always does); NULL = no file */
+  float proj_frac_tol;  /* 'projFracTol'    3 (CGIHTprojected, gaga_gen.cu:190) */
 } gb_options;
 
 /* A recovery problem in "given data" form. */

@@ -643,8 +643,186 @@ int gbo_solve(const gbo_op *op, const float *y, int k, const gbo_opts *o, float 
   /* HTP (and NIHT_dct) pass max_value as maxChange to force binning; with
    * minVal = 0 every algorithm bins here. */
   gbo_find_support_set(x, w.bins, w.counters, slope, max_value,
-                       (o->alg == GBO_HTP || o->alg == GBO_CSMPSP) ? max_value : 1.0f, &bs, n, k);
+                       (o->alg == GBO_HTP || o->alg == GBO_CSMPSP || o->alg == GBO_CGIHT_PROJ) ? max_value : 1.0f,
+                       &bs, n, k);
   gbo_threshold(x, w.bins, bs.k_bin, n);
+
+  if (o->alg == GBO_FIHT || o->alg == GBO_ALPS) {
+    /* FIHT_S_gen / ALPS_S_gen (GAGA/gaga/algorithms.cu:5430-5706, 6263-6534) with
+     * RestrictedFIHT_S_gen / RestrictedALPS_S_gen (GAGA/gaga/functions.cu:1668-1843) */
+    float *x_prev = w.gp, *extra = w.gpt, *vt = w.xt;
+    float *Apv = (float *)calloc((size_t)m, sizeof(float));
+    float *Aex = (float *)calloc((size_t)m, sizeof(float));
+    float *ru = w.ru;
+    /* one more iteration: x = H_k(x + A^T (y - A x)) */
+    gbo_A(op, x, ru);
+    saxpy(m, -1.0f, ru, w.resid);
+    s.err = nrm2f(w.resid, m);
+    w.prev[15] = s.err;
+    gbo_AT(op, w.resid, w.grad);
+    memcpy(x_prev, x, sizeof(float) * n);
+    memcpy(Apv, ru, sizeof(float) * m);
+    saxpy(n, 1.0f, w.grad, x);
+    bs.min_val = 0.0f;
+    max_value = gbo_max_magnitude(x, n);
+    slope = ((float)(o->num_bins - 1) / max_value);
+    gbo_find_support_set(x, w.bins, w.counters, slope, max_value, 1.0f, &bs, n, k);
+    gbo_threshold(x, w.bins, bs.k_bin, n);
+    gbo_A(op, x, ru);
+    memcpy(w.resid, y, sizeof(float) * m);
+    saxpy(m, -1.0f, ru, w.resid);
+    s.err = nrm2f(w.resid, m);
+    push16(w.prev, s.err);
+    for (int j = 0; j < 15; ++j) s.evol[j] = s.evol[j + 1];
+    s.evol[15] = w.prev[14] - w.prev[15];
+    s.resid_diff = max_list(s.evol, 16);
+    while (keep_going(&s, iter, o->maxiter)) {
+      /* extrapolated point v = x + tau (x_prev - x), tau from the residual line search */
+      saxpy(m, -1.0f, ru, Apv);
+      float tau = dotf(w.resid, Apv, m), tmp = dotf(Apv, Apv, m);
+      if (fabsf(tau) < 400.0f * fabsf(tmp)) tau = tau / tmp;
+      else tau = 0.0f;
+      memcpy(extra, x, sizeof(float) * n);
+      saxpy(n, -1.0f, x, x_prev);
+      saxpy(n, tau, x_prev, extra);
+      memcpy(Aex, ru, sizeof(float) * m);
+      saxpy(m, tau, Apv, Aex);
+      memcpy(w.resid, y, sizeof(float) * m);
+      saxpy(m, -1.0f, Aex, w.resid);
+      gbo_AT(op, w.resid, w.grad);
+      memcpy(x_prev, x, sizeof(float) * n);
+      memcpy(Apv, ru, sizeof(float) * m);
+      if (o->alg == GBO_FIHT) {
+        /* threshold_two: the gradient on the support of v */
+        for (int i = 0; i < n; ++i) vt[i] = extra[i] == 0.0f ? 0.0f : w.grad[i];
+      } else {
+        /* threshold_three, a local FindSupportSet on it (the bin state is passed by value,
+         * so alpha/MaxBin/minVal/k_bin changes stay local), threshold, threshold_four */
+        for (int i = 0; i < n; ++i) vt[i] = extra[i] == 0.0f ? w.grad[i] : 0.0f;
+        gbo_bin_state local = bs;
+        local.min_val = 0.0f;
+        float mv = gbo_max_magnitude(vt, n);
+        float sl = ((float)(o->num_bins - 1) / mv);
+        gbo_find_support_set(vt, w.bins, w.counters, sl, mv, 1.0f, &local, n, k);
+        bs.sum = local.sum;
+        gbo_threshold(vt, w.bins, local.k_bin, n);
+        for (int i = 0; i < n; ++i)
+          if (extra[i] != 0.0f) vt[i] = w.grad[i];
+      }
+      gbo_A(op, vt, Aex);
+      float mu2 = dotf(vt, vt, n);
+      tmp = dotf(Aex, Aex, m);
+      if (mu2 < 400.0f * tmp) mu2 = mu2 / tmp;
+      else mu2 = 1.0f;
+      memcpy(x, extra, sizeof(float) * n);
+      saxpy(n, mu2, w.grad, x);
+      /* new support */
+      bs.min_val = 0.0f;
+      max_value = gbo_max_magnitude(x, n);
+      slope = ((float)(o->num_bins - 1) / max_value);
+      gbo_find_support_set(x, w.bins, w.counters, slope, max_value, 1.0f, &bs, n, k);
+      gbo_threshold(x, w.bins, bs.k_bin, n);
+      gbo_A(op, x, ru);
+      memcpy(w.resid, y, sizeof(float) * m);
+      saxpy(m, -1.0f, ru, w.resid);
+      /* steepest descent on the support */
+      gbo_AT(op, w.resid, w.grad);
+      masked_copy(w.grad, vt, w.bins, bs.k_bin, n);
+      gbo_A(op, vt, Aex);
+      mu2 = dotf(vt, vt, n);
+      tmp = dotf(Aex, Aex, m);
+      if (mu2 < 400.0f * tmp) mu2 = mu2 / tmp;
+      else mu2 = 1.0f;
+      saxpy(n, mu2, vt, x);
+      saxpy(m, mu2, Aex, ru);
+      memcpy(w.resid, y, sizeof(float) * m);
+      saxpy(m, -1.0f, ru, w.resid);
+      s.err = nrm2f(w.resid, m);
+      push16(w.prev, s.err);
+      stop_update(&s, w.prev, iter, 749);
+      iter++;
+    }
+    free(Apv);
+    free(Aex);
+    goto done;
+  }
+  if (o->alg == GBO_CGIHT_PROJ) {
+    /* CGIHTprojected_S_gen (GAGA/gaga/algorithms.cu:4486-4690) */
+    float *vt = w.xt, *p = w.gp, *gpt = w.gpt, *ru = w.ru;
+    float *Ap = (float *)calloc((size_t)m, sizeof(float));
+    float *diff = (float *)calloc((size_t)n, sizeof(float));
+    gbo_A(op, x, ru);
+    saxpy(m, -1.0f, ru, w.resid);
+    s.err = nrm2f(w.resid, m);
+    w.prev[15] = s.err;
+    gbo_AT(op, w.resid, w.grad);
+    masked_copy(w.grad, vt, w.bins, bs.k_bin, n);
+    gbo_A(op, vt, ru);
+    for (int j = 0; j < 15; ++j) s.evol[j] = s.evol[j + 1];
+    s.evol[15] = w.prev[14] - w.prev[15];
+    int supp_change = 1;
+    while (keep_going(&s, iter, o->maxiter)) {
+      float tmp;
+      if (supp_change) {
+        mu = dotf(vt, vt, n);
+        tmp = dotf(ru, ru, m);
+        if (mu < 400.0f * tmp) mu = mu / tmp;
+        else mu = 1.0f;
+        saxpy(n, mu, w.grad, x);
+        bs.min_val = 0.0f;
+        max_value = gbo_max_magnitude(x, n);
+        slope = ((float)(o->num_bins - 1) / max_value);
+        gbo_find_support_set(x, w.bins, w.counters, slope, max_value, 1.0f, &bs, n, k);
+        gbo_threshold(x, w.bins, bs.k_bin, n);
+        gbo_A(op, x, ru);
+        memcpy(w.resid, y, sizeof(float) * m);
+        saxpy(m, -1.0f, ru, w.resid);
+        gbo_AT(op, w.resid, w.grad);
+        masked_copy(w.grad, vt, w.bins, bs.k_bin, n);
+        gbo_A(op, vt, ru);
+        memcpy(p, vt, sizeof(float) * n);
+        memcpy(Ap, ru, sizeof(float) * m);
+      } else {
+        mu = dotf(vt, vt, n);
+        tmp = dotf(Ap, Ap, m);
+        if (mu < 400.0f * tmp) mu = mu / tmp;
+        else mu = 1.0f;
+        saxpy(n, mu, p, x);
+        gbo_A(op, x, ru);
+        memcpy(w.resid, y, sizeof(float) * m);
+        saxpy(m, -1.0f, ru, w.resid);
+        memcpy(gpt, vt, sizeof(float) * n);
+        gbo_AT(op, w.resid, w.grad);
+        masked_copy(w.grad, vt, w.bins, bs.k_bin, n);
+        gbo_A(op, vt, ru);
+        float beta = dotf(vt, vt, n);
+        tmp = dotf(gpt, gpt, n);
+        if (beta < 400.0f * tmp) beta = beta / tmp;
+        else beta = 0.0f;
+        sscal(n, beta, p);
+        saxpy(n, 1.0f, vt, p);
+        sscal(m, beta, Ap);
+        saxpy(m, 1.0f, ru, Ap);
+      }
+      memcpy(diff, w.grad, sizeof(float) * n);
+      saxpy(n, -1.0f, p, diff);
+      float pf = nrm2f(diff, n);
+      tmp = nrm2f(vt, n);
+      if (pf < 1000.0f * tmp) {
+        pf = pf / tmp;
+        supp_change = pf > o->proj_frac_tol ? 1 : 0;
+      } else {
+        supp_change = 1;
+      }
+      s.err = nrm2f(w.resid, m);
+      push16(w.prev, s.err);
+      stop_update(&s, w.prev, iter, 749);
+      iter++;
+    }
+    free(Ap);
+    free(diff);
+    goto done;
+  }
 
   if (o->alg == GBO_CSMPSP) {
     /* CSMPSP_S_gen (GAGA/gaga/algorithms.cu:3372-3688) */
@@ -1046,7 +1224,7 @@ int gbo_solve_dense_trials(int ntrials, const int *nn, const int *mm, const int 
     int ksupp = gbo_gen_vector(n, k, 1, key, 0, xt);
     gbo_op op = {GBO_OP_DENSE, m, n, A, m, 0, 0, 0, 0};
     gbo_A(&op, xt, y);
-    gbo_opts o = {alg, tol_rel * nrm2f(y, m), maxiter, n / 20 > 1000 ? n / 20 : 1000, 0, 1, threads};
+    gbo_opts o = {alg, tol_rel * nrm2f(y, m), maxiter, n / 20 > 1000 ? n / 20 : 1000, 0, 1, threads, 3.0f};
     gbo_info info;
     gbo_solve(&op, y, ksupp, &o, x, &info);
     float norms[3];

@@ -38,7 +38,7 @@ extern "C" {
 
 /* algorithm ids (reference alg switch, GAGA/gaga/gaga_gen.cu:619-631, gaga_smv.cu:841-857) */
 enum { GBO_NIHT = 0, GBO_HTP = 1, GBO_IHT = 2, GBO_HT_SD = 3, GBO_HT_CG = 4, GBO_CSMPSP = 5, GBO_CGIHT = 6,
-       GBO_PARALLEL_L0 = 14, GBO_SERIAL_L0 = 15 };
+       GBO_FIHT = 7, GBO_ALPS = 8, GBO_CGIHT_PROJ = 9, GBO_PARALLEL_L0 = 14, GBO_SERIAL_L0 = 15 };
 /* operator kinds */
 enum { GBO_OP_DENSE = 0, GBO_OP_DCT = 1, GBO_OP_SMV = 2 };
 
@@ -64,6 +64,7 @@ typedef struct {
   int restart;       /* CGIHT restartFlag */
   int l0_thresh;     /* parallel_l0 / serial_l0 alpha */
   int threads;       /* OpenMP threads for operators (0 = runtime default) */
+  float proj_frac_tol; /* CGIHTprojected projFracTol (gaga_gen.cu:190: 3) */
 } gbo_opts;
 
 typedef struct {

@@ -6,10 +6,11 @@ import numpy as np
 
 from . import build as _build
 
-NIHT, HTP, IHT, HT_SD, HT_CG, CSMPSP, CGIHT, PARALLEL_L0, SERIAL_L0 = 0, 1, 2, 3, 4, 5, 6, 14, 15
+NIHT, HTP, IHT, HT_SD, HT_CG, CSMPSP, CGIHT, FIHT, ALPS, CGIHT_PROJ, PARALLEL_L0, SERIAL_L0 = (0, 1, 2, 3, 4, 5, 6, 7, 8,
+                                                                                        9, 14, 15)
 OP_DENSE, OP_DCT, OP_SMV = 0, 1, 2
 ALG_IDS = {"NIHT": NIHT, "HTP": HTP, "IHT": IHT, "ThresholdSD": HT_SD, "ThresholdCG": HT_CG, "CSMPSP": CSMPSP,
-           "CGIHT": CGIHT,
+           "CGIHT": CGIHT, "FIHT": FIHT, "ALPS": ALPS, "CGIHTprojected": CGIHT_PROJ,
            "parallel_l0": PARALLEL_L0, "serial_l0": SERIAL_L0}
 
 _lib = None
@@ -31,7 +32,7 @@ class GboOp(C.Structure):
 
 class GboOpts(C.Structure):
     _fields_ = [("alg", C.c_int), ("tol", C.c_float), ("maxiter", C.c_int), ("num_bins", C.c_int),
-                ("restart", C.c_int), ("l0_thresh", C.c_int), ("threads", C.c_int)]
+                ("restart", C.c_int), ("l0_thresh", C.c_int), ("threads", C.c_int), ("proj_frac_tol", C.c_float)]
 
 
 class GboInfo(C.Structure):
@@ -203,14 +204,14 @@ def default_num_bins(n):
     return max(n // 20, 1000)
 
 
-def solve(alg, op, y, k, tol, maxiter=None, num_bins=None, restart=0, threads=0):
+def solve(alg, op, y, k, tol, maxiter=None, num_bins=None, restart=0, threads=0, proj_frac_tol=3.0):
     alg_id = ALG_IDS[alg] if isinstance(alg, str) else alg
     if maxiter is None:
         maxiter = 300 if alg_id == HTP else 5000
     num_bins = num_bins or default_num_bins(op.n)
     y = f32(y)
     x = np.zeros(op.n, dtype=np.float32)
-    o = GboOpts(alg_id, tol, maxiter, num_bins, restart, 1, threads)
+    o = GboOpts(alg_id, tol, maxiter, num_bins, restart, 1, threads, proj_frac_tol)
     info = GboInfo()
     lib().gbo_solve(C.byref(op.c), _p(y), k, C.byref(o), _p(x), C.byref(info))
     return x, info

@@ -1,8 +1,9 @@
-"""IHT, ThresholdSD, ThresholdCG and CSMPSP on the GPU against the CPU oracle, on the dense,
-DCT and expander operators.
+"""IHT, ThresholdSD, ThresholdCG, CSMPSP, FIHT, ALPS and CGIHTprojected on the GPU against the
+CPU oracle, on the dense, DCT and expander operators.
 
-The oracle restates IHT_S_*, HT_SD_S_*, HT_CG_S_* and CSMPSP_S_* (GAGA/gaga/algorithms.cu:
-347-478, 785-906, 1826-1990, 3372-3688).  Each case compares the success verdict (relative l2 <= 1e-3 to the
+The oracle restates IHT_S_*, HT_SD_S_*, HT_CG_S_*, CSMPSP_S_*, FIHT_S_*, ALPS_S_* and
+CGIHTprojected_S_* (GAGA/gaga/algorithms.cu:347-478, 785-906, 1826-1990, 3372-3688,
+4486-4690, 5430-5706, 6263-6534).  Each case compares the success verdict (relative l2 <= 1e-3 to the
 planted signal), the solution against the oracle's, and the iteration count.  ThresholdSD /
 ThresholdCG fix the support after one hard threshold of A^T y, so a case with a larger k
 (a wrong support) checks that both sides reach the same least-squares fit on it.
@@ -12,7 +13,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-ALGS = ["IHT", "ThresholdSD", "ThresholdCG", "CSMPSP"]
+ALGS = ["IHT", "ThresholdSD", "ThresholdCG", "CSMPSP", "FIHT", "ALPS", "CGIHTprojected"]
 
 
 def _dense(gbo, k, seed):

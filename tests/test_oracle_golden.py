@@ -97,7 +97,7 @@ def test_ref_library_matches_fixtures_when_present(gbo):
     assert np.array_equal(bins, z[f"{name}__bins"])
 
 
-@pytest.mark.parametrize("alg", ["IHT", "ThresholdSD", "ThresholdCG", "CSMPSP"])
+@pytest.mark.parametrize("alg", ["IHT", "ThresholdSD", "ThresholdCG", "CSMPSP", "FIHT", "ALPS", "CGIHTprojected"])
 def test_oracle_remaining_algorithms_recover_easy_problem(gbo, alg):
     """IHT, ThresholdSD and ThresholdCG restated from the reference recover a problem well
     inside their recovery region (one-step thresholding needs a small rho)."""
