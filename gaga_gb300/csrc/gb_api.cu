@@ -48,6 +48,8 @@ extern "C" int gb_cs_alg_id(const char *alg) {
   if (!strcmp(alg, "CGIHTprojected")) return GB_ALG_CGIHT_PROJ;
   if (!strcmp(alg, "CGIHT")) return GB_ALG_CGIHT;
   if (!strcmp(alg, "parallel_l0")) return GB_ALG_PARALLEL_L0;
+  if (!strcmp(alg, "parallel_lddsr")) return GB_ALG_PARALLEL_LDDSR;
+  if (!strcmp(alg, "parallel_l0_swipe")) return GB_ALG_PARALLEL_L0_SWIPE;
   return -1;
 }
 
@@ -301,8 +303,8 @@ extern "C" gb_status gb_cs_solve(const char *alg, const gb_problem *p, const gb_
   if (!p || !x_out) return bad("null argument");
   const int alg_id = gb_cs_alg_id(alg);
   if (alg_id < 0) return bad("algorithm must be one of NIHT, HTP, IHT, ThresholdSD, ThresholdCG, CSMPSP, CGIHT, FIHT, ALPS, "
-                         "CGIHTprojected, parallel_l0");
-  if (alg_id == GB_ALG_PARALLEL_L0 && p->kind != GB_OP_SMV) return bad("parallel_l0 requires the smv operator");
+                         "CGIHTprojected, parallel_l0, parallel_lddsr, parallel_l0_swipe");
+  if (gb_is_l0(alg_id) && p->kind != GB_OP_SMV) return bad("the l0 decoders require the smv operator");
   gb_options o;
   if (opts) o = *opts;
   else gb_cs_default_options(&o, alg, p->n);
@@ -314,7 +316,7 @@ extern "C" gb_status gb_cs_solve(const char *alg, const gb_problem *p, const gb_
   GbWork w;
   memset(&w, 0, sizeof(w));
   GB_TRY(setup_problem(db, w, *p, s, o.num_bins, o.maxiter));
-  if (alg_id == GB_ALG_PARALLEL_L0) {
+  if (gb_is_l0(alg_id)) {
     if (o.l0_thresh < 1 || o.l0_thresh > w.op.d) o.l0_thresh = 1;  // gaga_smv.cu:313
   }
   if (o.learned_params && alg_id == GB_ALG_CGIHT) {
@@ -356,7 +358,7 @@ extern "C" gb_status gb_cs_solve(const char *alg, const gb_problem *p, const gb_
   GB_CUDA_TRY(cudaMemcpyAsync(x_out, w.x, sizeof(float) * p->n,
                               p->location == GB_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
   std::vector<float> rec;
-  if (alg_id == GB_ALG_PARALLEL_L0) {
+  if (gb_is_l0(alg_id)) {
     rec.resize((size_t)o.maxiter + 1);
     GB_CUDA_TRY(cudaMemcpyAsync(rec.data(), w.rec, sizeof(float) * (o.maxiter + 1), cudaMemcpyDeviceToHost, s));
   }
@@ -375,7 +377,7 @@ extern "C" gb_status gb_cs_solve(const char *alg, const gb_problem *p, const gb_
     r->times[0] = ms;
     r->times[1] = st.iter > 0 ? ms / st.iter : 0.0f;
     r->times[2] = ms;
-    if (alg_id == GB_ALG_PARALLEL_L0) {
+    if (gb_is_l0(alg_id)) {
       // the last <= 16 residual records become residNorm_prev (gaga_smv.cu:1013-1020)
       for (int j = 0; j < std::min(st.iter, 16); ++j) r->resid_prev[15 - j] = rec[st.iter - j];
       if (user_rec) memcpy(user_rec, rec.data(), sizeof(float) * (o.maxiter + 1));
@@ -458,8 +460,8 @@ extern "C" gb_status gb_cs_generate_and_solve(const char *alg, int kind, int k, 
   if (!x_out) return bad("null argument");
   const int alg_id = gb_cs_alg_id(alg);
   if (alg_id < 0) return bad("algorithm must be one of NIHT, HTP, IHT, ThresholdSD, ThresholdCG, CSMPSP, CGIHT, FIHT, ALPS, "
-                         "CGIHTprojected, parallel_l0");
-  if (alg_id == GB_ALG_PARALLEL_L0 && kind != GB_OP_SMV) return bad("parallel_l0 requires the smv operator");
+                         "CGIHTprojected, parallel_l0, parallel_lddsr, parallel_l0_swipe");
+  if (gb_is_l0(alg_id) && kind != GB_OP_SMV) return bad("the l0 decoders require the smv operator");
   if (k < 1 || m < 1 || n < 1 || (kind == GB_OP_SMV && d < 1)) return bad("k, m, n (and d) must be positive");
   gb_options o;
   if (opts) o = *opts;
@@ -512,7 +514,7 @@ extern "C" gb_status gb_cs_generate_and_solve(const char *alg, int kind, int k, 
     p.rows = rows.data();
   } else {
     int ens = o.matrix_ensemble ? o.matrix_ensemble : 3;
-    if (alg_id == GB_ALG_PARALLEL_L0) ens = 3;  // ccs algorithms force ones (gaga_smv.cu:403-405)
+    if (gb_is_l0(alg_id)) ens = 3;  // ccs algorithms force ones (gaga_smv.cu:403-405)
     rows.resize((size_t)n * d);
     vals.resize((size_t)n * d);
     float scale = (ens == 1 || ens == 2) ? 1.0f / sqrtf((float)d) : 1.0f;
@@ -572,7 +574,7 @@ extern "C" gb_status gb_cs_generate_and_solve(const char *alg, int kind, int k, 
     GB_CUDA_TRY(cudaMemcpy(w.y, yh.data(), sizeof(float) * m, cudaMemcpyHostToDevice));
   }
   GB_CUDA_TRY(cudaMemset(w.x, 0, sizeof(float) * n));
-  if (alg_id == GB_ALG_PARALLEL_L0 && (o.l0_thresh < 1 || o.l0_thresh > d)) o.l0_thresh = 1;
+  if (gb_is_l0(alg_id) && (o.l0_thresh < 1 || o.l0_thresh > d)) o.l0_thresh = 1;
   float tol_abs = o.tol;
   if (o.tol_is_relative) {
     std::vector<float> yh(m);
@@ -588,7 +590,7 @@ extern "C" gb_status gb_cs_generate_and_solve(const char *alg, int kind, int k, 
   GB_CUDA_TRY(cudaMemcpy(&st, w.st, sizeof(st), cudaMemcpyDeviceToHost));
   GB_CUDA_TRY(cudaMemcpy(x_out, w.x, sizeof(float) * n, cudaMemcpyDeviceToHost));
   std::vector<float> rec;
-  if (alg_id == GB_ALG_PARALLEL_L0) {
+  if (gb_is_l0(alg_id)) {
     rec.resize((size_t)o.maxiter + 1);
     GB_CUDA_TRY(cudaMemcpy(rec.data(), w.rec, sizeof(float) * (o.maxiter + 1), cudaMemcpyDeviceToHost));
   }
@@ -609,7 +611,7 @@ extern "C" gb_status gb_cs_generate_and_solve(const char *alg, int kind, int k, 
     r->iter = st.iter;
     r->k_used = ks;
     r->stop_reason = st.stop_reason;
-    if (alg_id == GB_ALG_PARALLEL_L0) {
+    if (gb_is_l0(alg_id)) {
       for (int j = 0; j < std::min(st.iter, 16); ++j) r->resid_prev[15 - j] = rec[st.iter - j];
       if (user_rec) memcpy(user_rec, rec.data(), sizeof(float) * (o.maxiter + 1));
     } else {

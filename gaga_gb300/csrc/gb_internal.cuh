@@ -64,7 +64,7 @@ struct GbState {
   int it_cg;
   float err_cg, tol_cg, tol2, diff_cg, prev_cg[16], evol_cg[16];
   // l0 decoding bookkeeping (GAGA/gaga/expander/parallel_l0.cu:36-60)
-  int found, l0_len, l0_offset;
+  int found, l0_len, l0_offset, l0_mode;  // l0_mode: 0 parallel_l0, 1 parallel_lddsr, 2 parallel_l0_swipe
   float norm, norm0, l0_diff, l0_prev[64], l0_evol[64], l0_cyc[64];
   // predicates and reduction results
   int flags[GB_NFLAG];
@@ -142,6 +142,11 @@ void gb_set_error_message(const char *msg, const char *file, int line);
     gb_status s_ = (call);      \
     if (s_ != GB_OK) return s_; \
   } while (0)
+
+// the expander decoders that share parallel_l0's kernels
+inline bool gb_is_l0(int alg) {
+  return alg == GB_ALG_PARALLEL_L0 || alg == GB_ALG_PARALLEL_LDDSR || alg == GB_ALG_PARALLEL_L0_SWIPE;
+}
 
 // ---------------------------------------------------------------- device helpers
 // Dimension arguments of the solver kernels: a value >= 0 is used as is; a negative code

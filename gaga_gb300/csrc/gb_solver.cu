@@ -32,8 +32,10 @@ __global__ void k_ctrl_l0(GbState *st, int phase, float *rec, cudaGraphCondition
       for (int i = 0; i < L; ++i) { st->l0_cyc[i] = 0.0f; st->l0_prev[i] = 0.0f; st->l0_evol[i] = 1.0f; }
       st->l0_diff = 1.0f;
       st->found = 1;
+      if (st->l0_mode == 2) st->l0_thresh = st->d - 1;  // parallel_l0_swipe.cu:11
       st->active = (st->iter < st->maxiter) & (st->norm > st->tol) & (st->norm < (100.0f * st->norm0)) &
-                   ((double)st->l0_diff > 0.000001) & (st->cycle != 0) & (st->found == 1);
+                   ((double)st->l0_diff > 0.000001) & (st->cycle != 0) & (st->found == 1) &
+                   (st->l0_mode != 2 || st->l0_thresh > 0);
       set_cond(h, st->active ? 1u : 0u);
       break;
     case C_L0_PRE:
@@ -42,7 +44,23 @@ __global__ void k_ctrl_l0(GbState *st, int phase, float *rec, cudaGraphCondition
       st->found = 0;
       break;
     case C_L0_STOP:
-      if (st->active) {
+      if (st->active && st->l0_mode == 2 && st->found == 0 && st->l0_thresh > 0) {
+        // parallel_l0_swipe: no column qualified; lower the threshold, keep the residual
+        // history (parallel_l0_swipe.cu:82-85)
+        st->l0_thresh--;
+        st->found = 1;
+        st->iter++;
+        st->passes++;
+        if (rec) rec[st->iter] = st->norm;
+        const int go = (st->iter < st->maxiter) & (st->norm > st->tol) & (st->norm < (100.0f * st->norm0)) &
+                       ((double)st->l0_diff > 0.000001) & (st->cycle != 0) & (st->l0_thresh > 0);
+        if (!go) st->stop_reason = !(st->iter < st->maxiter) ? 2 : 7;
+        st->active = go;
+        if (st->passes > st->pass_limit && st->active) {
+          st->active = 0;
+          st->status = GB_WATCHDOG;
+        }
+      } else if (st->active) {
         st->norm = sqrt_red(st, R_RES);
         for (int i = 0; i < L - 1; ++i) st->l0_prev[i] = st->l0_prev[i + 1];
         st->l0_prev[L - 1] = st->norm;
@@ -61,7 +79,8 @@ __global__ void k_ctrl_l0(GbState *st, int phase, float *rec, cudaGraphCondition
         st->passes++;
         if (rec) rec[st->iter] = st->norm;
         int go = (st->iter < st->maxiter) & (st->norm > st->tol) & (st->norm < (100.0f * st->norm0)) &
-                 ((double)st->l0_diff > 0.000001) & (cycling == 0) & (st->found == 1);
+                 ((double)st->l0_diff > 0.000001) & (cycling == 0) & (st->found == 1) &
+                 (st->l0_mode != 2 || st->l0_thresh > 0);
         if (!go) {
           if (!(st->norm > st->tol)) st->stop_reason = 1;
           else if (!(st->iter < st->maxiter)) st->stop_reason = 2;
@@ -377,6 +396,10 @@ __global__ void k_l0_scores(GbState *st, const float *__restrict__ res, float *_
   if (!st->active) return;
   const int thresh = st->l0_thresh;
   const int shift = st->l0_offset;
+  const bool lddsr = st->l0_mode == 1;
+  // cuda_compute_scores_lddsr (GAGA/gaga/expander/kernels.cu:309-345): matching rows only,
+  // more than d/2 of them
+  const float cut = lddsr ? ((float)d) / 2 : (float)thresh;
   const float EPS = 0.000001f;
   int found = 0;
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
@@ -388,9 +411,9 @@ __global__ void k_l0_scores(GbState *st, const float *__restrict__ res, float *_
       for (int i = 0; i < d; ++i) {
         const float ri = res[rows[idx + i]];
         if (fabsf(__fsub_rn(ri, omega)) <= EPS) score += 1.0f;
-        if (fabsf(ri) <= EPS) score -= 1.0f;
+        if (!lddsr && fabsf(ri) <= EPS) score -= 1.0f;
       }
-      if (score > (float)thresh) {
+      if (score > cut) {
         found = 1;
         x[j] = __fadd_rn(x[j], omega);
         u = omega;
@@ -642,7 +665,7 @@ static void enq_cgproj_body(SolvePlan &P, cudaStream_t s, cudaGraphConditionalHa
 void enq_prologue(SolvePlan &P, cudaStream_t s0, cudaGraphConditionalHandle h_outer) {
   GbWork &w = *P.w;
   const int n = argN(w), m = argM(w), k = P.k, num_bins = w.dyn ? D_NBINS : P.num_bins;
-  if (P.alg == GB_ALG_PARALLEL_L0) {
+  if (gb_is_l0(P.alg)) {
     // res = y - A x with x = 0 (computeResidual, GAGA/gaga/expander/functions.cu:73-79)
     enq_A(w, s0, w.x, w.resid, w.y, R_RES, F_ALWAYS);
     k_ctrl_l0<<<1, 32, 0, s0>>>(w.st, C_L0_INIT, w.rec, h_outer);
@@ -992,6 +1015,7 @@ static GbState initial_state(const GbWork &w, int alg, const gb_options &o, int 
   st.max_bin = (int)((float)o.num_bins * (1.0f - st.alpha_bin));
   if (alg == GB_ALG_IHT) st.mu = 0.65f;  // gaga_gen.cu:640 (case 2)
   st.proj_frac_tol = o.proj_frac_tol;
+  st.l0_mode = alg == GB_ALG_PARALLEL_LDDSR ? 1 : alg == GB_ALG_PARALLEL_L0_SWIPE ? 2 : 0;
   st.beta_to_zero = 1;
   st.supp_change = 1;
   st.tol_cg = tol_abs * tol_abs;
@@ -1005,7 +1029,7 @@ static GbState initial_state(const GbWork &w, int alg, const gb_options &o, int 
 
 // Runs one solve on the prepared workspace (x zero, y uploaded); results stay in GbState.
 gb_status gb_run_solver(GbWork &w, int alg, const gb_options &o, int k, cudaStream_t s, float tol_abs) {
-  if (alg == GB_ALG_PARALLEL_L0 && (w.op.d <= 0 || 2 * w.op.d > 64)) return GB_UNSUPPORTED;
+  if (gb_is_l0(alg) && (w.op.d <= 0 || 2 * w.op.d > 64)) return GB_UNSUPPORTED;
   GbState init = initial_state(w, alg, o, k, tol_abs);
   k_init_state<<<1, 1, 0, s>>>(w.st, init);
   GB_CUDA_TRY(cudaGetLastError());

@@ -1070,7 +1070,33 @@ void gbo_l0_update_residual(float *res, const int *rows, const float *updates, i
   }
 }
 
-/* parallel_l0 (GAGA/gaga/expander/parallel_l0.cu:9-151) */
+/* cuda_compute_scores_lddsr (GAGA/gaga/expander/kernels.cu:309-345): only matching rows
+ * count, a candidate needs more than d/2 of them */
+static void lddsr_scores(const float *res, float *x, float *updates, const int *rows, int n, int d, int shift,
+                         int *found) {
+  const float EPS = 0.000001f;
+  const float thresh = ((float)d) / 2;
+  for (int j = 0; j < n; ++j) {
+    int idx = d * j;
+    float score = 0.0f;
+    float omega = res[rows[idx + shift]];
+    updates[j] = 0.0f;
+    if (fabsf(omega) > EPS) {
+      for (int i = 0; i < d; ++i)
+        if (fabsf(res[rows[idx + i]] - omega) <= EPS) score += 1.0f;
+      if (score > thresh) {
+        *found = 1;
+        x[j] = x[j] + omega;
+        updates[j] = omega;
+      }
+    }
+  }
+}
+
+/* parallel_l0 (GAGA/gaga/expander/parallel_l0.cu:9-151); o->alg may also select
+ * parallel_lddsr (parallel_lddsr.cu: lddsr scores) or parallel_l0_swipe
+ * (parallel_l0_swipe.cu: the threshold starts at d - 1 and drops by one whenever no
+ * column qualifies; such a pass leaves the residual history alone) */
 int gbo_parallel_l0(const gbo_op *op, const float *y, const gbo_opts *o, float *x, float *res,
                     float *res_record, gbo_info *info) {
   int m = op->m, n = op->n, d = op->d;
@@ -1087,11 +1113,21 @@ int gbo_parallel_l0(const gbo_op *op, const float *y, const gbo_opts *o, float *
   for (int i = 0; i < L; ++i) evol[i] = 1.0f;
   float diff = 1.0f;
   int iter = 0, cycling = 0, found = 1;
+  const int swipe = o->alg == GBO_PARALLEL_L0_SWIPE;
+  int thresh = swipe ? d - 1 : o->l0_thresh;
   while ((iter < o->maxiter) & (norm > o->tol) & (norm < (100.0f * norm0)) & ((double)diff > 0.000001) &
-         (cycling == 0) & (found == 1)) {
+         (cycling == 0) & (found == 1) & (!swipe || thresh > 0)) {
     int offset = iter % d;
     found = 0;
-    gbo_l0_scores(res, x, upd, op->smv_rows, n, d, o->l0_thresh, offset, &found);
+    if (o->alg == GBO_PARALLEL_LDDSR) lddsr_scores(res, x, upd, op->smv_rows, n, d, offset, &found);
+    else gbo_l0_scores(res, x, upd, op->smv_rows, n, d, thresh, offset, &found);
+    if (swipe && found == 0 && thresh > 0) {
+      thresh--;
+      found = 1;
+      iter = iter + 1;
+      if (res_record) res_record[iter] = norm;
+      continue;
+    }
     gbo_l0_update_residual(res, op->smv_rows, upd, n, d);
     norm = nrm2f(res, m);
     for (int i = 0; i < L - 1; ++i) prev[i] = prev[i + 1];

@@ -38,7 +38,8 @@ extern "C" {
 
 /* algorithm ids (reference alg switch, GAGA/gaga/gaga_gen.cu:619-631, gaga_smv.cu:841-857) */
 enum { GBO_NIHT = 0, GBO_HTP = 1, GBO_IHT = 2, GBO_HT_SD = 3, GBO_HT_CG = 4, GBO_CSMPSP = 5, GBO_CGIHT = 6,
-       GBO_FIHT = 7, GBO_ALPS = 8, GBO_CGIHT_PROJ = 9, GBO_PARALLEL_L0 = 14, GBO_SERIAL_L0 = 15 };
+       GBO_FIHT = 7, GBO_ALPS = 8, GBO_CGIHT_PROJ = 9, GBO_PARALLEL_LDDSR = 13, GBO_PARALLEL_L0 = 14,
+       GBO_SERIAL_L0 = 15, GBO_PARALLEL_L0_SWIPE = 18 };
 /* operator kinds */
 enum { GBO_OP_DENSE = 0, GBO_OP_DCT = 1, GBO_OP_SMV = 2 };
 

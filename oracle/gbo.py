@@ -8,6 +8,7 @@ from . import build as _build
 
 NIHT, HTP, IHT, HT_SD, HT_CG, CSMPSP, CGIHT, FIHT, ALPS, CGIHT_PROJ, PARALLEL_L0, SERIAL_L0 = (0, 1, 2, 3, 4, 5, 6, 7, 8,
                                                                                         9, 14, 15)
+PARALLEL_LDDSR, PARALLEL_L0_SWIPE = 13, 18
 OP_DENSE, OP_DCT, OP_SMV = 0, 1, 2
 ALG_IDS = {"NIHT": NIHT, "HTP": HTP, "IHT": IHT, "ThresholdSD": HT_SD, "ThresholdCG": HT_CG, "CSMPSP": CSMPSP,
            "CGIHT": CGIHT, "FIHT": FIHT, "ALPS": ALPS, "CGIHTprojected": CGIHT_PROJ,
@@ -217,12 +218,14 @@ def solve(alg, op, y, k, tol, maxiter=None, num_bins=None, restart=0, threads=0,
     return x, info
 
 
-def parallel_l0(op, y, tol, maxiter, l0_thresh=1):
+def parallel_l0(op, y, tol, maxiter, l0_thresh=1, variant="parallel_l0"):
+    """parallel_l0, or its variants parallel_lddsr / parallel_l0_swipe."""
     y = f32(y)
     x = np.zeros(op.n, dtype=np.float32)
     res = np.zeros(op.m, dtype=np.float32)
     rec = np.zeros(maxiter + 1, dtype=np.float32)
-    o = GboOpts(PARALLEL_L0, tol, maxiter, 1000, 0, l0_thresh, 0)
+    alg = {"parallel_l0": PARALLEL_L0, "parallel_lddsr": PARALLEL_LDDSR, "parallel_l0_swipe": PARALLEL_L0_SWIPE}[variant]
+    o = GboOpts(alg, tol, maxiter, 1000, 0, l0_thresh, 0)
     info = GboInfo()
     lib().gbo_parallel_l0(C.byref(op.c), _p(y), C.byref(o), _p(x), _p(res), _p(rec), C.byref(info))
     return x, res, rec, info

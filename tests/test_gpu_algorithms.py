@@ -83,3 +83,23 @@ def test_generate_and_solve_new_algorithms(gb, alg):
     opts = gb.gaga_options("tol", 1e-5, "tol_is_relative", 1, "seed", 3)
     norms, times, iters, supp, conv, x = gb.gaga_cs(alg, "gen", 20, 1024, 4096, opts)
     assert norms[1] < 1e-3 and iters > 0
+
+
+@pytest.mark.parametrize("variant", ["parallel_lddsr", "parallel_l0_swipe"])
+@pytest.mark.parametrize("n,m", [(2 ** 14, 2 ** 12), (2 ** 18, 2 ** 16)])
+def test_l0_variants_bit_exact(gb, gbo, variant, n, m):
+    """parallel_lddsr (lddsr scores) and parallel_l0_swipe (falling threshold) on the
+    unit-valued expander with a +-1 signal: integer residuals, so x, the iteration count
+    and the residual record equal the oracle's bit for bit."""
+    d, k = 7, m // 20
+    rows, vals = gbo.gen_smv(m, n, d, 3, seed=19)
+    x0, ks = gbo.gen_vector(n, k, 1, seed=19)
+    op = gbo.Op.smv(m, n, d, rows, vals)
+    y = gbo.A(op, x0)
+    cols = np.repeat(np.arange(n, dtype=np.int32), d)
+    opts = gb.gaga_options("tol", 1e-6, "maxiter", 300)
+    x, iters, conv, rec, trec = gb.gaga_cs(variant, "smv", y, rows, cols, vals, ks, opts, index_base=0)
+    xo, reso, reco, info = gbo.parallel_l0(op, y, tol=1e-6, maxiter=300, variant=variant)
+    assert iters == info.iter
+    assert np.array_equal(np.asarray(x), xo)
+    assert np.array_equal(np.asarray(rec)[: iters + 1], reco[: iters + 1])

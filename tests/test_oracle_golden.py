@@ -108,3 +108,15 @@ def test_oracle_remaining_algorithms_recover_easy_problem(gbo, alg):
     y = gbo.A(op, x0)
     x, info = gbo.solve(alg, op, y, ks, 1e-5 * float(np.linalg.norm(y)))
     assert np.linalg.norm(x - x0) / np.linalg.norm(x0) < 1e-3, (alg, info.iter)
+
+
+@pytest.mark.parametrize("variant", ["parallel_l0", "parallel_lddsr", "parallel_l0_swipe"])
+def test_oracle_l0_variants_decode(gbo, variant):
+    """The expander decoders recover a +-1 signal well inside their recovery region."""
+    n, m, d = 4096, 1024, 7
+    rows, vals = gbo.gen_smv(m, n, d, 3, seed=23)
+    x0, ks = gbo.gen_vector(n, 20, 1, seed=23)
+    op = gbo.Op.smv(m, n, d, rows, vals)
+    y = gbo.A(op, x0)
+    x, res, rec, info = gbo.parallel_l0(op, y, tol=1e-6, maxiter=300, variant=variant)
+    assert np.array_equal(x, x0), (variant, info.iter)
