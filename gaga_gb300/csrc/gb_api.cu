@@ -49,6 +49,7 @@ extern "C" int gb_cs_alg_id(const char *alg) {
   if (!strcmp(alg, "CGIHT")) return GB_ALG_CGIHT;
   if (!strcmp(alg, "parallel_l0")) return GB_ALG_PARALLEL_L0;
   if (!strcmp(alg, "parallel_lddsr")) return GB_ALG_PARALLEL_LDDSR;
+  if (!strcmp(alg, "smp")) return GB_ALG_SMP;
   if (!strcmp(alg, "parallel_l0_swipe")) return GB_ALG_PARALLEL_L0_SWIPE;
   return -1;
 }
@@ -147,7 +148,7 @@ gb_status alloc_work(DeviceBuffers &db, GbWork &w, int m, int n, int lda, int nu
   GB_TRY(db.alloc(&w.bins_prev, n));
   GB_TRY(db.alloc(&w.counters, std::max(num_bins, 1)));
   GB_TRY(db.alloc(&w.S, n));
-  GB_TRY(db.alloc(&w.tile_cnt, (n + GB_TILE - 1) / GB_TILE));
+  GB_TRY(db.alloc(&w.tile_cnt, 2 * ((n + GB_TILE - 1) / GB_TILE)));  // second half: smp's k-th bin counts
   GB_TRY(db.alloc(&w.rec, (size_t)maxiter + 2));
   gb_dense_av_shape(m, w.num_sms, &w.av_ntile, &w.av_nsplit);
   w.part_cap = gb_dense_part_floats_av(w.av_ntile, w.av_nsplit);
@@ -303,8 +304,8 @@ extern "C" gb_status gb_cs_solve(const char *alg, const gb_problem *p, const gb_
   if (!p || !x_out) return bad("null argument");
   const int alg_id = gb_cs_alg_id(alg);
   if (alg_id < 0) return bad("algorithm must be one of NIHT, HTP, IHT, ThresholdSD, ThresholdCG, CSMPSP, CGIHT, FIHT, ALPS, "
-                         "CGIHTprojected, parallel_l0, parallel_lddsr, parallel_l0_swipe");
-  if (gb_is_l0(alg_id) && p->kind != GB_OP_SMV) return bad("the l0 decoders require the smv operator");
+                         "CGIHTprojected, smp, parallel_l0, parallel_lddsr, parallel_l0_swipe");
+  if (gb_is_ccs(alg_id) && p->kind != GB_OP_SMV) return bad("the expander decoders require the smv operator");
   gb_options o;
   if (opts) o = *opts;
   else gb_cs_default_options(&o, alg, p->n);
@@ -316,7 +317,7 @@ extern "C" gb_status gb_cs_solve(const char *alg, const gb_problem *p, const gb_
   GbWork w;
   memset(&w, 0, sizeof(w));
   GB_TRY(setup_problem(db, w, *p, s, o.num_bins, o.maxiter));
-  if (gb_is_l0(alg_id)) {
+  if (gb_is_ccs(alg_id)) {
     if (o.l0_thresh < 1 || o.l0_thresh > w.op.d) o.l0_thresh = 1;  // gaga_smv.cu:313
   }
   if (o.learned_params && alg_id == GB_ALG_CGIHT) {
@@ -358,7 +359,7 @@ extern "C" gb_status gb_cs_solve(const char *alg, const gb_problem *p, const gb_
   GB_CUDA_TRY(cudaMemcpyAsync(x_out, w.x, sizeof(float) * p->n,
                               p->location == GB_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
   std::vector<float> rec;
-  if (gb_is_l0(alg_id)) {
+  if (gb_is_ccs(alg_id)) {
     rec.resize((size_t)o.maxiter + 1);
     GB_CUDA_TRY(cudaMemcpyAsync(rec.data(), w.rec, sizeof(float) * (o.maxiter + 1), cudaMemcpyDeviceToHost, s));
   }
@@ -377,7 +378,7 @@ extern "C" gb_status gb_cs_solve(const char *alg, const gb_problem *p, const gb_
     r->times[0] = ms;
     r->times[1] = st.iter > 0 ? ms / st.iter : 0.0f;
     r->times[2] = ms;
-    if (gb_is_l0(alg_id)) {
+    if (gb_is_ccs(alg_id)) {
       // the last <= 16 residual records become residNorm_prev (gaga_smv.cu:1013-1020)
       for (int j = 0; j < std::min(st.iter, 16); ++j) r->resid_prev[15 - j] = rec[st.iter - j];
       if (user_rec) memcpy(user_rec, rec.data(), sizeof(float) * (o.maxiter + 1));
@@ -460,8 +461,8 @@ extern "C" gb_status gb_cs_generate_and_solve(const char *alg, int kind, int k, 
   if (!x_out) return bad("null argument");
   const int alg_id = gb_cs_alg_id(alg);
   if (alg_id < 0) return bad("algorithm must be one of NIHT, HTP, IHT, ThresholdSD, ThresholdCG, CSMPSP, CGIHT, FIHT, ALPS, "
-                         "CGIHTprojected, parallel_l0, parallel_lddsr, parallel_l0_swipe");
-  if (gb_is_l0(alg_id) && kind != GB_OP_SMV) return bad("the l0 decoders require the smv operator");
+                         "CGIHTprojected, smp, parallel_l0, parallel_lddsr, parallel_l0_swipe");
+  if (gb_is_ccs(alg_id) && kind != GB_OP_SMV) return bad("the expander decoders require the smv operator");
   if (k < 1 || m < 1 || n < 1 || (kind == GB_OP_SMV && d < 1)) return bad("k, m, n (and d) must be positive");
   gb_options o;
   if (opts) o = *opts;
@@ -514,7 +515,7 @@ extern "C" gb_status gb_cs_generate_and_solve(const char *alg, int kind, int k, 
     p.rows = rows.data();
   } else {
     int ens = o.matrix_ensemble ? o.matrix_ensemble : 3;
-    if (gb_is_l0(alg_id)) ens = 3;  // ccs algorithms force ones (gaga_smv.cu:403-405)
+    if (gb_is_ccs(alg_id)) ens = 3;  // ccs algorithms force ones (gaga_smv.cu:403-405)
     rows.resize((size_t)n * d);
     vals.resize((size_t)n * d);
     float scale = (ens == 1 || ens == 2) ? 1.0f / sqrtf((float)d) : 1.0f;
@@ -574,7 +575,7 @@ extern "C" gb_status gb_cs_generate_and_solve(const char *alg, int kind, int k, 
     GB_CUDA_TRY(cudaMemcpy(w.y, yh.data(), sizeof(float) * m, cudaMemcpyHostToDevice));
   }
   GB_CUDA_TRY(cudaMemset(w.x, 0, sizeof(float) * n));
-  if (gb_is_l0(alg_id) && (o.l0_thresh < 1 || o.l0_thresh > d)) o.l0_thresh = 1;
+  if (gb_is_ccs(alg_id) && (o.l0_thresh < 1 || o.l0_thresh > d)) o.l0_thresh = 1;
   float tol_abs = o.tol;
   if (o.tol_is_relative) {
     std::vector<float> yh(m);
@@ -590,7 +591,7 @@ extern "C" gb_status gb_cs_generate_and_solve(const char *alg, int kind, int k, 
   GB_CUDA_TRY(cudaMemcpy(&st, w.st, sizeof(st), cudaMemcpyDeviceToHost));
   GB_CUDA_TRY(cudaMemcpy(x_out, w.x, sizeof(float) * n, cudaMemcpyDeviceToHost));
   std::vector<float> rec;
-  if (gb_is_l0(alg_id)) {
+  if (gb_is_ccs(alg_id)) {
     rec.resize((size_t)o.maxiter + 1);
     GB_CUDA_TRY(cudaMemcpy(rec.data(), w.rec, sizeof(float) * (o.maxiter + 1), cudaMemcpyDeviceToHost));
   }
@@ -611,7 +612,7 @@ extern "C" gb_status gb_cs_generate_and_solve(const char *alg, int kind, int k, 
     r->iter = st.iter;
     r->k_used = ks;
     r->stop_reason = st.stop_reason;
-    if (gb_is_l0(alg_id)) {
+    if (gb_is_ccs(alg_id)) {
       for (int j = 0; j < std::min(st.iter, 16); ++j) r->resid_prev[15 - j] = rec[st.iter - j];
       if (user_rec) memcpy(user_rec, rec.data(), sizeof(float) * (o.maxiter + 1));
     } else {

@@ -73,7 +73,10 @@ enum {
   C_CP_MU,        // CGIHTprojected: step mu for the active branch
   C_CP_BIN,       // CGIHTprojected: forced binning in the steepest-descent branch
   C_CP_BETA,      // CGIHTprojected: CG direction weight
-  C_CP_PROJ       // CGIHTprojected: projection fraction -> next branch
+  C_CP_PROJ,      // CGIHTprojected: projection fraction -> next branch
+  C_SMP_INIT,     // smp: err of the zero start, first loop test
+  C_SMP_HK,       // smp: H_k's fresh binning of the vector whose max is in red[R_XMAX]
+  C_SMP_STOP      // smp: residual history and stopping rules
 };
 
 static __device__ float max_list(const float *a, int n) {

@@ -147,6 +147,8 @@ void gb_set_error_message(const char *msg, const char *file, int line);
 inline bool gb_is_l0(int alg) {
   return alg == GB_ALG_PARALLEL_L0 || alg == GB_ALG_PARALLEL_LDDSR || alg == GB_ALG_PARALLEL_L0_SWIPE;
 }
+// the expander (CCS) decoders: smv only, unit values, a residual record
+inline bool gb_is_ccs(int alg) { return gb_is_l0(alg) || alg == GB_ALG_SMP; }
 
 // ---------------------------------------------------------------- device helpers
 // Dimension arguments of the solver kernels: a value >= 0 is used as is; a negative code

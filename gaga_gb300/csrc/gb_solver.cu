@@ -38,6 +38,60 @@ __global__ void k_ctrl_l0(GbState *st, int phase, float *rec, cudaGraphCondition
                    (st->l0_mode != 2 || st->l0_thresh > 0);
       set_cond(h, st->active ? 1u : 0u);
       break;
+    case C_SMP_INIT:
+      // smp.cu:45-66: res = y - A x^0, err, records
+      st->err = sqrt_red(st, R_RES);
+      st->err_start = st->err;
+      if (rec) rec[0] = st->err;
+      for (int j = 0; j < 16; ++j) { st->prev[j] = 0.0f; st->evol[j] = 1.0f; }
+      st->resid_diff = 1.0f;
+      st->active = (st->iter < st->maxiter) & (st->err > st->tol) & (st->err < 100.0f * st->err_start) &
+                   ((double)st->resid_diff > 0.01 * (double)st->tol) & (st->fail == 0);
+      set_cond(h, st->active ? 1u : 0u);
+      break;
+    case C_SMP_HK:
+      if (!st->active) break;
+      // H_k (expander/functions.cu:125-144): maxChange = 2 max, minVal 0, alpha 0.25,
+      // MaxBin = num_bins, a forced binning
+      st->max_value = (float)st->red[R_XMAX];
+      st->max_change = 2.0f * st->max_value;
+      st->slope = ((float)(st->num_bins - 1) / st->max_value);
+      st->min_val = 0.0f;
+      st->alpha_bin = 0.25f;
+      st->max_bin = st->num_bins;
+      st->flags[F_DOBIN] = 1;
+      break;
+    case C_SMP_STOP:
+      if (st->active) {
+        st->err = sqrt_red(st, R_RES);
+        for (int j = 0; j < 15; ++j) { st->prev[j] = st->prev[j + 1]; st->evol[j] = st->evol[j + 1]; }
+        st->prev[15] = st->err;
+        st->evol[15] = st->prev[14] - st->prev[15];
+        st->resid_diff = max_list(st->evol, 16);
+        if (st->iter > (int)(0.4 * st->maxiter)) {
+          float rate = powf(st->prev[15] / st->prev[0], 1.0f / 15.0f);
+          if (rate > 0.999f) st->fail = 1;
+        }
+        st->iter++;
+        st->passes++;
+        if (rec) rec[st->iter] = st->err;
+        const int go = (st->iter < st->maxiter) & (st->err > st->tol) & (st->err < 100.0f * st->err_start) &
+                       ((double)st->resid_diff > 0.01 * (double)st->tol) & (st->fail == 0);
+        if (!go) {
+          if (!(st->err > st->tol)) st->stop_reason = 1;
+          else if (!(st->iter < st->maxiter)) st->stop_reason = 2;
+          else if (!(st->err < 100.0f * st->err_start)) st->stop_reason = 3;
+          else if (!((double)st->resid_diff > 0.01 * (double)st->tol)) st->stop_reason = 4;
+          else st->stop_reason = 6;
+        }
+        st->active = go;
+        if (st->passes > st->pass_limit && st->active) {
+          st->active = 0;
+          st->status = GB_WATCHDOG;
+        }
+      }
+      set_cond(h, st->active ? 1u : 0u);
+      break;
     case C_L0_PRE:
       if (!st->active) break;
       st->l0_offset = st->iter % st->d;
@@ -424,6 +478,85 @@ __global__ void k_l0_scores(GbState *st, const float *__restrict__ res, float *_
   if (__syncthreads_or(found) && threadIdx.x == 0) st->found = 1;
 }
 
+// cuda_compute_scores_smp (GAGA/gaga/expander/kernels.cu:79-104): u_j = median of the
+// residual over column j's d rows (d <= 32)
+__global__ void k_smp_scores(const GbState *st, const float *__restrict__ res, const int *__restrict__ rows, int n,
+                             int d, float *__restrict__ u) {
+  if (!st->active) return;
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    float b[32];
+    for (int i = 0; i < d; ++i) b[i] = res[rows[(size_t)j * d + i]];
+    for (int i = 0; i < d; ++i)
+      for (int q = 0; q < d - 1; ++q)
+        if (b[q] > b[q + 1]) {
+          const float t = b[q + 1];
+          b[q + 1] = b[q];
+          b[q] = t;
+        }
+    u[j] = (d % 2) == 0 ? (b[d / 2 - 1] + b[d / 2]) / 2 : b[(d - 1) / 2];
+  }
+}
+
+// ThresholdK (GAGA/gaga/expander/functions.cu:103-123): after Threshold, per-tile counts of
+// the support and of the entries in the k-th bin (second half of tile_cnt)
+__global__ void __launch_bounds__(256) k_hk_count(const GbState *st, const float *__restrict__ v,
+                                                  const int *__restrict__ bins, int n, int *__restrict__ tile_cnt) {
+  if (!st->active) return;
+  __shared__ float sm[32];
+  const int kb = st->k_bin, base = blockIdx.x * GB_TILE;
+  float nz = 0.0f, kc = 0.0f;
+  for (int q = threadIdx.x; q < GB_TILE; q += blockDim.x) {
+    const int i = base + q;
+    if (i < n) {
+      nz += v[i] != 0.0f ? 1.0f : 0.0f;
+      kc += bins[i] == kb ? 1.0f : 0.0f;
+    }
+  }
+  nz = block_reduce<0>(nz, sm);
+  if (threadIdx.x == 0) tile_cnt[blockIdx.x] = (int)nz;
+  kc = block_reduce<0>(kc, sm);
+  if (threadIdx.x == 0) tile_cnt[gridDim.x + blockIdx.x] = (int)kc;
+}
+
+// ... then the first (support - K) entries of the k-th bin, in index order, are zeroed
+// (the reference takes them in atomic order)
+__global__ void __launch_bounds__(256) k_hk_trim(const GbState *st, float *__restrict__ v, const int *__restrict__ bins,
+                                                 int n, const int *__restrict__ tile_cnt, int K) {
+  if (!st->active) return;
+  __shared__ int s_off, s_before;
+  __shared__ int warp_cnt[8];
+  if (threadIdx.x == 0) {
+    int tot = 0, before = 0;
+    for (int t = 0; t < (int)gridDim.x; ++t) {
+      tot += tile_cnt[t];
+      if (t < (int)blockIdx.x) before += tile_cnt[gridDim.x + t];
+    }
+    s_off = tot - K;
+    s_before = before;
+  }
+  __syncthreads();
+  const int offset = s_off;
+  if (offset <= 0 || s_before >= offset) return;  // uniform over the block
+  const int kb = st->k_bin, base = blockIdx.x * GB_TILE;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int running = s_before;
+  for (int q0 = 0; q0 < GB_TILE; q0 += blockDim.x) {
+    const int i = base + q0 + threadIdx.x;
+    const bool in = i < n && bins[i] == kb;
+    const unsigned bal = __ballot_sync(0xffffffffu, in);
+    if (lane == 0) warp_cnt[wid] = __popc(bal);
+    __syncthreads();
+    int wb = 0, tot = 0;
+    for (int w2 = 0; w2 < 8; ++w2) {
+      if (w2 < wid) wb += warp_cnt[w2];
+      tot += warp_cnt[w2];
+    }
+    if (in && running + wb + __popc(bal & ((1u << lane) - 1u)) < offset) v[i] = 0.0f;
+    running += tot;
+    __syncthreads();
+  }
+}
+
 // cuda_update_residual (GAGA/gaga/expander/kernels.cu:3-14) as a row gather over the CSR
 // copy: each row applies its accepted updates in ascending column order; ||res||^2
 __global__ void k_l0_update(GbState *st, float *__restrict__ res, const int *__restrict__ ptr,
@@ -659,12 +792,47 @@ static void enq_cgproj_body(SolvePlan &P, cudaStream_t s, cudaGraphConditionalHa
   enq_ctrl(w, s, C_CP_PROJ, h_outer);
 }
 
+// H_K of the expander decoders on v: a fresh binning, Threshold, ThresholdK
+static void enq_expander_hk(SolvePlan &P, cudaStream_t s, float *v, int K) {
+  GbWork &w = *P.w;
+  const int n = argN(w);
+  k_copy_norm<<<w.red_blocks, 256, 0, s>>>(w.st, F_ALWAYS, v, nullptr, n, -1, R_XMAX, w.red_part, w.tickets);
+  k_ctrl_l0<<<1, 32, 0, s>>>(w.st, C_SMP_HK, w.rec, 0);
+  cudaMemsetAsync(w.counters, 0, sizeof(int) * P.num_bins, s);
+  k_hist<<<w.red_blocks, 256, 0, s>>>(w.st, F_DOBIN, v, w.bins, nullptr, w.counters, n);
+  k_kbin<<<1, 1024, 0, s>>>(w.st, F_DOBIN, w.counters, K);
+  k_threshold<<<w.red_blocks, 256, 0, s>>>(w.st, F_ALWAYS, v, w.bins, n);
+  const int tiles = (n + GB_TILE - 1) / GB_TILE;
+  k_hk_count<<<tiles, 256, 0, s>>>(w.st, v, w.bins, n, w.tile_cnt);
+  k_hk_trim<<<tiles, 256, 0, s>>>(w.st, v, w.bins, n, w.tile_cnt, K);
+}
+
+// smp loop (GAGA/gaga/expander/smp.cu:67-131)
+static void enq_smp_body(SolvePlan &P, cudaStream_t s, cudaGraphConditionalHandle h_outer) {
+  GbWork &w = *P.w;
+  const int n = argN(w);
+  int blocks = (n + 255) / 256;
+  if (blocks > w.num_sms * 16) blocks = w.num_sms * 16;
+  k_smp_scores<<<blocks, 256, 0, s>>>(w.st, w.resid, w.op.smv_rows, n, w.op.d, w.grad);
+  enq_expander_hk(P, s, w.grad, 2 * P.k);
+  lin(w, s, F_ALWAYS, w.x, w.x, SC_ONE, w.grad, n);
+  enq_expander_hk(P, s, w.x, P.k);
+  enq_A(w, s, w.x, w.resid, w.y, R_RES, F_ALWAYS);
+  k_ctrl_l0<<<1, 32, 0, s>>>(w.st, C_SMP_STOP, w.rec, h_outer);
+}
+
 // The solve as pieces: prologue, loop body (with the HTP inner CG loop), run either as one
 // graph with WHILE nodes or eagerly (GB_CS_EAGER=1: same kernels, host-checked loops;
 // used for profiling, since kernels inside conditional graphs cannot be profiled).
 void enq_prologue(SolvePlan &P, cudaStream_t s0, cudaGraphConditionalHandle h_outer) {
   GbWork &w = *P.w;
   const int n = argN(w), m = argM(w), k = P.k, num_bins = w.dyn ? D_NBINS : P.num_bins;
+  if (P.alg == GB_ALG_SMP) {
+    // res = y - A x^0 (smp.cu:45-48)
+    enq_A(w, s0, w.x, w.resid, w.y, R_RES, F_ALWAYS);
+    k_ctrl_l0<<<1, 32, 0, s0>>>(w.st, C_SMP_INIT, w.rec, h_outer);
+    return;
+  }
   if (gb_is_l0(P.alg)) {
     // res = y - A x with x = 0 (computeResidual, GAGA/gaga/expander/functions.cu:73-79)
     enq_A(w, s0, w.x, w.resid, w.y, R_RES, F_ALWAYS);
@@ -775,6 +943,10 @@ void enq_body(SolvePlan &P, cudaStream_t s1, cudaGraphConditionalHandle h_outer)
   }
   if (P.alg == GB_ALG_FIHT || P.alg == GB_ALG_ALPS) {
     enq_fiht_body(P, s1, h_outer);
+    return;
+  }
+  if (P.alg == GB_ALG_SMP) {
+    enq_smp_body(P, s1, h_outer);
     return;
   }
   if (P.alg == GB_ALG_CGIHT_PROJ) {
@@ -1030,6 +1202,7 @@ static GbState initial_state(const GbWork &w, int alg, const gb_options &o, int 
 // Runs one solve on the prepared workspace (x zero, y uploaded); results stay in GbState.
 gb_status gb_run_solver(GbWork &w, int alg, const gb_options &o, int k, cudaStream_t s, float tol_abs) {
   if (gb_is_l0(alg) && (w.op.d <= 0 || 2 * w.op.d > 64)) return GB_UNSUPPORTED;
+  if (alg == GB_ALG_SMP && (w.op.d <= 0 || w.op.d > 32)) return GB_UNSUPPORTED;
   GbState init = initial_state(w, alg, o, k, tol_abs);
   k_init_state<<<1, 1, 0, s>>>(w.st, init);
   GB_CUDA_TRY(cudaGetLastError());

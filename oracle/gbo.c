@@ -1155,6 +1155,94 @@ int gbo_parallel_l0(const gbo_op *op, const float *y, const gbo_opts *o, float *
   return 0;
 }
 
+/* H_k of the expander decoders (GAGA/gaga/expander/functions.cu:103-144): a fresh binning
+ * (alpha 0.25, MaxBin = num_bins, minVal 0, maxChange = 2 max|v|), Threshold, then
+ * ThresholdK trims the support to exactly K entries by zeroing entries of the k-th bin.
+ * The reference picks those entries by atomic order; here they are the first ones in
+ * index order. */
+static int expander_hk(float *v, int K, int n, int num_bins, int *bins, int *counters) {
+  float mx = gbo_max_magnitude(v, n);
+  float slope = ((float)(num_bins - 1) / mx);
+  gbo_bin_state bs;
+  bs.num_bins = num_bins;
+  bs.alpha = 0.25f;
+  bs.max_bin = num_bins;
+  bs.min_val = 0.0f;
+  bs.k_bin = 0;
+  bs.sum = 0;
+  int sum = gbo_find_support_set(v, bins, counters, slope, mx, 2.0f * mx, &bs, n, K);
+  gbo_threshold(v, bins, bs.k_bin, n);
+  int supp = 0;
+  for (int i = 0; i < n; ++i) supp += v[i] != 0.0f;
+  int offset = supp - K;
+  for (int i = 0; i < n && offset > 0; ++i)
+    if (bins[i] == bs.k_bin) {
+      v[i] = 0.0f;
+      offset--;
+    }
+  return sum;
+}
+
+/* cuda_compute_scores_smp (GAGA/gaga/expander/kernels.cu:79-104): the median of the
+ * residual over each column's d rows */
+static void smp_scores(const float *res, const int *rows, int n, int d, float *u) {
+  float buf[64];
+  for (int j = 0; j < n; ++j) {
+    for (int i = 0; i < d; ++i) buf[i] = res[rows[(size_t)j * d + i]];
+    for (int i = 0; i < d; ++i)
+      for (int q = 0; q < d - 1; ++q)
+        if (buf[q] > buf[q + 1]) {
+          float t = buf[q + 1];
+          buf[q + 1] = buf[q];
+          buf[q] = t;
+        }
+    u[j] = (d % 2) == 0 ? (buf[d / 2 - 1] + buf[d / 2]) / 2 : buf[(d - 1) / 2];
+  }
+}
+
+int gbo_smp(const gbo_op *op, const float *y, int k, const gbo_opts *o, float *x, float *res, float *res_record,
+            gbo_info *info) {
+  int m = op->m, n = op->n, d = op->d;
+  float *ax = (float *)malloc(sizeof(float) * m);
+  float *u = (float *)calloc((size_t)n, sizeof(float));
+  int *bins = (int *)calloc((size_t)n, sizeof(int));
+  int *counters = (int *)calloc((size_t)o->num_bins, sizeof(int));
+  gbo_A(op, x, ax);
+  for (int i = 0; i < m; ++i) res[i] = fmaf(-1.0f, ax[i], y[i]);
+  float err = nrm2f(res, m), err_start = err;
+  if (res_record) res_record[0] = err;
+  float prev[16], evol[16], diff = 1.0f;
+  for (int i = 0; i < 16; ++i) { prev[i] = 0.0f; evol[i] = 1.0f; }
+  int iter = 0, fail = 0;
+  while ((iter < o->maxiter) & (err > o->tol) & (err < (100.0f * err_start)) & ((double)diff > 0.01 * (double)o->tol) &
+         (fail == 0)) {
+    smp_scores(res, op->smv_rows, n, d, u);
+    expander_hk(u, 2 * k, n, o->num_bins, bins, counters);
+    saxpy(n, 1.0f, u, x);
+    expander_hk(x, k, n, o->num_bins, bins, counters);
+    gbo_A(op, x, ax);
+    for (int i = 0; i < m; ++i) res[i] = fmaf(-1.0f, ax[i], y[i]);
+    err = nrm2f(res, m);
+    push16(prev, err);
+    for (int i = 0; i < 15; ++i) evol[i] = evol[i + 1];
+    evol[15] = prev[14] - prev[15];
+    diff = max_list(evol, 16);
+    if (iter > ((int)(0.4 * o->maxiter))) {
+      float rate = powf(prev[15] / prev[0], 1.0f / 15.0f);
+      if (rate > 0.999f) fail = 1;
+    }
+    iter = iter + 1;
+    if (res_record) res_record[iter] = err;
+  }
+  if (info) {
+    memset(info, 0, sizeof(*info));
+    info->iter = iter;
+    memcpy(info->resid_prev, prev, sizeof(prev));
+  }
+  free(ax); free(u); free(bins); free(counters);
+  return 0;
+}
+
 /* serial_l0 (GAGA/gaga/expander/serial_l0.cu:16-161): Gauss-Seidel, the residual is
  * updated as soon as a column is accepted.  res must hold y - A x on entry. */
 int gbo_serial_l0(const gbo_op *op, const float *y, const gbo_opts *o, float *x, float *res,

@@ -38,7 +38,7 @@ extern "C" {
 
 /* algorithm ids (reference alg switch, GAGA/gaga/gaga_gen.cu:619-631, gaga_smv.cu:841-857) */
 enum { GBO_NIHT = 0, GBO_HTP = 1, GBO_IHT = 2, GBO_HT_SD = 3, GBO_HT_CG = 4, GBO_CSMPSP = 5, GBO_CGIHT = 6,
-       GBO_FIHT = 7, GBO_ALPS = 8, GBO_CGIHT_PROJ = 9, GBO_PARALLEL_LDDSR = 13, GBO_PARALLEL_L0 = 14,
+       GBO_FIHT = 7, GBO_ALPS = 8, GBO_CGIHT_PROJ = 9, GBO_SMP = 10, GBO_PARALLEL_LDDSR = 13, GBO_PARALLEL_L0 = 14,
        GBO_SERIAL_L0 = 15, GBO_PARALLEL_L0_SWIPE = 18 };
 /* operator kinds */
 enum { GBO_OP_DENSE = 0, GBO_OP_DCT = 1, GBO_OP_SMV = 2 };
@@ -111,6 +111,9 @@ void gbo_threshold(float *v, const int *bins, int k_bin, int n);
 float gbo_max_magnitude(const float *v, int n);
 
 /* ---------------- solvers ---------------- */
+/* smp (GAGA/gaga/expander/smp.cu); res_record as for parallel_l0 */
+int gbo_smp(const gbo_op *op, const float *y, int k, const gbo_opts *o, float *x, float *res, float *res_record,
+            gbo_info *info);
 int gbo_solve(const gbo_op *op, const float *y, int k, const gbo_opts *o, float *x, gbo_info *info);
 /* parallel_l0 / serial_l0 write res_record (maxiter+1 entries, may be NULL) */
 int gbo_parallel_l0(const gbo_op *op, const float *y, const gbo_opts *o, float *x, float *res,

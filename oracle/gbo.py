@@ -8,7 +8,7 @@ from . import build as _build
 
 NIHT, HTP, IHT, HT_SD, HT_CG, CSMPSP, CGIHT, FIHT, ALPS, CGIHT_PROJ, PARALLEL_L0, SERIAL_L0 = (0, 1, 2, 3, 4, 5, 6, 7, 8,
                                                                                         9, 14, 15)
-PARALLEL_LDDSR, PARALLEL_L0_SWIPE = 13, 18
+PARALLEL_LDDSR, PARALLEL_L0_SWIPE, SMP = 13, 18, 10
 OP_DENSE, OP_DCT, OP_SMV = 0, 1, 2
 ALG_IDS = {"NIHT": NIHT, "HTP": HTP, "IHT": IHT, "ThresholdSD": HT_SD, "ThresholdCG": HT_CG, "CSMPSP": CSMPSP,
            "CGIHT": CGIHT, "FIHT": FIHT, "ALPS": ALPS, "CGIHTprojected": CGIHT_PROJ,
@@ -69,6 +69,7 @@ def _declare(L):
         "gbo_solve": (i, [vp, vp, i, vp, vp, vp]),
         "gbo_parallel_l0": (i, [vp, vp, vp, vp, vp, vp, vp]),
         "gbo_serial_l0": (i, [vp, vp, vp, vp, vp, vp, vp]),
+        "gbo_smp": (i, [vp, vp, i, vp, vp, vp, vp, vp]),
         "gbo_l0_scores": (None, [vp, vp, vp, vp, i, i, i, i, vp]),
         "gbo_l0_update_residual": (None, [vp, vp, vp, i, i]),
         "gbo_results": (None, [vp, vp, i, i, vp, vp]),
@@ -216,6 +217,18 @@ def solve(alg, op, y, k, tol, maxiter=None, num_bins=None, restart=0, threads=0,
     info = GboInfo()
     lib().gbo_solve(C.byref(op.c), _p(y), k, C.byref(o), _p(x), C.byref(info))
     return x, info
+
+
+def smp(op, y, k, tol, maxiter, num_bins=None):
+    """Sparse matching pursuit (smp) on an expander operator."""
+    y = f32(y)
+    x = np.zeros(op.n, dtype=np.float32)
+    res = np.zeros(op.m, dtype=np.float32)
+    rec = np.zeros(maxiter + 1, dtype=np.float32)
+    o = GboOpts(SMP, tol, maxiter, num_bins or default_num_bins(op.n), 0, 1, 0)
+    info = GboInfo()
+    lib().gbo_smp(C.byref(op.c), _p(y), int(k), C.byref(o), _p(x), _p(res), _p(rec), C.byref(info))
+    return x, res, rec, info
 
 
 def parallel_l0(op, y, tol, maxiter, l0_thresh=1, variant="parallel_l0"):

@@ -103,3 +103,24 @@ def test_l0_variants_bit_exact(gb, gbo, variant, n, m):
     assert iters == info.iter
     assert np.array_equal(np.asarray(x), xo)
     assert np.array_equal(np.asarray(rec)[: iters + 1], reco[: iters + 1])
+
+
+@pytest.mark.parametrize("n,m,k", [(2 ** 14, 2 ** 12, 40), (2 ** 14, 2 ** 12, 204), (2 ** 18, 2 ** 16, 300)])
+def test_smp_bit_exact(gb, gbo, n, m, k):
+    """smp on the unit-valued expander with a +-1 signal: medians, binning and residuals are
+    exact in FP32, so x, the iteration count and the residual record equal the oracle's
+    (with the exact-K trim in index order on both sides)."""
+    d = 7
+    rows, vals = gbo.gen_smv(m, n, d, 3, seed=29)
+    x0, ks = gbo.gen_vector(n, k, 1, seed=29)
+    op = gbo.Op.smv(m, n, d, rows, vals)
+    y = gbo.A(op, x0)
+    cols = np.repeat(np.arange(n, dtype=np.int32), d)
+    opts = gb.gaga_options("tol", 1e-6, "maxiter", 300)
+    x, iters, conv, rec, trec = gb.gaga_cs("smp", "smv", y, rows, cols, vals, ks, opts, index_base=0)
+    xo, reso, reco, info = gbo.smp(op, y, ks, 1e-6, 300)
+    assert iters == info.iter
+    assert np.array_equal(np.asarray(x), xo)
+    assert np.array_equal(np.asarray(rec)[: iters + 1], reco[: iters + 1])
+    if k == 40:
+        assert np.array_equal(xo, x0)
