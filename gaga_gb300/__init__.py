@@ -101,6 +101,35 @@ def _options(alg, n, opts, ens):
     return o
 
 
+_last_timings = None
+
+
+def _attach_timing(alg, o, r):
+    """Timing variants (timing 'on', NIHT / HTP): per-iteration buffers for the result."""
+    global _last_timings
+    _last_timings = None
+    if not o.timing or o.maxiter <= 0 or alg not in ("NIHT", "HTP"):
+        return None
+    bufs = {name: np.zeros(o.maxiter, dtype=np.float32)
+            for name in ("time_per_iteration", "time_supp_set", "cg_per_iteration", "time_for_cg")}
+    for name, b in bufs.items():
+        setattr(r, name, b.ctypes.data)
+    return bufs
+
+
+def _keep_timing(bufs, r):
+    global _last_timings
+    if bufs is not None and (r.time_per_iteration or 0):
+        _last_timings = {name: b[: r.iter].copy() for name, b in bufs.items()}
+
+
+def last_timings():
+    """Per-iteration times (ms) of the last solve run with timing 'on' (NIHT or HTP):
+    time_per_iteration, time_supp_set, cg_per_iteration, time_for_cg (the arrays the
+    reference's timing variants record, GAGA/gaga/algorithms_timings.cu), or None."""
+    return _last_timings
+
+
 def _is_device(a):
     return hasattr(a, "data_ptr") and getattr(a, "is_cuda", False)
 
@@ -157,7 +186,9 @@ def _solve(alg, kind, y, k, m, n, opts, ens, A=None, lda=0, rows=None, cols=None
     if want_record:
         rec = np.zeros(o.maxiter + 1, dtype=np.float32)
         r.res_record = rec.ctypes.data
+    tb = _attach_timing(alg, o, r)
     _lib.check(L.gb_cs_solve(alg.encode(), C.byref(p), C.byref(o), C.c_void_p(xptr), C.byref(r)))
+    _keep_timing(tb, r)
     return x, r, rec
 
 
@@ -229,8 +260,10 @@ def _generate(alg, kind, k, m, n, d, opts, ens):
     rec = np.zeros(o.maxiter + 1, dtype=np.float32) if kind == _lib.GB_OP_SMV else None
     if rec is not None:
         r.res_record = rec.ctypes.data
+    tb = _attach_timing(alg, o, r)
     _lib.check(L.gb_cs_generate_and_solve(alg.encode(), kind, int(k), int(m), int(n), int(d), C.byref(o),
                                           C.c_void_p(x.ctypes.data), C.c_void_p(xt.ctypes.data), C.byref(r)))
+    _keep_timing(tb, r)
     norms = np.array(r.norms, dtype=np.float32)
     times = np.array(r.times, dtype=np.float32)
     support = np.array(r.support, dtype=np.int32)
@@ -248,8 +281,10 @@ def generate_and_solve(alg, ens, k, m, n, d=0, opts=None):
     x = np.zeros(n, dtype=np.float32)
     xt = np.zeros(n, dtype=np.float32)
     r = _lib.Result()
+    tb = _attach_timing(alg, o, r)
     _lib.check(L.gb_cs_generate_and_solve(alg.encode(), kind, int(k), int(m), int(n), int(d), C.byref(o),
                                           C.c_void_p(x.ctypes.data), C.c_void_p(xt.ctypes.data), C.byref(r)))
+    _keep_timing(tb, r)
     return x, xt, r
 
 

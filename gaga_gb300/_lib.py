@@ -20,7 +20,7 @@ GB_ALG_FIHT, GB_ALG_ALPS, GB_ALG_CGIHT_PROJ, GB_ALG_PARALLEL_L0 = 7, 8, 9, 14
 
 # every symbol include/gb_cs.h declares
 EXPORTS = ["gb_cs_version", "gb_cs_last_error", "gb_cs_default_options", "gb_cs_alg_id", "gb_cs_solve",
-           "gb_cs_generate_and_solve", "gb_cs_linear_binning", "gb_cs_find_support_set",
+           "gb_cs_generate_and_solve", "gb_cs_linear_binning", "gb_cs_find_support_set", "gb_cs_find_support_set_sort",
            "gb_cs_operator_apply", "gb_cs_l0_step", "gb_cs_solve_batch", "gb_cs_batch_last_stats",
            "gb_cs_dense_apply_noalloc", "gb_cs_solve_shared_batch", "gb_cs_shared_last_stats",
            "gb_cs_gemm_bf16_tn", "gb_cs_mlp_num_params", "gb_cs_mlp_features", "gb_cs_mlp_forward",
@@ -46,7 +46,9 @@ class Problem(C.Structure):
 class Result(C.Structure):
     _fields_ = [("iter", C.c_int), ("conv_rate", C.c_float), ("norms", C.c_float * 3), ("times", C.c_float * 3),
                 ("support", C.c_int * 4), ("k_used", C.c_int), ("resid_prev", C.c_float * 16),
-                ("stop_reason", C.c_int), ("res_record", C.c_void_p), ("warm_start", C.c_int)]
+                ("stop_reason", C.c_int), ("res_record", C.c_void_p), ("warm_start", C.c_int),
+                ("time_per_iteration", C.c_void_p), ("time_supp_set", C.c_void_p),
+                ("cg_per_iteration", C.c_void_p), ("time_for_cg", C.c_void_p)]
 
 
 class BinState(C.Structure):
@@ -94,6 +96,8 @@ def load():
     L.gb_cs_linear_binning.restype = i
     L.gb_cs_find_support_set.argtypes = [vp, i, i, f, f, f, C.POINTER(BinState), vp, vp, i, vp]
     L.gb_cs_find_support_set.restype = i
+    L.gb_cs_find_support_set_sort.argtypes = [vp, vp, i, i, f, f, C.POINTER(C.c_float), vp]
+    L.gb_cs_find_support_set_sort.restype = i
     L.gb_cs_operator_apply.argtypes = [C.POINTER(Problem), i, vp, vp]
     L.gb_cs_operator_apply.restype = i
     L.gb_cs_l0_step.argtypes = [vp, vp, vp, vp, i, i, i, i, i, C.POINTER(C.c_int), vp]

@@ -150,6 +150,7 @@ gb_status alloc_work(DeviceBuffers &db, GbWork &w, int m, int n, int lda, int nu
   GB_TRY(db.alloc(&w.S, n));
   GB_TRY(db.alloc(&w.tile_cnt, 2 * ((n + GB_TILE - 1) / GB_TILE)));  // second half: smp's k-th bin counts
   GB_TRY(db.alloc(&w.rec, (size_t)maxiter + 2));
+  GB_TRY(db.alloc(&w.sel_hist, (size_t)3 * GB_SEL_BINS));  // zeroed; the select keeps it zero
   gb_dense_av_shape(m, w.num_sms, &w.av_ntile, &w.av_nsplit);
   w.part_cap = gb_dense_part_floats_av(w.av_ntile, w.av_nsplit);
   GB_TRY(db.alloc(&w.av_tickets, w.av_ntile));
@@ -291,9 +292,77 @@ float conv_rate_from(const float *prev, int iter, int conv_num) {
 
 gb_status check_options(const gb_options &o) {
   if (o.maxiter < 0) return bad("maxiter must be >= 0");
+  if (o.timing && (o.support_flag < 0 || o.support_flag > 3)) return bad("supportFlag must be 0, 1, 2 or 3");
+  if (o.timing && !(o.alpha >= 0.0f && o.alpha < 1.0f)) return bad("alpha must be in [0, 1)");
   if (o.num_bins < 1) return bad("numBins must be >= 1");
   if (o.conv_rate_num != 16) return bad("convRateNum other than 16 is not supported", GB_UNSUPPORTED);
   return GB_OK;
+}
+
+bool timing_applies(const gb_options &o, int alg_id) {
+  return o.timing && (alg_id == GB_ALG_NIHT || alg_id == GB_ALG_HTP);
+}
+
+// stamp buffers of the timing variants
+gb_status alloc_timing(DeviceBuffers &db, GbWork &w, const gb_options &o, int alg_id) {
+  if (!timing_applies(o, alg_id) || o.maxiter <= 0) return GB_OK;
+  GB_TRY(db.alloc(&w.tstamp, (size_t)o.maxiter * GB_NSTAMP));
+  GB_TRY(db.alloc(&w.tcg, (size_t)o.maxiter));
+  return GB_OK;
+}
+
+// Per-iteration times (ms) of a timing-variant solve from its stamps: iteration, support
+// identification, CG steps and CG time (HTP).  Returns their sum over iterations (time_sum,
+// algorithms_timings.cu:641).
+struct TimingRecord {
+  std::vector<float> iter_ms, supp_ms, cg_steps, cg_ms;
+  float sum = 0.0f;
+};
+gb_status collect_timing(const GbWork &w, int iters, TimingRecord *t) {
+  const int n = std::max(iters, 0);
+  std::vector<unsigned long long> ts((size_t)n * GB_NSTAMP);
+  std::vector<int> cg((size_t)n);
+  if (n > 0) {
+    GB_CUDA_TRY(cudaMemcpy(ts.data(), w.tstamp, sizeof(unsigned long long) * ts.size(), cudaMemcpyDeviceToHost));
+    GB_CUDA_TRY(cudaMemcpy(cg.data(), w.tcg, sizeof(int) * cg.size(), cudaMemcpyDeviceToHost));
+  }
+  t->iter_ms.assign(n, 0.0f);
+  t->supp_ms.assign(n, 0.0f);
+  t->cg_steps.assign(n, 0.0f);
+  t->cg_ms.assign(n, 0.0f);
+  t->sum = 0.0f;
+  auto ms = [](unsigned long long a, unsigned long long b) { return b >= a ? (float)((double)(b - a) * 1e-6) : 0.0f; };
+  for (int j = 0; j < n; ++j) {
+    const unsigned long long *q = &ts[(size_t)j * GB_NSTAMP];
+    t->iter_ms[j] = ms(q[0], q[5]);
+    t->supp_ms[j] = ms(q[1], q[2]);
+    t->cg_ms[j] = ms(q[3], q[4]);
+    t->cg_steps[j] = (float)cg[j];
+    t->sum += t->iter_ms[j];
+  }
+  return GB_OK;
+}
+
+void put_timing(const TimingRecord &t, gb_result *r, int iters) {
+  const size_t bytes = sizeof(float) * (size_t)std::max(iters, 0);
+  if (r->time_per_iteration) memcpy(r->time_per_iteration, t.iter_ms.data(), bytes);
+  if (r->time_supp_set) memcpy(r->time_supp_set, t.supp_ms.data(), bytes);
+  if (r->cg_per_iteration) memcpy(r->cg_per_iteration, t.cg_steps.data(), bytes);
+  if (r->time_for_cg) memcpy(r->time_for_cg, t.cg_ms.data(), bytes);
+  // h_times[1] = time_sum / iter (GAGA/gaga/results.cu:1430)
+  r->times[1] = iters > 0 ? t.sum / (float)iters : 0.0f;
+}
+
+// a result's caller-owned pointers survive its reset
+void reset_result(gb_result *r) {
+  float *rec = r->res_record, *a = r->time_per_iteration, *b = r->time_supp_set, *c = r->cg_per_iteration,
+        *d = r->time_for_cg;
+  memset(r, 0, sizeof(*r));
+  r->res_record = rec;
+  r->time_per_iteration = a;
+  r->time_supp_set = b;
+  r->cg_per_iteration = c;
+  r->time_for_cg = d;
 }
 
 }  // namespace
@@ -325,6 +394,7 @@ extern "C" gb_status gb_cs_solve(const char *alg, const gb_problem *p, const gb_
     GB_TRY(db.alloc(&w.ml_counts, gb_ml_rank_bins()));
     GB_TRY(db.alloc(&w.ml_cum, gb_ml_rank_bins()));
   }
+  GB_TRY(alloc_timing(db, w, o, alg_id));
   float tol_abs = o.tol;
   if (o.tol_is_relative) {
     std::vector<float> yh(p->m);
@@ -370,14 +440,18 @@ extern "C" gb_status gb_cs_solve(const char *alg, const gb_problem *p, const gb_
   cudaEventDestroy(e1);
   if (r) {
     float *user_rec = r->res_record;
-    memset(r, 0, sizeof(*r));
-    r->res_record = user_rec;
+    reset_result(r);
     r->iter = st.iter + warm_iters;
     r->stop_reason = st.stop_reason;
     r->warm_start = warm;
     r->times[0] = ms;
     r->times[1] = st.iter > 0 ? ms / st.iter : 0.0f;
     r->times[2] = ms;
+    if (w.tstamp) {
+      TimingRecord t;
+      GB_TRY(collect_timing(w, st.iter, &t));
+      put_timing(t, r, st.iter);
+    }
     if (gb_is_ccs(alg_id)) {
       // the last <= 16 residual records become residNorm_prev (gaga_smv.cu:1013-1020)
       for (int j = 0; j < std::min(st.iter, 16); ++j) r->resid_prev[15 - j] = rec[st.iter - j];
@@ -546,6 +620,7 @@ extern "C" gb_status gb_cs_generate_and_solve(const char *alg, int kind, int k, 
   GbWork w;
   memset(&w, 0, sizeof(w));
   GB_TRY(setup_problem(db, w, p, 0, o.num_bins, o.maxiter, false));
+  GB_TRY(alloc_timing(db, w, o, alg_id));
   // y = A x (createMeasurements_*), then optional noise (createProblem_gen.cu:244-254)
   float *dxt = nullptr;
   GB_TRY(db.alloc(&dxt, n, false));
@@ -605,10 +680,11 @@ extern "C" gb_status gb_cs_generate_and_solve(const char *alg, int kind, int k, 
   gb_result local_r;
   memset(&local_r, 0, sizeof(local_r));
   if (!r && o.results_dir) r = &local_r;
+  TimingRecord trec;
+  if (w.tstamp) GB_TRY(collect_timing(w, st.iter, &trec));
   if (r) {
     float *user_rec = r->res_record;
-    memset(r, 0, sizeof(*r));
-    r->res_record = user_rec;
+    reset_result(r);
     r->iter = st.iter;
     r->k_used = ks;
     r->stop_reason = st.stop_reason;
@@ -647,12 +723,21 @@ extern "C" gb_status gb_cs_generate_and_solve(const char *alg, int kind, int k, 
     r->times[0] = ms_alg;
     r->times[1] = st.iter > 0 ? ms_alg / st.iter : 0.0f;
     r->times[2] = ms_tot;
+    if (w.tstamp) put_timing(trec, r, st.iter);
   }
   if (st.status == GB_WATCHDOG) return bad("device iteration bound reached", GB_WATCHDOG);
   if (o.results_dir) {
     gb_options ow = o;
     ow.seed = seed;  // the seed of the drawn problem (kFixed may have advanced it)
-    GB_TRY(gb_cs_write_result(o.results_dir, alg, kind, k, m, n, d, &ow, r, nullptr, 0));
+    gb_result rw = *r;
+    if (w.tstamp) {
+      // the timing file lists every iteration's times (File_output_timings*)
+      rw.time_per_iteration = trec.iter_ms.data();
+      rw.time_supp_set = trec.supp_ms.data();
+      rw.cg_per_iteration = trec.cg_steps.data();
+      rw.time_for_cg = trec.cg_ms.data();
+    }
+    GB_TRY(gb_cs_write_result(o.results_dir, alg, kind, k, m, n, d, &ow, &rw, nullptr, 0));
   }
   return GB_OK;
 }
@@ -667,6 +752,55 @@ extern "C" gb_status gb_cs_write_result(const char *dir, const char *alg, int ki
   localtime_r(&raw, &tmv);
   const char *tag = kind == GB_OP_DENSE ? "gen" : kind == GB_OP_DCT ? "dct" : "smv";
   char fname[160];
+  const int alg_id = gb_cs_alg_id(alg);
+  if (o->timing && (alg_id == GB_ALG_NIHT || alg_id == GB_ALG_HTP)) {
+    // results_timings* (GAGA/gaga/results.cu:1195-1210, 1365-1380, 1535-1550 and the HTP
+    // forms 1705-1720, 1880-1895, 2050-2065): gpu_timings[_HTP]_data_<kind><date>.txt with the
+    // File_output_timings* lines (functions.cu:82-208), one line per iteration after the summary
+    const bool htp = alg_id == GB_ALG_HTP;
+    if (r->iter > 0 && (!r->time_per_iteration || !r->time_supp_set || (htp && (!r->cg_per_iteration || !r->time_for_cg))))
+      return bad("the timing results need the per-iteration time arrays");
+    snprintf(fname, sizeof(fname), "gpu_timings_%sdata_%s%d%02d%02d.txt", htp ? "HTP_" : "", tag, tmv.tm_year + 1900,
+             tmv.tm_mon + 1, tmv.tm_mday);
+    std::string path = (dir && *dir) ? std::string(dir) + "/" + fname : std::string(fname);
+    FILE *f = fopen(path.c_str(), "a+");
+    if (!f) return bad("results file did not open");
+    const float *e = r->norms, *t = r->times;
+    const int *sc = r->support;
+    fprintf(f, "%s_S_%s output: ", alg, tag);
+    fprintf(f, "k %d, m %d, n %d, vecDistribution %d ", k, m, n, o->vec_distribution);
+    fprintf(f, "errorl1 %0.7e errorl2 %0.7e errorlinf %0.7e ", e[0], e[1], e[2]);
+    fprintf(f, "timeALG %0.7e timeIter %0.7e timeTotal %0.7e ", t[0], t[1], t[2]);
+    fprintf(f, "iterations %d ", r->iter);
+    fprintf(f, "converge_rate %0.7e ", r->conv_rate);
+    fprintf(f, "TruePos %d FalsePos %d TrueNeg %d FalseNeg %d ", sc[0], sc[1], sc[2], sc[3]);
+    fprintf(f, "seed %u ", o->seed);
+    fprintf(f, "alpha %0.7e ", o->alpha);
+    if (kind == GB_OP_DCT) {
+      fprintf(f, "supp_flag %d \n", o->support_flag);
+    } else if (kind == GB_OP_DENSE) {
+      fprintf(f, "supp_flag %d ", o->support_flag);
+      fprintf(f, "matrixEnsemble %d \n", o->matrix_ensemble == 2 ? 2 : 1);
+    } else {
+      fprintf(f, "supp_flag %d ", o->support_flag);
+      fprintf(f, "NonzerosPerCol %d ", d);
+      fprintf(f, "matrixEnsemble %d \n", o->matrix_ensemble ? o->matrix_ensemble : 3);
+    }
+    for (int j = 0; j < r->iter; ++j) {
+      if (htp)
+        fprintf(f, "iteration %d time_iteration %0.7e time_supp_set %0.7e cg_per_iteration %0.0f time_for_cg %0.7e\n", j,
+                r->time_per_iteration[j], r->time_supp_set[j], r->cg_per_iteration[j], r->time_for_cg[j]);
+      else
+        fprintf(f, "iteration %d time_iteration %0.7e time_supp_set %0.7e\n", j, r->time_per_iteration[j],
+                r->time_supp_set[j]);
+    }
+    fclose(f);
+    if (path_out && path_len > 0) {
+      strncpy(path_out, path.c_str(), (size_t)path_len - 1);
+      path_out[path_len - 1] = 0;
+    }
+    return GB_OK;
+  }
   if (o->noise > 0.0f)
     snprintf(fname, sizeof(fname), "gpu_data_%s%d%02d%02d_noise%0.3f.txt", tag, tmv.tm_year + 1900, tmv.tm_mon + 1,
              tmv.tm_mday, o->noise);

@@ -108,10 +108,13 @@ static __device__ void stop_update(GbState *st, int fail_after) {
   for (int j = 0; j < 15; ++j) st->evol[j] = st->evol[j + 1];
   st->evol[15] = st->prev[14] - st->prev[15];
   st->resid_diff = max_list(st->evol, 16);
-  for (int j = 0; j < 15; ++j)
-    if ((st->prev[15] == st->prev[j]) && (st->iter > 4)) st->cycle = 0;
+  // the timing variants have no cycle test and take the 1/16-th root
+  // (GAGA/gaga/algorithms_timings.cu:610-624, 1509-1523)
+  if (!st->timing)
+    for (int j = 0; j < 15; ++j)
+      if ((st->prev[15] == st->prev[j]) && (st->iter > 4)) st->cycle = 0;
   if (st->iter > fail_after) {
-    float root = 1.0f / 15.0f;
+    float root = st->timing ? 1.0f / 16.0f : 1.0f / 15.0f;
     float rate = st->prev[15] / st->prev[0];
     rate = powf(rate, root);
     if (rate > 0.999f) st->fail = 1;
@@ -142,6 +145,32 @@ static __device__ void bin_decision(GbState *st) {
   } else {
     st->flags[F_DOBIN] = 0;
     st->min_val = st->min_val - st->max_change;
+  }
+}
+
+// The support decision after RestrictedSD (NIHT, HTP).  supportFlag 0 (and every
+// non-timing solve) is FindSupportSet's skip-or-bin rule.  The timing variants
+// (GAGA/gaga/algorithms_timings.cu:566-599): supportFlag 1 takes a new max when minVal <=
+// maxChange and bins every iteration (C_BINPREP decides with the new max); supportFlag 2
+// lowers the sort threshold T by maxChange while T > maxChange and sorts otherwise;
+// supportFlag 3 sorts every iteration (FindSupportSet_sort, functions.cu:446-465); both set
+// k_bin = 1.
+static __device__ void support_decision(GbState *st) {
+  if (st->supp_flag == 1) {
+    st->newmax = (st->min_val <= st->max_change);
+    st->flags[F_DOBIN] = 1;
+  } else if (st->supp_flag >= 2) {
+    st->flags[F_DOBIN] = 0;
+    st->k_bin = 1;
+    const float mc = st->supp_flag == 2 ? st->max_change : st->sort_T;
+    if (st->sort_T > mc) {
+      st->sort_T = st->sort_T - mc;
+      st->flags[F_SORT] = 0;
+    } else {
+      st->flags[F_SORT] = 1;
+    }
+  } else {
+    bin_decision(st);
   }
 }
 
@@ -208,7 +237,19 @@ __device__ __forceinline__ void ctrl_phase(GbState *st, int phase, cudaGraphCond
       break;
     case C_BINPREP:
       // if (minVal <= maxChange) { max_value = MaxMagnitude(d_vec,n); slope = ...; }
-      if (live && st->flags[F_DOBIN]) {
+      if (live && st->supp_flag == 1) {
+        // FindSupportSet(..., maxChange = max_value): bins unless minVal > max_value
+        if (st->newmax) {
+          st->max_value = (float)st->red[R_XMAX];
+          st->slope = ((float)(st->num_bins - 1) / st->max_value);
+        }
+        if (st->min_val <= st->max_value) {
+          st->flags[F_DOBIN] = 1;
+        } else {
+          st->flags[F_DOBIN] = 0;
+          st->min_val = st->min_val - st->max_value;
+        }
+      } else if (live && st->flags[F_DOBIN]) {
         st->max_value = (float)st->red[R_XMAX];
         st->slope = ((float)(st->num_bins - 1) / st->max_value);
       }
@@ -496,7 +537,7 @@ __device__ __forceinline__ void ctrl_phase(GbState *st, int phase, cudaGraphCond
       }
       st->mu = mu;
       st->max_change = 2.0f * mu * (float)st->red[R_GMAX];
-      bin_decision(st);
+      support_decision(st);
       break;
     }
     case C_NIHT_STOP:

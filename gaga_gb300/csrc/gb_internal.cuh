@@ -19,6 +19,8 @@
 #define GB_MAXRB 1024   // max blocks of a reducing kernel
 #define GB_NFLAG 8      // predicate flags
 #define GB_TILE 2048    // elements per block in the ordered compaction
+#define GB_SEL_BINS 2048  // radix-select digits per pass (11 bits)
+#define GB_NSTAMP 6       // timing variants: stamps per iteration (see k_stamp)
 
 // predicate flags (GbState::flags)
 enum {
@@ -28,7 +30,8 @@ enum {
   F_RCG = 3,     // CGIHT: restricted CG step this iteration
   F_CG = 4,      // HTP: inner CG loop running
   F_REMASK = 5,  // CGIHT: support changed, re-restrict the search direction
-  F_KBIN_ALT = 6 // CSMPSP: the k-th bin scan is for the gradient (k_bin_prev), not x
+  F_KBIN_ALT = 6, // CSMPSP: the k-th bin scan is for the gradient (k_bin_prev), not x
+  F_SORT = 7      // timing variants, supportFlag 2/3: a new k-th largest |x| this iteration
 };
 
 // reduction slots
@@ -80,6 +83,12 @@ struct GbState {
   // CGIHTprojected projFracTol; ALPS: the outer bin state kept across its local binning
   float proj_frac_tol, sv_alpha, sv_min_val;
   int sv_max_bin, sv_k_bin;
+  // NIHT / HTP timing variants (GAGA/gaga/algorithms_timings.cu): supportFlag, whether this
+  // iteration takes a new max for the bins (supportFlag 1), the sort threshold T and the
+  // radix-select state of the k-th largest |x| (supportFlag 2/3)
+  int timing, supp_flag, newmax, sel_need;
+  unsigned int sel_prefix;
+  float sort_T;
 };
 
 // Operator description on the device.
@@ -117,6 +126,9 @@ struct GbWork {
   int av_ntile, av_nsplit;   // A x_S launch shape
   float *upd;    // l0 updates (n)
   float *rec;    // l0 residual record (maxiter + 1)
+  unsigned int *sel_hist;    // timing variants: radix-select histograms (3 x GB_SEL_BINS, kept zero)
+  unsigned long long *tstamp;  // timing variants: GB_NSTAMP global-timer stamps per iteration (or null)
+  int *tcg;                  // timing variants: CG steps per iteration (HTP)
   GbOp op;          // dimensions here are capacities when dyn is set
   int dyn;          // 1: kernels read m, n, lda, num_bins, k of the current trial from GbState
   const float *ml_params;    // learned warm start: MLP parameters (null: plain start)
@@ -296,11 +308,13 @@ void enq_support_of_nonzeros(GbWork &w, cudaStream_t s, const float *v, int n);
 struct SolvePlan {
   GbWork *w;
   int alg, k, num_bins;
+  int supp_flag = 0;  // NIHT / HTP timing variants: supportFlag (2, 3: sort-based support)
 };
 void enq_prologue(SolvePlan &P, cudaStream_t s0, cudaGraphConditionalHandle h_outer);
 void enq_body(SolvePlan &P, cudaStream_t s1, cudaGraphConditionalHandle h_outer);
 void enq_cg_body(SolvePlan &P, cudaStream_t s2, cudaGraphConditionalHandle h_inner, int stop_phase = -1);
 void enq_ctrl_phase(GbWork &w, cudaStream_t s, int phase, cudaGraphConditionalHandle h);
+void enq_stamp(GbWork &w, cudaStream_t s, int which, int which2 = -1);
 gb_status gb_make_handle(cudaStream_t parent, cudaGraphConditionalHandle *h);
 gb_status gb_open_while(cudaStream_t parent, cudaStream_t body, cudaGraphConditionalHandle h);
 gb_status gb_close_while(cudaStream_t body);

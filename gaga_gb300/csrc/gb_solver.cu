@@ -442,6 +442,179 @@ __global__ void __launch_bounds__(256) k_compact(GbState *st, int pf, const int 
   if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) st->s_cnt = running;
 }
 
+// ------------------------------------------------------------------ sort-based support
+// The timing variants' supportFlag 2/3 (FindSupportSet_sort, GAGA/gaga/functions.cu:446-465)
+// threshold at T = the k-th largest |x|, which the reference reads from a full thrust::sort
+// of |x| (element n-k of the ascending order).  Here T comes from a three-pass radix select
+// over the bits of |x| (bit 31 is 0; digits of bits 30..21, 20..10, 9..0): each pass
+// histograms the digit of the entries whose higher bits match the prefix chosen so far,
+// then one block picks the digit where the count from the top reaches k.  Integer counts,
+// so T is exactly the sorted element and the result does not depend on the grid.
+__device__ __forceinline__ void sel_digit(int pass, int *shift, int *width) {
+  *shift = pass == 0 ? 21 : pass == 1 ? 10 : 0;
+  *width = pass == 1 ? 11 : 10;
+}
+
+__global__ void __launch_bounds__(256) k_sel_hist(const GbState *st, const float *__restrict__ v, int n,
+                                                  unsigned int *__restrict__ hist, int pass) {
+  if (!gb_pred(st, F_SORT)) return;
+  __shared__ unsigned int h[GB_SEL_BINS];
+  for (int i = threadIdx.x; i < GB_SEL_BINS; i += blockDim.x) h[i] = 0u;
+  __syncthreads();
+  int shift, width;
+  sel_digit(pass, &shift, &width);
+  const int hs = shift + width;  // the bits above this pass's digit
+  const unsigned int prefix = st->sel_prefix >> hs, mask = (1u << width) - 1u;
+  const int lane = threadIdx.x & 31;
+  // i0 is uniform in the block, so every lane of a warp takes part in each match
+  for (int i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
+    const int i = i0 + threadIdx.x;
+    unsigned int key = 0xffffffffu;
+    if (i < n) {
+      const unsigned int u = __float_as_uint(v[i]) & 0x7fffffffu;
+      if (hs >= 31 || (u >> hs) == prefix) key = (u >> shift) & mask;
+    }
+    const unsigned int peers = __match_any_sync(0xffffffffu, key);
+    if (key != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(&h[key], (unsigned int)__popc(peers));
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < GB_SEL_BINS; i += blockDim.x)
+    if (h[i]) atomicAdd(&hist[i], h[i]);
+}
+
+// one block of 1024 threads: thread t owns digits 2047-2t and 2046-2t (descending order);
+// picks the digit, narrows the prefix and the remaining count, and zeroes its histogram
+__global__ void __launch_bounds__(1024) k_sel_scan(GbState *st, unsigned int *__restrict__ hist, int pass) {
+  if (!gb_pred(st, F_SORT)) return;
+  int shift, width;
+  sel_digit(pass, &shift, &width);
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const int d0 = GB_SEL_BINS - 1 - 2 * t, d1 = d0 - 1;
+  const unsigned int c0 = hist[d0], c1 = hist[d1];
+  long long need;
+  if (pass == 0) {
+    const int n = st->n;
+    need = st->k < 1 ? 1 : (st->k > n ? n : st->k);
+  } else {
+    need = st->sel_need;
+  }
+  const unsigned int prefix = pass == 0 ? 0u : st->sel_prefix;
+  // exclusive scan of c0 + c1 over the threads
+  unsigned long long x = (unsigned long long)c0 + c1, inc = x;
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  __shared__ unsigned long long wsum[32];
+  if (lane == 31) wsum[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    unsigned long long ws = wsum[lane], wi = ws;
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += y;
+    }
+    wsum[lane] = wi - ws;  // exclusive over warps
+  }
+  __syncthreads();
+  const long long before = (long long)(wsum[wid] + inc - x);
+  int digit = -1;
+  long long rest = 0;
+  if (before < need && need <= before + (long long)c0) {
+    digit = d0;
+    rest = need - before;
+  } else if (before + (long long)c0 < need && need <= before + (long long)c0 + (long long)c1) {
+    digit = d1;
+    rest = need - before - (long long)c0;
+  }
+  if (digit >= 0) {
+    const unsigned int np = prefix | ((unsigned int)digit << shift);
+    st->sel_prefix = np;
+    st->sel_need = (int)rest;
+    if (pass == 2) st->sort_T = __uint_as_float(np);
+  }
+  hist[d0] = 0u;
+  hist[d1] = 0u;
+}
+
+// threshold_and_support (GAGA/gaga/kernels.cu:85-95) at T, after one_vector_int when a
+// new T was selected: |x| < T -> x = 0, bin 2; else bin 1 on a new T (bins of survivors of a
+// lowered T stay as they were).  Counts each tile's survivors for the support list.
+__global__ void __launch_bounds__(256) k_sort_thresh(GbState *st, float *__restrict__ v, int *__restrict__ bins,
+                                                     int n, int *__restrict__ tile_cnt) {
+  if (!gb_pred(st, F_ALWAYS)) return;
+  const bool reset = st->flags[F_SORT] != 0;
+  const float T = st->sort_T;
+  const int base = blockIdx.x * GB_TILE;
+  int cnt = 0;
+  for (int q = threadIdx.x; q < GB_TILE; q += blockDim.x) {
+    const int i = base + q;
+    if (i < n) {
+      if (fabsf(v[i]) < T) {
+        v[i] = 0.0f;
+        bins[i] = 2;
+      } else {
+        if (reset) bins[i] = 1;
+        cnt++;
+      }
+    }
+  }
+  __shared__ float sm[32];
+  const float tot = block_reduce<0>((float)cnt, sm);
+  if (threadIdx.x == 0) tile_cnt[blockIdx.x] = (int)tot;
+}
+
+// S = ascending { i : |x_i| >= T } after the threshold: every nonzero of x (which can lie
+// outside bins <= 1 after a lowered T) and every entry of bins <= 1, for the dense A x_S
+__global__ void __launch_bounds__(256) k_sort_compact(GbState *st, const float *__restrict__ v, int n,
+                                                      const int *__restrict__ tile_cnt, int *__restrict__ S) {
+  if (!gb_pred(st, F_ALWAYS)) return;
+  const float T = st->sort_T;
+  __shared__ float sm[32];
+  __shared__ int warp_base[8];
+  __shared__ int s_off;
+  float off = 0.0f;
+  for (int t = threadIdx.x; t < (int)blockIdx.x; t += blockDim.x) off += (float)tile_cnt[t];
+  const int offset = (int)block_reduce<0>(off, sm);
+  if (threadIdx.x == 0) s_off = offset;
+  __syncthreads();
+  int running = s_off;
+  const int base = blockIdx.x * GB_TILE;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int q0 = 0; q0 < GB_TILE; q0 += blockDim.x) {
+    const int i = base + q0 + threadIdx.x;
+    const bool in = i < n && !(fabsf(v[i]) < T);
+    const unsigned bal = __ballot_sync(0xffffffffu, in);
+    if (lane == 0) warp_base[wid] = __popc(bal);
+    __syncthreads();
+    int wb = 0, tot = 0;
+    for (int w2 = 0; w2 < 8; ++w2) {
+      if (w2 < wid) wb += warp_base[w2];
+      tot += warp_base[w2];
+    }
+    if (in) S[running + wb + __popc(bal & ((1u << lane) - 1u))] = i;
+    running += tot;
+    __syncthreads();
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) st->s_cnt = running;
+}
+
+// Timing variants: the global timer (ns) at a point of the current iteration, into
+// ts[iter * GB_NSTAMP + which] (and + which2).  Stamps: 0 iteration start, 1 support step
+// start, 2 support step end, 3 CG start (HTP), 4 CG end, 5 iteration end; with the end
+// stamp the HTP CG step count.  Kernels of one stream run in order, so a stamp kernel runs
+// after the kernels before it have finished.
+__global__ void k_stamp(const GbState *st, unsigned long long *ts, int *tcg, int which, int which2) {
+  if (!st->active) return;
+  const int it = st->iter;
+  if (it < 0 || it >= st->maxiter) return;
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  ts[(size_t)it * GB_NSTAMP + which] = t;
+  if (which2 >= 0) ts[(size_t)it * GB_NSTAMP + which2] = t;
+  if (tcg && (which == GB_NSTAMP - 1 || which2 == GB_NSTAMP - 1)) tcg[it] = st->it_cg;
+}
+
 // ------------------------------------------------------------------ l0 kernels
 // cuda_compute_scores_l0 (GAGA/gaga/expander/kernels.cu:353-388); the score stays a float
 // counter as in the reference
@@ -643,6 +816,23 @@ static void enq_support(GbWork &w, cudaStream_t s, int k, bool save_prev) {
   const int tiles = (w.op.n + GB_TILE - 1) / GB_TILE;  // capacity; tiles past n count 0
   k_thresh_count<<<tiles, 256, 0, s>>>(w.st, F_ALWAYS, w.x, w.bins, save_prev ? w.bins_prev : nullptr, n, w.tile_cnt);
   k_compact<<<tiles, 256, 0, s>>>(w.st, F_DOBIN, w.bins, n, w.tile_cnt, w.S);
+}
+
+// supportFlag 2/3: a new T when F_SORT (radix select), the threshold, and for the dense
+// operator the support list of the thresholded x
+static void enq_sort_support(GbWork &w, cudaStream_t s) {
+  const int n = argN(w);
+  for (int pass = 0; pass < 3; ++pass) {
+    k_sel_hist<<<w.red_blocks, 256, 0, s>>>(w.st, w.x, n, w.sel_hist + pass * GB_SEL_BINS, pass);
+    k_sel_scan<<<1, 1024, 0, s>>>(w.st, w.sel_hist + pass * GB_SEL_BINS, pass);
+  }
+  const int tiles = (n + GB_TILE - 1) / GB_TILE;
+  k_sort_thresh<<<tiles, 256, 0, s>>>(w.st, w.x, w.bins, n, w.tile_cnt);
+  if (w.op.kind == GB_OP_DENSE) k_sort_compact<<<tiles, 256, 0, s>>>(w.st, w.x, n, w.tile_cnt, w.S);
+}
+
+void enq_stamp(GbWork &w, cudaStream_t s, int which, int which2) {
+  if (w.tstamp) k_stamp<<<1, 1, 0, s>>>(w.st, w.tstamp, w.tcg, which, which2);
 }
 
 // CG start on the current support (HTP's projection, ThresholdCG, CSMPSP): r = y - A x,
@@ -955,6 +1145,7 @@ void enq_body(SolvePlan &P, cudaStream_t s1, cudaGraphConditionalHandle h_outer)
   }
   if (P.alg == GB_ALG_NIHT || P.alg == GB_ALG_HTP) {
     // RestrictedSD (GAGA/gaga/functions.cu:659-745)
+    enq_stamp(w, s1, 0);
     enq_A(w, s1, w.x, w.resid, w.y, R_RES, F_ALWAYS);
     enq_ctrl(w, s1, C_PUSH_RES);
     if (w.op.kind == GB_OP_DENSE) {
@@ -966,9 +1157,13 @@ void enq_body(SolvePlan &P, cudaStream_t s1, cudaGraphConditionalHandle h_outer)
     enq_A(w, s1, w.xt, w.ru, nullptr, R_AXT, F_ALWAYS);
     enq_ctrl(w, s1, C_SD_MU);
     enq_axpy(w, s1, F_ALWAYS, SC_MU, w.grad, w.x, n, R_XMAX, true, num_bins);
+    enq_stamp(w, s1, 1);
     enq_ctrl(w, s1, C_BINPREP);
-    enq_support(w, s1, k, false);
+    if (P.supp_flag >= 2) enq_sort_support(w, s1);
+    else enq_support(w, s1, k, false);
+    enq_stamp(w, s1, 2);
     if (P.alg == GB_ALG_NIHT) {
+      enq_stamp(w, s1, 5);
       enq_ctrl(w, s1, C_NIHT_STOP, h_outer);
     } else {
       // CG projection on the support (GAGA/gaga/algorithms.cu:2588-2669)
@@ -976,6 +1171,7 @@ void enq_body(SolvePlan &P, cudaStream_t s1, cudaGraphConditionalHandle h_outer)
       enq_AT(w, s1, w.resid, w.grad, F_ALWAYS);
       k_threshold<<<w.red_blocks, 256, 0, s1>>>(w.st, F_ALWAYS, w.grad, w.bins, n);
       k_copy_norm<<<w.red_blocks, 256, 0, s1>>>(w.st, F_ALWAYS, w.grad, w.gp, n, R_DOT1, -1, w.red_part, w.tickets);
+      enq_stamp(w, s1, 3);
     }
   } else if (P.alg == GB_ALG_CGIHT) {
     // RestrictedCGwithSupportEvolution (functions.cu:1004-1102) under F_RCG;
@@ -1094,6 +1290,7 @@ static gb_status build_graph(SolvePlan &P, cudaStream_t s0, cudaStream_t s1, cud
     GB_TRY(open_while(s1, s2, h_inner));
     enq_cg_body(P, s2, h_inner);
     GB_TRY(close_while(s2));
+    enq_stamp(w, s1, 4, 5);
     enq_ctrl(w, s1, C_HTP_STOP, h_outer);
   }
   GB_TRY(close_while(s1));
@@ -1154,6 +1351,7 @@ static gb_status run_eager(SolvePlan &P, cudaStream_t s) {
         enq_cg_body(P, s, 0);
         GB_TRY(read_int(&w.st->flags[F_CG], &cg, s));
       }
+      enq_stamp(w, s, 4, 5);
       enq_ctrl(w, s, C_HTP_STOP, 0);
     }
     GB_TRY(read_int(&w.st->active, &active, s));
@@ -1196,6 +1394,14 @@ static GbState initial_state(const GbWork &w, int alg, const gb_options &o, int 
   st.flags[F_ALWAYS] = 1;
   st.op_kind = w.op.kind;
   st.learned = (w.ml_params && alg == GB_ALG_CGIHT) ? 1 : 0;
+  // timing variants (NIHT, HTP only; gaga_gen.cu:331-334): alpha from the options
+  // (algorithms_timings.cu:477), supportFlag
+  if (o.timing && (alg == GB_ALG_NIHT || alg == GB_ALG_HTP)) {
+    st.timing = 1;
+    st.supp_flag = o.support_flag;
+    st.alpha_bin = o.alpha;
+    st.max_bin = (int)((float)o.num_bins * (1.0f - st.alpha_bin));
+  }
   return st;
 }
 
@@ -1207,6 +1413,7 @@ gb_status gb_run_solver(GbWork &w, int alg, const gb_options &o, int k, cudaStre
   k_init_state<<<1, 1, 0, s>>>(w.st, init);
   GB_CUDA_TRY(cudaGetLastError());
   SolvePlan P{&w, alg, k, o.num_bins};
+  if (o.timing && (alg == GB_ALG_NIHT || alg == GB_ALG_HTP)) P.supp_flag = o.support_flag;
   static const bool eager = getenv("GB_CS_EAGER") && atoi(getenv("GB_CS_EAGER")) != 0;
   if (eager) return run_eager(P, s);
   cudaStream_t s0, s1, s2;
@@ -1235,6 +1442,64 @@ gb_status gb_run_solver(GbWork &w, int alg, const gb_options &o, int k, cudaStre
   cudaStreamDestroy(s0);
   cudaStreamDestroy(s1);
   cudaStreamDestroy(s2);
+  return rc;
+}
+
+// ------------------------------------------------------------------ FindSupportSet_sort component
+// FindSupportSet_sort (GAGA/gaga/functions.cu:446-465) on a device vector: the solver's
+// radix select and threshold kernels with a one-off state.  Returns the new T.
+extern "C" gb_status gb_cs_find_support_set_sort(float *d_v, int *d_bins, int n, int k, float T, float max_change,
+                                                 float *T_out, void *stream) {
+  if (!d_v || !d_bins || !T_out || n < 1 || k < 1 || k > n) {
+    gb_set_error_message("bad FindSupportSet_sort arguments", __FILE__, __LINE__);
+    return GB_BAD_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  GbState h;
+  memset(&h, 0, sizeof(h));
+  h.active = 1;
+  h.n = n;
+  h.k = k;
+  h.flags[F_ALWAYS] = 1;
+  if (T > max_change) {
+    h.sort_T = T - max_change;
+    h.flags[F_SORT] = 0;
+  } else {
+    h.flags[F_SORT] = 1;
+  }
+  const int tiles = (n + GB_TILE - 1) / GB_TILE;
+  GbState *st = nullptr;
+  unsigned int *hist = nullptr;
+  int *tile_cnt = nullptr;
+  gb_status rc = GB_OK;
+  cudaError_t e = cudaMalloc(&st, sizeof(GbState));
+  if (e == cudaSuccess) e = cudaMalloc(&hist, sizeof(unsigned int) * 3 * GB_SEL_BINS);
+  if (e == cudaSuccess) e = cudaMalloc(&tile_cnt, sizeof(int) * tiles);
+  if (e == cudaSuccess) e = cudaMemsetAsync(hist, 0, sizeof(unsigned int) * 3 * GB_SEL_BINS, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(st, &h, sizeof(h), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int blocks = std::max(1, std::min(GB_MAXRB, 2 * sms));
+    for (int pass = 0; pass < 3; ++pass) {
+      k_sel_hist<<<blocks, 256, 0, s>>>(st, d_v, n, hist + pass * GB_SEL_BINS, pass);
+      k_sel_scan<<<1, 1024, 0, s>>>(st, hist + pass * GB_SEL_BINS, pass);
+    }
+    k_sort_thresh<<<tiles, 256, 0, s>>>(st, d_v, d_bins, n, tile_cnt);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, st, sizeof(h), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    gb_set_error_message(cudaGetErrorString(e), __FILE__, __LINE__);
+    rc = e == cudaErrorMemoryAllocation ? GB_OOM : GB_CUDA_ERROR;
+  } else {
+    *T_out = h.sort_T;
+  }
+  cudaFree(tile_cnt);
+  cudaFree(hist);
+  cudaFree(st);
   return rc;
 }
 

@@ -67,9 +67,14 @@ typedef struct {
   float noise;          /* 'noise'          0 */
   int gpu_number;       /* 'gpuNumber'      0 */
   int conv_rate_num;    /* 'convRateNum'    16 */
-  float alpha;          /* 'alpha'          0.25 (used by the timing variants only) */
-  int support_flag;     /* 'supportFlag'    0 (timing variants only) */
-  int timing;           /* 'timing'         0 (accepted; timing variants are not built) */
+  float alpha;          /* 'alpha'          0.25: initial MaxBin = numBins (1 - alpha) of the timing variants */
+  int support_flag;     /* 'supportFlag'    0 (timing variants only): 0 adaptive binning, 1 binning
+                           every iteration, 2 sort-based threshold lowered while it can, 3 sort
+                           every iteration (GAGA/gaga/algorithms_timings.cu:461-465) */
+  int timing;           /* 'timing'         0; 1 ('on') runs NIHT and HTP as their timing variants
+                           (algorithms_timings.cu; no cycle test, alpha and supportFlag used)
+                           and records per-iteration times; other algorithms ignore it
+                           (gaga_gen.cu:331-334) */
   const float *learned_params; /* extension: CGIHT only, device pointer to the warm-start
                            MLP's gb_cs_mlp_num_params() FP32 parameters; NULL = plain start */
   const char *results_dir;  /* extension: generate-and-solve appends the reference's result
@@ -106,6 +111,14 @@ typedef struct {
   float *res_record;    /* parallel_l0: caller buffer of maxiter+1 floats or NULL (resRecord) */
   int warm_start;       /* learned warm start: 0 not used, 1 used, 2 abandoned after 10
                            iterations and solved again from zero (iter counts both runs) */
+  /* timing variants (NIHT, HTP with timing on): caller buffers of maxiter floats or NULL,
+   * filled for the first `iter` iterations from device timer stamps: time_per_iteration,
+   * time_supp_set (support identification), and for HTP cg_per_iteration (CG steps) and
+   * time_for_cg, in ms (algorithms_timings.cu:635-636, 1536-1539) */
+  float *time_per_iteration;
+  float *time_supp_set;
+  float *cg_per_iteration;
+  float *time_for_cg;
 } gb_result;
 
 /* Support-selection state carried between FindSupportSet calls. */
@@ -168,6 +181,14 @@ gb_status gb_cs_find_support_set(float *d_v, int n, int k, float slope, float in
  * A_smv/AT_smv (smv_gpu.cu:108-135): out = A in (transpose 0) or A^T in (transpose 1).
  * p->location must be GB_DEVICE; y/k are ignored. */
 gb_status gb_cs_operator_apply(const gb_problem *p, int transpose, const float *d_in, float *d_out);
+
+/* FindSupportSet_sort (GAGA/gaga/functions.cu:446-465), the sort-based support of the timing
+ * variants (supportFlag 2/3): if T > max_change, T -= max_change; otherwise T = the k-th
+ * largest |v| (element n-k of |v| sorted ascending, exact) and every bin becomes 1; then
+ * entries with |v| < T are zeroed and their bin set to 2.  The new T goes to *T_out.  Device
+ * pointers, 1 <= k <= n; synchronises `stream`. */
+gb_status gb_cs_find_support_set_sort(float *d_v, int *d_bins, int n, int k, float T, float max_change,
+                                      float *T_out, void *stream);
 
 /* Dense operator apply that allocates nothing (no counterpart in the reference): out = A in
  * (transpose 0, in has n entries, out m) or A^T in (transpose 1), A column-major m x n with

@@ -564,6 +564,65 @@ static void stop_update(stop_t *s, const float *prev, int iter, int fail_after) 
   }
 }
 
+/* The timing variants' bookkeeping (GAGA/gaga/algorithms_timings.cu:610-624, 1509-1523):
+ * no cycle test, and the rate test takes the 1/16-th root. */
+static void stop_update_timing(stop_t *s, const float *prev, int iter, int fail_after) {
+  for (int j = 0; j < 15; ++j) s->evol[j] = s->evol[j + 1];
+  s->evol[15] = prev[14] - prev[15];
+  s->resid_diff = max_list(s->evol, 16);
+  if (iter > fail_after) {
+    float rate = powf(prev[15] / prev[0], 1.0f / 16.0f);
+    if (rate > 0.999f) s->fail = 1;
+  }
+}
+
+static int cmp_float_asc(const void *a, const void *b) {
+  const float x = *(const float *)a, y = *(const float *)b;
+  return (x > y) - (x < y);
+}
+
+/* FindSupportSet_sort (GAGA/gaga/functions.cu:446-465): while the threshold T exceeds the
+ * largest possible change, lower it by max_change and threshold (threshold_and_support,
+ * kernels.cu:85-95: |v| < T -> v = 0, bin 2); otherwise T = the k-th largest |v| (thrust::sort
+ * of |v| ascending, element n-k), every bin set to 1 (one_vector_int), then the threshold.
+ * Bins of entries that survive a dynamic threshold keep their previous value. */
+float gbo_find_support_set_sort(float *v, int *bins, float T, float max_change, float *buf, int n, int k) {
+  if (T > max_change) {
+    T = T - max_change;
+  } else {
+    for (int i = 0; i < n; ++i) buf[i] = fabsf(v[i]);
+    qsort(buf, (size_t)n, sizeof(float), cmp_float_asc);
+    T = buf[n - k];
+    for (int i = 0; i < n; ++i) bins[i] = 1;
+  }
+  for (int i = 0; i < n; ++i)
+    if (fabsf(v[i]) < T) {
+      v[i] = 0.0f;
+      bins[i] = 2;
+    }
+  return T;
+}
+
+/* The support step of NIHT_S_timings_* / HTP_S_timings_* (algorithms_timings.cu:566-599, 1392-1425)
+ * after RestrictedSD returned max_change. */
+static void timing_support_step(const gbo_opts *o, float *x, ws_t *w, gbo_bin_state *bs, float max_change,
+                                float *max_value, float *slope, float *T, float *buf, int n, int k) {
+  if (o->supp_flag < 2 && bs->min_val <= max_change) {
+    *max_value = gbo_max_magnitude(x, n);
+    *slope = ((float)(o->num_bins - 1) / *max_value);
+  }
+  if (o->supp_flag == 0 || o->supp_flag == 1) {
+    /* supportFlag 1 passes max_value as maxChange: a binning every iteration */
+    gbo_find_support_set(x, w->bins, w->counters, *slope, *max_value, o->supp_flag == 1 ? *max_value : max_change,
+                         bs, n, k);
+    gbo_threshold(x, w->bins, bs->k_bin, n);
+  } else {
+    bs->k_bin = 1;
+    /* supportFlag 3 passes T as maxChange: T > T fails, a sort every iteration */
+    *T = gbo_find_support_set_sort(x, w->bins, *T, o->supp_flag == 2 ? max_change : *T, buf, n, k);
+  }
+}
+
 int gbo_solve(const gbo_op *op, const float *y, int k, const gbo_opts *o, float *x, gbo_info *info) {
 #ifdef _OPENMP
   int saved_threads = omp_get_max_threads();
@@ -588,6 +647,9 @@ int gbo_solve(const gbo_op *op, const float *y, int k, const gbo_opts *o, float 
   /* ThresholdSD / ThresholdCG start with alpha = 0, i.e. MaxBin = num_bins
    * (GAGA/gaga/algorithms.cu:800-802,1838-1840) */
   bs.alpha = (o->alg == GBO_HT_SD || o->alg == GBO_HT_CG) ? 0.0f : 0.25f;
+  /* the timing variants take alpha from the options (gaga_gen.cu:329, algorithms_timings.cu:477) */
+  const int timing = o->timing && (o->alg == GBO_NIHT || o->alg == GBO_HTP);
+  if (timing) bs.alpha = o->alpha;
   bs.max_bin = (int)((float)o->num_bins * (1.0f - bs.alpha));
   bs.min_val = 0.0f;
   bs.k_bin = 0;
@@ -915,6 +977,18 @@ int gbo_solve(const gbo_op *op, const float *y, int k, const gbo_opts *o, float 
       s.resid_diff = max_list(s.evol, 16);
       iter++;
     }
+  } else if (o->alg == GBO_NIHT && timing) {
+    /* NIHT_S_timings_gen (GAGA/gaga/algorithms_timings.cu:453-650; _dct 35-240, _smv 246-450) */
+    float T = 0.0f;
+    float *buf = (float *)malloc(sizeof(float) * (size_t)n);
+    while (keep_going(&s, iter, o->maxiter)) {
+      float max_change = restricted_sd(&w, bs.k_bin);
+      timing_support_step(o, x, &w, &bs, max_change, &max_value, &slope, &T, buf, n, k);
+      s.err = w.prev[15];
+      stop_update_timing(&s, w.prev, iter, 749);
+      iter++;
+    }
+    free(buf);
   } else if (o->alg == GBO_NIHT) {
     /* NIHT_S_gen (GAGA/gaga/algorithms.cu:1274-1441) */
     while (keep_going(&s, iter, o->maxiter)) {
@@ -930,17 +1004,25 @@ int gbo_solve(const gbo_op *op, const float *y, int k, const gbo_opts *o, float 
       iter++;
     }
   } else if (o->alg == GBO_HTP) {
-    /* HTP_S_gen (GAGA/gaga/algorithms.cu:2491-2716) */
+    /* HTP_S_gen (GAGA/gaga/algorithms.cu:2491-2716); with timing on, HTP_S_timings_gen
+     * (algorithms_timings.cu:1266-1560): the support step of supportFlag, no cycle test,
+     * the rate test's 1/16-th root */
     float tol_cg = s.tol * s.tol;
     float tol2 = 10.0f * tol_cg;
+    float T = 0.0f;
+    float *buf = timing ? (float *)malloc(sizeof(float) * (size_t)n) : NULL;
     while (keep_going(&s, iter, o->maxiter)) {
       float max_change = restricted_sd(&w, bs.k_bin);
-      if (bs.min_val <= max_change) {
-        max_value = gbo_max_magnitude(x, n);
-        slope = ((float)(o->num_bins - 1) / max_value);
+      if (timing) {
+        timing_support_step(o, x, &w, &bs, max_change, &max_value, &slope, &T, buf, n, k);
+      } else {
+        if (bs.min_val <= max_change) {
+          max_value = gbo_max_magnitude(x, n);
+          slope = ((float)(o->num_bins - 1) / max_value);
+        }
+        gbo_find_support_set(x, w.bins, w.counters, slope, max_value, max_change, &bs, n, k);
+        gbo_threshold(x, w.bins, bs.k_bin, n);
       }
-      gbo_find_support_set(x, w.bins, w.counters, slope, max_value, max_change, &bs, n, k);
-      gbo_threshold(x, w.bins, bs.k_bin, n);
       float prevcg[16], evolcg[16];
       for (int j = 0; j < 16; ++j) { prevcg[j] = 0.0f; evolcg[j] = 1.0f; }
       float diffcg = 1.0f;
@@ -963,9 +1045,11 @@ int gbo_solve(const gbo_op *op, const float *y, int k, const gbo_opts *o, float 
       }
       s.err = sqrtf(errcg);
       push16(w.prev, s.err);
-      stop_update(&s, w.prev, iter, 125);
+      if (timing) stop_update_timing(&s, w.prev, iter, 125);
+      else stop_update(&s, w.prev, iter, 125);
       iter++;
     }
+    free(buf);
   } else if (o->alg == GBO_CGIHT) {
     /* CGIHT_S_gen (GAGA/gaga/algorithms.cu:3689-3942) */
     residual(&w, x, w.resid, w.ru);

@@ -66,6 +66,11 @@ typedef struct {
   int l0_thresh;     /* parallel_l0 / serial_l0 alpha */
   int threads;       /* OpenMP threads for operators (0 = runtime default) */
   float proj_frac_tol; /* CGIHTprojected projFracTol (gaga_gen.cu:190: 3) */
+  int timing;        /* 'timing' on: NIHT / HTP run as their timing variants
+                        (GAGA/gaga/algorithms_timings.cu); other algorithms ignore it */
+  int supp_flag;     /* 'supportFlag' of the timing variants: 0 adaptive binning, 1 binning every
+                        iteration, 2 sort with a dynamic threshold, 3 sort every iteration */
+  float alpha;       /* 'alpha' of the timing variants: initial MaxBin = num_bins (1 - alpha) */
 } gbo_opts;
 
 typedef struct {
@@ -108,6 +113,8 @@ typedef struct {
 int gbo_find_support_set(const float *v, int *bins, int *counters, float slope, float intercept,
                          float max_change, gbo_bin_state *st, int n, int k);
 void gbo_threshold(float *v, const int *bins, int k_bin, int n);
+/* FindSupportSet_sort (GAGA/gaga/functions.cu:446-465); buf: n floats of scratch; returns T */
+float gbo_find_support_set_sort(float *v, int *bins, float T, float max_change, float *buf, int n, int k);
 float gbo_max_magnitude(const float *v, int n);
 
 /* ---------------- solvers ---------------- */

@@ -33,7 +33,8 @@ class GboOp(C.Structure):
 
 class GboOpts(C.Structure):
     _fields_ = [("alg", C.c_int), ("tol", C.c_float), ("maxiter", C.c_int), ("num_bins", C.c_int),
-                ("restart", C.c_int), ("l0_thresh", C.c_int), ("threads", C.c_int), ("proj_frac_tol", C.c_float)]
+                ("restart", C.c_int), ("l0_thresh", C.c_int), ("threads", C.c_int), ("proj_frac_tol", C.c_float),
+                ("timing", C.c_int), ("supp_flag", C.c_int), ("alpha", C.c_float)]
 
 
 class GboInfo(C.Structure):
@@ -65,6 +66,7 @@ def _declare(L):
         "gbo_linear_binning": (None, [vp, i, i, i, f, f, vp, vp]),
         "gbo_find_support_set": (i, [vp, vp, vp, f, f, f, vp, i, i]),
         "gbo_threshold": (None, [vp, vp, i, i]),
+        "gbo_find_support_set_sort": (f, [vp, vp, f, f, vp, i, i]),
         "gbo_max_magnitude": (f, [vp, i]),
         "gbo_solve": (i, [vp, vp, i, vp, vp, vp]),
         "gbo_parallel_l0": (i, [vp, vp, vp, vp, vp, vp, vp]),
@@ -196,6 +198,15 @@ def find_support_set(v, k, num_bins, slope, intercept, max_change, state=None, b
     return s, bins, cnt, state
 
 
+def find_support_set_sort(v, bins, T, max_change, k):
+    """One FindSupportSet_sort call on copies of v and bins: (v, bins, T)."""
+    v = f32(v).copy()
+    bins = np.ascontiguousarray(bins, dtype=np.int32).copy()
+    buf = np.zeros(len(v), dtype=np.float32)
+    T = lib().gbo_find_support_set_sort(_p(v), _p(bins), T, max_change, _p(buf), len(v), k)
+    return v, bins, np.float32(T)
+
+
 def max_magnitude(v):
     v = f32(v)
     return lib().gbo_max_magnitude(_p(v), len(v))
@@ -206,14 +217,15 @@ def default_num_bins(n):
     return max(n // 20, 1000)
 
 
-def solve(alg, op, y, k, tol, maxiter=None, num_bins=None, restart=0, threads=0, proj_frac_tol=3.0):
+def solve(alg, op, y, k, tol, maxiter=None, num_bins=None, restart=0, threads=0, proj_frac_tol=3.0, timing=0,
+          supp_flag=0, alpha=0.25):
     alg_id = ALG_IDS[alg] if isinstance(alg, str) else alg
     if maxiter is None:
         maxiter = 300 if alg_id == HTP else 5000
     num_bins = num_bins or default_num_bins(op.n)
     y = f32(y)
     x = np.zeros(op.n, dtype=np.float32)
-    o = GboOpts(alg_id, tol, maxiter, num_bins, restart, 1, threads, proj_frac_tol)
+    o = GboOpts(alg_id, tol, maxiter, num_bins, restart, 1, threads, proj_frac_tol, timing, supp_flag, alpha)
     info = GboInfo()
     lib().gbo_solve(C.byref(op.c), _p(y), k, C.byref(o), _p(x), C.byref(info))
     return x, info

@@ -164,3 +164,50 @@ def test_result_file_lines_match_reference_format(gb, tmp_path):
     assert L.gb_cs_write_result(str(tmp_path).encode(), b"HTP", 1, 10, 100, 512, 0, C.byref(o), C.byref(r), buf,
                                 512) == 0
     assert open(buf.value.decode()).read().startswith("HTP_S_dct output: k 10, m 100, n 512, vecDistribution 1 error")
+
+
+def test_timing_result_file_lines_match_reference_format(gb, tmp_path):
+    """With timing on, NIHT and HTP results go to gpu_timings[_HTP]_data_* files: the
+    File_output_timings* summary line, then one line per iteration
+    (GAGA/gaga/functions.cu:82-208, results.cu:1206,1375,1545,1716,1890,2061)."""
+    L = gb._lib.load()
+    o = gb._lib.Options()
+    L.gb_cs_default_options(C.byref(o), b"NIHT", 4096)
+    o.seed, o.timing, o.support_flag, o.alpha = 5, 1, 2, 0.125
+    r = gb._lib.Result()
+    r.norms[0], r.norms[1], r.norms[2] = 1e-6, 2e-6, 3e-6
+    r.times[0], r.times[1], r.times[2] = 4.0, 2.0, 9.0
+    r.iter, r.conv_rate = 2, 0.5
+    for j, v in enumerate((20, 0, 4076, 0)):
+        r.support[j] = v
+    tpi = np.array([1.5, 2.5], dtype=np.float32)
+    tss = np.array([0.25, 0.5], dtype=np.float32)
+    cgi = np.array([3, 15], dtype=np.float32)
+    tcg = np.array([0.75, 1.25], dtype=np.float32)
+    r.time_per_iteration, r.time_supp_set = tpi.ctypes.data, tss.ctypes.data
+    r.cg_per_iteration, r.time_for_cg = cgi.ctypes.data, tcg.ctypes.data
+    buf = C.create_string_buffer(512)
+    d = str(tmp_path).encode()
+    assert L.gb_cs_write_result(d, b"NIHT", 0, 20, 1024, 4096, 0, C.byref(o), C.byref(r), buf, 512) == 0
+    path = buf.value.decode()
+    assert re.search(r"gpu_timings_data_gen\d{8}\.txt$", path)
+    head = ("NIHT_S_gen output: k 20, m 1024, n 4096, vecDistribution 1 errorl1 %0.7e errorl2 %0.7e "
+            "errorlinf %0.7e timeALG %0.7e timeIter %0.7e timeTotal %0.7e iterations 2 converge_rate %0.7e "
+            "TruePos 20 FalsePos 0 TrueNeg 4076 FalseNeg 0 seed 5 alpha %0.7e supp_flag 2 matrixEnsemble 1 \n" % (
+                np.float32(1e-6), np.float32(2e-6), np.float32(3e-6), 4.0, 2.0, 9.0, 0.5, 0.125))
+    body = "".join("iteration %d time_iteration %0.7e time_supp_set %0.7e\n" % (j, tpi[j], tss[j]) for j in range(2))
+    assert open(path).read() == head + body
+    # HTP on the DCT: its own file, the CG columns, no matrixEnsemble
+    assert L.gb_cs_write_result(d, b"HTP", 1, 20, 1024, 4096, 0, C.byref(o), C.byref(r), buf, 512) == 0
+    path = buf.value.decode()
+    assert re.search(r"gpu_timings_HTP_data_dct\d{8}\.txt$", path)
+    lines = open(path).read().splitlines(keepends=True)
+    assert lines[0].startswith("HTP_S_dct output: k 20,") and lines[0].endswith("alpha 1.2500000e-01 supp_flag 2 \n")
+    assert lines[2] == "iteration 1 time_iteration %0.7e time_supp_set %0.7e cg_per_iteration 15 time_for_cg %0.7e\n" % (
+        2.5, 0.5, 1.25)
+    # expander: NonzerosPerCol and matrixEnsemble close the summary line
+    assert L.gb_cs_write_result(d, b"NIHT", 2, 20, 1024, 4096, 7, C.byref(o), C.byref(r), buf, 512) == 0
+    assert open(buf.value.decode()).readline().endswith("supp_flag 2 NonzerosPerCol 7 matrixEnsemble 3 \n")
+    # without the per-iteration arrays the timing file cannot be written
+    r.time_per_iteration = None
+    assert L.gb_cs_write_result(d, b"NIHT", 0, 20, 1024, 4096, 0, C.byref(o), C.byref(r), buf, 512) != 0

@@ -120,3 +120,34 @@ def test_oracle_l0_variants_decode(gbo, variant):
     y = gbo.A(op, x0)
     x, res, rec, info = gbo.parallel_l0(op, y, tol=1e-6, maxiter=300, variant=variant)
     assert np.array_equal(x, x0), (variant, info.iter)
+
+
+def test_oracle_sort_support(gbo):
+    """FindSupportSet_sort restated: T is element n-k of |v| sorted ascending and the new
+    bins are 1 / 2 around it; a lowered T thresholds without touching surviving bins
+    (GAGA/gaga/functions.cu:446-465, kernels.cu:85-95)."""
+    rng = np.random.default_rng(3)
+    v = np.round(rng.standard_normal(5000) * 8).astype(np.float32) / 8  # many ties
+    k = 300
+    x, b, T = gbo.find_support_set_sort(v, np.full(5000, 7, np.int32), 0.0, 1.0, k)
+    assert T == np.sort(np.abs(v))[5000 - k]
+    keep = np.abs(v) >= T
+    assert np.array_equal(x, np.where(keep, v, 0)) and np.array_equal(b, np.where(keep, 1, 2))
+    b[:10] = 9
+    x2, b2, T2 = gbo.find_support_set_sort(x, b, T, np.float32(0.25), k)
+    assert T2 == np.float32(T - np.float32(0.25))
+    assert np.array_equal(b2[:10], np.where(np.abs(x[:10]) < T2, 2, 9))
+
+
+@pytest.mark.parametrize("alg", ["NIHT", "HTP"])
+@pytest.mark.parametrize("supp_flag", [0, 1, 2, 3])
+def test_oracle_timing_variants_recover(gbo, alg, supp_flag):
+    """The timing variants (algorithms_timings.cu) recover an easy dense problem with every
+    supportFlag, as the plain loops do."""
+    n, m, k = 2048, 512, 25
+    A = gbo.gen_dense(m, n, 8)
+    x0, ks = gbo.gen_vector(n, k, 1, 8)
+    op = gbo.Op.dense(A, m, n)
+    y = gbo.A(op, x0)
+    x, info = gbo.solve(alg, op, y, ks, 1e-5 * float(np.linalg.norm(y)), timing=1, supp_flag=supp_flag)
+    assert np.linalg.norm(x - x0) / np.linalg.norm(x0) < 1e-3 and info.iter > 0
