@@ -51,6 +51,10 @@ extern "C" int gb_cs_alg_id(const char *alg) {
   if (!strcmp(alg, "parallel_lddsr")) return GB_ALG_PARALLEL_LDDSR;
   if (!strcmp(alg, "smp")) return GB_ALG_SMP;
   if (!strcmp(alg, "parallel_l0_swipe")) return GB_ALG_PARALLEL_L0_SWIPE;
+  if (!strcmp(alg, "ssmp")) return GB_ALG_SSMP;
+  if (!strcmp(alg, "er")) return GB_ALG_ER;
+  if (!strcmp(alg, "ssmp_naive")) return GB_ALG_SSMP_NAIVE;
+  if (!strcmp(alg, "er_naive")) return GB_ALG_ER_NAIVE;
   return -1;
 }
 
@@ -373,7 +377,7 @@ extern "C" gb_status gb_cs_solve(const char *alg, const gb_problem *p, const gb_
   if (!p || !x_out) return bad("null argument");
   const int alg_id = gb_cs_alg_id(alg);
   if (alg_id < 0) return bad("algorithm must be one of NIHT, HTP, IHT, ThresholdSD, ThresholdCG, CSMPSP, CGIHT, FIHT, ALPS, "
-                         "CGIHTprojected, smp, parallel_l0, parallel_lddsr, parallel_l0_swipe");
+                         "CGIHTprojected, smp, ssmp, er, ssmp_naive, er_naive, parallel_l0, parallel_lddsr, parallel_l0_swipe");
   if (gb_is_ccs(alg_id) && p->kind != GB_OP_SMV) return bad("the expander decoders require the smv operator");
   gb_options o;
   if (opts) o = *opts;
@@ -535,7 +539,7 @@ extern "C" gb_status gb_cs_generate_and_solve(const char *alg, int kind, int k, 
   if (!x_out) return bad("null argument");
   const int alg_id = gb_cs_alg_id(alg);
   if (alg_id < 0) return bad("algorithm must be one of NIHT, HTP, IHT, ThresholdSD, ThresholdCG, CSMPSP, CGIHT, FIHT, ALPS, "
-                         "CGIHTprojected, smp, parallel_l0, parallel_lddsr, parallel_l0_swipe");
+                         "CGIHTprojected, smp, ssmp, er, ssmp_naive, er_naive, parallel_l0, parallel_lddsr, parallel_l0_swipe");
   if (gb_is_ccs(alg_id) && kind != GB_OP_SMV) return bad("the expander decoders require the smv operator");
   if (k < 1 || m < 1 || n < 1 || (kind == GB_OP_SMV && d < 1)) return bad("k, m, n (and d) must be positive");
   gb_options o;

@@ -76,7 +76,11 @@ enum {
   C_CP_PROJ,      // CGIHTprojected: projection fraction -> next branch
   C_SMP_INIT,     // smp: err of the zero start, first loop test
   C_SMP_HK,       // smp: H_k's fresh binning of the vector whose max is in red[R_XMAX]
-  C_SMP_STOP      // smp: residual history and stopping rules
+  C_SMP_STOP,     // smp: residual history and stopping rules
+  C_SEQ_INIT,     // ssmp / er: err of the start, records, first loop test
+  C_SEQ_STOP,     // ssmp / er: residual history (ssmp) or cycle test (er), stopping rules
+  C_SEQ_END1,     // ssmp: reopen the predicates for the final H_k
+  C_SEQ_END2      // ssmp: close them again
 };
 
 static __device__ float max_list(const float *a, int n) {

@@ -45,7 +45,9 @@ enum {
   R_DOT2 = 6,
   R_DOT3 = 7,
   R_DOT4 = 8,
-  R_CG = 9     // HTP inner CG: ||A grad||^2
+  R_CG = 9,    // HTP inner CG: ||A grad||^2
+  R_SEQ_VAL = 12,  // ssmp / er argmax: block partials of the best score (ticket 12)
+  R_SEQ_IDX = 13   // and of its index
 };
 
 struct GbState {
@@ -89,6 +91,9 @@ struct GbState {
   int timing, supp_flag, newmax, sel_need;
   unsigned int sel_prefix;
   float sort_T;
+  // sequential decoders: the node picked this iteration, whether ssmp takes its periodic
+  // H_k step this iteration
+  int h_node, periodic;
 };
 
 // Operator description on the device.
@@ -160,7 +165,11 @@ inline bool gb_is_l0(int alg) {
   return alg == GB_ALG_PARALLEL_L0 || alg == GB_ALG_PARALLEL_LDDSR || alg == GB_ALG_PARALLEL_L0_SWIPE;
 }
 // the expander (CCS) decoders: smv only, unit values, a residual record
-inline bool gb_is_ccs(int alg) { return gb_is_l0(alg) || alg == GB_ALG_SMP; }
+// the sequential decoders: one node per iteration (ssmp, er and their naive forms)
+inline bool gb_is_seq(int alg) {
+  return alg == GB_ALG_SSMP || alg == GB_ALG_ER || alg == GB_ALG_SSMP_NAIVE || alg == GB_ALG_ER_NAIVE;
+}
+inline bool gb_is_ccs(int alg) { return gb_is_l0(alg) || alg == GB_ALG_SMP || gb_is_seq(alg); }
 
 // ---------------------------------------------------------------- device helpers
 // Dimension arguments of the solver kernels: a value >= 0 is used as is; a negative code

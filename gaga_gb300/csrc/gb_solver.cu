@@ -92,6 +92,69 @@ __global__ void k_ctrl_l0(GbState *st, int phase, float *rec, cudaGraphCondition
       }
       set_cond(h, st->active ? 1u : 0u);
       break;
+    case C_SEQ_INIT: {
+      // ssmp.cu:56-81 / er.cu:43-68: res = y - A x^0, err, records
+      st->err = sqrt_red(st, R_RES);
+      st->err_start = st->err;
+      if (rec) rec[0] = st->err;
+      for (int j = 0; j < 16; ++j) { st->prev[j] = 0.0f; st->evol[j] = 1.0f; }
+      for (int i = 0; i < L; ++i) st->l0_cyc[i] = 0.0f;
+      st->resid_diff = 1.0f;
+      st->cycle = 1;
+      const bool er = st->alg == GB_ALG_ER || st->alg == GB_ALG_ER_NAIVE;
+      st->active = (st->iter < st->maxiter) & (st->err > st->tol) & (st->err < 100.0f * st->err_start) &
+                   (er ? 1 : ((double)st->resid_diff > 0.01 * (double)st->tol));
+      set_cond(h, st->active ? 1u : 0u);
+      break;
+    }
+    case C_SEQ_STOP:
+      if (st->active) {
+        const bool er = st->alg == GB_ALG_ER || st->alg == GB_ALG_ER_NAIVE;
+        st->err = sqrt_red(st, R_RES);
+        int cycling = 0;
+        if (er) {
+          // er.cu:97-110: the last 2p residuals alternate between two values (er only)
+          st->iter++;
+          for (int i = 0; i < L - 1; ++i) st->l0_cyc[i] = st->l0_cyc[i + 1];
+          st->l0_cyc[L - 1] = st->err;
+          if (st->alg == GB_ALG_ER && st->iter > L) {
+            cycling = 1;
+            for (int i = 3; i < L; i += 2) cycling = cycling * (st->l0_cyc[i] == st->l0_cyc[i - 2]);
+          }
+          st->cycle = cycling ? 0 : 1;
+        } else {
+          // ssmp.cu:124-131: residual history
+          for (int j = 0; j < 15; ++j) { st->prev[j] = st->prev[j + 1]; st->evol[j] = st->evol[j + 1]; }
+          st->prev[15] = st->err;
+          st->evol[15] = st->prev[14] - st->prev[15];
+          st->resid_diff = max_list(st->evol, 16);
+          st->iter++;
+        }
+        st->passes++;
+        if (rec) rec[st->iter] = st->err;
+        const int go = (st->iter < st->maxiter) & (st->err > st->tol) & (st->err < 100.0f * st->err_start) &
+                       (er ? (cycling == 0) : ((double)st->resid_diff > 0.01 * (double)st->tol));
+        if (!go) {
+          if (!(st->err > st->tol)) st->stop_reason = 1;
+          else if (!(st->iter < st->maxiter)) st->stop_reason = 2;
+          else if (!(st->err < 100.0f * st->err_start)) st->stop_reason = 3;
+          else if (er) st->stop_reason = 5;
+          else st->stop_reason = 4;
+        }
+        st->active = go;
+        if (st->passes > st->pass_limit && st->active) {
+          st->active = 0;
+          st->status = GB_WATCHDOG;
+        }
+      }
+      set_cond(h, st->active ? 1u : 0u);
+      break;
+    case C_SEQ_END1:
+      st->active = 1;
+      break;
+    case C_SEQ_END2:
+      st->active = 0;
+      break;
     case C_L0_PRE:
       if (!st->active) break;
       st->l0_offset = st->iter % st->d;
@@ -670,6 +733,145 @@ __global__ void k_smp_scores(const GbState *st, const float *__restrict__ res, c
   }
 }
 
+// ------------------------------------------------------------------ sequential decoders
+// Node scores of ssmp and er (GAGA/gaga/expander/kernels.cu:115-145, 195-245): the d residual
+// entries of node j, bubble-sorted as the reference does; ssmp: the median and its
+// magnitude; er: the mode (the value before the first longest run of entries within 1e-7 of
+// their neighbour) and its run length as the score (0 when |mode| <= 1e-7).
+__device__ __forceinline__ void seq_score(int er, const float *__restrict__ res, const int *__restrict__ rows_j,
+                                          int d, float *upd, float *score) {
+  float b[32];
+  for (int i = 0; i < d; ++i) b[i] = res[rows_j[i]];
+  for (int i = 0; i < d; ++i)
+    for (int q = 0; q < d - 1; ++q)
+      if (b[q] > b[q + 1]) {
+        const float t = b[q + 1];
+        b[q + 1] = b[q];
+        b[q] = t;
+      }
+  if (!er) {
+    const float z = (d % 2) == 0 ? (b[d / 2 - 1] + b[d / 2]) / 2 : b[(d - 1) / 2];
+    *upd = z;
+    *score = fabsf(z);
+  } else {
+    const float eps = 0.0000001f;
+    float mode = b[0], count = 1.0f, count_mode = 1.0f;
+    for (int i = 1; i < d; ++i) {
+      if (fabsf(__fsub_rn(b[i], b[i - 1])) <= eps) {
+        count = count + 1.0f;
+        if (count > count_mode) {
+          count_mode = count;
+          mode = b[i - 1];
+        }
+      } else {
+        count = 1.0f;
+      }
+    }
+    *upd = mode;
+    *score = fabsf(mode) > eps ? count_mode : 0.0f;
+  }
+}
+
+// every node's score (cuda_compute_scores_ssmp / _er)
+__global__ void k_seq_scores(const GbState *st, int er, const float *__restrict__ res, const int *__restrict__ rows,
+                             int n, int d, float *__restrict__ upd, float *__restrict__ score) {
+  if (!st->active) return;
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+    seq_score(er, res, rows + (size_t)j * d, d, &upd[j], &score[j]);
+}
+
+// the scores of the nodes that share a row with the node just updated (cuda_update_scores_ssmp
+// / _er, kernels.cu:147-193, 247-305): block b walks row rows[h d + b] of the row-major copy.
+// A node on several of those rows is scored by several blocks, with the same result.
+__global__ void k_seq_rescore(const GbState *st, int er, const float *__restrict__ res, const int *__restrict__ rows,
+                              const int *__restrict__ ptr, const int *__restrict__ col, int d,
+                              float *__restrict__ upd, float *__restrict__ score) {
+  if (!st->active) return;
+  const int h = st->h_node;
+  const int r = rows[(size_t)h * d + blockIdx.x];
+  for (int e = ptr[r] + threadIdx.x; e < ptr[r + 1]; e += blockDim.x) {
+    const int j = col[e];
+    seq_score(er, res, rows + (size_t)j * d, d, &upd[j], &score[j]);
+  }
+}
+
+// cublasIsamax over the scores: the first index of the largest |score|, as a grid reduction in
+// a fixed order (each block its best (value, index), the last block to arrive picks among them)
+__device__ __forceinline__ void better(float &v, int &i, float v2, int i2) {
+  if (v2 > v || (v2 == v && i2 < i)) {
+    v = v2;
+    i = i2;
+  }
+}
+__global__ void __launch_bounds__(256) k_seq_argmax(GbState *st, const float *__restrict__ score, int n,
+                                                    float *parts, unsigned int *tickets) {
+  if (!st->active) return;
+  float bv = -1.0f;
+  int bi = 0x7fffffff;
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const float v = fabsf(score[j]);
+    if (v > bv) {
+      bv = v;
+      bi = j;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) better(bv, bi, __shfl_xor_sync(0xffffffffu, bv, o), __shfl_xor_sync(0xffffffffu, bi, o));
+  __shared__ float sv[32];
+  __shared__ int si[32];
+  __shared__ int last;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0) {
+    sv[wid] = bv;
+    si[wid] = bi;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int q = 1; q < nw; ++q) better(bv, bi, sv[q], si[q]);
+    parts[R_SEQ_VAL * GB_MAXRB + blockIdx.x] = bv;
+    parts[R_SEQ_IDX * GB_MAXRB + blockIdx.x] = __int_as_float(bi);
+    __threadfence();
+    const unsigned int t = atomicAdd(&tickets[R_SEQ_VAL], 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    float v = -1.0f;
+    int i = 0x7fffffff;
+    for (int q = 0; q < (int)gridDim.x; ++q)
+      better(v, i, __ldcg(&parts[R_SEQ_VAL * GB_MAXRB + q]), __float_as_int(__ldcg(&parts[R_SEQ_IDX * GB_MAXRB + q])));
+    st->h_node = (i >= 0 && i < n) ? i : 0;
+    tickets[R_SEQ_VAL] = 0u;
+  }
+}
+
+// cudaUpdateSignal + cudaUpdateResidual (GAGA/gaga/expander/kernels.cu:1014-1032) for node h:
+// x_h += update_h and, unless ssmp takes its periodic H_k step this iteration (iter % k == 0,
+// iter > 0, ssmp.cu:102-117), res -= update_h * A_h (one lane per row of the column)
+__global__ void k_seq_node(GbState *st, float *__restrict__ x, float *__restrict__ res, const int *__restrict__ rows,
+                           const float *__restrict__ vals, const float *__restrict__ upd, int d,
+                           cudaGraphConditionalHandle h_if) {
+  if (!st->active) {
+    if (threadIdx.x == 0) set_cond(h_if, 0u);
+    return;
+  }
+  const int h = st->h_node;
+  const bool ssmp = st->alg == GB_ALG_SSMP || st->alg == GB_ALG_SSMP_NAIVE;
+  const bool periodic = ssmp && st->k > 0 && (st->iter % st->k == 0) && (st->iter > 0);
+  const float u = upd[h];
+  if (!periodic && (int)threadIdx.x < d) {
+    const size_t e = (size_t)h * d + threadIdx.x;
+    const int r = rows[e];
+    res[r] = fmaf(-u, vals[e], res[r]);
+  }
+  if (threadIdx.x == 0) {
+    x[h] = x[h] + u;
+    st->periodic = periodic ? 1 : 0;
+    set_cond(h_if, periodic ? 1u : 0u);
+  }
+}
+
 // ThresholdK (GAGA/gaga/expander/functions.cu:103-123): after Threshold, per-tile counts of
 // the support and of the entries in the k-th bin (second half of tile_cnt)
 __global__ void __launch_bounds__(256) k_hk_count(const GbState *st, const float *__restrict__ v,
@@ -768,7 +970,7 @@ gb_status make_handle(cudaStream_t parent, cudaGraphConditionalHandle *h) {
   return GB_OK;
 }
 
-gb_status open_while(cudaStream_t parent, cudaStream_t body, cudaGraphConditionalHandle h) {
+gb_status open_cond(cudaStream_t parent, cudaStream_t body, cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type) {
   cudaStreamCaptureStatus cs;
   cudaGraph_t g;
   const cudaGraphNode_t *deps = nullptr;
@@ -777,7 +979,7 @@ gb_status open_while(cudaStream_t parent, cudaStream_t body, cudaGraphConditiona
   cudaGraphNodeParams p = {};
   p.type = cudaGraphNodeTypeConditional;
   p.conditional.handle = h;
-  p.conditional.type = cudaGraphCondTypeWhile;
+  p.conditional.type = type;
   p.conditional.size = 1;
   cudaGraphNode_t node;
   GB_CUDA_TRY(cudaGraphAddNode(&node, g, deps, nullptr, nd, &p));
@@ -785,6 +987,10 @@ gb_status open_while(cudaStream_t parent, cudaStream_t body, cudaGraphConditiona
   GB_CUDA_TRY(cudaStreamBeginCaptureToGraph(body, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
                                             cudaStreamCaptureModeRelaxed));
   return GB_OK;
+}
+
+gb_status open_while(cudaStream_t parent, cudaStream_t body, cudaGraphConditionalHandle h) {
+  return open_cond(parent, body, h, cudaGraphCondTypeWhile);
 }
 
 gb_status close_while(cudaStream_t body) {
@@ -997,6 +1203,68 @@ static void enq_expander_hk(SolvePlan &P, cudaStream_t s, float *v, int K) {
   k_hk_trim<<<tiles, 256, 0, s>>>(w.st, v, w.bins, n, w.tile_cnt, K);
 }
 
+// ssmp / er: every node's score into w.grad (update) and w.xt (score)
+static void enq_seq_scores(SolvePlan &P, cudaStream_t s) {
+  GbWork &w = *P.w;
+  const int n = argN(w);
+  int blocks = (n + 255) / 256;
+  if (blocks > w.num_sms * 16) blocks = w.num_sms * 16;
+  const int er = (P.alg == GB_ALG_ER || P.alg == GB_ALG_ER_NAIVE) ? 1 : 0;
+  k_seq_scores<<<blocks, 256, 0, s>>>(w.st, er, w.resid, w.op.smv_rows, n, w.op.d, w.grad, w.xt);
+}
+
+static void enq_seq_tail(SolvePlan &P, cudaStream_t s, cudaGraphConditionalHandle h_outer);
+
+// One iteration of ssmp / er (GAGA/gaga/expander/ssmp.cu:82-145, er.cu:69-125; the naive
+// forms, ssmp.cu:235-295 and er.cu:186-225, score every node each iteration instead of the
+// neighbours of the node updated): the node of the largest score, its update, ssmp's
+// periodic H_k with a fresh residual (an IF node, h_if, when s_if is a capture stream), the
+// rescoring, ||res||, the stopping rules.  With h_if == 0 (eager), the periodic step is left
+// to the caller.
+static gb_status enq_seq_body(SolvePlan &P, cudaStream_t s, cudaStream_t s_if, cudaGraphConditionalHandle h_outer,
+                              bool graph) {
+  GbWork &w = *P.w;
+  const int n = argN(w), m = argM(w), d = w.op.d;
+  const bool er = P.alg == GB_ALG_ER || P.alg == GB_ALG_ER_NAIVE;
+  const bool naive = P.alg == GB_ALG_SSMP_NAIVE || P.alg == GB_ALG_ER_NAIVE;
+  const int ier = er ? 1 : 0;
+  if (naive) enq_seq_scores(P, s);
+  k_seq_argmax<<<w.red_blocks, 256, 0, s>>>(w.st, w.xt, n, w.red_part, w.tickets);
+  cudaGraphConditionalHandle h_if = 0;
+  if (graph && !er) GB_TRY(make_handle(s, &h_if));
+  k_seq_node<<<1, 32, 0, s>>>(w.st, w.x, w.resid, w.op.smv_rows, w.op.smv_vals, w.grad, d, h_if);
+  if (graph && !er) {
+    // ssmp: every k-th iteration H_k(x) and res = y - A x (ssmp.cu:102-110)
+    GB_TRY(open_cond(s, s_if, h_if, cudaGraphCondTypeIf));
+    enq_expander_hk(P, s_if, w.x, P.k);
+    enq_A(w, s_if, w.x, w.resid, w.y, -1, F_ALWAYS);
+    if (!naive) enq_seq_scores(P, s_if);
+    GB_TRY(close_while(s_if));
+  }
+  if (!naive)
+    k_seq_rescore<<<d, 128, 0, s>>>(w.st, ier, w.resid, w.op.smv_rows, w.op.csr_ptr, w.op.csr_col, d, w.grad, w.xt);
+  if (graph) enq_seq_tail(P, s, h_outer);
+  (void)m;
+  return GB_OK;
+}
+
+// ||res|| and the stopping rules of one ssmp / er iteration
+static void enq_seq_tail(SolvePlan &P, cudaStream_t s, cudaGraphConditionalHandle h_outer) {
+  GbWork &w = *P.w;
+  k_copy_norm<<<w.red_blocks, 256, 0, s>>>(w.st, F_ALWAYS, w.resid, nullptr, argM(w), R_RES, -1, w.red_part,
+                                           w.tickets);
+  k_ctrl_l0<<<1, 32, 0, s>>>(w.st, C_SEQ_STOP, w.rec, h_outer);
+}
+
+// ssmp's final H_k after the loop (ssmp.cu:146-148)
+static void enq_seq_final(SolvePlan &P, cudaStream_t s) {
+  GbWork &w = *P.w;
+  if (P.alg != GB_ALG_SSMP && P.alg != GB_ALG_SSMP_NAIVE) return;
+  k_ctrl_l0<<<1, 32, 0, s>>>(w.st, C_SEQ_END1, w.rec, 0);
+  enq_expander_hk(P, s, w.x, P.k);
+  k_ctrl_l0<<<1, 32, 0, s>>>(w.st, C_SEQ_END2, w.rec, 0);
+}
+
 // smp loop (GAGA/gaga/expander/smp.cu:67-131)
 static void enq_smp_body(SolvePlan &P, cudaStream_t s, cudaGraphConditionalHandle h_outer) {
   GbWork &w = *P.w;
@@ -1021,6 +1289,13 @@ void enq_prologue(SolvePlan &P, cudaStream_t s0, cudaGraphConditionalHandle h_ou
     // res = y - A x^0 (smp.cu:45-48)
     enq_A(w, s0, w.x, w.resid, w.y, R_RES, F_ALWAYS);
     k_ctrl_l0<<<1, 32, 0, s0>>>(w.st, C_SMP_INIT, w.rec, h_outer);
+    return;
+  }
+  if (gb_is_seq(P.alg)) {
+    // res = y - A x^0, err, the first scores (ssmp.cu:56-75, er.cu:43-61)
+    enq_A(w, s0, w.x, w.resid, w.y, R_RES, F_ALWAYS);
+    k_ctrl_l0<<<1, 32, 0, s0>>>(w.st, C_SEQ_INIT, w.rec, h_outer);
+    enq_seq_scores(P, s0);
     return;
   }
   if (gb_is_l0(P.alg)) {
@@ -1261,6 +1536,15 @@ static gb_status build_graph(SolvePlan &P, cudaStream_t s0, cudaStream_t s1, cud
   cudaGraphConditionalHandle h_outer = 0, h_inner = 0;
   GB_TRY(make_handle(s0, &h_outer));
   enq_prologue(P, s0, h_outer);
+  if (gb_is_seq(P.alg)) {
+    // WHILE(outer) { argmax; node update; IF(periodic) { H_k; res }; rescore; stop }; final H_k
+    GB_TRY(open_while(s0, s1, h_outer));
+    GB_TRY(enq_seq_body(P, s1, s2, h_outer, true));
+    GB_TRY(close_while(s1));
+    enq_seq_final(P, s0);
+    GB_CUDA_TRY(cudaStreamEndCapture(s0, graph));
+    return GB_OK;
+  }
   if (P.alg == GB_ALG_CSMPSP) {
     // first projection, then WHILE(outer) { join; WHILE(CG) { step }; rebin; stop }
     cudaGraphConditionalHandle h_first = 0;
@@ -1320,6 +1604,25 @@ static gb_status run_cg_eager(SolvePlan &P, cudaStream_t s, int stop_phase) {
 static gb_status run_eager(SolvePlan &P, cudaStream_t s) {
   GbWork &w = *P.w;
   enq_prologue(P, s, 0);
+  if (gb_is_seq(P.alg)) {
+    const bool naive = P.alg == GB_ALG_SSMP_NAIVE || P.alg == GB_ALG_ER_NAIVE;
+    int active = 0, guard = 0, periodic = 0;
+    GB_TRY(read_int(&w.st->active, &active, s));
+    while (active && guard++ <= w.op.n + 4 + 100000) {
+      GB_TRY(enq_seq_body(P, s, s, 0, false));
+      GB_TRY(read_int(&w.st->periodic, &periodic, s));
+      if (periodic) {
+        enq_expander_hk(P, s, w.x, P.k);
+        enq_A(w, s, w.x, w.resid, w.y, -1, F_ALWAYS);
+        if (!naive) enq_seq_scores(P, s);
+      }
+      enq_seq_tail(P, s, 0);
+      GB_TRY(read_int(&w.st->active, &active, s));
+    }
+    enq_seq_final(P, s);
+    GB_CUDA_TRY(cudaGetLastError());
+    return GB_OK;
+  }
   if (P.alg == GB_ALG_CSMPSP) {
     GB_TRY(run_cg_eager(P, s, C_HTP_CG3));
     enq_ctrl(w, s, C_CSMPSP_INIT_DONE, 0);
@@ -1408,7 +1711,8 @@ static GbState initial_state(const GbWork &w, int alg, const gb_options &o, int 
 // Runs one solve on the prepared workspace (x zero, y uploaded); results stay in GbState.
 gb_status gb_run_solver(GbWork &w, int alg, const gb_options &o, int k, cudaStream_t s, float tol_abs) {
   if (gb_is_l0(alg) && (w.op.d <= 0 || 2 * w.op.d > 64)) return GB_UNSUPPORTED;
-  if (alg == GB_ALG_SMP && (w.op.d <= 0 || w.op.d > 32)) return GB_UNSUPPORTED;
+  if ((alg == GB_ALG_SMP || gb_is_seq(alg)) && (w.op.d <= 0 || w.op.d > 32)) return GB_UNSUPPORTED;
+  if (gb_is_seq(alg) && k < 1) return GB_BAD_ARG;
   GbState init = initial_state(w, alg, o, k, tol_abs);
   k_init_state<<<1, 1, 0, s>>>(w.st, init);
   GB_CUDA_TRY(cudaGetLastError());

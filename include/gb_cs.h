@@ -45,11 +45,12 @@ enum { GB_HOST = 0, GB_DEVICE = 1 };
 
 /* Reference algorithm numbers (GAGA/gaga/gaga_gen.cu:619-631, gaga_smv.cu:841-857):
  * "NIHT", "HTP", "IHT", "ThresholdSD", "ThresholdCG", "CSMPSP", "CGIHT", "FIHT", "ALPS",
- * "CGIHTprojected"; expander decoders "smp", "parallel_lddsr", "parallel_l0", "parallel_l0_swipe". */
+ * "CGIHTprojected"; expander decoders "smp", "ssmp", "er", "parallel_lddsr", "parallel_l0",
+ * "er_naive", "ssmp_naive", "parallel_l0_swipe". */
 enum { GB_ALG_NIHT = 0, GB_ALG_HTP = 1, GB_ALG_IHT = 2, GB_ALG_HT_SD = 3, GB_ALG_HT_CG = 4, GB_ALG_CSMPSP = 5,
        GB_ALG_CGIHT = 6, GB_ALG_FIHT = 7, GB_ALG_ALPS = 8, GB_ALG_CGIHT_PROJ = 9, GB_ALG_SMP = 10,
-       GB_ALG_PARALLEL_LDDSR = 13,
-       GB_ALG_PARALLEL_L0 = 14, GB_ALG_PARALLEL_L0_SWIPE = 18 };
+       GB_ALG_SSMP = 11, GB_ALG_ER = 12, GB_ALG_PARALLEL_LDDSR = 13,
+       GB_ALG_PARALLEL_L0 = 14, GB_ALG_ER_NAIVE = 16, GB_ALG_SSMP_NAIVE = 17, GB_ALG_PARALLEL_L0_SWIPE = 18 };
 
 /* Options: the gagaOptions name/value list (GAGA/gaga/gagaOptions.m:8-58) as a struct. */
 typedef struct {

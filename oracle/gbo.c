@@ -1327,6 +1327,143 @@ int gbo_smp(const gbo_op *op, const float *y, int k, const gbo_opts *o, float *x
   return 0;
 }
 
+/* Node score of ssmp (median) or er (mode and its run length), cuda_compute_scores_ssmp /
+ * cuda_compute_scores_er (GAGA/gaga/expander/kernels.cu:115-145, 195-245): bubble sort of
+ * the node's d residual entries; ssmp: median, score |median|; er: the value before the first
+ * longest run of neighbours within 1e-7, score its run length (0 if |mode| <= 1e-7). */
+static void seq_score(int er, const float *res, const int *rows_j, int d, float *upd, float *score) {
+  float b[64];
+  for (int i = 0; i < d; ++i) b[i] = res[rows_j[i]];
+  for (int i = 0; i < d; ++i)
+    for (int q = 0; q < d - 1; ++q)
+      if (b[q] > b[q + 1]) {
+        float t = b[q + 1];
+        b[q + 1] = b[q];
+        b[q] = t;
+      }
+  if (!er) {
+    float z = (d % 2) == 0 ? (b[d / 2 - 1] + b[d / 2]) / 2 : b[(d - 1) / 2];
+    *upd = z;
+    *score = fabsf(z);
+  } else {
+    const float eps = 0.0000001f;
+    float mode = b[0], count = 1.0f, count_mode = 1.0f;
+    for (int i = 1; i < d; ++i) {
+      if (fabsf(b[i] - b[i - 1]) <= eps) {
+        count = count + 1.0f;
+        if (count > count_mode) {
+          count_mode = count;
+          mode = b[i - 1];
+        }
+      } else {
+        count = 1.0f;
+      }
+    }
+    *upd = mode;
+    *score = fabsf(mode) > eps ? count_mode : 0.0f;
+  }
+}
+
+/* ssmp and er, sequential: one node per iteration (GAGA/gaga/expander/ssmp.cu:9-160, er.cu:9-137;
+ * variant 0 ssmp, 1 er, 2 ssmp_naive, 3 er_naive).  The node is the first of the largest
+ * score (cublasIsamax), x_h += update_h, res -= update_h A_h (one fused multiply-add per row),
+ * and the scores of the nodes sharing a row with h are recomputed (the naive forms recompute
+ * all scores each iteration: the same values).  ssmp takes H_k(x) and a fresh residual every
+ * k-th iteration and once after the loop; its loop stops on the residual history, er's on
+ * a residual cycling between two values over the last 2d iterations (er_naive: no cycle test).
+ * x and res: x^0 and scratch on entry. */
+int gbo_seq_decode(const gbo_op *op, const float *y, int k, const gbo_opts *o, int variant, float *x, float *res,
+                   float *res_record, gbo_info *info) {
+  const int m = op->m, n = op->n, d = op->d;
+  const int er = variant & 1, naive = variant >> 1;
+  const int *rows = op->smv_rows;
+  const float *vals = op->smv_vals;
+  if (d < 1 || d > 64 || k < 1) return -1;
+  /* row -> columns, ascending (create_row_index, kernels.cu:44-70) */
+  int *ptr = (int *)calloc((size_t)m + 1, sizeof(int));
+  int *col = (int *)malloc(sizeof(int) * (size_t)n * d);
+  for (size_t e = 0; e < (size_t)n * d; ++e) ptr[rows[e] + 1]++;
+  for (int i = 0; i < m; ++i) ptr[i + 1] += ptr[i];
+  int *fill = (int *)malloc(sizeof(int) * (size_t)m);
+  memcpy(fill, ptr, sizeof(int) * (size_t)m);
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < d; ++i) col[fill[rows[(size_t)j * d + i]]++] = j;
+  float *ax = (float *)malloc(sizeof(float) * m);
+  float *upd = (float *)calloc((size_t)n, sizeof(float));
+  float *score = (float *)calloc((size_t)n, sizeof(float));
+  int *bins = (int *)calloc((size_t)n, sizeof(int));
+  int *counters = (int *)calloc((size_t)o->num_bins, sizeof(int));
+  gbo_A(op, x, ax);
+  for (int i = 0; i < m; ++i) res[i] = fmaf(-1.0f, ax[i], y[i]);
+  float err = nrm2f(res, m), err_start = err;
+  if (res_record) res_record[0] = err;
+  float prev[16], evol[16], diff = 1.0f, cyc[128];
+  const int L = 2 * d;
+  for (int i = 0; i < 16; ++i) { prev[i] = 0.0f; evol[i] = 1.0f; }
+  for (int i = 0; i < L; ++i) cyc[i] = 0.0f;
+  for (int j = 0; j < n; ++j) seq_score(er, res, rows + (size_t)j * d, d, &upd[j], &score[j]);
+  int iter = 0, cycling = 0;
+  while ((iter < o->maxiter) & (err > o->tol) & (err < (100.0f * err_start)) &
+         (er ? (cycling == 0) : ((double)diff > 0.01 * (double)o->tol))) {
+    if (naive)
+      for (int j = 0; j < n; ++j) seq_score(er, res, rows + (size_t)j * d, d, &upd[j], &score[j]);
+    int h = 0;
+    float best = fabsf(score[0]);
+    for (int j = 1; j < n; ++j)
+      if (fabsf(score[j]) > best) {
+        best = fabsf(score[j]);
+        h = j;
+      }
+    const float u = upd[h];
+    x[h] = x[h] + u;
+    if (!er && (iter % k == 0) && (iter > 0)) {
+      expander_hk(x, k, n, o->num_bins, bins, counters);
+      gbo_A(op, x, ax);
+      for (int i = 0; i < m; ++i) res[i] = fmaf(-1.0f, ax[i], y[i]);
+      if (!naive)
+        for (int j = 0; j < n; ++j) seq_score(er, res, rows + (size_t)j * d, d, &upd[j], &score[j]);
+    } else {
+      for (int i = 0; i < d; ++i) {
+        const size_t e = (size_t)h * d + i;
+        res[rows[e]] = fmaf(-u, vals[e], res[rows[e]]);
+      }
+      if (!naive)
+        for (int i = 0; i < d; ++i) {
+          const int r = rows[(size_t)h * d + i];
+          for (int e = ptr[r]; e < ptr[r + 1]; ++e) {
+            const int j = col[e];
+            seq_score(er, res, rows + (size_t)j * d, d, &upd[j], &score[j]);
+          }
+        }
+    }
+    err = nrm2f(res, m);
+    if (er) {
+      iter++;
+      for (int i = 0; i < L - 1; ++i) cyc[i] = cyc[i + 1];
+      cyc[L - 1] = err;
+      if (!naive && iter > L) {
+        cycling = 1;
+        for (int i = 3; i < L; i += 2) cycling = cycling * (cyc[i] == cyc[i - 2]);
+      }
+    } else {
+      push16(prev, err);
+      for (int i = 0; i < 15; ++i) evol[i] = evol[i + 1];
+      evol[15] = prev[14] - prev[15];
+      diff = max_list(evol, 16);
+      iter++;
+    }
+    if (res_record) res_record[iter] = err;
+  }
+  if (!er) expander_hk(x, k, n, o->num_bins, bins, counters);
+  if (info) {
+    memset(info, 0, sizeof(*info));
+    info->iter = iter;
+    memcpy(info->resid_prev, prev, sizeof(prev));
+  }
+  free(ptr); free(col); free(fill); free(ax); free(upd); free(score); free(bins); free(counters);
+  return 0;
+}
+
 /* serial_l0 (GAGA/gaga/expander/serial_l0.cu:16-161): Gauss-Seidel, the residual is
  * updated as soon as a column is accepted.  res must hold y - A x on entry. */
 int gbo_serial_l0(const gbo_op *op, const float *y, const gbo_opts *o, float *x, float *res,

@@ -121,6 +121,9 @@ float gbo_max_magnitude(const float *v, int n);
 /* smp (GAGA/gaga/expander/smp.cu); res_record as for parallel_l0 */
 int gbo_smp(const gbo_op *op, const float *y, int k, const gbo_opts *o, float *x, float *res, float *res_record,
             gbo_info *info);
+/* ssmp / er and their naive forms (variant 0 ssmp, 1 er, 2 ssmp_naive, 3 er_naive) */
+int gbo_seq_decode(const gbo_op *op, const float *y, int k, const gbo_opts *o, int variant, float *x, float *res,
+                   float *res_record, gbo_info *info);
 int gbo_solve(const gbo_op *op, const float *y, int k, const gbo_opts *o, float *x, gbo_info *info);
 /* parallel_l0 / serial_l0 write res_record (maxiter+1 entries, may be NULL) */
 int gbo_parallel_l0(const gbo_op *op, const float *y, const gbo_opts *o, float *x, float *res,

@@ -72,6 +72,7 @@ def _declare(L):
         "gbo_parallel_l0": (i, [vp, vp, vp, vp, vp, vp, vp]),
         "gbo_serial_l0": (i, [vp, vp, vp, vp, vp, vp, vp]),
         "gbo_smp": (i, [vp, vp, i, vp, vp, vp, vp, vp]),
+        "gbo_seq_decode": (i, [vp, vp, i, vp, i, vp, vp, vp, vp]),
         "gbo_l0_scores": (None, [vp, vp, vp, vp, i, i, i, i, vp]),
         "gbo_l0_update_residual": (None, [vp, vp, vp, i, i]),
         "gbo_results": (None, [vp, vp, i, i, vp, vp]),
@@ -240,6 +241,24 @@ def smp(op, y, k, tol, maxiter, num_bins=None):
     o = GboOpts(SMP, tol, maxiter, num_bins or default_num_bins(op.n), 0, 1, 0)
     info = GboInfo()
     lib().gbo_smp(C.byref(op.c), _p(y), int(k), C.byref(o), _p(x), _p(res), _p(rec), C.byref(info))
+    return x, res, rec, info
+
+
+SEQ_VARIANTS = {"ssmp": 0, "er": 1, "ssmp_naive": 2, "er_naive": 3}
+
+
+def seq_decode(alg, op, y, k, tol, maxiter, num_bins=None):
+    """The sequential expander decoders ssmp, er, ssmp_naive, er_naive."""
+    y = f32(y)
+    x = np.zeros(op.n, dtype=np.float32)
+    res = np.zeros(op.m, dtype=np.float32)
+    rec = np.zeros(maxiter + 1, dtype=np.float32)
+    o = GboOpts(0, tol, maxiter, num_bins or default_num_bins(op.n), 0, 1, 0)
+    info = GboInfo()
+    rc = lib().gbo_seq_decode(C.byref(op.c), _p(y), int(k), C.byref(o), SEQ_VARIANTS[alg], _p(x), _p(res), _p(rec),
+                              C.byref(info))
+    if rc != 0:
+        raise ValueError("gbo_seq_decode: unsupported arguments")
     return x, res, rec, info
 
 

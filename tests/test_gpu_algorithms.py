@@ -124,3 +124,60 @@ def test_smp_bit_exact(gb, gbo, n, m, k):
     assert np.array_equal(np.asarray(rec)[: iters + 1], reco[: iters + 1])
     if k == 40:
         assert np.array_equal(xo, x0)
+
+
+SEQ = ["ssmp", "er", "ssmp_naive", "er_naive"]
+
+
+@pytest.mark.parametrize("alg", SEQ)
+@pytest.mark.parametrize("n,m,k", [(2 ** 14, 2 ** 12, 40), (2 ** 14, 2 ** 12, 204), (2 ** 18, 2 ** 16, 300)])
+def test_sequential_decoders_bit_exact(gb, gbo, alg, n, m, k):
+    """ssmp / er (one node per iteration: argmax of the scores, node update, rescoring of the
+    node's neighbours; ssmp's periodic H_k) on the unit-valued expander with a +-1 signal:
+    integer residuals, so x, the iteration count and the residual record equal the oracle's."""
+    if alg.endswith("_naive") and n > 2 ** 14:
+        pytest.skip("the oracle's naive form rescores every node each iteration")
+    d = 7
+    rows, vals = gbo.gen_smv(m, n, d, 3, seed=33)
+    x0, ks = gbo.gen_vector(n, k, 1, seed=33)
+    op = gbo.Op.smv(m, n, d, rows, vals)
+    y = gbo.A(op, x0)
+    cols = np.repeat(np.arange(n, dtype=np.int32), d)
+    maxiter = 4 * k
+    opts = gb.gaga_options("tol", 1e-6, "maxiter", maxiter)
+    x, iters, conv, rec, trec = gb.gaga_cs(alg, "smv", y, rows, cols, vals, ks, opts, index_base=0)
+    xo, reso, reco, info = gbo.seq_decode(alg, op, y, ks, 1e-6, maxiter)
+    assert iters == info.iter
+    assert np.array_equal(np.asarray(x), xo)
+    assert np.array_equal(np.asarray(rec)[: iters + 1], reco[: iters + 1])
+    if k == 40:
+        assert np.array_equal(xo, x0)
+
+
+@pytest.mark.parametrize("alg", ["ssmp", "er"])
+def test_sequential_decoders_scaled_expander(gb, gbo, alg):
+    """On the 1/sqrt(d)-valued expander with a Gaussian signal the residuals are not integers:
+    same verdict as the oracle, and the decoded x within 1e-5 of the oracle's."""
+    n, m, d, k = 2 ** 14, 2 ** 12, 7, 60
+    rows, vals = gbo.gen_smv(m, n, d, 1, seed=34)
+    x0, ks = gbo.gen_vector(n, k, 2, seed=34)
+    op = gbo.Op.smv(m, n, d, rows, vals)
+    y = gbo.A(op, x0)
+    cols = np.repeat(np.arange(n, dtype=np.int32), d)
+    tol = 1e-5 * float(np.linalg.norm(y))
+    opts = gb.gaga_options("tol", tol, "maxiter", 2000)
+    x, iters, conv, rec, trec = gb.gaga_cs(alg, "smv", y, rows, cols, vals, ks, opts, index_base=0)
+    xo, reso, reco, info = gbo.seq_decode(alg, op, y, ks, tol, 2000)
+    x = np.asarray(x)
+    ok_g = np.linalg.norm(x - x0) / np.linalg.norm(x0) <= 1e-3
+    ok_o = np.linalg.norm(xo - x0) / np.linalg.norm(x0) <= 1e-3
+    assert ok_g == ok_o
+    assert np.linalg.norm(x - xo) <= 1e-5 * max(1.0, float(np.linalg.norm(xo)))
+
+
+def test_sequential_generate_and_solve(gb):
+    """The generate-and-solve usage takes the ssmp / er strings (gaga_smv.cu:842-848)."""
+    for alg in SEQ:
+        opts = gb.gaga_options("tol", 1e-6, "seed", 9, "maxiter", 400)
+        out = gb.gaga_cs(alg, "smv", 30, 1024, 4096, 7, opts)
+        assert out[0][1] < 1e-3 and out[2] > 0, alg

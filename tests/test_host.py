@@ -53,8 +53,9 @@ def test_default_options_mirror_reference(gb):
 def test_alg_ids(gb):
     L = gb._lib.load()
     names = (b"NIHT", b"HTP", b"IHT", b"ThresholdSD", b"ThresholdCG", b"CSMPSP", b"CGIHT", b"FIHT", b"ALPS",
-             b"CGIHTprojected", b"smp", b"parallel_lddsr", b"parallel_l0", b"parallel_l0_swipe", b"ALPS2")
-    assert [L.gb_cs_alg_id(a) for a in names] == [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 13, 14, 18, -1]
+             b"CGIHTprojected", b"smp", b"ssmp", b"er", b"parallel_lddsr", b"parallel_l0", b"er_naive",
+             b"ssmp_naive", b"parallel_l0_swipe", b"ALPS2")
+    assert [L.gb_cs_alg_id(a) for a in names] == [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 16, 17, 18, -1]
 
 
 def test_bad_arguments_rejected_before_device_work(gb):

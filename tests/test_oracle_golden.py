@@ -151,3 +151,19 @@ def test_oracle_timing_variants_recover(gbo, alg, supp_flag):
     y = gbo.A(op, x0)
     x, info = gbo.solve(alg, op, y, ks, 1e-5 * float(np.linalg.norm(y)), timing=1, supp_flag=supp_flag)
     assert np.linalg.norm(x - x0) / np.linalg.norm(x0) < 1e-3 and info.iter > 0
+
+
+@pytest.mark.parametrize("alg", ["ssmp", "er", "ssmp_naive", "er_naive"])
+def test_oracle_sequential_decoders(gbo, alg):
+    """ssmp / er and their naive forms decode a +-1 signal on the unit expander exactly; the
+    naive forms (every score recomputed) follow the same path as the incremental ones."""
+    n, m, d, k = 2 ** 12, 2 ** 10, 7, 40
+    rows, vals = gbo.gen_smv(m, n, d, 3, seed=5)
+    x0, ks = gbo.gen_vector(n, k, 1, seed=5)
+    op = gbo.Op.smv(m, n, d, rows, vals)
+    y = gbo.A(op, x0)
+    x, res, rec, info = gbo.seq_decode(alg, op, y, ks, 1e-6, 2000)
+    assert np.array_equal(x, x0)
+    base = alg.replace("_naive", "")
+    xb, resb, recb, infob = gbo.seq_decode(base, op, y, ks, 1e-6, 2000)
+    assert info.iter == infob.iter and np.array_equal(rec, recb)
