@@ -182,14 +182,16 @@ def _solve(alg, kind, y, k, m, n, opts, ens, A=None, lda=0, rows=None, cols=None
         x = np.zeros(n, dtype=np.float32)
         xptr = x.ctypes.data
     r = _lib.Result()
-    rec = None
+    rec = trec = None
     if want_record:
         rec = np.zeros(o.maxiter + 1, dtype=np.float32)
+        trec = np.zeros(o.maxiter + 1, dtype=np.float32)
         r.res_record = rec.ctypes.data
+        r.time_record = trec.ctypes.data
     tb = _attach_timing(alg, o, r)
     _lib.check(L.gb_cs_solve(alg.encode(), C.byref(p), C.byref(o), C.c_void_p(xptr), C.byref(r)))
     _keep_timing(tb, r)
-    return x, r, rec
+    return x, r, (rec, trec)
 
 
 def _size(a):
@@ -241,9 +243,9 @@ def gaga_cs(alg, ens, *args, index_base=1, stream=None):
                 p_ += 1
             m = int(r_.max()) + 1 - index_base
             n = int(c.max()) + 1 - index_base
-            x, r, rec = _solve(alg, _lib.GB_OP_SMV, y, k, m, n, opts, ens, rows=rows, cols=cols, vals=vals, d=p_,
-                               index_base=index_base, want_record=True, stream=stream)
-            return x, r.iter, r.conv_rate, rec, np.zeros_like(rec)
+            x, r, (rec, trec) = _solve(alg, _lib.GB_OP_SMV, y, k, m, n, opts, ens, rows=rows, cols=cols, vals=vals,
+                                       d=p_, index_base=index_base, want_record=True, stream=stream)
+            return x, r.iter, r.conv_rate, rec, trec
         if len(args) in (4, 5):
             k, m, n, p_ = args[:4]
             return _generate(alg, _lib.GB_OP_SMV, k, m, n, p_, args[4] if len(args) == 5 else None, ens)
@@ -258,8 +260,10 @@ def _generate(alg, kind, k, m, n, d, opts, ens):
     xt = np.zeros(n, dtype=np.float32)
     r = _lib.Result()
     rec = np.zeros(o.maxiter + 1, dtype=np.float32) if kind == _lib.GB_OP_SMV else None
+    trec = np.zeros(o.maxiter + 1, dtype=np.float32) if kind == _lib.GB_OP_SMV else None
     if rec is not None:
         r.res_record = rec.ctypes.data
+        r.time_record = trec.ctypes.data
     tb = _attach_timing(alg, o, r)
     _lib.check(L.gb_cs_generate_and_solve(alg.encode(), kind, int(k), int(m), int(n), int(d), C.byref(o),
                                           C.c_void_p(x.ctypes.data), C.c_void_p(xt.ctypes.data), C.byref(r)))
@@ -269,7 +273,7 @@ def _generate(alg, kind, k, m, n, d, opts, ens):
     support = np.array(r.support, dtype=np.int32)
     out = (norms, times, np.int32(r.iter), support, np.float32(r.conv_rate), x)
     if kind == _lib.GB_OP_SMV:
-        out = out + (rec, np.zeros_like(rec))
+        out = out + (rec, trec)
     return out
 
 

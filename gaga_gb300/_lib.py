@@ -48,7 +48,7 @@ class Result(C.Structure):
                 ("support", C.c_int * 4), ("k_used", C.c_int), ("resid_prev", C.c_float * 16),
                 ("stop_reason", C.c_int), ("res_record", C.c_void_p), ("warm_start", C.c_int),
                 ("time_per_iteration", C.c_void_p), ("time_supp_set", C.c_void_p),
-                ("cg_per_iteration", C.c_void_p), ("time_for_cg", C.c_void_p)]
+                ("cg_per_iteration", C.c_void_p), ("time_for_cg", C.c_void_p), ("time_record", C.c_void_p)]
 
 
 class BinState(C.Structure):

@@ -307,8 +307,9 @@ bool timing_applies(const gb_options &o, int alg_id) {
   return o.timing && (alg_id == GB_ALG_NIHT || alg_id == GB_ALG_HTP);
 }
 
-// stamp buffers of the timing variants
+// stamp buffers of the timing variants and of the expander decoders' time record
 gb_status alloc_timing(DeviceBuffers &db, GbWork &w, const gb_options &o, int alg_id) {
+  if (gb_is_ccs(alg_id)) GB_TRY(db.alloc(&w.tlog, (size_t)std::max(o.maxiter, 0) + 1));
   if (!timing_applies(o, alg_id) || o.maxiter <= 0) return GB_OK;
   GB_TRY(db.alloc(&w.tstamp, (size_t)o.maxiter * GB_NSTAMP));
   GB_TRY(db.alloc(&w.tcg, (size_t)o.maxiter));
@@ -357,11 +358,23 @@ void put_timing(const TimingRecord &t, gb_result *r, int iters) {
   r->times[1] = iters > 0 ? t.sum / (float)iters : 0.0f;
 }
 
+// timeRecord of the expander decoders: ms from the loop start to the end of each iteration
+gb_status put_time_record(const GbWork &w, int iters, int maxiter, float *out) {
+  if (!out || !w.tlog) return GB_OK;
+  const int n = std::min(std::max(iters, 0), maxiter);
+  std::vector<unsigned long long> t((size_t)n + 1);
+  GB_CUDA_TRY(cudaMemcpy(t.data(), w.tlog, sizeof(unsigned long long) * t.size(), cudaMemcpyDeviceToHost));
+  memset(out, 0, sizeof(float) * ((size_t)maxiter + 1));
+  for (int j = 1; j <= n; ++j) out[j] = t[j] >= t[0] ? (float)((double)(t[j] - t[0]) * 1e-6) : 0.0f;
+  return GB_OK;
+}
+
 // a result's caller-owned pointers survive its reset
 void reset_result(gb_result *r) {
   float *rec = r->res_record, *a = r->time_per_iteration, *b = r->time_supp_set, *c = r->cg_per_iteration,
-        *d = r->time_for_cg;
+        *d = r->time_for_cg, *tr = r->time_record;
   memset(r, 0, sizeof(*r));
+  r->time_record = tr;
   r->res_record = rec;
   r->time_per_iteration = a;
   r->time_supp_set = b;
@@ -460,6 +473,7 @@ extern "C" gb_status gb_cs_solve(const char *alg, const gb_problem *p, const gb_
       // the last <= 16 residual records become residNorm_prev (gaga_smv.cu:1013-1020)
       for (int j = 0; j < std::min(st.iter, 16); ++j) r->resid_prev[15 - j] = rec[st.iter - j];
       if (user_rec) memcpy(user_rec, rec.data(), sizeof(float) * (o.maxiter + 1));
+      GB_TRY(put_time_record(w, st.iter, o.maxiter, r->time_record));
     } else {
       memcpy(r->resid_prev, st.prev, sizeof(st.prev));
     }
@@ -695,6 +709,7 @@ extern "C" gb_status gb_cs_generate_and_solve(const char *alg, int kind, int k, 
     if (gb_is_ccs(alg_id)) {
       for (int j = 0; j < std::min(st.iter, 16); ++j) r->resid_prev[15 - j] = rec[st.iter - j];
       if (user_rec) memcpy(user_rec, rec.data(), sizeof(float) * (o.maxiter + 1));
+      GB_TRY(put_time_record(w, st.iter, o.maxiter, r->time_record));
     } else {
       memcpy(r->resid_prev, st.prev, sizeof(st.prev));
     }

@@ -94,6 +94,9 @@ struct GbState {
   // sequential decoders: the node picked this iteration, whether ssmp takes its periodic
   // H_k step this iteration
   int h_node, periodic;
+  // expander decoders: global-timer stamp at the loop start (entry 0) and at the end of each
+  // iteration (entry iter), for their cumulative time record; null when not recorded
+  unsigned long long *tlog;
 };
 
 // Operator description on the device.
@@ -134,6 +137,7 @@ struct GbWork {
   unsigned int *sel_hist;    // timing variants: radix-select histograms (3 x GB_SEL_BINS, kept zero)
   unsigned long long *tstamp;  // timing variants: GB_NSTAMP global-timer stamps per iteration (or null)
   int *tcg;                  // timing variants: CG steps per iteration (HTP)
+  unsigned long long *tlog;  // expander decoders: loop start + per-iteration end stamps (maxiter + 1)
   GbOp op;          // dimensions here are capacities when dyn is set
   int dyn;          // 1: kernels read m, n, lda, num_bins, k of the current trial from GbState
   const float *ml_params;    // learned warm start: MLP parameters (null: plain start)

@@ -20,9 +20,20 @@ __global__ void k_ctrl(GbState *st, int phase, cudaGraphConditionalHandle h) {
 }
 
 // ------------------------------------------------------------------ l0 control
+// the time record of the expander decoders (timeRecord of GAGA/gaga/expander/*.cu): the
+// global timer when the loop starts and as each iteration ends
+__device__ __forceinline__ void tlog_mark(GbState *st) {
+  if (st->tlog && st->iter >= 0 && st->iter <= st->maxiter) {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    st->tlog[st->iter] = t;
+  }
+}
+
 __global__ void k_ctrl_l0(GbState *st, int phase, float *rec, cudaGraphConditionalHandle h) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const int L = st->l0_len;
+  const int iter0 = st->iter;
   switch (phase) {
     case C_L0_INIT:
       // parallel_l0 (GAGA/gaga/expander/parallel_l0.cu:31-60)
@@ -215,6 +226,8 @@ __global__ void k_ctrl_l0(GbState *st, int phase, float *rec, cudaGraphCondition
       set_cond(h, st->active ? 1u : 0u);
       break;
   }
+  // the loop start, and each finished iteration
+  if (phase == C_L0_INIT || phase == C_SMP_INIT || phase == C_SEQ_INIT || st->iter != iter0) tlog_mark(st);
 }
 
 // ------------------------------------------------------------------ vector kernels
@@ -1697,6 +1710,7 @@ static GbState initial_state(const GbWork &w, int alg, const gb_options &o, int 
   st.flags[F_ALWAYS] = 1;
   st.op_kind = w.op.kind;
   st.learned = (w.ml_params && alg == GB_ALG_CGIHT) ? 1 : 0;
+  st.tlog = w.tlog;
   // timing variants (NIHT, HTP only; gaga_gen.cu:331-334): alpha from the options
   // (algorithms_timings.cu:477), supportFlag
   if (o.timing && (alg == GB_ALG_NIHT || alg == GB_ALG_HTP)) {

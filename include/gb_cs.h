@@ -120,6 +120,9 @@ typedef struct {
   float *time_supp_set;
   float *cg_per_iteration;
   float *time_for_cg;
+  float *time_record;   /* expander decoders: caller buffer of maxiter+1 floats or NULL
+                           (timeRecord): ms from the loop start to the end of each iteration,
+                           0 at entry 0, from device timer stamps */
 } gb_result;
 
 /* Support-selection state carried between FindSupportSet calls. */

@@ -181,3 +181,21 @@ def test_sequential_generate_and_solve(gb):
         opts = gb.gaga_options("tol", 1e-6, "seed", 9, "maxiter", 400)
         out = gb.gaga_cs(alg, "smv", 30, 1024, 4096, 7, opts)
         assert out[0][1] < 1e-3 and out[2] > 0, alg
+
+
+@pytest.mark.parametrize("alg", ["parallel_l0", "smp", "ssmp", "er"])
+def test_decoder_time_record(gb, gbo, alg):
+    """timeRecord of the expander decoders: 0 at entry 0, then the cumulative ms to the end of
+    each iteration (non-decreasing, growing overall), 0 past the last iteration."""
+    n, m, d, k = 2 ** 14, 2 ** 12, 7, 60
+    rows, vals = gbo.gen_smv(m, n, d, 3, seed=35)
+    x0, ks = gbo.gen_vector(n, k, 1, seed=35)
+    op = gbo.Op.smv(m, n, d, rows, vals)
+    y = gbo.A(op, x0)
+    cols = np.repeat(np.arange(n, dtype=np.int32), d)
+    opts = gb.gaga_options("tol", 1e-6, "maxiter", 500)
+    x, iters, conv, rec, trec = gb.gaga_cs(alg, "smv", y, rows, cols, vals, ks, opts, index_base=0)
+    trec = np.asarray(trec)
+    assert iters > 0 and trec[0] == 0.0
+    assert np.all(np.diff(trec[: iters + 1]) >= 0) and trec[iters] > 0
+    assert np.all(trec[iters + 1:] == 0.0)
