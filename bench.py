@@ -355,10 +355,19 @@ def gemm_roofline(tpeak, tpeak_kind, M=4096, N=1024, K=3 * 8192, reps=10):
     ach = 2.0 * M * N * K / t / 1e12
     del A, B, Y
     torch.cuda.empty_cache()
-    kern = "k_gemm_tn_mma (mma.sync)" if os.environ.get("GB_CS_GEMM") == "mma" else "k_gemm_tn_tc (tcgen05 + TMA)"
-    return {"bound": "tensor", "achieved": ach, "peak": tpeak, "unit": "TFLOP/s", "frac": ach / tpeak,
-            "kernel": kern, "shape": "M=%d N=%d K=%d (bf16 in, fp32 accumulate, Y - AB^T epilogue)" % (
-                M, N, K), "us_per_launch": t * 1e6, "peak_source": tpeak_kind}
+    mma = os.environ.get("GB_CS_GEMM") == "mma"
+    kern = "k_gemm_tn_mma (mma.sync)" if mma else "k_gemm_tn_tc (tcgen05 + TMA)"
+    out = {"bound": "tensor", "achieved": ach, "peak": tpeak, "unit": "TFLOP/s", "frac": ach / tpeak,
+           "kernel": kern, "shape": "M=%d N=%d K=%d (bf16 in, fp32 accumulate, Y - AB^T epilogue)" % (
+               M, N, K), "us_per_launch": t * 1e6, "peak_source": tpeak_kind, "traffic": None}
+    key = "%s M=%d N=%d K=%d" % ("k_gemm_tn_mma" if mma else "k_gemm_tn_tc", M, N, K)
+    tr = ncu_traffic()
+    if key in tr:
+        out["traffic"] = tr[key]["read"] + tr[key]["write"]
+        out["traffic_unit"] = "bytes"
+        out["traffic_source"] = "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, same shape " \
+                                "(profiles/dram_traffic.json)"
+    return out
 
 
 def matvec_roofline(peak, peak_kind, m=14746, n=16384, k=5000, reps=20):
