@@ -286,6 +286,7 @@ def bench_ours(args):
     line["roofline"] = mv["at"]
     line["matvec"] = mv
     line["gemm"] = gemm_roofline(tpeak, tpeak_kind)
+    line["operators"] = operators_roofline(peak, peak_kind)
     if args.plain_trials > 0 and world == 1:
         line["plain"] = bench_plain(args, first_step)
         line["tuned_vs_plain"] = value / line["plain"]["value"] if line["plain"]["value"] else None
@@ -342,6 +343,7 @@ def gemm_roofline(tpeak, tpeak_kind, M=4096, N=1024, K=3 * 8192, reps=10):
     B = torch.randn(N, K, device="cuda", generator=g).to(torch.bfloat16)
     Y = torch.randn(N, M, device="cuda", generator=g)
     s = torch.cuda.Stream()
+    torch.cuda.synchronize()  # the operands come from torch's stream; s does not wait for it
     with torch.cuda.stream(s):
         for _ in range(3):
             gb.gemm_bf16_tn(A, B, Y=Y, want_bf16=True)
@@ -370,6 +372,69 @@ def gemm_roofline(tpeak, tpeak_kind, M=4096, N=1024, K=3 * 8192, reps=10):
     return out
 
 
+def operators_roofline(peak, peak_kind, reps=20):
+    """Every operator kernel at its workload's size with a cold L2 (a 256 MB buffer is
+    overwritten before each application, outside the CUDA events): the dense operator at the
+    single-trial NIHT size (n=4096, m=1024) and the sweep's largest trial, the subsampled DCT at
+    n=2^20, m=2^18 and the expander at n=2^18, m=2^16, d=7, and each of the last two also at
+    n=2^22 (working set well above L2).  Algorithmic bytes per
+    application: dense A^T r 4mn+4m+4n, A x 4mn+4n+4m; DCT A or A^T 4n+8m; expander A^T r
+    8nd+4m+4n, A x 8nd+4n+4m (rows+values, x, y)."""
+    import ctypes as C
+
+    import torch
+
+    import gaga_gb300 as gb
+    from gaga_gb300 import _lib
+
+    L = gb._lib.load()
+    g = torch.Generator(device="cuda").manual_seed(3)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.Stream()
+    out = {}
+
+    def one(name, p, m, n, tr, nbytes, what):
+        vin = torch.randn(m if tr else n, device="cuda", generator=g)
+        vout = torch.empty(n if tr else m, device="cuda")
+        torch.cuda.synchronize()  # the inputs come from torch's stream; s does not wait for it
+        p.stream = C.c_void_p(s.cuda_stream)
+        ms = C.c_float(0)
+        _lib.check(L.gb_cs_operator_time(C.byref(p), tr, vin.data_ptr(), vout.data_ptr(), 3, reps, flush.data_ptr(),
+                                         flush.numel(), C.byref(ms)))
+        t = ms.value / 1e3
+        ach = nbytes / t / 1e9
+        out[name] = {"achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "us_per_launch": t * 1e6,
+                     "shape": what, "bytes": nbytes, "l2": "cold (flushed before each application)",
+                     "peak_source": peak_kind}
+
+    for (m, n) in ((1024, 4096), (14746, 16384)):
+        lda = (m + 31) // 32 * 32  # the library's own layout: 128-byte aligned columns
+        A = torch.randn(n * lda, device="cuda", generator=g) / np.sqrt(m)
+        p = _lib.Problem(_lib.GB_OP_DENSE, m, n, 0, None, A.data_ptr(), lda, None, None, None, 0, 0, _lib.GB_DEVICE,
+                         None)
+        one("dense_at_n%d" % n, p, m, n, 1, 4.0 * m * n + 4 * m + 4 * n, "k_dense_at m=%d n=%d" % (m, n))
+        one("dense_ax_n%d" % n, p, m, n, 0, 4.0 * m * n + 4 * n + 4 * m, "k_dense_av m=%d n=%d, full x" % (m, n))
+        del A
+    for ln in (20, 22):
+        n, m = 2 ** ln, 2 ** (ln - 2)
+        rows = torch.randperm(n, device="cuda", generator=g)[:m].to(torch.int32)
+        p = _lib.Problem(_lib.GB_OP_DCT, m, n, 0, None, None, 0, rows.data_ptr(), None, None, 0, 0, _lib.GB_DEVICE,
+                         None)
+        one("dct_at_n2^%d" % ln, p, m, n, 1, 4.0 * n + 8 * m, "k_dct_scatter + 2 k_fft_pass, n=2^%d m=n/4" % ln)
+        one("dct_a_n2^%d" % ln, p, m, n, 0, 4.0 * n + 8 * m, "2 k_fft_pass + k_dct_select, n=2^%d m=n/4" % ln)
+    for ln in (18, 22):
+        n, m, d = 2 ** ln, 2 ** (ln - 2), 7
+        rows = torch.randint(0, m, (n * d,), device="cuda", generator=g, dtype=torch.int32)
+        vals = torch.full((n * d,), 1.0 / np.sqrt(d), device="cuda")
+        p = _lib.Problem(_lib.GB_OP_SMV, m, n, 0, None, None, 0, rows.data_ptr(), None, vals.data_ptr(), d, 0,
+                         _lib.GB_DEVICE, None)
+        one("smv_at_n2^%d" % ln, p, m, n, 1, 8.0 * n * d + 4 * m + 4 * n, "k_smv_AT n=2^%d m=n/4 d=7" % ln)
+        one("smv_a_n2^%d" % ln, p, m, n, 0, 8.0 * n * d + 4 * n + 4 * m, "k_smv_A n=2^%d m=n/4 d=7" % ln)
+    del flush
+    torch.cuda.empty_cache()
+    return out
+
+
 def matvec_roofline(peak, peak_kind, m=14746, n=16384, k=5000, reps=20):
     """Dense A^T r (k_dense_at, the dominant kernel) and A x_S (k_dense_av) on the sweep's
     largest trial shape, timed with CUDA events on the stream they run on."""
@@ -388,6 +453,7 @@ def matvec_roofline(peak, peak_kind, m=14746, n=16384, k=5000, reps=20):
     x[torch.randperm(n, device="cuda", generator=g)[:k]] = 1.0
     g_out, y_out = torch.empty(n, device="cuda"), torch.empty(m, device="cuda")
     s = torch.cuda.Stream()
+    torch.cuda.synchronize()  # the inputs come from torch's stream; s does not wait for it
     res = {}
     # A x_S is timed on a fixed support (transpose 2: the support scan of the first call is
     # reused), so the events bracket the k_dense_av launches alone
@@ -506,6 +572,8 @@ def bench_only(args):
         out = matvec_roofline(*peaks())
     elif args.only == "gemm":
         out = gemm_roofline(*tensor_peak())
+    elif args.only == "operators":
+        out = operators_roofline(*peaks())
     elif args.only == "learned":
         out = bench_learned(args)
     else:
@@ -532,7 +600,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--learned-trials", type=int, default=2048)
     ap.add_argument("--retune", action="store_true", help="ignore the autotuner's cache")
-    ap.add_argument("--only", choices=["matvec", "gemm", "plain", "learned"],
+    ap.add_argument("--only", choices=["matvec", "gemm", "operators", "plain", "learned"],
                     help="run one measurement alone and print its JSON (for profiling)")
     args = ap.parse_args()
     if args.warmup < 3:

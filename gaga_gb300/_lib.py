@@ -21,7 +21,7 @@ GB_ALG_FIHT, GB_ALG_ALPS, GB_ALG_CGIHT_PROJ, GB_ALG_PARALLEL_L0 = 7, 8, 9, 14
 # every symbol include/gb_cs.h declares
 EXPORTS = ["gb_cs_version", "gb_cs_last_error", "gb_cs_default_options", "gb_cs_alg_id", "gb_cs_solve",
            "gb_cs_generate_and_solve", "gb_cs_linear_binning", "gb_cs_find_support_set", "gb_cs_find_support_set_sort",
-           "gb_cs_operator_apply", "gb_cs_l0_step", "gb_cs_solve_batch", "gb_cs_batch_last_stats",
+           "gb_cs_operator_apply", "gb_cs_operator_time", "gb_cs_l0_step", "gb_cs_solve_batch", "gb_cs_batch_last_stats",
            "gb_cs_dense_apply_noalloc", "gb_cs_solve_shared_batch", "gb_cs_shared_last_stats",
            "gb_cs_gemm_bf16_tn", "gb_cs_mlp_num_params", "gb_cs_mlp_features", "gb_cs_mlp_forward",
            "gb_cs_mlp_grad", "gb_cs_mlp_train", "gb_cs_write_result"]
@@ -100,6 +100,8 @@ def load():
     L.gb_cs_find_support_set_sort.restype = i
     L.gb_cs_operator_apply.argtypes = [C.POINTER(Problem), i, vp, vp]
     L.gb_cs_operator_apply.restype = i
+    L.gb_cs_operator_time.argtypes = [C.POINTER(Problem), i, vp, vp, i, i, vp, C.c_size_t, C.POINTER(C.c_float)]
+    L.gb_cs_operator_time.restype = i
     L.gb_cs_l0_step.argtypes = [vp, vp, vp, vp, i, i, i, i, i, C.POINTER(C.c_int), vp]
     L.gb_cs_l0_step.restype = i
     L.gb_cs_solve_batch.argtypes = [C.POINTER(Batch), vp, vp, vp, C.POINTER(C.c_int)]

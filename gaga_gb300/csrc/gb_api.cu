@@ -943,6 +943,56 @@ extern "C" gb_status gb_cs_find_support_set(float *d_v, int n, int k, float slop
   return GB_OK;
 }
 
+// Device time of one operator application, set up once: each of `reps` applications is
+// bracketed by CUDA events on the problem's stream (after `warmup` untimed ones); with a
+// flush buffer, it is overwritten before each application so that every timed application
+// reads its operands from HBM, not L2.  *ms_out: mean ms per application.  For the dense
+// A x the support list of d_in is built once, outside the timed region.
+extern "C" gb_status gb_cs_operator_time(const gb_problem *p, int transpose, const float *d_in, float *d_out,
+                                         int warmup, int reps, void *d_flush, size_t flush_bytes, float *ms_out) {
+  if (!p || !d_in || !d_out || !ms_out || reps < 1 || warmup < 0) return bad("bad gb_cs_operator_time arguments");
+  if (p->location != GB_DEVICE) return bad("gb_cs_operator_time takes device buffers");
+  GB_TRY(select_device(0));
+  cudaStream_t s = (cudaStream_t)p->stream;
+  DeviceBuffers db;
+  GbWork w;
+  memset(&w, 0, sizeof(w));
+  GB_TRY(setup_problem(db, w, *p, s, 1, 0, false));
+  GbState st0;
+  memset(&st0, 0, sizeof(st0));
+  st0.active = 1;
+  st0.flags[F_ALWAYS] = 1;
+  GB_CUDA_TRY(cudaMemcpyAsync(w.st, &st0, sizeof(st0), cudaMemcpyHostToDevice, s));
+  if (transpose) GB_CUDA_TRY(cudaMemcpyAsync(w.resid, d_in, sizeof(float) * p->m, cudaMemcpyDeviceToDevice, s));
+  else if (w.op.kind == GB_OP_DENSE) enq_support_of_nonzeros(w, s, d_in, p->n);
+  cudaEvent_t e0, e1;
+  GB_CUDA_TRY(cudaEventCreate(&e0));
+  GB_CUDA_TRY(cudaEventCreate(&e1));
+  double total = 0.0;
+  gb_status rc = GB_OK;
+  for (int r = 0; r < warmup + reps && rc == GB_OK; ++r) {
+    if (d_flush && flush_bytes) cudaMemsetAsync(d_flush, r & 0xff, flush_bytes, s);
+    cudaEventRecord(e0, s);
+    if (transpose) enq_AT(w, s, w.resid, d_out, F_ALWAYS);
+    else enq_A(w, s, d_in, d_out, nullptr, -1, F_ALWAYS);
+    cudaEventRecord(e1, s);
+    cudaError_t e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      gb_set_error_message(cudaGetErrorString(e), __FILE__, __LINE__);
+      rc = GB_CUDA_ERROR;
+      break;
+    }
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (r >= warmup) total += ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc == GB_OK) *ms_out = (float)(total / reps);
+  return rc;
+}
+
 extern "C" gb_status gb_cs_operator_apply(const gb_problem *p, int transpose, const float *d_in, float *d_out) {
   if (!p || !d_in || !d_out) return bad("null argument");
   if (p->location != GB_DEVICE) return bad("gb_cs_operator_apply takes device buffers");

@@ -397,23 +397,63 @@ __global__ void k_dct_scatter(const GbState *st, int pf, const int *__restrict__
 }
 
 // ------------------------------------------------------------------ smv
-__global__ void k_smv_A(GbState *st, int pf, const int *__restrict__ ptr, const int *__restrict__ col,
-                        const float *__restrict__ val, int m, const float *__restrict__ v,
-                        const float *__restrict__ y, float *__restrict__ out, int slot, float *red_part,
-                        unsigned int *tickets) {
+// The expander A x stages each row group's entries through shared memory so that every
+// global read is a coalesced warp-wide read and the gathers of x are issued by the whole
+// warp at once; each lane then sums its own row in the fixed entry order (bit-identical to
+// a sequential per-row sum).
+#define SMV_WARPS 8
+#define SMV_CHUNK 256  // entries of a row group staged per warp and step
+
+// A x over the row-major copy (rows ascending, each row's columns ascending): a warp takes
+// 32 consecutive rows, reads their entry range in coalesced chunks, and lane r sums row r
+__global__ void __launch_bounds__(SMV_WARPS * 32) k_smv_A(GbState *st, int pf, const int *__restrict__ ptr,
+                                                          const int *__restrict__ col, const float *__restrict__ val,
+                                                          int m, const float *__restrict__ v,
+                                                          const float *__restrict__ y, float *__restrict__ out,
+                                                          int slot, float *red_part, unsigned int *tickets) {
   if (!gb_pred(st, pf)) return;
+  __shared__ float prod[SMV_WARPS][SMV_CHUNK];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nwarps = gridDim.x * SMV_WARPS;
   float acc2 = 0.0f;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+  for (int r0 = (blockIdx.x * SMV_WARPS + wid) * 32; r0 < m; r0 += nwarps * 32) {
+    const int r = r0 + lane;
+    const int lo = r < m ? ptr[r] : 0, hi = r < m ? ptr[r + 1] : 0;
+    const int g_lo = __shfl_sync(0xffffffffu, lo, 0);
+    const int g_hi = __shfl_sync(0xffffffffu, hi, min(m - r0, 32) - 1);
     float sum = 0.0f;
-    const int e1 = ptr[i + 1];
-    for (int e = ptr[i]; e < e1; ++e) sum = __fadd_rn(sum, __fmul_rn(val[e], v[col[e]]));
-    const float o = y ? __fsub_rn(y[i], sum) : sum;
-    out[i] = o;
-    acc2 = fmaf(o, o, acc2);
+    for (int c0 = g_lo; c0 < g_hi; c0 += SMV_CHUNK) {
+      const int cn = min(SMV_CHUNK, g_hi - c0);
+      // all 8 column indices and values of this lane first, then all 8 gathers in flight
+      int ci[SMV_CHUNK / 32];
+      float cv[SMV_CHUNK / 32], xv[SMV_CHUNK / 32];
+#pragma unroll
+      for (int u = 0; u < SMV_CHUNK / 32; ++u) {
+        const int t = lane + 32 * u;
+        ci[u] = t < cn ? col[c0 + t] : 0;
+        cv[u] = t < cn ? val[c0 + t] : 0.0f;
+      }
+#pragma unroll
+      for (int u = 0; u < SMV_CHUNK / 32; ++u) xv[u] = lane + 32 * u < cn ? v[ci[u]] : 0.0f;
+#pragma unroll
+      for (int u = 0; u < SMV_CHUNK / 32; ++u)
+        if (lane + 32 * u < cn) prod[wid][lane + 32 * u] = __fmul_rn(cv[u], xv[u]);
+      __syncwarp();
+      const int a = max(lo, c0), b = min(hi, c0 + cn);
+      for (int e = a; e < b; ++e) sum = __fadd_rn(sum, prod[wid][e - c0]);
+      __syncwarp();
+    }
+    if (r < m) {
+      const float o = y ? __fsub_rn(y[r], sum) : sum;
+      out[r] = o;
+      acc2 = fmaf(o, o, acc2);
+    }
   }
   if (slot >= 0) grid_reduce_publish<0>(acc2, slot, st, red_part, tickets);
 }
 
+// A^T r over the column-grouped layout: one thread per column, its d entries in order.  No
+// shared memory, so L1 keeps the gathered r (all of it at m = 2^16).
 __global__ void k_smv_AT(const GbState *st, int pf, const int *__restrict__ rows, const float *__restrict__ vals,
                          int n, int d, const float *__restrict__ r, float *__restrict__ g) {
   if (!gb_pred(st, pf)) return;
@@ -426,6 +466,17 @@ __global__ void k_smv_AT(const GbState *st, int pf, const int *__restrict__ rows
 }
 
 // ------------------------------------------------------------------ enqueue
+// resident CTAs per SM of the expander A x kernel (queried once): its grid is one wave
+static int smv_a_blocks_per_sm() {
+  static int b = 0;
+  if (b == 0) {
+    int v = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_smv_A, SMV_WARPS * 32, 0);
+    b = v > 0 ? v : 1;
+  }
+  return b;
+}
+
 static int fft_smem(int logL) { return (FFT_ELEMS + (1 << logL) / 2) * (int)sizeof(float2); }
 
 template <int INV, int LOAD, int STORE>
@@ -482,7 +533,10 @@ void enq_A(GbWork &w, cudaStream_t s, const float *v, float *out, const float *y
     k_dct_select<<<w.red_blocks, 256, 0, s>>>(w.st, pf, op.cbuf1, op.rows, op.m, op.n, y, out, slot,
                                                w.red_part, w.tickets);
   } else {
-    k_smv_A<<<w.red_blocks, 256, 0, s>>>(w.st, pf, op.csr_ptr, op.csr_col, op.csr_val, op.m, v, y, out, slot,
+    // one resident wave, at most GB_MAXRB CTAs (the grid reduction)
+    int blocks = (op.m + 32 * SMV_WARPS - 1) / (32 * SMV_WARPS);
+    blocks = std::min(std::min(blocks, GB_MAXRB), smv_a_blocks_per_sm() * w.num_sms);
+    k_smv_A<<<std::max(blocks, 1), SMV_WARPS * 32, 0, s>>>(w.st, pf, op.csr_ptr, op.csr_col, op.csr_val, op.m, v, y, out, slot,
                                          w.red_part, w.tickets);
   }
 }

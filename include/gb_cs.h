@@ -186,6 +186,13 @@ gb_status gb_cs_find_support_set(float *d_v, int n, int k, float slope, float in
  * p->location must be GB_DEVICE; y/k are ignored. */
 gb_status gb_cs_operator_apply(const gb_problem *p, int transpose, const float *d_in, float *d_out);
 
+/* Measurement helper (no reference counterpart): the device time of gb_cs_operator_apply's
+ * kernels, set up once, CUDA events around each of `reps` applications after `warmup`
+ * untimed ones; a non-NULL d_flush of flush_bytes is overwritten before each application
+ * (outside the events) so operands come from HBM.  *ms_out = mean ms per application. */
+gb_status gb_cs_operator_time(const gb_problem *p, int transpose, const float *d_in, float *d_out, int warmup,
+                              int reps, void *d_flush, size_t flush_bytes, float *ms_out);
+
 /* FindSupportSet_sort (GAGA/gaga/functions.cu:446-465), the sort-based support of the timing
  * variants (supportFlag 2/3): if T > max_change, T -= max_change; otherwise T = the k-th
  * largest |v| (element n-k of |v| sorted ascending, exact) and every bin becomes 1; then
