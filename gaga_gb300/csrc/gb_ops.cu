@@ -257,6 +257,7 @@ __global__ void __launch_bounds__(DA_THREADS, DA_BLOCKS_PER_SM) k_dense_at(GbSta
 // Each block transforms FFT_ELEMS / L sequences of length L in shared memory.
 #define FFT_ELEMS 4096
 #define FFT_THREADS 512
+#define FFT_PAD(i) ((i) + ((i) >> 5))
 
 enum { LOAD_MAKHOUL = 0, LOAD_FREQ = 1, LOAD_CPLX = 2 };
 enum { STORE_CPLX_T = 0, STORE_CPLX_NAT = 1, STORE_MAKHOUL_REAL = 2 };
@@ -283,13 +284,21 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_pass(const GbState *__restr
   extern __shared__ float2 sm[];
   const int L = 1 << logL;
   const int B = FFT_ELEMS / L;  // sequences per block (L <= FFT_ELEMS)
-  float2 *buf = sm;             // B * L
-  float2 *tw = sm + FFT_ELEMS;  // L / 2 twiddles exp(-+2 pi i t / L)
+  // element i of the B sequences lives at FFT_PAD(i): one float2 of padding per 32 breaks
+  // the power-of-two strides of the bit-reversed scatter and the butterflies into distinct
+  // banks.  Stage s reads its own contiguous twiddle table (entries half - 1 .. 2 half - 2),
+  // so consecutive butterflies read consecutive twiddles.
+  float2 *buf = sm;                               // FFT_PAD(B * L)
+  float2 *tw = sm + FFT_PAD(FFT_ELEMS);           // L - 1 twiddles, stage by stage
   const int n1 = 1 << log1, n2 = 1 << log2;
   const int N = n1 * n2;
   const int nseq = pass == 1 ? n2 : n1;
   const float sgn = INV ? 1.0f : -1.0f;
-  for (int t = threadIdx.x; t < L / 2; t += blockDim.x) tw[t] = cis_pi(sgn, (2.0f * t) / (float)L);
+  for (int s = 1; s <= logL; ++s) {
+    const int half = 1 << (s - 1);
+    for (int t = threadIdx.x; t < half; t += blockDim.x)
+      tw[half - 1 + t] = cis_pi(sgn, (2.0f * (t << (logL - s))) / (float)L);  // exp(-+2 pi i t / 2 half)
+  }
   const float wn0 = sqrtf(1.0f / (float)N), wn = sqrtf(2.0f / (float)N);
   for (int seq0 = blockIdx.x * B; seq0 < nseq; seq0 += gridDim.x * B) {
     __syncthreads();
@@ -322,7 +331,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_pass(const GbState *__restr
         }
       }
       const int pos = (int)(__brev((unsigned)e) >> (32 - logL));
-      buf[b * L + pos] = val;
+      buf[FFT_PAD(b * L + pos)] = val;
     }
     __syncthreads();
     // radix-2 decimation-in-time stages
@@ -332,9 +341,9 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_pass(const GbState *__restr
         const int b = u >> (logL - 1);
         const int q = u & (L / 2 - 1);
         const int pos = q & (half - 1);
-        const int i0 = b * L + ((q >> (s - 1)) << s) + pos;
-        const int i1 = i0 + half;
-        const float2 w = tw[pos << (logL - s)];
+        const int i0 = FFT_PAD(b * L + ((q >> (s - 1)) << s) + pos);
+        const int i1 = FFT_PAD(b * L + ((q >> (s - 1)) << s) + pos + half);
+        const float2 w = tw[half - 1 + pos];
         const float2 a = buf[i0];
         const float2 bb = cmul(buf[i1], w);
         buf[i0] = make_float2(a.x + bb.x, a.y + bb.y);
@@ -349,7 +358,7 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_pass(const GbState *__restr
       else { b = q % B; e = q / B; }  // pass 2 stores k1 + n1*k2: consecutive b contiguous
       const int sq = seq0 + b;
       if (sq >= nseq) continue;
-      float2 val = buf[b * L + e];
+      float2 val = buf[FFT_PAD(b * L + e)];
       if (pass == 1) {
         // twiddle exp(-+2 pi i j2 k1 / N), j2 = sq, k1 = e
         const int prod = (int)(((long long)sq * e) & (N - 1));
@@ -477,7 +486,7 @@ static int smv_a_blocks_per_sm() {
   return b;
 }
 
-static int fft_smem(int logL) { return (FFT_ELEMS + (1 << logL) / 2) * (int)sizeof(float2); }
+static int fft_smem(int logL) { return (FFT_PAD(FFT_ELEMS) + (1 << logL)) * (int)sizeof(float2); }
 
 template <int INV, int LOAD, int STORE>
 static void launch_fft(GbWork &w, cudaStream_t s, int pf, int pass, const float *vin, const float2 *cin,
