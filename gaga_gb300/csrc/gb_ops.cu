@@ -412,9 +412,11 @@ __global__ void k_dct_scatter(const GbState *st, int pf, const int *__restrict__
 // a sequential per-row sum).
 #define SMV_WARPS 8
 #define SMV_CHUNK 256  // entries of a row group staged per warp and step
+#define SMV_RPW 8      // rows per warp
 
 // A x over the row-major copy (rows ascending, each row's columns ascending): a warp takes
-// 32 consecutive rows, reads their entry range in coalesced chunks, and lane r sums row r
+// SMV_RPW consecutive rows, reads their entry range in coalesced chunks with all 32 lanes,
+// and lane r < SMV_RPW sums row r (few rows per warp: many warps even at small m)
 __global__ void __launch_bounds__(SMV_WARPS * 32) k_smv_A(GbState *st, int pf, const int *__restrict__ ptr,
                                                           const int *__restrict__ col, const float *__restrict__ val,
                                                           int m, const float *__restrict__ v,
@@ -425,11 +427,12 @@ __global__ void __launch_bounds__(SMV_WARPS * 32) k_smv_A(GbState *st, int pf, c
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int nwarps = gridDim.x * SMV_WARPS;
   float acc2 = 0.0f;
-  for (int r0 = (blockIdx.x * SMV_WARPS + wid) * 32; r0 < m; r0 += nwarps * 32) {
+  for (int r0 = (blockIdx.x * SMV_WARPS + wid) * SMV_RPW; r0 < m; r0 += nwarps * SMV_RPW) {
     const int r = r0 + lane;
-    const int lo = r < m ? ptr[r] : 0, hi = r < m ? ptr[r + 1] : 0;
+    const bool own = lane < SMV_RPW && r < m;
+    const int lo = own ? ptr[r] : 0, hi = own ? ptr[r + 1] : 0;
     const int g_lo = __shfl_sync(0xffffffffu, lo, 0);
-    const int g_hi = __shfl_sync(0xffffffffu, hi, min(m - r0, 32) - 1);
+    const int g_hi = __shfl_sync(0xffffffffu, hi, min(m - r0, SMV_RPW) - 1);
     float sum = 0.0f;
     for (int c0 = g_lo; c0 < g_hi; c0 += SMV_CHUNK) {
       const int cn = min(SMV_CHUNK, g_hi - c0);
@@ -452,7 +455,7 @@ __global__ void __launch_bounds__(SMV_WARPS * 32) k_smv_A(GbState *st, int pf, c
       for (int e = a; e < b; ++e) sum = __fadd_rn(sum, prod[wid][e - c0]);
       __syncwarp();
     }
-    if (r < m) {
+    if (own) {
       const float o = y ? __fsub_rn(y[r], sum) : sum;
       out[r] = o;
       acc2 = fmaf(o, o, acc2);
@@ -543,7 +546,7 @@ void enq_A(GbWork &w, cudaStream_t s, const float *v, float *out, const float *y
                                                w.red_part, w.tickets);
   } else {
     // one resident wave, at most GB_MAXRB CTAs (the grid reduction)
-    int blocks = (op.m + 32 * SMV_WARPS - 1) / (32 * SMV_WARPS);
+    int blocks = (op.m + SMV_RPW * SMV_WARPS - 1) / (SMV_RPW * SMV_WARPS);
     blocks = std::min(std::min(blocks, GB_MAXRB), smv_a_blocks_per_sm() * w.num_sms);
     k_smv_A<<<std::max(blocks, 1), SMV_WARPS * 32, 0, s>>>(w.st, pf, op.csr_ptr, op.csr_col, op.csr_val, op.m, v, y, out, slot,
                                          w.red_part, w.tickets);
