@@ -209,3 +209,32 @@ def test_operator_apply(gb, gbo, kind):
         np.testing.assert_allclose(ya, yo, rtol=0, atol=2e-5 * np.abs(yo).max())
         np.testing.assert_allclose(ga, go, rtol=0, atol=2e-5 * np.abs(go).max())
     del keep
+
+
+@pytest.mark.parametrize("logn", [20, 22])
+def test_dct_operator_large(gb, gbo, logn):
+    """The subsampled DCT at the workload sizes (n = 2^20: both FFT passes are 1024-point,
+    the register 32 x 32 transform; n = 2^22: 2048-point, the shared-memory radix-2 pass)
+    against the oracle's FP64 DCT, A and A^T."""
+    torch = _torch()
+    L = gb._lib.load()
+    n = 2 ** logn
+    m = n // 4
+    rows = gbo.gen_dct_rows(n, m, seed=logn)
+    op = gbo.Op.dct(n, rows)
+    rng = np.random.default_rng(logn)
+    x = rng.standard_normal(n).astype(np.float32)
+    x[rng.random(n) < 0.5] = 0.0
+    r = rng.standard_normal(m).astype(np.float32)
+    dr = torch.tensor(rows, device="cuda")
+    p = gb._lib.Problem(1, m, n, 0, None, None, 0, dr.data_ptr(), None, None, 0, 0, 1, None)
+    dx, drr = torch.tensor(x, device="cuda"), torch.tensor(r, device="cuda")
+    out_m, out_n = torch.zeros(m, device="cuda"), torch.zeros(n, device="cuda")
+    assert L.gb_cs_operator_apply(C.byref(p), 0, dx.data_ptr(), out_m.data_ptr()) == 0
+    assert L.gb_cs_operator_apply(C.byref(p), 1, drr.data_ptr(), out_n.data_ptr()) == 0
+    ya, ga = out_m.cpu().numpy(), out_n.cpu().numpy()
+    yo, go = gbo.A(op, x), gbo.AT(op, r)
+    np.testing.assert_allclose(ya, yo, rtol=0, atol=2e-5 * np.abs(yo).max())
+    np.testing.assert_allclose(ga, go, rtol=0, atol=2e-5 * np.abs(go).max())
+    assert np.linalg.norm(ya - yo) / np.linalg.norm(yo) < 1e-5
+    assert np.linalg.norm(ga - go) / np.linalg.norm(go) < 1e-5
