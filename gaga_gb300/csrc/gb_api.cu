@@ -120,12 +120,8 @@ gb_status select_device(int gpu) {
   if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return bad("no CUDA device", GB_NO_DEVICE);
   if (gpu < 0 || gpu >= count) gpu = 0;  // gaga_gen.cu:233-241 resets to 0
   GB_CUDA_TRY(cudaSetDevice(gpu));
-  static thread_local int attr_done = -1;
-  if (attr_done != gpu) {
-    GB_TRY(gb_ops_init_attributes());
-    attr_done = gpu;
-  }
-  return GB_OK;
+  static std::atomic<unsigned long long> attr_done{0};
+  return gb_once_per_device(attr_done, gb_ops_init_attributes);
 }
 
 gb_status alloc_work(DeviceBuffers &db, GbWork &w, int m, int n, int lda, int num_bins, int maxiter) {

@@ -226,11 +226,11 @@ gb_status gb_gemm(const GbGemm &g, cudaStream_t s) {
     s_max = GB_GEMM_SPLIT_MAX;
   }
   const int smem = GT_STAGES * (GT_M + GT_N) * GT_LD * 2;
-  static bool attr = false;
-  if (!attr) {
+  static std::atomic<unsigned long long> attr_done{0};
+  GB_TRY(gb_once_per_device(attr_done, [&]() -> gb_status {
     GB_CUDA_TRY(cudaFuncSetAttribute(k_gemm_tn_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    attr = true;
-  }
+    return GB_OK;
+  }));
   dim3 grid(g.M / GT_M, (g.N / GT_N) * s_max);
   k_gemm_tn_mma<<<grid, 256, smem, s>>>(g, ws, s_max);
   GB_CUDA_TRY(cudaGetLastError());

@@ -366,11 +366,11 @@ gb_status tensor_map(CUtensorMap *map, const void *base, int rows, int K, int ld
 // tcgen05 path of gb_gemm (gb_gemm.cu decides): M % 128, N % 256, K % 64, 16-byte aligned
 // operands with row strides that are multiples of 8 elements.
 gb_status gb_gemm_tc(const GbGemm &g, cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
+  static std::atomic<unsigned long long> attr_done{0};
+  GB_TRY(gb_once_per_device(attr_done, []() -> gb_status {
     GB_CUDA_TRY(cudaFuncSetAttribute(k_gemm_tn_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
-    attr = true;
-  }
+    return GB_OK;
+  }));
   const void *B = g.B;
   int ldb = g.ldb;
   if (g.nmap) {

@@ -13,6 +13,8 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include <atomic>
+
 #include "../../include/gb_cs.h"
 
 #define GB_NSLOT 16     // reduction result slots
@@ -148,6 +150,22 @@ struct GbWork {
 };
 
 void gb_set_error_message(const char *msg, const char *file, int line);
+
+// Runs `f` (a one-time setup such as a kernel attribute, which CUDA keeps per device) once
+// for the current device, from any thread; a repeat from a racing thread is harmless.
+template <class F>
+gb_status gb_once_per_device(std::atomic<unsigned long long> &done, F f) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    gb_set_error_message("cudaGetDevice failed", __FILE__, __LINE__);
+    return GB_CUDA_ERROR;
+  }
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (done.load(std::memory_order_acquire) & bit) return GB_OK;
+  const gb_status rc = f();
+  if (rc == GB_OK) done.fetch_or(bit, std::memory_order_release);
+  return rc;
+}
 
 #define GB_CUDA_TRY(call)                                               \
   do {                                                                  \

@@ -407,11 +407,11 @@ extern "C" gb_status gb_cs_mlp_forward(const float *d_params, const float *d_fea
 
 static gb_status ml_grad_launch(const float *params, const float *feat, const float *tgt, const int *idx, int ns,
                                 float scale, float *partial, float *lossp, cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
+  static std::atomic<unsigned long long> attr_done{0};
+  GB_TRY(gb_once_per_device(attr_done, []() -> gb_status {
     GB_CUDA_TRY(cudaFuncSetAttribute(k_ml_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ml_grad_smem()));
-    attr = true;
-  }
+    return GB_OK;
+  }));
   k_ml_grad<<<ML_TRAIN_BLOCKS, 256, ml_grad_smem(), s>>>(params, feat, tgt, idx, ns, scale, partial, lossp);
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;

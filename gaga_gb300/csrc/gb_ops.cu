@@ -633,13 +633,14 @@ __global__ void k_smv_AT(const GbState *st, int pf, const int *__restrict__ rows
 // ------------------------------------------------------------------ enqueue
 // resident CTAs per SM of the expander A x kernel (queried once): its grid is one wave
 static int smv_a_blocks_per_sm() {
-  static int b = 0;
-  if (b == 0) {
-    int v = 0;
+  static std::atomic<int> b{0};  // the same on every GB300 of a process
+  int v = b.load(std::memory_order_relaxed);
+  if (v == 0) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_smv_A, SMV_WARPS * 32, 0);
-    b = v > 0 ? v : 1;
+    v = v > 0 ? v : 1;
+    b.store(v, std::memory_order_relaxed);
   }
-  return b;
+  return v;
 }
 
 static int fft_smem(int logL) { return (FFT_PAD(FFT_ELEMS) + (1 << logL)) * (int)sizeof(float2); }
