@@ -443,6 +443,7 @@ def matvec_roofline(peak, peak_kind, m=14746, n=16384, k=5000, reps=20):
     import torch
 
     import gaga_gb300 as gb
+    from gaga_gb300 import _lib
 
     L = gb._lib.load()
     g = torch.Generator(device="cuda").manual_seed(1)
@@ -461,17 +462,17 @@ def matvec_roofline(peak, peak_kind, m=14746, n=16384, k=5000, reps=20):
                                         ("av", 2, x, y_out, 4.0 * m * k + 8 * k + 4 * m)):
         with torch.cuda.stream(s):
             if tr == 2:
-                L.gb_cs_dense_apply_noalloc(A.data_ptr(), lda, m, n, 0, vin.data_ptr(), vout.data_ptr(),
-                                            C.c_void_p(s.cuda_stream))
+                _lib.check(L.gb_cs_dense_apply_noalloc(A.data_ptr(), lda, m, n, 0, vin.data_ptr(), vout.data_ptr(),
+                                                       C.c_void_p(s.cuda_stream)))
             for _ in range(3):
-                L.gb_cs_dense_apply_noalloc(A.data_ptr(), lda, m, n, tr, vin.data_ptr(), vout.data_ptr(),
-                                            C.c_void_p(s.cuda_stream))
+                _lib.check(L.gb_cs_dense_apply_noalloc(A.data_ptr(), lda, m, n, tr, vin.data_ptr(), vout.data_ptr(),
+                                                       C.c_void_p(s.cuda_stream)))
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             s.synchronize()
             e0.record(s)
             for _ in range(reps):
-                L.gb_cs_dense_apply_noalloc(A.data_ptr(), lda, m, n, tr, vin.data_ptr(), vout.data_ptr(),
-                                            C.c_void_p(s.cuda_stream))
+                _lib.check(L.gb_cs_dense_apply_noalloc(A.data_ptr(), lda, m, n, tr, vin.data_ptr(), vout.data_ptr(),
+                                                       C.c_void_p(s.cuda_stream)))
             e1.record(s)
         e1.synchronize()
         t = e0.elapsed_time(e1) / 1e3 / reps
