@@ -40,6 +40,9 @@ sys.path.insert(0, ROOT)
 
 METRIC = "trials recovered/s (rel err<=1e-3), tuned vs plain on 1 GB300; matvec % HBM peak"
 TOTAL, SHARED, PARTS, SEED, TOL_REL, MAXITER = 4096, 1024, 4, 20240607, 1e-4, 5000
+WORKLOAD = ("dense phase-transition sweep: 4096 NIHT trials = 3072 independent (n 1024-16384, delta 0.1-0.9, "
+            "rho 0.02-0.5) + 1024 sharing one A (n 8192, m 4096, rho 0.02-0.5); tol 1e-4*||y||; one quarter of "
+            "the sweep per step per GPU")
 SHARED_SEED = SEED + 1000003  # keys of the shared subset stay clear of the independent trials' seed + id
 
 
@@ -140,7 +143,7 @@ def run_cpu(w, count):
     ok, iters, err = gbo.solve_dense_trials(n, m, k, SEED, tid, alg="NIHT", tol_rel=TOL_REL, maxiter=MAXITER,
                                             threads=cores)
     dt = time.perf_counter() - t0
-    return {"value": ok / dt, "unit": "trials/s", "cores": cores, "kind": "port",
+    return {"value": ok / dt, "unit": "trials/s", "cores": cores, "kind": "port", "seconds": dt,
             "sample": "%d trials of wave %d (every %d-th; n=%s), NIHT, CPU oracle oracle/gbo.c with OpenMP inside each "
                       "trial, generation included; %d recovered in %.1f s" % (len(n), w, len(wave_arrays(w)[0]) // count,
                                                                                sorted(set(n.tolist())), ok, dt)}
@@ -159,9 +162,12 @@ def bench_reference(args):
         last = r
     value = float(np.mean([r["value"] for r in t_steps]))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "trials/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": float(np.mean([r["seconds"] for r in t_steps])) * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded Philox trials)",
-            "config": {"workload": "dense phase-transition sweep, NIHT, bounded CPU sample per wave",
+            "config": {"workload": WORKLOAD, "form": "reference: the CPU restatement of the algorithm (oracle), a "
+                                                     "bounded sample of each step's trials",
+                       "trials_per_step": TOTAL // PARTS,
                        "trials_per_sample": args.cpu_trials},
             "cpu_baseline": dict(last, value=value),
             "e2e": {"value": value, "unit": "trials/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -252,9 +258,7 @@ def bench_ours(args):
             "warmup": args.warmup, "ms_per_step": acc["kms"] / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32 (shared-matrix part: bf16 GEMM, fp32 accumulate)",
             "data": "synthetic (seeded Philox Gaussian trials drawn on device)",
-            "config": {"workload": "dense phase-transition sweep: 4096 NIHT trials = 3072 independent (n 1024-16384, "
-                                   "delta 0.1-0.9, rho 0.02-0.5) + 1024 sharing one A (n 8192, m 4096, rho 0.02-0.5); "
-                                   "tol 1e-4*||y||; one quarter of the sweep per step per GPU",
+            "config": {"workload": WORKLOAD,
                        "form": "tuned: batched slot graphs (device trial queue, device generation) + shared-matrix "
                                "BF16 tensor-core GEMM form",
                        "schedule": {"slots": sched["slots"], "sm_share": sched["sm_share"],
