@@ -201,7 +201,8 @@ def bench_ours(args):
         n, m, k, tid = wave_arrays(w)
         t0 = time.perf_counter()
         ns, iters, err, ok = gb.solve_batch(n, m, k, SEED, tid, alg="NIHT", tol_rel=TOL_REL, maxiter=MAXITER,
-                                            slots=sched["slots"], sm_share=sched["sm_share"])
+                                            slots=sched["slots"], sm_share=sched["sm_share"],
+                                            cluster=sched.get("cluster", 0))
         t1 = time.perf_counter()
         nbytes, kms = gb.batch_last_stats()
         ks, first = shared_part(w)
@@ -234,9 +235,9 @@ def bench_ours(args):
         for key in ("ok", "trials", "wall", "kms", "bytes", "flops", "kms_batch", "kms_shared", "ok_batch", "ok_shared",
                     "n_batch", "n_shared", "wall_batch", "wall_shared", "h2d", "d2h"):
             acc[key] = acc.get(key, 0) + r[key]
-        # host-issued launches: one graph per slot stream of the batched form; the shared
-        # form's 6 setup kernels, its graph and its verdict kernel
-        launches += sched["slots"] + 8
+        # host-issued launches: one graph per slot stream and the cluster-resident kernel of
+        # the batched form; the shared form's 6 setup kernels, its graph and its verdict kernel
+        launches += sched["slots"] + 1 + 8
     torch.cuda.synchronize()
     clocks = sampler.stop()
     if world > 1:
@@ -259,9 +260,11 @@ def bench_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32 (shared-matrix part: bf16 GEMM, fp32 accumulate)",
             "data": "synthetic (seeded Philox Gaussian trials drawn on device)",
             "config": {"workload": WORKLOAD,
-                       "form": "tuned: batched slot graphs (device trial queue, device generation) + shared-matrix "
-                               "BF16 tensor-core GEMM form",
+                       "form": "tuned: batched form (n <= 8192: cluster-resident NIHT kernel, one thread-block "
+                               "cluster per trial; larger: slot graphs; device trial queues, device generation) + "
+                               "shared-matrix BF16 tensor-core GEMM form",
                        "schedule": {"slots": sched["slots"], "sm_share": sched["sm_share"],
+                                    "cluster": sched.get("cluster", 0),
                                     "picked_by": "autotune over %d candidates on %d probe trials%s" % (
                                         len(sched["candidates"]), sched["probe_trials"],
                                         " (cached)" if sched.get("cached") else "")},

@@ -1,12 +1,13 @@
 """Autotuner for the batched form's schedule.
 
-The batched form (gb_cs_solve_batch) runs `slots` trials at a time, each slot's kernels
-shaped for `sm_share` SMs (the dense A^T r grid is 4 CTAs per shared SM, the reductions one
-CTA per shared SM, and the A x_S row tiles x support splits fill whole waves of that many
-SMs).  Which pair is fastest depends on the GPU and on the mix of trial sizes, so it is
-measured: every candidate solves the same probe subset of the workload (every `stride`-th
-trial, all trial sizes represented), the second run of each is timed on the device, and the
-fastest candidate wins.  Results are cached per GPU, algorithm and trial-size mix in a JSON
+The batched form (gb_cs_solve_batch) runs `slots` trials at a time in slot graphs, each
+slot's kernels shaped for `sm_share` SMs (the dense A^T r grid is 4 CTAs per shared SM, the
+reductions one CTA per shared SM, and the A x_S row tiles x support splits fill whole waves
+of that many SMs), while NIHT trials with n <= 8192 go to the cluster-resident kernel with
+`cluster` CTAs per trial.  Which combination is fastest depends on the GPU and on the mix of
+trial sizes, so it is measured: every candidate solves the same probe subset of the workload
+(every `stride`-th trial, all trial sizes represented), the second run of each is timed on
+the device, and the fastest candidate wins.  Results are cached per GPU, algorithm and trial-size mix in a JSON
 file (GB_CS_TUNE_CACHE, default ~/.cache/gaga_gb300/autotune.json).
 """
 import json
@@ -14,8 +15,9 @@ import os
 
 import numpy as np
 
-SLOTS = (8, 12, 16, 24)
-SHARE_FRACTIONS = (0.25, 0.5, 1.0)
+SLOTS = (8, 16, 24)
+SHARE_FRACTIONS = (0.25, 0.5)
+CLUSTERS = (4, 8)
 
 
 def _cache_path():
@@ -33,9 +35,11 @@ def _key(alg, n, m):
 
 
 def tune_batch(n, m, k, seed, trial_ids=None, alg="NIHT", tol_rel=1e-4, maxiter=5000, stride=4, use_cache=True,
-               slots=SLOTS, fractions=SHARE_FRACTIONS, log=None):
-    """Pick (slots, sm_share) for solving trials like (n, m, k); returns a dict with the
-    choice and the measured device milliseconds of every candidate on the probe."""
+               slots=SLOTS, fractions=SHARE_FRACTIONS, clusters=CLUSTERS, log=None):
+    """Pick (slots, sm_share, cluster) for solving trials like (n, m, k); returns a dict with
+    the choice and the measured device milliseconds of every candidate on the probe.  The
+    cluster size only matters for NIHT (the resident kernel); other algorithms tune with
+    cluster 0."""
     import torch
 
     import gaga_gb300 as gb
@@ -59,19 +63,20 @@ def tune_batch(n, m, k, seed, trial_ids=None, alg="NIHT", tol_rel=1e-4, maxiter=
     probe = np.sort(order[::stride])
     pn, pm, pk, pt = n[probe], m[probe], k[probe], tid[probe]
     table = []
-    for s in slots:
-        for fr in fractions:
-            share = max(1, int(round(sms * fr)))
-            for rep in range(2):  # the first run builds the engine and its graphs
-                ns, it, err, ok = gb.solve_batch(pn, pm, pk, seed, pt, alg=alg, tol_rel=tol_rel, maxiter=maxiter,
-                                                 slots=s, sm_share=share)
-            _, ms = gb.batch_last_stats()
-            table.append({"slots": s, "sm_share": share, "ms": ms, "recovered": int(ns)})
-            if log:
-                log(json.dumps(table[-1]))
+    for c in (clusters if alg == "NIHT" else (0,)):
+        for s in slots:
+            for fr in fractions:
+                share = max(1, int(round(sms * fr)))
+                for rep in range(2):  # the first run builds the engine and its graphs
+                    ns, it, err, ok = gb.solve_batch(pn, pm, pk, seed, pt, alg=alg, tol_rel=tol_rel,
+                                                     maxiter=maxiter, slots=s, sm_share=share, cluster=c)
+                _, ms = gb.batch_last_stats()
+                table.append({"slots": s, "sm_share": share, "cluster": c, "ms": ms, "recovered": int(ns)})
+                if log:
+                    log(json.dumps(table[-1]))
     best = min(table, key=lambda r: r["ms"])
-    res = {"slots": best["slots"], "sm_share": best["sm_share"], "probe_trials": int(len(probe)),
-           "candidates": table, "key": key}
+    res = {"slots": best["slots"], "sm_share": best["sm_share"], "cluster": best["cluster"],
+           "probe_trials": int(len(probe)), "candidates": table, "key": key}
     if use_cache:
         cache[key] = res
         try:

@@ -15,7 +15,7 @@ LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libgb_cs.so")
 ROOT = os.path.dirname(HERE)
 SOURCES = ["gb_ops.cu", "gb_solver.cu", "gb_api.cu", "gb_batch.cu", "gb_noalloc.cu", "gb_gemm.cu", "gb_gemm_tc.cu",
-           "gb_shared.cu", "gb_learned.cu"]
+           "gb_shared.cu", "gb_learned.cu", "gb_resident.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr",

@@ -23,8 +23,10 @@
 #include <map>
 #include <vector>
 
+#include "gb_ctrl.cuh"
 #include "gb_internal.cuh"
 #include "gb_philox.cuh"
+#include "gb_resident.h"
 
 __global__ void k_hist(const GbState *st, int pf, const float *__restrict__ v, int *__restrict__ bins,
                        int *__restrict__ bins_prev, int *__restrict__ counters, int n);
@@ -74,19 +76,7 @@ __device__ void load_trial(GbState *st, const BatchParams *bp, int q, cudaGraphC
     return;
   }
   const int t = bp->order[q];
-  st->trial = t;
-  st->m = bp->m[t];
-  st->n = bp->n[t];
-  st->k = bp->k[t];
-  st->num_bins = max(st->n / 20, 1000);
-  st->maxiter = bp->maxiter;
-  st->alg = bp->alg;
-  st->restart = 0;
-  st->op_kind = GB_OP_DENSE;
-  st->active = 1;
-  for (int f = 0; f < GB_NFLAG; ++f) st->flags[f] = 0;
-  st->flags[F_ALWAYS] = 1;
-  st->bytes = 0.0;
+  batch_trial_fields(st, t, bp->m[t], bp->n[t], bp->k[t], bp->maxiter, bp->alg);
   cudaGraphSetConditional(h_trial, 1u);
 }
 
@@ -143,27 +133,7 @@ __global__ void k_b_ctrl(GbState *st, const BatchParams *bp, int phase, cudaGrap
     st->k = st->sum;  // |support| >= k, the k the solver is given
   } else if (phase == B_INIT) {
     if (!st->active) return;
-    // the solver's initial state (initial_state in gb_solver.cu) with tol = tol_rel ||y||
-    const float tol = bp->tol_rel * (float)sqrt(st->red[R_RES]);
-    st->tol = tol;
-    st->iter = 0; st->fail = 0; st->cycle = 1; st->passes = 0; st->pass_limit = st->maxiter + 4;
-    st->status = 0; st->stop_reason = 0;
-    st->err = 0.0f; st->err_start = 0.0f; st->resid_diff = 1.0f;
-    for (int j = 0; j < 16; ++j) { st->prev[j] = 0.0f; st->evol[j] = 1.0f; }
-    st->alpha_bin = 0.25f;
-    st->max_bin = (int)((float)st->num_bins * (1.0f - st->alpha_bin));
-    st->k_bin = 0; st->sum = 0; st->k_bin_prev = 0;
-    st->min_val = 0.0f; st->slope = 0.0f; st->max_value = 0.0f; st->max_change = 0.0f;
-    st->mu = 0.0f; st->cg_alpha = 0.0f; st->cg_beta = 0.0f;
-    st->beta_to_zero = 1; st->supp_change = 1;
-    st->it_cg = 0; st->tol_cg = tol * tol; st->tol2 = 10.0f * st->tol_cg;
-    for (int f = 0; f < GB_NFLAG; ++f) st->flags[f] = 0;
-    st->flags[F_ALWAYS] = 1;
-    st->changed = 0;
-    st->bytes = 0.0;
-    st->learned = bp->learned;
-    st->fell_back = 0;
-    st->err_warm0 = 0.0f;
+    batch_solver_init(st, bp->tol_rel, bp->learned);
   } else {
     // verdict of the finished trial (results.cu:468-475), then the next trial
     if (st->trial >= 0) {
@@ -425,9 +395,38 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
       gb_set_error_message("trial sizes must satisfy 1 <= k, 1 <= m <= n, 16 <= n <= 2^22", __FILE__, __LINE__);
       return GB_BAD_ARG;
     }
-    n_cap = std::max(n_cap, b->n[t]);
-    m_cap = std::max(m_cap, b->m[t]);
   }
+  // NIHT trials with n <= resident_n go to the cluster-resident kernel (gb_resident.cu),
+  // the others to the slot graphs; both run at the same time
+  int rn = b->resident_n;
+  if (rn == 0) {
+    rn = GB_RESIDENT_N_DEFAULT;
+    if (const char *e = getenv("GB_CS_RESIDENT_N")) rn = atoi(e);
+  }
+  if (b->alg != GB_ALG_NIHT) rn = -1;
+  std::vector<char> resident(T, 0);
+  int rn_cap = 16, rm_cap = 1, n_res = 0;
+  for (int t = 0; t < T; ++t)
+    if (rn > 0 && b->n[t] <= rn) {
+      resident[t] = 1;
+      rn_cap = std::max(rn_cap, b->n[t]);
+      rm_cap = std::max(rm_cap, b->m[t]);
+      n_res++;
+    }
+  if (n_res > 0 && gb_resident_pick_cluster(rn_cap, rm_cap, b->cluster) <= 0) {
+    if (b->cluster > 0 || b->resident_n > 0) {
+      gb_set_error_message("resident form: the requested cluster size does not fit these trials", __FILE__,
+                           __LINE__);
+      return GB_BAD_ARG;
+    }
+    std::fill(resident.begin(), resident.end(), 0);
+    n_res = 0;
+  }
+  for (int t = 0; t < T; ++t)
+    if (!resident[t]) {
+      n_cap = std::max(n_cap, b->n[t]);
+      m_cap = std::max(m_cap, b->m[t]);
+    }
   if (num_success) *num_success = 0;
   if (T == 0) return GB_OK;
   int dev = 0;
@@ -448,14 +447,16 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
   }
   cudaStream_t s = (cudaStream_t)b->stream;
   // trial table, longest (m*n) first
-  std::vector<int> order(T);
-  for (int t = 0; t < T; ++t) order[t] = t;
-  std::stable_sort(order.begin(), order.end(),
-                   [&](int x, int y) { return (double)b->m[x] * b->n[x] > (double)b->m[y] * b->n[y]; });
+  std::vector<int> order, rorder;
+  for (int t = 0; t < T; ++t) (resident[t] ? rorder : order).push_back(t);
+  auto larger = [&](int x, int y) { return (double)b->m[x] * b->n[x] > (double)b->m[y] * b->n[y]; };
+  std::stable_sort(order.begin(), order.end(), larger);
+  std::stable_sort(rorder.begin(), rorder.end(), larger);
+  const int T_slot = (int)order.size();
   std::vector<unsigned> tid(T);
   for (int t = 0; t < T; ++t) tid[t] = b->trial_id ? b->trial_id[t] : (unsigned)t;
   BatchParams bp;
-  bp.T = T; bp.seed = b->seed; bp.tol_rel = b->tol_rel; bp.maxiter = b->maxiter; bp.alg = b->alg;
+  bp.T = T_slot; bp.seed = b->seed; bp.tol_rel = b->tol_rel; bp.maxiter = b->maxiter; bp.alg = b->alg;
   bp.n = E.dn; bp.m = E.dm; bp.k = E.dk; bp.tid = E.dtid; bp.order = E.dorder; bp.queue = E.dqueue;
   bp.iters = E.diters; bp.err = E.derr; bp.ok = E.dok; bp.bytes = E.dbytes;
   bp.learned = learned;
@@ -467,18 +468,30 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
   GB_CUDA_TRY(cudaMemcpyAsync(E.dm, b->m, (size_t)T * 4, cudaMemcpyHostToDevice, s));
   GB_CUDA_TRY(cudaMemcpyAsync(E.dk, b->k, (size_t)T * 4, cudaMemcpyHostToDevice, s));
   GB_CUDA_TRY(cudaMemcpyAsync(E.dtid, tid.data(), (size_t)T * 4, cudaMemcpyHostToDevice, s));
-  GB_CUDA_TRY(cudaMemcpyAsync(E.dorder, order.data(), (size_t)T * 4, cudaMemcpyHostToDevice, s));
+  if (T_slot > 0)
+    GB_CUDA_TRY(cudaMemcpyAsync(E.dorder, order.data(), (size_t)T_slot * 4, cudaMemcpyHostToDevice, s));
   GB_CUDA_TRY(cudaMemcpyAsync(E.d_params, &bp, sizeof(bp), cudaMemcpyHostToDevice, s));
   GB_CUDA_TRY(cudaMemsetAsync(E.dqueue, 0, 4, s));
   GB_CUDA_TRY(cudaMemsetAsync(E.dbytes, 0, 8, s));
   GB_CUDA_TRY(cudaEventRecord(E.e0, s));
-  for (size_t i = 0; i < E.slot.size(); ++i) {
+  const size_t nslot = T_slot > 0 ? E.slot.size() : 0;
+  for (size_t i = 0; i < nslot; ++i) {
     Slot &S = E.slot[i];
     GB_CUDA_TRY(cudaStreamWaitEvent(S.stream, E.e0, 0));
     GB_CUDA_TRY(cudaGraphLaunch(S.exec, S.stream));
     GB_CUDA_TRY(cudaEventRecord(E.done[i], S.stream));
-    GB_CUDA_TRY(cudaStreamWaitEvent(s, E.done[i], 0));
   }
+  if (n_res > 0) {
+    GbResidentArgs ra;
+    ra.count = n_res;
+    ra.order = rorder.data();
+    ra.n = E.dn; ra.m = E.dm; ra.k = E.dk; ra.tid = E.dtid;
+    ra.seed = b->seed; ra.tol_rel = b->tol_rel; ra.maxiter = b->maxiter;
+    ra.iters = E.diters; ra.err = E.derr; ra.ok = E.dok; ra.bytes = E.dbytes;
+    ra.n_cap = rn_cap; ra.m_cap = rm_cap; ra.cluster = b->cluster;
+    GB_TRY(gb_resident_enqueue(ra, s));
+  }
+  for (size_t i = 0; i < nslot; ++i) GB_CUDA_TRY(cudaStreamWaitEvent(s, E.done[i], 0));
   GB_CUDA_TRY(cudaEventRecord(E.e1, s));
   std::vector<int> hit(T), hok(T), hfb(T, 0);
   std::vector<float> herr(T);

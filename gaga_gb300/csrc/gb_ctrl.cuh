@@ -689,3 +689,46 @@ __device__ __forceinline__ void ctrl_phase(GbState *st, int phase, cudaGraphCond
   }
 }
 
+
+// ------------------------------------------------------------------ batched trials
+// The fields of GbState a batched trial starts from (dense operator, its own m, n, k).
+static __device__ void batch_trial_fields(GbState *st, int trial, int m, int n, int k, int maxiter, int alg) {
+  st->trial = trial;
+  st->m = m;
+  st->n = n;
+  st->k = k;
+  st->num_bins = max(n / 20, 1000);
+  st->maxiter = maxiter;
+  st->alg = alg;
+  st->restart = 0;
+  st->op_kind = GB_OP_DENSE;
+  st->active = 1;
+  for (int f = 0; f < GB_NFLAG; ++f) st->flags[f] = 0;
+  st->flags[F_ALWAYS] = 1;
+  st->bytes = 0.0;
+}
+
+// The solver's initial state of a batched trial (initial_state of the single-trial solver)
+// with tol = tol_rel ||y||, red[R_RES] holding ||y||^2.
+static __device__ void batch_solver_init(GbState *st, float tol_rel, int learned) {
+  const float tol = tol_rel * (float)sqrt(st->red[R_RES]);
+  st->tol = tol;
+  st->iter = 0; st->fail = 0; st->cycle = 1; st->passes = 0; st->pass_limit = st->maxiter + 4;
+  st->status = 0; st->stop_reason = 0;
+  st->err = 0.0f; st->err_start = 0.0f; st->resid_diff = 1.0f;
+  for (int j = 0; j < 16; ++j) { st->prev[j] = 0.0f; st->evol[j] = 1.0f; }
+  st->alpha_bin = 0.25f;
+  st->max_bin = (int)((float)st->num_bins * (1.0f - st->alpha_bin));
+  st->k_bin = 0; st->sum = 0; st->k_bin_prev = 0;
+  st->min_val = 0.0f; st->slope = 0.0f; st->max_value = 0.0f; st->max_change = 0.0f;
+  st->mu = 0.0f; st->cg_alpha = 0.0f; st->cg_beta = 0.0f;
+  st->beta_to_zero = 1; st->supp_change = 1;
+  st->it_cg = 0; st->tol_cg = tol * tol; st->tol2 = 10.0f * st->tol_cg;
+  for (int f = 0; f < GB_NFLAG; ++f) st->flags[f] = 0;
+  st->flags[F_ALWAYS] = 1;
+  st->changed = 0;
+  st->bytes = 0.0;
+  st->learned = learned;
+  st->fell_back = 0;
+  st->err_warm0 = 0.0f;
+}

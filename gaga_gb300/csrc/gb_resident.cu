@@ -1,0 +1,808 @@
+// gb_resident.cu -- cluster-resident NIHT: the batched form's small trials, one
+// thread-block cluster per trial and one persistent launch for all of them.
+//
+// The slot graphs of gb_batch.cu run about a dozen kernels per NIHT iteration; for trials
+// of a few MB that is bound by kernel dispatch, not by HBM.  Here each trial is solved
+// start to finish by one cluster of C CTAs (one CTA per SM):
+//
+//   * CTA r owns a contiguous range of columns: its slab of A (generated in place, rows
+//     padded with zeros to lda = roundup(m, 32)) and its entries of x, grad, bins and x0,
+//     which live in shared memory.  Every CTA keeps the whole residual (m floats).
+//   * A^T r: each CTA over its own columns (lane groups per column, float4 streams).
+//   * A v_S: each CTA over its own support columns into a partial m-vector; the partials
+//     are summed in rank order through distributed shared memory, each CTA summing its
+//     share of the rows, then every CTA gathers the rows it needs.
+//   * Every CTA keeps its own copy of the solver state and runs the control phases of the
+//     single-trial solver (gb_ctrl.cuh) itself.  The reductions those phases read are
+//     combined from the CTAs' partials in rank order, and the bin counts are exact
+//     integers, so every copy holds the same bits and every CTA takes the same branches
+//     (and so meets the same cluster barriers).
+//
+// The solve is NIHT_S_gen (GAGA/gaga/algorithms.cu:1296-1421) with the same steps and
+// control as the graph path (enq_prologue / enq_body in gb_solver.cu); only the order of
+// floating-point sums differs.  The problem is the one gb_cs_generate_and_solve draws with
+// seed + trial id (Gaussian A, +-1 signal on the createVector support).
+#include <cooperative_groups.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <map>
+#include <vector>
+
+#include "gb_ctrl.cuh"
+#include "gb_internal.cuh"
+#include "gb_philox.cuh"
+#include "gb_resident.h"
+
+namespace cg = cooperative_groups;
+
+#define RS_THREADS 512
+#define RS_WARPS (RS_THREADS / 32)
+#define RS_NPUB 16
+
+namespace {
+
+struct RsParams {
+  int T;  // resident trials (entries of order)
+  unsigned int seed;
+  float tol_rel;
+  int maxiter;
+  const int *n, *m, *k;
+  const unsigned int *tid;
+  const int *order;  // resident trials, largest first
+  int *queue;
+  int *iters;
+  float *err;
+  int *ok;
+  double *bytes;
+  float *A;        // per cluster: a_stride floats
+  size_t a_stride;
+  int *xhist;      // per cluster: n_cap key bins
+  int n_cap, m_cap;
+};
+
+// Shared-memory layout of one CTA (the same on host and device).
+struct RsLayout {
+  int nc_cap, lda_cap, rc4_cap, nb_cap;
+  size_t o_st, o_pub, o_x, o_grad, o_x0, o_bins, o_sidx, o_r, o_part, o_rowp, o_ypart, o_cnt, o_cntf, o_gscr, o_scan,
+      bytes;
+};
+
+__host__ __device__ inline size_t rs_take(size_t &o, size_t b) {
+  const size_t r = o;
+  o += (b + 15) / 16 * 16;
+  return r;
+}
+
+__host__ __device__ inline RsLayout rs_layout(int n_cap, int m_cap, int C) {
+  RsLayout L;
+  L.nc_cap = ((n_cap + C - 1) / C + 3) / 4 * 4;
+  L.lda_cap = (m_cap + 31) / 32 * 32;
+  L.rc4_cap = (L.lda_cap / 4 + C - 1) / C;
+  L.nb_cap = ((n_cap / 20 > 1000 ? n_cap / 20 : 1000) + 3) / 4 * 4;
+  size_t o = 0;
+  L.o_st = rs_take(o, sizeof(GbState));
+  L.o_pub = rs_take(o, RS_NPUB * 8);  // RS_NPUB floats, then RS_NPUB ints
+  L.o_x = rs_take(o, (size_t)L.nc_cap * 4);
+  L.o_grad = rs_take(o, (size_t)L.nc_cap * 4);
+  L.o_x0 = rs_take(o, (size_t)L.nc_cap * 4);
+  L.o_bins = rs_take(o, (size_t)L.nc_cap * 4);
+  L.o_sidx = rs_take(o, (size_t)L.nc_cap * 4);
+  L.o_r = rs_take(o, (size_t)L.lda_cap * 4);
+  L.o_part = rs_take(o, (size_t)L.lda_cap * 4);
+  L.o_rowp = rs_take(o, (size_t)L.rc4_cap * 16);
+  L.o_ypart = rs_take(o, (size_t)L.rc4_cap * 16);
+  L.o_cnt = rs_take(o, (size_t)L.nb_cap * 4);
+  L.o_cntf = rs_take(o, (size_t)L.nb_cap * 4);
+  L.o_gscr = rs_take(o, (size_t)RS_THREADS * 16);
+  L.o_scan = rs_take(o, (size_t)RS_THREADS * 4);
+  L.bytes = o;
+  return L;
+}
+
+template <class T>
+__device__ __forceinline__ T *peer(cg::cluster_group &cl, T *p, int rank) {
+  return cl.map_shared_rank(p, rank);
+}
+
+__device__ __forceinline__ float4 f4zero() { return make_float4(0.0f, 0.0f, 0.0f, 0.0f); }
+
+// st->red[slot] = sum (rank order, in double) / max of the CTAs' published partials
+__device__ double combine_sum(cg::cluster_group &cl, int C, float *pub, int slot) {
+  double a = 0.0;
+  for (int c = 0; c < C; ++c) a += (double)peer(cl, pub, c)[slot];
+  return a;
+}
+__device__ float combine_max(cg::cluster_group &cl, int C, float *pub, int slot) {
+  float a = 0.0f;
+  for (int c = 0; c < C; ++c) a = fmaxf(a, peer(cl, pub, c)[slot]);
+  return a;
+}
+
+// out[c] = A[:, c0 + c] . r for the CTA's columns.  G lanes per column, each lane keeping
+// U x V float4 loads in flight over V adjacent columns.  r is the full residual in shared
+// memory, zero in the padding rows (as A is).
+template <int G, int U, int V>
+__device__ void at_own_t(const float *A, int lda, int q4, int c0, int nc, const float *r, float *out) {
+  constexpr int PW = 32 / G;
+  constexpr int STEP = RS_WARPS * PW * V;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int gl = lane % G, gsub = lane / G;
+  const float4 *r4 = reinterpret_cast<const float4 *>(r);
+  for (int base = 0; base < nc; base += STEP) {
+    const int col0 = base + (wid * PW + gsub) * V;
+    float acc[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) acc[v] = 0.0f;
+    for (int i0 = gl; i0 < q4; i0 += U * G) {
+      float4 a[V][U];
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        const float4 *a4 = reinterpret_cast<const float4 *>(A + (size_t)(c0 + col0 + v) * lda);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int i = i0 + u * G;
+          a[v][u] = (col0 + v < nc && i < q4) ? __ldcg(a4 + i) : f4zero();
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int i = i0 + u * G;
+        if (i < q4) {
+          const float4 rr = r4[i];
+#pragma unroll
+          for (int v = 0; v < V; ++v) {
+            acc[v] = fmaf(a[v][u].x, rr.x, acc[v]);
+            acc[v] = fmaf(a[v][u].y, rr.y, acc[v]);
+            acc[v] = fmaf(a[v][u].z, rr.z, acc[v]);
+            acc[v] = fmaf(a[v][u].w, rr.w, acc[v]);
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      float s = acc[v];
+#pragma unroll
+      for (int o = G >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (gl == 0 && col0 + v < nc) out[col0 + v] = s;
+    }
+  }
+}
+
+__device__ void at_own(const float *A, int lda, int q4, int c0, int nc, const float *r, float *out) {
+  if (q4 >= 256) at_own_t<32, 8, 1>(A, lda, q4, c0, nc, r, out);
+  else if (q4 >= 128) at_own_t<32, 4, 2>(A, lda, q4, c0, nc, r, out);
+  else if (q4 >= 64) at_own_t<32, 2, 4>(A, lda, q4, c0, nc, r, out);
+  else if (q4 >= 32) at_own_t<16, 2, 4>(A, lda, q4, c0, nc, r, out);
+  else at_own_t<8, 4, 2>(A, lda, q4, c0, nc, r, out);
+}
+
+// part (lda floats) = sum over the CTA's support entries e (ascending) of
+// A[:, c0 + sidx[e]] * v[sidx[e]].  Up to 512 row quads: one pass of the CTA, entries split
+// over P = 512 / TG thread groups whose partial vectors are then summed in group order.
+__device__ void av_own_partial(const float *A, int lda, int q4, int c0, const int *sidx, int s_own,
+                               const float *v, float *part, float4 *gscr) {
+  float4 *part4 = reinterpret_cast<float4 *>(part);
+  const int tg = q4 >= RS_THREADS ? RS_THREADS : (q4 + 31) / 32 * 32;
+  const int P = RS_THREADS / tg;
+  if (P == 1) {
+    // rows t, t + 512, t + 1024, t + 1536 (q4 <= 2048)
+    const int t = threadIdx.x;
+    float4 acc[4] = {f4zero(), f4zero(), f4zero(), f4zero()};
+    int e = 0;
+    for (; e + 1 < s_own; e += 2) {
+      const int ca = sidx[e], cb = sidx[e + 1];
+      const float wa = v[ca], wb = v[cb];
+      const float4 *aa = reinterpret_cast<const float4 *>(A + (size_t)(c0 + ca) * lda);
+      const float4 *ab = reinterpret_cast<const float4 *>(A + (size_t)(c0 + cb) * lda);
+      float4 la[4], lb[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int i = t + q * RS_THREADS;
+        la[q] = i < q4 ? __ldcg(aa + i) : f4zero();
+        lb[q] = i < q4 ? __ldcg(ab + i) : f4zero();
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        acc[q].x = fmaf(la[q].x, wa, acc[q].x); acc[q].y = fmaf(la[q].y, wa, acc[q].y);
+        acc[q].z = fmaf(la[q].z, wa, acc[q].z); acc[q].w = fmaf(la[q].w, wa, acc[q].w);
+        acc[q].x = fmaf(lb[q].x, wb, acc[q].x); acc[q].y = fmaf(lb[q].y, wb, acc[q].y);
+        acc[q].z = fmaf(lb[q].z, wb, acc[q].z); acc[q].w = fmaf(lb[q].w, wb, acc[q].w);
+      }
+    }
+    if (e < s_own) {
+      const int ca = sidx[e];
+      const float wa = v[ca];
+      const float4 *aa = reinterpret_cast<const float4 *>(A + (size_t)(c0 + ca) * lda);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int i = t + q * RS_THREADS;
+        const float4 la = i < q4 ? __ldcg(aa + i) : f4zero();
+        acc[q].x = fmaf(la.x, wa, acc[q].x); acc[q].y = fmaf(la.y, wa, acc[q].y);
+        acc[q].z = fmaf(la.z, wa, acc[q].z); acc[q].w = fmaf(la.w, wa, acc[q].w);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int i = t + q * RS_THREADS;
+      if (i < q4) part4[i] = acc[q];
+    }
+  } else {
+    // one row quad per thread; group p takes entries p, p + P, ... four at a time
+    const int p = threadIdx.x / tg, t = threadIdx.x % tg;
+    float4 acc = f4zero();
+    if (p < P && t < q4) {
+      int e = p;
+      for (; e + 3 * P < s_own; e += 4 * P) {
+        float4 l[4];
+        float w[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int c = sidx[e + u * P];
+          w[u] = v[c];
+          l[u] = __ldcg(reinterpret_cast<const float4 *>(A + (size_t)(c0 + c) * lda) + t);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          acc.x = fmaf(l[u].x, w[u], acc.x); acc.y = fmaf(l[u].y, w[u], acc.y);
+          acc.z = fmaf(l[u].z, w[u], acc.z); acc.w = fmaf(l[u].w, w[u], acc.w);
+        }
+      }
+      for (; e < s_own; e += P) {
+        const int c = sidx[e];
+        const float w = v[c];
+        const float4 l = __ldcg(reinterpret_cast<const float4 *>(A + (size_t)(c0 + c) * lda) + t);
+        acc.x = fmaf(l.x, w, acc.x); acc.y = fmaf(l.y, w, acc.y);
+        acc.z = fmaf(l.z, w, acc.z); acc.w = fmaf(l.w, w, acc.w);
+      }
+      gscr[p * tg + t] = acc;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < q4; i += RS_THREADS) {
+      float4 s = gscr[i];
+      for (int pp = 1; pp < P; ++pp) {
+        const float4 g = gscr[pp * tg + i];
+        s.x += g.x; s.y += g.y; s.z += g.z; s.w += g.w;
+      }
+      part4[i] = s;
+    }
+  }
+}
+
+// Rows [rr0, rr1) (row quads) of the cluster sum of the CTAs' partials (rank order); with
+// sub_y the result is y - sum.  Stored in rowp (and ycopy) when given; returns this thread's
+// sum of squares.
+__device__ float reduce_rows(cg::cluster_group &cl, int C, float *part, int rr0, int rr1, const float *ypart,
+                             float *rowp, float *ycopy) {
+  float s2 = 0.0f;
+  const float4 *y4 = reinterpret_cast<const float4 *>(ypart);
+  float4 *o4 = reinterpret_cast<float4 *>(rowp);
+  float4 *c4 = reinterpret_cast<float4 *>(ycopy);
+  for (int i = rr0 + threadIdx.x; i < rr1; i += RS_THREADS) {
+    float4 s = f4zero();
+    for (int c = 0; c < C; ++c) {
+      const float4 p = reinterpret_cast<const float4 *>(peer(cl, part, c))[i];
+      s.x += p.x; s.y += p.y; s.z += p.z; s.w += p.w;
+    }
+    if (ypart) {
+      const float4 yy = y4[i - rr0];
+      s.x = yy.x - s.x; s.y = yy.y - s.y; s.z = yy.z - s.z; s.w = yy.w - s.w;
+    }
+    if (rowp) o4[i - rr0] = s;
+    if (ycopy) c4[i - rr0] = s;
+    s2 = fmaf(s.x, s.x, s2);
+    s2 = fmaf(s.y, s.y, s2);
+    s2 = fmaf(s.z, s.z, s2);
+    s2 = fmaf(s.w, s.w, s2);
+  }
+  return s2;
+}
+
+// r (all q4 row quads) from the CTAs' row shares
+__device__ void gather_rows(cg::cluster_group &cl, int C, int q4, int RB, float *rowp, float *r) {
+  float4 *r4 = reinterpret_cast<float4 *>(r);
+  for (int c = 0; c < C; ++c) {
+    const int a = min(q4, c * RB), b = min(q4, a + RB);
+    const float4 *src = reinterpret_cast<const float4 *>(peer(cl, rowp, c));
+    for (int i = a + threadIdx.x; i < b; i += RS_THREADS) r4[i] = src[i - a];
+  }
+}
+
+// the k-th bin scan of k_kbin (gb_solver.cu) by the CTA over counters cnt[0, max_bin)
+// (shared memory, or the cluster's global key histogram read at L2); same results.
+template <bool GLOBAL>
+__device__ void block_kbin(GbState *st, const int *cnt, int k, int *scan, int *res) {
+  const int t = threadIdx.x;
+  const int max_bin = st->max_bin;
+  const int CH = (max_bin + RS_THREADS - 1) / RS_THREADS;
+  const int b0 = t * CH, b1 = min(b0 + CH, max_bin);
+  auto ld = [&](int b) { return GLOBAL ? __ldcg(cnt + b) : cnt[b]; };
+  int csum = 0;
+  for (int b = b0; b < b1; ++b) csum += ld(b);
+  scan[t] = csum;
+  if (t == 0) { res[0] = -2; res[1] = 0; }
+  __syncthreads();
+  for (int off = 1; off < RS_THREADS; off <<= 1) {
+    const int v = t >= off ? scan[t - off] : 0;
+    __syncthreads();
+    scan[t] += v;
+    __syncthreads();
+  }
+  const int incl = scan[t], excl = incl - csum;
+  if (k > 0 && excl < k && incl >= k) {
+    int s = excl;
+    for (int b = b0; b < b1; ++b) {
+      s += ld(b);
+      if (s >= k) { res[0] = b; res[1] = s; break; }
+    }
+  }
+  __syncthreads();
+  if (t == 0) {
+    int k_bin, sum;
+    if (k <= 0) { k_bin = -1; sum = 0; }
+    else if (res[0] == -2) { k_bin = max_bin - 1; sum = scan[RS_THREADS - 1]; }
+    else { k_bin = res[0]; sum = res[1]; }
+    const float intercept = st->max_value;
+    const float slope = st->slope;
+    if (sum < k) {
+      st->alpha_bin = st->alpha_bin * 0.5f;
+      st->max_bin = (int)((float)st->num_bins * (1.0f - st->alpha_bin));
+    }
+    st->min_val = intercept - (float)(k_bin + 1) / slope;
+    st->k_bin = k_bin;
+    st->sum = sum;
+  }
+  __syncthreads();
+}
+
+// sidx = ascending { c < nc : bins[c] <= kb }; returns the count (every thread)
+__device__ int compact_own(const int *bins, int nc, int kb, int *sidx, int *wcnt) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int running = 0;
+  for (int base = 0; base < nc; base += RS_THREADS) {
+    const int c = base + threadIdx.x;
+    const bool in = c < nc && bins[c] <= kb;
+    const unsigned bal = __ballot_sync(0xffffffffu, in);
+    if (lane == 0) wcnt[wid] = __popc(bal);
+    __syncthreads();
+    int wb = 0, tot = 0;
+    for (int w = 0; w < RS_WARPS; ++w) {
+      const int cw = wcnt[w];
+      if (w < wid) wb += cw;
+      tot += cw;
+    }
+    if (in) sidx[running + wb + __popc(bal & ((1u << lane) - 1u))] = c;
+    running += tot;
+    __syncthreads();
+  }
+  return running;
+}
+
+// LinearBinning of the CTA's entries of v into bins and the CTA's counters (k_hist)
+__device__ void hist_own(const GbState *st, const float *v, int *bins, int nc, int *cnt, int *gcnt) {
+  const float intercept = st->max_value;
+  const float slope = st->slope;
+  const float small_f = __double2float_rd((double)intercept * 0.000001);
+  const int max_bin = st->max_bin;
+  for (int c = threadIdx.x; c < nc; c += RS_THREADS) {
+    bool counted;
+    const int b = lin_bin(v[c], slope, intercept, small_f, counted);
+    bins[c] = b;
+    if (counted && b < max_bin) {
+      const unsigned act = __activemask();
+      const unsigned same = __match_any_sync(act, b);
+      if ((int)(threadIdx.x & 31) == __ffs(same) - 1) {
+        if (gcnt) atomicAdd(&gcnt[b], __popc(same));
+        else atomicAdd(&cnt[b], __popc(same));
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(RS_THREADS, 1) k_resident_niht(const RsParams P) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int s_q;
+  __shared__ float red32[32];
+  __shared__ int wcnt[RS_WARPS];
+  __shared__ int kres[2];
+  cg::cluster_group cl = cg::this_cluster();
+  const int C = (int)cl.num_blocks(), rank = (int)cl.block_rank();
+  const int cid = blockIdx.x / C;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const RsLayout L = rs_layout(P.n_cap, P.m_cap, C);
+  GbState *st = reinterpret_cast<GbState *>(smem + L.o_st);
+  float *pub = reinterpret_cast<float *>(smem + L.o_pub);
+  int *ipub = reinterpret_cast<int *>(pub + RS_NPUB);
+  float *x = reinterpret_cast<float *>(smem + L.o_x);
+  float *grad = reinterpret_cast<float *>(smem + L.o_grad);
+  float *x0 = reinterpret_cast<float *>(smem + L.o_x0);
+  int *bins = reinterpret_cast<int *>(smem + L.o_bins);
+  int *sidx = reinterpret_cast<int *>(smem + L.o_sidx);
+  float *r = reinterpret_cast<float *>(smem + L.o_r);
+  float *part = reinterpret_cast<float *>(smem + L.o_part);
+  float *rowp = reinterpret_cast<float *>(smem + L.o_rowp);
+  float *ypart = reinterpret_cast<float *>(smem + L.o_ypart);
+  int *cnt = reinterpret_cast<int *>(smem + L.o_cnt);
+  int *cntf = reinterpret_cast<int *>(smem + L.o_cntf);
+  float4 *gscr = reinterpret_cast<float4 *>(smem + L.o_gscr);
+  int *scan = reinterpret_cast<int *>(smem + L.o_scan);
+  float *A = P.A + (size_t)cid * P.a_stride;
+  int *xh = P.xhist + (size_t)cid * P.n_cap;
+  {
+    unsigned int *w = reinterpret_cast<unsigned int *>(st);
+    for (int i = tid; i < (int)(sizeof(GbState) / 4); i += RS_THREADS) w[i] = 0u;
+  }
+  __syncthreads();
+  for (;;) {
+    // ---- next trial: rank 0 takes it from the queue, the others read it from rank 0
+    if (rank == 0 && tid == 0) s_q = atomicAdd(P.queue, 1);
+    cl.sync();
+    const int q = *peer(cl, &s_q, 0);
+    if (q >= P.T) break;
+    const int t = P.order[q];
+    const int m = P.m[t], n = P.n[t];
+    const int lda = (m + 31) / 32 * 32, q4 = lda / 4;
+    const int CH = (n + C - 1) / C;
+    const int c0 = min(n, rank * CH), nc = min(n, c0 + CH) - c0;
+    const int RB = (q4 + C - 1) / C;
+    const int rr0 = min(q4, rank * RB), rr1 = min(q4, rr0 + RB);
+    const uint32_t key = P.seed + (P.tid ? P.tid[t] : (uint32_t)t);
+    if (tid == 0) {
+      batch_trial_fields(st, t, m, n, P.k[t], P.maxiter, GB_ALG_NIHT);
+      st->lda = lda;
+    }
+    // ---- draw the trial (k_b_gen_A, k_b_gen_x, key bins, y = A x0 of gb_batch.cu)
+    for (int col = wid; col < nc; col += RS_WARPS) {
+      const int j = c0 + col;
+      float *cp = A + (size_t)j * lda;
+      gbgen::gen_dense_column(cp, j, m, key, 0u, 1, lane, 32);
+      for (int i = m + lane; i < lda; i += 32) cp[i] = 0.0f;
+    }
+    float mx = 0.0f;
+    for (int c = tid; c < nc; c += RS_THREADS) {
+      const int j = c0 + c;
+      uint32_t o[4];
+      gbgen::philox((uint32_t)(j >> 2), 0u, gbgen::ST_VALUES, 0u, key, gbgen::KEY_HI, o);
+      x0[c] = signbit(gbgen::u01(o[j & 3]) - 0.5f) ? -1.0f : 1.0f;
+      gbgen::philox((uint32_t)(j >> 2), 0u, gbgen::ST_SUPPORT, 0u, key, gbgen::KEY_HI, o);
+      const float u = gbgen::u01(o[j & 3]);
+      grad[c] = u;  // the support keys, until the solve starts
+      mx = fmaxf(mx, u);
+      __stcg(xh + j, 0);
+    }
+    {
+      const float b = block_reduce<1>(mx, red32);
+      if (tid == 0) pub[R_XMAX] = b;
+    }
+    __threadfence();
+    cl.sync();
+    if (tid == 0) {
+      // n linear bins over the keys (createVector.cu:236-248)
+      st->red[R_XMAX] = (double)combine_max(cl, C, pub, R_XMAX);
+      st->max_value = (float)st->red[R_XMAX];
+      st->slope = ((float)(st->n - 1) / st->max_value);
+      st->max_bin = st->n;
+      st->alpha_bin = 0.25f;
+      st->flags[F_DOBIN] = 1;
+    }
+    __syncthreads();
+    hist_own(st, grad, bins, nc, nullptr, xh);
+    __threadfence();
+    cl.sync();
+    block_kbin<true>(st, xh, st->k, scan, kres);
+    // the counts came through global memory: every CTA takes rank 0's scan result, so the
+    // copies of the state stay identical whatever each CTA read
+    cl.sync();
+    if (tid == 0) {
+      if (rank != 0) {
+        const GbState *s0 = peer(cl, st, 0);
+        st->k_bin = s0->k_bin;
+        st->sum = s0->sum;
+        st->min_val = s0->min_val;
+        st->alpha_bin = s0->alpha_bin;
+        st->max_bin = s0->max_bin;
+      }
+      st->k = st->sum;  // |support| >= k, the k the solver is given
+    }
+    __syncthreads();
+    {
+      const int kb = st->k_bin;
+      for (int c = tid; c < nc; c += RS_THREADS)
+        if (bins[c] > kb) x0[c] = 0.0f;
+    }
+    int s_own = compact_own(bins, nc, st->k_bin, sidx, wcnt);
+    av_own_partial(A, lda, q4, c0, sidx, s_own, x0, part, gscr);
+    cl.sync();
+    {
+      const float s2 = reduce_rows(cl, C, part, rr0, rr1, nullptr, rowp, ypart);
+      const float b = block_reduce<0>(s2, red32);
+      if (tid == 0) pub[R_RES] = b;
+    }
+    cl.sync();
+    gather_rows(cl, C, q4, RB, rowp, r);
+    if (tid == 0) {
+      st->red[R_RES] = combine_sum(cl, C, pub, R_RES);
+      batch_solver_init(st, P.tol_rel, 0);
+      // NIHT prologue (algorithms.cu:1296-1354): resid = y; err = ||y||
+      ctrl_phase(st, C_INIT0, 0);
+    }
+    __syncthreads();
+    // x = A^T y ; max|x| ; FindSupportSet ; Threshold
+    at_own(A, lda, q4, c0, nc, r, x);
+    __syncthreads();
+    {
+      float mxx = 0.0f;
+      for (int c = tid; c < nc; c += RS_THREADS) mxx = fmaxf(mxx, fabsf(x[c]));
+      for (int b = tid; b < L.nb_cap; b += RS_THREADS) cnt[b] = 0;
+      const float b = block_reduce<1>(mxx, red32);
+      if (tid == 0) pub[R_XMAX] = b;
+    }
+    cl.sync();
+    if (tid == 0) {
+      st->red[R_XMAX] = (double)combine_max(cl, C, pub, R_XMAX);
+      ctrl_phase(st, C_INIT_BINPREP, 0);
+    }
+    __syncthreads();
+    // the support step (enq_support): bins and the k-th bin when binning, threshold always
+    auto support = [&]() {
+      const bool dobin = st->flags[F_DOBIN] != 0;
+      if (dobin) {
+        hist_own(st, x, bins, nc, cnt, nullptr);
+        cl.sync();
+        const int mb = st->max_bin;
+        for (int b = tid; b < mb; b += RS_THREADS) {
+          int s = 0;
+          for (int c = 0; c < C; ++c) s += peer(cl, cnt, c)[b];
+          cntf[b] = s;
+        }
+        __syncthreads();
+        block_kbin<false>(st, cntf, st->k, scan, kres);
+      }
+      const int kb = st->k_bin;
+      for (int c = tid; c < nc; c += RS_THREADS)
+        if (bins[c] > kb) x[c] = 0.0f;
+      if (dobin) s_own = compact_own(bins, nc, kb, sidx, wcnt);
+      __syncthreads();
+    };
+    support();
+    if (tid == 0) ctrl_phase(st, C_INIT_DONE, 0);
+    __syncthreads();
+    // ---- NIHT iterations (RestrictedSD, GAGA/gaga/functions.cu:659-745, then the support)
+    while (st->active) {
+      // resid = y - A x_S ; ||resid||^2
+      av_own_partial(A, lda, q4, c0, sidx, s_own, x, part, gscr);
+      if (tid == 0) ipub[0] = s_own;
+      cl.sync();
+      {
+        const float s2 = reduce_rows(cl, C, part, rr0, rr1, ypart, rowp, nullptr);
+        const float b = block_reduce<0>(s2, red32);
+        if (tid == 0) pub[R_RES] = b;
+      }
+      cl.sync();
+      gather_rows(cl, C, q4, RB, rowp, r);
+      if (tid == 0) {
+        st->red[R_RES] = combine_sum(cl, C, pub, R_RES);
+        int sc = 0;
+        for (int c = 0; c < C; ++c) sc += peer(cl, ipub, c)[0];
+        st->s_cnt = sc;
+        ctrl_phase(st, C_PUSH_RES, 0);
+      }
+      __syncthreads();
+      // grad = A^T resid ; ||grad on the support||^2 ; max|grad|
+      at_own(A, lda, q4, c0, nc, r, grad);
+      __syncthreads();
+      {
+        const int kb = st->k_bin;
+        float s2 = 0.0f, gm = 0.0f;
+        for (int c = tid; c < nc; c += RS_THREADS) {
+          const float g = grad[c];
+          const float o = bins[c] <= kb ? g : 0.0f;
+          s2 = fmaf(o, o, s2);
+          gm = fmaxf(gm, fabsf(g));
+        }
+        const float b1 = block_reduce<0>(s2, red32);
+        if (tid == 0) pub[R_XT] = b1;
+        const float b2 = block_reduce<1>(gm, red32);
+        if (tid == 0) pub[R_GMAX] = b2;
+      }
+      cl.sync();
+      if (tid == 0) {
+        st->red[R_XT] = combine_sum(cl, C, pub, R_XT);
+        st->red[R_GMAX] = (double)combine_max(cl, C, pub, R_GMAX);
+      }
+      // ||A x_thres||^2 (x_thres = grad on the support)
+      av_own_partial(A, lda, q4, c0, sidx, s_own, grad, part, gscr);
+      cl.sync();
+      {
+        const float s2 = reduce_rows(cl, C, part, rr0, rr1, nullptr, nullptr, nullptr);
+        const float b = block_reduce<0>(s2, red32);
+        if (tid == 0) pub[R_AXT] = b;
+      }
+      cl.sync();
+      if (tid == 0) {
+        st->red[R_AXT] = combine_sum(cl, C, pub, R_AXT);
+        ctrl_phase(st, C_SD_MU, 0);
+      }
+      __syncthreads();
+      // x += mu grad ; max|x| ; counters cleared
+      {
+        const float mu = st->mu;
+        float mxx = 0.0f;
+        for (int c = tid; c < nc; c += RS_THREADS) {
+          const float o = fmaf(mu, grad[c], x[c]);
+          x[c] = o;
+          mxx = fmaxf(mxx, fabsf(o));
+        }
+        for (int b = tid; b < L.nb_cap; b += RS_THREADS) cnt[b] = 0;
+        const float b = block_reduce<1>(mxx, red32);
+        if (tid == 0) pub[R_XMAX] = b;
+      }
+      cl.sync();
+      if (tid == 0) {
+        st->red[R_XMAX] = (double)combine_max(cl, C, pub, R_XMAX);
+        ctrl_phase(st, C_BINPREP, 0);
+      }
+      __syncthreads();
+      support();
+      if (tid == 0) ctrl_phase(st, C_NIHT_STOP, 0);
+      __syncthreads();
+    }
+    // ---- verdict (k_b_err and the result phase of gb_batch.cu)
+    {
+      float e2 = 0.0f, x2 = 0.0f;
+      for (int c = tid; c < nc; c += RS_THREADS) {
+        const float d = x0[c] - x[c];
+        e2 = fmaf(d, d, e2);
+        x2 = fmaf(x0[c], x0[c], x2);
+      }
+      const float b1 = block_reduce<0>(e2, red32);
+      if (tid == 0) pub[R_DOT1] = b1;
+      const float b2 = block_reduce<0>(x2, red32);
+      if (tid == 0) pub[R_DOT2] = b2;
+    }
+    cl.sync();
+    if (rank == 0 && tid == 0) {
+      const double e2 = combine_sum(cl, C, pub, R_DOT1), x2 = combine_sum(cl, C, pub, R_DOT2);
+      const float rel = (float)(sqrt(e2) / sqrt(x2));
+      P.iters[t] = st->iter;
+      P.err[t] = rel;
+      P.ok[t] = rel <= 1e-3f ? 1 : 0;
+      atomicAdd(P.bytes, st->bytes);
+    }
+  }
+  cl.sync();  // no CTA leaves while a peer may still read its shared memory
+}
+
+struct ResEngine {
+  int dev = -1, n_cap = 0, m_cap = 0, C = 0, ncl = 0, t_cap = 0;
+  size_t smem = 0, a_stride = 0;
+  float *A = nullptr;
+  int *xhist = nullptr;
+  int *order = nullptr, *queue = nullptr;
+};
+std::map<int, ResEngine> g_res;
+std::atomic<unsigned long long> g_attr_done{0};
+
+void res_release(ResEngine &R) {
+  if (R.A) cudaFree(R.A);
+  if (R.xhist) cudaFree(R.xhist);
+  if (R.order) cudaFree(R.order);
+  R = ResEngine();
+}
+
+}  // namespace
+
+int gb_resident_max_smem() {
+  int dev = 0, optin = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, (const void *)k_resident_niht) != cudaSuccess) return 0;
+  return optin - (int)fa.sharedSizeBytes;
+}
+
+size_t gb_resident_smem(int n_cap, int m_cap, int C) { return rs_layout(n_cap, m_cap, C).bytes; }
+
+int gb_resident_pick_cluster(int n_cap, int m_cap, int requested) {
+  const int cap = gb_resident_max_smem();
+  if (m_cap > 8192 || n_cap > 20000 || cap <= 0) return 0;
+  auto fits = [&](int C) { return (long long)gb_resident_smem(n_cap, m_cap, C) <= (long long)cap; };
+  if (requested > 0) return (requested <= 16 && fits(requested)) ? requested : 0;
+  // four CTAs per trial measured best over the sweep's mix (n = 1024 ... 8192) on GB300
+  int C = 4;
+  while (C < 16 && !fits(C)) C *= 2;
+  return fits(C) ? C : 0;
+}
+
+gb_status gb_resident_enqueue(const GbResidentArgs &a, cudaStream_t s) {
+  int dev = 0;
+  GB_CUDA_TRY(cudaGetDevice(&dev));
+  const int C = gb_resident_pick_cluster(a.n_cap, a.m_cap, a.cluster);
+  if (C <= 0) {
+    gb_set_error_message("resident form: no cluster size fits the trial sizes", __FILE__, __LINE__);
+    return GB_BAD_ARG;
+  }
+  GB_TRY(gb_once_per_device(g_attr_done, [&]() -> gb_status {
+    const int cap = gb_resident_max_smem();
+    GB_CUDA_TRY(cudaFuncSetAttribute((const void *)k_resident_niht, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+    GB_CUDA_TRY(cudaFuncSetAttribute((const void *)k_resident_niht, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    return GB_OK;
+  }));
+  ResEngine &R = g_res[dev];
+  const size_t smem = gb_resident_smem(a.n_cap, a.m_cap, C);
+  cudaLaunchConfig_t cfg;
+  memset(&cfg, 0, sizeof(cfg));
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(RS_THREADS, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (R.dev != dev || R.n_cap < a.n_cap || R.m_cap < a.m_cap || R.C != C || R.t_cap < a.count) {
+    res_release(R);
+    int sms = 0;
+    GB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    cfg.gridDim = dim3(sms / C * C, 1, 1);
+    int ncl = 0;
+    GB_CUDA_TRY(cudaOccupancyMaxActiveClusters(&ncl, (void *)k_resident_niht, &cfg));
+    if (ncl <= 0) {
+      gb_set_error_message("resident form: no cluster can be resident", __FILE__, __LINE__);
+      return GB_CUDA_ERROR;
+    }
+    const size_t a_stride = (size_t)((a.m_cap + 31) / 32 * 32) * a.n_cap;
+    size_t free_b = 0, total_b = 0;
+    GB_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+    while (ncl > 1 && (double)ncl * a_stride * 4.0 > 0.5 * (double)free_b) ncl--;
+    R.dev = dev;
+    R.n_cap = a.n_cap;
+    R.m_cap = a.m_cap;
+    R.C = C;
+    R.ncl = ncl;
+    R.smem = smem;
+    R.a_stride = a_stride;
+    R.t_cap = std::max(a.count, 1024);
+    GB_CUDA_TRY(cudaMalloc(&R.A, (size_t)ncl * a_stride * 4));
+    GB_CUDA_TRY(cudaMalloc(&R.xhist, (size_t)ncl * a.n_cap * 4));
+    GB_CUDA_TRY(cudaMalloc(&R.order, (size_t)(R.t_cap + 64) * 4));
+    R.queue = R.order + R.t_cap;
+  }
+  GB_CUDA_TRY(cudaMemcpyAsync(R.order, a.order, (size_t)a.count * 4, cudaMemcpyHostToDevice, s));
+  GB_CUDA_TRY(cudaMemsetAsync(R.queue, 0, 4, s));
+  RsParams P;
+  P.T = a.count;
+  P.seed = a.seed;
+  P.tol_rel = a.tol_rel;
+  P.maxiter = a.maxiter;
+  P.n = a.n;
+  P.m = a.m;
+  P.k = a.k;
+  P.tid = a.tid;
+  P.order = R.order;
+  P.queue = R.queue;
+  P.iters = a.iters;
+  P.err = a.err;
+  P.ok = a.ok;
+  P.bytes = a.bytes;
+  P.A = R.A;
+  P.a_stride = R.a_stride;
+  P.xhist = R.xhist;
+  P.n_cap = R.n_cap;
+  P.m_cap = R.m_cap;
+  cfg.gridDim = dim3(R.ncl * C, 1, 1);
+  cfg.dynamicSmemBytes = gb_resident_smem(R.n_cap, R.m_cap, C);
+  GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_resident_niht, P));
+  return GB_OK;
+}
+
+int gb_resident_last_cluster() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  auto it = g_res.find(dev);
+  return it == g_res.end() ? 0 : it->second.C;
+}

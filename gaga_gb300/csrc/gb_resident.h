@@ -1,0 +1,36 @@
+// gb_resident.h -- the cluster-resident NIHT kernel of the batched form (gb_resident.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "gb_internal.cuh"
+
+// trials with n <= this go to the resident kernel unless the caller says otherwise
+#define GB_RESIDENT_N_DEFAULT 8192
+
+// One launch solving `count` NIHT trials, trial order[q] for q < count (indices into the
+// batch tables n, m, k, tid and the result arrays, all device pointers), each by one
+// cluster of CTAs.  n_cap / m_cap bound the trials' n and m; cluster = CTAs per cluster
+// (0: four, or the smallest power of two above that the sizes fit).
+struct GbResidentArgs {
+  int count;
+  const int *order;  // host array of count trial indices, largest first
+  const int *n, *m, *k;
+  const unsigned int *tid;
+  unsigned int seed;
+  float tol_rel;
+  int maxiter;
+  int *iters;
+  float *err;
+  int *ok;
+  double *bytes;
+  int n_cap, m_cap, cluster;
+};
+
+gb_status gb_resident_enqueue(const GbResidentArgs &a, cudaStream_t s);
+// CTAs per cluster the resident form uses for these sizes (0: the sizes do not fit)
+int gb_resident_pick_cluster(int n_cap, int m_cap, int requested);
+// shared memory per CTA, and the most a CTA can have
+size_t gb_resident_smem(int n_cap, int m_cap, int C);
+int gb_resident_max_smem();
+// cluster size of the last resident launch on this device (0: none)
+int gb_resident_last_cluster();

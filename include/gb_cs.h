@@ -243,6 +243,11 @@ typedef struct {
   int slots;                     /* schedule: concurrent trial slots (0: 16, fewer if memory is short) */
   int sm_share;                  /* schedule: SMs each slot's kernels are shaped for (0: half the GPU) */
   void *stream;
+  int resident_n;                /* NIHT: trials with n <= resident_n are solved by the cluster-resident
+                                    kernel, one thread-block cluster per trial, while the slots take
+                                    the others (0: 8192; < 0: slots only) */
+  int cluster;                   /* CTAs per cluster of the resident kernel (0: 4, more if the
+                                    trial sizes need more shared memory than 4 CTAs have) */
 } gb_batch;
 
 gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float *rel_err_out,

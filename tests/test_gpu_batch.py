@@ -80,12 +80,13 @@ def test_batch_schedule_and_autotune(gb, tmp_path, monkeypatch):
     tid = np.arange(len(n), dtype=np.uint32)
     ref = gb.solve_batch(n, m, k, SEED, tid, alg="NIHT", maxiter=1000)
     for slots, share in ((4, 38), (12, 152)):
-        got = gb.solve_batch(n, m, k, SEED, tid, alg="NIHT", maxiter=1000, slots=slots, sm_share=share)
+        got = gb.solve_batch(n, m, k, SEED, tid, alg="NIHT", maxiter=1000, slots=slots, sm_share=share,
+                             resident_n=-1)
         assert got[0] == ref[0] == len(n)
     res = autotune.tune_batch(n, m, k, SEED, tid, alg="NIHT", maxiter=1000, stride=2, slots=(4, 8),
-                              fractions=(0.5, 1.0))
+                              fractions=(0.5, 1.0), clusters=(4,))
     assert (res["slots"], res["sm_share"]) in {(c["slots"], c["sm_share"]) for c in res["candidates"]}
     assert len(res["candidates"]) == 4 and not res["cached"]
     again = autotune.tune_batch(n, m, k, SEED, tid, alg="NIHT", maxiter=1000, stride=2, slots=(4, 8),
-                                fractions=(0.5, 1.0))
+                                fractions=(0.5, 1.0), clusters=(4,))
     assert again["cached"] and again["slots"] == res["slots"]
