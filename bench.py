@@ -292,6 +292,7 @@ def bench_ours(args):
     mv = matvec_roofline(peak, peak_kind)
     line["roofline"] = mv["at"]
     line["matvec"] = mv
+    line["resident"] = resident_roofline(peak, peak_kind, cluster=sched.get("cluster", 0))
     line["gemm"] = gemm_roofline(tpeak, tpeak_kind)
     line["operators"] = operators_roofline(peak, peak_kind)
     if args.plain_trials > 0 and world == 1:
@@ -500,6 +501,36 @@ def matvec_roofline(peak, peak_kind, m=14746, n=16384, k=5000, reps=20):
     return res
 
 
+def resident_roofline(peak, peak_kind, max_n=8192, sample=0, cluster=0):
+    """The cluster-resident NIHT kernel alone (k_resident_niht, one launch) on the first
+    wave's trials with n <= max_n (every one, or `sample` evenly spaced), timed with CUDA
+    events around the batched call; algorithmic operator bytes of its iterations per second.
+    Trials whose slab of A fits in L2 re-read it from there, so the DRAM traffic can be
+    below the algorithmic bytes."""
+    import gaga_gb300 as gb
+
+    n, m, k, tid = wave_arrays(0)
+    sel = np.flatnonzero(n <= max_n)
+    if sample:
+        sel = sel[np.linspace(0, len(sel) - 1, min(sample, len(sel))).astype(int)]
+    n, m, k, tid = n[sel], m[sel], k[sel], tid[sel]
+    for _ in range(2):  # the first call sizes the kernel's buffers
+        ns, iters, err, ok = gb.solve_batch(n, m, k, SEED, tid, alg="NIHT", tol_rel=TOL_REL, maxiter=MAXITER,
+                                            resident_n=max_n, cluster=cluster)
+    nbytes, ms = gb.batch_last_stats()
+    achieved = nbytes / (ms / 1e3) / 1e9
+    out = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+           "kernel": "k_resident_niht", "trials": int(len(n)), "recovered": int(ns), "iterations": int(iters.sum()),
+           "sizes": "n=%s" % sorted(set(n.tolist())), "ms": ms, "algorithmic_bytes": nbytes,
+           "cluster": gb._lib.load().gb_cs_batch_last_cluster(), "peak_source": peak_kind}
+    tr = ncu_traffic().get("k_resident_niht")
+    if tr and not sample and max_n == 8192:
+        out["traffic"] = tr
+        out["traffic_source"] = "ncu dram__bytes_read.sum + dram__bytes_write.sum of the same launch " \
+                                "(profiles/dram_traffic.json)"
+    return out
+
+
 def ncu_traffic():
     """Per-launch DRAM bytes of the dense kernels from the committed ncu summary."""
     try:
@@ -584,6 +615,8 @@ def bench_only(args):
         out = operators_roofline(*peaks())
     elif args.only == "learned":
         out = bench_learned(args)
+    elif args.only == "resident":
+        out = resident_roofline(*peaks(), max_n=args.resident_max_n, sample=args.resident_sample)
     else:
         w = args.warmup
         n, m, k, tid = wave_arrays(w)
@@ -608,7 +641,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--learned-trials", type=int, default=2048)
     ap.add_argument("--retune", action="store_true", help="ignore the autotuner's cache")
-    ap.add_argument("--only", choices=["matvec", "gemm", "operators", "plain", "learned"],
+    ap.add_argument("--resident-max-n", type=int, default=8192, help="--only resident: largest trial n")
+    ap.add_argument("--resident-sample", type=int, default=0, help="--only resident: trials (0: all)")
+    ap.add_argument("--only", choices=["matvec", "gemm", "operators", "plain", "learned", "resident"],
                     help="run one measurement alone and print its JSON (for profiling)")
     args = ap.parse_args()
     if args.warmup < 3:

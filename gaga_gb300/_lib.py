@@ -22,6 +22,7 @@ GB_ALG_FIHT, GB_ALG_ALPS, GB_ALG_CGIHT_PROJ, GB_ALG_PARALLEL_L0 = 7, 8, 9, 14
 EXPORTS = ["gb_cs_version", "gb_cs_last_error", "gb_cs_default_options", "gb_cs_alg_id", "gb_cs_solve",
            "gb_cs_generate_and_solve", "gb_cs_linear_binning", "gb_cs_find_support_set", "gb_cs_find_support_set_sort",
            "gb_cs_operator_apply", "gb_cs_operator_time", "gb_cs_l0_step", "gb_cs_solve_batch", "gb_cs_batch_last_stats",
+           "gb_cs_batch_last_cluster",
            "gb_cs_dense_apply_noalloc", "gb_cs_solve_shared_batch", "gb_cs_shared_last_stats",
            "gb_cs_gemm_bf16_tn", "gb_cs_mlp_num_params", "gb_cs_mlp_features", "gb_cs_mlp_forward",
            "gb_cs_mlp_grad", "gb_cs_mlp_train", "gb_cs_write_result"]
@@ -109,6 +110,8 @@ def load():
     L.gb_cs_solve_batch.restype = i
     L.gb_cs_batch_last_stats.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_float)]
     L.gb_cs_batch_last_stats.restype = None
+    L.gb_cs_batch_last_cluster.argtypes = []
+    L.gb_cs_batch_last_cluster.restype = i
     L.gb_cs_dense_apply_noalloc.argtypes = [vp, i, i, i, i, vp, vp, vp]
     L.gb_cs_dense_apply_noalloc.restype = i
     L.gb_cs_solve_shared_batch.argtypes = [C.POINTER(SharedBatch), vp, vp, vp, C.POINTER(C.c_int)]

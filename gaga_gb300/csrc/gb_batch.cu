@@ -556,3 +556,5 @@ extern "C" void gb_cs_batch_last_stats(double *bytes, float *kernel_ms) {
   if (bytes) *bytes = g_last_bytes;
   if (kernel_ms) *kernel_ms = g_last_kernel_ms;
 }
+
+extern "C" int gb_cs_batch_last_cluster(void) { return gb_resident_last_cluster(); }

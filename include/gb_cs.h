@@ -258,6 +258,10 @@ gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float *rel_err_ou
  * counterpart; used for roofline reporting). */
 void gb_cs_batch_last_stats(double *bytes, float *kernel_ms);
 
+/* CTAs per cluster of the last cluster-resident launch of gb_cs_solve_batch on the current
+ * device (0: none yet). */
+int gb_cs_batch_last_cluster(void);
+
 /* ---- shared-matrix batched form (no reference counterpart) ----
  * ntrials NIHT trials y_t = A x0_t that share one dense Gaussian A (drawn from `seed` as
  * gb_cs_generate_and_solve draws it; trial t's +-1 signal x0_t with k[t] nonzeros uses the
