@@ -96,3 +96,32 @@ def test_resident_rejects_oversized_cluster(gb):
     n, m, k, tid = pick([1024], 2)
     with pytest.raises(gb.GagaError):
         gb.solve_batch(n, m, k, SEED, tid, alg="NIHT", resident_n=4096, cluster=32)
+
+
+@pytest.mark.parametrize("cluster", [1, 3, 4, 8])
+def test_resident_ragged_sizes(gb, cluster):
+    """n and m that are not multiples of 4, 32 or the cluster size, tiny and one-row
+    problems: the column and row shares and the zero-padded rows must cover every entry
+    exactly once, so verdicts match the slot graphs."""
+    n = np.array([16, 17, 33, 100, 257, 1000, 1001, 2047, 3001, 5000, 777, 64], dtype=np.int32)
+    m = np.array([1, 9, 20, 37, 130, 333, 500, 999, 1500, 2501, 388, 63], dtype=np.int32)
+    k = np.maximum(1, (m // 8)).astype(np.int32)
+    tid = np.arange(len(n), dtype=np.uint32) + 40000
+    res = gb.solve_batch(n, m, k, SEED, tid, alg="NIHT", maxiter=500, resident_n=8192, cluster=cluster)
+    slots = gb.solve_batch(n, m, k, SEED, tid, alg="NIHT", maxiter=500, resident_n=-1)
+    assert np.all(np.isfinite(res[2]))
+    assert np.sum(res[3] == slots[3]) >= len(n) - 1, (res[3], slots[3])
+    both = (res[3] == 1) & (slots[3] == 1)
+    assert np.all(res[2][both] < 1e-3)
+
+
+def test_resident_largest_rows(gb):
+    """m up to 8192 rows (four row quads per thread in A x_S) at n = 8192."""
+    n = np.array([8192, 8192, 8192], dtype=np.int32)
+    m = np.array([8192, 7373, 4096], dtype=np.int32)
+    k = np.array([400, 1500, 800], dtype=np.int32)
+    tid = np.arange(3, dtype=np.uint32) + 50000
+    res = gb.solve_batch(n, m, k, SEED, tid, alg="NIHT", maxiter=400, resident_n=8192, cluster=8)
+    slots = gb.solve_batch(n, m, k, SEED, tid, alg="NIHT", maxiter=400, resident_n=-1)
+    assert np.array_equal(res[3], slots[3])
+    assert np.all(res[2][res[3] == 1] < 1e-3)
