@@ -21,6 +21,7 @@
 
 #include <algorithm>
 #include <map>
+#include <mutex>
 #include <vector>
 
 #include "gb_ctrl.cuh"
@@ -370,6 +371,14 @@ int slots_for(int n_cap, int m_cap, size_t free_bytes, int T, int requested) {
 static thread_local double g_last_bytes = 0.0;
 static thread_local float g_last_kernel_ms = 0.0f;
 
+// The engines (slot graphs, resident buffers) are per device and shared by every caller, so
+// calls from several host threads run one at a time; recursive because the learned warm
+// start's fallback pass calls back in.
+std::recursive_mutex &gb_batch_mutex() {
+  static std::recursive_mutex mu;
+  return mu;
+}
+
 extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float *rel_err_out, int *success_out,
                                        int *num_success) {
   if (!b || b->ntrials < 0 || (b->ntrials > 0 && (!b->n || !b->m || !b->k))) {
@@ -388,6 +397,7 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
     gb_set_error_message("maxiter must be >= 0", __FILE__, __LINE__);
     return GB_BAD_ARG;
   }
+  std::lock_guard<std::recursive_mutex> lock(gb_batch_mutex());
   const int T = b->ntrials;
   int n_cap = 16, m_cap = 1;
   for (int t = 0; t < T; ++t) {

@@ -801,6 +801,7 @@ gb_status gb_resident_enqueue(const GbResidentArgs &a, cudaStream_t s) {
 }
 
 int gb_resident_last_cluster() {
+  std::lock_guard<std::recursive_mutex> lock(gb_batch_mutex());
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
   auto it = g_res.find(dev);

@@ -2,6 +2,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "gb_internal.cuh"
 
 // trials with n <= this go to the resident kernel unless the caller says otherwise
@@ -34,3 +36,5 @@ size_t gb_resident_smem(int n_cap, int m_cap, int C);
 int gb_resident_max_smem();
 // cluster size of the last resident launch on this device (0: none)
 int gb_resident_last_cluster();
+// held for the whole of gb_cs_solve_batch (gb_batch.cu): the engines are shared per device
+std::recursive_mutex &gb_batch_mutex();

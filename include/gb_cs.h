@@ -250,6 +250,8 @@ typedef struct {
                                     trial sizes need more shared memory than 4 CTAs have) */
 } gb_batch;
 
+/* Calls from several host threads run one at a time (the batched form's engines are
+ * shared per device). */
 gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float *rel_err_out,
                             int *success_out, int *num_success);
 

@@ -90,3 +90,25 @@ def test_batch_schedule_and_autotune(gb, tmp_path, monkeypatch):
     again = autotune.tune_batch(n, m, k, SEED, tid, alg="NIHT", maxiter=1000, stride=2, slots=(4, 8),
                                 fractions=(0.5, 1.0), clusters=(4,))
     assert again["cached"] and again["slots"] == res["slots"]
+
+
+def test_batch_calls_from_two_threads(gb):
+    """Two host threads calling the batched form at once (ctypes releases the GIL): the
+    calls are serialised on the shared engines and each returns the single-call result."""
+    import threading
+
+    n, m, k, tid = pick([1024, 2048, 8192, 16384], 12)
+    ref = gb.solve_batch(n, m, k, SEED, tid, alg="NIHT", tol_rel=1e-4, maxiter=600)
+    out = [None, None]
+
+    def work(i):
+        out[i] = gb.solve_batch(n, m, k, SEED, tid, alg="NIHT", tol_rel=1e-4, maxiter=600)
+
+    th = [threading.Thread(target=work, args=(i,)) for i in range(2)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    for o in out:
+        assert o is not None
+        assert np.array_equal(o[1], ref[1]) and np.array_equal(o[2], ref[2]) and np.array_equal(o[3], ref[3])
