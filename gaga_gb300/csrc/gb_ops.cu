@@ -273,6 +273,7 @@ __device__ __forceinline__ float2 cis_pi(float sgn, float num_over_den) {
   return make_float2(c, sgn * s);
 }
 
+
 template <int INV, int LOAD, int STORE>
 __global__ void __launch_bounds__(FFT_THREADS) k_fft_pass(const GbState *__restrict__ st, int pf, int pass,
                                                           int logL, int log1, int log2,
@@ -400,34 +401,56 @@ __host__ __device__ constexpr int brev5(int i) {
   return ((i & 1) << 4) | ((i & 2) << 2) | (i & 4) | ((i & 8) >> 2) | ((i & 16) >> 4);
 }
 
-// radix-2 stage S (half = 2^(S-1)) of a 32-point DIT transform, all indices compile-time
-template <int S>
-__device__ __forceinline__ void dft32_stage(float2 (&a)[32], const float2 *__restrict__ w32) {
+// cos and sin of 2 pi j / 32, j < 16 (the 32nd roots of unity, rounded to float)
+__device__ __forceinline__ float cos32(int j) {
+  constexpr float t[16] = {1.0f,           9.807852507e-01f, 9.238795042e-01f, 8.314695954e-01f,
+                           7.071067691e-01f, 5.555702448e-01f, 3.826834261e-01f, 1.950903237e-01f,
+                           0.0f,           -1.950903237e-01f, -3.826834261e-01f, -5.555702448e-01f,
+                           -7.071067691e-01f, -8.314695954e-01f, -9.238795042e-01f, -9.807852507e-01f};
+  return t[j];
+}
+// sin(2 pi j / 32) = cos(2 pi (8 - j) / 32) for j <= 8, cos(2 pi (j - 8) / 32) above
+__device__ __forceinline__ float sin32(int j) { return j == 0 ? 0.0f : cos32(j < 8 ? 8 - j : j - 8); }
+
+// radix-2 stage S (half = 2^(S-1)) of a 32-point DIT transform with exp(sgn 2 pi i j / 32)
+// twiddles; every index and twiddle is a compile-time constant once unrolled, so the
+// products by 1 and by +-i (46 of the 80 butterflies) become moves and sign flips
+template <int S, int INV>
+__device__ __forceinline__ void dft32_stage(float2 (&a)[32]) {
   constexpr int half = 1 << (S - 1);
+  constexpr float sg = INV ? 1.0f : -1.0f;
 #pragma unroll
   for (int g = 0; g < 32 / (2 * half); ++g) {
 #pragma unroll
     for (int p = 0; p < half; ++p) {
       const int i0 = g * 2 * half + p, i1 = i0 + half;
-      const float2 w = w32[p << (5 - S)];
+      const int j = p << (5 - S);
       const float2 u = a[i0];
-      const float2 v = cmul(a[i1], w);
+      float2 v;
+      if (j == 0) {
+        v = a[i1];
+      } else if (j == 8) {
+        v = make_float2(-sg * a[i1].y, sg * a[i1].x);  // times sg * i
+      } else {
+        v = cmul(a[i1], make_float2(cos32(j), sg * sin32(j)));
+      }
       a[i0] = make_float2(u.x + v.x, u.y + v.y);
       a[i1] = make_float2(u.x - v.x, u.y - v.y);
     }
   }
 }
 
-// 32-point DFT of a[0..31] in place, natural order in and out; w32[j] = exp(sgn 2 pi i j / 32)
-__device__ __forceinline__ void dft32(float2 (&a)[32], const float2 *__restrict__ w32) {
+// 32-point DFT of a[0..31] in place, natural order in and out, exp(sgn 2 pi i jk / 32)
+template <int INV>
+__device__ __forceinline__ void dft32(float2 (&a)[32]) {
   float2 b[32];
 #pragma unroll
   for (int i = 0; i < 32; ++i) b[brev5(i)] = a[i];
-  dft32_stage<1>(b, w32);
-  dft32_stage<2>(b, w32);
-  dft32_stage<3>(b, w32);
-  dft32_stage<4>(b, w32);
-  dft32_stage<5>(b, w32);
+  dft32_stage<1, INV>(b);
+  dft32_stage<2, INV>(b);
+  dft32_stage<3, INV>(b);
+  dft32_stage<4, INV>(b);
+  dft32_stage<5, INV>(b);
 #pragma unroll
   for (int i = 0; i < 32; ++i) a[i] = b[i];
 }
@@ -440,7 +463,6 @@ __global__ void __launch_bounds__(F1K_THREADS) k_fft1024(const GbState *__restri
   if (!gb_pred(st, pf)) return;
   __shared__ float2 buf[F1K_SEQ * F1K_STRIDE];
   __shared__ float2 tw[1024];  // exp(-+2 pi i t / 1024)
-  __shared__ float2 w32[32];   // exp(-+2 pi i j / 32)
   const int L = 1024, B = F1K_SEQ;
   const int n1 = 1 << log1, n2 = 1 << log2;
   const int N = n1 * n2;
@@ -448,7 +470,6 @@ __global__ void __launch_bounds__(F1K_THREADS) k_fft1024(const GbState *__restri
   const float sgn = INV ? 1.0f : -1.0f;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int t = threadIdx.x; t < 1024; t += blockDim.x) tw[t] = cis_pi(sgn, (2.0f * t) / 1024.0f);
-  if (threadIdx.x < 32) w32[threadIdx.x] = cis_pi(sgn, (2.0f * threadIdx.x) / 32.0f);
   const float wn0 = sqrtf(1.0f / (float)N), wn = sqrtf(2.0f / (float)N);
   for (int seq0 = blockIdx.x * B; seq0 < nseq; seq0 += gridDim.x * B) {
     __syncthreads();
@@ -490,7 +511,7 @@ __global__ void __launch_bounds__(F1K_THREADS) k_fft1024(const GbState *__restri
       float2 a[32];
 #pragma unroll
       for (int e1 = 0; e1 < 32; ++e1) a[e1] = sb[f1k_idx(32 * e1 + lane)];
-      dft32(a, w32);
+      dft32<INV>(a);
 #pragma unroll
       for (int k1 = 1; k1 < 32; ++k1) a[k1] = cmul(a[k1], tw[(lane * k1) & 1023]);
       __syncwarp();
@@ -500,7 +521,7 @@ __global__ void __launch_bounds__(F1K_THREADS) k_fft1024(const GbState *__restri
       __syncwarp();
 #pragma unroll
       for (int e2 = 0; e2 < 32; ++e2) a[e2] = sb[lane * 33 + e2];
-      dft32(a, w32);
+      dft32<INV>(a);
       __syncwarp();
       // X[k1 + 32 k2] back in natural order
 #pragma unroll
