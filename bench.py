@@ -293,6 +293,8 @@ def bench_ours(args):
     line["roofline"] = mv["at"]
     line["matvec"] = mv
     line["resident"] = resident_roofline(peak, peak_kind, cluster=sched.get("cluster", 0))
+    if not args.no_configs:
+        line["single_trial_configs"] = bench_configs(cpu=not args.no_cpu)
     line["gemm"] = gemm_roofline(tpeak, tpeak_kind)
     line["operators"] = operators_roofline(peak, peak_kind)
     if args.plain_trials > 0 and world == 1:
@@ -538,6 +540,74 @@ def resident_roofline(peak, peak_kind, max_n=8192, sample=0, cluster=0):
     return out
 
 
+# The reference's single-trial configurations (dense, DCT, expander), each through the drop-in
+# generate-and-solve call: (name, algorithm, operator, k, m, n, d, options, seed)
+SINGLE_CONFIGS = (
+    ("dense NIHT n=4096 m=1024 k=102", "NIHT", "gen", 102, 1024, 4096, 0, (), 101),
+    ("DCT CGIHT n=2^20 m=2^18 k=26214", "CGIHT", "dct", 26214, 2 ** 18, 2 ** 20, 0, ("vecDistribution", "gaussian"), 202),
+    ("DCT HTP n=2^20 m=2^18 k=26214", "HTP", "dct", 26214, 2 ** 18, 2 ** 20, 0, ("vecDistribution", "gaussian"), 203),
+    ("expander NIHT n=2^18 m=2^16 d=7 k=3276", "NIHT", "smv", 3276, 2 ** 16, 2 ** 18, 7, ("matrixEnsemble", "ones"), 303),
+    ("expander parallel_l0 n=2^18 m=2^16 d=7 k=3276", "parallel_l0", "smv", 3276, 2 ** 16, 2 ** 18, 7,
+     ("matrixEnsemble", "expander"), 304),
+)
+
+
+def bench_configs(cpu=True, cpu_iters=3):
+    """Each single-trial configuration solved by the drop-in on the GPU (generation included
+    in `ms_total`, the solve alone in `ms_algorithm`, the library's own events), and the CPU
+    oracle's time per iteration on the same problem (regenerated from the same keys by the
+    oracle's generators; at most `cpu_iters` iterations, all of them for the dense case,
+    OpenMP over the host cores)."""
+    import gaga_gb300 as gb
+
+    out = {}
+    for name, alg, ens, k, m, n, d, extra, seed in SINGLE_CONFIGS:
+        opts = gb.gaga_options("tol", TOL_REL, "tol_is_relative", 1, "maxiter", MAXITER, "seed", seed, *extra)
+        for _ in range(2):  # the first call loads the kernels
+            t0 = time.perf_counter()
+            x, xt, r = gb.generate_and_solve(alg, ens, k, m, n, d, opts)
+            wall = time.perf_counter() - t0
+        rec = {"algorithm": alg, "iterations": int(r.iter), "rel_l2": float(r.norms[1]),
+               "recovered": bool(r.norms[1] <= 1e-3), "ms_algorithm": float(r.times[0]),
+               "ms_per_iteration": float(r.times[0]) / max(1, int(r.iter)), "ms_total": float(r.times[2]),
+               "wall_ms": wall * 1e3}
+        if cpu:
+            rec["cpu"] = _config_cpu(alg, ens, k, m, n, d, dict(zip(extra[::2], extra[1::2])), seed, int(r.iter),
+                                     cpu_iters)
+            rec["cpu_vs_gpu_per_iteration"] = rec["cpu"]["ms_per_iteration"] / rec["ms_per_iteration"]
+        out[name] = rec
+    return out
+
+
+def _config_cpu(alg, ens, k, m, n, d, extra, seed, gpu_iters, cpu_iters):
+    """CPU oracle timing of one single-trial configuration (the problem regenerated on the host)."""
+    import os
+
+    from oracle import gbo
+
+    vec = {"uniform": 0, "binary": 1, "gaussian": 2}[extra.get("vecDistribution", "binary")]
+    x0, ks = gbo.gen_vector(n, k, vec, seed)
+    if ens == "gen":
+        op = gbo.Op.dense(gbo.gen_dense(m, n, seed, 0, 1), m, n)
+    elif ens == "dct":
+        op = gbo.Op.dct(n, gbo.gen_dct_rows(n, m, seed))
+    else:
+        ensn = {"ones": 1, "binary": 2, "expander": 3}[extra.get("matrixEnsemble", "ones")]
+        rows, vals = gbo.gen_smv(m, n, d, ensn, seed)
+        op = gbo.Op.smv(m, n, d, rows, vals)
+    y = gbo.A(op, x0)
+    tol = TOL_REL * float(np.linalg.norm(y))
+    iters = gpu_iters if ens == "gen" else max(1, min(cpu_iters, gpu_iters))
+    t0 = time.perf_counter()
+    if alg == "parallel_l0":
+        _, _, _, info = gbo.parallel_l0(op, y, tol, iters)
+    else:
+        _, info = gbo.solve(alg, op, y, ks, tol, maxiter=iters)
+    t = time.perf_counter() - t0
+    return {"ms_per_iteration": t * 1e3 / max(1, int(info.iter)), "iterations_timed": int(info.iter),
+            "cores": os.cpu_count(), "kind": "port"}
+
+
 def ncu_traffic():
     """Per-launch DRAM bytes of the dense kernels from the committed ncu summary."""
     try:
@@ -622,6 +692,8 @@ def bench_only(args):
         out = operators_roofline(*peaks())
     elif args.only == "learned":
         out = bench_learned(args)
+    elif args.only == "configs":
+        out = bench_configs(cpu=not args.no_cpu)
     elif args.only == "resident":
         out = resident_roofline(*peaks(), max_n=args.resident_max_n, sample=args.resident_sample)
     else:
@@ -650,7 +722,8 @@ def main():
     ap.add_argument("--retune", action="store_true", help="ignore the autotuner's cache")
     ap.add_argument("--resident-max-n", type=int, default=8192, help="--only resident: largest trial n")
     ap.add_argument("--resident-sample", type=int, default=0, help="--only resident: trials (0: all)")
-    ap.add_argument("--only", choices=["matvec", "gemm", "operators", "plain", "learned", "resident"],
+    ap.add_argument("--no-configs", action="store_true", help="skip the single-trial configurations")
+    ap.add_argument("--only", choices=["matvec", "gemm", "operators", "plain", "learned", "resident", "configs"],
                     help="run one measurement alone and print its JSON (for profiling)")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -59,7 +59,15 @@ struct RsParams {
   float *A;        // per cluster: a_stride floats
   size_t a_stride;
   int *xhist;      // per cluster: n_cap key bins
-  int n_cap, m_cap;
+  int n_cap, m_cap, nb_cap;
+  // single given-data solve (the drop-in): A (column-major, lda_u, m % 4 == 0), y, the
+  // initial state in st_io (written back at the end), x out; one cluster, T = 1
+  int single;
+  const float *Ag;
+  int lda_u;
+  const float *yg;
+  float *xg;
+  GbState *st_io;
 };
 
 // Shared-memory layout of one CTA (the same on host and device).
@@ -75,12 +83,15 @@ __host__ __device__ inline size_t rs_take(size_t &o, size_t b) {
   return r;
 }
 
-__host__ __device__ inline RsLayout rs_layout(int n_cap, int m_cap, int C) {
+// the batched trials' bin count, max(n / 20, 1000) (batch_trial_fields)
+__host__ __device__ inline int rs_default_bins(int n_cap) { return n_cap / 20 > 1000 ? n_cap / 20 : 1000; }
+
+__host__ __device__ inline RsLayout rs_layout(int n_cap, int m_cap, int C, int nb) {
   RsLayout L;
   L.nc_cap = ((n_cap + C - 1) / C + 3) / 4 * 4;
   L.lda_cap = (m_cap + 31) / 32 * 32;
   L.rc4_cap = (L.lda_cap / 4 + C - 1) / C;
-  L.nb_cap = ((n_cap / 20 > 1000 ? n_cap / 20 : 1000) + 3) / 4 * 4;
+  L.nb_cap = (nb + 3) / 4 * 4;
   size_t o = 0;
   L.o_st = rs_take(o, sizeof(GbState));
   L.o_pub = rs_take(o, RS_NPUB * 8);  // RS_NPUB floats, then RS_NPUB ints
@@ -411,7 +422,7 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident_niht(const RsParams 
   const int C = (int)cl.num_blocks(), rank = (int)cl.block_rank();
   const int cid = blockIdx.x / C;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const RsLayout L = rs_layout(P.n_cap, P.m_cap, C);
+  const RsLayout L = rs_layout(P.n_cap, P.m_cap, C, P.nb_cap);
   GbState *st = reinterpret_cast<GbState *>(smem + L.o_st);
   float *pub = reinterpret_cast<float *>(smem + L.o_pub);
   int *ipub = reinterpret_cast<int *>(pub + RS_NPUB);
@@ -428,26 +439,58 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident_niht(const RsParams 
   int *cntf = reinterpret_cast<int *>(smem + L.o_cntf);
   float4 *gscr = reinterpret_cast<float4 *>(smem + L.o_gscr);
   int *scan = reinterpret_cast<int *>(smem + L.o_scan);
-  float *A = P.A + (size_t)cid * P.a_stride;
-  int *xh = P.xhist + (size_t)cid * P.n_cap;
+  float *A = P.single ? const_cast<float *>(P.Ag) : P.A + (size_t)cid * P.a_stride;
+  int *xh = P.single ? nullptr : P.xhist + (size_t)cid * P.n_cap;
   {
     unsigned int *w = reinterpret_cast<unsigned int *>(st);
     for (int i = tid; i < (int)(sizeof(GbState) / 4); i += RS_THREADS) w[i] = 0u;
   }
   __syncthreads();
-  for (;;) {
-    // ---- next trial: rank 0 takes it from the queue, the others read it from rank 0
-    if (rank == 0 && tid == 0) s_q = atomicAdd(P.queue, 1);
-    cl.sync();
-    const int q = *peer(cl, &s_q, 0);
+  for (int pass = 0;; ++pass) {
+    // ---- next trial: rank 0 takes it from the queue, the others read it from rank 0 (the
+    // single given-data solve has one trial and no queue)
+    int q = pass;
+    if (!P.single) {
+      if (rank == 0 && tid == 0) s_q = atomicAdd(P.queue, 1);
+      cl.sync();
+      q = *peer(cl, &s_q, 0);
+    }
     if (q >= P.T) break;
-    const int t = P.order[q];
-    const int m = P.m[t], n = P.n[t];
-    const int lda = (m + 31) / 32 * 32, q4 = lda / 4;
+    const int t = P.single ? 0 : P.order[q];
+    const int m = P.single ? P.m_cap : P.m[t], n = P.single ? P.n_cap : P.n[t];
+    const int lda = P.single ? P.lda_u : (m + 31) / 32 * 32, q4 = P.single ? m / 4 : lda / 4;
     const int CH = (n + C - 1) / C;
     const int c0 = min(n, rank * CH), nc = min(n, c0 + CH) - c0;
     const int RB = (q4 + C - 1) / C;
     const int rr0 = min(q4, rank * RB), rr1 = min(q4, rr0 + RB);
+    int s_own = 0;
+    if (P.single) {
+      // ---- the caller's problem: initial state, y (whole in r, own rows in ypart), ||y||^2
+      if (tid == 0) {
+        const unsigned int *src = reinterpret_cast<const unsigned int *>(P.st_io);
+        unsigned int *dst = reinterpret_cast<unsigned int *>(st);
+        for (int i = 0; i < (int)(sizeof(GbState) / 4); ++i) dst[i] = src[i];
+      }
+      const float4 *y4 = reinterpret_cast<const float4 *>(P.yg);
+      float4 *r4 = reinterpret_cast<float4 *>(r);
+      float4 *yp4 = reinterpret_cast<float4 *>(ypart);
+      for (int i = tid; i < q4; i += RS_THREADS) r4[i] = __ldcg(y4 + i);
+      float s2 = 0.0f;
+      for (int i = rr0 + tid; i < rr1; i += RS_THREADS) {
+        const float4 v = __ldcg(y4 + i);
+        yp4[i - rr0] = v;
+        s2 = fmaf(v.x, v.x, s2); s2 = fmaf(v.y, v.y, s2); s2 = fmaf(v.z, v.z, s2); s2 = fmaf(v.w, v.w, s2);
+      }
+      const float b = block_reduce<0>(s2, red32);
+      if (tid == 0) pub[R_RES] = b;
+      cl.sync();
+      if (tid == 0) {
+        st->red[R_RES] = combine_sum(cl, C, pub, R_RES);
+        // NIHT prologue (algorithms.cu:1296-1354): resid = y; err = ||y||
+        ctrl_phase(st, C_INIT0, 0);
+      }
+      __syncthreads();
+    } else {
     const uint32_t key = P.seed + (P.tid ? P.tid[t] : (uint32_t)t);
     if (tid == 0) {
       batch_trial_fields(st, t, m, n, P.k[t], P.maxiter, GB_ALG_NIHT);
@@ -512,7 +555,7 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident_niht(const RsParams 
       for (int c = tid; c < nc; c += RS_THREADS)
         if (bins[c] > kb) x0[c] = 0.0f;
     }
-    int s_own = compact_own(bins, nc, st->k_bin, sidx, wcnt);
+    s_own = compact_own(bins, nc, st->k_bin, sidx, wcnt);
     av_own_partial(A, lda, q4, c0, sidx, s_own, x0, part, gscr);
     cl.sync();
     {
@@ -529,6 +572,7 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident_niht(const RsParams 
       ctrl_phase(st, C_INIT0, 0);
     }
     __syncthreads();
+    }
     // x = A^T y ; max|x| ; FindSupportSet ; Threshold
     at_own(A, lda, q4, c0, nc, r, x);
     __syncthreads();
@@ -649,6 +693,16 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident_niht(const RsParams 
       if (tid == 0) ctrl_phase(st, C_NIHT_STOP, 0);
       __syncthreads();
     }
+    if (P.single) {
+      // ---- x and the final state back to the caller's workspace
+      for (int c = tid; c < nc; c += RS_THREADS) P.xg[c0 + c] = x[c];
+      if (rank == 0 && tid == 0) {
+        const unsigned int *src = reinterpret_cast<const unsigned int *>(st);
+        unsigned int *dst = reinterpret_cast<unsigned int *>(P.st_io);
+        for (int i = 0; i < (int)(sizeof(GbState) / 4); ++i) dst[i] = src[i];
+      }
+      continue;
+    }
     // ---- verdict (k_b_err and the result phase of gb_batch.cu)
     {
       float e2 = 0.0f, x2 = 0.0f;
@@ -703,7 +757,7 @@ int gb_resident_max_smem() {
   return optin - (int)fa.sharedSizeBytes;
 }
 
-size_t gb_resident_smem(int n_cap, int m_cap, int C) { return rs_layout(n_cap, m_cap, C).bytes; }
+size_t gb_resident_smem(int n_cap, int m_cap, int C) { return rs_layout(n_cap, m_cap, C, rs_default_bins(n_cap)).bytes; }
 
 int gb_resident_pick_cluster(int n_cap, int m_cap, int requested) {
   const int cap = gb_resident_max_smem();
@@ -794,6 +848,13 @@ gb_status gb_resident_enqueue(const GbResidentArgs &a, cudaStream_t s) {
   P.xhist = R.xhist;
   P.n_cap = R.n_cap;
   P.m_cap = R.m_cap;
+  P.nb_cap = rs_default_bins(R.n_cap);
+  P.single = 0;
+  P.Ag = nullptr;
+  P.lda_u = 0;
+  P.yg = nullptr;
+  P.xg = nullptr;
+  P.st_io = nullptr;
   cfg.gridDim = dim3(R.ncl * C, 1, 1);
   cfg.dynamicSmemBytes = gb_resident_smem(R.n_cap, R.m_cap, C);
   GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_resident_niht, P));
@@ -807,3 +868,61 @@ int gb_resident_last_cluster() {
   auto it = g_res.find(dev);
   return it == g_res.end() ? 0 : it->second.C;
 }
+
+// The drop-in's dense NIHT on one cluster (the caller checked that the state is the plain
+// NIHT start: no timing variant, no warm start).  The cluster takes up to 16 CTAs with at
+// least 128 columns each; *used = 0 when the problem does not fit (the graph path solves it).
+gb_status gb_resident_solve_single(GbWork &w, int num_bins, cudaStream_t s, int *used) {
+  *used = 0;
+  const GbOp &op = w.op;
+  if (op.kind != GB_OP_DENSE || !op.vec4 || (op.m % 4) || op.m > 8192 || op.n > 20000 || w.dyn) return GB_OK;
+  const int cap = gb_resident_max_smem();
+  if (cap <= 0) return GB_OK;
+  GB_TRY(gb_once_per_device(g_attr_done, [&]() -> gb_status {
+    GB_CUDA_TRY(cudaFuncSetAttribute((const void *)k_resident_niht, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+    GB_CUDA_TRY(cudaFuncSetAttribute((const void *)k_resident_niht, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    return GB_OK;
+  }));
+  cudaLaunchConfig_t cfg;
+  memset(&cfg, 0, sizeof(cfg));
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(RS_THREADS, 1, 1);
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  // up to 16 CTAs with at least 128 columns each, halved while the GPU cannot place such a
+  // cluster; fewer CTAs need more shared memory each, so a size that does not fit ends it
+  int C = 16;
+  while (C > 1 && op.n / C < 128) C /= 2;
+  for (;;) {
+    const size_t smem = rs_layout(op.n, op.m, C, num_bins).bytes;
+    if ((long long)smem > cap) return GB_OK;
+    attr[0].val.clusterDim.x = C;
+    cfg.gridDim = dim3(C, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    int ncl = 0;
+    if (cudaOccupancyMaxActiveClusters(&ncl, (void *)k_resident_niht, &cfg) == cudaSuccess && ncl > 0) break;
+    cudaGetLastError();
+    if (C == 1) return GB_OK;
+    C /= 2;
+  }
+  RsParams P;
+  memset(&P, 0, sizeof(P));
+  P.T = 1;
+  P.n_cap = op.n;
+  P.m_cap = op.m;
+  P.nb_cap = num_bins;
+  P.single = 1;
+  P.Ag = op.A;
+  P.lda_u = op.lda;
+  P.yg = w.y;
+  P.xg = w.x;
+  P.st_io = w.st;
+  GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_resident_niht, P));
+  *used = 1;
+  return GB_OK;
+}
+

@@ -38,3 +38,7 @@ int gb_resident_max_smem();
 int gb_resident_last_cluster();
 // held for the whole of gb_cs_solve_batch (gb_batch.cu): the engines are shared per device
 std::recursive_mutex &gb_batch_mutex();
+// The single-trial drop-in's dense NIHT (state initialised in w.st, y in w.y) on one
+// cluster; x to w.x and the final state to w.st.  *used = 0: not eligible, nothing launched.
+gb_status gb_resident_solve_single(GbWork &w, int num_bins, cudaStream_t s, int *used);
+

@@ -11,6 +11,7 @@
 #include <string.h>
 
 #include "gb_internal.cuh"
+#include "gb_resident.h"
 
 #include "gb_ctrl.cuh"
 
@@ -1734,6 +1735,14 @@ gb_status gb_run_solver(GbWork &w, int alg, const gb_options &o, int k, cudaStre
   if (o.timing && (alg == GB_ALG_NIHT || alg == GB_ALG_HTP)) P.supp_flag = o.support_flag;
   static const bool eager = getenv("GB_CS_EAGER") && atoi(getenv("GB_CS_EAGER")) != 0;
   if (eager) return run_eager(P, s);
+  // dense NIHT with the plain start: one thread-block cluster runs the whole solve
+  // (gb_resident.cu), without a kernel launch per step
+  static const bool no_resident = getenv("GB_CS_SINGLE_RESIDENT") && atoi(getenv("GB_CS_SINGLE_RESIDENT")) == 0;
+  if (!no_resident && alg == GB_ALG_NIHT && !o.timing && !w.ml_params && !w.tstamp) {
+    int used = 0;
+    GB_TRY(gb_resident_solve_single(w, o.num_bins, s, &used));
+    if (used) return GB_OK;
+  }
   cudaStream_t s0, s1, s2;
   GB_CUDA_TRY(cudaStreamCreateWithFlags(&s0, cudaStreamNonBlocking));
   GB_CUDA_TRY(cudaStreamCreateWithFlags(&s1, cudaStreamNonBlocking));
