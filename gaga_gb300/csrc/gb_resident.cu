@@ -73,8 +73,7 @@ struct RsParams {
 // Shared-memory layout of one CTA (the same on host and device).
 struct RsLayout {
   int nc_cap, lda_cap, rc4_cap, nb_cap;
-  size_t o_st, o_pub, o_x, o_grad, o_x0, o_bins, o_sidx, o_r, o_part, o_rowp, o_ypart, o_cnt, o_cntf, o_gscr, o_scan,
-      bytes;
+  size_t o_st, o_pub, o_x, o_grad, o_x0, o_bins, o_sidx, o_r, o_part, o_rowp, o_ypart, o_cnt, o_cntf, o_gscr, bytes;
 };
 
 __host__ __device__ inline size_t rs_take(size_t &o, size_t b) {
@@ -107,7 +106,6 @@ __host__ __device__ inline RsLayout rs_layout(int n_cap, int m_cap, int C, int n
   L.o_cnt = rs_take(o, (size_t)L.nb_cap * 4);
   L.o_cntf = rs_take(o, (size_t)L.nb_cap * 4);
   L.o_gscr = rs_take(o, (size_t)RS_THREADS * 16);
-  L.o_scan = rs_take(o, (size_t)RS_THREADS * 4);
   L.bytes = o;
   return L;
 }
@@ -131,8 +129,26 @@ __device__ float combine_max(cg::cluster_group &cl, int C, float *pub, int slot)
   return a;
 }
 
+// sum and max of the CTA's threads in one pass (thread 0 gets both)
+__device__ __forceinline__ void block_reduce_sum_max(float s, float m, float *red32, float *out_s, float *out_m) {
+  s = warp_sum(s);
+  m = warp_max(m);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) { red32[wid] = s; red32[16 + wid] = m; }
+  __syncthreads();
+  if (wid == 0) {
+    float a = lane < RS_WARPS ? red32[lane] : 0.0f;
+    float b = lane < RS_WARPS ? red32[16 + lane] : 0.0f;
+    a = warp_sum(a);
+    b = warp_max(b);
+    if (lane == 0) { *out_s = a; *out_m = b; }
+  }
+}
+
 // out[c] = A[:, c0 + c] . r for the CTA's columns.  G lanes per column, each lane keeping
-// U x V float4 loads in flight over V adjacent columns.  r is the full residual in shared
+// U x V float4 loads in flight over V adjacent columns (one SM streams about as many bytes
+// per second as it has in flight per memory latency).  r is the full residual in shared
 // memory, zero in the padding rows (as A is).
 template <int G, int U, int V>
 __device__ void at_own_t(const float *A, int lda, int q4, int c0, int nc, const float *r, float *out) {
@@ -182,12 +198,24 @@ __device__ void at_own_t(const float *A, int lda, int q4, int c0, int nc, const 
   }
 }
 
+// DEEP: 16 float4 loads in flight per lane (one cluster alone on the GPU, reading from L2);
+// otherwise 8 (every SM streaming from HBM: more requests in flight measured slower)
+template <bool DEEP>
 __device__ void at_own(const float *A, int lda, int q4, int c0, int nc, const float *r, float *out) {
-  if (q4 >= 256) at_own_t<32, 8, 1>(A, lda, q4, c0, nc, r, out);
-  else if (q4 >= 128) at_own_t<32, 4, 2>(A, lda, q4, c0, nc, r, out);
-  else if (q4 >= 64) at_own_t<32, 2, 4>(A, lda, q4, c0, nc, r, out);
-  else if (q4 >= 32) at_own_t<16, 2, 4>(A, lda, q4, c0, nc, r, out);
-  else at_own_t<8, 4, 2>(A, lda, q4, c0, nc, r, out);
+  if (DEEP) {
+    if (q4 >= 512) at_own_t<32, 16, 1>(A, lda, q4, c0, nc, r, out);
+    else if (q4 >= 256) at_own_t<32, 8, 2>(A, lda, q4, c0, nc, r, out);
+    else if (q4 >= 128) at_own_t<32, 4, 4>(A, lda, q4, c0, nc, r, out);
+    else if (q4 >= 64) at_own_t<32, 2, 8>(A, lda, q4, c0, nc, r, out);
+    else if (q4 >= 32) at_own_t<16, 2, 8>(A, lda, q4, c0, nc, r, out);
+    else at_own_t<8, 4, 4>(A, lda, q4, c0, nc, r, out);
+  } else {
+    if (q4 >= 256) at_own_t<32, 8, 1>(A, lda, q4, c0, nc, r, out);
+    else if (q4 >= 128) at_own_t<32, 4, 2>(A, lda, q4, c0, nc, r, out);
+    else if (q4 >= 64) at_own_t<32, 2, 4>(A, lda, q4, c0, nc, r, out);
+    else if (q4 >= 32) at_own_t<16, 2, 4>(A, lda, q4, c0, nc, r, out);
+    else at_own_t<8, 4, 2>(A, lda, q4, c0, nc, r, out);
+  }
 }
 
 // part (lda floats) = sum over the CTA's support entries e (ascending) of
@@ -321,49 +349,57 @@ __device__ void gather_rows(cg::cluster_group &cl, int C, int q4, int RB, float 
   }
 }
 
-// the k-th bin scan of k_kbin (gb_solver.cu) by the CTA over counters cnt[0, max_bin)
-// (shared memory, or the cluster's global key histogram read at L2); same results.
+// the k-th bin scan of k_kbin (gb_solver.cu) over counters cnt[0, max_bin) (shared memory,
+// or the cluster's global key histogram read at L2), same results, by warp 0 alone: lane l
+// sums a contiguous chunk, a shuffle scan finds the lane whose chunk reaches k, that lane
+// walks its chunk.  One CTA barrier at the end publishes the state.
 template <bool GLOBAL>
-__device__ void block_kbin(GbState *st, const int *cnt, int k, int *scan, int *res) {
-  const int t = threadIdx.x;
-  const int max_bin = st->max_bin;
-  const int CH = (max_bin + RS_THREADS - 1) / RS_THREADS;
-  const int b0 = t * CH, b1 = min(b0 + CH, max_bin);
-  auto ld = [&](int b) { return GLOBAL ? __ldcg(cnt + b) : cnt[b]; };
-  int csum = 0;
-  for (int b = b0; b < b1; ++b) csum += ld(b);
-  scan[t] = csum;
-  if (t == 0) { res[0] = -2; res[1] = 0; }
-  __syncthreads();
-  for (int off = 1; off < RS_THREADS; off <<= 1) {
-    const int v = t >= off ? scan[t - off] : 0;
-    __syncthreads();
-    scan[t] += v;
-    __syncthreads();
-  }
-  const int incl = scan[t], excl = incl - csum;
-  if (k > 0 && excl < k && incl >= k) {
-    int s = excl;
-    for (int b = b0; b < b1; ++b) {
-      s += ld(b);
-      if (s >= k) { res[0] = b; res[1] = s; break; }
+__device__ void block_kbin(GbState *st, const int *cnt, int k) {
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    const int max_bin = st->max_bin;
+    const int CH = (max_bin + 31) / 32;
+    const int b0 = min(lane * CH, max_bin), b1 = min(b0 + CH, max_bin);
+    auto ld = [&](int b) { return GLOBAL ? __ldcg(cnt + b) : cnt[b]; };
+    int csum = 0;
+    for (int b = b0; b < b1; ++b) csum += ld(b);
+    int incl = csum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
     }
-  }
-  __syncthreads();
-  if (t == 0) {
-    int k_bin, sum;
-    if (k <= 0) { k_bin = -1; sum = 0; }
-    else if (res[0] == -2) { k_bin = max_bin - 1; sum = scan[RS_THREADS - 1]; }
-    else { k_bin = res[0]; sum = res[1]; }
-    const float intercept = st->max_value;
-    const float slope = st->slope;
-    if (sum < k) {
-      st->alpha_bin = st->alpha_bin * 0.5f;
-      st->max_bin = (int)((float)st->num_bins * (1.0f - st->alpha_bin));
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    const int excl = incl - csum;
+    const unsigned hit = __ballot_sync(0xffffffffu, k > 0 && excl < k && incl >= k);
+    int res_kbin = -2, res_sum = 0;
+    if (hit) {
+      const int owner = __ffs(hit) - 1;
+      if (lane == owner) {
+        int s2 = excl;
+        for (int b = b0; b < b1; ++b) {
+          s2 += ld(b);
+          if (s2 >= k) { res_kbin = b; res_sum = s2; break; }
+        }
+      }
+      res_kbin = __shfl_sync(0xffffffffu, res_kbin, owner);
+      res_sum = __shfl_sync(0xffffffffu, res_sum, owner);
     }
-    st->min_val = intercept - (float)(k_bin + 1) / slope;
-    st->k_bin = k_bin;
-    st->sum = sum;
+    if (lane == 0) {
+      int k_bin, sum;
+      if (k <= 0) { k_bin = -1; sum = 0; }
+      else if (res_kbin == -2) { k_bin = max_bin - 1; sum = total; }
+      else { k_bin = res_kbin; sum = res_sum; }
+      const float intercept = st->max_value;
+      const float slope = st->slope;
+      if (sum < k) {
+        st->alpha_bin = st->alpha_bin * 0.5f;
+        st->max_bin = (int)((float)st->num_bins * (1.0f - st->alpha_bin));
+      }
+      st->min_val = intercept - (float)(k_bin + 1) / slope;
+      st->k_bin = k_bin;
+      st->sum = sum;
+    }
   }
   __syncthreads();
 }
@@ -412,12 +448,14 @@ __device__ void hist_own(const GbState *st, const float *v, int *bins, int nc, i
   }
 }
 
+// DEEP: the single given-data solve's deeper A^T r pipeline (a separate instance, so the
+// batched kernel keeps its own register allocation)
+template <bool DEEP>
 __global__ void __launch_bounds__(RS_THREADS, 1) k_resident_niht(const RsParams P) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int s_q;
   __shared__ float red32[32];
   __shared__ int wcnt[RS_WARPS];
-  __shared__ int kres[2];
   cg::cluster_group cl = cg::this_cluster();
   const int C = (int)cl.num_blocks(), rank = (int)cl.block_rank();
   const int cid = blockIdx.x / C;
@@ -438,7 +476,6 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident_niht(const RsParams 
   int *cnt = reinterpret_cast<int *>(smem + L.o_cnt);
   int *cntf = reinterpret_cast<int *>(smem + L.o_cntf);
   float4 *gscr = reinterpret_cast<float4 *>(smem + L.o_gscr);
-  int *scan = reinterpret_cast<int *>(smem + L.o_scan);
   float *A = P.single ? const_cast<float *>(P.Ag) : P.A + (size_t)cid * P.a_stride;
   int *xh = P.single ? nullptr : P.xhist + (size_t)cid * P.n_cap;
   {
@@ -534,7 +571,7 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident_niht(const RsParams 
     hist_own(st, grad, bins, nc, nullptr, xh);
     __threadfence();
     cl.sync();
-    block_kbin<true>(st, xh, st->k, scan, kres);
+    block_kbin<true>(st, xh, st->k);
     // the counts came through global memory: every CTA takes rank 0's scan result, so the
     // copies of the state stay identical whatever each CTA read
     cl.sync();
@@ -574,7 +611,7 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident_niht(const RsParams 
     __syncthreads();
     }
     // x = A^T y ; max|x| ; FindSupportSet ; Threshold
-    at_own(A, lda, q4, c0, nc, r, x);
+    at_own<DEEP>(A, lda, q4, c0, nc, r, x);
     __syncthreads();
     {
       float mxx = 0.0f;
@@ -602,7 +639,7 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident_niht(const RsParams 
           cntf[b] = s;
         }
         __syncthreads();
-        block_kbin<false>(st, cntf, st->k, scan, kres);
+        block_kbin<false>(st, cntf, st->k);
       }
       const int kb = st->k_bin;
       for (int c = tid; c < nc; c += RS_THREADS)
@@ -635,7 +672,7 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident_niht(const RsParams 
       }
       __syncthreads();
       // grad = A^T resid ; ||grad on the support||^2 ; max|grad|
-      at_own(A, lda, q4, c0, nc, r, grad);
+      at_own<DEEP>(A, lda, q4, c0, nc, r, grad);
       __syncthreads();
       {
         const int kb = st->k_bin;
@@ -646,15 +683,8 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident_niht(const RsParams 
           s2 = fmaf(o, o, s2);
           gm = fmaxf(gm, fabsf(g));
         }
-        const float b1 = block_reduce<0>(s2, red32);
-        if (tid == 0) pub[R_XT] = b1;
-        const float b2 = block_reduce<1>(gm, red32);
-        if (tid == 0) pub[R_GMAX] = b2;
-      }
-      cl.sync();
-      if (tid == 0) {
-        st->red[R_XT] = combine_sum(cl, C, pub, R_XT);
-        st->red[R_GMAX] = (double)combine_max(cl, C, pub, R_GMAX);
+        // published now, combined after the next two cluster barriers with ||A x_thres||^2
+        block_reduce_sum_max(s2, gm, red32, &pub[R_XT], &pub[R_GMAX]);
       }
       // ||A x_thres||^2 (x_thres = grad on the support)
       av_own_partial(A, lda, q4, c0, sidx, s_own, grad, part, gscr);
@@ -666,6 +696,8 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident_niht(const RsParams 
       }
       cl.sync();
       if (tid == 0) {
+        st->red[R_XT] = combine_sum(cl, C, pub, R_XT);
+        st->red[R_GMAX] = (double)combine_max(cl, C, pub, R_GMAX);
         st->red[R_AXT] = combine_sum(cl, C, pub, R_AXT);
         ctrl_phase(st, C_SD_MU, 0);
       }
@@ -753,7 +785,7 @@ int gb_resident_max_smem() {
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
   if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
   cudaFuncAttributes fa;
-  if (cudaFuncGetAttributes(&fa, (const void *)k_resident_niht) != cudaSuccess) return 0;
+  if (cudaFuncGetAttributes(&fa, (const void *)k_resident_niht<false>) != cudaSuccess) return 0;
   return optin - (int)fa.sharedSizeBytes;
 }
 
@@ -780,8 +812,8 @@ gb_status gb_resident_enqueue(const GbResidentArgs &a, cudaStream_t s) {
   }
   GB_TRY(gb_once_per_device(g_attr_done, [&]() -> gb_status {
     const int cap = gb_resident_max_smem();
-    GB_CUDA_TRY(cudaFuncSetAttribute((const void *)k_resident_niht, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
-    GB_CUDA_TRY(cudaFuncSetAttribute((const void *)k_resident_niht, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    GB_CUDA_TRY(cudaFuncSetAttribute((const void *)k_resident_niht<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+    GB_CUDA_TRY(cudaFuncSetAttribute((const void *)k_resident_niht<false>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     return GB_OK;
   }));
   ResEngine &R = g_res[dev];
@@ -804,7 +836,7 @@ gb_status gb_resident_enqueue(const GbResidentArgs &a, cudaStream_t s) {
     GB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     cfg.gridDim = dim3(sms / C * C, 1, 1);
     int ncl = 0;
-    GB_CUDA_TRY(cudaOccupancyMaxActiveClusters(&ncl, (void *)k_resident_niht, &cfg));
+    GB_CUDA_TRY(cudaOccupancyMaxActiveClusters(&ncl, (void *)k_resident_niht<false>, &cfg));
     if (ncl <= 0) {
       gb_set_error_message("resident form: no cluster can be resident", __FILE__, __LINE__);
       return GB_CUDA_ERROR;
@@ -857,7 +889,7 @@ gb_status gb_resident_enqueue(const GbResidentArgs &a, cudaStream_t s) {
   P.st_io = nullptr;
   cfg.gridDim = dim3(R.ncl * C, 1, 1);
   cfg.dynamicSmemBytes = gb_resident_smem(R.n_cap, R.m_cap, C);
-  GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_resident_niht, P));
+  GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_resident_niht<false>, P));
   return GB_OK;
 }
 
@@ -869,6 +901,10 @@ int gb_resident_last_cluster() {
   return it == g_res.end() ? 0 : it->second.C;
 }
 
+namespace {
+std::atomic<unsigned long long> g_attr_done_deep{0};
+}  // namespace
+
 // The drop-in's dense NIHT on one cluster (the caller checked that the state is the plain
 // NIHT start: no timing variant, no warm start).  The cluster takes up to 16 CTAs with at
 // least 128 columns each; *used = 0 when the problem does not fit (the graph path solves it).
@@ -876,11 +912,14 @@ gb_status gb_resident_solve_single(GbWork &w, int num_bins, cudaStream_t s, int 
   *used = 0;
   const GbOp &op = w.op;
   if (op.kind != GB_OP_DENSE || !op.vec4 || (op.m % 4) || op.m > 8192 || op.n > 20000 || w.dyn) return GB_OK;
+  // 16 SMs stream a 48 MB matrix in about the time the per-step kernels take over the whole
+  // GPU; larger ones are faster there
+  if (4.0 * op.m * op.n > 48e6) return GB_OK;
   const int cap = gb_resident_max_smem();
   if (cap <= 0) return GB_OK;
-  GB_TRY(gb_once_per_device(g_attr_done, [&]() -> gb_status {
-    GB_CUDA_TRY(cudaFuncSetAttribute((const void *)k_resident_niht, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
-    GB_CUDA_TRY(cudaFuncSetAttribute((const void *)k_resident_niht, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  GB_TRY(gb_once_per_device(g_attr_done_deep, [&]() -> gb_status {
+    GB_CUDA_TRY(cudaFuncSetAttribute((const void *)k_resident_niht<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+    GB_CUDA_TRY(cudaFuncSetAttribute((const void *)k_resident_niht<true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     return GB_OK;
   }));
   cudaLaunchConfig_t cfg;
@@ -897,6 +936,7 @@ gb_status gb_resident_solve_single(GbWork &w, int num_bins, cudaStream_t s, int 
   // cluster; fewer CTAs need more shared memory each, so a size that does not fit ends it
   int C = 16;
   while (C > 1 && op.n / C < 128) C /= 2;
+  if (const char *e = getenv("GB_CS_SINGLE_CLUSTER")) C = std::max(1, std::min(16, atoi(e)));
   for (;;) {
     const size_t smem = rs_layout(op.n, op.m, C, num_bins).bytes;
     if ((long long)smem > cap) return GB_OK;
@@ -904,7 +944,7 @@ gb_status gb_resident_solve_single(GbWork &w, int num_bins, cudaStream_t s, int 
     cfg.gridDim = dim3(C, 1, 1);
     cfg.dynamicSmemBytes = smem;
     int ncl = 0;
-    if (cudaOccupancyMaxActiveClusters(&ncl, (void *)k_resident_niht, &cfg) == cudaSuccess && ncl > 0) break;
+    if (cudaOccupancyMaxActiveClusters(&ncl, (void *)k_resident_niht<true>, &cfg) == cudaSuccess && ncl > 0) break;
     cudaGetLastError();
     if (C == 1) return GB_OK;
     C /= 2;
@@ -921,7 +961,7 @@ gb_status gb_resident_solve_single(GbWork &w, int num_bins, cudaStream_t s, int 
   P.yg = w.y;
   P.xg = w.x;
   P.st_io = w.st;
-  GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_resident_niht, P));
+  GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_resident_niht<true>, P));
   *used = 1;
   return GB_OK;
 }
