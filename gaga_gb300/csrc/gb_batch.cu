@@ -413,7 +413,7 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
     rn = GB_RESIDENT_N_DEFAULT;
     if (const char *e = getenv("GB_CS_RESIDENT_N")) rn = atoi(e);
   }
-  if (b->alg != GB_ALG_NIHT) rn = -1;
+  if ((b->alg != GB_ALG_NIHT && b->alg != GB_ALG_CGIHT) || b->use_learned) rn = -1;
   std::vector<char> resident(T, 0);
   int rn_cap = 16, rm_cap = 1, n_res = 0;
   for (int t = 0; t < T; ++t)
@@ -423,7 +423,7 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
       rm_cap = std::max(rm_cap, b->m[t]);
       n_res++;
     }
-  if (n_res > 0 && gb_resident_pick_cluster(rn_cap, rm_cap, b->cluster) <= 0) {
+  if (n_res > 0 && gb_resident_pick_cluster(rn_cap, rm_cap, b->cluster, b->alg) <= 0) {
     if (b->cluster > 0 || b->resident_n > 0) {
       gb_set_error_message("resident form: the requested cluster size does not fit these trials", __FILE__,
                            __LINE__);
@@ -498,7 +498,7 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
     ra.n = E.dn; ra.m = E.dm; ra.k = E.dk; ra.tid = E.dtid;
     ra.seed = b->seed; ra.tol_rel = b->tol_rel; ra.maxiter = b->maxiter;
     ra.iters = E.diters; ra.err = E.derr; ra.ok = E.dok; ra.bytes = E.dbytes;
-    ra.n_cap = rn_cap; ra.m_cap = rm_cap; ra.cluster = b->cluster;
+    ra.n_cap = rn_cap; ra.m_cap = rm_cap; ra.cluster = b->cluster; ra.alg = b->alg;
     GB_TRY(gb_resident_enqueue(ra, s));
   }
   for (size_t i = 0; i < nslot; ++i) GB_CUDA_TRY(cudaStreamWaitEvent(s, E.done[i], 0));

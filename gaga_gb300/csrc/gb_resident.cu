@@ -41,6 +41,9 @@ namespace cg = cooperative_groups;
 #define RS_WARPS (RS_THREADS / 32)
 #define RS_NPUB 16
 
+// algorithms of the resident kernel
+enum { RS_NIHT = 0, RS_CGIHT = 1 };
+
 namespace {
 
 struct RsParams {
@@ -73,7 +76,9 @@ struct RsParams {
 // Shared-memory layout of one CTA (the same on host and device).
 struct RsLayout {
   int nc_cap, lda_cap, rc4_cap, nb_cap;
-  size_t o_st, o_pub, o_x, o_grad, o_x0, o_bins, o_sidx, o_r, o_part, o_rowp, o_ypart, o_cnt, o_cntf, o_gscr, bytes;
+  size_t o_st, o_pub, o_x, o_grad, o_x0, o_bins, o_sidx, o_r, o_part, o_rowp, o_ypart, o_cnt, o_cntf, o_gscr;
+  size_t o_gp, o_gpt, o_binsp, o_rowa, o_rowb;  // CGIHT only (zero bytes for NIHT)
+  size_t bytes;
 };
 
 __host__ __device__ inline size_t rs_take(size_t &o, size_t b) {
@@ -85,7 +90,7 @@ __host__ __device__ inline size_t rs_take(size_t &o, size_t b) {
 // the batched trials' bin count, max(n / 20, 1000) (batch_trial_fields)
 __host__ __device__ inline int rs_default_bins(int n_cap) { return n_cap / 20 > 1000 ? n_cap / 20 : 1000; }
 
-__host__ __device__ inline RsLayout rs_layout(int n_cap, int m_cap, int C, int nb) {
+__host__ __device__ inline RsLayout rs_layout(int n_cap, int m_cap, int C, int nb, int alg = RS_NIHT) {
   RsLayout L;
   L.nc_cap = ((n_cap + C - 1) / C + 3) / 4 * 4;
   L.lda_cap = (m_cap + 31) / 32 * 32;
@@ -106,6 +111,12 @@ __host__ __device__ inline RsLayout rs_layout(int n_cap, int m_cap, int C, int n
   L.o_cnt = rs_take(o, (size_t)L.nb_cap * 4);
   L.o_cntf = rs_take(o, (size_t)L.nb_cap * 4);
   L.o_gscr = rs_take(o, (size_t)RS_THREADS * 16);
+  const size_t cg = alg == RS_CGIHT ? 1 : 0;
+  L.o_gp = rs_take(o, cg * L.nc_cap * 4);      // grad_previous (own columns)
+  L.o_gpt = rs_take(o, cg * L.nc_cap * 4);     // grad_prev_thres
+  L.o_binsp = rs_take(o, cg * L.nc_cap * 4);   // bins before the last binning
+  L.o_rowa = rs_take(o, cg * L.rc4_cap * 16);  // own rows of A grad_prev_thres, then of A gp
+  L.o_rowb = rs_take(o, cg * L.rc4_cap * 16);  // own rows of A x_thres
   L.bytes = o;
   return L;
 }
@@ -449,9 +460,9 @@ __device__ void hist_own(const GbState *st, const float *v, int *bins, int nc, i
 }
 
 // DEEP: the single given-data solve's deeper A^T r pipeline (a separate instance, so the
-// batched kernel keeps its own register allocation)
-template <bool DEEP>
-__global__ void __launch_bounds__(RS_THREADS, 1) k_resident_niht(const RsParams P) {
+// batched kernel keeps its own register allocation).  ALG: RS_NIHT or RS_CGIHT.
+template <bool DEEP, int ALG>
+__global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int s_q;
   __shared__ float red32[32];
@@ -460,7 +471,7 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident_niht(const RsParams 
   const int C = (int)cl.num_blocks(), rank = (int)cl.block_rank();
   const int cid = blockIdx.x / C;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const RsLayout L = rs_layout(P.n_cap, P.m_cap, C, P.nb_cap);
+  const RsLayout L = rs_layout(P.n_cap, P.m_cap, C, P.nb_cap, ALG);
   GbState *st = reinterpret_cast<GbState *>(smem + L.o_st);
   float *pub = reinterpret_cast<float *>(smem + L.o_pub);
   int *ipub = reinterpret_cast<int *>(pub + RS_NPUB);
@@ -476,6 +487,11 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident_niht(const RsParams 
   int *cnt = reinterpret_cast<int *>(smem + L.o_cnt);
   int *cntf = reinterpret_cast<int *>(smem + L.o_cntf);
   float4 *gscr = reinterpret_cast<float4 *>(smem + L.o_gscr);
+  float *gp = reinterpret_cast<float *>(smem + L.o_gp);
+  float *gpt = reinterpret_cast<float *>(smem + L.o_gpt);
+  int *binsp = reinterpret_cast<int *>(smem + L.o_binsp);
+  float *rowa = reinterpret_cast<float *>(smem + L.o_rowa);
+  float *rowb = reinterpret_cast<float *>(smem + L.o_rowb);
   float *A = P.single ? const_cast<float *>(P.Ag) : P.A + (size_t)cid * P.a_stride;
   int *xh = P.single ? nullptr : P.xhist + (size_t)cid * P.n_cap;
   {
@@ -530,7 +546,7 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident_niht(const RsParams 
     } else {
     const uint32_t key = P.seed + (P.tid ? P.tid[t] : (uint32_t)t);
     if (tid == 0) {
-      batch_trial_fields(st, t, m, n, P.k[t], P.maxiter, GB_ALG_NIHT);
+      batch_trial_fields(st, t, m, n, P.k[t], P.maxiter, ALG == RS_CGIHT ? GB_ALG_CGIHT : GB_ALG_NIHT);
       st->lda = lda;
     }
     // ---- draw the trial (k_b_gen_A, k_b_gen_x, key bins, y = A x0 of gb_batch.cu)
@@ -626,10 +642,14 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident_niht(const RsParams 
       ctrl_phase(st, C_INIT_BINPREP, 0);
     }
     __syncthreads();
-    // the support step (enq_support): bins and the k-th bin when binning, threshold always
-    auto support = [&]() {
+    // the support step (enq_support): bins and the k-th bin when binning, threshold always;
+    // with save_prev (CGIHT) the previous bins are kept and a support entry that left is
+    // flagged (checkSupportEvolution, GAGA/gaga/kernels.cu:178-193) in st->changed
+    auto support = [&](bool save_prev) {
       const bool dobin = st->flags[F_DOBIN] != 0;
       if (dobin) {
+        if (save_prev)
+          for (int c = tid; c < nc; c += RS_THREADS) binsp[c] = bins[c];  // the same thread bins c next
         hist_own(st, x, bins, nc, cnt, nullptr);
         cl.sync();
         const int mb = st->max_bin;
@@ -641,17 +661,30 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident_niht(const RsParams 
         __syncthreads();
         block_kbin<false>(st, cntf, st->k);
       }
-      const int kb = st->k_bin;
-      for (int c = tid; c < nc; c += RS_THREADS)
+      const int kb = st->k_bin, kbp = st->k_bin_prev;
+      int chg = 0;
+      for (int c = tid; c < nc; c += RS_THREADS) {
         if (bins[c] > kb) x[c] = 0.0f;
+        if (save_prev && dobin && binsp[c] <= kbp && bins[c] > kb) chg = 1;
+      }
       if (dobin) s_own = compact_own(bins, nc, kb, sidx, wcnt);
+      if (save_prev && dobin) {
+        const int any = __syncthreads_or(chg);
+        if (tid == 0) ipub[1] = any;
+        cl.sync();
+        if (tid == 0) {
+          int a = 0;
+          for (int c = 0; c < C; ++c) a |= peer(cl, ipub, c)[1];
+          st->changed = a;
+        }
+      }
       __syncthreads();
     };
-    support();
-    if (tid == 0) ctrl_phase(st, C_INIT_DONE, 0);
+    support(false);
+    if (ALG == RS_NIHT && tid == 0) ctrl_phase(st, C_INIT_DONE, 0);
     __syncthreads();
     // ---- NIHT iterations (RestrictedSD, GAGA/gaga/functions.cu:659-745, then the support)
-    while (st->active) {
+    while (ALG == RS_NIHT && st->active) {
       // resid = y - A x_S ; ||resid||^2
       av_own_partial(A, lda, q4, c0, sidx, s_own, x, part, gscr);
       if (tid == 0) ipub[0] = s_own;
@@ -721,9 +754,183 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident_niht(const RsParams 
         ctrl_phase(st, C_BINPREP, 0);
       }
       __syncthreads();
-      support();
+      support(false);
       if (tid == 0) ctrl_phase(st, C_NIHT_STOP, 0);
       __syncthreads();
+    }
+    if (ALG == RS_CGIHT) {
+      // A v_S of the own support into an m-vector (2 cluster barriers): own rows into rows,
+      // y - A v_S with sub_y; every row gathered into full when given; the CTA's partial of
+      // the squared norm into pub[slot], combined by the caller before its next barrier
+      auto av_rows = [&](const float *v, bool sub_y, float *rows, float *full, int slot) {
+        av_own_partial(A, lda, q4, c0, sidx, s_own, v, part, gscr);
+        if (tid == 0) ipub[0] = s_own;
+        cl.sync();
+        const float s2 = reduce_rows(cl, C, part, rr0, rr1, sub_y ? ypart : nullptr, rows, nullptr);
+        const float b = block_reduce<0>(s2, red32);
+        if (tid == 0 && slot >= 0) pub[slot] = b;
+        cl.sync();
+        if (full) gather_rows(cl, C, q4, RB, rows, full);
+      };
+      // prologue tail (GAGA/gaga/algorithms.cu:3776-3808): r0 = y - A x, grad_previous =
+      // A^T r0, grad_prev_thres
+      av_rows(x, true, rowp, r, R_RES);
+      if (tid == 0) st->red[R_RES] = combine_sum(cl, C, pub, R_RES);
+      __syncthreads();
+      at_own<DEEP>(A, lda, q4, c0, nc, r, gp);
+      __syncthreads();
+      {
+        const int kb = st->k_bin;
+        for (int c = tid; c < nc; c += RS_THREADS) gpt[c] = bins[c] <= kb ? gp[c] : 0.0f;
+      }
+      if (tid == 0) ctrl_phase(st, C_CGIHT_INIT, 0);
+      __syncthreads();
+      // ---- CGIHT iterations: RestrictedCGwithSupportEvolution (F_RCG,
+      // GAGA/gaga/functions.cu:1004-1102) or UnrestrictedCG (F_UCG, :1107-1220), then
+      // x += alpha p and the support (algorithms.cu:3849-3899)
+      while (st->active) {
+        const bool rcg = st->flags[F_RCG] != 0;
+        av_rows(x, true, rowp, r, R_RES);  // r = y - A x_S
+        if (tid == 0) {
+          st->red[R_RES] = combine_sum(cl, C, pub, R_RES);
+          int sc = 0;
+          for (int c = 0; c < C; ++c) sc += peer(cl, ipub, c)[0];
+          st->s_cnt = sc;
+          ctrl_phase(st, C_PUSH_RES, 0);
+        }
+        __syncthreads();
+        at_own<DEEP>(A, lda, q4, c0, nc, r, grad);  // grad = A^T r; x_thres = grad on the support
+        __syncthreads();
+        const int kb = st->k_bin;
+        float sxt = 0.0f;
+        for (int c = tid; c < nc; c += RS_THREADS) {
+          const float o = bins[c] <= kb ? grad[c] : 0.0f;
+          sxt = fmaf(o, o, sxt);
+        }
+        if (rcg) {
+          {
+            const float b = block_reduce<0>(sxt, red32);
+            if (tid == 0) pub[R_XT] = b;
+          }
+          cl.sync();
+          if (tid == 0) {
+            st->red[R_XT] = combine_sum(cl, C, pub, R_XT);
+            ctrl_phase(st, C_RCG_BETA, 0);
+          }
+          __syncthreads();
+          {
+            const float beta = st->cg_beta;
+            float gm = 0.0f;
+            for (int c = tid; c < nc; c += RS_THREADS) {
+              const float g = fmaf(1.0f, grad[c], beta * gp[c]);  // k_scale_add
+              gp[c] = g;
+              gpt[c] = bins[c] <= kb ? g : 0.0f;
+              gm = fmaxf(gm, fabsf(g));
+            }
+            const float b = block_reduce<1>(gm, red32);
+            if (tid == 0) pub[R_GMAX] = b;  // combined after the next product
+          }
+          av_rows(gpt, false, rowa, nullptr, R_AXT);  // ||A grad_prev_thres||^2
+          if (tid == 0) {
+            st->red[R_GMAX] = (double)combine_max(cl, C, pub, R_GMAX);
+            st->red[R_AXT] = combine_sum(cl, C, pub, R_AXT);
+            ctrl_phase(st, C_RCG_ALPHA, 0);
+          }
+          __syncthreads();
+        } else {
+          {
+            const float b = block_reduce<0>(sxt, red32);
+            if (tid == 0) pub[R_XT] = b;  // combined with the dot products below
+          }
+          av_rows(gpt, false, rowa, nullptr, -1);  // own rows of A grad_prev_thres
+          av_rows(grad, false, rowb, nullptr, -1);  // own rows of A x_thres
+          {
+            const float4 *a4 = reinterpret_cast<const float4 *>(rowa);
+            const float4 *b4 = reinterpret_cast<const float4 *>(rowb);
+            float d1 = 0.0f, d2 = 0.0f;
+            for (int i = tid; i < rr1 - rr0; i += RS_THREADS) {
+              const float4 a = a4[i], bb = b4[i];
+              d1 = fmaf(a.x, bb.x, d1); d1 = fmaf(a.y, bb.y, d1); d1 = fmaf(a.z, bb.z, d1); d1 = fmaf(a.w, bb.w, d1);
+              d2 = fmaf(a.x, a.x, d2); d2 = fmaf(a.y, a.y, d2); d2 = fmaf(a.z, a.z, d2); d2 = fmaf(a.w, a.w, d2);
+            }
+            const float b1 = block_reduce<0>(d1, red32);
+            if (tid == 0) pub[R_DOT1] = b1;
+            const float b2 = block_reduce<0>(d2, red32);
+            if (tid == 0) pub[R_DOT2] = b2;
+          }
+          cl.sync();
+          if (tid == 0) {
+            st->red[R_XT] = combine_sum(cl, C, pub, R_XT);
+            st->red[R_DOT1] = combine_sum(cl, C, pub, R_DOT1);
+            st->red[R_DOT2] = combine_sum(cl, C, pub, R_DOT2);
+            ctrl_phase(st, C_UCG_BETA, 0);
+          }
+          __syncthreads();
+          {
+            const float beta = st->cg_beta;
+            float gm = 0.0f, d3 = 0.0f, d4 = 0.0f;
+            for (int c = tid; c < nc; c += RS_THREADS) {
+              const float g = fmaf(1.0f, grad[c], beta * gp[c]);  // k_scale_add
+              gp[c] = g;
+              const bool in = bins[c] <= kb;
+              const float pt = in ? g : 0.0f;
+              gpt[c] = pt;
+              gm = fmaxf(gm, fabsf(g));
+              d3 = fmaf(pt, in ? grad[c] : 0.0f, d3);  // <grad_prev_thres, x_thres>
+            }
+            float4 *a4 = reinterpret_cast<float4 *>(rowa);
+            const float4 *b4 = reinterpret_cast<const float4 *>(rowb);
+            for (int i = tid; i < rr1 - rr0; i += RS_THREADS) {  // A p = A x_thres + beta A p_prev
+              float4 a = a4[i];
+              const float4 bb = b4[i];
+              a.x = fmaf(1.0f, bb.x, beta * a.x); a.y = fmaf(1.0f, bb.y, beta * a.y);
+              a.z = fmaf(1.0f, bb.z, beta * a.z); a.w = fmaf(1.0f, bb.w, beta * a.w);
+              a4[i] = a;
+              d4 = fmaf(a.x, a.x, d4); d4 = fmaf(a.y, a.y, d4); d4 = fmaf(a.z, a.z, d4); d4 = fmaf(a.w, a.w, d4);
+            }
+            block_reduce_sum_max(d3, gm, red32, &pub[R_DOT3], &pub[R_GMAX]);
+            const float b4s = block_reduce<0>(d4, red32);
+            if (tid == 0) pub[R_DOT4] = b4s;
+          }
+          cl.sync();
+          if (tid == 0) {
+            st->red[R_DOT3] = combine_sum(cl, C, pub, R_DOT3);
+            st->red[R_DOT4] = combine_sum(cl, C, pub, R_DOT4);
+            st->red[R_GMAX] = (double)combine_max(cl, C, pub, R_GMAX);
+            ctrl_phase(st, C_UCG_ALPHA, 0);
+          }
+          __syncthreads();
+        }
+        // x += alpha grad_previous ; max|x| ; counters cleared
+        {
+          const float alpha = st->cg_alpha;
+          float mxx = 0.0f;
+          for (int c = tid; c < nc; c += RS_THREADS) {
+            const float o = fmaf(alpha, gp[c], x[c]);
+            x[c] = o;
+            mxx = fmaxf(mxx, fabsf(o));
+          }
+          for (int b = tid; b < L.nb_cap; b += RS_THREADS) cnt[b] = 0;
+          const float b = block_reduce<1>(mxx, red32);
+          if (tid == 0) pub[R_XMAX] = b;
+        }
+        cl.sync();
+        if (tid == 0) {
+          st->red[R_XMAX] = (double)combine_max(cl, C, pub, R_XMAX);
+          ctrl_phase(st, C_CGIHT_BINDEC, 0);
+          ctrl_phase(st, C_BINPREP, 0);
+        }
+        __syncthreads();
+        support(true);
+        if (tid == 0) ctrl_phase(st, C_CGIHT_POST, 0);
+        __syncthreads();
+        if (st->flags[F_REMASK]) {
+          const int kb2 = st->k_bin;
+          for (int c = tid; c < nc; c += RS_THREADS) gpt[c] = bins[c] <= kb2 ? gp[c] : 0.0f;
+        }
+        if (tid == 0) ctrl_phase(st, C_CGIHT_STOP, 0);
+        __syncthreads();
+      }
     }
     if (P.single) {
       // ---- x and the final state back to the caller's workspace
@@ -769,7 +976,6 @@ struct ResEngine {
   int *order = nullptr, *queue = nullptr;
 };
 std::map<int, ResEngine> g_res;
-std::atomic<unsigned long long> g_attr_done{0};
 
 void res_release(ResEngine &R) {
   if (R.A) cudaFree(R.A);
@@ -778,23 +984,49 @@ void res_release(ResEngine &R) {
   R = ResEngine();
 }
 
+// the kernel instance for (single given-data solve or batched trials, algorithm), with its
+// attributes set once per device: dynamic shared memory up to the opt-in maximum and
+// clusters of up to 16 CTAs
+using RsKernel = void (*)(const RsParams);
+RsKernel rs_kernel(bool deep, int alg) {
+  if (deep) return alg == RS_CGIHT ? k_resident<true, RS_CGIHT> : k_resident<true, RS_NIHT>;
+  return alg == RS_CGIHT ? k_resident<false, RS_CGIHT> : k_resident<false, RS_NIHT>;
+}
+std::atomic<unsigned long long> g_attr_done[4];
+
 }  // namespace
+
+int gb_resident_max_smem();
+
+static gb_status rs_attrs(bool deep, int alg) {
+  const int cap = gb_resident_max_smem();
+  return gb_once_per_device(g_attr_done[(deep ? 2 : 0) + alg], [&]() -> gb_status {
+    const void *fn = (const void *)rs_kernel(deep, alg);
+    GB_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+    GB_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    return GB_OK;
+  });
+}
+
+int gb_resident_alg(int gb_alg) { return gb_alg == GB_ALG_CGIHT ? RS_CGIHT : gb_alg == GB_ALG_NIHT ? RS_NIHT : -1; }
 
 int gb_resident_max_smem() {
   int dev = 0, optin = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
   if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
   cudaFuncAttributes fa;
-  if (cudaFuncGetAttributes(&fa, (const void *)k_resident_niht<false>) != cudaSuccess) return 0;
+  if (cudaFuncGetAttributes(&fa, (const void *)k_resident<false, RS_NIHT>) != cudaSuccess) return 0;
   return optin - (int)fa.sharedSizeBytes;
 }
 
-size_t gb_resident_smem(int n_cap, int m_cap, int C) { return rs_layout(n_cap, m_cap, C, rs_default_bins(n_cap)).bytes; }
+size_t gb_resident_smem(int n_cap, int m_cap, int C, int gb_alg) {
+  return rs_layout(n_cap, m_cap, C, rs_default_bins(n_cap), gb_resident_alg(gb_alg)).bytes;
+}
 
-int gb_resident_pick_cluster(int n_cap, int m_cap, int requested) {
+int gb_resident_pick_cluster(int n_cap, int m_cap, int requested, int gb_alg) {
   const int cap = gb_resident_max_smem();
-  if (m_cap > 8192 || n_cap > 20000 || cap <= 0) return 0;
-  auto fits = [&](int C) { return (long long)gb_resident_smem(n_cap, m_cap, C) <= (long long)cap; };
+  if (m_cap > 8192 || n_cap > 20000 || cap <= 0 || gb_resident_alg(gb_alg) < 0) return 0;
+  auto fits = [&](int C) { return (long long)gb_resident_smem(n_cap, m_cap, C, gb_alg) <= (long long)cap; };
   if (requested > 0) return (requested <= 16 && fits(requested)) ? requested : 0;
   // four CTAs per trial measured best over the sweep's mix (n = 1024 ... 8192) on GB300
   int C = 4;
@@ -805,19 +1037,16 @@ int gb_resident_pick_cluster(int n_cap, int m_cap, int requested) {
 gb_status gb_resident_enqueue(const GbResidentArgs &a, cudaStream_t s) {
   int dev = 0;
   GB_CUDA_TRY(cudaGetDevice(&dev));
-  const int C = gb_resident_pick_cluster(a.n_cap, a.m_cap, a.cluster);
-  if (C <= 0) {
+  const int alg = gb_resident_alg(a.alg);
+  const int C = gb_resident_pick_cluster(a.n_cap, a.m_cap, a.cluster, a.alg);
+  if (C <= 0 || alg < 0) {
     gb_set_error_message("resident form: no cluster size fits the trial sizes", __FILE__, __LINE__);
     return GB_BAD_ARG;
   }
-  GB_TRY(gb_once_per_device(g_attr_done, [&]() -> gb_status {
-    const int cap = gb_resident_max_smem();
-    GB_CUDA_TRY(cudaFuncSetAttribute((const void *)k_resident_niht<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
-    GB_CUDA_TRY(cudaFuncSetAttribute((const void *)k_resident_niht<false>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    return GB_OK;
-  }));
-  ResEngine &R = g_res[dev];
-  const size_t smem = gb_resident_smem(a.n_cap, a.m_cap, C);
+  GB_TRY(rs_attrs(false, alg));
+  const RsKernel kern = rs_kernel(false, alg);
+  ResEngine &R = g_res[dev * 2 + alg];
+  const size_t smem = gb_resident_smem(a.n_cap, a.m_cap, C, a.alg);
   cudaLaunchConfig_t cfg;
   memset(&cfg, 0, sizeof(cfg));
   cudaLaunchAttribute attr[1];
@@ -836,7 +1065,7 @@ gb_status gb_resident_enqueue(const GbResidentArgs &a, cudaStream_t s) {
     GB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     cfg.gridDim = dim3(sms / C * C, 1, 1);
     int ncl = 0;
-    GB_CUDA_TRY(cudaOccupancyMaxActiveClusters(&ncl, (void *)k_resident_niht<false>, &cfg));
+    GB_CUDA_TRY(cudaOccupancyMaxActiveClusters(&ncl, (void *)kern, &cfg));
     if (ncl <= 0) {
       gb_set_error_message("resident form: no cluster can be resident", __FILE__, __LINE__);
       return GB_CUDA_ERROR;
@@ -888,8 +1117,8 @@ gb_status gb_resident_enqueue(const GbResidentArgs &a, cudaStream_t s) {
   P.xg = nullptr;
   P.st_io = nullptr;
   cfg.gridDim = dim3(R.ncl * C, 1, 1);
-  cfg.dynamicSmemBytes = gb_resident_smem(R.n_cap, R.m_cap, C);
-  GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_resident_niht<false>, P));
+  cfg.dynamicSmemBytes = gb_resident_smem(R.n_cap, R.m_cap, C, a.alg);
+  GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, P));
   return GB_OK;
 }
 
@@ -901,15 +1130,13 @@ int gb_resident_last_cluster() {
   return it == g_res.end() ? 0 : it->second.C;
 }
 
-namespace {
-std::atomic<unsigned long long> g_attr_done_deep{0};
-}  // namespace
-
-// The drop-in's dense NIHT on one cluster (the caller checked that the state is the plain
-// NIHT start: no timing variant, no warm start).  The cluster takes up to 16 CTAs with at
+// The drop-in's dense NIHT or CGIHT on one cluster (the caller checked that the state is
+// the plain start: no timing variant, no warm start).  The cluster takes up to 16 CTAs with at
 // least 128 columns each; *used = 0 when the problem does not fit (the graph path solves it).
-gb_status gb_resident_solve_single(GbWork &w, int num_bins, cudaStream_t s, int *used) {
+gb_status gb_resident_solve_single(GbWork &w, int gb_alg, int num_bins, cudaStream_t s, int *used) {
   *used = 0;
+  const int alg = gb_resident_alg(gb_alg);
+  if (alg < 0) return GB_OK;
   const GbOp &op = w.op;
   if (op.kind != GB_OP_DENSE || !op.vec4 || (op.m % 4) || op.m > 8192 || op.n > 20000 || w.dyn) return GB_OK;
   // 16 SMs stream a 48 MB matrix in about the time the per-step kernels take over the whole
@@ -917,11 +1144,8 @@ gb_status gb_resident_solve_single(GbWork &w, int num_bins, cudaStream_t s, int 
   if (4.0 * op.m * op.n > 48e6) return GB_OK;
   const int cap = gb_resident_max_smem();
   if (cap <= 0) return GB_OK;
-  GB_TRY(gb_once_per_device(g_attr_done_deep, [&]() -> gb_status {
-    GB_CUDA_TRY(cudaFuncSetAttribute((const void *)k_resident_niht<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
-    GB_CUDA_TRY(cudaFuncSetAttribute((const void *)k_resident_niht<true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    return GB_OK;
-  }));
+  GB_TRY(rs_attrs(true, alg));
+  const RsKernel kern = rs_kernel(true, alg);
   cudaLaunchConfig_t cfg;
   memset(&cfg, 0, sizeof(cfg));
   cudaLaunchAttribute attr[1];
@@ -938,13 +1162,13 @@ gb_status gb_resident_solve_single(GbWork &w, int num_bins, cudaStream_t s, int 
   while (C > 1 && op.n / C < 128) C /= 2;
   if (const char *e = getenv("GB_CS_SINGLE_CLUSTER")) C = std::max(1, std::min(16, atoi(e)));
   for (;;) {
-    const size_t smem = rs_layout(op.n, op.m, C, num_bins).bytes;
+    const size_t smem = rs_layout(op.n, op.m, C, num_bins, alg).bytes;
     if ((long long)smem > cap) return GB_OK;
     attr[0].val.clusterDim.x = C;
     cfg.gridDim = dim3(C, 1, 1);
     cfg.dynamicSmemBytes = smem;
     int ncl = 0;
-    if (cudaOccupancyMaxActiveClusters(&ncl, (void *)k_resident_niht<true>, &cfg) == cudaSuccess && ncl > 0) break;
+    if (cudaOccupancyMaxActiveClusters(&ncl, (void *)kern, &cfg) == cudaSuccess && ncl > 0) break;
     cudaGetLastError();
     if (C == 1) return GB_OK;
     C /= 2;
@@ -961,7 +1185,7 @@ gb_status gb_resident_solve_single(GbWork &w, int num_bins, cudaStream_t s, int 
   P.yg = w.y;
   P.xg = w.x;
   P.st_io = w.st;
-  GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_resident_niht<true>, P));
+  GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, P));
   *used = 1;
   return GB_OK;
 }

@@ -9,7 +9,7 @@
 // trials with n <= this go to the resident kernel unless the caller says otherwise
 #define GB_RESIDENT_N_DEFAULT 8192
 
-// One launch solving `count` NIHT trials, trial order[q] for q < count (indices into the
+// One launch solving `count` NIHT or CGIHT trials, trial order[q] for q < count (indices into the
 // batch tables n, m, k, tid and the result arrays, all device pointers), each by one
 // cluster of CTAs.  n_cap / m_cap bound the trials' n and m; cluster = CTAs per cluster
 // (0: four, or the smallest power of two above that the sizes fit).
@@ -26,19 +26,21 @@ struct GbResidentArgs {
   int *ok;
   double *bytes;
   int n_cap, m_cap, cluster;
+  int alg;  // GB_ALG_NIHT or GB_ALG_CGIHT
 };
 
 gb_status gb_resident_enqueue(const GbResidentArgs &a, cudaStream_t s);
 // CTAs per cluster the resident form uses for these sizes (0: the sizes do not fit)
-int gb_resident_pick_cluster(int n_cap, int m_cap, int requested);
+int gb_resident_pick_cluster(int n_cap, int m_cap, int requested, int gb_alg);
 // shared memory per CTA, and the most a CTA can have
-size_t gb_resident_smem(int n_cap, int m_cap, int C);
+size_t gb_resident_smem(int n_cap, int m_cap, int C, int gb_alg);
 int gb_resident_max_smem();
 // cluster size of the last resident launch on this device (0: none)
 int gb_resident_last_cluster();
 // held for the whole of gb_cs_solve_batch (gb_batch.cu): the engines are shared per device
 std::recursive_mutex &gb_batch_mutex();
-// The single-trial drop-in's dense NIHT (state initialised in w.st, y in w.y) on one
-// cluster; x to w.x and the final state to w.st.  *used = 0: not eligible, nothing launched.
-gb_status gb_resident_solve_single(GbWork &w, int num_bins, cudaStream_t s, int *used);
+// The single-trial drop-in's dense NIHT or CGIHT (state initialised in w.st, y in w.y) on
+// one cluster; x to w.x and the final state to w.st.  *used = 0: not eligible, nothing
+// launched.
+gb_status gb_resident_solve_single(GbWork &w, int gb_alg, int num_bins, cudaStream_t s, int *used);
 
