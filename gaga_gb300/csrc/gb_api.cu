@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "gb_internal.cuh"
+#include "gb_resident.h"
 #include "gb_philox.cuh"
 
 gb_status gb_ops_init_attributes();
@@ -427,6 +428,7 @@ extern "C" gb_status gb_cs_solve(const char *alg, const gb_problem *p, const gb_
   if (w.ml_params) {
     GB_CUDA_TRY(cudaMemcpyAsync(&st, w.st, sizeof(st), cudaMemcpyDeviceToHost, s));
     GB_CUDA_TRY(cudaStreamSynchronize(s));
+    GB_TRY(gb_resident_check());
     warm = 1;
     if (st.fell_back) {
       // the warm start did not reduce the residual: plain zero-initialised CGIHT decides
@@ -447,6 +449,7 @@ extern "C" gb_status gb_cs_solve(const char *alg, const gb_problem *p, const gb_
     GB_CUDA_TRY(cudaMemcpyAsync(rec.data(), w.rec, sizeof(float) * (o.maxiter + 1), cudaMemcpyDeviceToHost, s));
   }
   GB_CUDA_TRY(cudaStreamSynchronize(s));
+  GB_TRY(gb_resident_check());
   float ms = 0.0f;
   cudaEventElapsedTime(&ms, e0, e1);
   cudaEventDestroy(e0);
@@ -678,6 +681,7 @@ extern "C" gb_status gb_cs_generate_and_solve(const char *alg, int kind, int k, 
   cudaEventRecord(t2, 0);
   GbState st;
   GB_CUDA_TRY(cudaMemcpy(&st, w.st, sizeof(st), cudaMemcpyDeviceToHost));
+  GB_TRY(gb_resident_check());
   GB_CUDA_TRY(cudaMemcpy(x_out, w.x, sizeof(float) * n, cudaMemcpyDeviceToHost));
   std::vector<float> rec;
   if (gb_is_ccs(alg_id)) {

@@ -413,7 +413,7 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
     rn = GB_RESIDENT_N_DEFAULT;
     if (const char *e = getenv("GB_CS_RESIDENT_N")) rn = atoi(e);
   }
-  if ((b->alg != GB_ALG_NIHT && b->alg != GB_ALG_CGIHT) || b->use_learned) rn = -1;
+  if (b->alg != GB_ALG_NIHT && b->alg != GB_ALG_CGIHT) rn = -1;
   std::vector<char> resident(T, 0);
   int rn_cap = 16, rm_cap = 1, n_res = 0;
   for (int t = 0; t < T; ++t)
@@ -423,7 +423,7 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
       rm_cap = std::max(rm_cap, b->m[t]);
       n_res++;
     }
-  if (n_res > 0 && gb_resident_pick_cluster(rn_cap, rm_cap, b->cluster, b->alg) <= 0) {
+  if (n_res > 0 && gb_resident_pick_cluster(rn_cap, rm_cap, b->cluster, b->alg, b->use_learned ? 1 : 0) <= 0) {
     if (b->cluster > 0 || b->resident_n > 0) {
       gb_set_error_message("resident form: the requested cluster size does not fit these trials", __FILE__,
                            __LINE__);
@@ -499,6 +499,8 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
     ra.seed = b->seed; ra.tol_rel = b->tol_rel; ra.maxiter = b->maxiter;
     ra.iters = E.diters; ra.err = E.derr; ra.ok = E.dok; ra.bytes = E.dbytes;
     ra.n_cap = rn_cap; ra.m_cap = rm_cap; ra.cluster = b->cluster; ra.alg = b->alg;
+    ra.ml_params = learned ? E.ml_params : nullptr;
+    ra.fb = learned ? E.dfb : nullptr;
     GB_TRY(gb_resident_enqueue(ra, s));
   }
   for (size_t i = 0; i < nslot; ++i) GB_CUDA_TRY(cudaStreamWaitEvent(s, E.done[i], 0));
@@ -512,6 +514,7 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
   GB_CUDA_TRY(cudaMemcpyAsync(hok.data(), E.dok, (size_t)T * 4, cudaMemcpyDeviceToHost, s));
   GB_CUDA_TRY(cudaMemcpyAsync(&hbytes, E.dbytes, 8, cudaMemcpyDeviceToHost, s));
   GB_CUDA_TRY(cudaStreamSynchronize(s));
+  if (n_res > 0) GB_TRY(gb_resident_check());
   cudaEventElapsedTime(&g_last_kernel_ms, E.e0, E.e1);
   g_last_bytes = hbytes;
   if (learned) {

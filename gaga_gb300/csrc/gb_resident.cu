@@ -32,6 +32,7 @@
 
 #include "gb_ctrl.cuh"
 #include "gb_internal.cuh"
+#include "gb_mlp.cuh"
 #include "gb_philox.cuh"
 #include "gb_resident.h"
 
@@ -41,8 +42,8 @@ namespace cg = cooperative_groups;
 #define RS_WARPS (RS_THREADS / 32)
 #define RS_NPUB 16
 
-// algorithms of the resident kernel
-enum { RS_NIHT = 0, RS_CGIHT = 1 };
+// algorithms of the resident kernel (RS_CGIHT_ML: CGIHT from the learned warm start)
+enum { RS_NIHT = 0, RS_CGIHT = 1, RS_CGIHT_ML = 2 };
 
 namespace {
 
@@ -71,6 +72,9 @@ struct RsParams {
   const float *yg;
   float *xg;
   GbState *st_io;
+  // learned warm start (RS_CGIHT_ML): the MLP parameters; per trial whether it fell back
+  const float *ml_params;
+  int *fb;
 };
 
 // Shared-memory layout of one CTA (the same on host and device).
@@ -78,6 +82,7 @@ struct RsLayout {
   int nc_cap, lda_cap, rc4_cap, nb_cap;
   size_t o_st, o_pub, o_x, o_grad, o_x0, o_bins, o_sidx, o_r, o_part, o_rowp, o_ypart, o_cnt, o_cntf, o_gscr;
   size_t o_gp, o_gpt, o_binsp, o_rowa, o_rowb;  // CGIHT only (zero bytes for NIHT)
+  size_t o_mlh, o_mlc;                         // learned warm start only
   size_t bytes;
 };
 
@@ -111,12 +116,17 @@ __host__ __device__ inline RsLayout rs_layout(int n_cap, int m_cap, int C, int n
   L.o_cnt = rs_take(o, (size_t)L.nb_cap * 4);
   L.o_cntf = rs_take(o, (size_t)L.nb_cap * 4);
   L.o_gscr = rs_take(o, (size_t)RS_THREADS * 16);
-  const size_t cg = alg == RS_CGIHT ? 1 : 0;
+  const size_t cg = alg == RS_CGIHT || alg == RS_CGIHT_ML ? 1 : 0;
   L.o_gp = rs_take(o, cg * L.nc_cap * 4);      // grad_previous (own columns)
   L.o_gpt = rs_take(o, cg * L.nc_cap * 4);     // grad_prev_thres
   L.o_binsp = rs_take(o, cg * L.nc_cap * 4);   // bins before the last binning
   L.o_rowa = rs_take(o, cg * L.rc4_cap * 16);  // own rows of A grad_prev_thres, then of A gp
   L.o_rowb = rs_take(o, cg * L.rc4_cap * 16);  // own rows of A x_thres
+  const size_t ml = alg == RS_CGIHT_ML ? 1 : 0;
+  // (32 KB: more shared memory leaves the SM's L1 too small; a 66 KB layout measured 12%
+  // slower over the whole solve)
+  L.o_mlh = rs_take(o, ml * ML_RANK_BINS * 4);  // the CTA's |g| rank histogram
+  L.o_mlc = rs_take(o, ml * ML_RANK_BINS * 4);  // the cluster's: 2 * exclusive prefix + count
   L.bytes = o;
   return L;
 }
@@ -459,6 +469,53 @@ __device__ void hist_own(const GbState *st, const float *v, int *bins, int nc, i
   }
 }
 
+// ml_forward1 (gb_mlp.cuh) with the weights read from global memory (cached) and rounded to
+// BF16 at every use: the same arithmetic, no shared memory
+__device__ __forceinline__ float ml_w(const float *__restrict__ p, int i) { return ml_bf16(__ldg(p + i)); }
+__device__ float ml_forward1_g(const float *__restrict__ p, const float f[ML_IN]) {
+  float h1[ML_H];
+#pragma unroll
+  for (int j = 0; j < ML_H; ++j) {
+    float a = ml_w(p, ML_OFF_B1 + j);
+#pragma unroll
+    for (int q = 0; q < ML_IN; ++q) a = fmaf(ml_w(p, ML_OFF_W1 + j * ML_IN + q), f[q], a);
+    h1[j] = ml_gelu(a);
+  }
+  float out = ml_w(p, ML_OFF_B3);
+  for (int j = 0; j < ML_H; ++j) {
+    float a = ml_w(p, ML_OFF_B2 + j);
+#pragma unroll
+    for (int i = 0; i < ML_H; ++i) a = fmaf(ml_w(p, ML_OFF_W2 + j * ML_H + i), h1[i], a);
+    out = fmaf(ml_w(p, ML_OFF_W3 + j), ml_gelu(a), out);
+  }
+  return out;
+}
+
+// x_c = g_c * net(features_c) over the CTA's columns (g in x; bins: each entry's rank bin;
+// mlc: 2 * exclusive prefix + count per bin); returns the thread's max |x|.  Not inlined: the
+// network's registers stay out of the solver loop's allocation.
+__device__ __noinline__ float ml_warm_own(float *x, const int *bins, int nc, int n, float mx, float delta, float rho,
+                                          const int *mlc, const float *__restrict__ p) {
+  float mxx = 0.0f;
+  for (int c = threadIdx.x; c < nc; c += RS_THREADS) {
+    const float gi = x[c];
+    const int b = bins[c];
+    float f[ML_IN];
+    f[0] = mx > 0.0f ? fabsf(gi) / mx : 0.0f;
+    f[1] = (0.5f * (float)mlc[b]) / (float)n;  // (cum[b] + counts[b] / 2) / n, exact
+    f[2] = delta;
+    f[3] = rho;
+    const float v = gi * ml_forward1_g(p, f);
+    x[c] = v;
+    mxx = fmaxf(mxx, fabsf(v));
+  }
+  return mxx;
+}
+
+// set by a launch whose dynamic shared memory is smaller than the layout its parameters imply
+// (every CTA then returns before touching memory); read and cleared by gb_resident_check
+__device__ int g_rs_guard;
+
 // DEEP: the single given-data solve's deeper A^T r pipeline (a separate instance, so the
 // batched kernel keeps its own register allocation).  ALG: RS_NIHT or RS_CGIHT.
 template <bool DEEP, int ALG>
@@ -472,6 +529,14 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
   const int cid = blockIdx.x / C;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const RsLayout L = rs_layout(P.n_cap, P.m_cap, C, P.nb_cap, ALG);
+  {
+    unsigned int dsmem;
+    asm volatile("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dsmem));
+    if ((size_t)dsmem < L.bytes) {  // the same for every CTA of the launch
+      if (threadIdx.x == 0) atomicExch(&g_rs_guard, 1);
+      return;
+    }
+  }
   GbState *st = reinterpret_cast<GbState *>(smem + L.o_st);
   float *pub = reinterpret_cast<float *>(smem + L.o_pub);
   int *ipub = reinterpret_cast<int *>(pub + RS_NPUB);
@@ -492,6 +557,9 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
   int *binsp = reinterpret_cast<int *>(smem + L.o_binsp);
   float *rowa = reinterpret_cast<float *>(smem + L.o_rowa);
   float *rowb = reinterpret_cast<float *>(smem + L.o_rowb);
+  int *mlh = reinterpret_cast<int *>(smem + L.o_mlh);
+  int *mlc = reinterpret_cast<int *>(smem + L.o_mlc);
+  constexpr bool IS_CG = ALG == RS_CGIHT || ALG == RS_CGIHT_ML;
   float *A = P.single ? const_cast<float *>(P.Ag) : P.A + (size_t)cid * P.a_stride;
   int *xh = P.single ? nullptr : P.xhist + (size_t)cid * P.n_cap;
   {
@@ -546,7 +614,7 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
     } else {
     const uint32_t key = P.seed + (P.tid ? P.tid[t] : (uint32_t)t);
     if (tid == 0) {
-      batch_trial_fields(st, t, m, n, P.k[t], P.maxiter, ALG == RS_CGIHT ? GB_ALG_CGIHT : GB_ALG_NIHT);
+      batch_trial_fields(st, t, m, n, P.k[t], P.maxiter, IS_CG ? GB_ALG_CGIHT : GB_ALG_NIHT);
       st->lda = lda;
     }
     // ---- draw the trial (k_b_gen_A, k_b_gen_x, key bins, y = A x0 of gb_batch.cu)
@@ -620,177 +688,153 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
     gather_rows(cl, C, q4, RB, rowp, r);
     if (tid == 0) {
       st->red[R_RES] = combine_sum(cl, C, pub, R_RES);
-      batch_solver_init(st, P.tol_rel, 0);
+      batch_solver_init(st, P.tol_rel, ALG == RS_CGIHT_ML ? 1 : 0);
       // NIHT prologue (algorithms.cu:1296-1354): resid = y; err = ||y||
       ctrl_phase(st, C_INIT0, 0);
     }
     __syncthreads();
     }
-    // x = A^T y ; max|x| ; FindSupportSet ; Threshold
-    at_own<DEEP>(A, lda, q4, c0, nc, r, x);
-    __syncthreads();
-    {
-      float mxx = 0.0f;
-      for (int c = tid; c < nc; c += RS_THREADS) mxx = fmaxf(mxx, fabsf(x[c]));
-      for (int b = tid; b < L.nb_cap; b += RS_THREADS) cnt[b] = 0;
-      const float b = block_reduce<1>(mxx, red32);
-      if (tid == 0) pub[R_XMAX] = b;
-    }
-    cl.sync();
-    if (tid == 0) {
-      st->red[R_XMAX] = (double)combine_max(cl, C, pub, R_XMAX);
-      ctrl_phase(st, C_INIT_BINPREP, 0);
-    }
-    __syncthreads();
-    // the support step (enq_support): bins and the k-th bin when binning, threshold always;
-    // with save_prev (CGIHT) the previous bins are kept and a support entry that left is
-    // flagged (checkSupportEvolution, GAGA/gaga/kernels.cu:178-193) in st->changed
-    auto support = [&](bool save_prev) {
-      const bool dobin = st->flags[F_DOBIN] != 0;
-      if (dobin) {
-        if (save_prev)
-          for (int c = tid; c < nc; c += RS_THREADS) binsp[c] = bins[c];  // the same thread bins c next
-        hist_own(st, x, bins, nc, cnt, nullptr);
-        cl.sync();
-        const int mb = st->max_bin;
-        for (int b = tid; b < mb; b += RS_THREADS) {
-          int s = 0;
-          for (int c = 0; c < C; ++c) s += peer(cl, cnt, c)[b];
-          cntf[b] = s;
-        }
-        __syncthreads();
-        block_kbin<false>(st, cntf, st->k);
-      }
-      const int kb = st->k_bin, kbp = st->k_bin_prev;
-      int chg = 0;
-      for (int c = tid; c < nc; c += RS_THREADS) {
-        if (bins[c] > kb) x[c] = 0.0f;
-        if (save_prev && dobin && binsp[c] <= kbp && bins[c] > kb) chg = 1;
-      }
-      if (dobin) s_own = compact_own(bins, nc, kb, sidx, wcnt);
-      if (save_prev && dobin) {
-        const int any = __syncthreads_or(chg);
-        if (tid == 0) ipub[1] = any;
-        cl.sync();
+    // A learned warm start abandoned after 10 iterations (C_CGIHT_STOP) is solved again from
+    // zero by plain CGIHT on the same cluster, its slab of A still in place, and the
+    // iterations add up (the batched form's fallback, gb_cs_solve_batch)
+    int warm_iters = 0;
+    double warm_bytes = 0.0;
+    const double y2 = st->red[R_RES];
+    for (int attempt = 0;; ++attempt) {
+      if (attempt > 0) {
+        warm_iters = st->iter;
+        warm_bytes = st->bytes;
+        __syncthreads();  // every thread has read the state before thread 0 resets it
         if (tid == 0) {
-          int a = 0;
-          for (int c = 0; c < C; ++c) a |= peer(cl, ipub, c)[1];
-          st->changed = a;
+          st->red[R_RES] = y2;
+          st->active = 1;
+          batch_solver_init(st, P.tol_rel, 0);
+          ctrl_phase(st, C_INIT0, 0);
         }
+        gather_rows(cl, C, q4, RB, ypart, r);  // r = y again (every CTA's rows of y are unchanged)
+        __syncthreads();
       }
-      __syncthreads();
-    };
-    support(false);
-    if (ALG == RS_NIHT && tid == 0) ctrl_phase(st, C_INIT_DONE, 0);
-    __syncthreads();
-    // ---- NIHT iterations (RestrictedSD, GAGA/gaga/functions.cu:659-745, then the support)
-    while (ALG == RS_NIHT && st->active) {
-      // resid = y - A x_S ; ||resid||^2
-      av_own_partial(A, lda, q4, c0, sidx, s_own, x, part, gscr);
-      if (tid == 0) ipub[0] = s_own;
-      cl.sync();
-      {
-        const float s2 = reduce_rows(cl, C, part, rr0, rr1, ypart, rowp, nullptr);
-        const float b = block_reduce<0>(s2, red32);
-        if (tid == 0) pub[R_RES] = b;
-      }
-      cl.sync();
-      gather_rows(cl, C, q4, RB, rowp, r);
-      if (tid == 0) {
-        st->red[R_RES] = combine_sum(cl, C, pub, R_RES);
-        int sc = 0;
-        for (int c = 0; c < C; ++c) sc += peer(cl, ipub, c)[0];
-        st->s_cnt = sc;
-        ctrl_phase(st, C_PUSH_RES, 0);
-      }
-      __syncthreads();
-      // grad = A^T resid ; ||grad on the support||^2 ; max|grad|
-      at_own<DEEP>(A, lda, q4, c0, nc, r, grad);
+      // x = A^T y ; max|x| ; FindSupportSet ; Threshold
+      at_own<DEEP>(A, lda, q4, c0, nc, r, x);
       __syncthreads();
       {
-        const int kb = st->k_bin;
-        float s2 = 0.0f, gm = 0.0f;
-        for (int c = tid; c < nc; c += RS_THREADS) {
-          const float g = grad[c];
-          const float o = bins[c] <= kb ? g : 0.0f;
-          s2 = fmaf(o, o, s2);
-          gm = fmaxf(gm, fabsf(g));
-        }
-        // published now, combined after the next two cluster barriers with ||A x_thres||^2
-        block_reduce_sum_max(s2, gm, red32, &pub[R_XT], &pub[R_GMAX]);
-      }
-      // ||A x_thres||^2 (x_thres = grad on the support)
-      av_own_partial(A, lda, q4, c0, sidx, s_own, grad, part, gscr);
-      cl.sync();
-      {
-        const float s2 = reduce_rows(cl, C, part, rr0, rr1, nullptr, nullptr, nullptr);
-        const float b = block_reduce<0>(s2, red32);
-        if (tid == 0) pub[R_AXT] = b;
-      }
-      cl.sync();
-      if (tid == 0) {
-        st->red[R_XT] = combine_sum(cl, C, pub, R_XT);
-        st->red[R_GMAX] = (double)combine_max(cl, C, pub, R_GMAX);
-        st->red[R_AXT] = combine_sum(cl, C, pub, R_AXT);
-        ctrl_phase(st, C_SD_MU, 0);
-      }
-      __syncthreads();
-      // x += mu grad ; max|x| ; counters cleared
-      {
-        const float mu = st->mu;
         float mxx = 0.0f;
-        for (int c = tid; c < nc; c += RS_THREADS) {
-          const float o = fmaf(mu, grad[c], x[c]);
-          x[c] = o;
-          mxx = fmaxf(mxx, fabsf(o));
-        }
+        for (int c = tid; c < nc; c += RS_THREADS) mxx = fmaxf(mxx, fabsf(x[c]));
         for (int b = tid; b < L.nb_cap; b += RS_THREADS) cnt[b] = 0;
         const float b = block_reduce<1>(mxx, red32);
         if (tid == 0) pub[R_XMAX] = b;
       }
       cl.sync();
-      if (tid == 0) {
-        st->red[R_XMAX] = (double)combine_max(cl, C, pub, R_XMAX);
-        ctrl_phase(st, C_BINPREP, 0);
+      if (tid == 0) st->red[R_XMAX] = (double)combine_max(cl, C, pub, R_XMAX);
+      __syncthreads();
+      if (ALG == RS_CGIHT_ML && st->learned) {
+        // learned warm start (enq_learned_warm, gb_learned.cu): x_i = g_i * net(features_i) with
+        // g = A^T y in x; the rank feature from the cluster's 4096-bin histogram of |g|
+        const float mx = (float)st->red[R_XMAX];
+        const float slope = mx > 0.0f ? (float)(ML_RANK_BINS - 1) / mx : 0.0f;
+        for (int b = tid; b < ML_RANK_BINS; b += RS_THREADS) mlh[b] = 0;
+        __syncthreads();
+        for (int c = tid; c < nc; c += RS_THREADS) {
+          int b = (int)((mx - fabsf(x[c])) * slope);
+          b = min(max(b, 0), ML_RANK_BINS - 1);
+          bins[c] = b;
+          atomicAdd(&mlh[b], 1);
+        }
+        cl.sync();
+        {
+          // the cluster's counts (rank order) and, in place, 2 * exclusive prefix + count:
+          // rank feature (cum + count / 2) / n exactly as ml_features computes it
+          constexpr int PER = ML_RANK_BINS / RS_THREADS;
+          int loc[PER], tot = 0;
+#pragma unroll
+          for (int q = 0; q < PER; ++q) {
+            const int b = tid * PER + q;
+            int sum = 0;
+            for (int c = 0; c < C; ++c) sum += peer(cl, mlh, c)[b];
+            loc[q] = sum;
+            tot += sum;
+          }
+          int incl = tot;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+          }
+          if (lane == 31) wcnt[wid] = incl;
+          __syncthreads();
+          int run = incl - tot;
+          for (int w2 = 0; w2 < wid; ++w2) run += wcnt[w2];
+#pragma unroll
+          for (int q = 0; q < PER; ++q) {
+            mlc[tid * PER + q] = 2 * run + loc[q];
+            run += loc[q];
+          }
+        }
+        __syncthreads();
+        const float delta = (float)st->m / (float)st->n, rho = (float)st->k / (float)st->m;
+        const float mxx = ml_warm_own(x, bins, nc, n, mx, delta, rho, mlc, P.ml_params);
+        const float b = block_reduce<1>(mxx, red32);
+        if (tid == 0) pub[R_XMAX] = b;
+        cl.sync();
+        if (tid == 0) st->red[R_XMAX] = (double)combine_max(cl, C, pub, R_XMAX);
+        __syncthreads();
       }
+      if (tid == 0) ctrl_phase(st, C_INIT_BINPREP, 0);
       __syncthreads();
+      // the support step (enq_support): bins and the k-th bin when binning, threshold always;
+      // with save_prev (CGIHT) the previous bins are kept and a support entry that left is
+      // flagged (checkSupportEvolution, GAGA/gaga/kernels.cu:178-193) in st->changed
+      auto support = [&](bool save_prev) {
+        const bool dobin = st->flags[F_DOBIN] != 0;
+        if (dobin) {
+          if (save_prev)
+            for (int c = tid; c < nc; c += RS_THREADS) binsp[c] = bins[c];  // the same thread bins c next
+          hist_own(st, x, bins, nc, cnt, nullptr);
+          cl.sync();
+          const int mb = st->max_bin;
+          for (int b = tid; b < mb; b += RS_THREADS) {
+            int s = 0;
+            for (int c = 0; c < C; ++c) s += peer(cl, cnt, c)[b];
+            cntf[b] = s;
+          }
+          __syncthreads();
+          block_kbin<false>(st, cntf, st->k);
+        }
+        const int kb = st->k_bin, kbp = st->k_bin_prev;
+        int chg = 0;
+        for (int c = tid; c < nc; c += RS_THREADS) {
+          if (bins[c] > kb) x[c] = 0.0f;
+          if (save_prev && dobin && binsp[c] <= kbp && bins[c] > kb) chg = 1;
+        }
+        if (dobin) s_own = compact_own(bins, nc, kb, sidx, wcnt);
+        if (save_prev && dobin) {
+          const int any = __syncthreads_or(chg);
+          if (tid == 0) ipub[1] = any;
+          cl.sync();
+          if (tid == 0) {
+            int a = 0;
+            for (int c = 0; c < C; ++c) a |= peer(cl, ipub, c)[1];
+            st->changed = a;
+          }
+        }
+        __syncthreads();
+      };
       support(false);
-      if (tid == 0) ctrl_phase(st, C_NIHT_STOP, 0);
+      if (ALG == RS_NIHT && tid == 0) ctrl_phase(st, C_INIT_DONE, 0);
       __syncthreads();
-    }
-    if (ALG == RS_CGIHT) {
-      // A v_S of the own support into an m-vector (2 cluster barriers): own rows into rows,
-      // y - A v_S with sub_y; every row gathered into full when given; the CTA's partial of
-      // the squared norm into pub[slot], combined by the caller before its next barrier
-      auto av_rows = [&](const float *v, bool sub_y, float *rows, float *full, int slot) {
-        av_own_partial(A, lda, q4, c0, sidx, s_own, v, part, gscr);
+      // ---- NIHT iterations (RestrictedSD, GAGA/gaga/functions.cu:659-745, then the support)
+      while (ALG == RS_NIHT && st->active) {
+        // resid = y - A x_S ; ||resid||^2
+        av_own_partial(A, lda, q4, c0, sidx, s_own, x, part, gscr);
         if (tid == 0) ipub[0] = s_own;
         cl.sync();
-        const float s2 = reduce_rows(cl, C, part, rr0, rr1, sub_y ? ypart : nullptr, rows, nullptr);
-        const float b = block_reduce<0>(s2, red32);
-        if (tid == 0 && slot >= 0) pub[slot] = b;
+        {
+          const float s2 = reduce_rows(cl, C, part, rr0, rr1, ypart, rowp, nullptr);
+          const float b = block_reduce<0>(s2, red32);
+          if (tid == 0) pub[R_RES] = b;
+        }
         cl.sync();
-        if (full) gather_rows(cl, C, q4, RB, rows, full);
-      };
-      // prologue tail (GAGA/gaga/algorithms.cu:3776-3808): r0 = y - A x, grad_previous =
-      // A^T r0, grad_prev_thres
-      av_rows(x, true, rowp, r, R_RES);
-      if (tid == 0) st->red[R_RES] = combine_sum(cl, C, pub, R_RES);
-      __syncthreads();
-      at_own<DEEP>(A, lda, q4, c0, nc, r, gp);
-      __syncthreads();
-      {
-        const int kb = st->k_bin;
-        for (int c = tid; c < nc; c += RS_THREADS) gpt[c] = bins[c] <= kb ? gp[c] : 0.0f;
-      }
-      if (tid == 0) ctrl_phase(st, C_CGIHT_INIT, 0);
-      __syncthreads();
-      // ---- CGIHT iterations: RestrictedCGwithSupportEvolution (F_RCG,
-      // GAGA/gaga/functions.cu:1004-1102) or UnrestrictedCG (F_UCG, :1107-1220), then
-      // x += alpha p and the support (algorithms.cu:3849-3899)
-      while (st->active) {
-        const bool rcg = st->flags[F_RCG] != 0;
-        av_rows(x, true, rowp, r, R_RES);  // r = y - A x_S
+        gather_rows(cl, C, q4, RB, rowp, r);
         if (tid == 0) {
           st->red[R_RES] = combine_sum(cl, C, pub, R_RES);
           int sc = 0;
@@ -799,114 +843,43 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
           ctrl_phase(st, C_PUSH_RES, 0);
         }
         __syncthreads();
-        at_own<DEEP>(A, lda, q4, c0, nc, r, grad);  // grad = A^T r; x_thres = grad on the support
+        // grad = A^T resid ; ||grad on the support||^2 ; max|grad|
+        at_own<DEEP>(A, lda, q4, c0, nc, r, grad);
         __syncthreads();
-        const int kb = st->k_bin;
-        float sxt = 0.0f;
-        for (int c = tid; c < nc; c += RS_THREADS) {
-          const float o = bins[c] <= kb ? grad[c] : 0.0f;
-          sxt = fmaf(o, o, sxt);
-        }
-        if (rcg) {
-          {
-            const float b = block_reduce<0>(sxt, red32);
-            if (tid == 0) pub[R_XT] = b;
-          }
-          cl.sync();
-          if (tid == 0) {
-            st->red[R_XT] = combine_sum(cl, C, pub, R_XT);
-            ctrl_phase(st, C_RCG_BETA, 0);
-          }
-          __syncthreads();
-          {
-            const float beta = st->cg_beta;
-            float gm = 0.0f;
-            for (int c = tid; c < nc; c += RS_THREADS) {
-              const float g = fmaf(1.0f, grad[c], beta * gp[c]);  // k_scale_add
-              gp[c] = g;
-              gpt[c] = bins[c] <= kb ? g : 0.0f;
-              gm = fmaxf(gm, fabsf(g));
-            }
-            const float b = block_reduce<1>(gm, red32);
-            if (tid == 0) pub[R_GMAX] = b;  // combined after the next product
-          }
-          av_rows(gpt, false, rowa, nullptr, R_AXT);  // ||A grad_prev_thres||^2
-          if (tid == 0) {
-            st->red[R_GMAX] = (double)combine_max(cl, C, pub, R_GMAX);
-            st->red[R_AXT] = combine_sum(cl, C, pub, R_AXT);
-            ctrl_phase(st, C_RCG_ALPHA, 0);
-          }
-          __syncthreads();
-        } else {
-          {
-            const float b = block_reduce<0>(sxt, red32);
-            if (tid == 0) pub[R_XT] = b;  // combined with the dot products below
-          }
-          av_rows(gpt, false, rowa, nullptr, -1);  // own rows of A grad_prev_thres
-          av_rows(grad, false, rowb, nullptr, -1);  // own rows of A x_thres
-          {
-            const float4 *a4 = reinterpret_cast<const float4 *>(rowa);
-            const float4 *b4 = reinterpret_cast<const float4 *>(rowb);
-            float d1 = 0.0f, d2 = 0.0f;
-            for (int i = tid; i < rr1 - rr0; i += RS_THREADS) {
-              const float4 a = a4[i], bb = b4[i];
-              d1 = fmaf(a.x, bb.x, d1); d1 = fmaf(a.y, bb.y, d1); d1 = fmaf(a.z, bb.z, d1); d1 = fmaf(a.w, bb.w, d1);
-              d2 = fmaf(a.x, a.x, d2); d2 = fmaf(a.y, a.y, d2); d2 = fmaf(a.z, a.z, d2); d2 = fmaf(a.w, a.w, d2);
-            }
-            const float b1 = block_reduce<0>(d1, red32);
-            if (tid == 0) pub[R_DOT1] = b1;
-            const float b2 = block_reduce<0>(d2, red32);
-            if (tid == 0) pub[R_DOT2] = b2;
-          }
-          cl.sync();
-          if (tid == 0) {
-            st->red[R_XT] = combine_sum(cl, C, pub, R_XT);
-            st->red[R_DOT1] = combine_sum(cl, C, pub, R_DOT1);
-            st->red[R_DOT2] = combine_sum(cl, C, pub, R_DOT2);
-            ctrl_phase(st, C_UCG_BETA, 0);
-          }
-          __syncthreads();
-          {
-            const float beta = st->cg_beta;
-            float gm = 0.0f, d3 = 0.0f, d4 = 0.0f;
-            for (int c = tid; c < nc; c += RS_THREADS) {
-              const float g = fmaf(1.0f, grad[c], beta * gp[c]);  // k_scale_add
-              gp[c] = g;
-              const bool in = bins[c] <= kb;
-              const float pt = in ? g : 0.0f;
-              gpt[c] = pt;
-              gm = fmaxf(gm, fabsf(g));
-              d3 = fmaf(pt, in ? grad[c] : 0.0f, d3);  // <grad_prev_thres, x_thres>
-            }
-            float4 *a4 = reinterpret_cast<float4 *>(rowa);
-            const float4 *b4 = reinterpret_cast<const float4 *>(rowb);
-            for (int i = tid; i < rr1 - rr0; i += RS_THREADS) {  // A p = A x_thres + beta A p_prev
-              float4 a = a4[i];
-              const float4 bb = b4[i];
-              a.x = fmaf(1.0f, bb.x, beta * a.x); a.y = fmaf(1.0f, bb.y, beta * a.y);
-              a.z = fmaf(1.0f, bb.z, beta * a.z); a.w = fmaf(1.0f, bb.w, beta * a.w);
-              a4[i] = a;
-              d4 = fmaf(a.x, a.x, d4); d4 = fmaf(a.y, a.y, d4); d4 = fmaf(a.z, a.z, d4); d4 = fmaf(a.w, a.w, d4);
-            }
-            block_reduce_sum_max(d3, gm, red32, &pub[R_DOT3], &pub[R_GMAX]);
-            const float b4s = block_reduce<0>(d4, red32);
-            if (tid == 0) pub[R_DOT4] = b4s;
-          }
-          cl.sync();
-          if (tid == 0) {
-            st->red[R_DOT3] = combine_sum(cl, C, pub, R_DOT3);
-            st->red[R_DOT4] = combine_sum(cl, C, pub, R_DOT4);
-            st->red[R_GMAX] = (double)combine_max(cl, C, pub, R_GMAX);
-            ctrl_phase(st, C_UCG_ALPHA, 0);
-          }
-          __syncthreads();
-        }
-        // x += alpha grad_previous ; max|x| ; counters cleared
         {
-          const float alpha = st->cg_alpha;
+          const int kb = st->k_bin;
+          float s2 = 0.0f, gm = 0.0f;
+          for (int c = tid; c < nc; c += RS_THREADS) {
+            const float g = grad[c];
+            const float o = bins[c] <= kb ? g : 0.0f;
+            s2 = fmaf(o, o, s2);
+            gm = fmaxf(gm, fabsf(g));
+          }
+          // published now, combined after the next two cluster barriers with ||A x_thres||^2
+          block_reduce_sum_max(s2, gm, red32, &pub[R_XT], &pub[R_GMAX]);
+        }
+        // ||A x_thres||^2 (x_thres = grad on the support)
+        av_own_partial(A, lda, q4, c0, sidx, s_own, grad, part, gscr);
+        cl.sync();
+        {
+          const float s2 = reduce_rows(cl, C, part, rr0, rr1, nullptr, nullptr, nullptr);
+          const float b = block_reduce<0>(s2, red32);
+          if (tid == 0) pub[R_AXT] = b;
+        }
+        cl.sync();
+        if (tid == 0) {
+          st->red[R_XT] = combine_sum(cl, C, pub, R_XT);
+          st->red[R_GMAX] = (double)combine_max(cl, C, pub, R_GMAX);
+          st->red[R_AXT] = combine_sum(cl, C, pub, R_AXT);
+          ctrl_phase(st, C_SD_MU, 0);
+        }
+        __syncthreads();
+        // x += mu grad ; max|x| ; counters cleared
+        {
+          const float mu = st->mu;
           float mxx = 0.0f;
           for (int c = tid; c < nc; c += RS_THREADS) {
-            const float o = fmaf(alpha, gp[c], x[c]);
+            const float o = fmaf(mu, grad[c], x[c]);
             x[c] = o;
             mxx = fmaxf(mxx, fabsf(o));
           }
@@ -917,20 +890,188 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
         cl.sync();
         if (tid == 0) {
           st->red[R_XMAX] = (double)combine_max(cl, C, pub, R_XMAX);
-          ctrl_phase(st, C_CGIHT_BINDEC, 0);
           ctrl_phase(st, C_BINPREP, 0);
         }
         __syncthreads();
-        support(true);
-        if (tid == 0) ctrl_phase(st, C_CGIHT_POST, 0);
-        __syncthreads();
-        if (st->flags[F_REMASK]) {
-          const int kb2 = st->k_bin;
-          for (int c = tid; c < nc; c += RS_THREADS) gpt[c] = bins[c] <= kb2 ? gp[c] : 0.0f;
-        }
-        if (tid == 0) ctrl_phase(st, C_CGIHT_STOP, 0);
+        support(false);
+        if (tid == 0) ctrl_phase(st, C_NIHT_STOP, 0);
         __syncthreads();
       }
+      if (IS_CG) {
+        // A v_S of the own support into an m-vector (2 cluster barriers): own rows into rows,
+        // y - A v_S with sub_y; every row gathered into full when given; the CTA's partial of
+        // the squared norm into pub[slot], combined by the caller before its next barrier
+        auto av_rows = [&](const float *v, bool sub_y, float *rows, float *full, int slot) {
+          av_own_partial(A, lda, q4, c0, sidx, s_own, v, part, gscr);
+          if (tid == 0) ipub[0] = s_own;
+          cl.sync();
+          const float s2 = reduce_rows(cl, C, part, rr0, rr1, sub_y ? ypart : nullptr, rows, nullptr);
+          const float b = block_reduce<0>(s2, red32);
+          if (tid == 0 && slot >= 0) pub[slot] = b;
+          cl.sync();
+          if (full) gather_rows(cl, C, q4, RB, rows, full);
+        };
+        // prologue tail (GAGA/gaga/algorithms.cu:3776-3808): r0 = y - A x, grad_previous =
+        // A^T r0, grad_prev_thres
+        av_rows(x, true, rowp, r, R_RES);
+        if (tid == 0) st->red[R_RES] = combine_sum(cl, C, pub, R_RES);
+        __syncthreads();
+        at_own<DEEP>(A, lda, q4, c0, nc, r, gp);
+        __syncthreads();
+        {
+          const int kb = st->k_bin;
+          for (int c = tid; c < nc; c += RS_THREADS) gpt[c] = bins[c] <= kb ? gp[c] : 0.0f;
+        }
+        if (tid == 0) ctrl_phase(st, C_CGIHT_INIT, 0);
+        __syncthreads();
+        // ---- CGIHT iterations: RestrictedCGwithSupportEvolution (F_RCG,
+        // GAGA/gaga/functions.cu:1004-1102) or UnrestrictedCG (F_UCG, :1107-1220), then
+        // x += alpha p and the support (algorithms.cu:3849-3899)
+        while (st->active) {
+          const bool rcg = st->flags[F_RCG] != 0;
+          av_rows(x, true, rowp, r, R_RES);  // r = y - A x_S
+          if (tid == 0) {
+            st->red[R_RES] = combine_sum(cl, C, pub, R_RES);
+            int sc = 0;
+            for (int c = 0; c < C; ++c) sc += peer(cl, ipub, c)[0];
+            st->s_cnt = sc;
+            ctrl_phase(st, C_PUSH_RES, 0);
+          }
+          __syncthreads();
+          at_own<DEEP>(A, lda, q4, c0, nc, r, grad);  // grad = A^T r; x_thres = grad on the support
+          __syncthreads();
+          const int kb = st->k_bin;
+          float sxt = 0.0f;
+          for (int c = tid; c < nc; c += RS_THREADS) {
+            const float o = bins[c] <= kb ? grad[c] : 0.0f;
+            sxt = fmaf(o, o, sxt);
+          }
+          if (rcg) {
+            {
+              const float b = block_reduce<0>(sxt, red32);
+              if (tid == 0) pub[R_XT] = b;
+            }
+            cl.sync();
+            if (tid == 0) {
+              st->red[R_XT] = combine_sum(cl, C, pub, R_XT);
+              ctrl_phase(st, C_RCG_BETA, 0);
+            }
+            __syncthreads();
+            {
+              const float beta = st->cg_beta;
+              float gm = 0.0f;
+              for (int c = tid; c < nc; c += RS_THREADS) {
+                const float g = fmaf(1.0f, grad[c], beta * gp[c]);  // k_scale_add
+                gp[c] = g;
+                gpt[c] = bins[c] <= kb ? g : 0.0f;
+                gm = fmaxf(gm, fabsf(g));
+              }
+              const float b = block_reduce<1>(gm, red32);
+              if (tid == 0) pub[R_GMAX] = b;  // combined after the next product
+            }
+            av_rows(gpt, false, rowa, nullptr, R_AXT);  // ||A grad_prev_thres||^2
+            if (tid == 0) {
+              st->red[R_GMAX] = (double)combine_max(cl, C, pub, R_GMAX);
+              st->red[R_AXT] = combine_sum(cl, C, pub, R_AXT);
+              ctrl_phase(st, C_RCG_ALPHA, 0);
+            }
+            __syncthreads();
+          } else {
+            {
+              const float b = block_reduce<0>(sxt, red32);
+              if (tid == 0) pub[R_XT] = b;  // combined with the dot products below
+            }
+            av_rows(gpt, false, rowa, nullptr, -1);  // own rows of A grad_prev_thres
+            av_rows(grad, false, rowb, nullptr, -1);  // own rows of A x_thres
+            {
+              const float4 *a4 = reinterpret_cast<const float4 *>(rowa);
+              const float4 *b4 = reinterpret_cast<const float4 *>(rowb);
+              float d1 = 0.0f, d2 = 0.0f;
+              for (int i = tid; i < rr1 - rr0; i += RS_THREADS) {
+                const float4 a = a4[i], bb = b4[i];
+                d1 = fmaf(a.x, bb.x, d1); d1 = fmaf(a.y, bb.y, d1); d1 = fmaf(a.z, bb.z, d1); d1 = fmaf(a.w, bb.w, d1);
+                d2 = fmaf(a.x, a.x, d2); d2 = fmaf(a.y, a.y, d2); d2 = fmaf(a.z, a.z, d2); d2 = fmaf(a.w, a.w, d2);
+              }
+              const float b1 = block_reduce<0>(d1, red32);
+              if (tid == 0) pub[R_DOT1] = b1;
+              const float b2 = block_reduce<0>(d2, red32);
+              if (tid == 0) pub[R_DOT2] = b2;
+            }
+            cl.sync();
+            if (tid == 0) {
+              st->red[R_XT] = combine_sum(cl, C, pub, R_XT);
+              st->red[R_DOT1] = combine_sum(cl, C, pub, R_DOT1);
+              st->red[R_DOT2] = combine_sum(cl, C, pub, R_DOT2);
+              ctrl_phase(st, C_UCG_BETA, 0);
+            }
+            __syncthreads();
+            {
+              const float beta = st->cg_beta;
+              float gm = 0.0f, d3 = 0.0f, d4 = 0.0f;
+              for (int c = tid; c < nc; c += RS_THREADS) {
+                const float g = fmaf(1.0f, grad[c], beta * gp[c]);  // k_scale_add
+                gp[c] = g;
+                const bool in = bins[c] <= kb;
+                const float pt = in ? g : 0.0f;
+                gpt[c] = pt;
+                gm = fmaxf(gm, fabsf(g));
+                d3 = fmaf(pt, in ? grad[c] : 0.0f, d3);  // <grad_prev_thres, x_thres>
+              }
+              float4 *a4 = reinterpret_cast<float4 *>(rowa);
+              const float4 *b4 = reinterpret_cast<const float4 *>(rowb);
+              for (int i = tid; i < rr1 - rr0; i += RS_THREADS) {  // A p = A x_thres + beta A p_prev
+                float4 a = a4[i];
+                const float4 bb = b4[i];
+                a.x = fmaf(1.0f, bb.x, beta * a.x); a.y = fmaf(1.0f, bb.y, beta * a.y);
+                a.z = fmaf(1.0f, bb.z, beta * a.z); a.w = fmaf(1.0f, bb.w, beta * a.w);
+                a4[i] = a;
+                d4 = fmaf(a.x, a.x, d4); d4 = fmaf(a.y, a.y, d4); d4 = fmaf(a.z, a.z, d4); d4 = fmaf(a.w, a.w, d4);
+              }
+              block_reduce_sum_max(d3, gm, red32, &pub[R_DOT3], &pub[R_GMAX]);
+              const float b4s = block_reduce<0>(d4, red32);
+              if (tid == 0) pub[R_DOT4] = b4s;
+            }
+            cl.sync();
+            if (tid == 0) {
+              st->red[R_DOT3] = combine_sum(cl, C, pub, R_DOT3);
+              st->red[R_DOT4] = combine_sum(cl, C, pub, R_DOT4);
+              st->red[R_GMAX] = (double)combine_max(cl, C, pub, R_GMAX);
+              ctrl_phase(st, C_UCG_ALPHA, 0);
+            }
+            __syncthreads();
+          }
+          // x += alpha grad_previous ; max|x| ; counters cleared
+          {
+            const float alpha = st->cg_alpha;
+            float mxx = 0.0f;
+            for (int c = tid; c < nc; c += RS_THREADS) {
+              const float o = fmaf(alpha, gp[c], x[c]);
+              x[c] = o;
+              mxx = fmaxf(mxx, fabsf(o));
+            }
+            for (int b = tid; b < L.nb_cap; b += RS_THREADS) cnt[b] = 0;
+            const float b = block_reduce<1>(mxx, red32);
+            if (tid == 0) pub[R_XMAX] = b;
+          }
+          cl.sync();
+          if (tid == 0) {
+            st->red[R_XMAX] = (double)combine_max(cl, C, pub, R_XMAX);
+            ctrl_phase(st, C_CGIHT_BINDEC, 0);
+            ctrl_phase(st, C_BINPREP, 0);
+          }
+          __syncthreads();
+          support(true);
+          if (tid == 0) ctrl_phase(st, C_CGIHT_POST, 0);
+          __syncthreads();
+          if (st->flags[F_REMASK]) {
+            const int kb2 = st->k_bin;
+            for (int c = tid; c < nc; c += RS_THREADS) gpt[c] = bins[c] <= kb2 ? gp[c] : 0.0f;
+          }
+          if (tid == 0) ctrl_phase(st, C_CGIHT_STOP, 0);
+          __syncthreads();
+        }
+      }
+      if (!(ALG == RS_CGIHT_ML && !P.single && attempt == 0 && st->fell_back)) break;
     }
     if (P.single) {
       // ---- x and the final state back to the caller's workspace
@@ -959,10 +1100,11 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
     if (rank == 0 && tid == 0) {
       const double e2 = combine_sum(cl, C, pub, R_DOT1), x2 = combine_sum(cl, C, pub, R_DOT2);
       const float rel = (float)(sqrt(e2) / sqrt(x2));
-      P.iters[t] = st->iter;
+      P.iters[t] = warm_iters + st->iter;
       P.err[t] = rel;
       P.ok[t] = rel <= 1e-3f ? 1 : 0;
-      atomicAdd(P.bytes, st->bytes);
+      if (P.fb) P.fb[t] = 0;  // an abandoned warm start was solved again above
+      atomicAdd(P.bytes, warm_bytes + st->bytes);
     }
   }
   cl.sync();  // no CTA leaves while a peer may still read its shared memory
@@ -989,10 +1131,13 @@ void res_release(ResEngine &R) {
 // clusters of up to 16 CTAs
 using RsKernel = void (*)(const RsParams);
 RsKernel rs_kernel(bool deep, int alg) {
-  if (deep) return alg == RS_CGIHT ? k_resident<true, RS_CGIHT> : k_resident<true, RS_NIHT>;
-  return alg == RS_CGIHT ? k_resident<false, RS_CGIHT> : k_resident<false, RS_NIHT>;
+  if (deep)
+    return alg == RS_CGIHT_ML ? k_resident<true, RS_CGIHT_ML>
+                              : alg == RS_CGIHT ? k_resident<true, RS_CGIHT> : k_resident<true, RS_NIHT>;
+  return alg == RS_CGIHT_ML ? k_resident<false, RS_CGIHT_ML>
+                            : alg == RS_CGIHT ? k_resident<false, RS_CGIHT> : k_resident<false, RS_NIHT>;
 }
-std::atomic<unsigned long long> g_attr_done[4];
+std::atomic<unsigned long long> g_attr_done[6];
 
 }  // namespace
 
@@ -1000,7 +1145,7 @@ int gb_resident_max_smem();
 
 static gb_status rs_attrs(bool deep, int alg) {
   const int cap = gb_resident_max_smem();
-  return gb_once_per_device(g_attr_done[(deep ? 2 : 0) + alg], [&]() -> gb_status {
+  return gb_once_per_device(g_attr_done[(deep ? 3 : 0) + alg], [&]() -> gb_status {
     const void *fn = (const void *)rs_kernel(deep, alg);
     GB_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
     GB_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
@@ -1008,7 +1153,11 @@ static gb_status rs_attrs(bool deep, int alg) {
   });
 }
 
-int gb_resident_alg(int gb_alg) { return gb_alg == GB_ALG_CGIHT ? RS_CGIHT : gb_alg == GB_ALG_NIHT ? RS_NIHT : -1; }
+// the resident algorithm of a library algorithm id (learned: CGIHT from the warm start)
+int gb_resident_alg(int gb_alg, int learned) {
+  if (gb_alg == GB_ALG_CGIHT) return learned ? RS_CGIHT_ML : RS_CGIHT;
+  return gb_alg == GB_ALG_NIHT && !learned ? RS_NIHT : -1;
+}
 
 int gb_resident_max_smem() {
   int dev = 0, optin = 0;
@@ -1019,14 +1168,16 @@ int gb_resident_max_smem() {
   return optin - (int)fa.sharedSizeBytes;
 }
 
-size_t gb_resident_smem(int n_cap, int m_cap, int C, int gb_alg) {
-  return rs_layout(n_cap, m_cap, C, rs_default_bins(n_cap), gb_resident_alg(gb_alg)).bytes;
+size_t gb_resident_smem(int n_cap, int m_cap, int C, int gb_alg, int learned) {
+  return rs_layout(n_cap, m_cap, C, rs_default_bins(n_cap), gb_resident_alg(gb_alg, learned)).bytes;
 }
 
-int gb_resident_pick_cluster(int n_cap, int m_cap, int requested, int gb_alg) {
+int gb_resident_pick_cluster(int n_cap, int m_cap, int requested, int gb_alg, int learned) {
   const int cap = gb_resident_max_smem();
-  if (m_cap > 8192 || n_cap > 20000 || cap <= 0 || gb_resident_alg(gb_alg) < 0) return 0;
-  auto fits = [&](int C) { return (long long)gb_resident_smem(n_cap, m_cap, C, gb_alg) <= (long long)cap; };
+  if (m_cap > 8192 || n_cap > 20000 || cap <= 0 || gb_resident_alg(gb_alg, learned) < 0) return 0;
+  auto fits = [&](int C) {
+    return (long long)gb_resident_smem(n_cap, m_cap, C, gb_alg, learned) <= (long long)cap;
+  };
   if (requested > 0) return (requested <= 16 && fits(requested)) ? requested : 0;
   // four CTAs per trial measured best over the sweep's mix (n = 1024 ... 8192) on GB300
   int C = 4;
@@ -1037,16 +1188,23 @@ int gb_resident_pick_cluster(int n_cap, int m_cap, int requested, int gb_alg) {
 gb_status gb_resident_enqueue(const GbResidentArgs &a, cudaStream_t s) {
   int dev = 0;
   GB_CUDA_TRY(cudaGetDevice(&dev));
-  const int alg = gb_resident_alg(a.alg);
-  const int C = gb_resident_pick_cluster(a.n_cap, a.m_cap, a.cluster, a.alg);
+  const int alg = gb_resident_alg(a.alg, a.ml_params != nullptr);
+  const int C = gb_resident_pick_cluster(a.n_cap, a.m_cap, a.cluster, a.alg, a.ml_params != nullptr);
   if (C <= 0 || alg < 0) {
     gb_set_error_message("resident form: no cluster size fits the trial sizes", __FILE__, __LINE__);
     return GB_BAD_ARG;
   }
   GB_TRY(rs_attrs(false, alg));
   const RsKernel kern = rs_kernel(false, alg);
-  ResEngine &R = g_res[dev * 2 + alg];
-  const size_t smem = gb_resident_smem(a.n_cap, a.m_cap, C, a.alg);
+  ResEngine &R = g_res[dev * 3 + alg];
+  const int learned = a.ml_params != nullptr;
+  // the kernel lays out shared memory for the engine's capacities, which a reused engine can
+  // have above this call's sizes: the launch provides that layout's size, and an engine whose
+  // layout no longer fits is rebuilt for this call
+  const bool reuse = R.dev == dev && R.n_cap >= a.n_cap && R.m_cap >= a.m_cap && R.C == C &&
+                     R.t_cap >= a.count &&
+                     (long long)gb_resident_smem(R.n_cap, R.m_cap, C, a.alg, learned) <= gb_resident_max_smem();
+  const size_t smem = gb_resident_smem(a.n_cap, a.m_cap, C, a.alg, learned);
   cudaLaunchConfig_t cfg;
   memset(&cfg, 0, sizeof(cfg));
   cudaLaunchAttribute attr[1];
@@ -1059,7 +1217,7 @@ gb_status gb_resident_enqueue(const GbResidentArgs &a, cudaStream_t s) {
   cfg.stream = s;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  if (R.dev != dev || R.n_cap < a.n_cap || R.m_cap < a.m_cap || R.C != C || R.t_cap < a.count) {
+  if (!reuse) {
     res_release(R);
     int sms = 0;
     GB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -1116,8 +1274,10 @@ gb_status gb_resident_enqueue(const GbResidentArgs &a, cudaStream_t s) {
   P.yg = nullptr;
   P.xg = nullptr;
   P.st_io = nullptr;
+  P.ml_params = a.ml_params;
+  P.fb = a.fb;
   cfg.gridDim = dim3(R.ncl * C, 1, 1);
-  cfg.dynamicSmemBytes = gb_resident_smem(R.n_cap, R.m_cap, C, a.alg);
+  cfg.dynamicSmemBytes = gb_resident_smem(R.n_cap, R.m_cap, C, a.alg, learned);
   GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, P));
   return GB_OK;
 }
@@ -1135,7 +1295,7 @@ int gb_resident_last_cluster() {
 // least 128 columns each; *used = 0 when the problem does not fit (the graph path solves it).
 gb_status gb_resident_solve_single(GbWork &w, int gb_alg, int num_bins, cudaStream_t s, int *used) {
   *used = 0;
-  const int alg = gb_resident_alg(gb_alg);
+  const int alg = gb_resident_alg(gb_alg, w.ml_params != nullptr);
   if (alg < 0) return GB_OK;
   const GbOp &op = w.op;
   if (op.kind != GB_OP_DENSE || !op.vec4 || (op.m % 4) || op.m > 8192 || op.n > 20000 || w.dyn) return GB_OK;
@@ -1185,8 +1345,21 @@ gb_status gb_resident_solve_single(GbWork &w, int gb_alg, int num_bins, cudaStre
   P.yg = w.y;
   P.xg = w.x;
   P.st_io = w.st;
+  P.ml_params = w.ml_params;
   GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, P));
   *used = 1;
+  return GB_OK;
+}
+
+gb_status gb_resident_check() {
+  int v = 0;
+  GB_CUDA_TRY(cudaMemcpyFromSymbol(&v, g_rs_guard, sizeof(int)));
+  if (v) {
+    const int zero = 0;
+    cudaMemcpyToSymbol(g_rs_guard, &zero, sizeof(int));
+    gb_set_error_message("resident kernel launched with less shared memory than its layout", __FILE__, __LINE__);
+    return GB_CUDA_ERROR;
+  }
   return GB_OK;
 }
 

@@ -27,20 +27,25 @@ struct GbResidentArgs {
   double *bytes;
   int n_cap, m_cap, cluster;
   int alg;  // GB_ALG_NIHT or GB_ALG_CGIHT
+  const float *ml_params;  // CGIHT from the learned warm start (device MLP parameters) or null
+  int *fb;                 // with it: per trial, 1 when the warm start was abandoned
 };
 
 gb_status gb_resident_enqueue(const GbResidentArgs &a, cudaStream_t s);
 // CTAs per cluster the resident form uses for these sizes (0: the sizes do not fit)
-int gb_resident_pick_cluster(int n_cap, int m_cap, int requested, int gb_alg);
+int gb_resident_pick_cluster(int n_cap, int m_cap, int requested, int gb_alg, int learned = 0);
 // shared memory per CTA, and the most a CTA can have
-size_t gb_resident_smem(int n_cap, int m_cap, int C, int gb_alg);
+size_t gb_resident_smem(int n_cap, int m_cap, int C, int gb_alg, int learned = 0);
 int gb_resident_max_smem();
 // cluster size of the last resident launch on this device (0: none)
 int gb_resident_last_cluster();
 // held for the whole of gb_cs_solve_batch (gb_batch.cu): the engines are shared per device
 std::recursive_mutex &gb_batch_mutex();
-// The single-trial drop-in's dense NIHT or CGIHT (state initialised in w.st, y in w.y) on
-// one cluster; x to w.x and the final state to w.st.  *used = 0: not eligible, nothing
+// The single-trial drop-in's dense NIHT or CGIHT (the learned warm start when w.ml_params;
+// state initialised in w.st, y in w.y) on one cluster; x to w.x and the final state to w.st.  *used = 0: not eligible, nothing
 // launched.
 gb_status gb_resident_solve_single(GbWork &w, int gb_alg, int num_bins, cudaStream_t s, int *used);
+// after a synchronisation: GB_CUDA_ERROR if a resident launch found its shared memory smaller
+// than its layout (it then did nothing)
+gb_status gb_resident_check();
 
