@@ -511,7 +511,7 @@ def matvec_roofline(peak, peak_kind, m=14746, n=16384, k=5000, reps=20):
 
 
 def resident_roofline(peak, peak_kind, max_n=8192, sample=0, cluster=0):
-    """The cluster-resident NIHT kernel alone (k_resident_niht, one launch) on the first
+    """The cluster-resident kernel's NIHT instance alone (k_resident, one launch) on the first
     wave's trials with n <= max_n (every one, or `sample` evenly spaced), timed with CUDA
     events around the batched call; algorithmic operator bytes of its iterations per second.
     Trials whose slab of A fits in L2 re-read it from there, so the DRAM traffic can be
@@ -529,10 +529,10 @@ def resident_roofline(peak, peak_kind, max_n=8192, sample=0, cluster=0):
     nbytes, ms = gb.batch_last_stats()
     achieved = nbytes / (ms / 1e3) / 1e9
     out = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-           "kernel": "k_resident_niht", "trials": int(len(n)), "recovered": int(ns), "iterations": int(iters.sum()),
+           "kernel": "k_resident<NIHT>", "trials": int(len(n)), "recovered": int(ns), "iterations": int(iters.sum()),
            "sizes": "n=%s" % sorted(set(n.tolist())), "ms": ms, "algorithmic_bytes": nbytes,
            "cluster": gb._lib.load().gb_cs_batch_last_cluster(), "peak_source": peak_kind}
-    tr = ncu_traffic().get("k_resident_niht")
+    tr = ncu_traffic().get("k_resident<NIHT>")
     if tr and not sample and max_n == 8192:
         out["traffic"] = tr
         out["traffic_source"] = "ncu dram__bytes_read.sum + dram__bytes_write.sum of the same launch " \
