@@ -413,7 +413,7 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
     rn = GB_RESIDENT_N_DEFAULT;
     if (const char *e = getenv("GB_CS_RESIDENT_N")) rn = atoi(e);
   }
-  if (b->alg != GB_ALG_NIHT && b->alg != GB_ALG_CGIHT) rn = -1;
+  if (b->alg != GB_ALG_NIHT && b->alg != GB_ALG_CGIHT && b->alg != GB_ALG_HTP) rn = -1;
   std::vector<char> resident(T, 0);
   int rn_cap = 16, rm_cap = 1, n_res = 0;
   for (int t = 0; t < T; ++t)

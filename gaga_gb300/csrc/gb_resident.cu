@@ -43,7 +43,7 @@ namespace cg = cooperative_groups;
 #define RS_NPUB 16
 
 // algorithms of the resident kernel (RS_CGIHT_ML: CGIHT from the learned warm start)
-enum { RS_NIHT = 0, RS_CGIHT = 1, RS_CGIHT_ML = 2 };
+enum { RS_NIHT = 0, RS_CGIHT = 1, RS_CGIHT_ML = 2, RS_HTP = 3 };
 
 namespace {
 
@@ -116,7 +116,7 @@ __host__ __device__ inline RsLayout rs_layout(int n_cap, int m_cap, int C, int n
   L.o_cnt = rs_take(o, (size_t)L.nb_cap * 4);
   L.o_cntf = rs_take(o, (size_t)L.nb_cap * 4);
   L.o_gscr = rs_take(o, (size_t)RS_THREADS * 16);
-  const size_t cg = alg == RS_CGIHT || alg == RS_CGIHT_ML ? 1 : 0;
+  const size_t cg = alg == RS_CGIHT || alg == RS_CGIHT_ML || alg == RS_HTP ? 1 : 0;
   L.o_gp = rs_take(o, cg * L.nc_cap * 4);      // grad_previous (own columns)
   L.o_gpt = rs_take(o, cg * L.nc_cap * 4);     // grad_prev_thres
   L.o_binsp = rs_take(o, cg * L.nc_cap * 4);   // bins before the last binning
@@ -614,7 +614,8 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
     } else {
     const uint32_t key = P.seed + (P.tid ? P.tid[t] : (uint32_t)t);
     if (tid == 0) {
-      batch_trial_fields(st, t, m, n, P.k[t], P.maxiter, IS_CG ? GB_ALG_CGIHT : GB_ALG_NIHT);
+      batch_trial_fields(st, t, m, n, P.k[t], P.maxiter,
+                         IS_CG ? GB_ALG_CGIHT : ALG == RS_HTP ? GB_ALG_HTP : GB_ALG_NIHT);
       st->lda = lda;
     }
     // ---- draw the trial (k_b_gen_A, k_b_gen_x, key bins, y = A x0 of gb_batch.cu)
@@ -820,10 +821,10 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
         __syncthreads();
       };
       support(false);
-      if (ALG == RS_NIHT && tid == 0) ctrl_phase(st, C_INIT_DONE, 0);
+      if ((ALG == RS_NIHT || ALG == RS_HTP) && tid == 0) ctrl_phase(st, C_INIT_DONE, 0);
       __syncthreads();
       // ---- NIHT iterations (RestrictedSD, GAGA/gaga/functions.cu:659-745, then the support)
-      while (ALG == RS_NIHT && st->active) {
+      while ((ALG == RS_NIHT || ALG == RS_HTP) && st->active) {
         // resid = y - A x_S ; ||resid||^2
         av_own_partial(A, lda, q4, c0, sidx, s_own, x, part, gscr);
         if (tid == 0) ipub[0] = s_own;
@@ -894,7 +895,85 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
         }
         __syncthreads();
         support(false);
-        if (tid == 0) ctrl_phase(st, C_NIHT_STOP, 0);
+        if (ALG == RS_HTP) {
+          // CG projection on the support (GAGA/gaga/algorithms.cu:2588-2669), then up to 15
+          // RestrictedCG steps (functions.cu:922-1000), as enq_body / enq_cg_body run them
+          auto av_rows = [&](const float *v, bool sub_y, float *rows, float *full, int slot) {
+            av_own_partial(A, lda, q4, c0, sidx, s_own, v, part, gscr);
+            cl.sync();
+            const float s2 = reduce_rows(cl, C, part, rr0, rr1, sub_y ? ypart : nullptr, rows, nullptr);
+            const float b = block_reduce<0>(s2, red32);
+            if (tid == 0 && slot >= 0) pub[slot] = b;
+            cl.sync();
+            if (full) gather_rows(cl, C, q4, RB, rows, full);
+          };
+          av_rows(x, true, rowp, r, R_RES);  // resid = y - A x_S
+          if (tid == 0) st->red[R_RES] = combine_sum(cl, C, pub, R_RES);
+          __syncthreads();
+          at_own<DEEP>(A, lda, q4, c0, nc, r, grad);  // grad = (A^T resid) on the support; gp = grad
+          __syncthreads();
+          {
+            const int kb = st->k_bin;
+            float s2 = 0.0f;
+            for (int c = tid; c < nc; c += RS_THREADS) {
+              const float g = bins[c] > kb ? 0.0f : grad[c];
+              grad[c] = g;
+              gp[c] = g;
+              s2 = fmaf(g, g, s2);
+            }
+            const float b = block_reduce<0>(s2, red32);
+            if (tid == 0) pub[R_DOT1] = b;
+          }
+          cl.sync();
+          if (tid == 0) {
+            st->red[R_DOT1] = combine_sum(cl, C, pub, R_DOT1);
+            ctrl_phase(st, C_HTP_CGINIT, 0);
+          }
+          __syncthreads();
+          while (st->flags[F_CG] && st->active) {
+            av_rows(grad, false, rowp, r, R_CG);  // resid = A grad_S
+            if (tid == 0) {
+              st->red[R_CG] = combine_sum(cl, C, pub, R_CG);
+              ctrl_phase(st, C_HTP_CG1, 0);
+            }
+            __syncthreads();
+            const float alpha = st->cg_alpha;
+            for (int c = tid; c < nc; c += RS_THREADS) x[c] = fmaf(alpha, grad[c], x[c]);
+            at_own<DEEP>(A, lda, q4, c0, nc, r, gpt);  // x_thres = (A^T A grad_S) on the support
+            __syncthreads();
+            {
+              const int kb = st->k_bin;
+              float s3 = 0.0f;
+              for (int c = tid; c < nc; c += RS_THREADS) {
+                const float xtv = bins[c] > kb ? 0.0f : gpt[c];
+                const float o = fmaf(-alpha, xtv, gp[c]);
+                gp[c] = o;
+                s3 = fmaf(o, o, s3);
+              }
+              const float b = block_reduce<0>(s3, red32);
+              if (tid == 0) pub[R_DOT3] = b;
+            }
+            cl.sync();
+            if (tid == 0) {
+              st->red[R_DOT3] = combine_sum(cl, C, pub, R_DOT3);
+              ctrl_phase(st, C_HTP_CG2, 0);
+            }
+            __syncthreads();
+            {
+              const float beta = st->cg_beta;
+              for (int c = tid; c < nc; c += RS_THREADS) grad[c] = fmaf(1.0f, gp[c], beta * grad[c]);
+            }
+            av_rows(x, true, rowa, nullptr, R_RES);  // ||y - A x_S||^2
+            if (tid == 0) {
+              st->red[R_RES] = combine_sum(cl, C, pub, R_RES);
+              ctrl_phase(st, C_HTP_CG3, 0);
+            }
+            __syncthreads();
+          }
+          if (tid == 0) ctrl_phase(st, C_HTP_STOP, 0);
+        } else {
+          if (tid == 0) ctrl_phase(st, C_NIHT_STOP, 0);
+        }
         __syncthreads();
       }
       if (IS_CG) {
@@ -1133,11 +1212,15 @@ using RsKernel = void (*)(const RsParams);
 RsKernel rs_kernel(bool deep, int alg) {
   if (deep)
     return alg == RS_CGIHT_ML ? k_resident<true, RS_CGIHT_ML>
-                              : alg == RS_CGIHT ? k_resident<true, RS_CGIHT> : k_resident<true, RS_NIHT>;
+           : alg == RS_CGIHT  ? k_resident<true, RS_CGIHT>
+           : alg == RS_HTP    ? k_resident<true, RS_HTP>
+                              : k_resident<true, RS_NIHT>;
   return alg == RS_CGIHT_ML ? k_resident<false, RS_CGIHT_ML>
-                            : alg == RS_CGIHT ? k_resident<false, RS_CGIHT> : k_resident<false, RS_NIHT>;
+         : alg == RS_CGIHT  ? k_resident<false, RS_CGIHT>
+         : alg == RS_HTP    ? k_resident<false, RS_HTP>
+                            : k_resident<false, RS_NIHT>;
 }
-std::atomic<unsigned long long> g_attr_done[6];
+std::atomic<unsigned long long> g_attr_done[8];
 
 }  // namespace
 
@@ -1145,7 +1228,7 @@ int gb_resident_max_smem();
 
 static gb_status rs_attrs(bool deep, int alg) {
   const int cap = gb_resident_max_smem();
-  return gb_once_per_device(g_attr_done[(deep ? 3 : 0) + alg], [&]() -> gb_status {
+  return gb_once_per_device(g_attr_done[(deep ? 4 : 0) + alg], [&]() -> gb_status {
     const void *fn = (const void *)rs_kernel(deep, alg);
     GB_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
     GB_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
@@ -1156,7 +1239,8 @@ static gb_status rs_attrs(bool deep, int alg) {
 // the resident algorithm of a library algorithm id (learned: CGIHT from the warm start)
 int gb_resident_alg(int gb_alg, int learned) {
   if (gb_alg == GB_ALG_CGIHT) return learned ? RS_CGIHT_ML : RS_CGIHT;
-  return gb_alg == GB_ALG_NIHT && !learned ? RS_NIHT : -1;
+  if (learned) return -1;
+  return gb_alg == GB_ALG_NIHT ? RS_NIHT : gb_alg == GB_ALG_HTP ? RS_HTP : -1;
 }
 
 int gb_resident_max_smem() {
@@ -1196,7 +1280,7 @@ gb_status gb_resident_enqueue(const GbResidentArgs &a, cudaStream_t s) {
   }
   GB_TRY(rs_attrs(false, alg));
   const RsKernel kern = rs_kernel(false, alg);
-  ResEngine &R = g_res[dev * 3 + alg];
+  ResEngine &R = g_res[dev * 4 + alg];
   const int learned = a.ml_params != nullptr;
   // the kernel lays out shared memory for the engine's capacities, which a reused engine can
   // have above this call's sizes: the launch provides that layout's size, and an engine whose

@@ -1735,12 +1735,12 @@ gb_status gb_run_solver(GbWork &w, int alg, const gb_options &o, int k, cudaStre
   if (o.timing && (alg == GB_ALG_NIHT || alg == GB_ALG_HTP)) P.supp_flag = o.support_flag;
   static const bool eager = getenv("GB_CS_EAGER") && atoi(getenv("GB_CS_EAGER")) != 0;
   if (eager) return run_eager(P, s);
-  // dense NIHT or CGIHT (plain or learned start): one thread-block cluster runs the whole
-  // solve (gb_resident.cu), without a kernel launch per step
+  // dense NIHT, HTP or CGIHT (plain or learned start): one thread-block cluster runs the
+  // whole solve (gb_resident.cu), without a kernel launch per step
   static const bool no_resident = getenv("GB_CS_SINGLE_RESIDENT") && atoi(getenv("GB_CS_SINGLE_RESIDENT")) == 0;
-  // (timing on selects NIHT's timing variant; CGIHT ignores it, gaga_gen.cu:331-334)
-  if (!no_resident && (alg == GB_ALG_NIHT || alg == GB_ALG_CGIHT) && !(o.timing && alg == GB_ALG_NIHT) &&
-      !w.tstamp) {
+  // (timing on selects NIHT's and HTP's timing variants; CGIHT ignores it, gaga_gen.cu:331-334)
+  if (!no_resident && (alg == GB_ALG_NIHT || alg == GB_ALG_CGIHT || alg == GB_ALG_HTP) &&
+      !(o.timing && (alg == GB_ALG_NIHT || alg == GB_ALG_HTP)) && !w.tstamp) {
     int used = 0;
     GB_TRY(gb_resident_solve_single(w, alg, o.num_bins, s, &used));
     if (used) return GB_OK;

@@ -134,10 +134,10 @@ def _dense(gbo, n, m, k, seed):
     return A, x0, ks, op, gbo.A(op, x0)
 
 
-@pytest.mark.parametrize("alg,restart", [("NIHT", "off"), ("CGIHT", "off"), ("CGIHT", "on")])
+@pytest.mark.parametrize("alg,restart", [("NIHT", "off"), ("HTP", "off"), ("CGIHT", "off"), ("CGIHT", "on")])
 @pytest.mark.parametrize("n,m,k", [(1024, 400, 40), (2048, 1024, 200), (4096, 1024, 102), (3000, 1200, 330)])
 def test_single_trial_on_one_cluster_matches_oracle(gb, gbo, alg, restart, n, m, k):
-    """The drop-in's dense NIHT / CGIHT (restartFlag off and on), which runs on one cluster at
+    """The drop-in's dense NIHT / HTP / CGIHT (restartFlag off and on), which runs on one cluster at
     these sizes: same verdict as the oracle's solve of the same problem; when recovered, x
     within 1e-4, the same support and iterations within 3."""
     A, x0, ks, op, y = _dense(gbo, n, m, k, seed=n + m + k)
@@ -153,13 +153,14 @@ def test_single_trial_on_one_cluster_matches_oracle(gb, gbo, alg, restart, n, m,
         assert abs(int(iters) - int(info.iter)) <= 3
 
 
-def test_batched_cgiht_resident_matches_slots(gb):
-    """Batched CGIHT: the resident kernel against the slot graphs on the same trials
+@pytest.mark.parametrize("alg", ["CGIHT", "HTP"])
+def test_batched_resident_matches_slots(gb, alg):
+    """Batched CGIHT and HTP: the resident kernel against the slot graphs on the same trials
     (n = 1024 ... 8192), verdicts agreeing on all but at most one, repeat runs bit-identical."""
     n, m, k, tid = pick([1024, 2048, 4096, 8192], 40)
-    res = gb.solve_batch(n, m, k, SEED, tid, alg="CGIHT", maxiter=800, resident_n=8192)
-    again = gb.solve_batch(n, m, k, SEED, tid, alg="CGIHT", maxiter=800, resident_n=8192)
-    slots = gb.solve_batch(n, m, k, SEED, tid, alg="CGIHT", maxiter=800, resident_n=-1)
+    res = gb.solve_batch(n, m, k, SEED, tid, alg=alg, maxiter=800, resident_n=8192)
+    again = gb.solve_batch(n, m, k, SEED, tid, alg=alg, maxiter=800, resident_n=8192)
+    slots = gb.solve_batch(n, m, k, SEED, tid, alg=alg, maxiter=800, resident_n=-1)
     assert np.array_equal(res[1], again[1]) and np.array_equal(res[2], again[2])
     assert np.sum(res[3] == slots[3]) >= len(n) - 1, (res[3], slots[3])
     both = (res[3] == 1) & (slots[3] == 1)
@@ -167,10 +168,11 @@ def test_batched_cgiht_resident_matches_slots(gb):
     assert 0 < res[0] < len(n)
 
 
+@pytest.mark.parametrize("alg", ["CGIHT", "HTP"])
 @pytest.mark.parametrize("cluster", [1, 4])
-def test_batched_cgiht_resident_matches_oracle(gb, gbo, cluster):
+def test_batched_resident_matches_oracle(gb, gbo, alg, cluster):
     n, m, k, tid = pick([1024, 2048], 8)
-    ns, iters, err, ok = gb.solve_batch(n, m, k, SEED, tid, alg="CGIHT", maxiter=1000, resident_n=4096,
+    ns, iters, err, ok = gb.solve_batch(n, m, k, SEED, tid, alg=alg, maxiter=1000, resident_n=4096,
                                         cluster=cluster)
-    ok_o, it_o, err_o = gbo.solve_dense_trials(n, m, k, SEED, tid, alg="CGIHT", tol_rel=1e-4, maxiter=1000)
+    ok_o, it_o, err_o = gbo.solve_dense_trials(n, m, k, SEED, tid, alg=alg, tol_rel=1e-4, maxiter=1000)
     assert np.sum((err_o <= 1e-3) == ok.astype(bool)) >= len(n) - 1
