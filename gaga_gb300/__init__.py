@@ -297,7 +297,7 @@ def solve_batch(n, m, k, seed, trial_ids=None, alg="NIHT", tol_rel=1e-4, maxiter
     """Batched multi-trial dense form (gb_cs_solve_batch); learned_params (a CUDA tensor of
     MLP parameters, CGIHT only) turns on the learned warm start; slots / sm_share set the
     schedule of the slot graphs (0: automatic; gaga_gb300.autotune picks them by
-    measurement); NIHT trials with n <= resident_n (0: 8192, < 0: none) are solved by the
+    measurement); trials with n <= resident_n (0: 8192, < 0: none) are solved by the
     cluster-resident kernel with `cluster` CTAs per trial (0: 4, or more when the sizes need
     it)."""
     L = _lib.load()

@@ -225,8 +225,9 @@ gb_status gb_cs_l0_step(float *d_res, float *d_x, float *d_updates, const int *d
 /* ---- batched form (no reference counterpart: the reference solves one trial per call) ----
  * Thousands of independent dense Gaussian trials, each with its own (n, m, k) and its own
  * problem drawn on the device exactly as gb_cs_generate_and_solve draws it with seed
- * `seed + trial_id` (Gaussian A, +-1 signal), solved by NIHT in one persistent launch per
- * size class (n <= 20000).  Per-trial outputs (host or device arrays of ntrials entries, any may be NULL):
+ * `seed + trial_id` (Gaussian A, +-1 signal), solved by NIHT, HTP or CGIHT: trials with
+ * n <= resident_n by one thread-block cluster each in one persistent launch, the others by
+ * slot graphs over a device trial queue, both at once.  Per-trial outputs (host or device arrays of ntrials entries, any may be NULL):
  * iterations, relative l2 error against the generated x, and a verdict flag
  * (rel l2 <= 1e-3).  tol_rel is relative to ||y||. */
 typedef struct {
@@ -243,7 +244,7 @@ typedef struct {
   int slots;                     /* schedule: concurrent trial slots (0: 16, fewer if memory is short) */
   int sm_share;                  /* schedule: SMs each slot's kernels are shaped for (0: half the GPU) */
   void *stream;
-  int resident_n;                /* NIHT: trials with n <= resident_n are solved by the cluster-resident
+  int resident_n;                /* trials with n <= resident_n are solved by the cluster-resident
                                     kernel, one thread-block cluster per trial, while the slots take
                                     the others (0: 8192; < 0: slots only) */
   int cluster;                   /* CTAs per cluster of the resident kernel (0: 4, more if the
