@@ -235,7 +235,7 @@ typedef struct {
   const int *n, *m, *k;          /* host arrays */
   const unsigned int *trial_id;  /* host array (NULL: 0..ntrials-1) */
   unsigned int seed;
-  int alg;                       /* GB_ALG_NIHT or GB_ALG_CGIHT */
+  int alg;                       /* GB_ALG_NIHT, GB_ALG_HTP or GB_ALG_CGIHT */
   float tol_rel;
   int maxiter;
   int use_learned;               /* CGIHT only: learned warm start, falling back to a plain
