@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "gb_internal.cuh"
@@ -513,17 +514,62 @@ float h_gauss(uint32_t seed, uint32_t trial, uint32_t stream, uint64_t e) {
   return (float)((lane & 1) ? r * sin(t) : r * cos(t));
 }
 
+#define GB_HOST_THREADS 16
+// f(begin, end, part) over [0, count) split into at most GB_HOST_THREADS parts run on the
+// host's cores (one part for small counts); part p only writes its own range and slot p
+template <class F>
+void host_parallel_for(int64_t count, F f) {
+  const unsigned hw = std::max(1u, std::min((unsigned)GB_HOST_THREADS, std::thread::hardware_concurrency()));
+  if (count < (1 << 15) || hw == 1) {
+    f((int64_t)0, count, 0);
+    return;
+  }
+  const int64_t chunk = (count + hw - 1) / hw;
+  std::vector<std::thread> th;
+  for (unsigned t = 0; t < hw; ++t) {
+    const int64_t a = t * chunk, b = std::min<int64_t>(count, a + chunk);
+    if (a < b) th.emplace_back(f, a, b, (int)t);
+  }
+  for (auto &x : th) x.join();
+}
+
 // createVector (GAGA/gaga/createVector.cu:207-300): the support is the set of entries whose
-// uniform key falls in the top bins of an n-bin linear histogram, so |support| >= k
+// uniform key falls in the top bins of an n-bin linear histogram, so |support| >= k.  One
+// Philox block gives four consecutive entries (the values h_uniform / h_gauss return).
 int gen_vector(int n, int k, int dist, uint32_t seed, uint32_t trial, float *x) {
   std::vector<float> keys(n), vals(n);
+  const int64_t nblk = ((int64_t)n + 3) / 4;
+  std::vector<float> part_max(GB_HOST_THREADS, 0.0f);
+  host_parallel_for(nblk, [&](int64_t g0, int64_t g1, int part) {
+    float mloc = 0.0f;
+    for (int64_t g = g0; g < g1; ++g) {
+      uint32_t ov[4], os[4];
+      philox((uint32_t)g, (uint32_t)(g >> 32), ST_VALUES, trial, seed, KEY_HI, ov);
+      philox((uint32_t)g, (uint32_t)(g >> 32), ST_SUPPORT, trial, seed, KEY_HI, os);
+      for (int lane = 0; lane < 4; ++lane) {
+        const int64_t i = g * 4 + lane;
+        if (i >= n) break;
+        const float u = u01(ov[lane]);
+        float v;
+        if (dist == 1) {
+          v = signbit(u - 0.5f) ? -1.0f : 1.0f;
+        } else if (dist == 2) {
+          const uint32_t a = lane < 2 ? ov[0] : ov[2], b = lane < 2 ? ov[1] : ov[3];
+          const double r = sqrt(-2.0 * log((double)u01(a)));
+          const double t = 6.283185307179586 * u01(b);
+          v = (float)((lane & 1) ? r * sin(t) : r * cos(t));
+        } else {
+          v = u;
+        }
+        vals[i] = v;
+        keys[i] = u01(os[lane]);
+        mloc = std::max(mloc, keys[i]);
+      }
+    }
+    part_max[part] = mloc;
+  });
   float mx = 0.0f;
-  for (int i = 0; i < n; ++i) {
-    float u = h_uniform(seed, trial, ST_VALUES, i);
-    vals[i] = dist == 1 ? (signbit(u - 0.5f) ? -1.0f : 1.0f) : dist == 2 ? h_gauss(seed, trial, ST_VALUES, i) : u;
-    keys[i] = h_uniform(seed, trial, ST_SUPPORT, i);
-    mx = std::max(mx, keys[i]);
-  }
+  for (float v : part_max) mx = std::max(mx, v);
   const float slope = ((float)(n - 1) / mx);
   const double small = (double)mx * 0.000001;
   std::vector<int> bins(n), cnt(n, 0);
@@ -597,8 +643,22 @@ extern "C" gb_status gb_cs_generate_and_solve(const char *alg, int kind, int k, 
     // m of n rows by the reference's partial shuffle (createProblem_kernels.cu:65-75)
     std::vector<int> idx(n);
     for (int i = 0; i < n; ++i) idx[i] = i;
+    // the swaps are sequential, their uniforms are not: one Philox block per four j
+    std::vector<float> uj(n, 0.0f);
+    const int64_t jlo = n - m + 1;  // j runs n-1 .. n-m+1
+    host_parallel_for(((int64_t)n + 3) / 4 - jlo / 4, [&](int64_t a, int64_t b, int) {
+      for (int64_t gi = a; gi < b; ++gi) {
+        const int64_t g = jlo / 4 + gi;
+        uint32_t o[4];
+        philox((uint32_t)g, (uint32_t)(g >> 32), ST_ROWS, 0, seed, KEY_HI, o);
+        for (int lane = 0; lane < 4; ++lane) {
+          const int64_t j = g * 4 + lane;
+          if (j >= jlo && j < n) uj[j] = u01(o[lane]);
+        }
+      }
+    });
     for (int j = n - 1; j > n - m; --j) {
-      int kk = (int)((float)j * h_uniform(seed, 0, ST_ROWS, j));
+      int kk = (int)((float)j * uj[j]);
       std::swap(idx[j], idx[kk]);
     }
     rows.resize(m);
@@ -610,7 +670,8 @@ extern "C" gb_status gb_cs_generate_and_solve(const char *alg, int kind, int k, 
     rows.resize((size_t)n * d);
     vals.resize((size_t)n * d);
     float scale = (ens == 1 || ens == 2) ? 1.0f / sqrtf((float)d) : 1.0f;
-    for (int j = 0; j < n; ++j) {
+    host_parallel_for(n, [&](int64_t j0, int64_t j1, int) {
+    for (int j = (int)j0; j < (int)j1; ++j) {
       int have = 0;
       uint32_t draw = 0;
       while (have < d) {
@@ -630,6 +691,7 @@ extern "C" gb_status gb_cs_generate_and_solve(const char *alg, int kind, int k, 
         vals[(size_t)j * d + t] = v * scale;
       }
     }
+    });
     p.rows = rows.data();
     p.vals = vals.data();
     p.d = d;
