@@ -532,9 +532,10 @@ def resident_roofline(peak, peak_kind, max_n=8192, sample=0, cluster=0):
            "kernel": "k_resident<NIHT>", "trials": int(len(n)), "recovered": int(ns), "iterations": int(iters.sum()),
            "sizes": "n=%s" % sorted(set(n.tolist())), "ms": ms, "algorithmic_bytes": nbytes,
            "cluster": gb._lib.load().gb_cs_batch_last_cluster(), "peak_source": peak_kind}
-    tr = ncu_traffic().get("k_resident<NIHT>")
-    if tr and not sample and max_n == 8192:
-        out["traffic"] = tr
+    tr = ncu_traffic().get("k_resident<NIHT> sweep wave 0, 655 trials n=1024..8192, 4 CTAs per cluster")
+    if tr and not sample and max_n == 8192 and out["cluster"] == 4:
+        out["traffic"] = tr["read"] + tr["write"]
+        out["traffic_unit"] = "bytes"
         out["traffic_source"] = "ncu dram__bytes_read.sum + dram__bytes_write.sum of the same launch " \
                                 "(profiles/dram_traffic.json)"
     return out
