@@ -1,13 +1,16 @@
-// gb_resident.cu -- cluster-resident NIHT: the batched form's small trials, one
-// thread-block cluster per trial and one persistent launch for all of them.
+// gb_resident.cu -- the cluster-resident solver: one thread-block cluster per trial, whole
+// solves inside one persistent launch, for the batched form's trials with n <= 8192 and for
+// the drop-in's small dense solves.
 //
-// The slot graphs of gb_batch.cu run about a dozen kernels per NIHT iteration; for trials
-// of a few MB that is bound by kernel dispatch, not by HBM.  Here each trial is solved
-// start to finish by one cluster of C CTAs (one CTA per SM):
+// The slot graphs of gb_batch.cu and the single-trial graph run about a dozen kernels per
+// iteration; for problems of a few MB that is bound by kernel dispatch, not by HBM.  Here
+// each trial is solved start to finish by one cluster of C CTAs (one CTA per SM):
 //
-//   * CTA r owns a contiguous range of columns: its slab of A (generated in place, rows
-//     padded with zeros to lda = roundup(m, 32)) and its entries of x, grad, bins and x0,
-//     which live in shared memory.  Every CTA keeps the whole residual (m floats).
+//   * CTA r owns a contiguous range of columns: its slab of A (generated in place for the
+//     batched trials, rows padded with zeros to lda = roundup(m, 32); the caller's A for a
+//     single solve) and its entries of x, grad, bins and x0 (CGIHT and HTP: also
+//     grad_previous, its restriction and the previous bins), which live in shared memory.
+//     Every CTA keeps the whole residual (m floats).
 //   * A^T r: each CTA over its own columns (lane groups per column, float4 streams).
 //   * A v_S: each CTA over its own support columns into a partial m-vector; the partials
 //     are summed in rank order through distributed shared memory, each CTA summing its
@@ -18,9 +21,11 @@
 //     integers, so every copy holds the same bits and every CTA takes the same branches
 //     (and so meets the same cluster barriers).
 //
-// The solve is NIHT_S_gen (GAGA/gaga/algorithms.cu:1296-1421) with the same steps and
-// control as the graph path (enq_prologue / enq_body in gb_solver.cu); only the order of
-// floating-point sums differs.  The problem is the one gb_cs_generate_and_solve draws with
+// The algorithms (a template parameter, one kernel instance each) are NIHT_S_gen, HTP_S_gen
+// and CGIHT_S_gen (GAGA/gaga/algorithms.cu:1274-1441, 2491-2716, 3689-3942), and CGIHT from
+// the learned warm start (gb_learned.cu), with the same steps and control as the graph path
+// (enq_prologue / enq_body / enq_cg_body in gb_solver.cu); only the order of floating-point
+// sums differs.  A batched trial is the problem gb_cs_generate_and_solve draws with
 // seed + trial id (Gaussian A, +-1 signal on the createVector support).
 #include <cooperative_groups.h>
 #include <stdlib.h>
