@@ -2,12 +2,20 @@
 //
 //     Ct[N x M] = [Y -] (A[M x K] . B[N x K]^T)^T        A, B BF16, K-major; FP32 accumulate
 //
-// One CTA computes a 128 x 256 tile of C (M x N) with the accumulator in tensor memory:
-//   warp 0      TMA producer: 128B-swizzled 128 x 64 (A) and 256 x 64 (B) boxes into a
-//               4-stage shared-memory ring, completion counted on a per-stage mbarrier
-//   warp 1      allocates 256 TMEM columns; one elected lane issues tcgen05.mma
-//               (kind::f16, M = 128, N = 256, K = 16 per instruction, 4 per stage) and
-//               frees each stage with tcgen05.commit
+// Two instances of one kernel, each CTA holding a 128 x 256 tile of C (M x N) in tensor memory:
+//   pair (M % 256 == 0, the default): a cluster of two CTAs computes a 256 x 256 tile with
+//               tcgen05.mma.cta_group::2 (M = 256, N = 256, K = 16).  Each CTA stages its
+//               own 128 rows of A and one half (128 rows) of the B tile, 32 KB per k-block,
+//               in a 7-stage ring; both CTAs' copies complete on the even CTA's stage
+//               barrier, the even CTA issues the MMAs and its commits arrive on both CTAs'
+//               barriers (multicast).  Per k-block an SM receives 32 KB instead of 48 KB.
+//   single:     one CTA, tcgen05.mma.cta_group::1 (M = 128, N = 256), 128 x 64 (A) and
+//               256 x 64 (B) boxes in a 4-stage ring of 48 KB stages.
+// Roles in each CTA:
+//   warp 0      TMA producer: 128B-swizzled boxes into the ring, completion counted on a
+//               per-stage mbarrier (expect_tx by the issuing CTA of the MMAs)
+//   warp 1      allocates 256 TMEM columns; one elected lane issues the MMAs (4 per stage)
+//               and frees each stage with tcgen05.commit
 //   warps 2-5   epilogue: tcgen05.ld of their TMEM lane quarter (32 rows each), FP32
 //               [Y -] epilogue, optional BF16 / split-BF16 copies, or a split-K partial
 // Every mbarrier wait is bounded by the global timer; on a timeout the CTA records an
@@ -20,20 +28,29 @@
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
+#include <cstdlib>
 #include <mutex>
 
 #include "gb_internal.cuh"
 
-#define TC_BM 128
-#define TC_BN 256
-#define TC_BK 64  // 64 BF16 = 128 bytes = one swizzle row
-#define TC_STAGES 4
-#define TC_THREADS 192
+#define TC_BM 128  // rows of C per CTA
+#define TC_BN 256  // columns of C per tile
+#define TC_BK 64   // 64 BF16 = 128 bytes = one swizzle row
+#define TC_THREADS 192  // producer, MMA issuer, four epilogue warps
+#define TC_EPI_THREADS 128
 #define TC_A_BYTES (TC_BM * TC_BK * 2)
-#define TC_B_BYTES (TC_BN * TC_BK * 2)
-#define TC_STAGE_BYTES (TC_A_BYTES + TC_B_BYTES)
-#define TC_SMEM (TC_STAGES * TC_STAGE_BYTES + 1024)
 #define TC_TMEM_COLS 256
+
+// ring geometry of the two instances (PAIR: B rows per CTA are half the tile's columns)
+template <int PAIR>
+struct TcCfg {
+  static constexpr int B_ROWS = PAIR ? TC_BN / 2 : TC_BN;
+  static constexpr int STAGES = PAIR ? 7 : 4;
+  static constexpr int B_BYTES = B_ROWS * TC_BK * 2;
+  static constexpr int STAGE_BYTES = TC_A_BYTES + B_BYTES;
+  static constexpr int SMEM = STAGES * STAGE_BYTES + 1024;
+};
+static_assert(TcCfg<1>::SMEM <= 230400, "pair ring must fit 227 KB with the static barriers");
 #define TC_WAIT_NS 4000000000ull  // 4 s: far beyond any wait of a correct launch
 
 __device__ int g_tc_error = 0;  // first failure code of any tcgen05 GEMM launch
@@ -94,6 +111,34 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, u
       : "memory");
 }
 
+// The pair form: the box lands in this CTA's shared memory, its bytes complete on the mbarrier
+// at cluster address bar_cluster (the even CTA's stage barrier)
+__device__ __forceinline__ void tma_load_2d_pair(void *dst, const CUtensorMap *map, uint32_t bar_cluster, int x,
+                                                 int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.cta_group::2 [%0], [%1, {%3, "
+      "%4}], [%2];" ::"r"(smem_u32(dst)),
+      "l"((uint64_t)map), "r"(bar_cluster), "r"(x), "r"(y)
+      : "memory");
+}
+
+// shared::cluster address of the same shared-memory location in cluster CTA `rank`
+__device__ __forceinline__ uint32_t cluster_addr(const void *p, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
+  return r;
+}
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
 // Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, 8-row groups 1024 B
 // apart (the layout the TMA boxes above produce).
 __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
@@ -106,22 +151,70 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
   return d;
 }
 
-// Instruction descriptor, kind::f16: D FP32, A and B BF16, both K-major, N = 256, M = 128
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TC_BN >> 3) << 17) |
-                            ((uint32_t)(TC_BM >> 4) << 24);
-
-__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
-      "l"(da), "l"(db), "r"(kIdesc), "r"(accumulate)
-      : "memory");
+// Instruction descriptor, kind::f16: D FP32, A and B BF16, both K-major, N = 256, M = 128 per
+// CTA (256 for the pair)
+template <int PAIR>
+__host__ __device__ constexpr uint32_t tc_idesc() {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TC_BN >> 3) << 17) |
+         ((uint32_t)((TC_BM << PAIR) >> 4) << 24);
 }
 
+template <int PAIR>
+__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t accumulate) {
+  if constexpr (PAIR) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "l"(da), "l"(db), "r"(tc_idesc<1>()), "r"(accumulate)
+        : "memory");
+  } else {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "l"(da), "l"(db), "r"(tc_idesc<0>()), "r"(accumulate)
+        : "memory");
+  }
+}
+
+// arrive on `bar` once the MMAs issued so far complete; the pair form arrives on the barrier at
+// the same offset in both CTAs
+template <int PAIR>
 __device__ __forceinline__ void umma_commit(uint64_t *bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-               : "memory");
+  if constexpr (PAIR) {
+    asm volatile(
+        "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+            smem_u32(bar)),
+        "h"((uint16_t)3)
+        : "memory");
+  } else {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+  }
+}
+
+template <int PAIR>
+__device__ __forceinline__ void tmem_alloc(uint32_t *dst) {
+  if constexpr (PAIR) {
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)),
+                 "r"(TC_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+  } else {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)),
+                 "r"(TC_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+}
+
+template <int PAIR>
+__device__ __forceinline__ void tmem_dealloc(uint32_t tmem) {
+  if constexpr (PAIR)
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+  else
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
 }
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
@@ -144,7 +237,7 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
   for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
 }
 
-__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, %0;" ::"n"(TC_EPI_THREADS) : "memory"); }
 
 struct TcArgs {
   float *Ct;
@@ -157,10 +250,13 @@ struct TcArgs {
   GbGemmWs ws;
 };
 
+template <int PAIR>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_gemm_tn_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcArgs a) {
+  using Cfg = TcCfg<PAIR>;
+  constexpr int STAGES = Cfg::STAGES;
   extern __shared__ uint8_t tc_smem_raw[];
-  __shared__ __align__(8) uint64_t full_bar[TC_STAGES], empty_bar[TC_STAGES], accum_bar;
+  __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES], accum_bar;
   __shared__ uint32_t tmem_base_sh;
   __shared__ int abort_sh, last_sh;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -169,7 +265,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const int m0 = mt * TC_BM, n0 = nti * TC_BN;
   const int nkb = a.K / TC_BK;
   const int cnt = a.ncount ? *a.ncount : a.N;
+  // the pair's two CTAs share blockIdx.y, so they return (or not) together here and below
   if (n0 >= cnt) return;
+  const uint32_t rank = PAIR ? cluster_rank() : 0u;  // 0: this CTA issues the MMAs
   int S = 1;
   if (a.s_max > 1) {
     const int tiles = mtiles * ((cnt + TC_BN - 1) / TC_BN);
@@ -182,7 +280,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
   uint8_t *smem = (uint8_t *)(((uintptr_t)tc_smem_raw + 1023) & ~(uintptr_t)1023);
   if (threadIdx.x == 0) {
-    for (int s = 0; s < TC_STAGES; ++s) {
+    for (int s = 0; s < STAGES; ++s) {
       mbar_init(&full_bar[s], 1);
       mbar_init(&empty_bar[s], 1);
     }
@@ -190,14 +288,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     abort_sh = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_sh)),
-                 "r"(TC_TMEM_COLS)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-  }
+  if (warp == 1) tmem_alloc<PAIR>(&tmem_base_sh);
   tc_fence_before();
-  __syncthreads();
+  // the pair: the odd CTA's copies complete on the even CTA's barriers, initialised above
+  if constexpr (PAIR)
+    cluster_sync_all();
+  else
+    __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_base_sh;
   volatile int *abort_flag = &abort_sh;
@@ -206,43 +303,58 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // ---------------------------------------------------------------- TMA producer
     if (lane == 0) {
       int issued = 0;
+      const int b_row = n0 + (int)rank * Cfg::B_ROWS;  // the pair: B rows of this CTA's half
       for (int it = 0; it < nk; ++it) {
-        const int s = it % TC_STAGES;
-        const uint32_t ph = (uint32_t)(it / TC_STAGES) & 1u;
-        if (it >= TC_STAGES && !mbar_wait(&empty_bar[s], ph ^ 1u, abort_flag, 1)) break;
-        uint8_t *sa = smem + s * TC_STAGE_BYTES;
-        mbar_expect_tx(&full_bar[s], TC_STAGE_BYTES);
+        const int s = it % STAGES;
+        const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+        if (it >= STAGES && !mbar_wait(&empty_bar[s], ph ^ 1u, abort_flag, 1)) break;
+        uint8_t *sa = smem + s * Cfg::STAGE_BYTES;
         const int kx = (kb0 + it) * TC_BK;
-        tma_load_2d(sa, &tmA, &full_bar[s], kx, m0);
-        tma_load_2d(sa + TC_A_BYTES, &tmB, &full_bar[s], kx, n0);
+        if constexpr (PAIR) {
+          if (rank == 0) mbar_expect_tx(&full_bar[s], 2 * Cfg::STAGE_BYTES);
+          const uint32_t bar0 = cluster_addr(&full_bar[s], 0);
+          tma_load_2d_pair(sa, &tmA, bar0, kx, m0);
+          tma_load_2d_pair(sa + TC_A_BYTES, &tmB, bar0, kx, b_row);
+        } else {
+          mbar_expect_tx(&full_bar[s], Cfg::STAGE_BYTES);
+          tma_load_2d(sa, &tmA, &full_bar[s], kx, m0);
+          tma_load_2d(sa + TC_A_BYTES, &tmB, &full_bar[s], kx, b_row);
+        }
         issued = it + 1;
       }
-      // on an abort, wait (bounded) for the copies still in flight into the ring
+      // on an abort, wait (bounded) for the copies still in flight into the ring; the odd CTA
+      // of a pair has no barrier of its own for them and waits a fixed 1 ms instead
       if (*abort_flag) {
-        for (int it = max(0, issued - TC_STAGES); it < issued; ++it) {
+        if (PAIR && rank != 0) {
           const uint64_t t0 = global_ns();
-          while (!mbar_test(&full_bar[it % TC_STAGES], (uint32_t)(it / TC_STAGES) & 1u) &&
-                 global_ns() - t0 < TC_WAIT_NS) {
+          while (global_ns() - t0 < 1000000ull) {
+          }
+        } else {
+          for (int it = max(0, issued - STAGES); it < issued; ++it) {
+            const uint64_t t0 = global_ns();
+            while (!mbar_test(&full_bar[it % STAGES], (uint32_t)(it / STAGES) & 1u) && global_ns() - t0 < TC_WAIT_NS) {
+            }
           }
         }
       }
     }
   } else if (warp == 1) {
     // ---------------------------------------------------------------- MMA issuer
-    if (lane == 0) {
+    // (the pair: the even CTA only; its MMAs read both CTAs' stages at the same offsets)
+    if (lane == 0 && rank == 0) {
       for (int it = 0; it < nk; ++it) {
-        const int s = it % TC_STAGES;
-        const uint32_t ph = (uint32_t)(it / TC_STAGES) & 1u;
+        const int s = it % STAGES;
+        const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
         if (!mbar_wait(&full_bar[s], ph, abort_flag, 2)) break;
         tc_fence_after();
-        const uint32_t sa = smem_u32(smem + s * TC_STAGE_BYTES);
+        const uint32_t sa = smem_u32(smem + s * Cfg::STAGE_BYTES);
         const uint64_t da = sw128_desc(sa), db = sw128_desc(sa + TC_A_BYTES);
 #pragma unroll
         for (int k = 0; k < TC_BK / 16; ++k)  // 16 BF16 = 32 bytes = +2 in the descriptor
-          umma(tmem, da + 2 * k, db + 2 * k, (it | k) != 0 ? 1u : 0u);
-        umma_commit(&empty_bar[s]);
+          umma<PAIR>(tmem, da + 2 * k, db + 2 * k, (it | k) != 0 ? 1u : 0u);
+        umma_commit<PAIR>(&empty_bar[s]);
       }
-      umma_commit(&accum_bar);  // also on an abort: completes once every issued MMA has
+      umma_commit<PAIR>(&accum_bar);  // also on an abort: completes once every issued MMA has
     }
   } else {
     // ---------------------------------------------------------------- epilogue (warps 2-5)
@@ -274,6 +386,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
     if (do_store) {
       for (int c0 = 0; c0 < TC_BN; c0 += 32) {
+        // the 32 columns' map entries, then their Y values, all issued before any store (the
+        // stores may alias Y, so the compiler would otherwise wait out one load per column)
+        int colv[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int c = n0 + c0 + j;
+          colv[j] = c >= cnt ? -1 : (a.nmap ? a.nmap[c] : c);
+        }
+        float yv[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) yv[j] = (a.Y && colv[j] >= 0) ? a.Y[(size_t)colv[j] * a.M + row] : 0.0f;
         float v[32];
         if (S > 1) {
 #pragma unroll
@@ -288,11 +411,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
-          int col = n0 + c0 + j;
-          if (col >= cnt) continue;
-          if (a.nmap) col = a.nmap[col];
+          const int col = colv[j];
+          if (col < 0) continue;
           const size_t o = (size_t)col * a.M + row;
-          const float val = a.Y ? a.Y[o] - v[j] : v[j];
+          const float val = a.Y ? yv[j] - v[j] : v[j];
           a.Ct[o] = val;
           if (a.Cb) {
             const __nv_bfloat16 hi = __float2bfloat16_rn(val);
@@ -311,10 +433,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
   }
   tc_fence_before();
-  __syncthreads();
+  // the pair: neither CTA leaves (or frees tensor memory) while the other's MMAs or copies may
+  // still touch its shared memory
+  if constexpr (PAIR)
+    cluster_sync_all();
+  else
+    __syncthreads();
   if (warp == 1) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+    tmem_dealloc<PAIR>(tmem);
   }
 }
 
@@ -368,9 +495,15 @@ gb_status tensor_map(CUtensorMap *map, const void *base, int rows, int K, int ld
 gb_status gb_gemm_tc(const GbGemm &g, cudaStream_t s) {
   static std::atomic<unsigned long long> attr_done{0};
   GB_TRY(gb_once_per_device(attr_done, []() -> gb_status {
-    GB_CUDA_TRY(cudaFuncSetAttribute(k_gemm_tn_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+    GB_CUDA_TRY(
+        cudaFuncSetAttribute(k_gemm_tn_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcCfg<0>::SMEM));
+    GB_CUDA_TRY(
+        cudaFuncSetAttribute(k_gemm_tn_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcCfg<1>::SMEM));
     return GB_OK;
   }));
+  // the CTA-pair instance unless M is an odd number of 128-row tiles or GB_CS_GEMM_PAIR=0
+  const char *pe = getenv("GB_CS_GEMM_PAIR");
+  const bool pair = !(pe && atoi(pe) == 0) && g.M % (2 * TC_BM) == 0;
   const void *B = g.B;
   int ldb = g.ldb;
   if (g.nmap) {
@@ -386,7 +519,7 @@ gb_status gb_gemm_tc(const GbGemm &g, cudaStream_t s) {
   }
   CUtensorMap ta, tb;
   GB_TRY(tensor_map(&ta, g.A, g.M, g.K, g.lda, TC_BM));
-  GB_TRY(tensor_map(&tb, B, g.N, g.K, ldb, TC_BN));
+  GB_TRY(tensor_map(&tb, B, g.N, g.K, ldb, pair ? TcCfg<1>::B_ROWS : TcCfg<0>::B_ROWS));
   TcArgs a = {};
   a.Ct = g.Ct;
   a.M = g.M;
@@ -402,9 +535,25 @@ gb_status gb_gemm_tc(const GbGemm &g, cudaStream_t s) {
     a.ws = *g.ws;
     a.s_max = GB_GEMM_SPLIT_MAX;
   }
-  dim3 grid(g.M / TC_BM, (g.N / TC_BN) * a.s_max);
-  k_gemm_tn_tc<<<grid, TC_THREADS, TC_SMEM, s>>>(ta, tb, a);
-  GB_CUDA_TRY(cudaGetLastError());
+  const dim3 grid(g.M / TC_BM, (g.N / TC_BN) * a.s_max);
+  if (!pair) {
+    k_gemm_tn_tc<0><<<grid, TC_THREADS, TcCfg<0>::SMEM, s>>>(ta, tb, a);
+    GB_CUDA_TRY(cudaGetLastError());
+    return GB_OK;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(TC_THREADS, 1, 1);
+  cfg.dynamicSmemBytes = TcCfg<1>::SMEM;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_gemm_tn_tc<1>, ta, tb, a));
   return GB_OK;
 }
 

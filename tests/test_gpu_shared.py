@@ -47,10 +47,13 @@ def test_gemm_bf16_tn(gb, M, N, K):
     assert np.array_equal(Cb.float().cpu().numpy(), _bf16_round(got2))
 
 
-@pytest.mark.parametrize("M,N,K", [(128, 256, 64), (384, 512, 1024), (1024, 256, 24576)])
+@pytest.mark.parametrize("M,N,K", [(128, 256, 64), (384, 512, 1024), (1024, 256, 24576), (256, 256, 64),
+                                   (512, 768, 448), (768, 512, 960), (2048, 1024, 4096)])
 def test_gemm_tcgen05(gb, M, N, K):
-    """N % 256 == 0 and K % 64 == 0 run the tcgen05 + TMA kernel: check it against an FP64
-    product of the same BF16 operands and against the mma.sync kernel (GB_CS_GEMM=mma)."""
+    """N % 256 == 0 and K % 64 == 0 run the tcgen05 + TMA kernel (the CTA-pair instance when
+    M % 256 == 0; fewer, exactly as many and more k-blocks than ring stages): check it against an
+    FP64 product of the same BF16 operands, against the single-CTA instance (GB_CS_GEMM_PAIR=0)
+    and against the mma.sync kernel (GB_CS_GEMM=mma)."""
     import os
 
     import torch
@@ -76,6 +79,13 @@ def test_gemm_tcgen05(gb, M, N, K):
     finally:
         del os.environ["GB_CS_GEMM"]
     assert np.all(np.abs(got - Ct2.cpu().numpy()) <= 2 * bound)
+    os.environ["GB_CS_GEMM_PAIR"] = "0"
+    try:
+        Ct3, _ = gb.gemm_bf16_tn(dA, dB, Y=dY)
+        torch.cuda.synchronize()
+    finally:
+        del os.environ["GB_CS_GEMM_PAIR"]
+    assert np.all(np.abs(got - Ct3.cpu().numpy()) <= 2 * bound)
 
 
 def test_gemm_rejects_bad_shapes(gb):
