@@ -1379,7 +1379,7 @@ int gb_resident_last_cluster() {
   return it == g_res.end() ? 0 : it->second.C;
 }
 
-// The drop-in's dense NIHT or CGIHT on one cluster (the caller checked that the state is
+// The drop-in's dense NIHT, HTP or CGIHT on one cluster (the caller checked that the state is
 // the plain start: no timing variant, no warm start).  The cluster takes up to 16 CTAs with at
 // least 128 columns each; *used = 0 when the problem does not fit (the graph path solves it).
 gb_status gb_resident_solve_single(GbWork &w, int gb_alg, int num_bins, cudaStream_t s, int *used) {

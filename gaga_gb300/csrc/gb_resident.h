@@ -1,4 +1,5 @@
-// gb_resident.h -- the cluster-resident NIHT kernel of the batched form (gb_resident.cu).
+// gb_resident.h -- the cluster-resident NIHT / HTP / CGIHT kernel (gb_resident.cu): the batched
+// form's small trials and the single-trial drop-in's small dense solves.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -9,7 +10,7 @@
 // trials with n <= this go to the resident kernel unless the caller says otherwise
 #define GB_RESIDENT_N_DEFAULT 8192
 
-// One launch solving `count` NIHT or CGIHT trials, trial order[q] for q < count (indices into the
+// One launch solving `count` NIHT, HTP or CGIHT trials, trial order[q] for q < count (indices into the
 // batch tables n, m, k, tid and the result arrays, all device pointers), each by one
 // cluster of CTAs.  n_cap / m_cap bound the trials' n and m; cluster = CTAs per cluster
 // (0: four, or the smallest power of two above that the sizes fit).
@@ -26,7 +27,7 @@ struct GbResidentArgs {
   int *ok;
   double *bytes;
   int n_cap, m_cap, cluster;
-  int alg;  // GB_ALG_NIHT or GB_ALG_CGIHT
+  int alg;  // GB_ALG_NIHT, GB_ALG_HTP or GB_ALG_CGIHT
   const float *ml_params;  // CGIHT from the learned warm start (device MLP parameters) or null
   int *fb;                 // with it: per trial, 1 when the warm start was abandoned
 };
@@ -41,7 +42,7 @@ int gb_resident_max_smem();
 int gb_resident_last_cluster();
 // held for the whole of gb_cs_solve_batch (gb_batch.cu): the engines are shared per device
 std::recursive_mutex &gb_batch_mutex();
-// The single-trial drop-in's dense NIHT or CGIHT (the learned warm start when w.ml_params;
+// The single-trial drop-in's dense NIHT, HTP or CGIHT (the learned warm start when w.ml_params;
 // state initialised in w.st, y in w.y) on one cluster; x to w.x and the final state to w.st.  *used = 0: not eligible, nothing
 // launched.
 gb_status gb_resident_solve_single(GbWork &w, int gb_alg, int num_bins, cudaStream_t s, int *used);
