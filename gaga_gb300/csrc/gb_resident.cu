@@ -1379,8 +1379,8 @@ int gb_resident_last_cluster() {
   return it == g_res.end() ? 0 : it->second.C;
 }
 
-// The drop-in's dense NIHT, HTP or CGIHT on one cluster (the caller checked that the state is
-// the plain start: no timing variant, no warm start).  The cluster takes up to 16 CTAs with at
+// The drop-in's dense NIHT, HTP or CGIHT on one cluster (the caller checked that no timing
+// variant is asked for; with w.ml_params CGIHT runs the learned warm-start instance).  The cluster takes up to 16 CTAs with at
 // least 128 columns each; *used = 0 when the problem does not fit (the graph path solves it).
 gb_status gb_resident_solve_single(GbWork &w, int gb_alg, int num_bins, cudaStream_t s, int *used) {
   *used = 0;
