@@ -19,11 +19,18 @@
 #include "gb_internal.cuh"
 
 // ------------------------------------------------------------------ dense
-#define DV_THREADS 512  // A x_S: 16 warps share one 128-row tile
-#define DV_ROWS 128
+#define DV_THREADS 512  // A x_S: 16 warps share one row tile
+// float4 per lane per support column: a warp reads 512 * DV_R contiguous bytes of a column.
+// On GB300 at m = 14746, |S| = 5000: 1 -> 81%, 2 -> 86%, 4 -> 85% of the measured HBM peak
+// (longer runs per column open fewer DRAM pages; 4 halves the resident warps)
+#ifndef DV_R
+#define DV_R 2
+#endif
+#define DV_ROWS (128 * DV_R)
 #define DV_STAGE 512    // support entries staged in shared memory per pass
 #define DV_MIN_SPLIT 512  // support columns per CTA before the support is split further
-#define DV_BLOCKS_PER_SM 4  // 4 x 512 threads resident per SM (<= 32 registers per thread)
+#define DV_BLOCKS_PER_SM (DV_R == 1 ? 4 : 2)  // 512-thread CTAs resident per SM (32 / 64 registers)
+constexpr int kDvUnroll = DV_R == 1 ? 8 : (DV_R == 2 ? 4 : 2);  // support columns in flight per warp
 #define DA_THREADS 256  // A^T r: 8 warps, 4 columns per warp
 #define DA_BLOCKS_PER_SM 3  // resident A^T r CTAs per SM (<= 85 registers per thread)
 
@@ -38,10 +45,11 @@ __device__ __forceinline__ float4 ld_stream4(const float *p) {
 }
 
 // out_i = [y_i -] sum_{s < |S|} A[i, S[s]] v[S[s]]; st->red[slot] = ||out||^2.
-// CTA b works on row tile b % ntile (128 rows, float4 per lane) and on split b / ntile of
-// the support; its 16 warps take entries w, w+16, ... of each staged chunk.  With more
-// than one split, each CTA publishes its partial tile and the last CTA of the tile to
-// arrive adds the partials in split order (deterministic, no second kernel).
+// CTA b works on row tile b % ntile (DV_ROWS rows: DV_R float4 per lane, so a warp reads
+// 512 * DV_R contiguous bytes of each column) and on split b / ntile of the support; its 16
+// warps take entries w, w+16, ... of each staged chunk.  With more than one split, each CTA
+// publishes its partial tile and the last CTA of the tile to arrive adds the partials in
+// split order (deterministic, no second kernel).
 template <int VEC>
 __global__ void __launch_bounds__(DV_THREADS, DV_BLOCKS_PER_SM) k_dense_av(GbState *st, int pf, const float *__restrict__ A, int lda,
                                                          int m, int ntile_cap, int nsplit, const int *__restrict__ S,
@@ -49,6 +57,7 @@ __global__ void __launch_bounds__(DV_THREADS, DV_BLOCKS_PER_SM) k_dense_av(GbSta
                                                          float *__restrict__ out, float *__restrict__ part,
                                                          unsigned int *__restrict__ tile_tk, int slot, float *red_part,
                                                          unsigned int *tickets) {
+  constexpr int NA = 4 * DV_R;  // accumulators per lane
   if (!gb_pred(st, pf)) return;
   lda = dimv(st, lda);
   m = dimv(st, m);
@@ -56,18 +65,23 @@ __global__ void __launch_bounds__(DV_THREADS, DV_BLOCKS_PER_SM) k_dense_av(GbSta
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   __shared__ int sj[DV_STAGE];
   __shared__ float sv[DV_STAGE];
-  __shared__ float4 red[DV_THREADS / 32][32];
+  __shared__ float red[DV_THREADS / 32][NA][32];
   __shared__ int is_last;
   const int ntile = (m + DV_ROWS - 1) / DV_ROWS;
   const int tile = blockIdx.x % ntile_cap, split = blockIdx.x / ntile_cap;
   // splits actually used: at least DV_MIN_SPLIT support columns per CTA
   nsplit = max(1, min(nsplit, (s + DV_MIN_SPLIT - 1) / DV_MIN_SPLIT));
   float acc2 = 0.0f;
+  // accumulator c of a lane holds row r0 + row_of(c): (lane + 32 (c / 4)) * 4 + c % 4 for
+  // float4 rows, lane + 32 c otherwise
+  auto row_of = [&](int c) { return VEC == 4 ? (lane + 32 * (c >> 2)) * 4 + (c & 3) : lane + 32 * c; };
   if (tile < ntile && split < nsplit) {
     const int r0 = tile * DV_ROWS;
     const int chunk = ((s + nsplit - 1) / nsplit + 15) & ~15;
     const int s_lo = min(s, split * chunk), s_hi = min(s, s_lo + chunk);
-    float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+    float a[NA];
+#pragma unroll
+    for (int c = 0; c < NA; ++c) a[c] = 0.0f;
     for (int c0 = s_lo; c0 < s_hi; c0 += DV_STAGE) {
       const int cn = min(DV_STAGE, s_hi - c0);
       __syncthreads();
@@ -78,44 +92,50 @@ __global__ void __launch_bounds__(DV_THREADS, DV_BLOCKS_PER_SM) k_dense_av(GbSta
       }
       __syncthreads();
       if (VEC == 4) {
-        const int row = r0 + lane * 4;
-        if (row < m) {
-#pragma unroll 8
-          for (int c = warp; c < cn; c += DV_THREADS / 32) {
-            const float4 q = ld_stream4(A + (size_t)sj[c] * lda + row);
-            const float vj = sv[c];
-            a0 = fmaf(q.x, vj, a0);
-            a1 = fmaf(q.y, vj, a1);
-            a2 = fmaf(q.z, vj, a2);
-            a3 = fmaf(q.w, vj, a3);
+#pragma unroll kDvUnroll
+        for (int c = warp; c < cn; c += DV_THREADS / 32) {
+          const float *col = A + (size_t)sj[c] * lda + r0;
+          const float vj = sv[c];
+#pragma unroll
+          for (int u = 0; u < DV_R; ++u) {
+            const int rr = (lane + 32 * u) * 4;
+            if (r0 + rr < m) {
+              const float4 q = ld_stream4(col + rr);
+              a[4 * u] = fmaf(q.x, vj, a[4 * u]);
+              a[4 * u + 1] = fmaf(q.y, vj, a[4 * u + 1]);
+              a[4 * u + 2] = fmaf(q.z, vj, a[4 * u + 2]);
+              a[4 * u + 3] = fmaf(q.w, vj, a[4 * u + 3]);
+            }
           }
         }
       } else {
-        const int rb = r0 + lane;
-#pragma unroll 4
+#pragma unroll kDvUnroll
         for (int c = warp; c < cn; c += DV_THREADS / 32) {
-          const float *col = A + (size_t)sj[c] * lda;
+          const float *col = A + (size_t)sj[c] * lda + r0;
           const float vj = sv[c];
-          if (rb < m) a0 = fmaf(__ldg(col + rb), vj, a0);
-          if (rb + 32 < m) a1 = fmaf(__ldg(col + rb + 32), vj, a1);
-          if (rb + 64 < m) a2 = fmaf(__ldg(col + rb + 64), vj, a2);
-          if (rb + 96 < m) a3 = fmaf(__ldg(col + rb + 96), vj, a3);
+#pragma unroll
+          for (int e = 0; e < NA; ++e)
+            if (r0 + lane + 32 * e < m) a[e] = fmaf(__ldg(col + lane + 32 * e), vj, a[e]);
         }
       }
     }
-    red[warp][lane] = make_float4(a0, a1, a2, a3);
-    __syncthreads();
-    float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (warp == 0) {
-      t = red[0][lane];
 #pragma unroll
-      for (int w2 = 1; w2 < DV_THREADS / 32; ++w2) {
-        const float4 q = red[w2][lane];
-        t.x += q.x; t.y += q.y; t.z += q.z; t.w += q.w;
+    for (int c = 0; c < NA; ++c) red[warp][c][lane] = a[c];
+    __syncthreads();
+    float t[NA];
+    if (warp == 0) {
+#pragma unroll
+      for (int c = 0; c < NA; ++c) {
+        t[c] = red[0][c][lane];
+#pragma unroll
+        for (int w2 = 1; w2 < DV_THREADS / 32; ++w2) t[c] += red[w2][c][lane];
       }
     }
     if (nsplit > 1) {
-      if (warp == 0) reinterpret_cast<float4 *>(part)[((size_t)tile * nsplit + split) * 32 + lane] = t;
+      if (warp == 0) {
+#pragma unroll
+        for (int c = 0; c < NA; ++c) part[(((size_t)tile * nsplit + split) * NA + c) * 32 + lane] = t[c];
+      }
       __threadfence();
       __syncthreads();
       if (threadIdx.x == 0) {
@@ -125,11 +145,12 @@ __global__ void __launch_bounds__(DV_THREADS, DV_BLOCKS_PER_SM) k_dense_av(GbSta
       __syncthreads();
       if (is_last && warp == 0) {
         __threadfence();
-        const float4 *pp = reinterpret_cast<const float4 *>(part) + (size_t)tile * nsplit * 32 + lane;
-        t = __ldcg(pp);
+        const float *pp = part + (size_t)tile * nsplit * NA * 32 + lane;
+#pragma unroll
+        for (int c = 0; c < NA; ++c) t[c] = __ldcg(pp + c * 32);
         for (int q = 1; q < nsplit; ++q) {
-          const float4 u = __ldcg(pp + q * 32);
-          t.x += u.x; t.y += u.y; t.z += u.z; t.w += u.w;
+#pragma unroll
+          for (int c = 0; c < NA; ++c) t[c] += __ldcg(pp + ((size_t)q * NA + c) * 32);
         }
         if (lane == 0) tile_tk[tile] = 0u;
       }
@@ -138,12 +159,11 @@ __global__ void __launch_bounds__(DV_THREADS, DV_BLOCKS_PER_SM) k_dense_av(GbSta
     }
     __syncthreads();
     if (is_last && warp == 0) {
-      const float o4[4] = {t.x, t.y, t.z, t.w};
 #pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        const int i = VEC == 4 ? r0 + lane * 4 + c : r0 + lane + 32 * c;
+      for (int c = 0; c < NA; ++c) {
+        const int i = r0 + row_of(c);
         if (i < m) {
-          const float o = y ? y[i] - o4[c] : o4[c];
+          const float o = y ? y[i] - t[c] : t[c];
           out[i] = o;
           acc2 = fmaf(o, o, acc2);
         }
