@@ -28,7 +28,8 @@
 #endif
 #define DV_ROWS (128 * DV_R)
 #define DV_STAGE 512    // support entries staged in shared memory per pass
-#define DV_MIN_SPLIT 512  // support columns per CTA before the support is split further
+#define DV_MIN_SPLIT 512  // support columns per CTA before the support is split further ...
+#define DV_MIN_SPLIT_FEW 64  // ... and with fewer than 16 row tiles, where splits are the parallelism
 #define DV_BLOCKS_PER_SM (DV_R == 1 ? 4 : 2)  // 512-thread CTAs resident per SM (32 / 64 registers)
 constexpr int kDvUnroll = DV_R == 1 ? 8 : (DV_R == 2 ? 4 : 2);  // support columns in flight per warp
 #define DA_THREADS 256  // A^T r: 8 warps, 4 columns per warp
@@ -69,8 +70,9 @@ __global__ void __launch_bounds__(DV_THREADS, DV_BLOCKS_PER_SM) k_dense_av(GbSta
   __shared__ int is_last;
   const int ntile = (m + DV_ROWS - 1) / DV_ROWS;
   const int tile = blockIdx.x % ntile_cap, split = blockIdx.x / ntile_cap;
-  // splits actually used: at least DV_MIN_SPLIT support columns per CTA
-  nsplit = max(1, min(nsplit, (s + DV_MIN_SPLIT - 1) / DV_MIN_SPLIT));
+  // splits actually used: at least DV_MIN_SPLIT (DV_MIN_SPLIT_FEW) support columns per CTA
+  const int min_split = ntile < 16 ? DV_MIN_SPLIT_FEW : DV_MIN_SPLIT;
+  nsplit = max(1, min(nsplit, (s + min_split - 1) / min_split));
   float acc2 = 0.0f;
   // accumulator c of a lane holds row r0 + row_of(c): (lane + 32 (c / 4)) * 4 + c % 4 for
   // float4 rows, lane + 32 c otherwise
@@ -716,7 +718,9 @@ void gb_dense_av_shape(int m, int num_sms, int *ntile, int *nsplit) {
   const double slots = (double)DV_BLOCKS_PER_SM * num_sms;
   int best = 1;
   double best_fill = -1.0;
-  for (int sp = 1; sp <= 16 && t * sp <= GB_MAXRB; ++sp) {
+  // up to 16 splits, more when the row tiles alone fill less than one wave (small m)
+  const int sp_max = std::max(16, (int)std::ceil(slots / t));
+  for (int sp = 1; sp <= sp_max && t * sp <= GB_MAXRB; ++sp) {
     const double x = t * sp / slots;
     const double fill = x < 1.0 ? x : x / std::ceil(x);
     if (fill > best_fill + 1e-3) {
