@@ -153,8 +153,8 @@ gb_status alloc_work(DeviceBuffers &db, GbWork &w, int m, int n, int lda, int nu
   GB_TRY(db.alloc(&w.tile_cnt, 2 * ((n + GB_TILE - 1) / GB_TILE)));  // second half: smp's k-th bin counts
   GB_TRY(db.alloc(&w.rec, (size_t)maxiter + 2));
   GB_TRY(db.alloc(&w.sel_hist, (size_t)3 * GB_SEL_BINS));  // zeroed; the select keeps it zero
-  gb_dense_av_shape(m, w.num_sms, &w.av_ntile, &w.av_nsplit);
-  w.part_cap = gb_dense_part_floats_av(w.av_ntile, w.av_nsplit);
+  gb_dense_av_shape(m, w.num_sms, false, &w.av_ntile, &w.av_nsplit, &w.av_rows);
+  w.part_cap = gb_dense_part_floats_av(w.av_ntile, w.av_nsplit, w.av_rows);
   GB_TRY(db.alloc(&w.av_tickets, w.av_ntile));
   return GB_OK;
 }

@@ -130,10 +130,10 @@ struct GbWork {
   int *bins, *bins_prev, *counters;
   int *S;        // support list (n)
   int *tile_cnt; // per-tile counts for ordered compaction
-  float *part;   // dense A x_S partial tiles (av_ntile * av_nsplit * 128 floats)
+  float *part;   // dense A x_S partial tiles (av_ntile * av_nsplit * av_rows floats)
   size_t part_cap;
   unsigned int *av_tickets;  // per row tile arrival counters
-  int av_ntile, av_nsplit;   // A x_S launch shape
+  int av_ntile, av_nsplit, av_rows;   // A x_S launch shape (row tiles of 128 or 256 rows)
   float *upd;    // l0 updates (n)
   float *rec;    // l0 residual record (maxiter + 1)
   unsigned int *sel_hist;    // timing variants: radix-select histograms (3 x GB_SEL_BINS, kept zero)
@@ -290,8 +290,8 @@ void enq_AT(GbWork &w, cudaStream_t s, const float *r, float *g, int pf);
 // dense only: g = A^T r fused with xt = g on the support, ||xt||^2 and max|g|
 void enq_AT_mask(GbWork &w, cudaStream_t s, const float *r, float *g, float *xt, int slot_sq, int slot_max, int pf);
 // dense A x_S launch shape for (capacity) m and its partial buffer size in floats
-void gb_dense_av_shape(int m, int num_sms, int *ntile, int *nsplit);
-size_t gb_dense_part_floats_av(int ntile, int nsplit);
+void gb_dense_av_shape(int m, int num_sms, bool share, int *ntile, int *nsplit, int *rows);
+size_t gb_dense_part_floats_av(int ntile, int nsplit, int rows);
 
 // BF16 TN GEMM with FP32 accumulation (gb_gemm.cu):
 //   Ct[N x M] = [Y -] (A[M x K] . B[N x K]^T)^T,  A, B row-major with row strides lda, ldb,

@@ -92,7 +92,7 @@ extern "C" gb_status gb_cs_dense_apply_noalloc(const float *d_A, int lda, int m,
   op.lda = lda;
   op.A = d_A;
   op.vec4 = (lda % 4 == 0) && (((uintptr_t)d_A & 15) == 0);
-  gb_dense_av_shape(m, w.num_sms, &w.av_ntile, &w.av_nsplit);
+  gb_dense_av_shape(m, w.num_sms, false, &w.av_ntile, &w.av_nsplit, &w.av_rows);
   // carve the scratch: state | support list | tile counts | arrival counters | partial tiles
   size_t off = 0;
   w.st = (GbState *)(base + off);
@@ -105,7 +105,7 @@ extern "C" gb_status gb_cs_dense_apply_noalloc(const float *d_A, int lda, int m,
   const size_t tickets_bytes = align256((size_t)w.av_ntile * 4);
   off += tickets_bytes;
   w.part = (float *)(base + off);
-  w.part_cap = gb_dense_part_floats_av(w.av_ntile, w.av_nsplit);
+  w.part_cap = gb_dense_part_floats_av(w.av_ntile, w.av_nsplit, w.av_rows);
   off += align256(w.part_cap * 4);
   if (off > GB_NOALLOC_SCRATCH_BYTES) {
     gb_set_error_message("gb_cs_dense_apply_noalloc: scratch too small for this shape", __FILE__, __LINE__);

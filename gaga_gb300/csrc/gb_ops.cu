@@ -20,18 +20,20 @@
 
 // ------------------------------------------------------------------ dense
 #define DV_THREADS 512  // A x_S: 16 warps share one row tile
-// float4 per lane per support column: a warp reads 512 * DV_R contiguous bytes of a column.
-// On GB300 at m = 14746, |S| = 5000: 1 -> 81%, 2 -> 86%, 4 -> 85% of the measured HBM peak
-// (longer runs per column open fewer DRAM pages; 4 halves the resident warps)
-#ifndef DV_R
-#define DV_R 2
-#endif
-#define DV_ROWS (128 * DV_R)
 #define DV_STAGE 512    // support entries staged in shared memory per pass
 #define DV_MIN_SPLIT 512  // support columns per CTA before the support is split further ...
-#define DV_MIN_SPLIT_FEW 64  // ... and with fewer than 16 row tiles, where splits are the parallelism
-#define DV_BLOCKS_PER_SM (DV_R == 1 ? 4 : 2)  // 512-thread CTAs resident per SM (32 / 64 registers)
-constexpr int kDvUnroll = DV_R == 1 ? 8 : (DV_R == 2 ? 4 : 2);  // support columns in flight per warp
+#define DV_MIN_SPLIT_FEW 64  // ... and, for 256-row tiles, with fewer than 16 row tiles
+// Row tiles of A x_S: R float4 per lane per support column, so a warp reads 512 R contiguous
+// bytes of a column.  A launch that owns the GPU takes R = 2 (on GB300 at m = 14746, |S| =
+// 5000: 81% -> 86% of the measured HBM peak, longer runs per column opening fewer DRAM
+// pages); the batched form's slots, each on a share of the SMs beside other slots, keep R = 1
+// (R = 2 there, with half the tiles and half the resident CTAs, made the sweep 5% slower).
+template <int R>
+struct DvCfg {
+  static constexpr int ROWS = 128 * R;
+  static constexpr int BLOCKS_PER_SM = R == 1 ? 4 : 2;  // 512-thread CTAs per SM (32 / 64 registers)
+  static constexpr int UNROLL = R == 1 ? 8 : 4;         // support columns in flight per warp
+};
 #define DA_THREADS 256  // A^T r: 8 warps, 4 columns per warp
 #define DA_BLOCKS_PER_SM 3  // resident A^T r CTAs per SM (<= 85 registers per thread)
 
@@ -46,19 +48,20 @@ __device__ __forceinline__ float4 ld_stream4(const float *p) {
 }
 
 // out_i = [y_i -] sum_{s < |S|} A[i, S[s]] v[S[s]]; st->red[slot] = ||out||^2.
-// CTA b works on row tile b % ntile (DV_ROWS rows: DV_R float4 per lane, so a warp reads
-// 512 * DV_R contiguous bytes of each column) and on split b / ntile of the support; its 16
+// CTA b works on row tile b % ntile (128 R rows: R float4 per lane, so a warp reads 512 R
+// contiguous bytes of each column) and on split b / ntile of the support; its 16
 // warps take entries w, w+16, ... of each staged chunk.  With more than one split, each CTA
 // publishes its partial tile and the last CTA of the tile to arrive adds the partials in
 // split order (deterministic, no second kernel).
-template <int VEC>
-__global__ void __launch_bounds__(DV_THREADS, DV_BLOCKS_PER_SM) k_dense_av(GbState *st, int pf, const float *__restrict__ A, int lda,
+template <int VEC, int R>
+__global__ void __launch_bounds__(DV_THREADS, DvCfg<R>::BLOCKS_PER_SM) k_dense_av(GbState *st, int pf, const float *__restrict__ A, int lda,
                                                          int m, int ntile_cap, int nsplit, const int *__restrict__ S,
                                                          const float *__restrict__ v, const float *__restrict__ y,
                                                          float *__restrict__ out, float *__restrict__ part,
                                                          unsigned int *__restrict__ tile_tk, int slot, float *red_part,
                                                          unsigned int *tickets) {
-  constexpr int NA = 4 * DV_R;  // accumulators per lane
+  constexpr int NA = 4 * R;  // accumulators per lane
+  constexpr int ROWS = DvCfg<R>::ROWS;
   if (!gb_pred(st, pf)) return;
   lda = dimv(st, lda);
   m = dimv(st, m);
@@ -68,17 +71,17 @@ __global__ void __launch_bounds__(DV_THREADS, DV_BLOCKS_PER_SM) k_dense_av(GbSta
   __shared__ float sv[DV_STAGE];
   __shared__ float red[DV_THREADS / 32][NA][32];
   __shared__ int is_last;
-  const int ntile = (m + DV_ROWS - 1) / DV_ROWS;
+  const int ntile = (m + ROWS - 1) / ROWS;
   const int tile = blockIdx.x % ntile_cap, split = blockIdx.x / ntile_cap;
   // splits actually used: at least DV_MIN_SPLIT (DV_MIN_SPLIT_FEW) support columns per CTA
-  const int min_split = ntile < 16 ? DV_MIN_SPLIT_FEW : DV_MIN_SPLIT;
+  const int min_split = (R > 1 && ntile < 16) ? DV_MIN_SPLIT_FEW : DV_MIN_SPLIT;
   nsplit = max(1, min(nsplit, (s + min_split - 1) / min_split));
   float acc2 = 0.0f;
   // accumulator c of a lane holds row r0 + row_of(c): (lane + 32 (c / 4)) * 4 + c % 4 for
   // float4 rows, lane + 32 c otherwise
   auto row_of = [&](int c) { return VEC == 4 ? (lane + 32 * (c >> 2)) * 4 + (c & 3) : lane + 32 * c; };
   if (tile < ntile && split < nsplit) {
-    const int r0 = tile * DV_ROWS;
+    const int r0 = tile * ROWS;
     const int chunk = ((s + nsplit - 1) / nsplit + 15) & ~15;
     const int s_lo = min(s, split * chunk), s_hi = min(s, s_lo + chunk);
     float a[NA];
@@ -94,12 +97,12 @@ __global__ void __launch_bounds__(DV_THREADS, DV_BLOCKS_PER_SM) k_dense_av(GbSta
       }
       __syncthreads();
       if (VEC == 4) {
-#pragma unroll kDvUnroll
+#pragma unroll DvCfg<R>::UNROLL
         for (int c = warp; c < cn; c += DV_THREADS / 32) {
           const float *col = A + (size_t)sj[c] * lda + r0;
           const float vj = sv[c];
 #pragma unroll
-          for (int u = 0; u < DV_R; ++u) {
+          for (int u = 0; u < R; ++u) {
             const int rr = (lane + 32 * u) * 4;
             if (r0 + rr < m) {
               const float4 q = ld_stream4(col + rr);
@@ -111,7 +114,8 @@ __global__ void __launch_bounds__(DV_THREADS, DV_BLOCKS_PER_SM) k_dense_av(GbSta
           }
         }
       } else {
-#pragma unroll kDvUnroll
+        constexpr int U1 = DvCfg<R>::UNROLL / 2;  // scalar loads: half the columns in flight
+#pragma unroll U1
         for (int c = warp; c < cn; c += DV_THREADS / 32) {
           const float *col = A + (size_t)sj[c] * lda + r0;
           const float vj = sv[c];
@@ -711,15 +715,20 @@ static void launch_fft(GbWork &w, cudaStream_t s, int pf, int pass, const float 
 
 // A x_S launch shape: row tiles of the (capacity) m times support splits, <= GB_MAXRB CTAs.
 // The split count is the smallest that best fills whole waves of the resident CTA slots
-// (DV_BLOCKS_PER_SM per SM): a grid of 1.5 waves leaves half the GPU idle in its tail.
-void gb_dense_av_shape(int m, int num_sms, int *ntile, int *nsplit) {
-  int t = (m + DV_ROWS - 1) / DV_ROWS;
+// (blocks per SM of the tile height): a grid of 1.5 waves leaves half the GPU idle in its
+// tail.  share: the launch runs on a share of the SMs beside other launches (the batched
+// form's slots), which keeps 128-row tiles and at most 16 splits.
+void gb_dense_av_shape(int m, int num_sms, bool share, int *ntile, int *nsplit, int *rows) {
+  const int R = share ? 1 : 2;
+  const int bps = R == 1 ? DvCfg<1>::BLOCKS_PER_SM : DvCfg<2>::BLOCKS_PER_SM;
+  *rows = 128 * R;
+  int t = (m + *rows - 1) / *rows;
   if (t > GB_MAXRB) t = GB_MAXRB;
-  const double slots = (double)DV_BLOCKS_PER_SM * num_sms;
+  const double slots = (double)bps * num_sms;
   int best = 1;
   double best_fill = -1.0;
-  // up to 16 splits, more when the row tiles alone fill less than one wave (small m)
-  const int sp_max = std::max(16, (int)std::ceil(slots / t));
+  // up to 16 splits; a whole-GPU launch takes more when its row tiles fill less than a wave
+  const int sp_max = share ? 16 : std::max(16, (int)std::ceil(slots / t));
   for (int sp = 1; sp <= sp_max && t * sp <= GB_MAXRB; ++sp) {
     const double x = t * sp / slots;
     const double fill = x < 1.0 ? x : x / std::ceil(x);
@@ -732,18 +741,16 @@ void gb_dense_av_shape(int m, int num_sms, int *ntile, int *nsplit) {
   *nsplit = best;
 }
 
-size_t gb_dense_part_floats_av(int ntile, int nsplit) { return (size_t)ntile * nsplit * DV_ROWS; }
+size_t gb_dense_part_floats_av(int ntile, int nsplit, int rows) { return (size_t)ntile * nsplit * rows; }
 
 void enq_A(GbWork &w, cudaStream_t s, const float *v, float *out, const float *y, int slot, int pf) {
   const GbOp &op = w.op;
   if (op.kind == GB_OP_DENSE) {
     const int grid = w.av_ntile * w.av_nsplit;
-    if (op.vec4)
-      k_dense_av<4><<<grid, DV_THREADS, 0, s>>>(w.st, pf, op.A, argLDA(w), argM(w), w.av_ntile, w.av_nsplit, w.S, v,
-                                                 y, out, w.part, w.av_tickets, slot, w.red_part, w.tickets);
-    else
-      k_dense_av<1><<<grid, DV_THREADS, 0, s>>>(w.st, pf, op.A, argLDA(w), argM(w), w.av_ntile, w.av_nsplit, w.S, v,
-                                                 y, out, w.part, w.av_tickets, slot, w.red_part, w.tickets);
+    auto kern = op.vec4 ? (w.av_rows == 256 ? k_dense_av<4, 2> : k_dense_av<4, 1>)
+                        : (w.av_rows == 256 ? k_dense_av<1, 2> : k_dense_av<1, 1>);
+    kern<<<grid, DV_THREADS, 0, s>>>(w.st, pf, op.A, argLDA(w), argM(w), w.av_ntile, w.av_nsplit, w.S, v, y, out,
+                                     w.part, w.av_tickets, slot, w.red_part, w.tickets);
   } else if (op.kind == GB_OP_DCT) {
     launch_fft<0, LOAD_MAKHOUL, STORE_CPLX_T>(w, s, pf, 1, v, nullptr, op.cbuf0, nullptr);
     launch_fft<0, LOAD_CPLX, STORE_CPLX_NAT>(w, s, pf, 2, nullptr, op.cbuf0, op.cbuf1, nullptr);
