@@ -165,6 +165,28 @@ def test_l0_step_golden(gb):
         assert np.array_equal(res.cpu().numpy(), g("res_after"))
 
 
+@pytest.mark.parametrize("m,n,frac", [(257, 700, 0.5), (513, 2000, 1.0), (1001, 3000, 0.05), (1001, 1200, 1.0),
+                                      (4099, 1500, 0.9)])
+def test_dense_apply_row_tiles(gb, gbo, m, n, frac):
+    """A x_S of the drop-in's operator apply (256-row tiles, the support split down to 64
+    columns per CTA when there are few tiles): m one past a tile boundary, m not a multiple
+    of 4 (scalar loads), tiny and full supports, many tiles; against the oracle's product."""
+    torch = _torch()
+    L = gb._lib.load()
+    rng = np.random.default_rng(m + n)
+    A = gbo.gen_dense(m, n, seed=m)
+    op = gbo.Op.dense(A, m, n)
+    dA = torch.tensor(A, device="cuda")
+    p = gb._lib.Problem(0, m, n, 0, None, dA.data_ptr(), m, None, None, None, 0, 0, 1, None)
+    x = rng.standard_normal(n).astype(np.float32)
+    x[rng.random(n) >= frac] = 0.0
+    dx = torch.tensor(x, device="cuda")
+    out = torch.full((m,), 7.0, device="cuda")
+    assert L.gb_cs_operator_apply(C.byref(p), 0, dx.data_ptr(), out.data_ptr()) == 0
+    yo = gbo.A(op, x)
+    np.testing.assert_allclose(out.cpu().numpy(), yo, rtol=0, atol=2e-5 * max(np.abs(yo).max(), 1e-30))
+
+
 @pytest.mark.parametrize("kind", ["dense", "dct", "smv"])
 def test_operator_apply(gb, gbo, kind):
     torch = _torch()
