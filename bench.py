@@ -368,7 +368,10 @@ def gemm_roofline(tpeak, tpeak_kind, M=4096, N=1024, K=3 * 8192, reps=10):
     del A, B, Y
     torch.cuda.empty_cache()
     mma = os.environ.get("GB_CS_GEMM") == "mma"
-    kern = "k_gemm_tn_mma (mma.sync)" if mma else "k_gemm_tn_tc (tcgen05 + TMA)"
+    single = os.environ.get("GB_CS_GEMM_PAIR") == "0" or M % 256 != 0
+    kern = "k_gemm_tn_mma (mma.sync)" if mma else (
+        "k_gemm_tn_tc<0> (tcgen05 cta_group::1 + TMA, 128x256 tiles)" if single else
+        "k_gemm_tn_tc<1> (tcgen05 cta_group::2 on CTA pairs + TMA, 256x256 tiles)")
     out = {"bound": "tensor", "achieved": ach, "peak": tpeak, "unit": "TFLOP/s", "frac": ach / tpeak,
            "kernel": kern, "shape": "M=%d N=%d K=%d (bf16 in, fp32 accumulate, Y - AB^T epilogue)" % (
                M, N, K), "us_per_launch": t * 1e6, "peak_source": tpeak_kind, "traffic": None}
