@@ -27,7 +27,7 @@
 // bytes of a column.  A launch that owns the GPU takes R = 2 (on GB300 at m = 14746, |S| =
 // 5000: 81% -> 86% of the measured HBM peak, longer runs per column opening fewer DRAM
 // pages); the batched form's slots, each on a share of the SMs beside other slots, keep R = 1
-// (R = 2 there, with half the tiles and half the resident CTAs, made the sweep 5% slower).
+// (R = 2 there, with half the tiles and half the resident CTAs, made the sweep 3-5% slower).
 template <int R>
 struct DvCfg {
   static constexpr int ROWS = 128 * R;
