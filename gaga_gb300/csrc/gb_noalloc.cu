@@ -14,7 +14,11 @@
 //   - all calls share the one scratch array, which keeps the previous call's contents:
 //     calls whose work overlaps on the GPU (different streams or threads without
 //     ordering) race on it and must be serialised by the caller;
-//   - m <= GB_NOALLOC_MAX_M and n <= GB_NOALLOC_MAX_N, otherwise GB_BAD_ARG.
+//   - m <= GB_NOALLOC_MAX_M and n <= GB_NOALLOC_MAX_N, otherwise GB_BAD_ARG; every such
+//     shape fits, since the A x split count is lowered until its partial tiles fit;
+//   - transpose == 2 reuses the support list of the previous transpose == 0 call on the
+//     device, which must have had the same A, lda, m and n, with no transpose == 1 call in
+//     between (that call rebuilds the scratch state); otherwise GB_BAD_ARG.
 #include <string.h>
 
 #include <algorithm>
@@ -34,7 +38,13 @@ namespace {
 
 const int kMaxDevices = 64;
 unsigned char *g_scratch_ptr[kMaxDevices] = {nullptr};
-int g_support_n[kMaxDevices] = {0};  // n of the support list the last transpose == 0 call built
+// the operator of the support list the last transpose == 0 call built (cleared by a
+// transpose == 1 call, which reinitialises the scratch state)
+struct SupportKey {
+  const float *A;
+  int lda, m, n;
+};
+SupportKey g_support[kMaxDevices] = {};
 std::mutex g_scratch_mu;
 
 // device address of the scratch array for the current device (looked up once)
@@ -91,7 +101,8 @@ extern "C" gb_status gb_cs_dense_apply_noalloc(const float *d_A, int lda, int m,
   op.n = n;
   op.lda = lda;
   op.A = d_A;
-  op.vec4 = (lda % 4 == 0) && (((uintptr_t)d_A & 15) == 0);
+  // float4 streams of A, and for A^T r of the input too (A x reads its input per entry)
+  op.vec4 = (lda % 4 == 0) && (((uintptr_t)d_A & 15) == 0) && (transpose != 1 || (((uintptr_t)d_in & 15) == 0));
   gb_dense_av_shape(m, w.num_sms, false, &w.av_ntile, &w.av_nsplit, &w.av_rows);
   // carve the scratch: state | support list | tile counts | arrival counters | partial tiles
   size_t off = 0;
@@ -105,6 +116,11 @@ extern "C" gb_status gb_cs_dense_apply_noalloc(const float *d_A, int lda, int m,
   const size_t tickets_bytes = align256((size_t)w.av_ntile * 4);
   off += tickets_bytes;
   w.part = (float *)(base + off);
+  // fewer support splits until the partial tiles fit (one split, which writes no
+  // partials, fits every m <= GB_NOALLOC_MAX_M)
+  while (w.av_nsplit > 1 &&
+         off + align256(gb_dense_part_floats_av(w.av_ntile, w.av_nsplit, w.av_rows) * 4) > GB_NOALLOC_SCRATCH_BYTES)
+    --w.av_nsplit;
   w.part_cap = gb_dense_part_floats_av(w.av_ntile, w.av_nsplit, w.av_rows);
   off += align256(w.part_cap * 4);
   if (off > GB_NOALLOC_SCRATCH_BYTES) {
@@ -121,16 +137,18 @@ extern "C" gb_status gb_cs_dense_apply_noalloc(const float *d_A, int lda, int m,
   init.flags[F_ALWAYS] = 1;
   if (transpose == 2) {
     // A x on the support list of the previous transpose == 0 call: the state and the
-    // list are still in the scratch array, and the tile tickets are zero after any
-    // completed launch
+    // list are still in the scratch array when that call was for the same operator
     {
       std::lock_guard<std::mutex> lock(g_scratch_mu);
-      if (g_support_n[dev] != n) {
+      const SupportKey &k = g_support[dev];
+      if (k.A != d_A || k.lda != lda || k.m != m || k.n != n) {
         gb_set_error_message("gb_cs_dense_apply_noalloc: transpose == 2 needs a previous transpose == 0 call "
-                             "with the same n on this device", __FILE__, __LINE__);
+                             "with the same A, lda, m and n on this device (and no transpose == 1 call since)",
+                             __FILE__, __LINE__);
         return GB_BAD_ARG;
       }
     }
+    GB_CUDA_TRY(cudaMemsetAsync(w.av_tickets, 0, tickets_bytes, s));
     enq_A(w, s, d_in, d_out, nullptr, -1, F_ALWAYS);
     GB_CUDA_TRY(cudaGetLastError());
     return GB_OK;
@@ -138,12 +156,16 @@ extern "C" gb_status gb_cs_dense_apply_noalloc(const float *d_A, int lda, int m,
   GB_CUDA_TRY(cudaMemsetAsync(w.av_tickets, 0, tickets_bytes, s));
   k_init_state<<<1, 1, 0, s>>>(w.st, init);
   if (transpose) {
+    {
+      std::lock_guard<std::mutex> lock(g_scratch_mu);
+      g_support[dev] = SupportKey{};
+    }
     enq_AT(w, s, d_in, d_out, F_ALWAYS);
   } else {
     enq_support_of_nonzeros(w, s, d_in, n);
     enq_A(w, s, d_in, d_out, nullptr, -1, F_ALWAYS);
     std::lock_guard<std::mutex> lock(g_scratch_mu);
-    g_support_n[dev] = n;
+    g_support[dev] = SupportKey{d_A, lda, m, n};
   }
   GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;

@@ -8,8 +8,8 @@
  *     gaga_smv  GAGA/gaga/gaga_smv.cu:39-1198  sparse expander (d nonzeros per column)
  * each with a "generate and solve" usage and a "solve given data" usage
  * (GAGA/gaga/gaga_cs.m:7-64).  This header exports both usages as plain C calls on
- * host or device pointers.  A MEX shim maps MATLAB arrays onto
- * these calls one to one.  Names use the gb_cs_ prefix; the GAGA licence
+ * host or device pointers.  A MEX shim maps MATLAB arrays onto these calls one to one
+ * (1-based indices become 0-based there).  Names use the gb_cs_ prefix; the GAGA licence
  * (GAGA/GAGA_license:5) reserves the gaga_* function names.
  *
  * Semantics kept from the reference:
@@ -211,8 +211,9 @@ gb_status gb_cs_find_support_set_sort(float *d_v, int *d_bins, int n, int k, flo
  * resolves the array's address and must happen outside a stream capture.  All calls share
  * the array: calls that overlap on the GPU race and must be serialised by the caller.
  * transpose 2 is A in on the support (nonzero pattern) found by the previous transpose 0
- * call with the same n on this device, skipping the support scan: repeated applications
- * with a fixed support, as in a CG solve on the support. */
+ * call on this device, skipping the support scan: repeated applications with a fixed
+ * support, as in a CG solve on the support.  That call must have had the same d_A, lda, m
+ * and n, with no transpose 1 call since (GB_BAD_ARG otherwise). */
 gb_status gb_cs_dense_apply_noalloc(const float *d_A, int lda, int m, int n, int transpose,
                                     const float *d_in, float *d_out, void *stream);
 
