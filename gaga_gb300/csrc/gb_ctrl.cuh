@@ -141,6 +141,11 @@ static __device__ void finish_iteration(GbState *st, int fail_after) {
   }
 }
 
+// FIHT / ALPS step-size guard factor: 1000 in the reference's _dct forms, 400 in _gen, _smv
+static __device__ __forceinline__ float fiht_guard(const GbState *st) {
+  return st->op_kind == GB_OP_DCT ? 1000.0f : 400.0f;
+}
+
 // the binning decision shared by every algorithm: FindSupportSet's skip path
 // (GAGA/gaga/functions.cu:401-403) or a new binning with a new max (algorithms.cu:1380-1383)
 static __device__ void bin_decision(GbState *st) {
@@ -332,11 +337,14 @@ __device__ __forceinline__ void ctrl_phase(GbState *st, int phase, cudaGraphCond
     case C_CSMPSP_GBIN:
       if (!live) break;
       // max_value = MaxMagnitude(grad); minVal = 0; FindSupportSet(grad, ..., max_value)
-      // into d_bin_grad / k_bin_grad (algorithms.cu:3519-3526)
+      // into d_bin_grad / k_bin_grad (algorithms.cu:3519-3526).  CSMPSP_S_dct does not
+      // reset minVal (algorithms.cu:2907), so its FindSupportSet may skip the binning and
+      // keep the previous gradient bins and k_bin_grad.
       st->max_value = (float)st->red[R_XMAX];
-      st->min_val = 0.0f;
+      if (st->op_kind != GB_OP_DCT) st->min_val = 0.0f;
       st->slope = ((float)(st->num_bins - 1) / st->max_value);
-      st->flags[F_DOBIN] = 1;
+      st->max_change = st->max_value;
+      bin_decision(st);
       st->flags[F_KBIN_ALT] = 1;
       break;
     case C_CSMPSP_JOIN:
@@ -349,7 +357,9 @@ __device__ __forceinline__ void ctrl_phase(GbState *st, int phase, cudaGraphCond
         st->it_cg++;
         for (int j = 0; j < 15; ++j) st->evol_cg[j] = st->evol_cg[j + 1];
         st->evol_cg[15] = st->prev_cg[14] - st->prev_cg[15];
-        st->diff_cg = 10.0f;  // the reference disables the stall test here (algorithms.cu:3577)
+        // CSMPSP_S_gen disables the stall test here (algorithms.cu:3600); the _dct and _smv
+        // forms keep it (algorithms.cu:2963,3285)
+        st->diff_cg = st->op_kind == GB_OP_DENSE ? 10.0f : max_list(st->evol_cg, 16);
         st->flags[F_CG] = (st->err_cg > st->tol_cg) & (st->it_cg < 15) & (st->diff_cg > st->tol2);
       } else {
         st->flags[F_CG] = 0;
@@ -358,10 +368,13 @@ __device__ __forceinline__ void ctrl_phase(GbState *st, int phase, cudaGraphCond
       break;
     case C_CSMPSP_XBIN:
       if (!live) break;
+      // forced binning of x (algorithms.cu:3606-3612); without the minVal reset in the _dct
+      // form (algorithms.cu:2973)
       st->max_value = (float)st->red[R_XMAX];
-      st->min_val = 0.0f;
+      if (st->op_kind != GB_OP_DCT) st->min_val = 0.0f;
       st->slope = ((float)(st->num_bins - 1) / st->max_value);
-      st->flags[F_DOBIN] = 1;
+      st->max_change = st->max_value;
+      bin_decision(st);
       break;
     case C_CSMPSP_STOP:
       if (live) {
@@ -392,17 +405,20 @@ __device__ __forceinline__ void ctrl_phase(GbState *st, int phase, cudaGraphCond
       break;
     case C_FH_TAU: {
       if (!live) break;
-      // RestrictedFIHT/ALPS (GAGA/gaga/functions.cu:1680-1686)
+      // RestrictedFIHT/ALPS (GAGA/gaga/functions.cu:1680-1686); the guard is 1000 x the
+      // denominator in the _dct forms (functions.cu:1867,1948), 400 x otherwise
       float tau = (float)st->red[R_DOT1], tmp = (float)st->red[R_DOT2];
-      if (fabsf(tau) < 400.0f * fabsf(tmp)) tau = tau / tmp;
+      if (fabsf(tau) < fiht_guard(st) * fabsf(tmp)) tau = tau / tmp;
       else tau = 0.0f;
       st->cg_beta = tau;
       break;
     }
     case C_FH_MU: {
       if (!live) break;
+      // functions.cu:1733 and algorithms.cu:5633 (1000 x in the _dct forms: functions.cu:1918,
+      // algorithms.cu:5912)
       float mu = (float)st->red[R_XT], tmp = (float)st->red[R_AXT];
-      if (mu < 400.0f * tmp) mu = mu / tmp;
+      if (mu < fiht_guard(st) * tmp) mu = mu / tmp;
       else mu = 1.0f;
       st->mu = mu;
       break;

@@ -1080,7 +1080,8 @@ static void enq_csmpsp_join(SolvePlan &P, cudaStream_t s) {
   k_join<<<w.red_blocks, 256, 0, s>>>(w.st, w.bins, w.bins_prev, n);
   const int tiles = (w.op.n + GB_TILE - 1) / GB_TILE;
   k_thresh_count<<<tiles, 256, 0, s>>>(w.st, F_ALWAYS, w.x, w.bins, nullptr, n, w.tile_cnt);
-  k_compact<<<tiles, 256, 0, s>>>(w.st, F_DOBIN, w.bins, n, w.tile_cnt, w.S);
+  // the join changes the bins even when the gradient's binning was skipped
+  k_compact<<<tiles, 256, 0, s>>>(w.st, F_ALWAYS, w.bins, n, w.tile_cnt, w.S);
   enq_cg_start(w, s);
 }
 

@@ -713,6 +713,11 @@ int gbo_solve(const gbo_op *op, const float *y, int k, const gbo_opts *o, float 
     /* FIHT_S_gen / ALPS_S_gen (GAGA/gaga/algorithms.cu:5430-5706, 6263-6534) with
      * RestrictedFIHT_S_gen / RestrictedALPS_S_gen (GAGA/gaga/functions.cu:1668-1843) */
     float *x_prev = w.gp, *extra = w.gpt, *vt = w.xt;
+    /* the step-size guards are 1000 x the denominator in the _dct forms
+     * (functions.cu:1867,1918,1948,2022; algorithms.cu:5912,6741) and 400 x in the _gen
+     * and _smv forms (functions.cu:1682,1733,1765,1840,2051,2102,2132,2206;
+     * algorithms.cu:5633,6188,6463,7022) */
+    const float guard = op->kind == GBO_OP_DCT ? 1000.0f : 400.0f;
     float *Apv = (float *)calloc((size_t)m, sizeof(float));
     float *Aex = (float *)calloc((size_t)m, sizeof(float));
     float *ru = w.ru;
@@ -742,7 +747,7 @@ int gbo_solve(const gbo_op *op, const float *y, int k, const gbo_opts *o, float 
       /* extrapolated point v = x + tau (x_prev - x), tau from the residual line search */
       saxpy(m, -1.0f, ru, Apv);
       float tau = dotf(w.resid, Apv, m), tmp = dotf(Apv, Apv, m);
-      if (fabsf(tau) < 400.0f * fabsf(tmp)) tau = tau / tmp;
+      if (fabsf(tau) < guard * fabsf(tmp)) tau = tau / tmp;
       else tau = 0.0f;
       memcpy(extra, x, sizeof(float) * n);
       saxpy(n, -1.0f, x, x_prev);
@@ -774,7 +779,7 @@ int gbo_solve(const gbo_op *op, const float *y, int k, const gbo_opts *o, float 
       gbo_A(op, vt, Aex);
       float mu2 = dotf(vt, vt, n);
       tmp = dotf(Aex, Aex, m);
-      if (mu2 < 400.0f * tmp) mu2 = mu2 / tmp;
+      if (mu2 < guard * tmp) mu2 = mu2 / tmp;
       else mu2 = 1.0f;
       memcpy(x, extra, sizeof(float) * n);
       saxpy(n, mu2, w.grad, x);
@@ -793,7 +798,7 @@ int gbo_solve(const gbo_op *op, const float *y, int k, const gbo_opts *o, float 
       gbo_A(op, vt, Aex);
       mu2 = dotf(vt, vt, n);
       tmp = dotf(Aex, Aex, m);
-      if (mu2 < 400.0f * tmp) mu2 = mu2 / tmp;
+      if (mu2 < guard * tmp) mu2 = mu2 / tmp;
       else mu2 = 1.0f;
       saxpy(n, mu2, vt, x);
       saxpy(m, mu2, Aex, ru);
@@ -887,7 +892,15 @@ int gbo_solve(const gbo_op *op, const float *y, int k, const gbo_opts *o, float 
   }
 
   if (o->alg == GBO_CSMPSP) {
-    /* CSMPSP_S_gen (GAGA/gaga/algorithms.cu:3372-3688) */
+    /* CSMPSP_S_gen (GAGA/gaga/algorithms.cu:3372-3688), with the two places where the
+     * reference's operator forms differ: _gen and _smv reset minVal before both forced
+     * binnings of the loop (algorithms.cu:3540,3606; 3225,3291), _dct does not, so its
+     * FindSupportSet may skip the binning and keep the previous bins and k-th bin
+     * (algorithms.cu:2907,2973); the loop's CG projection has no stall test in _gen
+     * (algorithms.cu:3600) and has one in _dct and _smv (algorithms.cu:2963,3285). */
+    const int reset_min = op->kind != GBO_OP_DCT;
+    const int loop_stall = op->kind != GBO_OP_DENSE;
+    int k_bin_grad = 0;
     const float tol_cg = s.tol * s.tol;
     const float tol2 = 10.0f * tol_cg;
     float prevcg[16], evolcg[16], errcg, diffcg;
@@ -923,18 +936,19 @@ int gbo_solve(const gbo_op *op, const float *y, int k, const gbo_opts *o, float 
     while (keep_going(&s, iter, o->maxiter)) {
       gbo_AT(op, w.resid, w.grad);
       max_value = gbo_max_magnitude(w.grad, n);
-      bs.min_val = 0.0f;
+      if (reset_min) bs.min_val = 0.0f;
       slope = ((float)(o->num_bins - 1) / max_value);
       int k_bin_x = bs.k_bin;
+      bs.k_bin = k_bin_grad;
       gbo_find_support_set(w.grad, bins_grad, w.counters, slope, max_value, max_value, &bs, n, k);
-      int k_bin_grad = bs.k_bin;
+      k_bin_grad = bs.k_bin;
       bs.k_bin = k_bin_x;
       /* joinSupports (GAGA/gaga/kernels.cu:162-172) */
       for (int i = 0; i < n; ++i)
         if (bins_grad[i] <= k_bin_grad && w.bins[i] > bs.k_bin) w.bins[i] = bs.k_bin;
-      CSMPSP_PROJECT(0);
+      CSMPSP_PROJECT(loop_stall);
       max_value = gbo_max_magnitude(x, n);
-      bs.min_val = 0.0f;
+      if (reset_min) bs.min_val = 0.0f;
       slope = ((float)(o->num_bins - 1) / max_value);
       gbo_find_support_set(x, w.bins, w.counters, slope, max_value, max_value, &bs, n, k);
       gbo_threshold(x, w.bins, bs.k_bin, n);
