@@ -110,12 +110,11 @@ class ClockSampler:
 
 
 def wave_arrays(w):
-    """Independent trials of step w: one of PARTS interleaved waves of the 3072."""
+    """Independent trials of step w: one of PARTS interleaved waves of the 3072 (waves beyond
+    PARTS repeat the grid points with new trial ids, so no two steps share a trial)."""
     from gaga_gb300 import sweep
 
-    n, m, k, tid = sweep.sweep_trials(TOTAL - SHARED)
-    idx = sweep.wave(TOTAL - SHARED, PARTS, w % PARTS)
-    return n[idx], m[idx], k[idx], tid[idx]
+    return sweep.wave_trials(TOTAL - SHARED, PARTS, w)
 
 
 def shared_part(w):

@@ -25,7 +25,8 @@ __all__ = ["gaga_cs", "gaga_options", "GagaError", "solve_batch", "version"]
 _OPTION_NAMES = {"tol", "maxiter", "vecDistribution", "matrixEnsemble", "seed", "numBins", "threadsPerBlockn",
                  "threadsPerBlockm", "threadsPerBlocknp", "threadsPerBlockBin", "convRateNum", "kFixed", "noise",
                  "gpuNumber", "timing", "alpha", "supportFlag", "restartFlag", "projFracTol", "l0_thresh",
-                 "band_percentage", "debug_mode", "tol_is_relative", "learnedWarmStart", "resultsDir"}
+                 "band_percentage", "debug_mode", "tol_is_relative", "learnedWarmStart", "resultsDir",
+                 "watchdogPasses"}
 
 
 def version():
@@ -90,6 +91,9 @@ def _options(alg, n, opts, ens):
             o.timing = 1 if v in ("on", 1, True) else 0
         elif name == "projFracTol":
             o.proj_frac_tol = float(v)
+        elif name == "watchdogPasses":
+            # extension: bound on the device-side loop passes (0: maxiter + 4) -> GB_WATCHDOG
+            o.watchdog_passes = int(v)
         elif name == "resultsDir":
             # extension: append the reference's result line to the dated file in this directory
             o._results_dir = None if v is None else str(v).encode()

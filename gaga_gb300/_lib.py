@@ -34,7 +34,7 @@ class Options(C.Structure):
                 ("matrix_ensemble", C.c_int), ("k_fixed", C.c_int), ("seed", C.c_uint), ("noise", C.c_float),
                 ("gpu_number", C.c_int), ("conv_rate_num", C.c_int), ("alpha", C.c_float),
                 ("support_flag", C.c_int), ("timing", C.c_int), ("learned_params", C.c_void_p),
-                ("results_dir", C.c_char_p), ("proj_frac_tol", C.c_float)]
+                ("results_dir", C.c_char_p), ("proj_frac_tol", C.c_float), ("watchdog_passes", C.c_int)]
 
 
 class Problem(C.Structure):

@@ -79,6 +79,7 @@ extern "C" void gb_cs_default_options(gb_options *o, const char *alg, int n) {
   o->support_flag = 0;
   o->timing = 0;
   o->proj_frac_tol = 3.0f;
+  o->watchdog_passes = 0;
 }
 
 // ------------------------------------------------------------------ workspace
@@ -161,6 +162,15 @@ gb_status alloc_work(DeviceBuffers &db, GbWork &w, int m, int n, int lda, int nu
 
 // Normalise a problem onto the device.  Host data is copied; dense A gets a leading
 // dimension rounded up to 32 floats (128-byte aligned columns).
+// Sets *flag when a rows x cols column-major block (leading dimension ld) holds NaN or Inf:
+// one pass over the caller's data, read back with the solve's final state.
+__global__ void k_nonfinite(const float *__restrict__ a, int rows, int cols, int ld, int *flag) {
+  int bad = 0;
+  for (int j = blockIdx.x; j < cols; j += gridDim.x)
+    for (int i = threadIdx.x; i < rows; i += blockDim.x) bad |= !isfinite(__ldg(a + (size_t)j * ld + i));
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flag, 1);
+}
+
 gb_status setup_problem(DeviceBuffers &db, GbWork &w, const gb_problem &p, cudaStream_t s, int num_bins,
                         int maxiter, bool need_y = true) {
   GbOp &op = w.op;
@@ -233,6 +243,8 @@ gb_status setup_problem(DeviceBuffers &db, GbWork &w, const gb_problem &p, cudaS
         GB_CUDA_TRY(cudaMemcpy(cols.data(), p.cols, sizeof(int) * nz, cudaMemcpyDeviceToHost));
       }
     }
+    for (size_t e = 0; e < nz; ++e)
+      if (!std::isfinite(vals[e])) return bad("smv values hold non-finite values");
     for (size_t e = 0; e < nz; ++e) {
       rows[e] -= base;
       if (rows[e] < 0 || rows[e] >= m) return bad("smv row index out of range");
@@ -280,6 +292,17 @@ gb_status setup_problem(DeviceBuffers &db, GbWork &w, const gb_problem &p, cudaS
     GB_CUDA_TRY(cudaMemcpyAsync(w.y, p.y, sizeof(float) * op.m,
                                 host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
   }
+  return GB_OK;
+}
+
+// the caller's dense A and y, once, into w.nonfinite (read back after the solve)
+gb_status check_finite_inputs(DeviceBuffers &db, GbWork &w, cudaStream_t s) {
+  GB_TRY(db.alloc(&w.nonfinite, 1));
+  if (w.op.kind == GB_OP_DENSE)
+    k_nonfinite<<<std::max(1, std::min(w.num_sms * 8, w.op.n)), 256, 0, s>>>(w.op.A, w.op.m, w.op.n, w.op.lda,
+                                                                               w.nonfinite);
+  k_nonfinite<<<1, 256, 0, s>>>(w.y, w.op.m, 1, w.op.m, w.nonfinite);
+  GB_CUDA_TRY(cudaGetLastError());
   return GB_OK;
 }
 
@@ -383,6 +406,18 @@ void reset_result(gb_result *r) {
 }  // namespace
 
 // ------------------------------------------------------------------ gb_cs_solve
+// Non-finite data: the reference's loops have no check (a NaN residual ends them through
+// the comparisons of the stopping rules, GAGA/gaga/algorithms.cu:1365); here such a run
+// returns GB_BAD_ARG instead of GB_OK.  ||y|| (err_start, or norm0 for the expander
+// decoders) not finite: y holds NaN or Inf; the last residual norm not finite: A or y does.
+static gb_status check_finite_run(const GbState &st, int alg_id) {
+  const float start = gb_is_ccs(alg_id) ? st.norm0 : st.err_start;
+  const float last = gb_is_ccs(alg_id) ? st.norm : st.err;
+  if (!std::isfinite(start)) return bad("y holds non-finite values");
+  if (!std::isfinite(last)) return bad("the residual norm is not finite: A or y holds non-finite values");
+  return GB_OK;
+}
+
 extern "C" gb_status gb_cs_solve(const char *alg, const gb_problem *p, const gb_options *opts, float *x_out,
                                  gb_result *r) {
   if (!p || !x_out) return bad("null argument");
@@ -395,12 +430,16 @@ extern "C" gb_status gb_cs_solve(const char *alg, const gb_problem *p, const gb_
   else gb_cs_default_options(&o, alg, p->n);
   GB_TRY(check_options(o));
   if (p->k < 0) return bad("k must be >= 0");
+  if (p->location == GB_HOST && p->y)
+    for (int i = 0; i < p->m; ++i)
+      if (!std::isfinite(p->y[i])) return bad("y holds non-finite values");
   GB_TRY(select_device(o.gpu_number));
   cudaStream_t s = (cudaStream_t)p->stream;
   DeviceBuffers db;
   GbWork w;
   memset(&w, 0, sizeof(w));
   GB_TRY(setup_problem(db, w, *p, s, o.num_bins, o.maxiter));
+  GB_TRY(check_finite_inputs(db, w, s));
   if (gb_is_ccs(alg_id)) {
     if (o.l0_thresh < 1 || o.l0_thresh > w.op.d) o.l0_thresh = 1;  // gaga_smv.cu:313
   }
@@ -442,6 +481,8 @@ extern "C" gb_status gb_cs_solve(const char *alg, const gb_problem *p, const gb_
   }
   GB_CUDA_TRY(cudaEventRecord(e1, s));
   GB_CUDA_TRY(cudaMemcpyAsync(&st, w.st, sizeof(st), cudaMemcpyDeviceToHost, s));
+  int nonfinite = 0;
+  GB_CUDA_TRY(cudaMemcpyAsync(&nonfinite, w.nonfinite, sizeof(int), cudaMemcpyDeviceToHost, s));
   GB_CUDA_TRY(cudaMemcpyAsync(x_out, w.x, sizeof(float) * p->n,
                               p->location == GB_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
   std::vector<float> rec;
@@ -479,7 +520,9 @@ extern "C" gb_status gb_cs_solve(const char *alg, const gb_problem *p, const gb_
     }
     r->conv_rate = conv_rate_from(r->resid_prev, st.iter, 16);
   }
+  if (nonfinite) return bad("A or y holds non-finite values");
   if (st.status == GB_WATCHDOG) return bad("device iteration bound reached", GB_WATCHDOG);
+  GB_TRY(check_finite_run(st, alg_id));
   return GB_OK;
 }
 

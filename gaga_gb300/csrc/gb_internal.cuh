@@ -144,6 +144,7 @@ struct GbWork {
   int dyn;          // 1: kernels read m, n, lda, num_bins, k of the current trial from GbState
   const float *ml_params;    // learned warm start: MLP parameters (null: plain start)
   int *ml_counts, *ml_cum;   // its rank histogram (4096 bins) and prefix
+  int *nonfinite;   // set when the caller's A or y holds NaN / Inf (gb_cs_solve)
   int num_sms;
   int red_blocks;   // grid of reducing kernels (fixed -> deterministic reductions)
   int wide_blocks;  // grid of the dense streaming kernels

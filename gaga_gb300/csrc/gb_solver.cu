@@ -1695,7 +1695,7 @@ static GbState initial_state(const GbWork &w, int alg, const gb_options &o, int 
   st.tol = tol_abs;
   st.active = 1;
   st.cycle = 1;
-  st.pass_limit = o.maxiter + 4;
+  st.pass_limit = o.watchdog_passes > 0 ? o.watchdog_passes : o.maxiter + 4;
   st.resid_diff = 1.0f;
   for (int j = 0; j < 16; ++j) { st.prev[j] = 0.0f; st.evol[j] = 1.0f; }
   // ThresholdSD / ThresholdCG start with alpha = 0 (MaxBin = num_bins, algorithms.cu:800-802)

@@ -37,6 +37,16 @@ def wave(total, waves, w):
     return np.arange(w, total, waves)
 
 
+def wave_trials(total, waves, w):
+    """Arrays (n, m, k, trial_id) of wave w of a sweep of `total` trials split into `waves`
+    interleaved waves.  Waves w and w + waves cover the same grid points with distinct
+    trials: the trial ids of round w // waves are offset by that many sweeps, so every wave
+    index names its own seeded problems (ranks beyond the wave count never repeat a trial)."""
+    n, m, k, tid = sweep_trials(total)
+    idx = wave(total, waves, w % waves)
+    return n[idx], m[idx], k[idx], (tid[idx] + np.uint32((w // waves) * total)).astype(np.uint32)
+
+
 def shard(indices, rank, world):
     """Trials of one rank: every world-th index starting at rank."""
     indices = np.asarray(indices)

@@ -82,6 +82,9 @@ typedef struct {
                            line to the dated file in this directory ("" = current directory,
                            as the reference always does); NULL = no file */
   float proj_frac_tol;  /* 'projFracTol'    3 (CGIHTprojected, gaga_gen.cu:190) */
+  int watchdog_passes;  /* extension: bound on the device-side passes of a solve's loop
+                           (0: maxiter + 4); a loop still running past it stops with
+                           GB_WATCHDOG.  The reference's host loop has no such bound. */
 } gb_options;
 
 /* A recovery problem in "given data" form. */

@@ -110,9 +110,10 @@ void run_launch(dim3 g, dim3 b, const void *kernel, const std::function<void()> 
   const bool first = g_seen.insert(kernel).second;
   g_barrier_hit = false;
   if (!direct) ensure_fibers(nt);
-  for (unsigned bz = 0; bz < g.z; ++bz)
-    for (unsigned by = 0; by < g.y; ++by)
-      for (unsigned bx = 0; bx < g.x; ++bx) {
+  // the scheduler's locals live in memory (volatile): _setjmp / _longjmp restore registers
+  for (volatile unsigned bz = 0; bz < g.z; ++bz)
+    for (volatile unsigned by = 0; by < g.y; ++by)
+      for (volatile unsigned bx = 0; bx < g.x; ++bx) {
         blockIdx.x = bx;
         blockIdx.y = by;
         blockIdx.z = bz;
@@ -126,10 +127,10 @@ void run_launch(dim3 g, dim3 b, const void *kernel, const std::function<void()> 
           continue;
         }
         for (int t = 0; t < nt; ++t) g_fibers[t]->state = F_RUN;
-        int live = nt;
+        volatile int live = nt;
         while (live > 0) {
-          for (int t = 0; t < nt; ++t) {
-            Fiber *f = g_fibers[t];
+          for (volatile int t = 0; t < nt; ++t) {
+            Fiber *volatile f = g_fibers[t];
             if (f->state == F_DONE) continue;
             f->state = F_RUN;
             set_thread(t, b);
@@ -253,6 +254,18 @@ int mexPrintf(const char *fmt, ...) {
   va_end(ap);
   return r;
 }
+
+static char g_mex_error[1024];
+void mexErrMsgIdAndTxt(const char *id, const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  int off = snprintf(g_mex_error, sizeof g_mex_error, "%s: ", id);
+  if (off < 0) off = 0;
+  vsnprintf(g_mex_error + off, sizeof g_mex_error - off, fmt, ap);
+  va_end(ap);
+}
+const char *gbmx_last_error(void) { return g_mex_error; }
+void gbmx_clear_error(void) { g_mex_error[0] = 0; }
 
 mxArray *gbmx_numeric(int cls, int m, int n, const void *data) {
   mxArray *a = mxCreateNumericMatrix(m, n, (mxClassID)cls, mxREAL);

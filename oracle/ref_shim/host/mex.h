@@ -42,6 +42,11 @@ int mxIsCell(const mxArray *a);
 mxArray *mxGetCell(const mxArray *a, size_t index);
 size_t mxCalcSingleSubscript(const mxArray *a, size_t nsubs, const int *subs);
 int mexPrintf(const char *fmt, ...);
+/* the gateway's entry point, with C linkage as MATLAB declares it */
+void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]);
+/* MATLAB raises an error and leaves the MEX function; the stand-in records the message
+ * (gbmx_last_error) and returns, so a gateway returns right after calling it */
+void mexErrMsgIdAndTxt(const char *id, const char *fmt, ...);
 
 /* test-side construction of arguments (not part of MATLAB's API) */
 mxArray *gbmx_numeric(int cls, int m, int n, const void *data);
@@ -49,6 +54,8 @@ mxArray *gbmx_string(const char *s);
 mxArray *gbmx_cell(int m, int n);
 void gbmx_cell_set(mxArray *cell, int index, mxArray *elem);
 int gbmx_class(const mxArray *a);
+const char *gbmx_last_error(void);
+void gbmx_clear_error(void);
 void gbmx_free(mxArray *a);
 #ifdef __cplusplus
 }

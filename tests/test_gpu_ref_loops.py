@@ -12,7 +12,10 @@ import ref_loops_fixture as F
 
 pytestmark = pytest.mark.gpu
 
-ALL = F.cases()
+# serial_l0 is Gauss-Seidel, sequential by construction; the reference runs it on the host
+# (GAGA/gaga/gaga_smv.cu:951) and this library does not offer it on the GPU (the oracle's
+# restatement is pinned to the reference in tests/test_oracle_ref_loops.py)
+ALL = [c for c in F.cases() if c["alg"] != "serial_l0"]
 
 
 @pytest.mark.parametrize("case", ALL, ids=[c["id"] for c in ALL])

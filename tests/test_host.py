@@ -212,3 +212,31 @@ def test_timing_result_file_lines_match_reference_format(gb, tmp_path):
     # without the per-iteration arrays the timing file cannot be written
     r.time_per_iteration = None
     assert L.gb_cs_write_result(d, b"NIHT", 0, 20, 1024, 4096, 0, C.byref(o), C.byref(r), buf, 512) != 0
+
+
+def test_mex_shim_builds_and_rejects_bad_calls(gb):
+    """The MEX gateways (gaga_gb300/mex/gb_gaga_mex.cpp) compile against a MATLAB API
+    (the stand-in mex.h) with -Wall -Wextra -Werror and link to libgb_cs.so.  Calls that
+    the reference rejects (unknown algorithm, wrong output count, GAGA/gaga/gaga_gen.cu:49-50,
+    85-87) raise the gateway error and leave every output unset; none reaches the GPU."""
+    import numpy as np
+
+    import mex_shim
+    from oracle import ref_gateway as rg
+
+    for g in ("gen", "dct", "smv"):
+        L = mex_shim.load(g)
+        y = np.ones(8, np.float32)
+        if g == "gen":
+            args = rg.gen_args(L, "NOT_AN_ALG", y, np.ones((8, 16), np.float32), 2)
+        elif g == "dct":
+            args = rg.dct_args(L, "NOT_AN_ALG", y, np.arange(1, 9, dtype=np.int32), 2, 8, 16)
+        else:
+            cols = np.repeat(np.arange(1, 17, dtype=np.int32), 2)
+            args = rg.smv_args(L, "NOT_AN_ALG", y, np.ones(32, np.int32), cols, np.ones(32, np.float32), 2)
+        L.gbmx_clear_error()
+        outs = rg.call(L, 5 if g == "smv" else 3, args)
+        assert all(o is None for o in outs) and b"unknown algorithm" in L.gbmx_last_error()
+        L.gbmx_clear_error()
+        outs = rg.call(L, 2, rg.gen_args(L, "NIHT", y, np.ones((8, 16), np.float32), 2))
+        assert all(o is None for o in outs) and b"usage" in L.gbmx_last_error()

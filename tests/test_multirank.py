@@ -70,3 +70,19 @@ def test_rank_waves_are_disjoint():
     assert len(set(waves)) == world * steps
     parts = [set(sweep.shard(np.arange(100), r, 3)) for r in range(3)]
     assert set().union(*parts) == set(range(100)) and sum(len(p) for p in parts) == 100
+
+
+@pytest.mark.parametrize("world", [2, 4, 8, 16])
+def test_rank_trials_are_disjoint(world):
+    """Every rank's waves hold distinct trials for any world size: the trial ids (the seeds
+    of A and x) never repeat across ranks and steps, while the grid points do."""
+    from gaga_gb300 import sweep
+
+    steps, total, parts = 3, 3072, 4
+    seen = []
+    for r in range(world):
+        for s in range(steps):
+            n, m, k, tid = sweep.wave_trials(total, parts, sweep.rank_wave(r, world, s))
+            assert len(tid) == total // parts
+            seen.extend(tid.tolist())
+    assert len(seen) == len(set(seen))
