@@ -54,7 +54,8 @@ def _solve(gb, gbo, kind, alg, y=None, A=None, **opt):
         opts = gb.gaga_options("tol", 1e-4 * float(np.linalg.norm(y0)), *[v for kv in opt.items() for v in kv])
         return lambda: gb.gaga_cs(alg, "dct", y, rows, ks, op.m, op.n, opts, index_base=0)
     ens = 3 if alg == "parallel_l0" else 1
-    op, rows, vals, x0, ks, y0 = _smv(gbo, ens=ens)
+    # parallel_l0 at k = 204 takes 7 iterations (at k = 60, 2)
+    op, rows, vals, x0, ks, y0 = _smv(gbo, k=204, seed=7, ens=3) if ens == 3 else _smv(gbo)
     y = y0 if y is None else y
     cols = np.repeat(np.arange(op.n, dtype=np.int32), 7)
     opts = gb.gaga_options("tol", 1e-6 if ens == 3 else 1e-4 * float(np.linalg.norm(y0)),
@@ -67,7 +68,7 @@ def _solve(gb, gbo, kind, alg, y=None, A=None, **opt):
 def test_pass_watchdog_returns_status(gb, gbo, kind, alg):
     """watchdog_passes bounds the passes of the device-side loop: a solve that needs more
     stops with GB_WATCHDOG; the same solve without the bound then completes."""
-    st, msg = _status(gb, _solve(gb, gbo, kind, alg, watchdogPasses=2))
+    st, msg = _status(gb, _solve(gb, gbo, kind, alg, watchdogPasses=1))
     assert st == gb._lib.GB_WATCHDOG, (st, msg)
     assert "iteration bound" in msg
     st, msg = _status(gb, _solve(gb, gbo, kind, alg))
