@@ -339,36 +339,49 @@ def batch_last_stats():
 
 
 def solve_shared_batch(m, n, k, seed, tol_rel=1e-4, maxiter=5000, precision=3, outputs=False, first_trial=0,
-                       stream=None):
-    """Shared-matrix batched form (gb_cs_solve_shared_batch): len(k) NIHT trials with one
-    dense Gaussian A, operator work as BF16 tensor-core GEMMs, least-squares debias.
+                       stream=None, alg="NIHT", learned_params=None):
+    """Shared-matrix batched form (gb_cs_solve_shared_batch): len(k) NIHT or CGIHT trials
+    with one dense Gaussian A, operator work as BF16 tensor-core GEMMs, least-squares debias.
     precision: bit 0 splits A^T r, bit 1 splits A x_thres into BF16 high/low parts.
+    learned_params: CGIHT's warm-start network (a CUDA tensor, gaga_gb300.learned), or None.
 
     Returns (num_success, iters, rel_err, ok) and, with outputs=True, also the generated
-    A (m x n column-major, as an (n, m) CUDA tensor), Y (T x m) and X0 (T x n) on the device.
+    A (m x n column-major, as an (n, m) CUDA tensor), Y (T x m) and X0 (T x n) on the device;
+    with outputs="x" also the final X (T x n).
     """
     L = _lib.load()
     k = np.ascontiguousarray(k, dtype=np.int32)
     T = len(k)
-    A = Y = X0 = None
+    A = Y = X0 = X = None
     if outputs:
         import torch
         A = torch.empty((n, m), dtype=torch.float32, device="cuda")
         Y = torch.empty((T, m), dtype=torch.float32, device="cuda")
         X0 = torch.empty((T, n), dtype=torch.float32, device="cuda")
+        if outputs == "x":
+            X = torch.empty((T, n), dtype=torch.float32, device="cuda")
     b = _lib.SharedBatch(T, int(m), int(n), k.ctypes.data, int(seed) & 0xFFFFFFFF, int(first_trial) & 0xFFFFFFFF,
                          float(tol_rel), int(maxiter),
                          int(precision), None if A is None else A.data_ptr(), None if Y is None else Y.data_ptr(),
-                         None if X0 is None else X0.data_ptr(), stream)
+                         None if X0 is None else X0.data_ptr(), stream, {"NIHT": 0, "CGIHT": 6}[alg],
+                         None if learned_params is None else learned_params.data_ptr(),
+                         None if X is None else X.data_ptr())
     iters = np.zeros(T, dtype=np.int32)
     err = np.zeros(T, dtype=np.float32)
     ok = np.zeros(T, dtype=np.int32)
     ns = C.c_int(0)
     _lib.check(L.gb_cs_solve_shared_batch(C.byref(b), C.c_void_p(iters.ctypes.data), C.c_void_p(err.ctypes.data),
                                           C.c_void_p(ok.ctypes.data), C.byref(ns)))
+    if outputs == "x":
+        return ns.value, iters, err, ok, A, Y, X0, X
     if outputs:
         return ns.value, iters, err, ok, A, Y, X0
     return ns.value, iters, err, ok
+
+
+def shared_last_fallbacks():
+    """Trials of the last solve_shared_batch call whose learned warm start was abandoned."""
+    return int(_lib.load().gb_cs_shared_last_fallbacks())
 
 
 def shared_last_stats():

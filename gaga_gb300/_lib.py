@@ -24,6 +24,7 @@ EXPORTS = ["gb_cs_version", "gb_cs_last_error", "gb_cs_default_options", "gb_cs_
            "gb_cs_operator_apply", "gb_cs_operator_time", "gb_cs_l0_step", "gb_cs_solve_batch", "gb_cs_batch_last_stats",
            "gb_cs_batch_last_cluster",
            "gb_cs_dense_apply_noalloc", "gb_cs_solve_shared_batch", "gb_cs_shared_last_stats",
+           "gb_cs_shared_last_fallbacks",
            "gb_cs_gemm_bf16_tn", "gb_cs_mlp_num_params", "gb_cs_mlp_features", "gb_cs_mlp_forward",
            "gb_cs_mlp_grad", "gb_cs_mlp_train", "gb_cs_write_result"]
 
@@ -69,7 +70,8 @@ class SharedBatch(C.Structure):
     _fields_ = [("ntrials", C.c_int), ("m", C.c_int), ("n", C.c_int), ("k", C.c_void_p), ("seed", C.c_uint),
                 ("first_trial", C.c_uint),
                 ("tol_rel", C.c_float), ("maxiter", C.c_int), ("precision", C.c_int), ("d_A_out", C.c_void_p), ("d_Y_out", C.c_void_p),
-                ("d_X0_out", C.c_void_p), ("stream", C.c_void_p)]
+                ("d_X0_out", C.c_void_p), ("stream", C.c_void_p), ("alg", C.c_int), ("learned_params", C.c_void_p),
+                ("d_X_out", C.c_void_p)]
 
 
 _lib = None
@@ -118,6 +120,8 @@ def load():
     L.gb_cs_solve_shared_batch.restype = i
     L.gb_cs_shared_last_stats.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_float)]
     L.gb_cs_shared_last_stats.restype = None
+    L.gb_cs_shared_last_fallbacks.argtypes = []
+    L.gb_cs_shared_last_fallbacks.restype = i
     L.gb_cs_gemm_bf16_tn.argtypes = [vp, vp, vp, i, i, i, vp, vp, vp]
     L.gb_cs_gemm_bf16_tn.restype = i
     L.gb_cs_mlp_num_params.argtypes = []

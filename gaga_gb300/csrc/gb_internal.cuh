@@ -84,6 +84,10 @@ struct GbState {
   // learned warm start (CGIHT): on, gave up after 10 iterations, residual at the warm x0
   int learned, fell_back;
   float err_warm0;
+  // shared-matrix CGIHT: iterations of an abandoned warm start (counted with the plain
+  // restart's), a pass that only ran the restart's prologue, GEMM flops of this trial
+  int warm_iters, sh_prologue;
+  double sh_flops;
   // CGIHTprojected projFracTol; ALPS: the outer bin state kept across its local binning
   float proj_frac_tol, sv_alpha, sv_min_val;
   int sv_max_bin, sv_k_bin;

@@ -17,6 +17,15 @@
 // arithmetic is a small fraction of the FP32 rate on this part, so no product runs in
 // it).  The verdict is the relative l2 error against the planted x0.
 //
+// CGIHT (restartFlag off, GAGA/gaga/algorithms.cu:3689-3942) runs in lockstep the same
+// way, with four products per pass: the residual R and G = A^T R for every active trial,
+// then Q = A p for the direction on the support (the restricted-CG branch's new direction,
+// the unrestricted branch's previous one) and, for the trials in the unrestricted branch
+// only, Q2 = A g_S (functions.cu:1004-1220).  With the learned warm start the prologue
+// starts each trial from H_k(w . A^T y) (w from the per-coordinate network, gb_mlp.cuh);
+// a trial that gives it up after 10 iterations is restarted inside the loop from the plain
+// start H_k(A^T y), its iterations added.
+//
 // The shared A is drawn from `seed` exactly as gb_cs_generate_and_solve draws it; trial
 // t's x0 uses the key seed + 1 + first_trial + t.
 #include <cuda_bf16.h>
@@ -27,6 +36,7 @@
 #include <vector>
 
 #include "gb_ctrl.cuh"
+#include "gb_mlp.cuh"
 #include "gb_philox.cuh"
 
 #define SH_THREADS 256
@@ -53,6 +63,17 @@ struct ShDev {
   float *P;                 // debias search directions, Tp x n
   __nv_bfloat16 *Rcat;      // debias residual split, Tp x 3m
   int *act, *act_cnt;       // trials still iterating (ascending) and their count
+  int alg;                  // GB_ALG_NIHT or GB_ALG_CGIHT
+  const float *ml;          // CGIHT: learned warm start's network parameters (null: plain start)
+  float *GP, *GPT;          // CGIHT: grad_previous and grad_prev_thres (Tp x n)
+  float *G0;                // CGIHT with the learned start: A^T y, the plain restart's start
+  float *Q2;                // CGIHT: A g_S of the unrestricted-branch trials (Tp x m)
+  __nv_bfloat16 *XT2;       // its BF16 operand (Tp x kq)
+  int *bins_prev;           // CGIHT: bins before this pass's binning (support evolution)
+  GbState *st0;             // CGIHT with the learned start: each trial's plain initial state
+  int *act_q, *act_q_cnt;   // CGIHT: trials whose pass runs the direction product
+  int *act_u, *act_u_cnt;   // CGIHT: the unrestricted-branch trials among them
+  int *fallbacks;           // CGIHT: trials restarted from the plain start
   int *iters;
   float *err;
   int *ok;
@@ -306,7 +327,8 @@ __global__ void __launch_bounds__(SH_THREADS) k_sh_y(ShDev d) {
     st->m = m; st->n = n; st->k = ks; st->lda = m;
     st->num_bins = max(n / 20, 1000);
     st->maxiter = d.maxiter;
-    st->alg = GB_ALG_NIHT;
+    st->alg = d.alg;
+    st->learned = d.ml ? 1 : 0;
     st->tol = d.tol_rel * (float)sqrt(ys);
     st->active = 1; st->cycle = 1; st->pass_limit = d.maxiter + 4;
     st->resid_diff = 1.0f;
@@ -428,14 +450,389 @@ __global__ void __launch_bounds__(SH_THREADS) k_sh_step(ShDev d) {
   }
 }
 
-// Ordered list of the trials still iterating (NIHT: active; debias: F_CG) for the GEMMs'
-// column maps, and the loop condition: any trial left (NIHT also bounded by maxiter + 4
-// passes).  One block of 1024 threads, each owning a contiguous run of trials.
-__global__ void __launch_bounds__(1024) k_sh_list(ShDev d, int which, int *passes, cudaGraphConditionalHandle h) {
+// ------------------------------------------------------------------ CGIHT in lockstep
+__device__ __forceinline__ void put_bf(__nv_bfloat16 *row, int n, int j, float v, bool split) {
+  const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+  if (split) {
+    row[j] = hi;
+    row[n + j] = hi;
+    row[2 * n + j] = __float2bfloat16_rn(v - __bfloat162float(hi));
+  } else {
+    row[j] = hi;
+  }
+}
+
+// cta_support with CGIHT's support evolution: the bins before a new binning go to
+// bins_prev, and st->changed is set when an entry of the previous support (bin <=
+// k_bin_prev) left it (checkSupportEvolution, GAGA/gaga/kernels.cu:178-193)
+__device__ void cta_support_evol(GbState *st, float *x, int *bins, int *bins_prev, int n, __nv_bfloat16 *xcat,
+                                 int *hist, int *scan) {
+  const bool dobin = st->flags[F_DOBIN] != 0;
+  if (dobin) {
+    const int max_bin = st->max_bin;
+    for (int b = threadIdx.x; b < max_bin; b += SH_THREADS) hist[b] = 0;
+    __syncthreads();
+    const float intercept = st->max_value, slope = st->slope;
+    const float small_f = __double2float_rd((double)intercept * 0.000001);
+    for (int j = threadIdx.x; j < n; j += SH_THREADS) {
+      bool counted;
+      const int b = lin_bin(x[j], slope, intercept, small_f, counted);
+      bins_prev[j] = bins[j];
+      bins[j] = b;
+      if (counted && b < max_bin) atomicAdd(&hist[b], 1);
+    }
+    __syncthreads();
+    int k_bin, sum;
+    cta_kbin(hist, max_bin, st->k, &k_bin, &sum, scan);
+    if (threadIdx.x == 0) {
+      if (sum < st->k) {
+        st->alpha_bin = st->alpha_bin * 0.5f;
+        st->max_bin = (int)((float)st->num_bins * (1.0f - st->alpha_bin));
+      }
+      st->min_val = intercept - (float)(k_bin + 1) / slope;
+      st->k_bin = k_bin;
+      st->sum = sum;
+    }
+    __syncthreads();
+  }
+  const int kb = st->k_bin, kbp = st->k_bin_prev;
+  int changed = 0;
+  for (int j = threadIdx.x; j < n; j += SH_THREADS) {
+    float v = x[j];
+    const int b = bins[j];
+    if (b > kb) {
+      v = 0.0f;
+      x[j] = 0.0f;
+    }
+    if (dobin && bins_prev[j] <= kbp && b > kb) changed = 1;
+    const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+    xcat[j] = hi;
+    xcat[n + j] = hi;
+    xcat[2 * n + j] = __float2bfloat16_rn(v - __bfloat162float(hi));
+  }
+  changed = __syncthreads_or(changed);
+  if (threadIdx.x == 0 && changed) st->changed = 1;
+  __syncthreads();
+}
+
+// the start x = H_k(v) of a trial (FindSupportSet + Threshold, algorithms.cu:3776-3790)
+// from v already in x; every thread calls it
+__device__ void cta_start_support(ShDev &d, int t, GbState *st, float *x, int *hist, int *scan, float *sm) {
+  const int n = d.n;
+  float mx = 0.0f;
+  for (int j = threadIdx.x; j < n; j += SH_THREADS) mx = fmaxf(mx, fabsf(x[j]));
+  mx = cta_max(mx, sm);
+  if (threadIdx.x == 0) {
+    st->red[R_XMAX] = mx;
+    ctrl_phase(st, C_INIT_BINPREP, 0);
+  }
+  __syncthreads();
+  cta_support(st, x, d.bins + (size_t)t * n, n, d.Xcat + (size_t)t * 3 * n, hist, scan);
+}
+
+// CGIHT prologue, first part: x = A^T y (G), with the learned start x = g . net(features
+// of g) (the single-trial k_ml_rank_hist / k_ml_warm in one CTA), then H_k(x).  The
+// plain initial state is kept for a fallback.  Dynamic shared memory: the network's
+// parameters, then the rank histogram and its prefix (reused for the bin counts).
+__global__ void __launch_bounds__(SH_THREADS) k_sc_init(ShDev d) {
+  extern __shared__ float dyn[];
+  __shared__ float sm[32];
+  __shared__ int scan[SH_THREADS];
+  const int t = blockIdx.x, n = d.n;
+  if (t >= d.T) return;
+  GbState *st = d.st + t;
+  float *x = d.X + (size_t)t * n;
+  const float *g = d.G + (size_t)t * n;
+  int *counts = (int *)(dyn + (d.ml ? ML_P : 0));
+  int *cum = counts + ML_RANK_BINS;
+  if (threadIdx.x == 0) {
+    ctrl_phase(st, C_INIT0, 0);
+    if (d.ml) {
+      d.st0[t] = *st;
+      d.st0[t].learned = 0;
+    }
+  }
+  float mx = 0.0f;
+  for (int j = threadIdx.x; j < n; j += SH_THREADS) {
+    const float v = g[j];
+    x[j] = v;
+    if (d.ml) d.G0[(size_t)t * n + j] = v;
+    mx = fmaxf(mx, fabsf(v));
+  }
+  mx = cta_max(mx, sm);
+  if (d.ml) {
+    // rank histogram of |g| below max|g| (bin 0: the largest), its exclusive prefix
+    int *rb = d.bins + (size_t)t * n;
+    for (int b = threadIdx.x; b < ML_RANK_BINS; b += SH_THREADS) counts[b] = 0;
+    __syncthreads();
+    const float slope = mx > 0.0f ? (float)(ML_RANK_BINS - 1) / mx : 0.0f;
+    for (int j = threadIdx.x; j < n; j += SH_THREADS) {
+      int b = (int)((mx - fabsf(g[j])) * slope);
+      b = min(max(b, 0), ML_RANK_BINS - 1);
+      rb[j] = b;
+      atomicAdd(&counts[b], 1);
+    }
+    __syncthreads();
+    constexpr int PER = ML_RANK_BINS / SH_THREADS;
+    int c[PER], tot = 0;
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      c[q] = counts[threadIdx.x * PER + q];
+      tot += c[q];
+    }
+    scan[threadIdx.x] = tot;
+    __syncthreads();
+    for (int off = 1; off < SH_THREADS; off <<= 1) {
+      const int v = threadIdx.x >= off ? scan[threadIdx.x - off] : 0;
+      __syncthreads();
+      scan[threadIdx.x] += v;
+      __syncthreads();
+    }
+    int run = scan[threadIdx.x] - tot;
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      cum[threadIdx.x * PER + q] = run;
+      run += c[q];
+    }
+    ml_load_params(d.ml, dyn);
+    const float delta = (float)d.m / (float)n, rho = (float)st->k / (float)d.m;
+    for (int j = threadIdx.x; j < n; j += SH_THREADS) {
+      const float gi = g[j];
+      float f[ML_IN];
+      ml_features(gi, mx, rb[j], cum, counts, n, delta, rho, f);
+      x[j] = gi * ml_forward1(dyn, f);
+    }
+    __syncthreads();
+  }
+  cta_start_support(d, t, st, x, counts, scan, sm);
+}
+
+// grad_previous = A^T r0, grad_prev_thres, and CGIHT's loop start (algorithms.cu:3791-3808)
+__device__ void cta_cgiht_prologue(ShDev &d, int t, GbState *st, float r2) {
+  const int n = d.n;
+  const float *g = d.G + (size_t)t * n;
+  float *gp = d.GP + (size_t)t * n, *gpt = d.GPT + (size_t)t * n;
+  const int *bins = d.bins + (size_t)t * n;
+  const int kb = st->k_bin;
+  for (int j = threadIdx.x; j < n; j += SH_THREADS) {
+    const float v = g[j];
+    gp[j] = v;
+    gpt[j] = bins[j] <= kb ? v : 0.0f;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    st->red[R_RES] = r2;
+    ctrl_phase(st, C_CGIHT_INIT, 0);
+  }
+  __syncthreads();
+}
+
+// CGIHT prologue, second part: after R = Y - A x and G = A^T R of every trial
+__global__ void __launch_bounds__(SH_THREADS) k_sc_init2(ShDev d) {
+  __shared__ float sm[32];
+  const int t = blockIdx.x, m = d.m;
+  if (t >= d.T) return;
+  GbState *st = d.st + t;
+  const float *r = d.R + (size_t)t * m;
+  float r2 = 0.0f;
+  for (int i = threadIdx.x; i < m; i += SH_THREADS) r2 = fmaf(r[i], r[i], r2);
+  r2 = cta_sum(r2, sm);
+  cta_cgiht_prologue(d, t, st, r2);
+}
+
+// CGIHT pass, first part (after R and G): ||r||^2 into the history; the restricted branch's
+// beta and new direction p (functions.cu:1020-1074), or the unrestricted branch's operands
+// p_prev_S and g_S (functions.cu:1134-1147); the direction product(s) follow
+__global__ void __launch_bounds__(SH_THREADS) k_sc_dir(ShDev d) {
+  __shared__ float sm[32];
+  const int t = blockIdx.x, n = d.n, m = d.m;
+  if (t >= d.T) return;
+  GbState *st = d.st + t;
+  if (!st->active) return;
+  const float *r = d.R + (size_t)t * m;
+  float r2 = 0.0f;
+  for (int i = threadIdx.x; i < m; i += SH_THREADS) r2 = fmaf(r[i], r[i], r2);
+  r2 = cta_sum(r2, sm);
+  if (st->fell_back == 1) {
+    // plain restart after an abandoned warm start: this pass is its prologue
+    cta_cgiht_prologue(d, t, st, r2);
+    if (threadIdx.x == 0) {
+      st->fell_back = 2;
+      st->sh_prologue = 1;
+    }
+    return;
+  }
+  if (threadIdx.x == 0) {
+    st->red[R_RES] = r2;
+    ctrl_phase(st, C_PUSH_RES, 0);
+  }
+  const float *g = d.G + (size_t)t * n;
+  const int *bins = d.bins + (size_t)t * n;
+  const int kb = st->k_bin;
+  const bool split = (d.prec & 2) != 0;
+  const size_t row = (size_t)t * (split ? 3 * n : n);
+  float s2 = 0.0f;
+  for (int j = threadIdx.x; j < n; j += SH_THREADS) {
+    const float o = bins[j] <= kb ? g[j] : 0.0f;
+    s2 = fmaf(o, o, s2);
+  }
+  s2 = cta_sum(s2, sm);
+  if (threadIdx.x == 0) {
+    st->red[R_XT] = s2;
+    ctrl_phase(st, C_RCG_BETA, 0);
+  }
+  __syncthreads();
+  float *gp = d.GP + (size_t)t * n, *gpt = d.GPT + (size_t)t * n;
+  if (st->flags[F_RCG]) {
+    const float beta = st->cg_beta;
+    float gm = 0.0f;
+    for (int j = threadIdx.x; j < n; j += SH_THREADS) {
+      const float v = fmaf(1.0f, g[j], beta * gp[j]);
+      gp[j] = v;
+      const float pt = bins[j] <= kb ? v : 0.0f;
+      gpt[j] = pt;
+      put_bf(d.XTbf + row, n, j, pt, split);
+      gm = fmaxf(gm, fabsf(v));
+    }
+    gm = cta_max(gm, sm);
+    if (threadIdx.x == 0) st->red[R_GMAX] = gm;
+  } else {
+    for (int j = threadIdx.x; j < n; j += SH_THREADS) {
+      put_bf(d.XTbf + row, n, j, gpt[j], split);
+      put_bf(d.XT2 + row, n, j, bins[j] <= kb ? g[j] : 0.0f, split);
+    }
+  }
+}
+
+// CGIHT pass, second part (after Q = A p, and Q2 = A g_S for the unrestricted branch):
+// alpha (and the unrestricted branch's beta, direction and A p), x += alpha p, the
+// support and its evolution, the stopping rules; a learned start given up after 10
+// iterations restarts from the plain start H_k(A^T y)
+__global__ void __launch_bounds__(SH_THREADS) k_sc_step(ShDev d) {
+  __shared__ float sm[32];
+  __shared__ int hist[SH_NBINS_MAX];
+  __shared__ int scan[SH_THREADS];
+  const int t = blockIdx.x, n = d.n, m = d.m;
+  if (t >= d.T) return;
+  GbState *st = d.st + t;
+  if (!st->active) return;
+  if (st->sh_prologue) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      st->sh_prologue = 0;
+      st->sh_flops += 2.0 * (3.0 * m * (double)n + (double)n * d.kg);
+    }
+    return;
+  }
+  const float *q = d.Q + (size_t)t * m;
+  const float *g = d.G + (size_t)t * n;
+  int *bins = d.bins + (size_t)t * n;
+  float *gp = d.GP + (size_t)t * n, *gpt = d.GPT + (size_t)t * n;
+  const int kb = st->k_bin;
+  const bool ucg = st->flags[F_UCG] != 0;
+  if (!ucg) {
+    float q2 = 0.0f;
+    for (int i = threadIdx.x; i < m; i += SH_THREADS) q2 = fmaf(q[i], q[i], q2);
+    q2 = cta_sum(q2, sm);
+    if (threadIdx.x == 0) {
+      st->red[R_AXT] = q2;
+      ctrl_phase(st, C_RCG_ALPHA, 0);
+    }
+  } else {
+    // beta = -<A p_prev_S, A g_S> / ||A p_prev_S||^2 (functions.cu:1169-1178)
+    const float *q2u = d.Q2 + (size_t)t * m;
+    float d1 = 0.0f, d2 = 0.0f;
+    for (int i = threadIdx.x; i < m; i += SH_THREADS) {
+      d1 = fmaf(q[i], q2u[i], d1);
+      d2 = fmaf(q[i], q[i], d2);
+    }
+    d1 = cta_sum(d1, sm);
+    d2 = cta_sum(d2, sm);
+    if (threadIdx.x == 0) {
+      st->red[R_DOT1] = d1;
+      st->red[R_DOT2] = d2;
+      ctrl_phase(st, C_UCG_BETA, 0);
+    }
+    __syncthreads();
+    const float beta = st->cg_beta;
+    float gm = 0.0f, d3 = 0.0f, d4 = 0.0f;
+    for (int j = threadIdx.x; j < n; j += SH_THREADS) {
+      const float v = fmaf(1.0f, g[j], beta * gp[j]);
+      gp[j] = v;
+      const float pt = bins[j] <= kb ? v : 0.0f;
+      gpt[j] = pt;
+      gm = fmaxf(gm, fabsf(v));
+      d3 = fmaf(pt, bins[j] <= kb ? g[j] : 0.0f, d3);
+    }
+    for (int i = threadIdx.x; i < m; i += SH_THREADS) {
+      const float ap = fmaf(1.0f, q2u[i], beta * q[i]);  // A p = beta A p_prev_S + A g_S
+      d4 = fmaf(ap, ap, d4);
+    }
+    gm = cta_max(gm, sm);
+    d3 = cta_sum(d3, sm);
+    d4 = cta_sum(d4, sm);
+    if (threadIdx.x == 0) {
+      st->red[R_GMAX] = gm;
+      st->red[R_DOT3] = d3;
+      st->red[R_DOT4] = d4;
+      ctrl_phase(st, C_UCG_ALPHA, 0);
+    }
+  }
+  __syncthreads();
+  // x += alpha grad_previous (algorithms.cu:3840-3845 through the CG step functions)
+  const float alpha = st->cg_alpha;
+  float *x = d.X + (size_t)t * n;
+  float mx = 0.0f;
+  for (int j = threadIdx.x; j < n; j += SH_THREADS) {
+    const float o = fmaf(alpha, gp[j], x[j]);
+    x[j] = o;
+    mx = fmaxf(mx, fabsf(o));
+  }
+  mx = cta_max(mx, sm);
+  if (threadIdx.x == 0) {
+    st->red[R_XMAX] = mx;
+    st->sh_flops += 2.0 * (3.0 * m * (double)n + (double)n * d.kg + (double)m * d.kq * (ucg ? 2 : 1));
+    ctrl_phase(st, C_CGIHT_BINDEC, 0);
+    ctrl_phase(st, C_BINPREP, 0);
+  }
+  __syncthreads();
+  cta_support_evol(st, x, bins, d.bins_prev + (size_t)t * n, n, d.Xcat + (size_t)t * 3 * n, hist, scan);
+  if (threadIdx.x == 0) ctrl_phase(st, C_CGIHT_POST, 0);
+  __syncthreads();
+  if (st->flags[F_REMASK]) {
+    const int kb2 = st->k_bin;
+    for (int j = threadIdx.x; j < n; j += SH_THREADS) gpt[j] = bins[j] <= kb2 ? gp[j] : 0.0f;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) ctrl_phase(st, C_CGIHT_STOP, 0);
+  __syncthreads();
+  if (d.ml && st->fell_back == 1 && !st->active && st->stop_reason == 8) {
+    // the warm start did not lower the residual within 10 iterations: the plain start,
+    // its prologue in the next pass
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const int warm = st->iter;
+      const double fl = st->sh_flops;
+      *st = d.st0[t];
+      st->warm_iters = warm;
+      st->sh_flops = fl;
+      st->fell_back = 1;
+      atomicAdd(d.fallbacks, 1);
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < n; j += SH_THREADS) x[j] = d.G0[(size_t)t * n + j];
+    __syncthreads();
+    cta_start_support(d, t, st, x, hist, scan, sm);
+  }
+}
+
+// Ordered list of the trials that satisfy `on`, written to list / *count; every thread of
+// the 1024-thread block calls it, each owning a contiguous run of trials.
+template <class F>
+__device__ int cta_list(int T, F on, int *list, int *count) {
   __shared__ int wsum[32];
-  const int T = d.T, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const int per = (T + 1023) / 1024, b0 = min(tid * per, T), b1 = min(b0 + per, T);
-  auto on = [&](int t) { return which == 0 ? d.st[t].active != 0 : d.st[t].flags[F_CG] != 0; };
   int c = 0;
   for (int t = b0; t < b1; ++t) c += on(t) ? 1 : 0;
   int incl = c;
@@ -444,6 +841,7 @@ __global__ void __launch_bounds__(1024) k_sh_list(ShDev d, int which, int *passe
     const int v = __shfl_up_sync(0xffffffffu, incl, o);
     if (lane >= o) incl += v;
   }
+  __syncthreads();
   if (lane == 31) wsum[w] = incl;
   __syncthreads();
   if (w == 0) {
@@ -458,14 +856,35 @@ __global__ void __launch_bounds__(1024) k_sh_list(ShDev d, int which, int *passe
   __syncthreads();
   int pos = incl - c + (w > 0 ? wsum[w - 1] : 0);
   for (int t = b0; t < b1; ++t)
-    if (on(t)) d.act[pos++] = t;
-  if (tid == 0) {
-    const int total = wsum[31];
-    *d.act_cnt = total;
+    if (on(t)) list[pos++] = t;
+  const int total = wsum[31];
+  if (tid == 0) *count = total;
+  return total;
+}
+
+// The GEMMs' column maps and the loop condition: which 0 -> the active trials (NIHT and
+// CGIHT; CGIHT also the trials that run this pass's direction product -- not the ones in a
+// restart's prologue -- and the unrestricted-branch trials among them), bounded by
+// max_passes; which 1 -> the debias trials (F_CG).  One block of 1024 threads.
+__global__ void __launch_bounds__(1024) k_sh_list(ShDev d, int which, int *passes, int max_passes,
+                                                  cudaGraphConditionalHandle h) {
+  const int T = d.T;
+  int total;
+  if (which == 0) {
+    total = cta_list(T, [&](int t) { return d.st[t].active != 0; }, d.act, d.act_cnt);
+    if (d.alg == GB_ALG_CGIHT) {
+      cta_list(T, [&](int t) { return d.st[t].active != 0 && d.st[t].fell_back != 1; }, d.act_q, d.act_q_cnt);
+      cta_list(T, [&](int t) { return d.st[t].active != 0 && d.st[t].fell_back != 1 && d.st[t].flags[F_UCG] != 0; },
+               d.act_u, d.act_u_cnt);
+    }
+  } else {
+    total = cta_list(T, [&](int t) { return d.st[t].flags[F_CG] != 0; }, d.act, d.act_cnt);
+  }
+  if (threadIdx.x == 0) {
     unsigned go = total > 0 ? 1u : 0u;
     if (which == 0) {
       const int p = ++passes[0];
-      if (p > d.maxiter + 4) go = 0u;
+      if (p > max_passes) go = 0u;
     }
     if (h) cudaGraphSetConditional(h, go);
   }
@@ -593,12 +1012,15 @@ __global__ void __launch_bounds__(SH_THREADS) k_sh_verdict(ShDev d) {
   if (threadIdx.x == 0) {
     const float rel = (float)(sqrt(e2) / sqrt(x2));
     const GbState *st = d.st + t;
-    d.iters[t] = st->iter;
+    d.iters[t] = st->iter + st->warm_iters;
     d.err[t] = rel;
     d.ok[t] = rel <= 1e-3f ? 1 : 0;
-    // GEMM flops this trial used: the initial A^T y, each NIHT iteration, and the debias
+    // GEMM flops this trial used: the initial A^T y, each iteration (CGIHT: counted per
+    // pass, plus its prologue's residual and gradient), and the debias
     const double mn3 = 3.0 * d.m * (double)d.n;
-    double f = 2.0 * d.n * (double)d.kg + st->iter * 2.0 * (mn3 + (double)d.n * d.kg + (double)d.m * d.kq);
+    double f = 2.0 * d.n * (double)d.kg;
+    if (d.alg == GB_ALG_CGIHT) f += st->sh_flops + 2.0 * (mn3 + (double)d.n * d.kg);
+    else f += st->iter * 2.0 * (mn3 + (double)d.n * d.kg + (double)d.m * d.kq);
     if (st->stop_reason == 1) f += (2.0 + st->it_cg) * 2.0 * mn3 * 2.0;
     atomicAdd(d.flops, f);
   }
@@ -623,6 +1045,7 @@ struct Buf {
 
 static thread_local float g_sh_ms = 0.0f;
 static thread_local double g_sh_gemm_flops = 0.0;
+static thread_local int g_sh_fallbacks = 0;
 
 extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *iters_out, float *rel_err_out,
                                               int *success_out, int *num_success) {
@@ -632,6 +1055,12 @@ extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *ite
                          __LINE__);
     return GB_BAD_ARG;
   }
+  if ((b->alg != GB_ALG_NIHT && b->alg != GB_ALG_CGIHT) || (b->learned_params && b->alg != GB_ALG_CGIHT)) {
+    gb_set_error_message("shared batch: alg is NIHT or CGIHT; the learned warm start is for CGIHT", __FILE__,
+                         __LINE__);
+    return GB_BAD_ARG;
+  }
+  const bool cgiht = b->alg == GB_ALG_CGIHT;
   const int m = b->m, n = b->n, T = b->ntrials, Tp = (T + 255) / 256 * 256;  // tcgen05 N tile
   for (int t = 0; t < T; ++t)
     if (b->k[t] < 1 || b->k[t] > m) {
@@ -645,6 +1074,8 @@ extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *ite
   d.m = m; d.n = n; d.T = T; d.Tp = Tp; d.maxiter = b->maxiter; d.tol_rel = b->tol_rel; d.seed = b->seed;
   d.prec = b->precision;
   d.first = b->first_trial;
+  d.alg = b->alg;
+  d.ml = b->learned_params;
   const int kg = (d.prec & 1) ? 3 * m : m, kq = (d.prec & 2) ? 3 * n : n;  // K of A^T r and A x_thres
   d.kg = kg;
   d.kq = kq;
@@ -671,6 +1102,24 @@ extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *ite
   GB_TRY(buf.get(&passes, 1));
   GB_TRY(buf.get(&d.act, Tp));
   GB_TRY(buf.get(&d.act_cnt, 1));
+  if (cgiht) {
+    for (float **v : {&d.GP, &d.GPT}) GB_TRY(buf.get(v, (size_t)Tp * n));
+    GB_TRY(buf.get(&d.Q2, (size_t)Tp * m));
+    GB_TRY(buf.get(&d.XT2, (size_t)Tp * 3 * n));
+    GB_TRY(buf.get(&d.bins_prev, (size_t)Tp * n));
+    GB_TRY(buf.get(&d.act_q, Tp));
+    GB_TRY(buf.get(&d.act_q_cnt, 1));
+    GB_TRY(buf.get(&d.act_u, Tp));
+    GB_TRY(buf.get(&d.act_u_cnt, 1));
+    GB_TRY(buf.get(&d.fallbacks, 1));
+    GB_CUDA_TRY(cudaMemsetAsync(d.fallbacks, 0, sizeof(int), s));
+    GB_CUDA_TRY(cudaMemsetAsync(d.bins_prev, 0, sizeof(int) * (size_t)Tp * n, s));
+    if (d.ml) {
+      GB_TRY(buf.get(&d.G0, (size_t)Tp * n));
+      GB_TRY(buf.get(&d.st0, (size_t)Tp));
+    }
+  }
+  const int max_passes = d.maxiter + 4 + (d.ml ? 11 : 0);
   GB_TRY(buf.get(&d.flops, 1));
   GB_CUDA_TRY(cudaMemsetAsync(d.flops, 0, sizeof(double), s));
   // split-K workspace of the GEMMs over the active trials (they run one after another)
@@ -690,18 +1139,23 @@ extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *ite
     ws.gather = gbuf;
   }
   GB_CUDA_TRY(cudaMemsetAsync(ws.tickets, 0, sizeof(unsigned) * ws.ticket_count, s));
-  // Ct[Tp x M] = [Y -] A . B^T over all trials, or over the listed ones (mapped)
-  auto gemm = [&](const void *A, const void *B, float *C, int M, int K, int lda, int ldb, const float *Y, void *Cb,
-                  int split, bool mapped, cudaStream_t st) {
+  // Ct[Tp x M] = [Y -] A . B^T over all trials, or over the listed ones (map / count)
+  auto gemm_map = [&](const void *A, const void *B, float *C, int M, int K, int lda, int ldb, const float *Y, void *Cb,
+                      int split, const int *map, const int *count, cudaStream_t st) {
     GbGemm g = {};
     g.A = A; g.B = B; g.Ct = C; g.M = M; g.N = Tp; g.K = K; g.lda = lda; g.ldb = ldb; g.Y = Y; g.Cb = Cb;
     g.cb_split = split;
-    if (mapped) {
-      g.nmap = d.act;
-      g.ncount = d.act_cnt;
+    if (map) {
+      g.nmap = map;
+      g.ncount = count;
       g.ws = &ws;
     }
     return gb_gemm(g, st);
+  };
+  auto gemm = [&](const void *A, const void *B, float *C, int M, int K, int lda, int ldb, const float *Y, void *Cb,
+                  int split, bool mapped, cudaStream_t st) {
+    return gemm_map(A, B, C, M, K, lda, ldb, Y, Cb, split, mapped ? d.act : nullptr, mapped ? d.act_cnt : nullptr,
+                    st);
   };
   GB_CUDA_TRY(cudaMemsetAsync(passes, 0, sizeof(int), s));
   GB_CUDA_TRY(cudaMemsetAsync(d.st, 0, sizeof(GbState) * Tp, s));
@@ -720,7 +1174,19 @@ extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *ite
   // ---- x = H_k(A^T y): G = A_hi^T bf16(y) (Rbf holds bf16(y) here)
   GB_TRY(gemm(d.ATcat, (d.prec & 1) ? (const void *)d.Rcat : d.Rbf, d.G, n, kg, 3 * m, kg, nullptr, nullptr, 0, false,
               s));
-  k_sh_init<<<Tp, SH_THREADS, 0, s>>>(d);
+  const int split_r = (d.prec & 1) != 0;
+  void *rb = split_r ? (void *)d.Rcat : (void *)d.Rbf;
+  if (!cgiht) {
+    k_sh_init<<<Tp, SH_THREADS, 0, s>>>(d);
+  } else {
+    // CGIHT: x = H_k(A^T y) or the learned start, then r0 = y - A x, grad_previous = A^T r0
+    const int smem = (ML_P + 2 * ML_RANK_BINS) * (int)sizeof(float);
+    GB_CUDA_TRY(cudaFuncSetAttribute(k_sc_init, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    k_sc_init<<<Tp, SH_THREADS, smem, s>>>(d);
+    GB_TRY(gemm(d.Acat, d.Xcat, d.R, m, 3 * n, 3 * n, 3 * n, d.Y, rb, split_r, false, s));
+    GB_TRY(gemm(d.ATcat, rb, d.G, n, kg, 3 * m, kg, nullptr, nullptr, 0, false, s));
+    k_sc_init2<<<Tp, SH_THREADS, 0, s>>>(d);
+  }
   GB_CUDA_TRY(cudaGetLastError());
   // ---- NIHT iterations in lockstep: one graph, WHILE any trial is active
   cudaStream_t c0, c1;
@@ -738,20 +1204,27 @@ extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *ite
     cudaGraphConditionalHandle h = 0;
     if (rc == GB_OK) rc = gb_make_handle(c0, &h);
     if (rc == GB_OK) {
-      k_sh_list<<<1, 1024, 0, c0>>>(d, 0, passes, h);
+      k_sh_list<<<1, 1024, 0, c0>>>(d, 0, passes, max_passes, h);
       rc = gb_open_while(c0, c1, h);
     }
     if (rc == GB_OK) {
-      // R = Y - A X (and its BF16 form for the next product), G = A^T R, Q = A x_thres;
-      // each over the active trials only
-      const int split_r = (d.prec & 1) != 0;
-      void *rb = split_r ? (void *)d.Rcat : (void *)d.Rbf;
+      // R = Y - A X (and its BF16 form for the next product), G = A^T R over the active
+      // trials; NIHT then Q = A x_thres, CGIHT Q = A p and (unrestricted branch) Q2 = A g_S
       rc = gemm(d.Acat, d.Xcat, d.R, m, 3 * n, 3 * n, 3 * n, d.Y, rb, split_r, true, c1);
       if (rc == GB_OK) rc = gemm(d.ATcat, rb, d.G, n, kg, 3 * m, kg, nullptr, nullptr, 0, true, c1);
-      k_sh_mask<<<Tp, SH_THREADS, 0, c1>>>(d);
-      if (rc == GB_OK) rc = gemm(d.Acat, d.XTbf, d.Q, m, kq, 3 * n, kq, nullptr, nullptr, 0, true, c1);
-      k_sh_step<<<Tp, SH_THREADS, 0, c1>>>(d);
-      k_sh_list<<<1, 1024, 0, c1>>>(d, 0, passes, h);
+      if (!cgiht) {
+        k_sh_mask<<<Tp, SH_THREADS, 0, c1>>>(d);
+        if (rc == GB_OK) rc = gemm(d.Acat, d.XTbf, d.Q, m, kq, 3 * n, kq, nullptr, nullptr, 0, true, c1);
+        k_sh_step<<<Tp, SH_THREADS, 0, c1>>>(d);
+      } else {
+        k_sc_dir<<<Tp, SH_THREADS, 0, c1>>>(d);
+        if (rc == GB_OK)
+          rc = gemm_map(d.Acat, d.XTbf, d.Q, m, kq, 3 * n, kq, nullptr, nullptr, 0, d.act_q, d.act_q_cnt, c1);
+        if (rc == GB_OK)
+          rc = gemm_map(d.Acat, d.XT2, d.Q2, m, kq, 3 * n, kq, nullptr, nullptr, 0, d.act_u, d.act_u_cnt, c1);
+        k_sc_step<<<Tp, SH_THREADS, 0, c1>>>(d);
+      }
+      k_sh_list<<<1, 1024, 0, c1>>>(d, 0, passes, max_passes, h);
       gb_status rc2 = gb_close_while(c1);
       if (rc == GB_OK) rc = rc2;
     }
@@ -760,7 +1233,7 @@ extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *ite
     cudaGraphConditionalHandle h2 = 0;
     if (rc == GB_OK) {
       k_cg_flags<<<(Tp + 255) / 256, 256, 0, c0>>>(d);
-      k_sh_list<<<1, 1024, 0, c0>>>(d, 1, passes, 0);
+      k_sh_list<<<1, 1024, 0, c0>>>(d, 1, passes, max_passes, 0);
       rc = gemm(d.Acat, d.Xcat, d.R, m, 3 * n, 3 * n, 3 * n, d.Y, nullptr, 0, true, c0);
     }
     if (rc == GB_OK) {
@@ -770,7 +1243,7 @@ extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *ite
     if (rc == GB_OK) rc = gb_make_handle(c0, &h2);
     if (rc == GB_OK) {
       k_cg_dir<<<Tp, SH_THREADS, 0, c0>>>(d);
-      k_sh_list<<<1, 1024, 0, c0>>>(d, 1, passes, h2);
+      k_sh_list<<<1, 1024, 0, c0>>>(d, 1, passes, max_passes, h2);
       rc = gb_open_while(c0, c1, h2);
     }
     if (rc == GB_OK) {
@@ -779,7 +1252,7 @@ extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *ite
       if (rc == GB_OK)
         rc = gemm(d.ATcat, d.Rcat, d.G, n, 3 * m, 3 * m, 3 * m, nullptr, nullptr, 0, true, c1);
       k_cg_dir<<<Tp, SH_THREADS, 0, c1>>>(d);
-      k_sh_list<<<1, 1024, 0, c1>>>(d, 1, passes, h2);
+      k_sh_list<<<1, 1024, 0, c1>>>(d, 1, passes, max_passes, h2);
       gb_status rc2 = gb_close_while(c1);
       if (rc == GB_OK) rc = rc2;
     }
@@ -805,9 +1278,12 @@ extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *ite
     if (b->d_A_out) cudaMemcpyAsync(b->d_A_out, d.A32, sizeof(float) * (size_t)m * n, cudaMemcpyDeviceToDevice, s);
     if (b->d_Y_out) cudaMemcpyAsync(b->d_Y_out, d.Y, sizeof(float) * (size_t)T * m, cudaMemcpyDeviceToDevice, s);
     if (b->d_X0_out) cudaMemcpyAsync(b->d_X0_out, d.X0, sizeof(float) * (size_t)T * n, cudaMemcpyDeviceToDevice, s);
+    if (b->d_X_out) cudaMemcpyAsync(b->d_X_out, d.X, sizeof(float) * (size_t)T * n, cudaMemcpyDeviceToDevice, s);
     std::vector<int> hit(T), hok(T);
     std::vector<float> herr(T);
     double hflops = 0.0;
+    int hfb = 0;
+    if (d.fallbacks) cudaMemcpyAsync(&hfb, d.fallbacks, sizeof(int), cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(hit.data(), d.iters, sizeof(int) * T, cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(herr.data(), d.err, sizeof(float) * T, cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(hok.data(), d.ok, sizeof(int) * T, cudaMemcpyDeviceToHost, s);
@@ -821,6 +1297,7 @@ extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *ite
     } else {
       cudaEventElapsedTime(&g_sh_ms, e0, e1);
       g_sh_gemm_flops = hflops;
+      g_sh_fallbacks = hfb;
       int ns = 0;
       for (int t = 0; t < T; ++t) {
         if (iters_out) iters_out[t] = hit[t];
@@ -844,3 +1321,5 @@ extern "C" void gb_cs_shared_last_stats(double *gemm_flops, float *ms) {
   if (gemm_flops) *gemm_flops = g_sh_gemm_flops;
   if (ms) *ms = g_sh_ms;
 }
+
+extern "C" int gb_cs_shared_last_fallbacks(void) { return g_sh_fallbacks; }

@@ -270,7 +270,7 @@ void gb_cs_batch_last_stats(double *bytes, float *kernel_ms);
 int gb_cs_batch_last_cluster(void);
 
 /* ---- shared-matrix batched form (no reference counterpart) ----
- * ntrials NIHT trials y_t = A x0_t that share one dense Gaussian A (drawn from `seed` as
+ * ntrials NIHT or CGIHT trials y_t = A x0_t that share one dense Gaussian A (drawn from `seed` as
  * gb_cs_generate_and_solve draws it; trial t's +-1 signal x0_t with k[t] nonzeros uses the
  * key seed + 1 + first_trial + t).  The operator applications of all trials run as BF16 tensor-core
  * GEMMs with FP32 accumulation; the residual keeps ~FP32 accuracy by splitting A and x
@@ -290,10 +290,21 @@ typedef struct {
   int precision;                 /* bit 0: split-BF16 A^T r, bit 1: split-BF16 A x_thres (0: plain BF16) */
   float *d_A_out, *d_Y_out, *d_X0_out;
   void *stream;
+  int alg;                       /* GB_ALG_NIHT (0, the default) or GB_ALG_CGIHT (restartFlag off) */
+  const float *learned_params;   /* CGIHT: device pointer to the warm-start MLP's parameters, or
+                                    NULL for the plain start; a trial whose residual has not
+                                    dropped below the warm start's within 10 iterations is
+                                    solved again from the plain start, iterations added */
+  float *d_X_out;                /* optional device copy of the final x of every trial (ntrials*n) */
 } gb_shared_batch;
 
 gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *iters_out, float *rel_err_out,
                                    int *success_out, int *num_success);
+
+/* Trials of the last gb_cs_solve_shared_batch call on this thread whose learned warm start
+ * was abandoned after 10 iterations and solved again from the plain start (no reference
+ * counterpart). */
+int gb_cs_shared_last_fallbacks(void);
 
 /* ---- learned warm start (no reference counterpart) ----
  * A per-coordinate MLP 4 -> 64 -> 64 -> 1 (GELU; weights rounded to BF16 at use, FP32

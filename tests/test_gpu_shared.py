@@ -152,3 +152,83 @@ def test_shared_batch_rejects_bad_sizes(gb):
         gb.solve_shared_batch(1024, 512, [10], SEED)
     with pytest.raises(gb.GagaError):
         gb.solve_shared_batch(512, 1024, [0], SEED)
+
+
+def test_shared_batch_debias_matches_fp64_least_squares(gb, gbo):
+    """The debias is conjugate gradients on the normal equations restricted to the final
+    support, with split-BF16 GEMM products and FP64 scalars -- a deliberate stand-in for an
+    FP64 least-squares solve on that support (FP64 arithmetic runs at a small fraction of the
+    FP32 rate on this part).  Against numpy's FP64 lstsq on the same support, A and y, the
+    debiased x agrees to 1e-5 relative (the CG stops at 1e-12 of its starting gradient)."""
+    import torch
+
+    m, n = 1024, 2048
+    ks = np.array([40, 80, 120, 160, 200] * 2, dtype=np.int32)
+    ns, iters, err, ok, A, Y, X0, X = gb.solve_shared_batch(m, n, ks, SEED + 9, tol_rel=1e-4, maxiter=1000,
+                                                             outputs="x")
+    torch.cuda.synchronize()
+    A64 = A.cpu().numpy().astype(np.float64).T  # m x n
+    Yh, Xh = Y.cpu().numpy().astype(np.float64), X.cpu().numpy().astype(np.float64)
+    checked = 0
+    for t in range(len(ks)):
+        if not ok[t]:
+            continue
+        S = np.flatnonzero(Xh[t])
+        z, *_ = np.linalg.lstsq(A64[:, S], Yh[t], rcond=None)
+        assert np.linalg.norm(Xh[t][S] - z) <= 1e-5 * np.linalg.norm(z), t
+        checked += 1
+    assert checked >= 6
+
+
+def _shared_cgiht_vs_plain(gb, gbo, ks, learned=None):
+    import torch
+
+    m, n = 512, 1024
+    ns, iters, err, ok, A, Y, X0 = gb.solve_shared_batch(m, n, ks, SEED + 3, tol_rel=1e-4, maxiter=1000,
+                                                          outputs=True, alg="CGIHT", learned_params=learned)
+    torch.cuda.synchronize()
+    X0 = X0.cpu().numpy()
+    assert ns == int(ok.sum())
+    res = []
+    for t in range(len(ks)):
+        k_t = int(np.count_nonzero(X0[t]))
+        opts = gb.gaga_options("tol", 1e-4, "tol_is_relative", 1, "maxiter", 1000)
+        x, it, _ = gb.gaga_cs("CGIHT", "gen", Y[t].contiguous(), A.t(), k_t, opts)
+        x = x.cpu().numpy()
+        rel = np.linalg.norm(x - X0[t]) / np.linalg.norm(X0[t])
+        res.append((bool(rel <= 1e-3), bool(ok[t]), int(it), int(iters[t])))
+    return ns, res
+
+
+def test_shared_cgiht_matches_plain(gb, gbo):
+    """CGIHT in lockstep with BF16 tensor-core products (restricted and unrestricted CG
+    branches, support evolution) against the FP32 single-trial CGIHT on the same A and y:
+    the same verdicts except at the edge of the phase transition, and iteration counts close
+    on the trials both recover."""
+    ks = np.round(np.linspace(0.04, 0.5, 96) * 512).astype(np.int32)
+    ns, res = _shared_cgiht_vs_plain(gb, gbo, ks)
+    agree = sum(int(p == s) for p, s, _, _ in res)
+    assert 0 < ns < len(ks)
+    assert agree >= len(ks) - 2, agree
+    both = [(ip, isb) for p, s, ip, isb in res if p and s]
+    assert len(both) > 20
+    assert np.median([abs(a - b) for a, b in both]) <= 2
+
+
+def test_shared_cgiht_learned_warm_start(gb, gbo):
+    """The learned warm start in the shared-matrix form: the trained network's start, the
+    fallback to the plain start after 10 iterations without progress (counted), verdicts
+    against the plain FP32 CGIHT, and fewer iterations on the trials both recover."""
+    from gaga_gb300 import learned
+
+    params = learned.load_weights()
+    ks = np.round(np.linspace(0.05, 0.45, 96) * 512).astype(np.int32)
+    ns, res = _shared_cgiht_vs_plain(gb, gbo, ks, learned=params)
+    fb = gb.shared_last_fallbacks()
+    assert 0 <= fb <= len(ks)
+    agree = sum(int(p == s) for p, s, _, _ in res)
+    assert agree >= len(ks) - 6, agree
+    only_plain = sum(int(p and not s) for p, s, _, _ in res)
+    assert only_plain <= 2
+    both = [(ip, isb) for p, s, ip, isb in res if p and s]
+    assert np.mean([b for _, b in both]) <= np.mean([a for a, _ in both]) + 1.0
