@@ -226,9 +226,10 @@ def test_shared_cgiht_learned_warm_start(gb, gbo):
     ns, res = _shared_cgiht_vs_plain(gb, gbo, ks, learned=params)
     fb = gb.shared_last_fallbacks()
     assert 0 <= fb <= len(ks)
-    agree = sum(int(p == s) for p, s, _, _ in res)
-    assert agree >= len(ks) - 6, agree
+    # the warm start changes which trials near the phase transition recover; it may gain
+    # trials over plain CGIHT but should lose almost none
     only_plain = sum(int(p and not s) for p, s, _, _ in res)
-    assert only_plain <= 2
+    only_learned = sum(int(s and not p) for p, s, _, _ in res)
+    assert only_plain <= 2, (only_plain, only_learned, fb)
     both = [(ip, isb) for p, s, ip, isb in res if p and s]
-    assert np.mean([b for _, b in both]) <= np.mean([a for a, _ in both]) + 1.0
+    assert np.mean([b for _, b in both]) <= np.mean([a for a, _ in both]) + 1.0, (only_plain, only_learned, fb)
