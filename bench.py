@@ -1,25 +1,30 @@
-"""Benchmark: trials recovered per second on the dense phase-transition sweep.
+"""Benchmark: trials recovered per second on the dense phase-transition sweep, the tuned
+form (batched + BF16 tensor cores + learned warm start) against the plain single-trial
+FP32 form.
 
-Workload: 4096 dense Gaussian NIHT trials with ||y - A x|| <= 1e-4 ||y||, maxiter 5000;
+Workload: 4096 dense Gaussian CGIHT trials with ||y - A x|| <= 1e-4 ||y||, maxiter 5000;
 a trial is recovered when its relative l2 error is <= 1e-3 (gaga_gb300/sweep.py):
   - 3072 independent trials (n in {1024,...,16384}, delta in {0.1,...,0.9}, rho on a
     0.02 grid up to 0.5), each with its own A and x drawn on the device from
-    (seed + trial id): the batched slot-graph form (gb_cs_solve_batch);
+    (seed + trial id): the batched form (gb_cs_solve_batch: cluster-resident kernel for
+    n <= 8192, slot graphs for the rest), learned warm start;
   - 1024 trials sharing one A (n = 8192, m = 4096, rho cycling the same grid): the
-    shared-matrix form (gb_cs_solve_shared_batch; BF16 tensor-core GEMMs, split-BF16
-    residual, least-squares debias).
+    shared-matrix form (gb_cs_solve_shared_batch; split-BF16 tcgen05 GEMMs in lockstep,
+    least-squares debias), learned warm start.
 A step is one quarter of the sweep: 768 independent trials plus 256 shared-matrix trials.
 Problem generation runs inside the timed region.
 
-  value : recovered trials / device time of both forms' kernels
+  value : recovered trials / device time of both forms
   e2e   : recovered trials / wall time of the two calls made with host arrays (trial
           tables in, per-trial iterations/errors/verdicts out)
-  plain : the single-trial FP32 drop-in on the first timed step's trials (all 768 + 256 by
-          default; gb_cs_generate_and_solve for independent trials, gb_cs_solve on the shared A
-          for shared trials), scaled to the 3072 + 1024 mix, for the tuned-vs-plain ratio; the
-          verdicts of the same trials give the agreement between the two forms
-  learned_warm_start : the trained MLP warm start for CGIHT against zero-initialised CGIHT
-          on 2048 fresh trials of its workload (n = 8192, delta 0.1-0.6, rho 0.05-0.45)
+  plain : the single-trial FP32 drop-in, zero-initialised CGIHT, on every trial of the
+          first timed step (gb_cs_generate_and_solve for the independent trials with the
+          same seeds, gb_cs_solve on the shared A and each y), each call timed with CUDA
+          events; scaled to the 3072 + 1024 mix for tuned_vs_plain; the verdicts of the same
+          trials give the agreement between the two forms, split by direction
+  niht_sweep : the same sweep with NIHT (batched + shared-matrix forms, no warm start)
+  learned_warm_start : the trained MLP warm start against zero-initialised CGIHT on 2048
+          fresh trials of its own workload (n = 8192, delta 0.1-0.6, rho 0.05-0.45)
   cpu_baseline / --impl reference : the CPU oracle (oracle/gbo.c, OpenMP inside each
           trial) on a bounded sample of the wave
 
@@ -40,7 +45,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "trials recovered/s (rel err<=1e-3), tuned vs plain on 1 GB300; matvec % HBM peak"
 TOTAL, SHARED, PARTS, SEED, TOL_REL, MAXITER = 4096, 1024, 4, 20240607, 1e-4, 5000
-WORKLOAD = ("dense phase-transition sweep: 4096 NIHT trials = 3072 independent (n 1024-16384, delta 0.1-0.9, "
+ALG = "CGIHT"
+WORKLOAD = ("dense phase-transition sweep: 4096 CGIHT trials = 3072 independent (n 1024-16384, delta 0.1-0.9, "
             "rho 0.02-0.5) + 1024 sharing one A (n 8192, m 4096, rho 0.02-0.5); tol 1e-4*||y||; one quarter of "
             "the sweep per step per GPU")
 SHARED_SEED = SEED + 1000003  # keys of the shared subset stay clear of the independent trials' seed + id
@@ -139,13 +145,13 @@ def run_cpu(w, count):
     n, m, k, tid = cpu_sample(w, count)
     cores = os.cpu_count() or 1
     t0 = time.perf_counter()
-    ok, iters, err = gbo.solve_dense_trials(n, m, k, SEED, tid, alg="NIHT", tol_rel=TOL_REL, maxiter=MAXITER,
+    ok, iters, err = gbo.solve_dense_trials(n, m, k, SEED, tid, alg=ALG, tol_rel=TOL_REL, maxiter=MAXITER,
                                             threads=cores)
     dt = time.perf_counter() - t0
     return {"value": ok / dt, "unit": "trials/s", "cores": cores, "kind": "port", "seconds": dt,
-            "sample": "%d trials of wave %d (every %d-th; n=%s), NIHT, CPU oracle oracle/gbo.c with OpenMP inside each "
-                      "trial, generation included; %d recovered in %.1f s" % (len(n), w, len(wave_arrays(w)[0]) // count,
-                                                                               sorted(set(n.tolist())), ok, dt)}
+            "sample": ("%d trials of wave %d (every %d-th; n=%s), %s, CPU oracle oracle/gbo.c with OpenMP inside "
+                       "each trial, generation included; %d recovered in %.1f s" % (
+                           len(n), w, len(wave_arrays(w)[0]) // count, sorted(set(n.tolist())), ALG, ok, dt))}
 
 
 def bench_reference(args):
@@ -192,26 +198,30 @@ def bench_ours(args):
     from gaga_gb300 import autotune
 
     n0, m0, k0, t0_ = wave_arrays(sweep_rank_first(rank, world))
-    sched = autotune.tune_batch(n0, m0, k0, SEED, t0_, alg="NIHT", tol_rel=TOL_REL, maxiter=MAXITER,
+    sched = autotune.tune_batch(n0, m0, k0, SEED, t0_, alg=ALG, tol_rel=TOL_REL, maxiter=MAXITER,
                                 use_cache=not args.retune)
+    params = gb.learned.load_weights()
 
-    def solve_step(w):
+    def solve_step(w, alg=ALG, lp=params, schedule=sched):
         """One quarter of the sweep: independent trials, then the shared-matrix trials."""
         n, m, k, tid = wave_arrays(w)
         t0 = time.perf_counter()
-        ns, iters, err, ok = gb.solve_batch(n, m, k, SEED, tid, alg="NIHT", tol_rel=TOL_REL, maxiter=MAXITER,
-                                            slots=sched["slots"], sm_share=sched["sm_share"],
-                                            cluster=sched.get("cluster", 0))
+        ns, iters, err, ok = gb.solve_batch(n, m, k, SEED, tid, alg=alg, tol_rel=TOL_REL, maxiter=MAXITER,
+                                            slots=schedule["slots"], sm_share=schedule["sm_share"],
+                                            cluster=schedule.get("cluster", 0), learned_params=lp)
         t1 = time.perf_counter()
         nbytes, kms = gb.batch_last_stats()
         ks, first = shared_part(w)
         ns2, it2, err2, ok2 = gb.solve_shared_batch(gb.sweep.SHARED_M, gb.sweep.SHARED_N, ks, SHARED_SEED,
-                                                    tol_rel=TOL_REL, maxiter=MAXITER, first_trial=first)
+                                                    tol_rel=TOL_REL, maxiter=MAXITER, first_trial=first, alg=alg,
+                                                    learned_params=lp)
         t2 = time.perf_counter()
         flops, kms2 = gb.shared_last_stats()
+        fb = gb.shared_last_fallbacks() if lp is not None else 0
         return dict(ok=ns + ns2, trials=len(n) + len(ks), wall=t2 - t0, kms=kms + kms2, bytes=nbytes, flops=flops,
                     kms_batch=kms, kms_shared=kms2, ok_batch=ns, ok_shared=ns2, n_batch=len(n), n_shared=len(ks),
-                    verdict_batch=ok, verdict_shared=ok2, wall_batch=t1 - t0, wall_shared=t2 - t1,
+                    verdict_batch=ok, verdict_shared=ok2, iters_batch=iters, iters_shared=it2, wall_batch=t1 - t0,
+                    wall_shared=t2 - t1, fallbacks_shared=fb,
                     h2d=12 * len(n) + 4 * len(ks), d2h=12 * (len(n) + len(ks)))
 
     from gaga_gb300 import sweep
@@ -232,11 +242,12 @@ def bench_ours(args):
         if first_step is None:
             first_step = (w, r)
         for key in ("ok", "trials", "wall", "kms", "bytes", "flops", "kms_batch", "kms_shared", "ok_batch", "ok_shared",
-                    "n_batch", "n_shared", "wall_batch", "wall_shared", "h2d", "d2h"):
+                    "n_batch", "n_shared", "wall_batch", "wall_shared", "h2d", "d2h", "fallbacks_shared"):
             acc[key] = acc.get(key, 0) + r[key]
         # host-issued launches: one graph per slot stream and the cluster-resident kernel of
-        # the batched form; the shared form's 6 setup kernels, its graph and its verdict kernel
-        launches += sched["slots"] + 1 + 8
+        # the batched form (twice with the warm start's fallback pass); the shared form's 9
+        # setup kernels and GEMMs, its graph and its verdict kernel
+        launches += 2 * (sched["slots"] + 1) + 11
     torch.cuda.synchronize()
     clocks = sampler.stop()
     if world > 1:
@@ -259,9 +270,10 @@ def bench_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32 (shared-matrix part: bf16 GEMM, fp32 accumulate)",
             "data": "synthetic (seeded Philox Gaussian trials drawn on device)",
             "config": {"workload": WORKLOAD,
-                       "form": "tuned: batched form (n <= 8192: cluster-resident NIHT kernel, one thread-block "
-                               "cluster per trial; larger: slot graphs; device trial queues, device generation) + "
-                               "shared-matrix BF16 tensor-core GEMM form",
+                       "form": "tuned: batched form (n <= 8192: cluster-resident learned-CGIHT kernel, one "
+                               "thread-block cluster per trial; larger: slot graphs; device trial queues, device "
+                               "generation) + shared-matrix form (CGIHT in lockstep, split-BF16 tcgen05 GEMMs, FP64-"
+                               "scalar CG debias), both starting from the learned warm start with the plain fallback",
                        "schedule": {"slots": sched["slots"], "sm_share": sched["sm_share"],
                                     "cluster": sched.get("cluster", 0),
                                     "picked_by": "autotune over %d candidates on %d probe trials%s" % (
@@ -275,6 +287,7 @@ def bench_ours(args):
                                       "recovered_per_s": acc["ok_batch"] / (acc["kms_batch"] / 1e3)},
                       "shared_matrix": {"trials": int(acc["n_shared"]), "recovered": int(acc["ok_shared"]),
                                         "kernel_ms": acc["kms_shared"],
+                                        "warm_start_fallbacks": int(acc["fallbacks_shared"]),
                                         "recovered_per_s": acc["ok_shared"] / (acc["kms_shared"] / 1e3),
                                         "gemm_tflops": gemm_tf,
                                         "gemm_frac": gemm_tf / tpeak if tpeak else None}},
@@ -299,6 +312,9 @@ def bench_ours(args):
     if args.plain_trials > 0 and world == 1:
         line["plain"] = bench_plain(args, first_step)
         line["tuned_vs_plain"] = value / line["plain"]["value"] if line["plain"]["value"] else None
+        line["tuned_vs_plain_e2e"] = e2e / line["plain"]["value"] if line["plain"]["value"] else None
+    if args.niht_steps > 0 and world == 1:
+        line["niht_sweep"] = bench_niht(args, solve_step)
     if args.learned_trials > 0 and world == 1:
         line["learned_warm_start"] = bench_learned(args)
     if not args.no_cpu and world == 1:
@@ -306,6 +322,30 @@ def bench_ours(args):
     print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def bench_niht(args, solve_step):
+    """The same sweep with NIHT (batched + shared-matrix forms, no warm start): the steps
+    after the headline's, device time of both forms."""
+    from gaga_gb300 import autotune
+
+    n0, m0, k0, t0_ = wave_arrays(0)
+    sched = autotune.tune_batch(n0, m0, k0, SEED, t0_, alg="NIHT", tol_rel=TOL_REL, maxiter=MAXITER,
+                                use_cache=not args.retune)
+    solve_step(PARTS - 1, alg="NIHT", lp=None, schedule=sched)  # warm-up
+    ok = trials = 0
+    kms = kb = ks = 0.0
+    for s in range(args.niht_steps):
+        r = solve_step(s, alg="NIHT", lp=None, schedule=sched)
+        ok += r["ok"]
+        trials += r["trials"]
+        kms += r["kms"]
+        kb += r["kms_batch"]
+        ks += r["kms_shared"]
+    return {"value": ok / (kms / 1e3), "unit": "trials/s", "steps": args.niht_steps, "recovered": int(ok),
+            "trials": int(trials), "ms_per_step": kms / args.niht_steps,
+            "independent_ms_per_step": kb / args.niht_steps, "shared_ms_per_step": ks / args.niht_steps,
+            "schedule": {"slots": sched["slots"], "sm_share": sched["sm_share"], "cluster": sched.get("cluster", 0)}}
 
 
 def bench_learned(args):
@@ -621,9 +661,11 @@ def ncu_traffic():
 
 
 def bench_plain(args, first_step):
-    """Single-trial FP32 drop-in on samples of the first timed step's trials: independent
-    trials by gb_cs_generate_and_solve (same seeds, so the same problems), shared-matrix
-    trials by gb_cs_solve on the shared A and the trial's y.  The rate is scaled to the
+    """Single-trial FP32 drop-in, zero-initialised CGIHT, on the first timed step's trials:
+    the independent trials by gb_cs_generate_and_solve (same seeds, so the same problems),
+    the shared-matrix trials by gb_cs_solve on the shared A and the trial's y.  Each call is
+    timed with CUDA events on the stream it runs on (per-call setup included, as a caller of
+    the drop-in sees it; its solver time alone is reported too).  The rate is scaled to the
     3072 + 1024 mix; verdicts are compared with the tuned form's on the same trials."""
     import torch
 
@@ -633,51 +675,67 @@ def bench_plain(args, first_step):
     n, m, k, tid = wave_arrays(w)
     cnt = args.plain_trials
     sel = np.linspace(0, len(n) - 1, min(cnt, len(n))).astype(int)
-    ok = agree = 0
-    t0 = time.perf_counter()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        ev0.record()
+        out = fn()
+        ev1.record()
+        ev1.synchronize()
+        return out, ev0.elapsed_time(ev1)
+
+    def count(pv, tv):
+        pv, tv = np.asarray(pv, bool), np.asarray(tv, bool)
+        return {"agree": int(np.sum(pv == tv)), "only_plain": int(np.sum(pv & ~tv)), "only_tuned": int(np.sum(tv & ~pv))}
+
+    pv, tv, t_call, t_solver = [], [], 0.0, 0.0
     for i in sel:
         opts = gb.gaga_options("tol", TOL_REL, "tol_is_relative", 1, "maxiter", MAXITER, "seed", int(SEED + tid[i]))
-        x, xt, res = gb.generate_and_solve("NIHT", "gen", int(k[i]), int(m[i]), int(n[i]), 0, opts)
-        v = res.norms[1] <= 1e-3
-        ok += int(v)
-        agree += int(v == bool(r["verdict_batch"][i]))
-    t_ind = (time.perf_counter() - t0) / len(sel)
-    ok_ind = ok / len(sel)
-    agree_ind = agree
+        (x, xt, res), ms = timed(lambda: gb.generate_and_solve(ALG, "gen", int(k[i]), int(m[i]), int(n[i]), 0, opts))
+        t_call += ms
+        t_solver += res.times[0]
+        pv.append(res.norms[1] <= 1e-3)
+        tv.append(bool(r["verdict_batch"][i]))
+    t_ind, ts_ind = t_call / 1e3 / len(sel), t_solver / 1e3 / len(sel)
+    ok_ind = float(np.mean(pv))
+    c_ind = count(pv, tv)
     # shared-matrix trials: regenerate the step's problems (same keys) to get A and y
     ks, first = shared_part(w)
-    _, _, _, ok2, A, Y, X0 = gb.solve_shared_batch(gb.sweep.SHARED_M, gb.sweep.SHARED_N, ks, SHARED_SEED,
-                                                   tol_rel=TOL_REL, maxiter=MAXITER, first_trial=first, outputs=True)
+    _, _, _, _, A, Y, X0 = gb.solve_shared_batch(gb.sweep.SHARED_M, gb.sweep.SHARED_N, ks, SHARED_SEED,
+                                                 tol_rel=TOL_REL, maxiter=MAXITER, first_trial=first, outputs=True,
+                                                 alg=ALG)
     torch.cuda.synchronize()
     X0h = X0.cpu().numpy()
+    At = A.t()
     sel2 = np.linspace(0, len(ks) - 1, min(len(ks), max(4, cnt // 3))).astype(int)
-    ok = agree = 0
-    tt = 0.0
+    pv2, tv2, tt = [], [], 0.0
     for t in sel2:
         kt = int(np.count_nonzero(X0h[t]))
         opts = gb.gaga_options("tol", TOL_REL, "tol_is_relative", 1, "maxiter", MAXITER)
         yt = Y[t].contiguous()
-        torch.cuda.synchronize()
-        a = time.perf_counter()
-        x, it, _ = gb.gaga_cs("NIHT", "gen", yt, A.t(), kt, opts)
-        torch.cuda.synchronize()
-        tt += time.perf_counter() - a
-        v = np.linalg.norm(x.cpu().numpy() - X0h[t]) / np.linalg.norm(X0h[t]) <= 1e-3
-        ok += int(v)
-        agree += int(v == bool(ok2[t]))
-    t_sh = tt / len(sel2)
-    ok_sh = ok / len(sel2)
+        (x, it, _), ms = timed(lambda: gb.gaga_cs(ALG, "gen", yt, At, kt, opts))
+        tt += ms
+        pv2.append(np.linalg.norm(x.cpu().numpy() - X0h[t]) / np.linalg.norm(X0h[t]) <= 1e-3)
+        tv2.append(bool(r["verdict_shared"][t]))
+    t_sh = tt / 1e3 / len(sel2)
+    ok_sh = float(np.mean(pv2))
+    c_sh = count(pv2, tv2)
     n_ind, n_sh = TOTAL - SHARED, SHARED
     est_time = n_ind * t_ind + n_sh * t_sh
     est_ok = n_ind * ok_ind + n_sh * ok_sh
-    return {"value": est_ok / est_time, "unit": "trials/s",
-            "independent": {"trials": int(len(sel)), "s_per_trial": t_ind, "recovered_frac": ok_ind,
-                            "verdict_agreement": agree_ind / len(sel)},
+    tot = len(sel) + len(sel2)
+    return {"value": est_ok / est_time, "unit": "trials/s", "algorithm": ALG + " (zero-initialised)",
+            "timing": "CUDA events around each call on its stream",
+            "independent": {"trials": int(len(sel)), "s_per_trial": t_ind, "solver_s_per_trial": ts_ind,
+                            "recovered_frac": ok_ind, "verdicts": c_ind},
             "shared_matrix": {"trials": int(len(sel2)), "s_per_trial": t_sh, "recovered_frac": ok_sh,
-                              "verdict_agreement": agree / len(sel2)},
-            "verdict_agreement": (agree_ind + agree) / (len(sel) + len(sel2)),
-            "sample": "%d independent + %d shared-matrix trials of step %d, evenly spaced; rate = estimated "
-                      "recovered / estimated time of the 3072 + 1024 sweep" % (len(sel), len(sel2), w)}
+                              "verdicts": c_sh},
+            "verdict_agreement": (c_ind["agree"] + c_sh["agree"]) / tot,
+            "verdicts": {"trials": tot, "agree": c_ind["agree"] + c_sh["agree"],
+                         "only_plain_recovers": c_ind["only_plain"] + c_sh["only_plain"],
+                         "only_tuned_recovers": c_ind["only_tuned"] + c_sh["only_tuned"]},
+            "sample": "%d independent + %d shared-matrix trials of step %d; rate = estimated recovered / estimated "
+                      "time of the 3072 + 1024 sweep" % (len(sel), len(sel2), w)}
 
 
 def bench_only(args):
@@ -702,10 +760,12 @@ def bench_only(args):
     else:
         w = args.warmup
         n, m, k, tid = wave_arrays(w)
-        ns, iters, err, ok = gb.solve_batch(n, m, k, SEED, tid, alg="NIHT", tol_rel=TOL_REL, maxiter=MAXITER)
+        lp = gb.learned.load_weights()
+        ns, iters, err, ok = gb.solve_batch(n, m, k, SEED, tid, alg=ALG, tol_rel=TOL_REL, maxiter=MAXITER,
+                                            learned_params=lp)
         ks, first = shared_part(w)
         _, _, _, ok2 = gb.solve_shared_batch(gb.sweep.SHARED_M, gb.sweep.SHARED_N, ks, SHARED_SEED, tol_rel=TOL_REL,
-                                             maxiter=MAXITER, first_trial=first)
+                                             maxiter=MAXITER, first_trial=first, alg=ALG, learned_params=lp)
         out = bench_plain(args, (w, {"verdict_batch": ok, "verdict_shared": ok2}))
     print(json.dumps(out))
 
@@ -718,7 +778,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--plain-trials", type=int, default=768,
                     help="independent trials of the first timed step solved by the plain form (768 = all); a third "
-                         "as many shared-matrix trials")
+                         "as many shared-matrix trials (256 = all)")
+    ap.add_argument("--niht-steps", type=int, default=2, help="steps of the NIHT sweep leg (0: skip)")
     ap.add_argument("--cpu-trials", type=int, default=32)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--learned-trials", type=int, default=2048)
