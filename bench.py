@@ -479,8 +479,10 @@ def operators_roofline(peak, peak_kind, reps=20):
         rows = torch.randperm(n, device="cuda", generator=g)[:m].to(torch.int32)
         p = _lib.Problem(_lib.GB_OP_DCT, m, n, 0, None, None, 0, rows.data_ptr(), None, None, 0, 0, _lib.GB_DEVICE,
                          None)
-        one("dct_at_n2^%d" % ln, p, m, n, 1, 4.0 * n + 8 * m, "k_dct_scatter + 2 k_fft_pass, n=2^%d m=n/4" % ln)
-        one("dct_a_n2^%d" % ln, p, m, n, 0, 4.0 * n + 8 * m, "2 k_fft_pass + k_dct_select, n=2^%d m=n/4" % ln)
+        one("dct_at_n2^%d" % ln, p, m, n, 1, 4.0 * n + 8 * m,
+            "k_dct_scatter + 2 k_dct_pass (n/2-point transform), n=2^%d m=n/4" % ln)
+        one("dct_a_n2^%d" % ln, p, m, n, 0, 4.0 * n + 8 * m,
+            "2 k_dct_pass (n/2-point transform) + k_dct_select_half, n=2^%d m=n/4" % ln)
     for ln in (18, 22):
         n, m, d = 2 ** ln, 2 ** (ln - 2), 7
         rows = torch.randint(0, m, (n * d,), device="cuda", generator=g, dtype=torch.int32)

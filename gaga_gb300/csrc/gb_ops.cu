@@ -578,6 +578,276 @@ __global__ void __launch_bounds__(F1K_THREADS) k_fft1024(const GbState *__restri
   }
 }
 
+// ------------------------------------------------------------------ half-length DCT
+// For n >= 128 the DCT runs on an M = n/2 point complex transform instead of an n-point
+// one (the input is real): the forward transform packs the Makhoul-reordered signal v as
+// z_p = v_2p + i v_2p+1, computes Z = FFT_M(z) and recovers V_k = E_k + e^{-2 pi i k/n} O_k
+// with E_k = (Z_k + conj Z_{M-k}) / 2, O_k = (Z_k - conj Z_{M-k}) / 2i at the sampled rows
+// only (k_dct_select_half).  The transpose builds the Hermitian part H of the weighted
+// frequency image V_j = w_j c_j e^{i pi j / 2n}, packs Z_k = (H_k + H_{k+M}) + i (H_k -
+// H_{k+M}) e^{2 pi i k / n} in its first pass's load, and the inverse transform's output z_p
+// holds v_2p and v_2p+1, written back through the inverse Makhoul order.
+// The M-point transform is two passes, M = M1 * M2 (M1 = 2^l1 strided sequences, then M2 =
+// 2^l2 contiguous ones, four-step twiddle between them).  Inside a CTA every sequence of
+// length L runs as a Stockham autosort FFT with L/EPT threads, each holding EPT elements in
+// registers per pass (EPT = 4: radix-4 passes; 8: radix-8), then one smaller radix for the
+// rest of log2 L, twiddles from a per-CTA table, one shared-memory exchange per pass (the
+// layout pads one float2 per 8 so strided exchanges spread over the banks).  EPT is chosen
+// by measurement (dc_ept).
+#define DC_THREADS 256
+#define DC_PAD(i) ((i) + ((i) >> 3))
+enum { DC_F1 = 0, DC_F2 = 1, DC_I1 = 2, DC_I2 = 3 };
+
+// DFT of a[0..R-1] in place (natural order), exp(sgn 2 pi i r k / R), R = 2, 4 or 8
+template <int R, int SGN>
+__device__ __forceinline__ void dc_dft(float2 *a) {
+  constexpr float sg = (float)SGN;
+  if (R == 2) {
+    const float2 u = a[0], v = a[1];
+    a[0] = make_float2(u.x + v.x, u.y + v.y);
+    a[1] = make_float2(u.x - v.x, u.y - v.y);
+  } else if (R == 4) {
+    const float2 s0 = make_float2(a[0].x + a[2].x, a[0].y + a[2].y);
+    const float2 d0 = make_float2(a[0].x - a[2].x, a[0].y - a[2].y);
+    const float2 s1 = make_float2(a[1].x + a[3].x, a[1].y + a[3].y);
+    const float2 d1 = make_float2(a[1].x - a[3].x, a[1].y - a[3].y);
+    const float2 jd1 = make_float2(-sg * d1.y, sg * d1.x);  // (sg i) d1
+    a[0] = make_float2(s0.x + s1.x, s0.y + s1.y);
+    a[2] = make_float2(s0.x - s1.x, s0.y - s1.y);
+    a[1] = make_float2(d0.x + jd1.x, d0.y + jd1.y);
+    a[3] = make_float2(d0.x - jd1.x, d0.y - jd1.y);
+  } else {
+    // 8 = two 4-point DFTs (even, odd inputs) and a radix-2 combination
+    float2 e[4] = {a[0], a[2], a[4], a[6]}, o[4] = {a[1], a[3], a[5], a[7]};
+    dc_dft<4, SGN>(e);
+    dc_dft<4, SGN>(o);
+    const float h = 0.70710678118654752f;
+    const float2 w1 = make_float2(h, sg * h), w3 = make_float2(-h, sg * h);
+    const float2 t0 = o[0];
+    const float2 t1 = cmul(o[1], w1);
+    const float2 t2 = make_float2(-sg * o[2].y, sg * o[2].x);
+    const float2 t3 = cmul(o[3], w3);
+    const float2 t[4] = {t0, t1, t2, t3};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      a[k] = make_float2(e[k].x + t[k].x, e[k].y + t[k].y);
+      a[k + 4] = make_float2(e[k].x - t[k].x, e[k].y - t[k].y);
+    }
+  }
+}
+
+// one Stockham pass of radix R on a sequence of L = 2^l elements (threads tid < L/EPT of the
+// sequence, EPT / R butterflies each)
+template <int R, int SGN, int EPT>
+__device__ __forceinline__ void dc_stockham_pass(float2 *data, int L, int Ns, int tid, const float2 *tw) {
+  constexpr int NB = EPT / R;
+  float2 v[EPT];
+  const int stride = L / R, tws = L / (Ns * R);
+#pragma unroll
+  for (int b = 0; b < NB; ++b) {
+    const int j = tid + b * (L / EPT);
+    const int jm = j & (Ns - 1);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const float2 x = data[DC_PAD(j + r * stride)];
+      v[b * R + r] = r == 0 ? x : cmul(x, tw[jm * r * tws]);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int b = 0; b < NB; ++b) dc_dft<R, SGN>(v + b * R);
+#pragma unroll
+  for (int b = 0; b < NB; ++b) {
+    const int j = tid + b * (L / EPT);
+    const int jm = j & (Ns - 1);
+    const int base = (j - jm) * R + jm;
+#pragma unroll
+    for (int r = 0; r < R; ++r) data[DC_PAD(base + r * Ns)] = v[b * R + r];
+  }
+  __syncthreads();
+}
+
+// the whole FFT of one sequence (every thread of the CTA calls it; the CTA's sequences
+// run side by side): radix-EPT passes, then one smaller radix for the rest
+template <int SGN, int EPT>
+__device__ void dc_seq_fft(float2 *data, int l, int tid, const float2 *tw) {
+  constexpr int LE = EPT == 8 ? 3 : 2;
+  const int L = 1 << l;
+  int Ns = 1, rem = l;
+  for (; rem >= LE; rem -= LE, Ns *= EPT) dc_stockham_pass<EPT, SGN, EPT>(data, L, Ns, tid, tw);
+  if (rem == 2) dc_stockham_pass<4, SGN, EPT>(data, L, Ns, tid, tw);
+  else if (rem == 1) dc_stockham_pass<2, SGN, EPT>(data, L, Ns, tid, tw);
+}
+
+// Z_k of the transpose's first pass from the frequency image c (zero except at the sampled
+// rows): V_j = w_j c_j e^{i pi j / 2N}, H_j = (V_j + conj V_{N-j}) / 2, and
+// Z_k = (H_k + H_{k+M}) + i (H_k - H_{k+M}) e^{2 pi i k / N}.  The four phases it needs,
+// pi j / 2N at j = k, N-k, k+M, M-k, are t, pi/2 - t, t + pi/4 and pi/4 - t for
+// t = pi k / 2N, so (cos t, sin t) gives them all (and e^{2 pi i k/N} = e^{4 i t}).
+__device__ __forceinline__ float2 dc_zfreq(const float *__restrict__ c, int k, int M, int N, float cs, float sn) {
+  const float c0 = __ldg(c + k), c1 = __ldg(c + ((N - k) & (N - 1))), c2 = __ldg(c + k + M),
+              c3 = __ldg(c + ((M - k) & (N - 1)));
+  const float wn = sqrtf(2.0f / (float)N);
+  const float w0 = k == 0 ? sqrtf(1.0f / (float)N) : wn;  // weights of j = k, N-k (N-k = 0 when k = 0)
+  const float h = 0.70710678118654752f;
+  // V at k, N-k, k+M, M-k (index N-k wraps to 0 for k = 0: then c1 = c0 and its phase is 0)
+  const float2 v0 = make_float2(w0 * c0 * cs, w0 * c0 * sn);
+  const float2 v1 = k == 0 ? v0 : make_float2(wn * c1 * sn, wn * c1 * cs);                    // e^{i(pi/2 - t)}
+  const float2 v2 = make_float2(wn * c2 * h * (cs - sn), wn * c2 * h * (cs + sn));             // e^{i(t + pi/4)}
+  const float2 v3 = make_float2(wn * c3 * h * (cs + sn), wn * c3 * h * (cs - sn));             // e^{i(pi/4 - t)}
+  const float2 h0 = make_float2(0.5f * (v0.x + v1.x), 0.5f * (v0.y - v1.y));
+  const float2 h1 = make_float2(0.5f * (v2.x + v3.x), 0.5f * (v2.y - v3.y));
+  const float2 sm = make_float2(h0.x + h1.x, h0.y + h1.y), d = make_float2(h0.x - h1.x, h0.y - h1.y);
+  // e^{4 i t} by two complex squarings of e^{i t}
+  float2 e2 = make_float2(cs * cs - sn * sn, 2.0f * cs * sn);
+  const float2 e4 = make_float2(e2.x * e2.x - e2.y * e2.y, 2.0f * e2.x * e2.y);
+  const float2 w = cmul(d, e4);
+  return make_float2(sm.x - w.y, sm.y + w.x);  // sm + i w
+}
+
+// One pass of the M-point transform.  F1 / I1: sequences j2 < M2 of length M1 (stride M2),
+// loaded from x (Makhoul packing) / from the frequency image, four-step twiddle, stored
+// transposed T[k1 M2 + j2].  F2 / I2: sequences k1 < M1 of length M2 (contiguous rows of T),
+// stored as Zt[k1 M2 + k2] / into x through the inverse Makhoul order.
+template <int MODE, int EPT>
+__global__ void __launch_bounds__(512) k_dct_pass(const GbState *__restrict__ st, int pf, int l1, int l2,
+                                                  const float *__restrict__ vin, const float2 *__restrict__ cin,
+                                                  float2 *__restrict__ cout, float *__restrict__ rout) {
+  if (!gb_pred(st, pf)) return;
+  extern __shared__ float2 dsm[];
+  constexpr bool FIRST = MODE == DC_F1 || MODE == DC_I1;
+  constexpr int SGN = (MODE == DC_F1 || MODE == DC_F2) ? -1 : 1;
+  const int l = FIRST ? l1 : l2;
+  const int L = 1 << l, T = L / EPT;
+  const int B = blockDim.x / T;  // sequences per CTA
+  const int LP = L + L / 8;       // padded sequence buffer
+  const int M1 = 1 << l1, M2 = 1 << l2, M = M1 * M2, N = 2 * M;
+  const int nseq = FIRST ? M2 : M1;
+  float2 *buf = dsm;
+  float2 *tw = dsm + B * LP;
+  for (int t = threadIdx.x; t < L; t += blockDim.x) tw[t] = cis_pi((float)SGN, (2.0f * t) / (float)L);
+  const int bl = threadIdx.x / T, tid = threadIdx.x % T;
+  const int lb = __ffs(B) - 1;  // B = blockDim / (L / EPT) is a power of two; each thread moves EPT elements
+  for (int seq0 = blockIdx.x * B; seq0 < nseq; seq0 += gridDim.x * B) {
+    __syncthreads();
+    // load: every thread's global reads first (all in flight together), then shared memory
+    float2 vals[EPT];
+    // a thread's elements share b and step e by blockDim / B: phases by recurrence from two
+    // sincospif (each product adds ~1 ulp; EPT - 1 of them)
+    const int e0 = threadIdx.x >> lb, de = (int)blockDim.x >> lb;
+    float2 ph = make_float2(1.0f, 0.0f), dph = make_float2(1.0f, 0.0f);
+    if (MODE == DC_I1) {
+      // e^{i pi k / 2N} at k = e0 M2 + sq, times e^{i pi de M2 / 2N} per step
+      ph = cis_pi(1.0f, (float)(e0 * M2 + seq0 + (threadIdx.x & (B - 1))) / (float)(2 * N));
+      dph = cis_pi(1.0f, (float)(de * M2) / (float)(2 * N));
+    }
+#pragma unroll
+    for (int u = 0; u < EPT; ++u) {
+      const int q = threadIdx.x + u * blockDim.x;
+      int b, e;
+      if (FIRST) { b = q & (B - 1); e = q >> lb; }  // consecutive threads -> consecutive j2
+      else { b = q >> l; e = q & (L - 1); }          // contiguous rows
+      const int sq = seq0 + b;
+      float2 val = make_float2(0.0f, 0.0f);
+      if (sq < nseq) {
+        if (MODE == DC_F1) {
+          const int p = e * M2 + sq;
+          if (p < N / 4) {
+            val = make_float2(__ldg(vin + 4 * p), __ldg(vin + 4 * p + 2));  // v_2p = x[4p], v_2p+1 = x[4p+2]
+          } else {
+            val = make_float2(__ldg(vin + 2 * N - 4 * p - 1), __ldg(vin + 2 * N - 4 * p - 3));
+          }
+        } else if (MODE == DC_I1) {
+          val = dc_zfreq(vin, e * M2 + sq, M, N, ph.x, ph.y);
+        } else {
+          val = cin[(size_t)sq * M2 + e];
+        }
+      }
+      vals[u] = val;
+      if (MODE == DC_I1) ph = cmul(ph, dph);
+    }
+#pragma unroll
+    for (int u = 0; u < EPT; ++u) {
+      const int q = threadIdx.x + u * blockDim.x;
+      const int b = FIRST ? (q & (B - 1)) : (q >> l), e = FIRST ? (q >> lb) : (q & (L - 1));
+      buf[b * LP + DC_PAD(e)] = vals[u];
+    }
+    __syncthreads();
+    dc_seq_fft<SGN, EPT>(buf + bl * LP, l, tid, tw);
+    // four-step twiddle exp(sgn 2 pi i j2 k1 / M) at k1 = e0 + u de: two sincospif, then steps
+    float2 tf = make_float2(1.0f, 0.0f), dtf = make_float2(1.0f, 0.0f);
+    if (FIRST) {
+      const long long j2 = seq0 + (threadIdx.x & (B - 1));
+      tf = cis_pi((float)SGN, (2.0f * (float)((j2 * e0) & (M - 1))) / (float)M);
+      dtf = cis_pi((float)SGN, (2.0f * (float)((j2 * de) & (M - 1))) / (float)M);
+    }
+#pragma unroll
+    for (int u = 0; u < EPT; ++u) {
+      const int q = threadIdx.x + u * blockDim.x;
+      int b, e;
+      if (MODE == DC_F2) { b = q >> l; e = q & (L - 1); }  // contiguous Zt rows
+      else { b = q & (B - 1); e = q >> lb; }                // runs of B across the sequences
+      const int sq = seq0 + b;
+      const float2 twu = tf;
+      if (FIRST) tf = cmul(tf, dtf);
+      if (sq >= nseq) continue;
+      float2 val = buf[b * LP + DC_PAD(e)];
+      if (FIRST) {
+        val = cmul(val, twu);
+        cout[(size_t)e * M2 + sq] = val;
+      } else if (MODE == DC_F2) {
+        cout[(size_t)sq * M2 + e] = val;
+      } else {
+        const int p = sq + M1 * e;  // z_p = v_2p + i v_2p+1; x[2q] = v_q, x[2q+1] = v_{N-1-q}
+        if (p < N / 4) {
+          rout[4 * p] = val.x;
+          rout[4 * p + 2] = val.y;
+        } else {
+          rout[2 * N - 4 * p - 1] = val.x;
+          rout[2 * N - 4 * p - 3] = val.y;
+        }
+      }
+    }
+  }
+}
+
+// forward post-processing at the sampled rows from Zt (Z_{k1 + M1 k2} at k1 M2 + k2):
+// V_k = E + e^{-2 pi i k/N} O (E, O at k mod M), X_k = w_k Re(V_k e^{-i pi k / 2N})
+__global__ void k_dct_select_half(GbState *st, int pf, const float2 *__restrict__ Zt, const int *__restrict__ rows,
+                                  int m, int l1, int l2, const float *__restrict__ y, float *__restrict__ out,
+                                  int slot, float *red_part, unsigned int *tickets) {
+  if (!gb_pred(st, pf)) return;
+  const int M1 = 1 << l1, M2 = 1 << l2, M = M1 * M2, N = 2 * M;
+  const float wn0 = sqrtf(1.0f / (float)N), wn = sqrtf(2.0f / (float)N);
+  auto zat = [&](int kp) { return Zt[(size_t)(kp & (M1 - 1)) * M2 + (kp >> l1)]; };
+  float acc2 = 0.0f;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    const int k = rows[i];
+    const int kp = k & (M - 1);
+    const float2 a = zat(kp), b = zat((M - kp) & (M - 1));
+    const float2 E = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y - b.y));
+    const float2 D = make_float2(a.x - b.x, a.y + b.y);  // Z_k - conj Z_{M-k}
+    const float2 O = make_float2(0.5f * D.y, -0.5f * D.x);  // D / 2i
+    // with u = e^{-i pi k' / 2N} (k' = k mod M): e^{-2 pi i k'/N} = u^4, e^{-i pi k / 2N} = u or
+    // u e^{-i pi / 4} (k >= M)
+    float su, cu;
+    sincospif((float)kp / (float)(2 * N), &su, &cu);
+    const float2 u = make_float2(cu, -su);
+    const float2 u2 = cmul(u, u);
+    float2 t = cmul(u2, u2);
+    if (k >= M) t = make_float2(-t.x, -t.y);
+    const float2 tO = cmul(O, t);
+    const float2 V = make_float2(E.x + tO.x, E.y + tO.y);
+    const float h = 0.70710678118654752f;
+    const float2 r = k >= M ? make_float2(h * (u.x + u.y), h * (u.y - u.x)) : u;  // e^{-i pi k / 2N}
+    const float X = (k == 0 ? wn0 : wn) * (V.x * r.x - V.y * r.y);
+    const float o = y ? y[i] - X : X;
+    out[i] = o;
+    acc2 = fmaf(o, o, acc2);
+  }
+  if (slot >= 0) grid_reduce_publish<0>(acc2, slot, st, red_part, tickets);
+}
+
 // forward post-processing at the sampled rows: X_k = w_k Re(W_k exp(-i pi k / 2N))
 __global__ void k_dct_select(GbState *st, int pf, const float2 *__restrict__ W, const int *__restrict__ rows,
                              int m, int N, const float *__restrict__ y, float *__restrict__ out, int slot,
@@ -713,7 +983,53 @@ static void launch_fft(GbWork &w, cudaStream_t s, int pf, int pass, const float 
                                                                   cin, cout, rout);
 }
 
-// A x_S launch shape: row tiles of the (capacity) m times support splits, <= GB_MAXRB CTAs.
+// one pass of the half-length DCT transform (l1 + l2 = log2(n) - 1)
+static int dc_split(int logn, int *l1, int *l2) {
+  const int lm = logn - 1;
+  *l1 = lm / 2;
+  *l2 = lm - *l1;
+  return *l1 >= 3;  // sequences of at least 8 elements
+}
+// elements per thread of the half-length transform's sequences: 8 (radix-8 passes) unless
+// GB_CS_DCT_EPT=4 (radix-4 passes, twice the threads: measured slower on GB300, n = 2^20
+// A 35.0 vs 30.3 us, A^T 41.5 vs 35.4 us)
+static int dc_ept() {
+  static const int e = (getenv("GB_CS_DCT_EPT") && atoi(getenv("GB_CS_DCT_EPT")) == 4) ? 4 : 8;
+  return e;
+}
+static int dc_threads(int l, int ept) {
+  const int T = (1 << l) / ept;  // threads per sequence (l >= 3)
+  return T > DC_THREADS ? T : DC_THREADS;
+}
+static size_t dc_smem(int l, int ept) {
+  const int L = 1 << l, B = dc_threads(l, ept) / (L / ept);
+  return (size_t)(B * (L + L / 8) + L) * sizeof(float2);
+}
+template <int MODE, int EPT>
+static void launch_dct_pass_e(GbWork &w, cudaStream_t s, int pf, const float *vin, const float2 *cin, float2 *cout,
+                              float *rout) {
+  int l1, l2;
+  dc_split(w.op.logn, &l1, &l2);
+  constexpr bool FIRST = MODE == DC_F1 || MODE == DC_I1;
+  const int l = FIRST ? l1 : l2;
+  const int L = 1 << l, thr = dc_threads(l, EPT), B = thr / (L / EPT);
+  const int nseq = 1 << (FIRST ? l2 : l1);
+  int blocks = (nseq + B - 1) / B;
+  if (blocks > w.num_sms * 8) blocks = w.num_sms * 8;
+  k_dct_pass<MODE, EPT><<<blocks, thr, dc_smem(l, EPT), s>>>(w.st, pf, l1, l2, vin, cin, cout, rout);
+}
+template <int MODE>
+static void launch_dct_pass(GbWork &w, cudaStream_t s, int pf, const float *vin, const float2 *cin, float2 *cout,
+                            float *rout) {
+  int l1, l2;
+  dc_split(w.op.logn, &l1, &l2);
+  const int l = (MODE == DC_F1 || MODE == DC_I1) ? l1 : l2;
+  // 4 elements per thread up to 2048-point sequences (512 threads, the kernel's bound)
+  if (dc_ept() == 8 || l > 11) launch_dct_pass_e<MODE, 8>(w, s, pf, vin, cin, cout, rout);
+  else launch_dct_pass_e<MODE, 4>(w, s, pf, vin, cin, cout, rout);
+}
+
+// A x_S launch shape: row tiles of the (capacity) m times support splits, <= GB_MAXRB CTAs.// A x_S launch shape: row tiles of the (capacity) m times support splits, <= GB_MAXRB CTAs.
 // The split count is the smallest that best fills whole waves of the resident CTA slots
 // (blocks per SM of the tile height): a grid of 1.5 waves leaves half the GPU idle in its
 // tail.  share: the launch runs on a share of the SMs beside other launches (the batched
@@ -752,10 +1068,20 @@ void enq_A(GbWork &w, cudaStream_t s, const float *v, float *out, const float *y
     kern<<<grid, DV_THREADS, 0, s>>>(w.st, pf, op.A, argLDA(w), argM(w), w.av_ntile, w.av_nsplit, w.S, v, y, out,
                                      w.part, w.av_tickets, slot, w.red_part, w.tickets);
   } else if (op.kind == GB_OP_DCT) {
-    launch_fft<0, LOAD_MAKHOUL, STORE_CPLX_T>(w, s, pf, 1, v, nullptr, op.cbuf0, nullptr);
-    launch_fft<0, LOAD_CPLX, STORE_CPLX_NAT>(w, s, pf, 2, nullptr, op.cbuf0, op.cbuf1, nullptr);
-    k_dct_select<<<w.red_blocks, 256, 0, s>>>(w.st, pf, op.cbuf1, op.rows, op.m, op.n, y, out, slot,
-                                               w.red_part, w.tickets);
+    int l1, l2;
+    if (dc_split(op.logn, &l1, &l2)) {
+      launch_dct_pass<DC_F1>(w, s, pf, v, nullptr, op.cbuf0, nullptr);
+      launch_dct_pass<DC_F2>(w, s, pf, nullptr, op.cbuf0, op.cbuf1, nullptr);
+      // one row per thread where the grid reduction allows (its dependent gathers overlap)
+      const int sel_blocks = std::max(1, std::min(GB_MAXRB, (op.m + 255) / 256));
+      k_dct_select_half<<<sel_blocks, 256, 0, s>>>(w.st, pf, op.cbuf1, op.rows, op.m, l1, l2, y, out, slot,
+                                                    w.red_part, w.tickets);
+    } else {
+      launch_fft<0, LOAD_MAKHOUL, STORE_CPLX_T>(w, s, pf, 1, v, nullptr, op.cbuf0, nullptr);
+      launch_fft<0, LOAD_CPLX, STORE_CPLX_NAT>(w, s, pf, 2, nullptr, op.cbuf0, op.cbuf1, nullptr);
+      k_dct_select<<<w.red_blocks, 256, 0, s>>>(w.st, pf, op.cbuf1, op.rows, op.m, op.n, y, out, slot,
+                                                 w.red_part, w.tickets);
+    }
   } else {
     // one resident wave, at most GB_MAXRB CTAs (the grid reduction)
     int blocks = (op.m + SMV_RPW * SMV_WARPS - 1) / (SMV_RPW * SMV_WARPS);
@@ -792,8 +1118,14 @@ void enq_AT(GbWork &w, cudaStream_t s, const float *r, float *g, int pf) {
     int blocks = (op.m + 255) / 256;
     if (blocks > w.num_sms * 8) blocks = w.num_sms * 8;
     k_dct_scatter<<<blocks, 256, 0, s>>>(w.st, pf, op.rows, op.m, r, op.freq);
-    launch_fft<1, LOAD_FREQ, STORE_CPLX_T>(w, s, pf, 1, op.freq, nullptr, op.cbuf0, nullptr);
-    launch_fft<1, LOAD_CPLX, STORE_MAKHOUL_REAL>(w, s, pf, 2, nullptr, op.cbuf0, nullptr, g);
+    int l1, l2;
+    if (dc_split(op.logn, &l1, &l2)) {
+      launch_dct_pass<DC_I1>(w, s, pf, op.freq, nullptr, op.cbuf0, nullptr);
+      launch_dct_pass<DC_I2>(w, s, pf, nullptr, op.cbuf0, nullptr, g);
+    } else {
+      launch_fft<1, LOAD_FREQ, STORE_CPLX_T>(w, s, pf, 1, op.freq, nullptr, op.cbuf0, nullptr);
+      launch_fft<1, LOAD_CPLX, STORE_MAKHOUL_REAL>(w, s, pf, 2, nullptr, op.cbuf0, nullptr, g);
+    }
   } else {
     int blocks = (op.n + 255) / 256;
     if (blocks > w.num_sms * 16) blocks = w.num_sms * 16;
@@ -812,5 +1144,15 @@ gb_status gb_ops_init_attributes() {
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   GB_CUDA_TRY(cudaFuncSetAttribute(k_fft_pass<1, LOAD_CPLX, STORE_MAKHOUL_REAL>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  // the half-length transform: sequences up to 2^12 (n = 2^24 = 2^11 x 2^12 x 2)
+  const int dsm = (int)std::max(dc_smem(12, 8), dc_smem(12, 4));
+  GB_CUDA_TRY(cudaFuncSetAttribute(k_dct_pass<DC_F1, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm));
+  GB_CUDA_TRY(cudaFuncSetAttribute(k_dct_pass<DC_F2, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm));
+  GB_CUDA_TRY(cudaFuncSetAttribute(k_dct_pass<DC_I1, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm));
+  GB_CUDA_TRY(cudaFuncSetAttribute(k_dct_pass<DC_I2, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm));
+  GB_CUDA_TRY(cudaFuncSetAttribute(k_dct_pass<DC_F1, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm));
+  GB_CUDA_TRY(cudaFuncSetAttribute(k_dct_pass<DC_F2, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm));
+  GB_CUDA_TRY(cudaFuncSetAttribute(k_dct_pass<DC_I1, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm));
+  GB_CUDA_TRY(cudaFuncSetAttribute(k_dct_pass<DC_I2, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm));
   return GB_OK;
 }

@@ -60,7 +60,7 @@ def test_dct_small(gb, gbo, alg):
     x, iters, conv = gb.gaga_cs(alg, "dct", y, rows, ks, m, n, opts, index_base=0)
     xo, info = gbo.solve(alg, op, y, ks, tol)
     assert np.linalg.norm(x - x0) / np.linalg.norm(x0) < 1e-3
-    assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-3
+    assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-4
 
 
 @pytest.mark.parametrize("alg", ["NIHT", "CGIHT"])
@@ -233,15 +233,17 @@ def test_operator_apply(gb, gbo, kind):
     del keep
 
 
-@pytest.mark.parametrize("logn", [20, 22])
+@pytest.mark.parametrize("logn", [5, 6, 7, 8, 9, 10, 11, 13, 16, 20, 22, 24])
 def test_dct_operator_large(gb, gbo, logn):
-    """The subsampled DCT at the workload sizes (n = 2^20: both FFT passes are 1024-point,
-    the register 32 x 32 transform; n = 2^22: 2048-point, the shared-memory radix-2 pass)
-    against the oracle's FP64 DCT, A and A^T."""
+    """The subsampled DCT against the oracle's FP64 DCT, A and A^T.  n < 128 runs the
+    n-point shared-memory transform; from n = 128 on, the n/2-point transform in two passes
+    of 2^l1 x 2^l2 (l1 + l2 = log2 n - 1) Stockham sequences with 8 elements per thread:
+    every pass-length class from 8 (radix-8 only) through 16 and 32 (a radix-2 / radix-4
+    tail) up to 4096 (512 threads per sequence, n = 2^24), and the workload size 2^20."""
     torch = _torch()
     L = gb._lib.load()
     n = 2 ** logn
-    m = n // 4
+    m = max(1, n // 4)
     rows = gbo.gen_dct_rows(n, m, seed=logn)
     op = gbo.Op.dct(n, rows)
     rng = np.random.default_rng(logn)
