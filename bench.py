@@ -432,7 +432,9 @@ def operators_roofline(peak, peak_kind, reps=20):
     n=2^20, m=2^18 and the expander at n=2^18, m=2^16, d=7, and each of the last two also at
     n=2^22 (working set well above L2).  Algorithmic bytes per
     application: dense A^T r 4mn+4m+4n, A x 4mn+4n+4m; DCT A or A^T 4n+8m; expander A^T r
-    8nd+4m+4n, A x 8nd+4n+4m (rows+values, x, y)."""
+    b nd+4m+4n (b = 2-byte row indices when m <= 65536, else 4; the values are all equal and
+    not streamed), A x 4nd+4(m+1)+4n+4m (column indices, row pointers, x, y); the int32 +
+    fp32 layout's 8nd-based figures are kept beside them."""
     import ctypes as C
 
     import torch
@@ -489,8 +491,15 @@ def operators_roofline(peak, peak_kind, reps=20):
         vals = torch.full((n * d,), 1.0 / np.sqrt(d), device="cuda")
         p = _lib.Problem(_lib.GB_OP_SMV, m, n, 0, None, None, 0, rows.data_ptr(), None, vals.data_ptr(), d, 0,
                          _lib.GB_DEVICE, None)
-        one("smv_at_n2^%d" % ln, p, m, n, 1, 8.0 * n * d + 4 * m + 4 * n, "k_smv_AT n=2^%d m=n/4 d=7" % ln)
-        one("smv_a_n2^%d" % ln, p, m, n, 0, 8.0 * n * d + 4 * n + 4 * m, "k_smv_A n=2^%d m=n/4 d=7" % ln)
+        # the kernels' own layout: one value for all entries (none streamed), row indices of
+        # 2 bytes when m <= 65536 (A^T), column indices of 4 bytes plus the row pointers (A)
+        ib = 2 if m <= 65536 else 4
+        one("smv_at_n2^%d" % ln, p, m, n, 1, float(ib * n * d + 4 * m + 4 * n),
+            "k_smv_AT n=2^%d m=n/4 d=7, values 1/sqrt(d), %d-byte row indices" % (ln, ib))
+        out["smv_at_n2^%d" % ln]["bytes_int32_fp32_layout"] = 8.0 * n * d + 4 * m + 4 * n
+        one("smv_a_n2^%d" % ln, p, m, n, 0, float(4 * n * d + 4 * (m + 1) + 4 * n + 4 * m),
+            "k_smv_A n=2^%d m=n/4 d=7, values 1/sqrt(d), full x" % ln)
+        out["smv_a_n2^%d" % ln]["bytes_int32_fp32_layout"] = 8.0 * n * d + 4 * n + 4 * m
     del flush
     torch.cuda.empty_cache()
     return out
@@ -597,7 +606,7 @@ SINGLE_CONFIGS = (
 )
 
 
-def bench_configs(cpu=True, cpu_iters=3):
+def bench_configs(cpu=True, cpu_iters=3, only=None):
     """Each single-trial configuration solved by the drop-in on the GPU (generation included
     in `ms_total`, the solve alone in `ms_algorithm`, the library's own events), and the CPU
     oracle's time per iteration on the same problem (regenerated from the same keys by the
@@ -607,6 +616,8 @@ def bench_configs(cpu=True, cpu_iters=3):
 
     out = {}
     for name, alg, ens, k, m, n, d, extra, seed in SINGLE_CONFIGS:
+        if only and only not in name:
+            continue
         opts = gb.gaga_options("tol", TOL_REL, "tol_is_relative", 1, "maxiter", MAXITER, "seed", seed, *extra)
         for _ in range(2):  # the first call loads the kernels
             t0 = time.perf_counter()
@@ -756,7 +767,7 @@ def bench_only(args):
     elif args.only == "learned":
         out = bench_learned(args)
     elif args.only == "configs":
-        out = bench_configs(cpu=not args.no_cpu)
+        out = bench_configs(cpu=not args.no_cpu, only=args.config)
     elif args.only == "resident":
         out = resident_roofline(*peaks(), max_n=args.resident_max_n, sample=args.resident_sample)
     else:
@@ -789,6 +800,8 @@ def main():
     ap.add_argument("--resident-max-n", type=int, default=8192, help="--only resident: largest trial n")
     ap.add_argument("--resident-sample", type=int, default=0, help="--only resident: trials (0: all)")
     ap.add_argument("--no-configs", action="store_true", help="skip the single-trial configurations")
+    ap.add_argument("--config", default=None,
+                    help="--only configs: run the configurations whose name contains this text")
     ap.add_argument("--only", choices=["matvec", "gemm", "operators", "plain", "learned", "resident", "configs"],
                     help="run one measurement alone and print its JSON (for profiling)")
     args = ap.parse_args()

@@ -282,6 +282,27 @@ gb_status setup_problem(DeviceBuffers &db, GbWork &w, const gb_problem &p, cudaS
     op.csr_ptr = dptr;
     op.csr_col = dcol;
     op.csr_val = dcval;
+    // one value for every entry (bitwise): the operator kernels multiply by it and stream no
+    // values (the products, and so the sums, are the same floats)
+    uint32_t v0;
+    memcpy(&v0, vals.data(), sizeof(v0));
+    op.smv_cv = 1;
+    for (size_t e = 0; e < nz && op.smv_cv; ++e) {
+      uint32_t ve;
+      memcpy(&ve, &vals[e], sizeof(ve));
+      op.smv_cv = ve == v0;
+    }
+    op.smv_cval = vals[0];
+    op.smv_r16 = nullptr;
+    if (m <= 65536) {
+      std::vector<unsigned short> r16(nz);
+      for (size_t e = 0; e < nz; ++e) r16[e] = (unsigned short)rows[e];
+      unsigned short *dr16;
+      GB_TRY(db.alloc(&dr16, nz, false));
+      GB_CUDA_TRY(cudaMemcpyAsync(dr16, r16.data(), sizeof(unsigned short) * nz, cudaMemcpyHostToDevice, s));
+      GB_CUDA_TRY(cudaStreamSynchronize(s));
+      op.smv_r16 = dr16;
+    }
   } else {
     return bad("unknown operator kind");
   }

@@ -122,6 +122,12 @@ struct GbOp {
   int d;
   const int *csr_ptr, *csr_col;
   const float *csr_val;
+  // the operator kernels' compact copies: the column-grouped rows as 16-bit indices when
+  // m <= 65536 (null otherwise), and whether every value is the one float smv_cval (then
+  // neither value stream is read)
+  const unsigned short *smv_r16;
+  int smv_cv;
+  float smv_cval;
 };
 
 struct GbWork {

@@ -394,40 +394,73 @@ __global__ void k_hist(const GbState *st, int pf, const float *__restrict__ v, i
 }
 
 // k-th largest bin: the reference copies the first MaxBin counters to the host and scans
-// (GAGA/gaga/functions.cu:412-433).  One block of 1024 threads does the same scan.
+// (GAGA/gaga/functions.cu:412-433).  One block of 1024 threads does the same scan: thread t
+// sums a contiguous run of C bins (its loads issued KB_BATCH at a time, so a run costs a
+// few memory trips, not C), a shuffle scan over the 1024 run sums finds the run where the
+// count reaches k, and that run's thread walks it bin by bin (the same batches, now hitting
+// L1).  Integer sums: the result is the sequential scan's.
+#define KB_BATCH 16
 __global__ void __launch_bounds__(1024) k_kbin(GbState *st, int pf, const int *__restrict__ counters, int k) {
   if (!gb_pred(st, pf)) return;
   k = dimv(st, k);
-  __shared__ int scan[1024];
-  __shared__ int res_kbin, res_sum;
+  __shared__ int wsum[32];
+  __shared__ int res_kbin, res_sum, total;
   const int max_bin = st->max_bin;
   const int C = (max_bin + 1023) / 1024;
-  const int t = threadIdx.x;
-  const int b0 = t * C, b1 = min(b0 + C, max_bin);
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const int b0 = min(t * C, max_bin), b1 = min(b0 + C, max_bin);
   int csum = 0;
-  for (int b = b0; b < b1; ++b) csum += counters[b];
-  scan[t] = csum;
-  if (t == 0) { res_kbin = -2; res_sum = 0; }
-  __syncthreads();
-  for (int off = 1; off < 1024; off <<= 1) {  // inclusive Hillis-Steele scan
-    int v = t >= off ? scan[t - off] : 0;
-    __syncthreads();
-    scan[t] += v;
-    __syncthreads();
+  for (int b = b0; b < b1; b += KB_BATCH) {
+    int v[KB_BATCH];
+#pragma unroll
+    for (int u = 0; u < KB_BATCH; ++u) v[u] = b + u < b1 ? counters[b + u] : 0;
+#pragma unroll
+    for (int u = 0; u < KB_BATCH; ++u) csum += v[u];
   }
-  const int incl = scan[t], excl = incl - csum;
-  if (k > 0 && excl < k && incl >= k) {
+  if (t == 0) { res_kbin = -2; res_sum = 0; }
+  // inclusive scan of csum over the block: in each warp, then over the warp totals
+  int incl = csum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) wsum[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    int ws = wsum[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, ws, o);
+      if (lane >= o) ws += y;
+    }
+    wsum[lane] = ws;  // inclusive over warps
+    if (lane == 31) total = ws;
+  }
+  __syncthreads();
+  incl += wid > 0 ? wsum[wid - 1] : 0;
+  const int excl = incl - csum;
+  if (k > 0 && excl < k && incl >= k) {  // exactly one thread
     int s = excl;
-    for (int b = b0; b < b1; ++b) {
-      s += counters[b];
-      if (s >= k) { res_kbin = b; res_sum = s; break; }
+    bool found = false;
+    for (int b = b0; b < b1 && !found; b += KB_BATCH) {
+      int v[KB_BATCH];
+#pragma unroll
+      for (int u = 0; u < KB_BATCH; ++u) v[u] = b + u < b1 ? counters[b + u] : 0;
+#pragma unroll
+      for (int u = 0; u < KB_BATCH; ++u) {
+        if (!found && b + u < b1) {
+          s += v[u];
+          if (s >= k) { res_kbin = b + u; res_sum = s; found = true; }
+        }
+      }
     }
   }
   __syncthreads();
   if (t == 0) {
     int k_bin, sum;
     if (k <= 0) { k_bin = -1; sum = 0; }
-    else if (res_kbin == -2) { k_bin = max_bin - 1; sum = scan[1023]; }
+    else if (res_kbin == -2) { k_bin = max_bin - 1; sum = total; }
     else { k_bin = res_kbin; sum = res_sum; }
     const float intercept = st->max_value;
     const float slope = st->slope;

@@ -233,6 +233,34 @@ def test_operator_apply(gb, gbo, kind):
     del keep
 
 
+@pytest.mark.parametrize("m,n,d,ens", [(512, 2048, 7, 2), (512, 2048, 7, 3), (65536, 4096, 7, 1),
+                                        (65537, 4096, 7, 1), (70000, 4096, 5, 2), (3000, 4096, 12, 1),
+                                        (3000, 4096, 12, 2), (3000, 1024, 20, 1), (4000, 2 ** 19 + 7, 3, 2),
+                                        (4000, 2 ** 19, 3, 1)])
+def test_smv_operator_layouts(gb, gbo, m, n, d, ens):
+    """Every layout of the expander kernels, bit for bit against the oracle: 16-bit row
+    indices (m <= 65536) or 32-bit, one value for all entries (ensembles 1 and 3: no value
+    stream) or the +-1/sqrt(d) values streamed (ensemble 2), d up to 8, up to 16 and above
+    (one entry after another), n up to and beyond 2^19."""
+    torch = _torch()
+    L = gb._lib.load()
+    rng = np.random.default_rng(m + d)
+    rows, vals = gbo.gen_smv(m, n, d, ens, seed=m + 3 * d + ens)
+    op = gbo.Op.smv(m, n, d, rows, vals)
+    dr, dv = torch.tensor(rows, device="cuda"), torch.tensor(vals, device="cuda")
+    p = gb._lib.Problem(2, m, n, 0, None, None, 0, dr.data_ptr(), None, dv.data_ptr(), d, 0, 1, None)
+    x = rng.standard_normal(n).astype(np.float32)
+    x[rng.random(n) < 0.5] = 0.0
+    r = rng.standard_normal(m).astype(np.float32)
+    dx, dr_ = torch.tensor(x, device="cuda"), torch.tensor(r, device="cuda")
+    out_m = torch.zeros(m, device="cuda")
+    out_n = torch.zeros(n, device="cuda")
+    assert L.gb_cs_operator_apply(C.byref(p), 0, dx.data_ptr(), out_m.data_ptr()) == 0
+    assert L.gb_cs_operator_apply(C.byref(p), 1, dr_.data_ptr(), out_n.data_ptr()) == 0
+    assert np.array_equal(out_m.cpu().numpy(), gbo.A(op, x))
+    assert np.array_equal(out_n.cpu().numpy(), gbo.AT(op, r))
+
+
 @pytest.mark.parametrize("logn", [5, 6, 7, 8, 9, 10, 11, 13, 16, 20, 22, 24])
 def test_dct_operator_large(gb, gbo, logn):
     """The subsampled DCT against the oracle's FP64 DCT, A and A^T.  n < 128 runs the
