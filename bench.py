@@ -198,17 +198,18 @@ def bench_ours(args):
     from gaga_gb300 import autotune
 
     n0, m0, k0, t0_ = wave_arrays(sweep_rank_first(rank, world))
-    sched = autotune.tune_batch(n0, m0, k0, SEED, t0_, alg=ALG, tol_rel=TOL_REL, maxiter=MAXITER,
-                                use_cache=not args.retune)
     params = gb.learned.load_weights()
+    sched = autotune.tune_batch(n0, m0, k0, SEED, t0_, alg=ALG, tol_rel=TOL_REL, maxiter=MAXITER,
+                                use_cache=not args.retune, learned_params=params, grad_format=args.grad_format)
 
-    def solve_step(w, alg=ALG, lp=params, schedule=sched):
+    def solve_step(w, alg=ALG, lp=params, schedule=sched, gfmt=args.grad_format):
         """One quarter of the sweep: independent trials, then the shared-matrix trials."""
         n, m, k, tid = wave_arrays(w)
         t0 = time.perf_counter()
         ns, iters, err, ok = gb.solve_batch(n, m, k, SEED, tid, alg=alg, tol_rel=TOL_REL, maxiter=MAXITER,
                                             slots=schedule["slots"], sm_share=schedule["sm_share"],
-                                            cluster=schedule.get("cluster", 0), learned_params=lp)
+                                            cluster=schedule.get("cluster", 0), learned_params=lp,
+                                            grad_format=gfmt)
         t1 = time.perf_counter()
         nbytes, kms = gb.batch_last_stats()
         ks, first = shared_part(w)
@@ -274,6 +275,9 @@ def bench_ours(args):
                                "thread-block cluster per trial; larger: slot graphs; device trial queues, device "
                                "generation) + shared-matrix form (CGIHT in lockstep, split-BF16 tcgen05 GEMMs, FP64-"
                                "scalar CG debias), both starting from the learned warm start with the plain fallback",
+                       "independent_grad_operand": {"fp32": "FP32 A", "a24": "A rounded to 24 bits (3 bytes per "
+                                                    "entry)", "bf16": "A rounded to BF16 (2 bytes per entry)"}[
+                           args.grad_format] + " for A^T r; A x, residual and stopping test on FP32 A",
                        "schedule": {"slots": sched["slots"], "sm_share": sched["sm_share"],
                                     "cluster": sched.get("cluster", 0),
                                     "picked_by": "autotune over %d candidates on %d probe trials%s" % (
@@ -332,11 +336,11 @@ def bench_niht(args, solve_step):
     n0, m0, k0, t0_ = wave_arrays(0)
     sched = autotune.tune_batch(n0, m0, k0, SEED, t0_, alg="NIHT", tol_rel=TOL_REL, maxiter=MAXITER,
                                 use_cache=not args.retune)
-    solve_step(PARTS - 1, alg="NIHT", lp=None, schedule=sched)  # warm-up
+    solve_step(PARTS - 1, alg="NIHT", lp=None, schedule=sched, gfmt="fp32")  # warm-up
     ok = trials = 0
     kms = kb = ks = 0.0
     for s in range(args.niht_steps):
-        r = solve_step(s, alg="NIHT", lp=None, schedule=sched)
+        r = solve_step(s, alg="NIHT", lp=None, schedule=sched, gfmt="fp32")
         ok += r["ok"]
         trials += r["trials"]
         kms += r["kms"]
@@ -775,7 +779,7 @@ def bench_only(args):
         n, m, k, tid = wave_arrays(w)
         lp = gb.learned.load_weights()
         ns, iters, err, ok = gb.solve_batch(n, m, k, SEED, tid, alg=ALG, tol_rel=TOL_REL, maxiter=MAXITER,
-                                            learned_params=lp)
+                                            learned_params=lp, grad_format=args.grad_format)
         ks, first = shared_part(w)
         _, _, _, ok2 = gb.solve_shared_batch(gb.sweep.SHARED_M, gb.sweep.SHARED_N, ks, SHARED_SEED, tol_rel=TOL_REL,
                                              maxiter=MAXITER, first_trial=first, alg=ALG, learned_params=lp)
@@ -800,6 +804,9 @@ def main():
     ap.add_argument("--resident-max-n", type=int, default=8192, help="--only resident: largest trial n")
     ap.add_argument("--resident-sample", type=int, default=0, help="--only resident: trials (0: all)")
     ap.add_argument("--no-configs", action="store_true", help="skip the single-trial configurations")
+    ap.add_argument("--grad-format", default="bf16", choices=["fp32", "a24", "bf16"],
+                    help="the tuned form's A^T r operand for the independent trials: FP32 A, A rounded to 24 bits "
+                         "(3 bytes per entry) or to BF16 (2 bytes); A x, the residual and the stopping test stay FP32")
     ap.add_argument("--config", default=None,
                     help="--only configs: run the configurations whose name contains this text")
     ap.add_argument("--only", choices=["matvec", "gemm", "operators", "plain", "learned", "resident", "configs"],

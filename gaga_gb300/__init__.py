@@ -296,14 +296,19 @@ def generate_and_solve(alg, ens, k, m, n, d=0, opts=None):
     return x, xt, r
 
 
+GRAD_FORMATS = {"fp32": 0, "a24": 1, "bf16": 2}
+
+
 def solve_batch(n, m, k, seed, trial_ids=None, alg="NIHT", tol_rel=1e-4, maxiter=5000, stream=None,
-                learned_params=None, slots=0, sm_share=0, resident_n=0, cluster=0):
+                learned_params=None, slots=0, sm_share=0, resident_n=0, cluster=0, grad_format="fp32"):
     """Batched multi-trial dense form (gb_cs_solve_batch); learned_params (a CUDA tensor of
     MLP parameters, CGIHT only) turns on the learned warm start; slots / sm_share set the
     schedule of the slot graphs (0: automatic; gaga_gb300.autotune picks them by
     measurement); trials with n <= resident_n (0: 8192, < 0: none) are solved by the
     cluster-resident kernel with `cluster` CTAs per trial (0: 4, or more when the sizes need
-    it)."""
+    it); grad_format ("fp32", "a24" or "bf16") is the operand of A^T r (24-bit or BF16
+    copies of A stream 3 or 2 bytes per entry; A x, the residual and the stopping test keep
+    FP32 A)."""
     L = _lib.load()
     n = np.ascontiguousarray(n, dtype=np.int32)
     m = np.ascontiguousarray(m, dtype=np.int32)
@@ -313,7 +318,7 @@ def solve_batch(n, m, k, seed, trial_ids=None, alg="NIHT", tol_rel=1e-4, maxiter
                    int(seed) & 0xFFFFFFFF, {"NIHT": 0, "HTP": 1, "CGIHT": 6}[alg], float(tol_rel), int(maxiter),
                    0 if learned_params is None else 1,
                    None if learned_params is None else learned_params.data_ptr(), int(slots), int(sm_share), stream,
-                   int(resident_n), int(cluster))
+                   int(resident_n), int(cluster), GRAD_FORMATS[grad_format])
     iters = np.zeros(len(n), dtype=np.int32)
     err = np.zeros(len(n), dtype=np.float32)
     ok = np.zeros(len(n), dtype=np.int32)

@@ -3,8 +3,9 @@
 The batched form (gb_cs_solve_batch) runs `slots` trials at a time in slot graphs, each
 slot's kernels shaped for `sm_share` SMs (the dense A^T r grid is 4 CTAs per shared SM, the
 reductions one CTA per shared SM, and the A x_S row tiles x support splits fill whole waves
-of that many SMs), while NIHT trials with n <= 8192 go to the cluster-resident kernel with
-`cluster` CTAs per trial.  Which combination is fastest depends on the GPU and on the mix of
+of that many SMs), while trials with n <= 8192 go to the cluster-resident kernel with
+`cluster` CTAs per trial.  The probe runs the form the caller will run (algorithm, learned
+warm start, A^T r operand format).  Which combination is fastest depends on the GPU and on the mix of
 trial sizes, so it is measured: every candidate solves the same probe subset of the workload
 (every `stride`-th trial, all trial sizes represented), the second run of each is timed on
 the device, and the fastest candidate wins.  Results are cached per GPU, algorithm and trial-size mix in a JSON
@@ -17,11 +18,12 @@ import numpy as np
 
 SLOTS = (8, 16, 24)
 SHARE_FRACTIONS = (0.25, 0.5)
-# The resident kernel's cluster size is not tuned on the probe by default: a probe holds a
-# quarter of the trials, so each cluster gets few of them and the longest trial's latency
-# decides, which favours 8 CTAs per trial; whole waves of the sweep run faster with 4 (1662
-# vs 1700 ms per wave on GB300).
-CLUSTERS = (4,)
+# CTAs per cluster of the resident kernel.  Alone, its CGIHT trials run much faster with 8
+# (n <= 8192 of one sweep wave on GB300: 673 vs 1072 ms) because 4 CTAs leave the n = 8192
+# trials latency-bound; next to the slot graphs, where the whole GPU's HBM bandwidth is the
+# limit, both take the same time (1998 ms per wave).  A probe holds a quarter of the trials,
+# so the longest trial weighs more there than in a whole wave.
+CLUSTERS = (4, 8)
 
 
 def _cache_path():
@@ -29,28 +31,28 @@ def _cache_path():
                           os.path.join(os.path.expanduser("~"), ".cache", "gaga_gb300", "autotune.json"))
 
 
-def _key(alg, n, m):
+def _key(alg, n, m, form=""):
     import torch
 
     name = torch.cuda.get_device_name()
     sizes = sorted(set(zip(np.asarray(n).tolist(), np.asarray(m).tolist())))
     h = hash(tuple(sizes)) & 0xFFFFFFFF
-    return "%s|%s|%d sizes|%08x" % (name, alg, len(sizes), h)
+    return "%s|%s%s|%d sizes|%08x" % (name, alg, form, len(sizes), h)
 
 
 def tune_batch(n, m, k, seed, trial_ids=None, alg="NIHT", tol_rel=1e-4, maxiter=5000, stride=4, use_cache=True,
-               slots=SLOTS, fractions=SHARE_FRACTIONS, clusters=CLUSTERS, log=None):
-    """Pick (slots, sm_share, cluster) for solving trials like (n, m, k); returns a dict with
-    the choice and the measured device milliseconds of every candidate on the probe.  The
-    cluster size only matters for NIHT (the resident kernel); other algorithms tune with
-    cluster 0."""
+               slots=SLOTS, fractions=SHARE_FRACTIONS, clusters=CLUSTERS, log=None, learned_params=None,
+               grad_format="fp32"):
+    """Pick (slots, sm_share, cluster) for solving trials like (n, m, k) with the given
+    form; returns a dict with the choice and the measured device milliseconds of every
+    candidate on the probe."""
     import torch
 
     import gaga_gb300 as gb
 
     n, m, k = (np.asarray(a, dtype=np.int32) for a in (n, m, k))
     tid = np.arange(len(n), dtype=np.uint32) if trial_ids is None else np.asarray(trial_ids, dtype=np.uint32)
-    key = _key(alg, n, m)
+    key = _key(alg, n, m, "%s|%s" % ("learned" if learned_params is not None else "plain", grad_format))
     path = _cache_path()
     cache = {}
     if use_cache and os.path.exists(path):
@@ -67,13 +69,14 @@ def tune_batch(n, m, k, seed, trial_ids=None, alg="NIHT", tol_rel=1e-4, maxiter=
     probe = np.sort(order[::stride])
     pn, pm, pk, pt = n[probe], m[probe], k[probe], tid[probe]
     table = []
-    for c in (clusters if alg == "NIHT" else (0,)):
+    for c in clusters:
         for s in slots:
             for fr in fractions:
                 share = max(1, int(round(sms * fr)))
                 for rep in range(2):  # the first run builds the engine and its graphs
                     ns, it, err, ok = gb.solve_batch(pn, pm, pk, seed, pt, alg=alg, tol_rel=tol_rel,
-                                                     maxiter=maxiter, slots=s, sm_share=share, cluster=c)
+                                                     maxiter=maxiter, slots=s, sm_share=share, cluster=c,
+                                                     learned_params=learned_params, grad_format=grad_format)
                 _, ms = gb.batch_last_stats()
                 table.append({"slots": s, "sm_share": share, "cluster": c, "ms": ms, "recovered": int(ns)})
                 if log:

@@ -54,6 +54,7 @@ struct BatchParams {
   double *bytes;
   int learned;  // learned warm start (CGIHT)
   int *fb;      // per trial: the warm start was abandoned (solve again from zero)
+  int gfmt;     // the A^T r operand (GB_GRAD_*)
 };
 
 using gbgen::KEY_HI;
@@ -78,6 +79,7 @@ __device__ void load_trial(GbState *st, const BatchParams *bp, int q, cudaGraphC
   }
   const int t = bp->order[q];
   batch_trial_fields(st, t, bp->m[t], bp->n[t], bp->k[t], bp->maxiter, bp->alg);
+  st->gfmt = bp->gfmt;
   cudaGraphSetConditional(h_trial, 1u);
 }
 
@@ -175,7 +177,7 @@ struct Slot {
 };
 
 struct Engine {
-  int dev = -1, alg = -1, n_cap = 0, m_cap = 0, t_cap = 0, slots = 0, learned = 0, sm_share = 0;
+  int dev = -1, alg = -1, n_cap = 0, m_cap = 0, t_cap = 0, slots = 0, learned = 0, sm_share = 0, gfmt = 0;
   float *ml_params = nullptr;  // the warm-start MLP parameters (copied in by every call)
   int *dfb = nullptr;
   std::vector<Slot> slot;
@@ -228,6 +230,7 @@ gb_status build_slot_graph(Engine &E, Slot &S) {
   {
     // ---- draw the trial on the device
     k_b_gen_A<<<w.num_sms * 8, 256, 0, s1>>>(w.st, E.d_params, const_cast<float *>(w.op.A));
+    if (E.gfmt != GB_GRAD_FP32) enq_split_a(w, s1);
     k_b_gen_x<<<w.red_blocks, 256, 0, s1>>>(w.st, E.d_params, S.x0, w.xt, S.hist, w.red_part, w.tickets);
     k_b_ctrl<<<1, 32, 0, s1>>>(w.st, E.d_params, B_KEYS, 0);
     // support of x0: keys in n linear bins, the top bins holding >= k keys
@@ -271,11 +274,12 @@ gb_status build_slot_graph(Engine &E, Slot &S) {
 }
 
 gb_status setup_engine(Engine &E, int dev, int alg, int n_cap, int m_cap, int T, int slots, int learned,
-                       int sm_share) {
+                       int sm_share, int gfmt) {
   if (E.dev == dev && E.alg == alg && E.n_cap >= n_cap && E.m_cap >= m_cap && E.t_cap >= T && E.slots == slots &&
-      E.learned == learned && E.sm_share == sm_share)
+      E.learned == learned && E.sm_share == sm_share && E.gfmt == gfmt)
     return GB_OK;
   release(E);
+  E.gfmt = gfmt;
   E.learned = learned;
   E.sm_share = sm_share;
   E.dev = dev;
@@ -323,6 +327,17 @@ gb_status setup_engine(Engine &E, int dev, int alg, int n_cap, int m_cap, int T,
     float *Abuf = nullptr;
     GB_TRY(A((void **)&Abuf, (size_t)lda * n_cap * 4));
     op.A = Abuf;
+    op.gfmt = gfmt;
+    if (gfmt != GB_GRAD_FP32) {
+      unsigned short *hi = nullptr;
+      GB_TRY(A((void **)&hi, (size_t)lda * n_cap * 2));
+      op.A_hi = hi;
+      if (gfmt == GB_GRAD_A24) {
+        unsigned char *lo = nullptr;
+        GB_TRY(A((void **)&lo, (size_t)lda * n_cap));
+        op.A_lo = lo;
+      }
+    }
     GB_TRY(A((void **)&w.st, sizeof(GbState)));
     GB_TRY(A((void **)&w.red_part, (size_t)GB_NSLOT * GB_MAXRB * 4));
     GB_TRY(A((void **)&w.tickets, GB_NSLOT * 4));
@@ -358,10 +373,11 @@ gb_status setup_engine(Engine &E, int dev, int alg, int n_cap, int m_cap, int T,
 
 // Number of slots: the requested count (default 16: enough concurrency for small trials),
 // within 60% of free memory.
-int slots_for(int n_cap, int m_cap, size_t free_bytes, int T, int requested) {
+int slots_for(int n_cap, int m_cap, size_t free_bytes, int T, int requested, int gfmt) {
   int s = requested > 0 ? requested : 16;
   if (const char *e = getenv("GB_CS_BATCH_SLOTS")) s = std::max(1, atoi(e));
-  const double per = (double)((m_cap + 31) / 32 * 32) * n_cap * 4.0 * 1.05 + 64.0 * n_cap + (1 << 24);
+  const double eb = 4.0 + (gfmt == GB_GRAD_A24 ? 3.0 : gfmt == GB_GRAD_BF16 ? 2.0 : 0.0);  // bytes per entry of A
+  const double per = (double)((m_cap + 31) / 32 * 32) * n_cap * eb * 1.05 + 64.0 * n_cap + (1 << 24);
   while (s > 1 && s * per > 0.6 * (double)free_bytes) s--;
   return std::max(1, std::min(s, T));
 }
@@ -395,6 +411,12 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
   }
   if (b->maxiter < 0) {
     gb_set_error_message("maxiter must be >= 0", __FILE__, __LINE__);
+    return GB_BAD_ARG;
+  }
+  if (b->grad_format < GB_GRAD_FP32 || b->grad_format > GB_GRAD_BF16 ||
+      (b->grad_format != GB_GRAD_FP32 && b->alg == GB_ALG_HTP)) {
+    gb_set_error_message("grad_format: 0, 1 or 2, and FP32 for HTP (its CG projection needs A^T A)", __FILE__,
+                         __LINE__);
     return GB_BAD_ARG;
   }
   std::lock_guard<std::recursive_mutex> lock(gb_batch_mutex());
@@ -447,13 +469,14 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
   GB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const int sm_share = b->sm_share > 0 ? std::min(b->sm_share, sms) : std::max(1, sms / 2);
   const bool reuse = E.dev == dev && E.alg == b->alg && E.n_cap >= n_cap && E.m_cap >= m_cap && E.t_cap >= T &&
-                     E.sm_share == sm_share && (b->slots <= 0 || E.slots == b->slots);
+                     E.sm_share == sm_share && (b->slots <= 0 || E.slots == b->slots) && E.gfmt == b->grad_format;
   if (!reuse) {
     release(E);
     size_t free_b = 0, total_b = 0;
     GB_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
     GB_TRY(setup_engine(E, dev, b->alg, n_cap, m_cap, T,
-                        slots_for(n_cap, m_cap, free_b, std::max(T, 16), b->slots), learned, sm_share));
+                        slots_for(n_cap, m_cap, free_b, std::max(T, 16), b->slots, b->grad_format), learned, sm_share,
+                        b->grad_format));
   }
   cudaStream_t s = (cudaStream_t)b->stream;
   // trial table, longest (m*n) first
@@ -471,6 +494,7 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
   bp.iters = E.diters; bp.err = E.derr; bp.ok = E.dok; bp.bytes = E.dbytes;
   bp.learned = learned;
   bp.fb = learned ? E.dfb : nullptr;
+  bp.gfmt = b->grad_format;
   if (learned)
     GB_CUDA_TRY(cudaMemcpyAsync(E.ml_params, b->learned_params, sizeof(float) * gb_ml_num_params(),
                                 cudaMemcpyDeviceToDevice, s));
@@ -501,6 +525,7 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
     ra.n_cap = rn_cap; ra.m_cap = rm_cap; ra.cluster = b->cluster; ra.alg = b->alg;
     ra.ml_params = learned ? E.ml_params : nullptr;
     ra.fb = learned ? E.dfb : nullptr;
+    ra.gfmt = b->grad_format;
     GB_TRY(gb_resident_enqueue(ra, s));
   }
   for (size_t i = 0; i < nslot; ++i) GB_CUDA_TRY(cudaStreamWaitEvent(s, E.done[i], 0));

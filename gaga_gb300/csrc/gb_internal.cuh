@@ -78,9 +78,11 @@ struct GbState {
   double red[GB_NSLOT];
   // CGIHT support-change detection
   int changed;
-  // batched form: current trial index and algorithmic operator bytes of this trial
+  // batched form: current trial index and algorithmic operator bytes of this trial; the
+  // format of the A^T r operand (GB_GRAD_*)
   int trial, op_kind;
   double bytes;
+  int gfmt;
   // learned warm start (CGIHT): on, gave up after 10 iterations, residual at the warm x0
   int learned, fell_back;
   float err_warm0;
@@ -128,6 +130,12 @@ struct GbOp {
   const unsigned short *smv_r16;
   int smv_cv;
   float smv_cval;
+  // dense, batched form: the A^T r operand in a compact format (gfmt != GB_GRAD_FP32): the
+  // top 16 bits of each entry of A rounded to 24 (A24) or 16 (BF16) bits, and for A24 the
+  // next 8 bits, both indexed like A (column j at j * lda)
+  const unsigned short *A_hi;
+  const unsigned char *A_lo;
+  int gfmt;
 };
 
 struct GbWork {
@@ -300,6 +308,8 @@ void enq_A(GbWork &w, cudaStream_t s, const float *v, float *out, const float *y
 void enq_AT(GbWork &w, cudaStream_t s, const float *r, float *g, int pf);
 // dense only: g = A^T r fused with xt = g on the support, ||xt||^2 and max|g|
 void enq_AT_mask(GbWork &w, cudaStream_t s, const float *r, float *g, float *xt, int slot_sq, int slot_max, int pf);
+// batched form: the compact A^T r operand (op.gfmt) of the current trial from op.A
+void enq_split_a(GbWork &w, cudaStream_t s);
 // dense A x_S launch shape for (capacity) m and its partial buffer size in floats
 void gb_dense_av_shape(int m, int num_sms, bool share, int *ntile, int *nsplit, int *rows);
 size_t gb_dense_part_floats_av(int ntile, int nsplit, int rows);
@@ -361,9 +371,41 @@ gb_status gb_make_handle(cudaStream_t parent, cudaGraphConditionalHandle *h);
 gb_status gb_open_while(cudaStream_t parent, cudaStream_t body, cudaGraphConditionalHandle h);
 gb_status gb_close_while(cudaStream_t body);
 enum { GB_PHASE_HTP_CGINIT = 1000, GB_PHASE_HTP_STOP = 1001 };
+// the compact A^T r operand (GB_GRAD_A24 / GB_GRAD_BF16): b rounded to nearest even at bit
+// `drop` (8: 24-bit entries, 16: BF16), the dropped bits zero
+__device__ __forceinline__ uint32_t round_top_bits(uint32_t b, int drop) {
+  const uint32_t half = (1u << (drop - 1)) - 1u;
+  return (b + half + ((b >> drop) & 1u)) & ~((1u << drop) - 1u);
+}
+
+// entry pair (2q, 2q+1) of a 32-bit word of high parts and the low bytes l0, l1
+__device__ __forceinline__ float dec_lo(uint32_t w, uint32_t l) { return __uint_as_float((w << 16) | (l << 8)); }
+__device__ __forceinline__ float dec_hi(uint32_t w, uint32_t l) {
+  return __uint_as_float((w & 0xffff0000u) | (l << 8));
+}
+
+// 8 consecutive rows of one column: hi (16 bytes) and lo (8 bytes, LO only) decoded into a
+__device__ __forceinline__ void dec8(const uint4 h, const uint2 l, float (&a)[8], bool lo) {
+  const uint32_t l0 = lo ? l.x : 0u, l1 = lo ? l.y : 0u;
+  a[0] = dec_lo(h.x, l0 & 0xffu);
+  a[1] = dec_hi(h.x, (l0 >> 8) & 0xffu);
+  a[2] = dec_lo(h.y, (l0 >> 16) & 0xffu);
+  a[3] = dec_hi(h.y, l0 >> 24);
+  a[4] = dec_lo(h.z, l1 & 0xffu);
+  a[5] = dec_hi(h.z, (l1 >> 8) & 0xffu);
+  a[6] = dec_lo(h.w, (l1 >> 16) & 0xffu);
+  a[7] = dec_hi(h.w, l1 >> 24);
+}
+
+__device__ __forceinline__ float dec1(const unsigned short *hi, const unsigned char *lo, size_t e, bool has_lo) {
+  return __uint_as_float(((uint32_t)hi[e] << 16) | (has_lo ? (uint32_t)lo[e] << 8 : 0u));
+}
+
 // per-iteration algorithmic operator bytes of the dense operator (survey formula):
-// A^T r: 4mn + 4m + 4n ; A x_S: 4 m s + 8 s + 4 m
+// A^T r: b mn + 4m + 4n (b = 4 bytes per entry of A, 3 or 2 in the compact A^T formats) ;
+// A x_S: 4 m s + 8 s + 4 m
 __device__ __forceinline__ double dense_bytes(const GbState *st, int n_at, int n_a) {
   const double m = st->m, n = st->n, s = st->s_cnt;
-  return n_at * (4.0 * m * n + 4.0 * m + 4.0 * n) + n_a * (4.0 * m * s + 8.0 * s + 4.0 * m);
+  const double b = st->gfmt == GB_GRAD_A24 ? 3.0 : st->gfmt == GB_GRAD_BF16 ? 2.0 : 4.0;
+  return n_at * (b * m * n + 4.0 * m + 4.0 * n) + n_a * (4.0 * m * s + 8.0 * s + 4.0 * m);
 }

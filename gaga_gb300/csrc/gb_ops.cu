@@ -277,6 +277,135 @@ __global__ void __launch_bounds__(DA_THREADS, DA_BLOCKS_PER_SM) k_dense_at(GbSta
   if (slot_max >= 0) grid_reduce_publish<1>(gmax, slot_max, st, red_part, tickets);
 }
 
+// ---- the compact A^T r operand of the batched form (GB_GRAD_A24 / GB_GRAD_BF16)
+// A24 keeps the top 24 bits of each entry of A (sign, exponent, 15 mantissa bits), rounded to
+// nearest even, as a 16-bit high part and an 8-bit low part; BF16 the top 16 bits, rounded
+// the same way.  Decoded entries are exact FP32 values, accumulated in FP32.
+// split the current trial's A (st->m rows of st->n columns, column stride st->lda) into the
+// compact copy; rows m..lda-1 of the copy are zero
+template <int LO>
+__global__ void k_split_a(const GbState *st, const float *__restrict__ A, unsigned short *__restrict__ hi,
+                          unsigned char *__restrict__ lo) {
+  if (!st->active) return;
+  const int m = st->m, n = st->n, lda = st->lda;
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  for (int j = gw; j < n; j += nw) {
+    const size_t c = (size_t)j * lda;
+    for (int i = lane; i < lda; i += 32) {
+      const uint32_t b = i < m ? round_top_bits(__float_as_uint(__ldcs(A + c + i)), LO ? 8 : 16) : 0u;
+      hi[c + i] = (unsigned short)(b >> 16);
+      if (LO) lo[c + i] = (unsigned char)(b >> 8);
+    }
+  }
+}
+
+// k_dense_at over the compact operand: the same outputs (g = A^T r, xt = g on the support,
+// ||xt||^2, max|g|), 8 rows per thread and step (lda a multiple of 8)
+template <int LO>
+__global__ void __launch_bounds__(DA_THREADS, DA_BLOCKS_PER_SM) k_dense_at_c(GbState *st, int pf,
+                                                           const unsigned short *__restrict__ Ah,
+                                                           const unsigned char *__restrict__ Al, int lda, int m,
+                                                           int n, const float *__restrict__ r,
+                                                           float *__restrict__ g, const int *__restrict__ bins,
+                                                           float *__restrict__ xt, int slot_sq, int slot_max,
+                                                           float *red_part, unsigned int *tickets) {
+  if (!gb_pred(st, pf)) return;
+  lda = dimv(st, lda);
+  m = dimv(st, m);
+  n = dimv(st, n);
+  const int kb = st->k_bin;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int NWARP = DA_THREADS / 32;
+  __shared__ float wpart[NWARP][4];
+  float s2 = 0.0f, gmax = 0.0f;
+  const int m8 = m & ~7;
+  for (int j0 = blockIdx.x * 4; j0 < n; j0 += gridDim.x * 4) {
+    const int nc = min(4, n - j0);
+    float acc[4][2];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) acc[c][0] = acc[c][1] = 0.0f;
+    const size_t base = (size_t)j0 * lda;
+    int i = (warp * 32 + lane) * 8;
+    if (nc == 4) {
+#pragma unroll 2
+      for (; i < m8; i += DA_THREADS * 8) {
+        const float4 b0 = __ldg(reinterpret_cast<const float4 *>(r + i));
+        const float4 b1 = __ldg(reinterpret_cast<const float4 *>(r + i + 4));
+        uint4 h[4];
+        uint2 l[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          const size_t e = base + (size_t)c * lda + i;
+          h[c] = __ldcs(reinterpret_cast<const uint4 *>(Ah + e));
+          l[c] = LO ? __ldcs(reinterpret_cast<const uint2 *>(Al + e)) : make_uint2(0u, 0u);
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          float a[8];
+          dec8(h[c], l[c], a, LO);
+          acc[c][0] = fmaf(a[0], b0.x, acc[c][0]);
+          acc[c][1] = fmaf(a[1], b0.y, acc[c][1]);
+          acc[c][0] = fmaf(a[2], b0.z, acc[c][0]);
+          acc[c][1] = fmaf(a[3], b0.w, acc[c][1]);
+          acc[c][0] = fmaf(a[4], b1.x, acc[c][0]);
+          acc[c][1] = fmaf(a[5], b1.y, acc[c][1]);
+          acc[c][0] = fmaf(a[6], b1.z, acc[c][0]);
+          acc[c][1] = fmaf(a[7], b1.w, acc[c][1]);
+        }
+      }
+    } else {
+      for (; i < m8; i += DA_THREADS * 8) {
+        const float4 b0 = __ldg(reinterpret_cast<const float4 *>(r + i));
+        const float4 b1 = __ldg(reinterpret_cast<const float4 *>(r + i + 4));
+        for (int c = 0; c < nc; ++c) {
+          const size_t e = base + (size_t)c * lda + i;
+          float a[8];
+          dec8(__ldcs(reinterpret_cast<const uint4 *>(Ah + e)),
+               LO ? __ldcs(reinterpret_cast<const uint2 *>(Al + e)) : make_uint2(0u, 0u), a, LO);
+          acc[c][0] = fmaf(a[0], b0.x, acc[c][0]);
+          acc[c][1] = fmaf(a[1], b0.y, acc[c][1]);
+          acc[c][0] = fmaf(a[2], b0.z, acc[c][0]);
+          acc[c][1] = fmaf(a[3], b0.w, acc[c][1]);
+          acc[c][0] = fmaf(a[4], b1.x, acc[c][0]);
+          acc[c][1] = fmaf(a[5], b1.y, acc[c][1]);
+          acc[c][0] = fmaf(a[6], b1.z, acc[c][0]);
+          acc[c][1] = fmaf(a[7], b1.w, acc[c][1]);
+        }
+      }
+    }
+    if (i < m) {  // ragged tail inside one group of 8 rows
+      for (int c = 0; c < nc; ++c) {
+        const size_t e = base + (size_t)c * lda;
+        for (int q = i; q < m; ++q) acc[c][0] = fmaf(dec1(Ah, Al, e + q, LO), __ldg(r + q), acc[c][0]);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const float t = warp_sum(acc[c][0] + acc[c][1]);
+      if (lane == 0) wpart[warp][c] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x < nc) {
+      const int c = threadIdx.x;
+      float t = wpart[0][c];
+#pragma unroll
+      for (int w2 = 1; w2 < NWARP; ++w2) t += wpart[w2][c];
+      const int j = j0 + c;
+      g[j] = t;
+      if (xt) {
+        const float o = bins[j] <= kb ? t : 0.0f;
+        xt[j] = o;
+        s2 = fmaf(o, o, s2);
+      }
+      gmax = fmaxf(gmax, fabsf(t));
+    }
+    __syncthreads();
+  }
+  if (slot_sq >= 0) grid_reduce_publish<0>(s2, slot_sq, st, red_part, tickets);
+  if (slot_max >= 0) grid_reduce_publish<1>(gmax, slot_max, st, red_part, tickets);
+}
+
 // ------------------------------------------------------------------ DCT
 // Two-pass FFT: n = n1 * n2, index j = j1*n2 + j2, frequency k = k1 + n1*k2.
 //   pass 1: for each j2, an n1-point FFT over j1 (stride n2), times exp(-+2 pi i j2 k1 / n),
@@ -1149,6 +1278,12 @@ static int dense_at_grid(const GbWork &w) {
 void enq_AT_mask(GbWork &w, cudaStream_t s, const float *r, float *g, float *xt, int slot_sq, int slot_max, int pf) {
   const GbOp &op = w.op;
   const int grid = dense_at_grid(w);
+  if (op.gfmt != GB_GRAD_FP32) {
+    auto kern = op.gfmt == GB_GRAD_A24 ? k_dense_at_c<1> : k_dense_at_c<0>;
+    kern<<<grid, DA_THREADS, 0, s>>>(w.st, pf, op.A_hi, op.A_lo, argLDA(w), argM(w), argN(w), r, g, w.bins, xt,
+                                     slot_sq, slot_max, w.red_part, w.tickets);
+    return;
+  }
   if (op.vec4)
     k_dense_at<4><<<grid, DA_THREADS, 0, s>>>(w.st, pf, op.A, argLDA(w), argM(w), argN(w), r, g, w.bins, xt, slot_sq,
                                                slot_max, w.red_part, w.tickets);
@@ -1207,4 +1342,14 @@ gb_status gb_ops_init_attributes() {
   GB_CUDA_TRY(cudaFuncSetAttribute(k_dct_pass<DC_I1, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm));
   GB_CUDA_TRY(cudaFuncSetAttribute(k_dct_pass<DC_I2, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm));
   return GB_OK;
+}
+
+// the compact A^T r operand of the slot's current trial, from its FP32 A
+void enq_split_a(GbWork &w, cudaStream_t s) {
+  const GbOp &op = w.op;
+  if (op.gfmt == GB_GRAD_A24)
+    k_split_a<1><<<w.num_sms * 8, 256, 0, s>>>(w.st, op.A, const_cast<unsigned short *>(op.A_hi),
+                                               const_cast<unsigned char *>(op.A_lo));
+  else if (op.gfmt == GB_GRAD_BF16)
+    k_split_a<0><<<w.num_sms * 8, 256, 0, s>>>(w.st, op.A, const_cast<unsigned short *>(op.A_hi), nullptr);
 }

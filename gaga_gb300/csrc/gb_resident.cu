@@ -80,6 +80,11 @@ struct RsParams {
   // learned warm start (RS_CGIHT_ML): the MLP parameters; per trial whether it fell back
   const float *ml_params;
   int *fb;
+  // batched trials: the A^T r operand (GB_GRAD_*) and, when compact, its per-cluster copies
+  // (a_stride entries each, indexed like A)
+  int gfmt;
+  unsigned short *Ah;
+  unsigned char *Al;
 };
 
 // Shared-memory layout of one CTA (the same on host and device).
@@ -242,6 +247,88 @@ __device__ void at_own(const float *A, int lda, int q4, int c0, int nc, const fl
     else if (q4 >= 32) at_own_t<16, 2, 4>(A, lda, q4, c0, nc, r, out);
     else at_own_t<8, 4, 2>(A, lda, q4, c0, nc, r, out);
   }
+}
+
+// at_own_t over the compact operand (GB_GRAD_A24 with LO, GB_GRAD_BF16 without): groups of
+// 8 rows (16 bytes of high parts, 8 of low bytes), q8 = lda / 8 groups
+template <int G, int U, int V, int LO>
+__device__ void at_own_c_t(const unsigned short *Ah, const unsigned char *Al, int lda, int q8, int c0, int nc,
+                           const float *r, float *out) {
+  constexpr int PW = 32 / G;
+  constexpr int STEP = RS_WARPS * PW * V;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int gl = lane % G, gsub = lane / G;
+  const float4 *r4 = reinterpret_cast<const float4 *>(r);
+  for (int base = 0; base < nc; base += STEP) {
+    const int col0 = base + (wid * PW + gsub) * V;
+    float acc[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) acc[v] = 0.0f;
+    for (int i0 = gl; i0 < q8; i0 += U * G) {
+      uint4 h[V][U];
+      uint2 l[V][U];
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        const size_t e = (size_t)(c0 + col0 + v) * lda;
+        const uint4 *h4 = reinterpret_cast<const uint4 *>(Ah + e);
+        const uint2 *l2 = reinterpret_cast<const uint2 *>(Al + e);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int i = i0 + u * G;
+          const bool ok = col0 + v < nc && i < q8;
+          h[v][u] = ok ? __ldcg(h4 + i) : make_uint4(0u, 0u, 0u, 0u);
+          l[v][u] = (LO && ok) ? __ldcg(l2 + i) : make_uint2(0u, 0u);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int i = i0 + u * G;
+        if (i < q8) {
+          const float4 ra = r4[2 * i], rb = r4[2 * i + 1];
+#pragma unroll
+          for (int v = 0; v < V; ++v) {
+            float a[8];
+            dec8(h[v][u], l[v][u], a, LO);
+            acc[v] = fmaf(a[0], ra.x, acc[v]);
+            acc[v] = fmaf(a[1], ra.y, acc[v]);
+            acc[v] = fmaf(a[2], ra.z, acc[v]);
+            acc[v] = fmaf(a[3], ra.w, acc[v]);
+            acc[v] = fmaf(a[4], rb.x, acc[v]);
+            acc[v] = fmaf(a[5], rb.y, acc[v]);
+            acc[v] = fmaf(a[6], rb.z, acc[v]);
+            acc[v] = fmaf(a[7], rb.w, acc[v]);
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      float s = acc[v];
+#pragma unroll
+      for (int o = G >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (gl == 0 && col0 + v < nc) out[col0 + v] = s;
+    }
+  }
+}
+
+template <int LO>
+__device__ void at_own_c(const unsigned short *Ah, const unsigned char *Al, int lda, int q8, int c0, int nc,
+                         const float *r, float *out) {
+  if (q8 >= 256) at_own_c_t<32, 8, 1, LO>(Ah, Al, lda, q8, c0, nc, r, out);
+  else if (q8 >= 128) at_own_c_t<32, 4, 2, LO>(Ah, Al, lda, q8, c0, nc, r, out);
+  else if (q8 >= 64) at_own_c_t<32, 2, 4, LO>(Ah, Al, lda, q8, c0, nc, r, out);
+  else if (q8 >= 32) at_own_c_t<16, 2, 4, LO>(Ah, Al, lda, q8, c0, nc, r, out);
+  else at_own_c_t<8, 4, 2, LO>(Ah, Al, lda, q8, c0, nc, r, out);
+}
+
+// A^T r for the trial's own columns in the launch's operand format
+template <bool DEEP>
+__device__ __forceinline__ void at_trial(const RsParams &P, const float *A, const unsigned short *Ah,
+                                         const unsigned char *Al, int lda, int q4, int c0, int nc, const float *r,
+                                         float *out) {
+  if (P.gfmt == GB_GRAD_A24) at_own_c<1>(Ah, Al, lda, q4 / 2, c0, nc, r, out);
+  else if (P.gfmt == GB_GRAD_BF16) at_own_c<0>(Ah, Al, lda, q4 / 2, c0, nc, r, out);
+  else at_own<DEEP>(A, lda, q4, c0, nc, r, out);
 }
 
 // part (lda floats) = sum over the CTA's support entries e (ascending) of
@@ -566,6 +653,8 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
   int *mlc = reinterpret_cast<int *>(smem + L.o_mlc);
   constexpr bool IS_CG = ALG == RS_CGIHT || ALG == RS_CGIHT_ML;
   float *A = P.single ? const_cast<float *>(P.Ag) : P.A + (size_t)cid * P.a_stride;
+  unsigned short *Ah = P.Ah ? P.Ah + (size_t)cid * P.a_stride : nullptr;
+  unsigned char *Al = P.Al ? P.Al + (size_t)cid * P.a_stride : nullptr;
   int *xh = P.single ? nullptr : P.xhist + (size_t)cid * P.n_cap;
   {
     unsigned int *w = reinterpret_cast<unsigned int *>(st);
@@ -622,6 +711,7 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
       batch_trial_fields(st, t, m, n, P.k[t], P.maxiter,
                          IS_CG ? GB_ALG_CGIHT : ALG == RS_HTP ? GB_ALG_HTP : GB_ALG_NIHT);
       st->lda = lda;
+      st->gfmt = P.gfmt;
     }
     // ---- draw the trial (k_b_gen_A, k_b_gen_x, key bins, y = A x0 of gb_batch.cu)
     for (int col = wid; col < nc; col += RS_WARPS) {
@@ -629,6 +719,16 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
       float *cp = A + (size_t)j * lda;
       gbgen::gen_dense_column(cp, j, m, key, 0u, 1, lane, 32);
       for (int i = m + lane; i < lda; i += 32) cp[i] = 0.0f;
+      if (P.gfmt != GB_GRAD_FP32) {
+        // the compact A^T r operand, from the column this warp just wrote
+        __syncwarp();
+        const size_t e = (size_t)j * lda;
+        for (int i = lane; i < lda; i += 32) {
+          const uint32_t b = round_top_bits(__float_as_uint(cp[i]), P.gfmt == GB_GRAD_A24 ? 8 : 16);
+          Ah[e + i] = (unsigned short)(b >> 16);
+          if (P.gfmt == GB_GRAD_A24) Al[e + i] = (unsigned char)(b >> 8);
+        }
+      }
     }
     float mx = 0.0f;
     for (int c = tid; c < nc; c += RS_THREADS) {
@@ -721,7 +821,7 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
         __syncthreads();
       }
       // x = A^T y ; max|x| ; FindSupportSet ; Threshold
-      at_own<DEEP>(A, lda, q4, c0, nc, r, x);
+      at_trial<DEEP>(P, A, Ah, Al, lda, q4, c0, nc, r, x);
       __syncthreads();
       {
         float mxx = 0.0f;
@@ -850,7 +950,7 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
         }
         __syncthreads();
         // grad = A^T resid ; ||grad on the support||^2 ; max|grad|
-        at_own<DEEP>(A, lda, q4, c0, nc, r, grad);
+        at_trial<DEEP>(P, A, Ah, Al, lda, q4, c0, nc, r, grad);
         __syncthreads();
         {
           const int kb = st->k_bin;
@@ -1000,7 +1100,7 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
         av_rows(x, true, rowp, r, R_RES);
         if (tid == 0) st->red[R_RES] = combine_sum(cl, C, pub, R_RES);
         __syncthreads();
-        at_own<DEEP>(A, lda, q4, c0, nc, r, gp);
+        at_trial<DEEP>(P, A, Ah, Al, lda, q4, c0, nc, r, gp);
         __syncthreads();
         {
           const int kb = st->k_bin;
@@ -1022,7 +1122,7 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
             ctrl_phase(st, C_PUSH_RES, 0);
           }
           __syncthreads();
-          at_own<DEEP>(A, lda, q4, c0, nc, r, grad);  // grad = A^T r; x_thres = grad on the support
+          at_trial<DEEP>(P, A, Ah, Al, lda, q4, c0, nc, r, grad);  // grad = A^T r; x_thres = grad on the support
           __syncthreads();
           const int kb = st->k_bin;
           float sxt = 0.0f;
@@ -1195,9 +1295,11 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
 }
 
 struct ResEngine {
-  int dev = -1, n_cap = 0, m_cap = 0, C = 0, ncl = 0, t_cap = 0;
+  int dev = -1, n_cap = 0, m_cap = 0, C = 0, ncl = 0, t_cap = 0, gfmt = 0;
   size_t smem = 0, a_stride = 0;
   float *A = nullptr;
+  unsigned short *Ah = nullptr;  // compact A^T r operand (gfmt != GB_GRAD_FP32)
+  unsigned char *Al = nullptr;
   int *xhist = nullptr;
   int *order = nullptr, *queue = nullptr;
 };
@@ -1205,6 +1307,8 @@ std::map<int, ResEngine> g_res;
 
 void res_release(ResEngine &R) {
   if (R.A) cudaFree(R.A);
+  if (R.Ah) cudaFree(R.Ah);
+  if (R.Al) cudaFree(R.Al);
   if (R.xhist) cudaFree(R.xhist);
   if (R.order) cudaFree(R.order);
   R = ResEngine();
@@ -1291,7 +1395,7 @@ gb_status gb_resident_enqueue(const GbResidentArgs &a, cudaStream_t s) {
   // have above this call's sizes: the launch provides that layout's size, and an engine whose
   // layout no longer fits is rebuilt for this call
   const bool reuse = R.dev == dev && R.n_cap >= a.n_cap && R.m_cap >= a.m_cap && R.C == C &&
-                     R.t_cap >= a.count &&
+                     R.t_cap >= a.count && R.gfmt == a.gfmt &&
                      (long long)gb_resident_smem(R.n_cap, R.m_cap, C, a.alg, learned) <= gb_resident_max_smem();
   const size_t smem = gb_resident_smem(a.n_cap, a.m_cap, C, a.alg, learned);
   cudaLaunchConfig_t cfg;
@@ -1320,8 +1424,10 @@ gb_status gb_resident_enqueue(const GbResidentArgs &a, cudaStream_t s) {
     const size_t a_stride = (size_t)((a.m_cap + 31) / 32 * 32) * a.n_cap;
     size_t free_b = 0, total_b = 0;
     GB_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
-    while (ncl > 1 && (double)ncl * a_stride * 4.0 > 0.5 * (double)free_b) ncl--;
+    const double eb = 4.0 + (a.gfmt == GB_GRAD_A24 ? 3.0 : a.gfmt == GB_GRAD_BF16 ? 2.0 : 0.0);
+    while (ncl > 1 && (double)ncl * a_stride * eb > 0.5 * (double)free_b) ncl--;
     R.dev = dev;
+    R.gfmt = a.gfmt;
     R.n_cap = a.n_cap;
     R.m_cap = a.m_cap;
     R.C = C;
@@ -1330,6 +1436,8 @@ gb_status gb_resident_enqueue(const GbResidentArgs &a, cudaStream_t s) {
     R.a_stride = a_stride;
     R.t_cap = std::max(a.count, 1024);
     GB_CUDA_TRY(cudaMalloc(&R.A, (size_t)ncl * a_stride * 4));
+    if (a.gfmt != GB_GRAD_FP32) GB_CUDA_TRY(cudaMalloc(&R.Ah, (size_t)ncl * a_stride * 2));
+    if (a.gfmt == GB_GRAD_A24) GB_CUDA_TRY(cudaMalloc(&R.Al, (size_t)ncl * a_stride));
     GB_CUDA_TRY(cudaMalloc(&R.xhist, (size_t)ncl * a.n_cap * 4));
     GB_CUDA_TRY(cudaMalloc(&R.order, (size_t)(R.t_cap + 64) * 4));
     R.queue = R.order + R.t_cap;
@@ -1365,6 +1473,9 @@ gb_status gb_resident_enqueue(const GbResidentArgs &a, cudaStream_t s) {
   P.st_io = nullptr;
   P.ml_params = a.ml_params;
   P.fb = a.fb;
+  P.gfmt = a.gfmt;
+  P.Ah = R.Ah;
+  P.Al = R.Al;
   cfg.gridDim = dim3(R.ncl * C, 1, 1);
   cfg.dynamicSmemBytes = gb_resident_smem(R.n_cap, R.m_cap, C, a.alg, learned);
   GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, P));

@@ -30,6 +30,7 @@ struct GbResidentArgs {
   int alg;  // GB_ALG_NIHT, GB_ALG_HTP or GB_ALG_CGIHT
   const float *ml_params;  // CGIHT from the learned warm start (device MLP parameters) or null
   int *fb;                 // with it: per trial, 1 when the warm start was abandoned
+  int gfmt = 0;            // the A^T r operand (GB_GRAD_*)
 };
 
 gb_status gb_resident_enqueue(const GbResidentArgs &a, cudaStream_t s);

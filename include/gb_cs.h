@@ -253,7 +253,15 @@ typedef struct {
                                     the others (0: 8192; < 0: slots only) */
   int cluster;                   /* CTAs per cluster of the resident kernel (0: 4, more if the
                                     trial sizes need more shared memory than 4 CTAs have) */
+  int grad_format;               /* the operand of A^T r (GB_GRAD_*): FP32 A (0, the default),
+                                    or a compact copy of A written beside it when the trial is
+                                    drawn -- each entry rounded to 24 bits (3 bytes) or to BF16
+                                    (2 bytes), FP32 accumulation.  A x_S, the residual and the
+                                    stopping test keep FP32 A, so a solution of y = A x stays a
+                                    fixed point; only the gradient directions change. */
 } gb_batch;
+
+enum { GB_GRAD_FP32 = 0, GB_GRAD_A24 = 1, GB_GRAD_BF16 = 2 };
 
 /* Calls from several host threads run one at a time (the batched form's engines are
  * shared per device). */

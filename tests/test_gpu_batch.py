@@ -90,6 +90,11 @@ def test_batch_schedule_and_autotune(gb, tmp_path, monkeypatch):
     again = autotune.tune_batch(n, m, k, SEED, tid, alg="NIHT", maxiter=1000, stride=2, slots=(4, 8),
                                 fractions=(0.5, 1.0), clusters=(4,))
     assert again["cached"] and again["slots"] == res["slots"]
+    # CGIHT with the BF16 A^T r operand tunes the resident cluster size too, under its own key
+    cg = autotune.tune_batch(n, m, k, SEED, tid, alg="CGIHT", maxiter=1000, stride=2, slots=(4,), fractions=(0.5,),
+                             clusters=(4, 8), grad_format="bf16")
+    assert {c["cluster"] for c in cg["candidates"]} == {4, 8} and cg["cluster"] in (4, 8)
+    assert cg["key"] != res["key"] and not cg["cached"]
 
 
 def test_batch_calls_from_two_threads(gb):
@@ -112,3 +117,36 @@ def test_batch_calls_from_two_threads(gb):
     for o in out:
         assert o is not None
         assert np.array_equal(o[1], ref[1]) and np.array_equal(o[2], ref[2]) and np.array_equal(o[3], ref[3])
+
+
+@pytest.mark.parametrize("fmt", ["a24", "bf16"])
+@pytest.mark.parametrize("resident_n", [0, -1])
+def test_batch_compact_gradient_operand(gb, fmt, resident_n):
+    """CGIHT with the A^T r operand rounded to 24 bits or to BF16 (A x, the residual and the
+    stopping test on FP32 A), in the cluster-resident kernel (resident_n 0) and in the slot
+    graphs (-1): recovered trials meet the same 1e-3 error bar, verdicts agree with the FP32
+    operand on all but a few trials at the phase transition (24 bits: rounding at 2^-16
+    leaves every verdict of this sample unchanged), and the operator bytes shrink by the
+    format's share of A^T r."""
+    n, m, k, tid = pick([1024, 2048, 4096], 48)
+    ns0, it0, err0, ok0 = gb.solve_batch(n, m, k, SEED, tid, alg="CGIHT", tol_rel=1e-4, maxiter=1000,
+                                         resident_n=resident_n)
+    b0, _ = gb.batch_last_stats()
+    ns1, it1, err1, ok1 = gb.solve_batch(n, m, k, SEED, tid, alg="CGIHT", tol_rel=1e-4, maxiter=1000,
+                                         resident_n=resident_n, grad_format=fmt)
+    b1, _ = gb.batch_last_stats()
+    assert np.all(err1[ok1 == 1] <= 1e-3)
+    agree = int((ok0 == ok1).sum())
+    assert agree >= (len(n) if fmt == "a24" else len(n) - 3), (agree, len(n))
+    assert 0 < ns1 < len(n)
+    # bytes per iteration: A^T r streams 3 (2) of the FP32 operand's 4 bytes per entry
+    per0, per1 = b0 / max(1, it0.sum()), b1 / max(1, it1.sum())
+    assert per1 < per0 * (0.95 if fmt == "a24" else 0.85), (per0, per1)
+
+
+def test_batch_compact_gradient_operand_rejected_for_htp(gb):
+    from gaga_gb300 import _lib
+
+    n, m, k, tid = pick([1024], 2)
+    with pytest.raises(_lib.GagaError):
+        gb.solve_batch(n, m, k, SEED, tid, alg="HTP", tol_rel=1e-4, maxiter=100, grad_format="a24")
