@@ -479,6 +479,11 @@ def operators_roofline(peak, peak_kind, reps=20):
                          None)
         one("dense_at_n%d" % n, p, m, n, 1, 4.0 * m * n + 4 * m + 4 * n, "k_dense_at m=%d n=%d" % (m, n))
         one("dense_ax_n%d" % n, p, m, n, 0, 4.0 * m * n + 4 * n + 4 * m, "k_dense_av m=%d n=%d, full x" % (m, n))
+        if n == 16384:  # the batched form's compact A^T r operands (3 and 2 bytes per entry)
+            one("dense_at_a24_n%d" % n, p, m, n, 2, 3.0 * m * n + 4 * m + 4 * n,
+                "k_dense_at_c<1> m=%d n=%d, A rounded to 24 bits" % (m, n))
+            one("dense_at_bf16_n%d" % n, p, m, n, 3, 2.0 * m * n + 4 * m + 4 * n,
+                "k_dense_at_c<0> m=%d n=%d, A rounded to BF16" % (m, n))
         del A
     for ln in (20, 22):
         n, m = 2 ** ln, 2 ** (ln - 2)

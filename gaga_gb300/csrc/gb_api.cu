@@ -1083,12 +1083,31 @@ extern "C" gb_status gb_cs_operator_time(const gb_problem *p, int transpose, con
   DeviceBuffers db;
   GbWork w;
   memset(&w, 0, sizeof(w));
+  if (transpose < 0 || transpose > 3 || (transpose >= 2 && p->kind != GB_OP_DENSE))
+    return bad("gb_cs_operator_time: transpose 0, 1, or 2 / 3 (dense A^T r with the batched form's 24-bit / BF16 operand)");
   GB_TRY(setup_problem(db, w, *p, s, 1, 0, false));
   GbState st0;
   memset(&st0, 0, sizeof(st0));
   st0.active = 1;
   st0.flags[F_ALWAYS] = 1;
+  st0.m = p->m;
+  st0.n = p->n;
+  st0.lda = w.op.lda;
   GB_CUDA_TRY(cudaMemcpyAsync(w.st, &st0, sizeof(st0), cudaMemcpyHostToDevice, s));
+  if (transpose >= 2) {
+    // the batched form's compact A^T r operand, split from A once (outside the timing)
+    if (w.op.lda % 8) return bad("gb_cs_operator_time: the compact operand needs lda % 8 == 0");
+    unsigned short *hi = nullptr;
+    GB_TRY(db.alloc(&hi, (size_t)w.op.lda * p->n, false));
+    w.op.A_hi = hi;
+    if (transpose == 2) {
+      unsigned char *lo = nullptr;
+      GB_TRY(db.alloc(&lo, (size_t)w.op.lda * p->n, false));
+      w.op.A_lo = lo;
+    }
+    w.op.gfmt = transpose == 2 ? GB_GRAD_A24 : GB_GRAD_BF16;
+    enq_split_a(w, s);
+  }
   if (transpose) GB_CUDA_TRY(cudaMemcpyAsync(w.resid, d_in, sizeof(float) * p->m, cudaMemcpyDeviceToDevice, s));
   else if (w.op.kind == GB_OP_DENSE) enq_support_of_nonzeros(w, s, d_in, p->n);
   cudaEvent_t e0, e1;

@@ -1188,14 +1188,79 @@ extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *ite
     k_sc_init2<<<Tp, SH_THREADS, 0, s>>>(d);
   }
   GB_CUDA_TRY(cudaGetLastError());
-  // ---- NIHT iterations in lockstep: one graph, WHILE any trial is active
-  cudaStream_t c0, c1;
-  GB_CUDA_TRY(cudaStreamCreateWithFlags(&c0, cudaStreamNonBlocking));
-  GB_CUDA_TRY(cudaStreamCreateWithFlags(&c1, cudaStreamNonBlocking));
+  // ---- NIHT / CGIHT iterations in lockstep, WHILE any trial is active; then the debias
+  // R = Y - A X (and its BF16 form for the next product), G = A^T R over the active trials;
+  // NIHT then Q = A x_thres, CGIHT Q = A p and (unrestricted branch) Q2 = A g_S
+  auto iter_body = [&](cudaStream_t c) -> gb_status {
+    gb_status r = gemm(d.Acat, d.Xcat, d.R, m, 3 * n, 3 * n, 3 * n, d.Y, rb, split_r, true, c);
+    if (r == GB_OK) r = gemm(d.ATcat, rb, d.G, n, kg, 3 * m, kg, nullptr, nullptr, 0, true, c);
+    if (!cgiht) {
+      k_sh_mask<<<Tp, SH_THREADS, 0, c>>>(d);
+      if (r == GB_OK) r = gemm(d.Acat, d.XTbf, d.Q, m, kq, 3 * n, kq, nullptr, nullptr, 0, true, c);
+      k_sh_step<<<Tp, SH_THREADS, 0, c>>>(d);
+    } else {
+      k_sc_dir<<<Tp, SH_THREADS, 0, c>>>(d);
+      if (r == GB_OK)
+        r = gemm_map(d.Acat, d.XTbf, d.Q, m, kq, 3 * n, kq, nullptr, nullptr, 0, d.act_q, d.act_q_cnt, c);
+      if (r == GB_OK)
+        r = gemm_map(d.Acat, d.XT2, d.Q2, m, kq, 3 * n, kq, nullptr, nullptr, 0, d.act_u, d.act_u_cnt, c);
+      k_sc_step<<<Tp, SH_THREADS, 0, c>>>(d);
+    }
+    return r;
+  };
+  // debias of the converged trials: r = y - A x, g = A^T r, then CG in lockstep while any
+  // of them iterates
+  auto cg_prologue = [&](cudaStream_t c) -> gb_status {
+    k_cg_flags<<<(Tp + 255) / 256, 256, 0, c>>>(d);
+    k_sh_list<<<1, 1024, 0, c>>>(d, 1, passes, max_passes, 0);
+    gb_status r = gemm(d.Acat, d.Xcat, d.R, m, 3 * n, 3 * n, 3 * n, d.Y, nullptr, 0, true, c);
+    if (r == GB_OK) {
+      k_cg_start<<<Tp, SH_THREADS, 0, c>>>(d);
+      r = gemm(d.ATcat, d.Rcat, d.G, n, 3 * m, 3 * m, 3 * m, nullptr, nullptr, 0, true, c);
+    }
+    if (r == GB_OK) k_cg_dir<<<Tp, SH_THREADS, 0, c>>>(d);
+    return r;
+  };
+  auto cg_body = [&](cudaStream_t c) -> gb_status {
+    gb_status r = gemm(d.Acat, d.Xcat, d.Q, m, 3 * n, 3 * n, 3 * n, nullptr, nullptr, 0, true, c);  // q = A p
+    k_cg_step<<<Tp, SH_THREADS, 0, c>>>(d);
+    if (r == GB_OK) r = gemm(d.ATcat, d.Rcat, d.G, n, 3 * m, 3 * m, 3 * m, nullptr, nullptr, 0, true, c);
+    k_cg_dir<<<Tp, SH_THREADS, 0, c>>>(d);
+    return r;
+  };
+  cudaStream_t c0 = nullptr, c1 = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   gb_status rc = GB_OK;
-  {
+  // GB_CS_EAGER=1: the same kernels launched one by one from the host, the loop conditions
+  // read back after every pass (slower; for profilers that cannot see inside graphs with
+  // conditional nodes)
+  static const bool eager = getenv("GB_CS_EAGER") && atoi(getenv("GB_CS_EAGER")) != 0;
+  if (eager) {
+    auto go = [&](int which, bool *more) -> gb_status {
+      k_sh_list<<<1, 1024, 0, s>>>(d, which, passes, max_passes, 0);
+      int cnt = 0, p = 0;
+      GB_CUDA_TRY(cudaMemcpyAsync(&cnt, d.act_cnt, sizeof(int), cudaMemcpyDeviceToHost, s));
+      GB_CUDA_TRY(cudaMemcpyAsync(&p, passes, sizeof(int), cudaMemcpyDeviceToHost, s));
+      GB_CUDA_TRY(cudaStreamSynchronize(s));
+      *more = cnt > 0 && (which != 0 || p <= max_passes);
+      return GB_OK;
+    };
+    bool more = false;
+    rc = go(0, &more);
+    while (rc == GB_OK && more) {
+      rc = iter_body(s);
+      if (rc == GB_OK) rc = go(0, &more);
+    }
+    if (rc == GB_OK) rc = cg_prologue(s);
+    if (rc == GB_OK) rc = go(1, &more);
+    for (int guard = 0; rc == GB_OK && more && guard <= 4 * SH_CG_MAX; ++guard) {
+      rc = cg_body(s);
+      if (rc == GB_OK) rc = go(1, &more);
+    }
+  } else {
+    GB_CUDA_TRY(cudaStreamCreateWithFlags(&c0, cudaStreamNonBlocking));
+    GB_CUDA_TRY(cudaStreamCreateWithFlags(&c1, cudaStreamNonBlocking));
     cudaError_t e = cudaStreamBeginCapture(c0, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) {
       gb_set_error_message(cudaGetErrorString(e), __FILE__, __LINE__);
@@ -1208,50 +1273,20 @@ extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *ite
       rc = gb_open_while(c0, c1, h);
     }
     if (rc == GB_OK) {
-      // R = Y - A X (and its BF16 form for the next product), G = A^T R over the active
-      // trials; NIHT then Q = A x_thres, CGIHT Q = A p and (unrestricted branch) Q2 = A g_S
-      rc = gemm(d.Acat, d.Xcat, d.R, m, 3 * n, 3 * n, 3 * n, d.Y, rb, split_r, true, c1);
-      if (rc == GB_OK) rc = gemm(d.ATcat, rb, d.G, n, kg, 3 * m, kg, nullptr, nullptr, 0, true, c1);
-      if (!cgiht) {
-        k_sh_mask<<<Tp, SH_THREADS, 0, c1>>>(d);
-        if (rc == GB_OK) rc = gemm(d.Acat, d.XTbf, d.Q, m, kq, 3 * n, kq, nullptr, nullptr, 0, true, c1);
-        k_sh_step<<<Tp, SH_THREADS, 0, c1>>>(d);
-      } else {
-        k_sc_dir<<<Tp, SH_THREADS, 0, c1>>>(d);
-        if (rc == GB_OK)
-          rc = gemm_map(d.Acat, d.XTbf, d.Q, m, kq, 3 * n, kq, nullptr, nullptr, 0, d.act_q, d.act_q_cnt, c1);
-        if (rc == GB_OK)
-          rc = gemm_map(d.Acat, d.XT2, d.Q2, m, kq, 3 * n, kq, nullptr, nullptr, 0, d.act_u, d.act_u_cnt, c1);
-        k_sc_step<<<Tp, SH_THREADS, 0, c1>>>(d);
-      }
+      rc = iter_body(c1);
       k_sh_list<<<1, 1024, 0, c1>>>(d, 0, passes, max_passes, h);
       gb_status rc2 = gb_close_while(c1);
       if (rc == GB_OK) rc = rc2;
     }
-    // debias of the converged trials: r = y - A x, g = A^T r, then CG in lockstep while
-    // any of them iterates
     cudaGraphConditionalHandle h2 = 0;
-    if (rc == GB_OK) {
-      k_cg_flags<<<(Tp + 255) / 256, 256, 0, c0>>>(d);
-      k_sh_list<<<1, 1024, 0, c0>>>(d, 1, passes, max_passes, 0);
-      rc = gemm(d.Acat, d.Xcat, d.R, m, 3 * n, 3 * n, 3 * n, d.Y, nullptr, 0, true, c0);
-    }
-    if (rc == GB_OK) {
-      k_cg_start<<<Tp, SH_THREADS, 0, c0>>>(d);
-      rc = gemm(d.ATcat, d.Rcat, d.G, n, 3 * m, 3 * m, 3 * m, nullptr, nullptr, 0, true, c0);
-    }
+    if (rc == GB_OK) rc = cg_prologue(c0);
     if (rc == GB_OK) rc = gb_make_handle(c0, &h2);
     if (rc == GB_OK) {
-      k_cg_dir<<<Tp, SH_THREADS, 0, c0>>>(d);
       k_sh_list<<<1, 1024, 0, c0>>>(d, 1, passes, max_passes, h2);
       rc = gb_open_while(c0, c1, h2);
     }
     if (rc == GB_OK) {
-      rc = gemm(d.Acat, d.Xcat, d.Q, m, 3 * n, 3 * n, 3 * n, nullptr, nullptr, 0, true, c1);  // q = A p
-      k_cg_step<<<Tp, SH_THREADS, 0, c1>>>(d);
-      if (rc == GB_OK)
-        rc = gemm(d.ATcat, d.Rcat, d.G, n, 3 * m, 3 * m, 3 * m, nullptr, nullptr, 0, true, c1);
-      k_cg_dir<<<Tp, SH_THREADS, 0, c1>>>(d);
+      rc = cg_body(c1);
       k_sh_list<<<1, 1024, 0, c1>>>(d, 1, passes, max_passes, h2);
       gb_status rc2 = gb_close_while(c1);
       if (rc == GB_OK) rc = rc2;
@@ -1263,13 +1298,13 @@ extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *ite
       rc = GB_CUDA_ERROR;
     }
     graph = g2;
-  }
-  if (rc == GB_OK) {
-    cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
-    if (e == cudaSuccess) e = cudaGraphLaunch(exec, s);
-    if (e != cudaSuccess) {
-      gb_set_error_message(cudaGetErrorString(e), __FILE__, __LINE__);
-      rc = GB_CUDA_ERROR;
+    if (rc == GB_OK) {
+      e = cudaGraphInstantiate(&exec, graph, 0);
+      if (e == cudaSuccess) e = cudaGraphLaunch(exec, s);
+      if (e != cudaSuccess) {
+        gb_set_error_message(cudaGetErrorString(e), __FILE__, __LINE__);
+        rc = GB_CUDA_ERROR;
+      }
     }
   }
   if (rc == GB_OK) {
@@ -1310,8 +1345,8 @@ extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *ite
   }
   if (exec) cudaGraphExecDestroy(exec);
   if (graph) cudaGraphDestroy(graph);
-  cudaStreamDestroy(c0);
-  cudaStreamDestroy(c1);
+  if (c0) cudaStreamDestroy(c0);
+  if (c1) cudaStreamDestroy(c1);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return rc;

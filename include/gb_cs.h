@@ -192,7 +192,9 @@ gb_status gb_cs_operator_apply(const gb_problem *p, int transpose, const float *
 /* Measurement helper (no reference counterpart): the device time of gb_cs_operator_apply's
  * kernels, set up once, CUDA events around each of `reps` applications after `warmup`
  * untimed ones; a non-NULL d_flush of flush_bytes is overwritten before each application
- * (outside the events) so operands come from HBM.  *ms_out = mean ms per application. */
+ * (outside the events) so operands come from HBM.  *ms_out = mean ms per application.
+ * transpose 2 / 3 (dense, lda % 8 == 0): A^T in with the batched form's compact operand,
+ * A rounded to 24 bits / to BF16 (gb_batch.grad_format), split from A before the timing. */
 gb_status gb_cs_operator_time(const gb_problem *p, int transpose, const float *d_in, float *d_out, int warmup,
                               int reps, void *d_flush, size_t flush_bytes, float *ms_out);
 

@@ -290,3 +290,33 @@ def test_dct_operator_large(gb, gbo, logn):
     np.testing.assert_allclose(ga, go, rtol=0, atol=2e-5 * np.abs(go).max())
     assert np.linalg.norm(ya - yo) / np.linalg.norm(yo) < 1e-5
     assert np.linalg.norm(ga - go) / np.linalg.norm(go) < 1e-5
+
+
+@pytest.mark.parametrize("tr,drop", [(2, 8), (3, 16)])
+def test_dense_compact_gradient_operand(gb, tr, drop):
+    """A^T r over the batched form's compact operand (A rounded to nearest even at bit 8:
+    24-bit entries, or at bit 16: BF16) against the same rounding done in numpy and an FP64
+    product; FP32 accumulation, so within 1e-5 of max |A^T r|.  Ragged m (a tail inside the
+    last group of 8 rows) and n not a multiple of 4."""
+    torch = _torch()
+    L = gb._lib.load()
+    m, n, lda = 301, 1003, 304
+    rng = np.random.default_rng(tr)
+    A = np.zeros((n, lda), dtype=np.float32)
+    A[:, :m] = rng.standard_normal((n, m)).astype(np.float32) / np.sqrt(m)
+    r = rng.standard_normal(m).astype(np.float32)
+    b = A[:, :m].view(np.uint32).astype(np.uint64)
+    half = (1 << (drop - 1)) - 1
+    q = ((b + half + ((b >> drop) & 1)) & ~np.uint64((1 << drop) - 1)).astype(np.uint32).view(np.float32)
+    want = q.astype(np.float64) @ r.astype(np.float64)
+    dA, dr = torch.tensor(A.ravel(), device="cuda"), torch.tensor(r, device="cuda")
+    out = torch.zeros(n, device="cuda")
+    p = gb._lib.Problem(0, m, n, 0, None, dA.data_ptr(), lda, None, None, None, 0, 0, 1, None)
+    ms = C.c_float(0)
+    assert L.gb_cs_operator_time(C.byref(p), tr, dr.data_ptr(), out.data_ptr(), 0, 1, None, 0, C.byref(ms)) == 0
+    got = out.cpu().numpy()
+    assert np.abs(got - want).max() <= 1e-5 * np.abs(want).max()
+    # and it is not the FP32 product: the rounding is visible at this tolerance for BF16
+    if drop == 16:
+        full = A[:, :m].astype(np.float64) @ r.astype(np.float64)
+        assert np.abs(got - full).max() > 1e-4 * np.abs(full).max()
