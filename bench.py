@@ -200,7 +200,8 @@ def bench_ours(args):
     n0, m0, k0, t0_ = wave_arrays(sweep_rank_first(rank, world))
     params = gb.learned.load_weights()
     sched = autotune.tune_batch(n0, m0, k0, SEED, t0_, alg=ALG, tol_rel=TOL_REL, maxiter=MAXITER,
-                                use_cache=not args.retune, learned_params=params, grad_format=args.grad_format)
+                                use_cache=not args.retune, learned_params=params, grad_format=args.grad_format,
+                                residual_refresh=args.residual_refresh)
 
     def solve_step(w, alg=ALG, lp=params, schedule=sched, gfmt=args.grad_format):
         """One quarter of the sweep: independent trials, then the shared-matrix trials."""
@@ -209,7 +210,7 @@ def bench_ours(args):
         ns, iters, err, ok = gb.solve_batch(n, m, k, SEED, tid, alg=alg, tol_rel=TOL_REL, maxiter=MAXITER,
                                             slots=schedule["slots"], sm_share=schedule["sm_share"],
                                             cluster=schedule.get("cluster", 0), learned_params=lp,
-                                            grad_format=gfmt)
+                                            grad_format=gfmt, residual_refresh=args.residual_refresh)
         t1 = time.perf_counter()
         nbytes, kms = gb.batch_last_stats()
         ks, first = shared_part(w)
@@ -278,6 +279,9 @@ def bench_ours(args):
                        "independent_grad_operand": {"fp32": "FP32 A", "a24": "A rounded to 24 bits (3 bytes per "
                                                     "entry)", "bf16": "A rounded to BF16 (2 bytes per entry)"}[
                            args.grad_format] + " for A^T r; A x, residual and stopping test on FP32 A",
+                       "independent_residual": ("y - A x every %d-th restricted step on an unchanged support, "
+                                                "r - alpha A p between" % args.residual_refresh)
+                       if args.residual_refresh > 0 else "y - A x at every step",
                        "schedule": {"slots": sched["slots"], "sm_share": sched["sm_share"],
                                     "cluster": sched.get("cluster", 0),
                                     "picked_by": "autotune over %d candidates on %d probe trials%s" % (
@@ -784,7 +788,8 @@ def bench_only(args):
         n, m, k, tid = wave_arrays(w)
         lp = gb.learned.load_weights()
         ns, iters, err, ok = gb.solve_batch(n, m, k, SEED, tid, alg=ALG, tol_rel=TOL_REL, maxiter=MAXITER,
-                                            learned_params=lp, grad_format=args.grad_format)
+                                            learned_params=lp, grad_format=args.grad_format,
+                                            residual_refresh=args.residual_refresh)
         ks, first = shared_part(w)
         _, _, _, ok2 = gb.solve_shared_batch(gb.sweep.SHARED_M, gb.sweep.SHARED_N, ks, SHARED_SEED, tol_rel=TOL_REL,
                                              maxiter=MAXITER, first_trial=first, alg=ALG, learned_params=lp)
@@ -812,6 +817,9 @@ def main():
     ap.add_argument("--grad-format", default="bf16", choices=["fp32", "a24", "bf16"],
                     help="the tuned form's A^T r operand for the independent trials: FP32 A, A rounded to 24 bits "
                          "(3 bytes per entry) or to BF16 (2 bytes); A x, the residual and the stopping test stay FP32")
+    ap.add_argument("--residual-refresh", type=int, default=8,
+                    help="the tuned form's CGIHT residual recurrence: y - A x every N-th restricted step on an "
+                         "unchanged support, r - alpha A p between (0: y - A x at every step)")
     ap.add_argument("--config", default=None,
                     help="--only configs: run the configurations whose name contains this text")
     ap.add_argument("--only", choices=["matvec", "gemm", "operators", "plain", "learned", "resident", "configs"],

@@ -42,7 +42,7 @@ def _key(alg, n, m, form=""):
 
 def tune_batch(n, m, k, seed, trial_ids=None, alg="NIHT", tol_rel=1e-4, maxiter=5000, stride=4, use_cache=True,
                slots=SLOTS, fractions=SHARE_FRACTIONS, clusters=CLUSTERS, log=None, learned_params=None,
-               grad_format="fp32"):
+               grad_format="fp32", residual_refresh=0):
     """Pick (slots, sm_share, cluster) for solving trials like (n, m, k) with the given
     form; returns a dict with the choice and the measured device milliseconds of every
     candidate on the probe."""
@@ -52,7 +52,8 @@ def tune_batch(n, m, k, seed, trial_ids=None, alg="NIHT", tol_rel=1e-4, maxiter=
 
     n, m, k = (np.asarray(a, dtype=np.int32) for a in (n, m, k))
     tid = np.arange(len(n), dtype=np.uint32) if trial_ids is None else np.asarray(trial_ids, dtype=np.uint32)
-    key = _key(alg, n, m, "%s|%s" % ("learned" if learned_params is not None else "plain", grad_format))
+    key = _key(alg, n, m, "%s|%s|r%d" % ("learned" if learned_params is not None else "plain", grad_format,
+                                          residual_refresh))
     path = _cache_path()
     cache = {}
     if use_cache and os.path.exists(path):
@@ -76,7 +77,8 @@ def tune_batch(n, m, k, seed, trial_ids=None, alg="NIHT", tol_rel=1e-4, maxiter=
                 for rep in range(2):  # the first run builds the engine and its graphs
                     ns, it, err, ok = gb.solve_batch(pn, pm, pk, seed, pt, alg=alg, tol_rel=tol_rel,
                                                      maxiter=maxiter, slots=s, sm_share=share, cluster=c,
-                                                     learned_params=learned_params, grad_format=grad_format)
+                                                     learned_params=learned_params, grad_format=grad_format,
+                                                     residual_refresh=residual_refresh)
                 _, ms = gb.batch_last_stats()
                 table.append({"slots": s, "sm_share": share, "cluster": c, "ms": ms, "recovered": int(ns)})
                 if log:

@@ -55,6 +55,7 @@ struct BatchParams {
   int learned;  // learned warm start (CGIHT)
   int *fb;      // per trial: the warm start was abandoned (solve again from zero)
   int gfmt;     // the A^T r operand (GB_GRAD_*)
+  int rec_every;  // CGIHT residual recurrence (GbState::rec_every)
 };
 
 using gbgen::KEY_HI;
@@ -80,6 +81,7 @@ __device__ void load_trial(GbState *st, const BatchParams *bp, int q, cudaGraphC
   const int t = bp->order[q];
   batch_trial_fields(st, t, bp->m[t], bp->n[t], bp->k[t], bp->maxiter, bp->alg);
   st->gfmt = bp->gfmt;
+  st->rec_every = bp->rec_every;
   cudaGraphSetConditional(h_trial, 1u);
 }
 
@@ -495,6 +497,7 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
   bp.learned = learned;
   bp.fb = learned ? E.dfb : nullptr;
   bp.gfmt = b->grad_format;
+  bp.rec_every = b->alg == GB_ALG_CGIHT ? std::max(0, b->residual_refresh) : 0;
   if (learned)
     GB_CUDA_TRY(cudaMemcpyAsync(E.ml_params, b->learned_params, sizeof(float) * gb_ml_num_params(),
                                 cudaMemcpyDeviceToDevice, s));
@@ -526,6 +529,7 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
     ra.ml_params = learned ? E.ml_params : nullptr;
     ra.fb = learned ? E.dfb : nullptr;
     ra.gfmt = b->grad_format;
+    ra.rec_every = bp.rec_every;
     GB_TRY(gb_resident_enqueue(ra, s));
   }
   for (size_t i = 0; i < nslot; ++i) GB_CUDA_TRY(cudaStreamWaitEvent(s, E.done[i], 0));

@@ -537,6 +537,9 @@ __device__ __forceinline__ void ctrl_phase(GbState *st, int phase, cudaGraphCond
       st->k_bin_prev = 0;
       st->flags[F_UCG] = st->restart ? 0 : 1;
       st->flags[F_RCG] = st->restart ? 1 : 0;
+      st->flags[F_RESX] = st->flags[F_RCG];
+      st->flags[F_RESR] = 0;
+      st->supp_same = 0;
       st->active = keep_going(st);
       set_cond(h, st->active ? 1u : 0u);
       break;
@@ -668,16 +671,20 @@ __device__ __forceinline__ void ctrl_phase(GbState *st, int phase, cudaGraphCond
         st->flags[F_DOBIN] = 1;
         st->k_bin_prev = st->k_bin;
         st->changed = 0;
+        st->s_cnt_prev = st->s_cnt;
       } else {
         st->flags[F_DOBIN] = 0;
         st->supp_change = 0;
         st->min_val = st->min_val - st->max_change;
+        st->supp_same = 1;  // no binning: the same bins threshold x
       }
       st->flags[F_REMASK] = 0;
       break;
     case C_CGIHT_POST:
       if (!live || !st->flags[F_DOBIN]) break;
       st->supp_change = st->changed ? 1 : 0;
+      // no entry left and as many entries as before: the same support set
+      st->supp_same = !st->changed && st->s_cnt == st->s_cnt_prev;
       if (st->supp_change) {
         if (st->restart) st->beta_to_zero = 1;
         else st->flags[F_REMASK] = 1;
@@ -685,7 +692,9 @@ __device__ __forceinline__ void ctrl_phase(GbState *st, int phase, cudaGraphCond
       break;
     case C_CGIHT_STOP:
       if (live) {
-        if (st->op_kind == GB_OP_DENSE) st->bytes += dense_bytes(st, 1, st->flags[F_UCG] ? 3 : 2);
+        if (st->op_kind == GB_OP_DENSE)
+          st->bytes += dense_bytes(st, 1, st->flags[F_UCG] ? 3 : st->flags[F_RESR] ? 1 : 2);
+        const bool was_rcg = st->flags[F_RCG] != 0;
         st->err = st->prev[15];
         finish_iteration(st, 749);
         // learned warm start: give up when the residual has not dropped below the warm
@@ -697,6 +706,12 @@ __device__ __forceinline__ void ctrl_phase(GbState *st, int phase, cudaGraphCond
         }
         if (st->restart) { st->flags[F_UCG] = 0; st->flags[F_RCG] = 1; }
         else { st->flags[F_UCG] = st->supp_change ? 1 : 0; st->flags[F_RCG] = st->supp_change ? 0 : 1; }
+        // x moved by alpha p on an unchanged support: r - alpha A p is y - A x in exact
+        // arithmetic; every rec_every-th iteration recomputes it from x
+        const bool rec = st->rec_every > 0 && was_rcg && st->supp_same && !st->supp_change &&
+                         (st->iter % st->rec_every) != 0;
+        st->flags[F_RESR] = st->flags[F_RCG] && rec;
+        st->flags[F_RESX] = st->flags[F_RCG] && !rec;
       }
       set_cond(h, st->active ? 1u : 0u);
       break;

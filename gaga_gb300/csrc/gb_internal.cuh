@@ -19,7 +19,7 @@
 
 #define GB_NSLOT 16     // reduction result slots
 #define GB_MAXRB 1024   // max blocks of a reducing kernel
-#define GB_NFLAG 8      // predicate flags
+#define GB_NFLAG 10     // predicate flags
 #define GB_TILE 2048    // elements per block in the ordered compaction
 #define GB_SEL_BINS 2048  // radix-select digits per pass (11 bits)
 #define GB_NSTAMP 6       // timing variants: stamps per iteration (see k_stamp)
@@ -33,7 +33,9 @@ enum {
   F_CG = 4,      // HTP: inner CG loop running
   F_REMASK = 5,  // CGIHT: support changed, re-restrict the search direction
   F_KBIN_ALT = 6, // CSMPSP: the k-th bin scan is for the gradient (k_bin_prev), not x
-  F_SORT = 7      // timing variants, supportFlag 2/3: a new k-th largest |x| this iteration
+  F_SORT = 7,     // timing variants, supportFlag 2/3: a new k-th largest |x| this iteration
+  F_RESX = 8,     // CGIHT restricted step: the residual y - A x computed from x
+  F_RESR = 9      // CGIHT restricted step: the residual by r -= alpha A p (batched, rec_every > 0)
 };
 
 // reduction slots
@@ -83,6 +85,11 @@ struct GbState {
   int trial, op_kind;
   double bytes;
   int gfmt;
+  // batched CGIHT: a restricted step whose predecessor was a restricted step on the same
+  // support updates the residual as r - alpha A p (the product that step already made)
+  // instead of y - A x, except every rec_every-th iteration (0: never); the support count
+  // before the last binning and whether the support set is unchanged since the last step
+  int rec_every, s_cnt_prev, supp_same;
   // learned warm start (CGIHT): on, gave up after 10 iterations, residual at the warm x0
   int learned, fell_back;
   float err_warm0;

@@ -85,6 +85,7 @@ struct RsParams {
   int gfmt;
   unsigned short *Ah;
   unsigned char *Al;
+  int rec_every;  // batched CGIHT: residual recurrence (GbState::rec_every)
 };
 
 // Shared-memory layout of one CTA (the same on host and device).
@@ -712,6 +713,7 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
                          IS_CG ? GB_ALG_CGIHT : ALG == RS_HTP ? GB_ALG_HTP : GB_ALG_NIHT);
       st->lda = lda;
       st->gfmt = P.gfmt;
+      st->rec_every = P.rec_every;
     }
     // ---- draw the trial (k_b_gen_A, k_b_gen_x, key bins, y = A x0 of gb_batch.cu)
     for (int col = wid; col < nc; col += RS_WARPS) {
@@ -915,12 +917,19 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
         if (dobin) s_own = compact_own(bins, nc, kb, sidx, wcnt);
         if (save_prev && dobin) {
           const int any = __syncthreads_or(chg);
-          if (tid == 0) ipub[1] = any;
+          if (tid == 0) {
+            ipub[1] = any;
+            ipub[2] = s_own;
+          }
           cl.sync();
           if (tid == 0) {
-            int a = 0;
-            for (int c = 0; c < C; ++c) a |= peer(cl, ipub, c)[1];
+            int a = 0, sc = 0;
+            for (int c = 0; c < C; ++c) {
+              a |= peer(cl, ipub, c)[1];
+              sc += peer(cl, ipub, c)[2];
+            }
             st->changed = a;
+            st->s_cnt = sc;  // the new support's size (C_CGIHT_POST compares it)
           }
         }
         __syncthreads();
@@ -1113,7 +1122,31 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
         // x += alpha p and the support (algorithms.cu:3849-3899)
         while (st->active) {
           const bool rcg = st->flags[F_RCG] != 0;
-          av_rows(x, true, rowp, r, R_RES);  // r = y - A x_S
+          if (st->flags[F_RESR]) {
+            // r = r - alpha A p over the own rows (A p from the last restricted step), then
+            // every CTA gathers the rows
+            const float alpha = st->cg_alpha;
+            float4 *rp4 = reinterpret_cast<float4 *>(rowp);
+            const float4 *ra4 = reinterpret_cast<const float4 *>(rowa);
+            float s2 = 0.0f;
+            for (int i = tid; i < rr1 - rr0; i += RS_THREADS) {
+              float4 v = rp4[i];
+              const float4 a = ra4[i];
+              v.x = fmaf(-alpha, a.x, v.x); v.y = fmaf(-alpha, a.y, v.y);
+              v.z = fmaf(-alpha, a.z, v.z); v.w = fmaf(-alpha, a.w, v.w);
+              rp4[i] = v;
+              s2 = fmaf(v.x, v.x, s2); s2 = fmaf(v.y, v.y, s2); s2 = fmaf(v.z, v.z, s2); s2 = fmaf(v.w, v.w, s2);
+            }
+            const float b = block_reduce<0>(s2, red32);
+            if (tid == 0) {
+              pub[R_RES] = b;
+              ipub[0] = s_own;
+            }
+            cl.sync();
+            gather_rows(cl, C, q4, RB, rowp, r);
+          } else {
+            av_rows(x, true, rowp, r, R_RES);  // r = y - A x_S
+          }
           if (tid == 0) {
             st->red[R_RES] = combine_sum(cl, C, pub, R_RES);
             int sc = 0;
@@ -1476,6 +1509,7 @@ gb_status gb_resident_enqueue(const GbResidentArgs &a, cudaStream_t s) {
   P.gfmt = a.gfmt;
   P.Ah = R.Ah;
   P.Al = R.Al;
+  P.rec_every = a.rec_every;
   cfg.gridDim = dim3(R.ncl * C, 1, 1);
   cfg.dynamicSmemBytes = gb_resident_smem(R.n_cap, R.m_cap, C, a.alg, learned);
   GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, P));

@@ -31,6 +31,7 @@ struct GbResidentArgs {
   const float *ml_params;  // CGIHT from the learned warm start (device MLP parameters) or null
   int *fb;                 // with it: per trial, 1 when the warm start was abandoned
   int gfmt = 0;            // the A^T r operand (GB_GRAD_*)
+  int rec_every = 0;       // CGIHT residual recurrence (GbState::rec_every)
 };
 
 gb_status gb_resident_enqueue(const GbResidentArgs &a, cudaStream_t s);

@@ -1499,7 +1499,10 @@ void enq_body(SolvePlan &P, cudaStream_t s1, cudaGraphConditionalHandle h_outer)
   } else if (P.alg == GB_ALG_CGIHT) {
     // RestrictedCGwithSupportEvolution (functions.cu:1004-1102) under F_RCG;
     // UnrestrictedCG (functions.cu:1107-1220) under F_UCG
-    enq_A(w, s1, w.x, w.resid, w.y, R_RES, F_RCG);
+    enq_A(w, s1, w.x, w.resid, w.y, R_RES, F_RESX);
+    // (batched, rec_every > 0) after a restricted step on an unchanged support: r -= alpha A p
+    k_lin<<<w.red_blocks, 256, 0, s1>>>(w.st, F_RESR, w.resid, w.resid, SC_NEG_CG_ALPHA, w.ru, m, nullptr, -1,
+                                        R_RES, w.red_part, w.tickets);
     enq_A(w, s1, w.x, w.ru, w.y, R_RES, F_UCG);
     enq_ctrl(w, s1, C_PUSH_RES);
     // RCG branch

@@ -261,6 +261,11 @@ typedef struct {
                                     (2 bytes), FP32 accumulation.  A x_S, the residual and the
                                     stopping test keep FP32 A, so a solution of y = A x stays a
                                     fixed point; only the gradient directions change. */
+  int residual_refresh;          /* CGIHT: 0 (the default) computes y - A x at every step, as the
+                                    reference does; N > 0 lets a restricted step that follows a
+                                    restricted step on the same support update the residual as
+                                    r - alpha A p (the product the previous step made, one pass
+                                    over A_S fewer), recomputing y - A x every N-th iteration */
 } gb_batch;
 
 enum { GB_GRAD_FP32 = 0, GB_GRAD_A24 = 1, GB_GRAD_BF16 = 2 };

@@ -1,4 +1,5 @@
-"""Parity at the full workload sizes through properties that do not depend on size.
+"""Parity at the full workload sizes: the GPU solve against the oracle's solve of the same
+problem, and properties that do not depend on size.
 
   DCT      n = 2^20, m = 2^18 rows, k = m/10, Gaussian values: CGIHT and HTP recover the
            planted signal (relative l2 <= 1e-3) and every significant entry of its support, and the returned
@@ -88,3 +89,43 @@ def test_expander_full_size_parallel_l0_bit_exact(gb, gbo):
     assert np.array_equal(x, xo)
     assert np.array_equal(rec[: iters + 1], reco[: iters + 1])
     assert np.array_equal(x, x0)
+
+
+@pytest.mark.parametrize("alg", ["CGIHT", "HTP"])
+def test_dct_full_size_matches_oracle_solve(gb, gbo, alg):
+    """n = 2^20, m = 2^18, k = m/10: the GPU's x against the oracle's x from the same y
+    (FP64 DCT in the oracle, the half-length FP32 transform on the GPU: the trajectories
+    differ in the last bits, the solutions agree to 1e-4 relative and the iteration counts
+    to within 2)."""
+    n, m = 2 ** 20, 2 ** 18
+    k = m // 10
+    rows = gbo.gen_dct_rows(n, m, seed=23)
+    x0, ks = gbo.gen_vector(n, k, 2, seed=23)
+    op = gbo.Op.dct(n, rows)
+    y = gbo.A(op, x0)
+    tol = 1e-4 * float(np.linalg.norm(y))
+    x, iters, conv = gb.gaga_cs(alg, "dct", y, rows, ks, m, n, gb.gaga_options("tol", tol), index_base=0)
+    xo, info = gbo.solve(alg, op, y, ks, tol)
+    assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-4
+    assert abs(int(iters) - int(info.iter)) <= 2, (iters, info.iter)
+
+
+@pytest.mark.parametrize("alg", ["NIHT", "CGIHT"])
+def test_expander_full_size_matches_oracle_solve(gb, gbo, alg):
+    """n = 2^18, m = 2^16, d = 7, k = m/20 on the 1/sqrt(d) matrix: the expander products are
+    bit-exact against the oracle's, the norms and step sizes are summed in another order, so
+    x agrees to 1e-4 relative and the iteration count to within 2."""
+    n, m, d = 2 ** 18, 2 ** 16, 7
+    k = m // 20
+    rows, vals = gbo.gen_smv(m, n, d, 1, seed=33)
+    x0, ks = gbo.gen_vector(n, k, 1, seed=33)
+    op = gbo.Op.smv(m, n, d, rows, vals)
+    y = gbo.A(op, x0)
+    tol = 1e-4 * float(np.linalg.norm(y))
+    cols = np.repeat(np.arange(n, dtype=np.int32), d)
+    x, iters, conv, rec, trec = gb.gaga_cs(alg, "smv", y, rows, cols, vals, ks, gb.gaga_options("tol", tol),
+                                           index_base=0)
+    xo, info = gbo.solve(alg, op, y, ks, tol)
+    assert abs(int(iters) - int(info.iter)) <= 2, (iters, info.iter)
+    assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-4
+
