@@ -309,10 +309,15 @@ def bench_ours(args):
             "gpu_launches_note": "host-issued launches (kernels and graphs); the graphs run the solver kernels in "
                                  "device-side WHILE loops",
             "clocks": clocks}
-    mv = matvec_roofline(peak, peak_kind)
-    line["roofline"] = mv["at"]
+    # the roofline of the tuned form's A^T r at the sweep's largest trial (the compact operand
+    # when the tuned form uses one; the FP32 kernels stay in "matvec")
+    mv = matvec_roofline(peak, peak_kind, grad_format=args.grad_format)
+    line["roofline"] = mv.get("at_c", mv["at"])
     line["matvec"] = mv
     line["resident"] = resident_roofline(peak, peak_kind, cluster=sched.get("cluster", 0))
+    line["resident_tuned"] = resident_roofline(peak, peak_kind, cluster=sched.get("cluster", 0), alg=ALG,
+                                               learned_params=params, grad_format=args.grad_format,
+                                               residual_refresh=args.residual_refresh)
     if not args.no_configs:
         line["single_trial_configs"] = bench_configs(cpu=not args.no_cpu)
     line["gemm"] = gemm_roofline(tpeak, tpeak_kind)
@@ -518,9 +523,10 @@ def operators_roofline(peak, peak_kind, reps=20):
     return out
 
 
-def matvec_roofline(peak, peak_kind, m=14746, n=16384, k=5000, reps=20):
-    """Dense A^T r (k_dense_at, the dominant kernel) and A x_S (k_dense_av) on the sweep's
-    largest trial shape, timed with CUDA events on the stream they run on."""
+def matvec_roofline(peak, peak_kind, m=14746, n=16384, k=5000, reps=20, grad_format="fp32"):
+    """Dense A^T r (k_dense_at) and A x_S (k_dense_av) on the sweep's largest trial shape,
+    timed with CUDA events on the stream they run on; with a compact A^T r operand also
+    k_dense_at_c (the tuned form's A^T r, "at_c": CUDA events inside gb_cs_operator_time)."""
     import ctypes as C
 
     import torch
@@ -565,9 +571,32 @@ def matvec_roofline(peak, peak_kind, m=14746, n=16384, k=5000, reps=20):
                      "shape": "m=%d n=%d lda=%d%s, A %.0f MB > L2" % (m, n, lda, "" if name == "at" else
                                                                       " |S|=%d" % k, 4.0 * m * n / 1e6),
                      "us_per_launch": t * 1e6, "peak_source": peak_kind}
+    if grad_format != "fp32":
+        code = {"a24": 2, "bf16": 3}[grad_format]
+        b = {"a24": 3.0, "bf16": 2.0}[grad_format]
+        p = _lib.Problem(_lib.GB_OP_DENSE, m, n, 0, None, A.data_ptr(), lda, None, None, None, 0, 0, _lib.GB_DEVICE,
+                         None)
+        p.stream = C.c_void_p(s.cuda_stream)
+        ms = C.c_float(0)
+        _lib.check(L.gb_cs_operator_time(C.byref(p), code, r.data_ptr(), g_out.data_ptr(), 3, reps, None, 0,
+                                         C.byref(ms)))
+        t = ms.value / 1e3
+        ach = (b * m * n + 4 * m + 4 * n) / t / 1e9
+        res["at_c"] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                       "traffic": None, "kernel": "k_dense_at_c<%d>" % (1 if grad_format == "a24" else 0),
+                       "shape": "m=%d n=%d lda=%d, %s A^T r operand %.0f MB > L2" % (
+                           m, n, lda, grad_format, b * m * n / 1e6),
+                       "us_per_launch": t * 1e6, "peak_source": peak_kind}
     del A
     torch.cuda.empty_cache()
     tr = ncu_traffic()
+    if "at_c" in res:
+        key = ("k_dense_at_c<0> (BF16 operand) m=14746 n=16384 lda=14752" if grad_format == "bf16" else
+               "k_dense_at_c<1> (24-bit operand) m=14746 n=16384 lda=14752")
+        if key in tr and (m, n) == (14746, 16384):
+            res["at_c"]["traffic"] = tr[key]["read"] + tr[key]["write"]
+            res["at_c"]["traffic_source"] = "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, same " \
+                                            "shape (profiles/dram_traffic.json)"
     for name, key in (("at", "k_dense_at m=14746 n=16384 lda=14752"), ("av", "k_dense_av m=14746 n=16384 lda=14752 |S|=5000")):
         if key in tr and (m, n, k) == (14746, 16384, 5000):
             res[name]["traffic"] = tr[key]["read"] + tr[key]["write"]
@@ -576,12 +605,14 @@ def matvec_roofline(peak, peak_kind, m=14746, n=16384, k=5000, reps=20):
     return res
 
 
-def resident_roofline(peak, peak_kind, max_n=8192, sample=0, cluster=0):
-    """The cluster-resident kernel's NIHT instance alone (k_resident, one launch) on the first
-    wave's trials with n <= max_n (every one, or `sample` evenly spaced), timed with CUDA
-    events around the batched call; algorithmic operator bytes of its iterations per second.
-    Trials whose slab of A fits in L2 re-read it from there, so the DRAM traffic can be
-    below the algorithmic bytes."""
+def resident_roofline(peak, peak_kind, max_n=8192, sample=0, cluster=0, alg="NIHT", learned_params=None,
+                      grad_format="fp32", residual_refresh=0):
+    """The cluster-resident kernel alone (k_resident, one launch; NIHT, or the tuned form's
+    instance: CGIHT from the learned start with its A^T r operand and residual recurrence)
+    on the first wave's trials with n <= max_n (every one, or `sample` evenly spaced), timed
+    with CUDA events around the batched call; algorithmic operator bytes of its iterations
+    per second.  Trials whose slab of A fits in L2 re-read it from there, so the DRAM
+    traffic can be below the algorithmic bytes."""
     import gaga_gb300 as gb
 
     n, m, k, tid = wave_arrays(0)
@@ -590,16 +621,19 @@ def resident_roofline(peak, peak_kind, max_n=8192, sample=0, cluster=0):
         sel = sel[np.linspace(0, len(sel) - 1, min(sample, len(sel))).astype(int)]
     n, m, k, tid = n[sel], m[sel], k[sel], tid[sel]
     for _ in range(2):  # the first call sizes the kernel's buffers
-        ns, iters, err, ok = gb.solve_batch(n, m, k, SEED, tid, alg="NIHT", tol_rel=TOL_REL, maxiter=MAXITER,
-                                            resident_n=max_n, cluster=cluster)
+        ns, iters, err, ok = gb.solve_batch(n, m, k, SEED, tid, alg=alg, tol_rel=TOL_REL, maxiter=MAXITER,
+                                            resident_n=max_n, cluster=cluster, learned_params=learned_params,
+                                            grad_format=grad_format, residual_refresh=residual_refresh)
     nbytes, ms = gb.batch_last_stats()
     achieved = nbytes / (ms / 1e3) / 1e9
+    what = "k_resident<%s%s%s>" % (alg, ", learned start" if learned_params is not None else "",
+                                   "" if grad_format == "fp32" else ", %s A^T r operand" % grad_format)
     out = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-           "kernel": "k_resident<NIHT>", "trials": int(len(n)), "recovered": int(ns), "iterations": int(iters.sum()),
+           "kernel": what, "trials": int(len(n)), "recovered": int(ns), "iterations": int(iters.sum()),
            "sizes": "n=%s" % sorted(set(n.tolist())), "ms": ms, "algorithmic_bytes": nbytes,
            "cluster": gb._lib.load().gb_cs_batch_last_cluster(), "peak_source": peak_kind}
     tr = ncu_traffic().get("k_resident<NIHT> sweep wave 0, 655 trials n=1024..8192, 4 CTAs per cluster")
-    if tr and not sample and max_n == 8192 and out["cluster"] == 4:
+    if tr and not sample and max_n == 8192 and out["cluster"] == 4 and alg == "NIHT":
         out["traffic"] = tr["read"] + tr["write"]
         out["traffic_unit"] = "bytes"
         out["traffic_source"] = "ncu dram__bytes_read.sum + dram__bytes_write.sum of the same launch " \
