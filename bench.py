@@ -22,6 +22,9 @@ Problem generation runs inside the timed region.
           same seeds, gb_cs_solve on the shared A and each y), each call timed with CUDA
           events; scaled to the 3072 + 1024 mix for tuned_vs_plain; the verdicts of the same
           trials give the agreement between the two forms, split by direction
+  faithful : the same sweep from the zero start with the 24-bit A^T r operand (the form whose
+          verdicts are meant to equal plain's), its rate over plain and its agreement with
+          the plain leg's verdicts
   niht_sweep : the same sweep with NIHT (batched + shared-matrix forms, no warm start)
   learned_warm_start : the trained MLP warm start against zero-initialised CGIHT on 2048
           fresh trials of its own workload (n = 8192, delta 0.1-0.6, rho 0.05-0.45)
@@ -323,9 +326,12 @@ def bench_ours(args):
     line["gemm"] = gemm_roofline(tpeak, tpeak_kind)
     line["operators"] = operators_roofline(peak, peak_kind)
     if args.plain_trials > 0 and world == 1:
-        line["plain"] = bench_plain(args, first_step)
+        pverd = {}
+        line["plain"] = bench_plain(args, first_step, pverd)
         line["tuned_vs_plain"] = value / line["plain"]["value"] if line["plain"]["value"] else None
         line["tuned_vs_plain_e2e"] = e2e / line["plain"]["value"] if line["plain"]["value"] else None
+        if args.faithful_steps > 0:
+            line["faithful"] = bench_faithful(args, solve_step, pverd, line["plain"]["value"], n0, m0, k0, t0_)
     if args.niht_steps > 0 and world == 1:
         line["niht_sweep"] = bench_niht(args, solve_step)
     if args.learned_trials > 0 and world == 1:
@@ -335,6 +341,49 @@ def bench_ours(args):
     print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def bench_faithful(args, solve_step, pverd, plain_value, n0, m0, k0, t0_):
+    """The same sweep in the form whose verdicts are meant to match the plain drop-in's:
+    batched + shared-matrix as in the headline, but from the zero start (no learned warm
+    start) and with the 24-bit A^T r operand (rounding at 2^-16 leaves the trajectories'
+    verdicts unchanged, where BF16's 2^-9 moves a few near the phase transition), residual
+    recurrence as the headline.  Device time over the timed steps' waves; verdicts of the
+    first timed step against the plain leg's on the same sampled trials."""
+    from gaga_gb300 import autotune, sweep
+
+    sched = autotune.tune_batch(n0, m0, k0, SEED, t0_, alg=ALG, tol_rel=TOL_REL, maxiter=MAXITER,
+                                use_cache=not args.retune, grad_format="a24", residual_refresh=args.residual_refresh)
+    kw = dict(lp=None, schedule=sched, gfmt="a24")
+    solve_step(sweep.rank_wave(0, 1, 0), **kw)  # warm-up: engines and graphs of this form
+    ok = trials = 0
+    kms = 0.0
+    first = None
+    for s_ in range(args.faithful_steps):
+        w = sweep.rank_wave(0, 1, args.warmup + s_)
+        r = solve_step(w, **kw)
+        ok += r["ok"]
+        trials += r["trials"]
+        kms += r["kms"]
+        if first is None:
+            first = (w, r)
+    value = ok / (kms / 1e3)
+    out = {"value": value, "unit": "trials/s", "steps": args.faithful_steps, "recovered": int(ok), "trials": int(trials),
+           "ms_per_step": kms / args.faithful_steps, "vs_plain": value / plain_value if plain_value else None,
+           "form": "batched + shared-matrix forms, zero start, 24-bit A^T r operand, residual recurrence every %d"
+                   % args.residual_refresh,
+           "schedule": {"slots": sched["slots"], "sm_share": sched["sm_share"], "cluster": sched.get("cluster", 0)}}
+    if pverd and first is not None and first[0] == pverd["w"]:
+        tv = np.asarray(first[1]["verdict_batch"], bool)[pverd["sel"]]
+        tv2 = np.asarray(first[1]["verdict_shared"], bool)[pverd["sel2"]]
+        pv, pv2 = pverd["pv"], pverd["pv2"]
+        agree = int(np.sum(pv == tv) + np.sum(pv2 == tv2))
+        tot = len(pv) + len(pv2)
+        out["verdict_agreement"] = agree / tot
+        out["verdicts"] = {"trials": tot, "agree": agree,
+                           "only_plain_recovers": int(np.sum(pv & ~tv) + np.sum(pv2 & ~tv2)),
+                           "only_faithful_recovers": int(np.sum(tv & ~pv) + np.sum(tv2 & ~pv2))}
+    return out
 
 
 def bench_niht(args, solve_step):
@@ -720,7 +769,7 @@ def ncu_traffic():
         return {}
 
 
-def bench_plain(args, first_step):
+def bench_plain(args, first_step, verdicts_out=None):
     """Single-trial FP32 drop-in, zero-initialised CGIHT, on the first timed step's trials:
     the independent trials by gb_cs_generate_and_solve (same seeds, so the same problems),
     the shared-matrix trials by gb_cs_solve on the shared A and the trial's y.  Each call is
@@ -784,6 +833,8 @@ def bench_plain(args, first_step):
     est_time = n_ind * t_ind + n_sh * t_sh
     est_ok = n_ind * ok_ind + n_sh * ok_sh
     tot = len(sel) + len(sel2)
+    if verdicts_out is not None:
+        verdicts_out.update(sel=sel, pv=np.asarray(pv, bool), sel2=sel2, pv2=np.asarray(pv2, bool), w=w)
     return {"value": est_ok / est_time, "unit": "trials/s", "algorithm": ALG + " (zero-initialised)",
             "timing": "CUDA events around each call on its stream",
             "independent": {"trials": int(len(sel)), "s_per_trial": t_ind, "solver_s_per_trial": ts_ind,
@@ -841,6 +892,8 @@ def main():
                     help="independent trials of the first timed step solved by the plain form (768 = all); a third "
                          "as many shared-matrix trials (256 = all)")
     ap.add_argument("--niht-steps", type=int, default=2, help="steps of the NIHT sweep leg (0: skip)")
+    ap.add_argument("--faithful-steps", type=int, default=3,
+                    help="steps of the verdict-faithful leg (zero start, 24-bit A^T r operand; 0: skip)")
     ap.add_argument("--cpu-trials", type=int, default=32)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--learned-trials", type=int, default=2048)
