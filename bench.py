@@ -143,18 +143,41 @@ def cpu_sample(w, count):
 
 
 def run_cpu(w, count):
+    """The CPU oracle on the step's mix: 3/4 of `count` independent trials (every few of the
+    wave, generated from the same keys) and 1/4 shared-matrix trials (the step's shared A and
+    signals, regenerated by the oracle's generators), so the rate covers the same 3:1 mix as
+    the GPU's value."""
+    from gaga_gb300 import sweep
     from oracle import gbo
 
-    n, m, k, tid = cpu_sample(w, count)
+    n_sh = max(1, count // 4)
+    n, m, k, tid = cpu_sample(w, count - n_sh)
     cores = os.cpu_count() or 1
     t0 = time.perf_counter()
     ok, iters, err = gbo.solve_dense_trials(n, m, k, SEED, tid, alg=ALG, tol_rel=TOL_REL, maxiter=MAXITER,
                                             threads=cores)
-    dt = time.perf_counter() - t0
-    return {"value": ok / dt, "unit": "trials/s", "cores": cores, "kind": "port", "seconds": dt,
-            "sample": ("%d trials of wave %d (every %d-th; n=%s), %s, CPU oracle oracle/gbo.c with OpenMP inside "
-                       "each trial, generation included; %d recovered in %.1f s" % (
-                           len(n), w, len(wave_arrays(w)[0]) // count, sorted(set(n.tolist())), ALG, ok, dt))}
+    t1 = time.perf_counter()
+    # shared-matrix trials: A from SHARED_SEED, x0_t from SHARED_SEED + 1 + trial (the GPU form's keys)
+    ks, first = shared_part(w)
+    sel = np.linspace(0, len(ks) - 1, n_sh).astype(int)
+    sm, sn = sweep.SHARED_M, sweep.SHARED_N
+    A = gbo.gen_dense(sm, sn, SHARED_SEED, 0, 1)
+    op = gbo.Op.dense(A, sm, sn)
+    ok_sh = 0
+    for t in sel:
+        x0, kt = gbo.gen_vector(sn, int(ks[t]), 1, SHARED_SEED + 1 + first + int(t), 0)
+        y = gbo.A(op, x0)
+        x, info = gbo.solve(ALG, op, y, kt, TOL_REL * float(np.linalg.norm(y)), maxiter=MAXITER, threads=cores)
+        ok_sh += int(np.linalg.norm(x - x0) <= 1e-3 * np.linalg.norm(x0))
+    t2 = time.perf_counter()
+    dt = t2 - t0
+    tot_ok = ok + ok_sh
+    return {"value": tot_ok / dt, "unit": "trials/s", "cores": cores, "kind": "port", "seconds": dt,
+            "sample": ("%d independent trials of wave %d (every %d-th; n=%s) and %d shared-matrix trials "
+                       "(n=%d, m=%d) of the step, %s, CPU oracle oracle/gbo.c with OpenMP inside each trial, "
+                       "generation included; %d + %d recovered in %.1f + %.1f s" % (
+                           len(n), w, len(wave_arrays(w)[0]) // max(1, count - n_sh), sorted(set(n.tolist())),
+                           len(sel), sn, sm, ALG, ok, ok_sh, t1 - t0, t2 - t1, ))}
 
 
 def bench_reference(args):
