@@ -233,10 +233,16 @@ def bench_ours(args):
         """One quarter of the sweep: independent trials, then the shared-matrix trials."""
         n, m, k, tid = wave_arrays(w)
         t0 = time.perf_counter()
+        per_trial = None
+        if gfmt == "transition":  # 24-bit operand near the phase transition, BF16 elsewhere
+            from gaga_gb300 import transition
+
+            per_trial = transition.operand_formats(n, m, k)
         ns, iters, err, ok = gb.solve_batch(n, m, k, SEED, tid, alg=alg, tol_rel=TOL_REL, maxiter=MAXITER,
                                             slots=schedule["slots"], sm_share=schedule["sm_share"],
                                             cluster=schedule.get("cluster", 0), learned_params=lp,
-                                            grad_format=gfmt, residual_refresh=args.residual_refresh)
+                                            grad_format="a24" if per_trial is not None else gfmt,
+                                            grad_formats=per_trial, residual_refresh=args.residual_refresh)
         t1 = time.perf_counter()
         nbytes, kms = gb.batch_last_stats()
         ks, first = shared_part(w)
@@ -377,7 +383,7 @@ def bench_faithful(args, solve_step, pverd, plain_value, n0, m0, k0, t0_):
 
     sched = autotune.tune_batch(n0, m0, k0, SEED, t0_, alg=ALG, tol_rel=TOL_REL, maxiter=MAXITER,
                                 use_cache=not args.retune, grad_format="a24", residual_refresh=args.residual_refresh)
-    kw = dict(lp=None, schedule=sched, gfmt="a24")
+    kw = dict(lp=None, schedule=sched, gfmt=args.faithful_format)
     solve_step(sweep.rank_wave(0, 1, 0), **kw)  # warm-up: engines and graphs of this form
     ok = trials = 0
     kms = 0.0
@@ -393,8 +399,9 @@ def bench_faithful(args, solve_step, pverd, plain_value, n0, m0, k0, t0_):
     value = ok / (kms / 1e3)
     out = {"value": value, "unit": "trials/s", "steps": args.faithful_steps, "recovered": int(ok), "trials": int(trials),
            "ms_per_step": kms / args.faithful_steps, "vs_plain": value / plain_value if plain_value else None,
-           "form": "batched + shared-matrix forms, zero start, 24-bit A^T r operand, residual recurrence every %d"
-                   % args.residual_refresh,
+           "form": "batched + shared-matrix forms, zero start, %s A^T r operand, residual recurrence every %d"
+                   % ({"a24": "24-bit", "transition": "24-bit near the phase transition (|rho - rho*(delta)| <= "
+                       "0.08) and BF16 elsewhere"}[args.faithful_format], args.residual_refresh),
            "schedule": {"slots": sched["slots"], "sm_share": sched["sm_share"], "cluster": sched.get("cluster", 0)}}
     if pverd and first is not None and first[0] == pverd["w"]:
         tv = np.asarray(first[1]["verdict_batch"], bool)[pverd["sel"]]
@@ -917,6 +924,9 @@ def main():
     ap.add_argument("--niht-steps", type=int, default=2, help="steps of the NIHT sweep leg (0: skip)")
     ap.add_argument("--faithful-steps", type=int, default=3,
                     help="steps of the verdict-faithful leg (zero start, 24-bit A^T r operand; 0: skip)")
+    ap.add_argument("--faithful-format", default="transition", choices=["a24", "transition"],
+                    help="the verdict-faithful leg's A^T r operand: 24-bit for every trial, or 24-bit near the "
+                         "phase transition and BF16 elsewhere (gaga_gb300/transition.py)")
     ap.add_argument("--cpu-trials", type=int, default=32)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--learned-trials", type=int, default=2048)

@@ -301,7 +301,7 @@ GRAD_FORMATS = {"fp32": 0, "a24": 1, "bf16": 2}
 
 def solve_batch(n, m, k, seed, trial_ids=None, alg="NIHT", tol_rel=1e-4, maxiter=5000, stream=None,
                 learned_params=None, slots=0, sm_share=0, resident_n=0, cluster=0, grad_format="fp32",
-                residual_refresh=0):
+                residual_refresh=0, grad_formats=None):
     """Batched multi-trial dense form (gb_cs_solve_batch); learned_params (a CUDA tensor of
     MLP parameters, CGIHT only) turns on the learned warm start; slots / sm_share set the
     schedule of the slot graphs (0: automatic; gaga_gb300.autotune picks them by
@@ -309,18 +309,24 @@ def solve_batch(n, m, k, seed, trial_ids=None, alg="NIHT", tol_rel=1e-4, maxiter
     cluster-resident kernel with `cluster` CTAs per trial (0: 4, or more when the sizes need
     it); grad_format ("fp32", "a24" or "bf16") is the operand of A^T r (24-bit or BF16
     copies of A stream 3 or 2 bytes per entry; A x, the residual and the stopping test keep
-    FP32 A); residual_refresh N > 0 (CGIHT) updates the residual of a restricted step on an
-    unchanged support as r - alpha A p, recomputing y - A x every N-th iteration."""
+    FP32 A); grad_formats (one of "a24" / "bf16" per trial) picks it per trial instead;
+    residual_refresh N > 0 (CGIHT) updates the residual of a restricted step on an unchanged
+    support as r - alpha A p, recomputing y - A x every N-th iteration."""
     L = _lib.load()
     n = np.ascontiguousarray(n, dtype=np.int32)
     m = np.ascontiguousarray(m, dtype=np.int32)
     k = np.ascontiguousarray(k, dtype=np.int32)
     tids = None if trial_ids is None else np.ascontiguousarray(trial_ids, dtype=np.uint32)
+    fmts = None
+    if grad_formats is not None:
+        fmts = np.ascontiguousarray([GRAD_FORMATS[f] if isinstance(f, str) else int(f) for f in grad_formats],
+                                    dtype=np.uint8)
     b = _lib.Batch(len(n), n.ctypes.data, m.ctypes.data, k.ctypes.data, None if tids is None else tids.ctypes.data,
                    int(seed) & 0xFFFFFFFF, {"NIHT": 0, "HTP": 1, "CGIHT": 6}[alg], float(tol_rel), int(maxiter),
                    0 if learned_params is None else 1,
                    None if learned_params is None else learned_params.data_ptr(), int(slots), int(sm_share), stream,
-                   int(resident_n), int(cluster), GRAD_FORMATS[grad_format], int(residual_refresh))
+                   int(resident_n), int(cluster), GRAD_FORMATS[grad_format],
+                   None if fmts is None else fmts.ctypes.data, int(residual_refresh))
     iters = np.zeros(len(n), dtype=np.int32)
     err = np.zeros(len(n), dtype=np.float32)
     ok = np.zeros(len(n), dtype=np.int32)

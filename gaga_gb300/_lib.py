@@ -63,7 +63,8 @@ class Batch(C.Structure):
                 ("trial_id", C.c_void_p), ("seed", C.c_uint), ("alg", C.c_int), ("tol_rel", C.c_float),
                 ("maxiter", C.c_int), ("use_learned", C.c_int), ("learned_params", C.c_void_p),
                 ("slots", C.c_int), ("sm_share", C.c_int), ("stream", C.c_void_p), ("resident_n", C.c_int),
-                ("cluster", C.c_int), ("grad_format", C.c_int), ("residual_refresh", C.c_int)]
+                ("cluster", C.c_int), ("grad_format", C.c_int), ("grad_formats", C.c_void_p),
+                ("residual_refresh", C.c_int)]
 
 
 class SharedBatch(C.Structure):

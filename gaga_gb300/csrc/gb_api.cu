@@ -1093,6 +1093,7 @@ extern "C" gb_status gb_cs_operator_time(const gb_problem *p, int transpose, con
   st0.m = p->m;
   st0.n = p->n;
   st0.lda = w.op.lda;
+  st0.gfmt = transpose == 2 ? GB_GRAD_A24 : transpose == 3 ? GB_GRAD_BF16 : GB_GRAD_FP32;
   GB_CUDA_TRY(cudaMemcpyAsync(w.st, &st0, sizeof(st0), cudaMemcpyHostToDevice, s));
   if (transpose >= 2) {
     // the batched form's compact A^T r operand, split from A once (outside the timing)

@@ -55,6 +55,7 @@ struct BatchParams {
   int learned;  // learned warm start (CGIHT)
   int *fb;      // per trial: the warm start was abandoned (solve again from zero)
   int gfmt;     // the A^T r operand (GB_GRAD_*)
+  const unsigned char *gfmts;  // per trial, or null: gfmt for every trial
   int rec_every;  // CGIHT residual recurrence (GbState::rec_every)
 };
 
@@ -80,7 +81,7 @@ __device__ void load_trial(GbState *st, const BatchParams *bp, int q, cudaGraphC
   }
   const int t = bp->order[q];
   batch_trial_fields(st, t, bp->m[t], bp->n[t], bp->k[t], bp->maxiter, bp->alg);
-  st->gfmt = bp->gfmt;
+  st->gfmt = bp->gfmts ? bp->gfmts[t] : bp->gfmt;
   st->rec_every = bp->rec_every;
   cudaGraphSetConditional(h_trial, 1u);
 }
@@ -182,6 +183,7 @@ struct Engine {
   int dev = -1, alg = -1, n_cap = 0, m_cap = 0, t_cap = 0, slots = 0, learned = 0, sm_share = 0, gfmt = 0;
   float *ml_params = nullptr;  // the warm-start MLP parameters (copied in by every call)
   int *dfb = nullptr;
+  unsigned char *dgfmt = nullptr;  // per-trial A^T r operand formats
   std::vector<Slot> slot;
   char *table = nullptr;
   BatchParams *d_params = nullptr;
@@ -291,7 +293,7 @@ gb_status setup_engine(Engine &E, int dev, int alg, int n_cap, int m_cap, int T,
   E.t_cap = std::max(T, 1024);
   E.slots = slots;
   const size_t tb = (size_t)E.t_cap * 4;
-  const size_t bytes = 11 * (tb + 256) + sizeof(BatchParams) + 2048 + (size_t)gb_ml_num_params() * 4 + 256;
+  const size_t bytes = 12 * (tb + 256) + sizeof(BatchParams) + 2048 + (size_t)gb_ml_num_params() * 4 + 256;
   GB_CUDA_TRY(cudaMalloc(&E.table, bytes));
   GB_CUDA_TRY(cudaMemset(E.table, 0, bytes));
   char *p = E.table;
@@ -304,6 +306,7 @@ gb_status setup_engine(Engine &E, int dev, int alg, int n_cap, int m_cap, int T,
   E.dorder = (int *)take(tb); E.diters = (int *)take(tb); E.derr = (float *)take(tb); E.dok = (int *)take(tb);
   E.dqueue = (int *)take(256); E.dbytes = (double *)take(256);
   E.dfb = (int *)take(tb);
+  E.dgfmt = (unsigned char *)take((size_t)E.t_cap);
   E.ml_params = (float *)take((size_t)gb_ml_num_params() * 4);
   E.d_params = (BatchParams *)take(sizeof(BatchParams));
   int sms = 0;
@@ -421,6 +424,24 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
                          __LINE__);
     return GB_BAD_ARG;
   }
+  // the operand format of the engines' buffers: per-trial formats are A24 or BF16 (A24's
+  // buffers hold both)
+  int gfmt = b->grad_format;
+  if (b->grad_formats && b->ntrials > 0) {
+    if (b->alg == GB_ALG_HTP) {
+      gb_set_error_message("grad_formats: HTP keeps FP32", __FILE__, __LINE__);
+      return GB_BAD_ARG;
+    }
+    gfmt = GB_GRAD_BF16;
+    for (int t = 0; t < b->ntrials; ++t) {
+      const int f = b->grad_formats[t];
+      if (f != GB_GRAD_A24 && f != GB_GRAD_BF16) {
+        gb_set_error_message("grad_formats: every entry GB_GRAD_A24 or GB_GRAD_BF16", __FILE__, __LINE__);
+        return GB_BAD_ARG;
+      }
+      if (f == GB_GRAD_A24) gfmt = GB_GRAD_A24;
+    }
+  }
   std::lock_guard<std::recursive_mutex> lock(gb_batch_mutex());
   const int T = b->ntrials;
   int n_cap = 16, m_cap = 1;
@@ -471,14 +492,14 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
   GB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const int sm_share = b->sm_share > 0 ? std::min(b->sm_share, sms) : std::max(1, sms / 2);
   const bool reuse = E.dev == dev && E.alg == b->alg && E.n_cap >= n_cap && E.m_cap >= m_cap && E.t_cap >= T &&
-                     E.sm_share == sm_share && (b->slots <= 0 || E.slots == b->slots) && E.gfmt == b->grad_format;
+                     E.sm_share == sm_share && (b->slots <= 0 || E.slots == b->slots) && E.gfmt == gfmt;
   if (!reuse) {
     release(E);
     size_t free_b = 0, total_b = 0;
     GB_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
     GB_TRY(setup_engine(E, dev, b->alg, n_cap, m_cap, T,
-                        slots_for(n_cap, m_cap, free_b, std::max(T, 16), b->slots, b->grad_format), learned, sm_share,
-                        b->grad_format));
+                        slots_for(n_cap, m_cap, free_b, std::max(T, 16), b->slots, gfmt), learned, sm_share,
+                        gfmt));
   }
   cudaStream_t s = (cudaStream_t)b->stream;
   // trial table, longest (m*n) first
@@ -496,7 +517,10 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
   bp.iters = E.diters; bp.err = E.derr; bp.ok = E.dok; bp.bytes = E.dbytes;
   bp.learned = learned;
   bp.fb = learned ? E.dfb : nullptr;
-  bp.gfmt = b->grad_format;
+  bp.gfmt = gfmt;
+  bp.gfmts = b->grad_formats ? E.dgfmt : nullptr;
+  if (b->grad_formats)
+    GB_CUDA_TRY(cudaMemcpyAsync(E.dgfmt, b->grad_formats, (size_t)T, cudaMemcpyHostToDevice, s));
   bp.rec_every = b->alg == GB_ALG_CGIHT ? std::max(0, b->residual_refresh) : 0;
   if (learned)
     GB_CUDA_TRY(cudaMemcpyAsync(E.ml_params, b->learned_params, sizeof(float) * gb_ml_num_params(),
@@ -528,7 +552,8 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
     ra.n_cap = rn_cap; ra.m_cap = rm_cap; ra.cluster = b->cluster; ra.alg = b->alg;
     ra.ml_params = learned ? E.ml_params : nullptr;
     ra.fb = learned ? E.dfb : nullptr;
-    ra.gfmt = b->grad_format;
+    ra.gfmt = gfmt;
+    ra.gfmts = bp.gfmts;
     ra.rec_every = bp.rec_every;
     GB_TRY(gb_resident_enqueue(ra, s));
   }
@@ -550,6 +575,7 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
     // trials whose warm start was abandoned: plain zero-initialised CGIHT decides
     std::vector<int> sn, sm, sk, idx;
     std::vector<unsigned> stid;
+    std::vector<unsigned char> sfmt;
     for (int t = 0; t < T; ++t)
       if (hfb[t]) {
         idx.push_back(t);
@@ -557,6 +583,7 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
         sm.push_back(b->m[t]);
         sk.push_back(b->k[t]);
         stid.push_back(tid[t]);
+        if (b->grad_formats) sfmt.push_back(b->grad_formats[t]);
       }
     if (!idx.empty()) {
       const float ms1 = g_last_kernel_ms;
@@ -567,6 +594,7 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
       pb.m = sm.data();
       pb.k = sk.data();
       pb.trial_id = stid.data();
+      pb.grad_formats = b->grad_formats ? sfmt.data() : nullptr;
       pb.use_learned = 0;
       pb.learned_params = nullptr;
       const int F = (int)idx.size();

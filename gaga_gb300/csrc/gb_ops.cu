@@ -282,20 +282,21 @@ __global__ void __launch_bounds__(DA_THREADS, DA_BLOCKS_PER_SM) k_dense_at(GbSta
 // nearest even, as a 16-bit high part and an 8-bit low part; BF16 the top 16 bits, rounded
 // the same way.  Decoded entries are exact FP32 values, accumulated in FP32.
 // split the current trial's A (st->m rows of st->n columns, column stride st->lda) into the
-// compact copy; rows m..lda-1 of the copy are zero
-template <int LO>
+// compact copy of the trial's format (st->gfmt: high parts, and for A24 the low parts);
+// rows m..lda-1 of the copy are zero
 __global__ void k_split_a(const GbState *st, const float *__restrict__ A, unsigned short *__restrict__ hi,
                           unsigned char *__restrict__ lo) {
-  if (!st->active) return;
+  if (!st->active || st->gfmt == GB_GRAD_FP32) return;
+  const bool has_lo = st->gfmt == GB_GRAD_A24;
   const int m = st->m, n = st->n, lda = st->lda;
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
   for (int j = gw; j < n; j += nw) {
     const size_t c = (size_t)j * lda;
     for (int i = lane; i < lda; i += 32) {
-      const uint32_t b = i < m ? round_top_bits(__float_as_uint(__ldcs(A + c + i)), LO ? 8 : 16) : 0u;
+      const uint32_t b = i < m ? round_top_bits(__float_as_uint(__ldcs(A + c + i)), has_lo ? 8 : 16) : 0u;
       hi[c + i] = (unsigned short)(b >> 16);
-      if (LO) lo[c + i] = (unsigned char)(b >> 8);
+      if (has_lo) lo[c + i] = (unsigned char)(b >> 8);
     }
   }
 }
@@ -303,17 +304,11 @@ __global__ void k_split_a(const GbState *st, const float *__restrict__ A, unsign
 // k_dense_at over the compact operand: the same outputs (g = A^T r, xt = g on the support,
 // ||xt||^2, max|g|), 8 rows per thread and step (lda a multiple of 8)
 template <int LO>
-__global__ void __launch_bounds__(DA_THREADS, DA_BLOCKS_PER_SM) k_dense_at_c(GbState *st, int pf,
-                                                           const unsigned short *__restrict__ Ah,
-                                                           const unsigned char *__restrict__ Al, int lda, int m,
-                                                           int n, const float *__restrict__ r,
-                                                           float *__restrict__ g, const int *__restrict__ bins,
-                                                           float *__restrict__ xt, int slot_sq, int slot_max,
-                                                           float *red_part, unsigned int *tickets) {
-  if (!gb_pred(st, pf)) return;
-  lda = dimv(st, lda);
-  m = dimv(st, m);
-  n = dimv(st, n);
+__device__ __forceinline__ void dense_at_c_body(GbState *st, const unsigned short *__restrict__ Ah,
+                                                const unsigned char *__restrict__ Al, int lda, int m, int n,
+                                                const float *__restrict__ r, float *__restrict__ g,
+                                                const int *__restrict__ bins, float *__restrict__ xt, int slot_sq,
+                                                int slot_max, float *red_part, unsigned int *tickets) {
   const int kb = st->k_bin;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   constexpr int NWARP = DA_THREADS / 32;
@@ -405,6 +400,24 @@ __global__ void __launch_bounds__(DA_THREADS, DA_BLOCKS_PER_SM) k_dense_at_c(GbS
   }
   if (slot_sq >= 0) grid_reduce_publish<0>(s2, slot_sq, st, red_part, tickets);
   if (slot_max >= 0) grid_reduce_publish<1>(gmax, slot_max, st, red_part, tickets);
+}
+
+// the trial's format (st->gfmt: A24 or BF16) picks the body; uniform over the launch
+__global__ void __launch_bounds__(DA_THREADS, DA_BLOCKS_PER_SM) k_dense_at_c(GbState *st, int pf,
+                                                           const unsigned short *__restrict__ Ah,
+                                                           const unsigned char *__restrict__ Al, int lda, int m,
+                                                           int n, const float *__restrict__ r,
+                                                           float *__restrict__ g, const int *__restrict__ bins,
+                                                           float *__restrict__ xt, int slot_sq, int slot_max,
+                                                           float *red_part, unsigned int *tickets) {
+  if (!gb_pred(st, pf)) return;
+  lda = dimv(st, lda);
+  m = dimv(st, m);
+  n = dimv(st, n);
+  if (st->gfmt == GB_GRAD_A24)
+    dense_at_c_body<1>(st, Ah, Al, lda, m, n, r, g, bins, xt, slot_sq, slot_max, red_part, tickets);
+  else
+    dense_at_c_body<0>(st, Ah, Al, lda, m, n, r, g, bins, xt, slot_sq, slot_max, red_part, tickets);
 }
 
 // ------------------------------------------------------------------ DCT
@@ -1280,9 +1293,8 @@ void enq_AT_mask(GbWork &w, cudaStream_t s, const float *r, float *g, float *xt,
   const GbOp &op = w.op;
   const int grid = dense_at_grid(w);
   if (op.gfmt != GB_GRAD_FP32) {
-    auto kern = op.gfmt == GB_GRAD_A24 ? k_dense_at_c<1> : k_dense_at_c<0>;
-    kern<<<grid, DA_THREADS, 0, s>>>(w.st, pf, op.A_hi, op.A_lo, argLDA(w), argM(w), argN(w), r, g, w.bins, xt,
-                                     slot_sq, slot_max, w.red_part, w.tickets);
+    k_dense_at_c<<<grid, DA_THREADS, 0, s>>>(w.st, pf, op.A_hi, op.A_lo, argLDA(w), argM(w), argN(w), r, g, w.bins,
+                                             xt, slot_sq, slot_max, w.red_part, w.tickets);
     return;
   }
   if (op.vec4)
@@ -1345,12 +1357,10 @@ gb_status gb_ops_init_attributes() {
   return GB_OK;
 }
 
-// the compact A^T r operand of the slot's current trial, from its FP32 A
+// the compact A^T r operand of the slot's current trial (its st->gfmt), from its FP32 A
 void enq_split_a(GbWork &w, cudaStream_t s) {
   const GbOp &op = w.op;
-  if (op.gfmt == GB_GRAD_A24)
-    k_split_a<1><<<w.num_sms * 8, 256, 0, s>>>(w.st, op.A, const_cast<unsigned short *>(op.A_hi),
-                                               const_cast<unsigned char *>(op.A_lo));
-  else if (op.gfmt == GB_GRAD_BF16)
-    k_split_a<0><<<w.num_sms * 8, 256, 0, s>>>(w.st, op.A, const_cast<unsigned short *>(op.A_hi), nullptr);
+  if (op.gfmt == GB_GRAD_FP32) return;
+  k_split_a<<<w.num_sms * 8, 256, 0, s>>>(w.st, op.A, const_cast<unsigned short *>(op.A_hi),
+                                          const_cast<unsigned char *>(op.A_lo));
 }

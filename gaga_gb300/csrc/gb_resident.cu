@@ -83,6 +83,7 @@ struct RsParams {
   // batched trials: the A^T r operand (GB_GRAD_*) and, when compact, its per-cluster copies
   // (a_stride entries each, indexed like A)
   int gfmt;
+  const unsigned char *gfmts;  // per trial (device, indexed like n, m, k), or null: gfmt for all
   unsigned short *Ah;
   unsigned char *Al;
   int rec_every;  // batched CGIHT: residual recurrence (GbState::rec_every)
@@ -322,13 +323,13 @@ __device__ void at_own_c(const unsigned short *Ah, const unsigned char *Al, int 
   else at_own_c_t<8, 4, 2, LO>(Ah, Al, lda, q8, c0, nc, r, out);
 }
 
-// A^T r for the trial's own columns in the launch's operand format
+// A^T r for the trial's own columns in the trial's operand format (gfmt)
 template <bool DEEP>
-__device__ __forceinline__ void at_trial(const RsParams &P, const float *A, const unsigned short *Ah,
+__device__ __forceinline__ void at_trial(int gfmt, const float *A, const unsigned short *Ah,
                                          const unsigned char *Al, int lda, int q4, int c0, int nc, const float *r,
                                          float *out) {
-  if (P.gfmt == GB_GRAD_A24) at_own_c<1>(Ah, Al, lda, q4 / 2, c0, nc, r, out);
-  else if (P.gfmt == GB_GRAD_BF16) at_own_c<0>(Ah, Al, lda, q4 / 2, c0, nc, r, out);
+  if (gfmt == GB_GRAD_A24) at_own_c<1>(Ah, Al, lda, q4 / 2, c0, nc, r, out);
+  else if (gfmt == GB_GRAD_BF16) at_own_c<0>(Ah, Al, lda, q4 / 2, c0, nc, r, out);
   else at_own<DEEP>(A, lda, q4, c0, nc, r, out);
 }
 
@@ -712,23 +713,24 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
       batch_trial_fields(st, t, m, n, P.k[t], P.maxiter,
                          IS_CG ? GB_ALG_CGIHT : ALG == RS_HTP ? GB_ALG_HTP : GB_ALG_NIHT);
       st->lda = lda;
-      st->gfmt = P.gfmt;
+      st->gfmt = P.gfmts ? P.gfmts[t] : P.gfmt;
       st->rec_every = P.rec_every;
     }
+    const int gfmt_t = P.gfmts ? P.gfmts[t] : P.gfmt;  // this trial's A^T r operand
     // ---- draw the trial (k_b_gen_A, k_b_gen_x, key bins, y = A x0 of gb_batch.cu)
     for (int col = wid; col < nc; col += RS_WARPS) {
       const int j = c0 + col;
       float *cp = A + (size_t)j * lda;
       gbgen::gen_dense_column(cp, j, m, key, 0u, 1, lane, 32);
       for (int i = m + lane; i < lda; i += 32) cp[i] = 0.0f;
-      if (P.gfmt != GB_GRAD_FP32) {
+      if (gfmt_t != GB_GRAD_FP32) {
         // the compact A^T r operand, from the column this warp just wrote
         __syncwarp();
         const size_t e = (size_t)j * lda;
         for (int i = lane; i < lda; i += 32) {
-          const uint32_t b = round_top_bits(__float_as_uint(cp[i]), P.gfmt == GB_GRAD_A24 ? 8 : 16);
+          const uint32_t b = round_top_bits(__float_as_uint(cp[i]), gfmt_t == GB_GRAD_A24 ? 8 : 16);
           Ah[e + i] = (unsigned short)(b >> 16);
-          if (P.gfmt == GB_GRAD_A24) Al[e + i] = (unsigned char)(b >> 8);
+          if (gfmt_t == GB_GRAD_A24) Al[e + i] = (unsigned char)(b >> 8);
         }
       }
     }
@@ -823,7 +825,7 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
         __syncthreads();
       }
       // x = A^T y ; max|x| ; FindSupportSet ; Threshold
-      at_trial<DEEP>(P, A, Ah, Al, lda, q4, c0, nc, r, x);
+      at_trial<DEEP>(st->gfmt, A, Ah, Al, lda, q4, c0, nc, r, x);
       __syncthreads();
       {
         float mxx = 0.0f;
@@ -959,7 +961,7 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
         }
         __syncthreads();
         // grad = A^T resid ; ||grad on the support||^2 ; max|grad|
-        at_trial<DEEP>(P, A, Ah, Al, lda, q4, c0, nc, r, grad);
+        at_trial<DEEP>(st->gfmt, A, Ah, Al, lda, q4, c0, nc, r, grad);
         __syncthreads();
         {
           const int kb = st->k_bin;
@@ -1109,7 +1111,7 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
         av_rows(x, true, rowp, r, R_RES);
         if (tid == 0) st->red[R_RES] = combine_sum(cl, C, pub, R_RES);
         __syncthreads();
-        at_trial<DEEP>(P, A, Ah, Al, lda, q4, c0, nc, r, gp);
+        at_trial<DEEP>(st->gfmt, A, Ah, Al, lda, q4, c0, nc, r, gp);
         __syncthreads();
         {
           const int kb = st->k_bin;
@@ -1155,7 +1157,7 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
             ctrl_phase(st, C_PUSH_RES, 0);
           }
           __syncthreads();
-          at_trial<DEEP>(P, A, Ah, Al, lda, q4, c0, nc, r, grad);  // grad = A^T r; x_thres = grad on the support
+          at_trial<DEEP>(st->gfmt, A, Ah, Al, lda, q4, c0, nc, r, grad);  // grad = A^T r; x_thres = grad on the support
           __syncthreads();
           const int kb = st->k_bin;
           float sxt = 0.0f;
@@ -1507,6 +1509,7 @@ gb_status gb_resident_enqueue(const GbResidentArgs &a, cudaStream_t s) {
   P.ml_params = a.ml_params;
   P.fb = a.fb;
   P.gfmt = a.gfmt;
+  P.gfmts = a.gfmts;
   P.Ah = R.Ah;
   P.Al = R.Al;
   P.rec_every = a.rec_every;

@@ -30,7 +30,8 @@ struct GbResidentArgs {
   int alg;  // GB_ALG_NIHT, GB_ALG_HTP or GB_ALG_CGIHT
   const float *ml_params;  // CGIHT from the learned warm start (device MLP parameters) or null
   int *fb;                 // with it: per trial, 1 when the warm start was abandoned
-  int gfmt = 0;            // the A^T r operand (GB_GRAD_*)
+  int gfmt = 0;            // the A^T r operand (GB_GRAD_*); the buffers' format (A24 covers both)
+  const unsigned char *gfmts = nullptr;  // per trial (device), or null: gfmt for all
   int rec_every = 0;       // CGIHT residual recurrence (GbState::rec_every)
 };
 

@@ -261,6 +261,8 @@ typedef struct {
                                     (2 bytes), FP32 accumulation.  A x_S, the residual and the
                                     stopping test keep FP32 A, so a solution of y = A x stays a
                                     fixed point; only the gradient directions change. */
+  const unsigned char *grad_formats; /* host array of ntrials entries GB_GRAD_A24 / GB_GRAD_BF16: the
+                                    operand per trial (NULL: grad_format for every trial) */
   int residual_refresh;          /* CGIHT: 0 (the default) computes y - A x at every step, as the
                                     reference does; N > 0 lets a restricted step that follows a
                                     restricted step on the same support update the residual as

@@ -171,3 +171,27 @@ def test_batch_cgiht_residual_recurrence(gb, resident_n):
     assert int((ok0 == ok1).sum()) >= len(n) - 2
     assert 0 < ns1 < len(n)
     assert b1 / max(1, it1.sum()) < 0.97 * b0 / max(1, it0.sum())
+
+
+@pytest.mark.parametrize("resident_n", [0, -1])
+def test_batch_per_trial_operand_formats(gb, resident_n):
+    """Per-trial A^T r operands (grad_formats): every trial's iterations and error equal its
+    result in the run where all trials use its format (trials never share reductions)."""
+    n, m, k, tid = pick([1024, 2048, 4096], 24)
+    fmts = np.where(np.arange(len(n)) % 3 == 0, "a24", "bf16")
+    res = {}
+    for f in ("a24", "bf16"):
+        res[f] = gb.solve_batch(n, m, k, SEED, tid, alg="CGIHT", tol_rel=1e-4, maxiter=1000, resident_n=resident_n,
+                                grad_format=f)
+    ns, it, err, ok = gb.solve_batch(n, m, k, SEED, tid, alg="CGIHT", tol_rel=1e-4, maxiter=1000,
+                                     resident_n=resident_n, grad_format="a24", grad_formats=fmts)
+    for i, f in enumerate(fmts):
+        assert it[i] == res[f][1][i] and err[i] == res[f][2][i], (i, f)
+
+
+def test_batch_per_trial_operand_formats_rejected(gb):
+    from gaga_gb300 import _lib
+
+    n, m, k, tid = pick([1024], 2)
+    with pytest.raises(_lib.GagaError):
+        gb.solve_batch(n, m, k, SEED, tid, alg="CGIHT", tol_rel=1e-4, maxiter=100, grad_formats=["a24", "fp32"])

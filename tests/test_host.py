@@ -240,3 +240,22 @@ def test_mex_shim_builds_and_rejects_bad_calls(gb):
         L.gbmx_clear_error()
         outs = rg.call(L, 2, rg.gen_args(L, "NIHT", y, np.ones((8, 16), np.float32), 2))
         assert all(o is None for o in outs) and b"usage" in L.gbmx_last_error()
+
+
+def test_transition_operand_policy():
+    """24-bit operand within the band around rho*(delta), BF16 elsewhere; rho* from verdicts
+    is the smallest 0.02-grid rho where fewer than half recover."""
+    import numpy as np
+
+    from gaga_gb300 import transition
+
+    n = np.full(5, 1000)
+    m = np.full(5, 500)  # delta 0.5: rho* = 0.32
+    k = np.array([50, 120, 160, 200, 240])  # rho 0.10, 0.24, 0.32, 0.40, 0.48
+    assert list(transition.operand_formats(n, m, k, band=0.08)) == ["bf16", "a24", "a24", "a24", "bf16"]
+    rho = np.round(np.arange(0.02, 0.52, 0.02), 2)
+    nn = np.full(len(rho), 1000)
+    mm = np.full(len(rho), 500)
+    kk = np.round(rho * 500).astype(int)
+    ok = (rho < 0.3).astype(int)
+    assert transition.rho_star_from_verdicts(nn, mm, kk, ok) == {0.5: 0.3}
