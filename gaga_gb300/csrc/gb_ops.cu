@@ -1174,12 +1174,24 @@ static int dc_ept() {
   static const int e = (getenv("GB_CS_DCT_EPT") && atoi(getenv("GB_CS_DCT_EPT")) == 4) ? 4 : 8;
   return e;
 }
-static int dc_threads(int l, int ept) {
-  const int T = (1 << l) / ept;  // threads per sequence (l >= 3)
-  return T > DC_THREADS ? T : DC_THREADS;
+// threads per CTA of the half-length transform's passes: whole sequences, at least 256 for
+// the forward passes and 512 for the transpose's (GB_CS_DCT_CTA=128/256/512 sets both).
+// Measured at n = 2^20 / 2^22, cold L2: A 29.2 / 74.3 us at 256 against 29.9 / 78.4 at 512;
+// A^T 35.3 / 111.9 at 256 against 33.4 / 103.9 at 512; 128 slower for both.
+static int dc_min_threads(bool inverse) {
+  static const int t = [] {
+    const char *e = getenv("GB_CS_DCT_CTA");
+    const int v = e ? atoi(e) : 0;
+    return (v == 128 || v == 256 || v == 512) ? v : 0;
+  }();
+  return t ? t : inverse ? 512 : DC_THREADS;
 }
-static size_t dc_smem(int l, int ept) {
-  const int L = 1 << l, B = dc_threads(l, ept) / (L / ept);
+static int dc_threads(int l, int ept, bool inverse) {
+  const int T = (1 << l) / ept;  // threads per sequence (l >= 3)
+  return T > dc_min_threads(inverse) ? T : dc_min_threads(inverse);
+}
+static size_t dc_smem(int l, int ept, bool inverse) {
+  const int L = 1 << l, B = dc_threads(l, ept, inverse) / (L / ept);
   return (size_t)(B * (L + L / 8) + L) * sizeof(float2);
 }
 template <int MODE, int EPT>
@@ -1188,12 +1200,13 @@ static void launch_dct_pass_e(GbWork &w, cudaStream_t s, int pf, const float *vi
   int l1, l2;
   dc_split(w.op.logn, &l1, &l2);
   constexpr bool FIRST = MODE == DC_F1 || MODE == DC_I1;
+  constexpr bool INV = MODE == DC_I1 || MODE == DC_I2;
   const int l = FIRST ? l1 : l2;
-  const int L = 1 << l, thr = dc_threads(l, EPT), B = thr / (L / EPT);
+  const int L = 1 << l, thr = dc_threads(l, EPT, INV), B = thr / (L / EPT);
   const int nseq = 1 << (FIRST ? l2 : l1);
   int blocks = (nseq + B - 1) / B;
   if (blocks > w.num_sms * 8) blocks = w.num_sms * 8;
-  k_dct_pass<MODE, EPT><<<blocks, thr, dc_smem(l, EPT), s>>>(w.st, pf, l1, l2, vin, cin, cout, rout);
+  k_dct_pass<MODE, EPT><<<blocks, thr, dc_smem(l, EPT, INV), s>>>(w.st, pf, l1, l2, vin, cin, cout, rout);
 }
 template <int MODE>
 static void launch_dct_pass(GbWork &w, cudaStream_t s, int pf, const float *vin, const float2 *cin, float2 *cout,
@@ -1206,7 +1219,7 @@ static void launch_dct_pass(GbWork &w, cudaStream_t s, int pf, const float *vin,
   else launch_dct_pass_e<MODE, 4>(w, s, pf, vin, cin, cout, rout);
 }
 
-// A x_S launch shape: row tiles of the (capacity) m times support splits, <= GB_MAXRB CTAs.// A x_S launch shape: row tiles of the (capacity) m times support splits, <= GB_MAXRB CTAs.
+// A x_S launch shape: row tiles of the (capacity) m times support splits, <= GB_MAXRB CTAs.
 // The split count is the smallest that best fills whole waves of the resident CTA slots
 // (blocks per SM of the tile height): a grid of 1.5 waves leaves half the GPU idle in its
 // tail.  share: the launch runs on a share of the SMs beside other launches (the batched
@@ -1345,7 +1358,10 @@ gb_status gb_ops_init_attributes() {
   GB_CUDA_TRY(cudaFuncSetAttribute(k_fft_pass<1, LOAD_CPLX, STORE_MAKHOUL_REAL>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   // the half-length transform: sequences up to 2^12 (n = 2^24 = 2^11 x 2^12 x 2)
-  const int dsm = (int)std::max(dc_smem(12, 8), dc_smem(12, 4));
+  size_t dsm_max = 0;
+  for (int l = 3; l <= 12; ++l)
+    for (int inv = 0; inv < 2; ++inv) dsm_max = std::max({dsm_max, dc_smem(l, 8, inv), dc_smem(l, 4, inv)});
+  const int dsm = (int)dsm_max;
   GB_CUDA_TRY(cudaFuncSetAttribute(k_dct_pass<DC_F1, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm));
   GB_CUDA_TRY(cudaFuncSetAttribute(k_dct_pass<DC_F2, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm));
   GB_CUDA_TRY(cudaFuncSetAttribute(k_dct_pass<DC_I1, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm));
