@@ -35,7 +35,7 @@ __global__ void k_kbin(GbState *st, int pf, const int *__restrict__ counters, in
 __global__ void k_thresh_count(GbState *st, int pf, float *__restrict__ v, const int *__restrict__ bins,
                                const int *__restrict__ bins_prev, int n, int *__restrict__ tile_cnt);
 __global__ void k_compact(GbState *st, int pf, const int *__restrict__ bins, int n, const int *__restrict__ tile_cnt,
-                          int *__restrict__ S);
+                          int *__restrict__ S, unsigned *__restrict__ bm);
 
 namespace {
 
@@ -243,7 +243,7 @@ gb_status build_slot_graph(Engine &E, Slot &S) {
     k_b_ctrl<<<1, 32, 0, s1>>>(w.st, E.d_params, B_X0, 0);
     const int tiles = (w.op.n + GB_TILE - 1) / GB_TILE;
     k_thresh_count<<<tiles, 256, 0, s1>>>(w.st, F_ALWAYS, S.x0, w.bins, nullptr, D_N, w.tile_cnt);
-    k_compact<<<tiles, 256, 0, s1>>>(w.st, F_DOBIN, w.bins, D_N, w.tile_cnt, w.S);
+    k_compact<<<tiles, 256, 0, s1>>>(w.st, F_DOBIN, w.bins, D_N, w.tile_cnt, w.S, nullptr);
     // y = A x0 and ||y||
     enq_A(w, s1, S.x0, w.y, nullptr, R_RES, F_ALWAYS);
     k_b_ctrl<<<1, 32, 0, s1>>>(w.st, E.d_params, B_INIT, 0);

@@ -21,6 +21,7 @@
 #define GB_MAXRB 1024   // max blocks of a reducing kernel
 #define GB_NFLAG 10     // predicate flags
 #define GB_TILE 2048    // elements per block in the ordered compaction
+#define GB_SMV_BM_MAX_N (1 << 19)  // expander A v: largest n whose support bitmap is staged
 #define GB_SEL_BINS 2048  // radix-select digits per pass (11 bits)
 #define GB_NSTAMP 6       // timing variants: stamps per iteration (see k_stamp)
 
@@ -154,6 +155,11 @@ struct GbWork {
   float *am1, *am2;  // FIHT / ALPS / CGIHTprojected: A x_prev, A v (or A p)
   int *bins, *bins_prev, *counters;
   int *S;        // support list (n)
+  // expander, n <= GB_SMV_BM_MAX_N: bitmap of the same support (bit i % 32 of word i / 32),
+  // written with S by k_compact; A v reads it when smv_bm_ok (v supported on S: every
+  // gen / dct / smv algorithm's products, not the expander decoders')
+  unsigned *smv_bm;
+  int smv_bm_ok;
   int *tile_cnt; // per-tile counts for ordered compaction
   float *part;   // dense A x_S partial tiles (av_ntile * av_nsplit * av_rows floats)
   size_t part_cap;

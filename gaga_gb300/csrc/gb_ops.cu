@@ -1082,6 +1082,64 @@ __global__ void __launch_bounds__(SMV_WARPS * 32) k_smv_A(GbState *st, int pf, c
   if (slot >= 0) grid_reduce_publish<0>(acc2, slot, st, red_part, tickets);
 }
 
+// A v for v supported on the solver's support set, whose bitmap (bit i % 32 of word i / 32,
+// nw words) each CTA stages in shared memory: k_smv_A's row groups with 32 warps per CTA,
+// one CTA per SM, and a gather of v only where the column's bit is set.  A skipped product is
+// val * 0 = +-0, which leaves a sum that starts at +0 unchanged, so the rows are the same
+// floats as k_smv_A's.
+#define SMB_THREADS 1024
+template <bool CV>
+__global__ void __launch_bounds__(SMB_THREADS) k_smv_A_bm(GbState *st, int pf, const unsigned *__restrict__ bm, int nw,
+                                                          const int *__restrict__ ptr, const int *__restrict__ col,
+                                                          const float *__restrict__ val, float cval, int m,
+                                                          const float *__restrict__ v, const float *__restrict__ y,
+                                                          float *__restrict__ out, int slot, float *red_part,
+                                                          unsigned int *tickets) {
+  if (!gb_pred(st, pf)) return;
+  extern __shared__ unsigned sbm[];
+  __shared__ float prod[SMB_THREADS / 32][SMV_CHUNK];
+  for (int i = threadIdx.x; i < nw; i += SMB_THREADS) sbm[i] = bm[i];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nwarps = gridDim.x * (SMB_THREADS / 32);
+  float acc2 = 0.0f;
+  for (int r0 = (blockIdx.x * (SMB_THREADS / 32) + wid) * SMV_RPW; r0 < m; r0 += nwarps * SMV_RPW) {
+    const int r = r0 + lane;
+    const bool own = lane < SMV_RPW && r < m;
+    const int lo = own ? ptr[r] : 0, hi = own ? ptr[r + 1] : 0;
+    const int g_lo = __shfl_sync(0xffffffffu, lo, 0);
+    const int g_hi = __shfl_sync(0xffffffffu, hi, min(m - r0, SMV_RPW) - 1);
+    float sum = 0.0f;
+    for (int c0 = g_lo; c0 < g_hi; c0 += SMV_CHUNK) {
+      const int cn = min(SMV_CHUNK, g_hi - c0);
+      int ci[SMV_CHUNK / 32];
+      float cv[SMV_CHUNK / 32], xv[SMV_CHUNK / 32];
+#pragma unroll
+      for (int u = 0; u < SMV_CHUNK / 32; ++u) {
+        const int t = lane + 32 * u;
+        ci[u] = t < cn ? col[c0 + t] : 0;
+        cv[u] = CV ? cval : (t < cn ? val[c0 + t] : 0.0f);
+      }
+#pragma unroll
+      for (int u = 0; u < SMV_CHUNK / 32; ++u)
+        xv[u] = (lane + 32 * u < cn && ((sbm[ci[u] >> 5] >> (ci[u] & 31)) & 1u)) ? v[ci[u]] : 0.0f;
+#pragma unroll
+      for (int u = 0; u < SMV_CHUNK / 32; ++u)
+        if (lane + 32 * u < cn) prod[wid][lane + 32 * u] = __fmul_rn(cv[u], xv[u]);
+      __syncwarp();
+      const int a = max(lo, c0), b = min(hi, c0 + cn);
+      for (int e = a; e < b; ++e) sum = __fadd_rn(sum, prod[wid][e - c0]);
+      __syncwarp();
+    }
+    if (own) {
+      const float o = y ? __fsub_rn(y[r], sum) : sum;
+      out[r] = o;
+      acc2 = fmaf(o, o, acc2);
+    }
+  }
+  if (slot >= 0) grid_reduce_publish<0>(acc2, slot, st, red_part, tickets);
+}
+
 // A^T r over the column-grouped layout: one thread per column, its d entries summed in
 // order.  For d <= MAXD the d row indices (and values) are loaded first and the d gathers
 // of r are then all in flight together, so a column costs two dependent memory trips, not
@@ -1276,6 +1334,14 @@ void enq_A(GbWork &w, cudaStream_t s, const float *v, float *out, const float *y
     // one resident wave, at most GB_MAXRB CTAs (the grid reduction)
     int blocks = (op.m + SMV_RPW * SMV_WARPS - 1) / (SMV_RPW * SMV_WARPS);
     blocks = std::min(std::min(blocks, GB_MAXRB), smv_a_blocks_per_sm() * w.num_sms);
+    if (w.smv_bm && w.smv_bm_ok) {
+      const int nw = (op.n + 31) / 32;
+      const int grid = std::min(w.num_sms, std::max(1, (op.m + SMV_RPW * 32 - 1) / (SMV_RPW * 32)));
+      auto kb = op.smv_cv ? k_smv_A_bm<true> : k_smv_A_bm<false>;
+      kb<<<grid, SMB_THREADS, nw * sizeof(unsigned), s>>>(w.st, pf, w.smv_bm, nw, op.csr_ptr, op.csr_col, op.csr_val,
+                                                        op.smv_cval, op.m, v, y, out, slot, w.red_part, w.tickets);
+      return;
+    }
     auto kern = op.smv_cv ? k_smv_A<true> : k_smv_A<false>;
     kern<<<std::max(blocks, 1), SMV_WARPS * 32, 0, s>>>(w.st, pf, op.csr_ptr, op.csr_col, op.csr_val, op.smv_cval, op.m,
                                                       v, y, out, slot, w.red_part, w.tickets);
@@ -1357,6 +1423,10 @@ gb_status gb_ops_init_attributes() {
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   GB_CUDA_TRY(cudaFuncSetAttribute(k_fft_pass<1, LOAD_CPLX, STORE_MAKHOUL_REAL>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  // the expander's support bitmap (up to 2^19 columns)
+  const int bms = (GB_SMV_BM_MAX_N / 32) * (int)sizeof(unsigned);
+  GB_CUDA_TRY(cudaFuncSetAttribute(k_smv_A_bm<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bms));
+  GB_CUDA_TRY(cudaFuncSetAttribute(k_smv_A_bm<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bms));
   // the half-length transform: sequences up to 2^12 (n = 2^24 = 2^11 x 2^12 x 2)
   size_t dsm_max = 0;
   for (int l = 3; l <= 12; ++l)

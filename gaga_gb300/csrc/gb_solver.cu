@@ -516,9 +516,10 @@ __global__ void __launch_bounds__(256) k_thresh_count(GbState *st, int pf, float
   if (bins_prev && __syncthreads_or(changed) && threadIdx.x == 0) atomicOr(&st->changed, 1);
 }
 
-// ordered compaction: S = ascending { i : bin_i <= k_bin }
+// ordered compaction: S = ascending { i : bin_i <= k_bin }; with bm, the same set as a bitmap
 __global__ void __launch_bounds__(256) k_compact(GbState *st, int pf, const int *__restrict__ bins, int n,
-                                                 const int *__restrict__ tile_cnt, int *__restrict__ S) {
+                                                 const int *__restrict__ tile_cnt, int *__restrict__ S,
+                                                 unsigned *__restrict__ bm) {
   if (!gb_pred(st, pf)) return;
   n = dimv(st, n);
   __shared__ float sm[32];
@@ -539,6 +540,7 @@ __global__ void __launch_bounds__(256) k_compact(GbState *st, int pf, const int 
     const bool in = i < n && bins[i] <= kb;
     const unsigned bal = __ballot_sync(0xffffffffu, in);
     if (lane == 0) warp_base[wid] = __popc(bal);
+    if (bm && lane == 0) bm[i >> 5] = bal;  // i - lane is a multiple of 32
     __syncthreads();
     int wb = 0, tot = 0;
     for (int w2 = 0; w2 < 8; ++w2) {
@@ -1068,7 +1070,7 @@ static void enq_support(GbWork &w, cudaStream_t s, int k, bool save_prev) {
   k_kbin<<<1, 1024, 0, s>>>(w.st, F_DOBIN, w.counters, w.dyn ? D_K : k);
   const int tiles = (w.op.n + GB_TILE - 1) / GB_TILE;  // capacity; tiles past n count 0
   k_thresh_count<<<tiles, 256, 0, s>>>(w.st, F_ALWAYS, w.x, w.bins, save_prev ? w.bins_prev : nullptr, n, w.tile_cnt);
-  k_compact<<<tiles, 256, 0, s>>>(w.st, F_DOBIN, w.bins, n, w.tile_cnt, w.S);
+  k_compact<<<tiles, 256, 0, s>>>(w.st, F_DOBIN, w.bins, n, w.tile_cnt, w.S, w.smv_bm);
 }
 
 // supportFlag 2/3: a new T when F_SORT (radix select), the threshold, and for the dense
@@ -1114,7 +1116,7 @@ static void enq_csmpsp_join(SolvePlan &P, cudaStream_t s) {
   const int tiles = (w.op.n + GB_TILE - 1) / GB_TILE;
   k_thresh_count<<<tiles, 256, 0, s>>>(w.st, F_ALWAYS, w.x, w.bins, nullptr, n, w.tile_cnt);
   // the join changes the bins even when the gradient's binning was skipped
-  k_compact<<<tiles, 256, 0, s>>>(w.st, F_ALWAYS, w.bins, n, w.tile_cnt, w.S);
+  k_compact<<<tiles, 256, 0, s>>>(w.st, F_ALWAYS, w.bins, n, w.tile_cnt, w.S, w.smv_bm);
   enq_cg_start(w, s);
 }
 
@@ -1186,7 +1188,8 @@ static void enq_fiht_body(SolvePlan &P, cudaStream_t s, cudaGraphConditionalHand
     enq_ctrl(w, s, C_ALPS_LRESTORE);
     k_flagmask<<<w.red_blocks, 256, 0, s>>>(w.st, F_ALWAYS, vt, w.grad, ex, 2, n);
   }
-  if (w.op.kind == GB_OP_DENSE) enq_support_of_nonzeros(w, s, vt, n);
+  // vt is not on the compacted support: the support the products read becomes vt's
+  if (w.op.kind == GB_OP_DENSE || w.smv_bm_ok) enq_support_of_nonzeros(w, s, vt, n);
   enq_A(w, s, vt, Aex, nullptr, R_AXT, F_ALWAYS);
   k_copy_norm<<<w.red_blocks, 256, 0, s>>>(w.st, F_ALWAYS, vt, nullptr, n, R_XT, -1, w.red_part, w.tickets);
   enq_ctrl(w, s, C_FH_MU);
@@ -1770,6 +1773,10 @@ gb_status gb_run_solver(GbWork &w, int alg, const gb_options &o, int k, cudaStre
   GB_CUDA_TRY(cudaGetLastError());
   SolvePlan P{&w, alg, k, o.num_bins};
   if (o.timing && (alg == GB_ALG_NIHT || alg == GB_ALG_HTP)) P.supp_flag = o.support_flag;
+  // the expander A v may skip the columns outside the support bitmap: every product of these
+  // algorithms is of a vector on the compacted support (as the dense A x_S assumes); the
+  // decoders and the sort-based support (which leaves S alone for the expander) do not use it
+  w.smv_bm_ok = w.smv_bm && !gb_is_ccs(alg) && P.supp_flag < 2;
   static const bool eager = getenv("GB_CS_EAGER") && atoi(getenv("GB_CS_EAGER")) != 0;
   if (eager) return run_eager(P, s);
   // dense NIHT, HTP or CGIHT (plain or learned start): one thread-block cluster runs the
@@ -1884,7 +1891,8 @@ __global__ void __launch_bounds__(256) k_nonzero_count(const float *__restrict__
 }
 
 __global__ void __launch_bounds__(256) k_nonzero_compact(GbState *st, const float *__restrict__ v, int n,
-                                                         const int *__restrict__ tile_cnt, int *__restrict__ S) {
+                                                         const int *__restrict__ tile_cnt, int *__restrict__ S,
+                                                         unsigned *__restrict__ bm) {
   __shared__ float sm[32];
   __shared__ int warp_base[8];
   __shared__ int s_off;
@@ -1901,6 +1909,7 @@ __global__ void __launch_bounds__(256) k_nonzero_compact(GbState *st, const floa
     const bool in = i < n && v[i] != 0.0f;
     const unsigned bal = __ballot_sync(0xffffffffu, in);
     if (lane == 0) warp_base[wid] = __popc(bal);
+    if (bm && lane == 0) bm[i >> 5] = bal;
     __syncthreads();
     int wb = 0, tot = 0;
     for (int w2 = 0; w2 < 8; ++w2) {
@@ -1914,8 +1923,9 @@ __global__ void __launch_bounds__(256) k_nonzero_compact(GbState *st, const floa
   if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) st->s_cnt = running;
 }
 
+// (and the expander's support bitmap when the products read it)
 void enq_support_of_nonzeros(GbWork &w, cudaStream_t s, const float *v, int n) {
   const int tiles = (n + GB_TILE - 1) / GB_TILE;
   k_nonzero_count<<<tiles, 256, 0, s>>>(v, n, w.tile_cnt);
-  k_nonzero_compact<<<tiles, 256, 0, s>>>(w.st, v, n, w.tile_cnt, w.S);
+  k_nonzero_compact<<<tiles, 256, 0, s>>>(w.st, v, n, w.tile_cnt, w.S, w.smv_bm_ok ? w.smv_bm : nullptr);
 }
