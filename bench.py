@@ -401,7 +401,7 @@ def bench_faithful(args, solve_step, pverd, plain_value, n0, m0, k0, t0_):
            "ms_per_step": kms / args.faithful_steps, "vs_plain": value / plain_value if plain_value else None,
            "form": "batched + shared-matrix forms, zero start, %s A^T r operand, residual recurrence every %d"
                    % ({"a24": "24-bit", "transition": "24-bit near the phase transition (|rho - rho*(delta)| <= "
-                       "0.08) and BF16 elsewhere"}[args.faithful_format], args.residual_refresh),
+                       "0.08 (1024/n)^0.3) and BF16 elsewhere"}[args.faithful_format], args.residual_refresh),
            "schedule": {"slots": sched["slots"], "sm_share": sched["sm_share"], "cluster": sched.get("cluster", 0)}}
     if pverd and first is not None and first[0] == pverd["w"]:
         tv = np.asarray(first[1]["verdict_batch"], bool)[pverd["sel"]]

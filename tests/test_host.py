@@ -252,7 +252,13 @@ def test_transition_operand_policy():
     n = np.full(5, 1000)
     m = np.full(5, 500)  # delta 0.5: rho* = 0.32
     k = np.array([50, 120, 160, 200, 240])  # rho 0.10, 0.24, 0.32, 0.40, 0.48
-    assert list(transition.operand_formats(n, m, k, band=0.08)) == ["bf16", "a24", "a24", "a24", "bf16"]
+    assert list(transition.operand_formats(n, m, k, band0=0.08, exp=0.0)) == ["bf16", "a24", "a24", "a24", "bf16"]
+    # the band narrows with n: 0.08 at n = 1024, 0.08 / 2 at n = 1024 * 2^(1 / 0.3)
+    assert abs(float(transition.band(1024)) - 0.08) < 1e-12
+    assert abs(float(transition.band(1024 * 2 ** (1 / 0.3))) - 0.04) < 1e-9
+    nn = np.full(3, 16384)
+    mm = np.full(3, 8192)  # rho* = 0.32, band 0.035
+    assert list(transition.operand_formats(nn, mm, np.array([2130, 2621, 2950]))) == ["bf16", "a24", "bf16"]
     rho = np.round(np.arange(0.02, 0.52, 0.02), 2)
     nn = np.full(len(rho), 1000)
     mm = np.full(len(rho), 500)
