@@ -240,7 +240,8 @@ def bench_ours(args):
             per_trial = transition.operand_formats(n, m, k)
         ns, iters, err, ok = gb.solve_batch(n, m, k, SEED, tid, alg=alg, tol_rel=TOL_REL, maxiter=MAXITER,
                                             slots=schedule["slots"], sm_share=schedule["sm_share"],
-                                            cluster=schedule.get("cluster", 0), learned_params=lp,
+                                            cluster=schedule.get("cluster", 0), av_rows=schedule.get("av_rows", 0),
+                                            learned_params=lp,
                                             grad_format="a24" if per_trial is not None else gfmt,
                                             grad_formats=per_trial, residual_refresh=args.residual_refresh)
         t1 = time.perf_counter()
@@ -315,7 +316,7 @@ def bench_ours(args):
                                                 "r - alpha A p between" % args.residual_refresh)
                        if args.residual_refresh > 0 else "y - A x at every step",
                        "schedule": {"slots": sched["slots"], "sm_share": sched["sm_share"],
-                                    "cluster": sched.get("cluster", 0),
+                                    "cluster": sched.get("cluster", 0), "av_rows": sched.get("av_rows", 128),
                                     "picked_by": "autotune over %d candidates on %d probe trials%s" % (
                                         len(sched["candidates"]), sched["probe_trials"],
                                         " (cached)" if sched.get("cached") else "")},

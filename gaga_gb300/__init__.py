@@ -301,7 +301,7 @@ GRAD_FORMATS = {"fp32": 0, "a24": 1, "bf16": 2}
 
 def solve_batch(n, m, k, seed, trial_ids=None, alg="NIHT", tol_rel=1e-4, maxiter=5000, stream=None,
                 learned_params=None, slots=0, sm_share=0, resident_n=0, cluster=0, grad_format="fp32",
-                residual_refresh=0, grad_formats=None):
+                residual_refresh=0, grad_formats=None, av_rows=0):
     """Batched multi-trial dense form (gb_cs_solve_batch); learned_params (a CUDA tensor of
     MLP parameters, CGIHT only) turns on the learned warm start; slots / sm_share set the
     schedule of the slot graphs (0: automatic; gaga_gb300.autotune picks them by
@@ -311,7 +311,8 @@ def solve_batch(n, m, k, seed, trial_ids=None, alg="NIHT", tol_rel=1e-4, maxiter
     copies of A stream 3 or 2 bytes per entry; A x, the residual and the stopping test keep
     FP32 A); grad_formats (one of "a24" / "bf16" per trial) picks it per trial instead;
     residual_refresh N > 0 (CGIHT) updates the residual of a restricted step on an unchanged
-    support as r - alpha A p, recomputing y - A x every N-th iteration."""
+    support as r - alpha A p, recomputing y - A x every N-th iteration; av_rows (128 or 256,
+    0: 128) is the row tile of the slot graphs' A x_S kernel."""
     L = _lib.load()
     n = np.ascontiguousarray(n, dtype=np.int32)
     m = np.ascontiguousarray(m, dtype=np.int32)
@@ -326,7 +327,7 @@ def solve_batch(n, m, k, seed, trial_ids=None, alg="NIHT", tol_rel=1e-4, maxiter
                    0 if learned_params is None else 1,
                    None if learned_params is None else learned_params.data_ptr(), int(slots), int(sm_share), stream,
                    int(resident_n), int(cluster), GRAD_FORMATS[grad_format],
-                   None if fmts is None else fmts.ctypes.data, int(residual_refresh))
+                   None if fmts is None else fmts.ctypes.data, int(av_rows), int(residual_refresh))
     iters = np.zeros(len(n), dtype=np.int32)
     err = np.zeros(len(n), dtype=np.float32)
     ok = np.zeros(len(n), dtype=np.int32)

@@ -64,7 +64,7 @@ class Batch(C.Structure):
                 ("maxiter", C.c_int), ("use_learned", C.c_int), ("learned_params", C.c_void_p),
                 ("slots", C.c_int), ("sm_share", C.c_int), ("stream", C.c_void_p), ("resident_n", C.c_int),
                 ("cluster", C.c_int), ("grad_format", C.c_int), ("grad_formats", C.c_void_p),
-                ("residual_refresh", C.c_int)]
+                ("av_rows", C.c_int), ("residual_refresh", C.c_int)]
 
 
 class SharedBatch(C.Structure):

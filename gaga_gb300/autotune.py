@@ -24,6 +24,9 @@ SHARE_FRACTIONS = (0.25, 0.5)
 # limit, both take the same time (1998 ms per wave).  A probe holds a quarter of the trials,
 # so the longest trial weighs more there than in a whole wave.
 CLUSTERS = (4, 8)
+# the slot graphs' A x_S row tile, tried at the best schedule (256-row tiles read 1 KB of a
+# column per warp instead of 512 B, with half the tiles and half the resident CTAs)
+AV_ROWS = (128, 256)
 
 
 def _cache_path():
@@ -42,18 +45,18 @@ def _key(alg, n, m, form=""):
 
 def tune_batch(n, m, k, seed, trial_ids=None, alg="NIHT", tol_rel=1e-4, maxiter=5000, stride=4, use_cache=True,
                slots=SLOTS, fractions=SHARE_FRACTIONS, clusters=CLUSTERS, log=None, learned_params=None,
-               grad_format="fp32", residual_refresh=0):
-    """Pick (slots, sm_share, cluster) for solving trials like (n, m, k) with the given
-    form; returns a dict with the choice and the measured device milliseconds of every
-    candidate on the probe."""
+               grad_format="fp32", residual_refresh=0, av_rows_candidates=AV_ROWS):
+    """Pick (slots, sm_share, cluster), then the A x_S row tile, for solving trials like
+    (n, m, k) with the given form; returns a dict with the choice and the measured device
+    milliseconds of every candidate on the probe."""
     import torch
 
     import gaga_gb300 as gb
 
     n, m, k = (np.asarray(a, dtype=np.int32) for a in (n, m, k))
     tid = np.arange(len(n), dtype=np.uint32) if trial_ids is None else np.asarray(trial_ids, dtype=np.uint32)
-    key = _key(alg, n, m, "%s|%s|r%d" % ("learned" if learned_params is not None else "plain", grad_format,
-                                          residual_refresh))
+    key = _key(alg, n, m, "%s|%s|r%d|v2" % ("learned" if learned_params is not None else "plain", grad_format,
+                                             residual_refresh))
     path = _cache_path()
     cache = {}
     if use_cache and os.path.exists(path):
@@ -84,8 +87,28 @@ def tune_batch(n, m, k, seed, trial_ids=None, alg="NIHT", tol_rel=1e-4, maxiter=
                 if log:
                     log(json.dumps(table[-1]))
     best = min(table, key=lambda r: r["ms"])
+    # second stage, at the best schedule: the slot graphs' A x_S row tile (128 or 256 rows)
+    best = dict(best, av_rows=128)
+    if av_rows_candidates:
+        for rows in av_rows_candidates:
+            if rows == 128:
+                continue
+            for rep in range(2):
+                ns, it, err, ok = gb.solve_batch(pn, pm, pk, seed, pt, alg=alg, tol_rel=tol_rel, maxiter=maxiter,
+                                                 slots=best["slots"], sm_share=best["sm_share"],
+                                                 cluster=best["cluster"], learned_params=learned_params,
+                                                 grad_format=grad_format, residual_refresh=residual_refresh,
+                                                 av_rows=rows)
+            _, ms = gb.batch_last_stats()
+            row = {"slots": best["slots"], "sm_share": best["sm_share"], "cluster": best["cluster"], "av_rows": rows,
+                   "ms": ms, "recovered": int(ns)}
+            table.append(row)
+            if log:
+                log(json.dumps(row))
+            if ms < best["ms"]:
+                best = row
     res = {"slots": best["slots"], "sm_share": best["sm_share"], "cluster": best["cluster"],
-           "probe_trials": int(len(probe)), "candidates": table, "key": key}
+           "av_rows": best.get("av_rows", 128), "probe_trials": int(len(probe)), "candidates": table, "key": key}
     if use_cache:
         cache[key] = res
         try:

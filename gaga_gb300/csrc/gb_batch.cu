@@ -180,7 +180,8 @@ struct Slot {
 };
 
 struct Engine {
-  int dev = -1, alg = -1, n_cap = 0, m_cap = 0, t_cap = 0, slots = 0, learned = 0, sm_share = 0, gfmt = 0;
+  int dev = -1, alg = -1, n_cap = 0, m_cap = 0, t_cap = 0, slots = 0, learned = 0, sm_share = 0, gfmt = 0,
+      av_rows = 0;
   float *ml_params = nullptr;  // the warm-start MLP parameters (copied in by every call)
   int *dfb = nullptr;
   unsigned char *dgfmt = nullptr;  // per-trial A^T r operand formats
@@ -278,12 +279,13 @@ gb_status build_slot_graph(Engine &E, Slot &S) {
 }
 
 gb_status setup_engine(Engine &E, int dev, int alg, int n_cap, int m_cap, int T, int slots, int learned,
-                       int sm_share, int gfmt) {
+                       int sm_share, int gfmt, int av_rows) {
   if (E.dev == dev && E.alg == alg && E.n_cap >= n_cap && E.m_cap >= m_cap && E.t_cap >= T && E.slots == slots &&
-      E.learned == learned && E.sm_share == sm_share && E.gfmt == gfmt)
+      E.learned == learned && E.sm_share == sm_share && E.gfmt == gfmt && E.av_rows == av_rows)
     return GB_OK;
   release(E);
   E.gfmt = gfmt;
+  E.av_rows = av_rows;
   E.learned = learned;
   E.sm_share = sm_share;
   E.dev = dev;
@@ -351,7 +353,7 @@ gb_status setup_engine(Engine &E, int dev, int alg, int n_cap, int m_cap, int T,
     for (int **v : {&w.bins, &w.bins_prev, &w.S, &S.hist}) GB_TRY(A((void **)v, (size_t)n_cap * 4));
     GB_TRY(A((void **)&w.counters, (size_t)std::max(n_cap / 20, 1000) * 4));
     GB_TRY(A((void **)&w.tile_cnt, (size_t)((n_cap + GB_TILE - 1) / GB_TILE) * 4));
-    gb_dense_av_shape(m_cap, sm_share, true, &w.av_ntile, &w.av_nsplit, &w.av_rows);
+    gb_dense_av_shape(m_cap, sm_share, true, &w.av_ntile, &w.av_nsplit, &w.av_rows, av_rows);
     w.part_cap = gb_dense_part_floats_av(w.av_ntile, w.av_nsplit, w.av_rows);
     GB_TRY(A((void **)&w.part, w.part_cap * 4));
     GB_TRY(A((void **)&w.av_tickets, (size_t)w.av_ntile * 4));
@@ -416,6 +418,10 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
   }
   if (b->maxiter < 0) {
     gb_set_error_message("maxiter must be >= 0", __FILE__, __LINE__);
+    return GB_BAD_ARG;
+  }
+  if (b->av_rows != 0 && b->av_rows != 128 && b->av_rows != 256) {
+    gb_set_error_message("av_rows: 0, 128 or 256", __FILE__, __LINE__);
     return GB_BAD_ARG;
   }
   if (b->grad_format < GB_GRAD_FP32 || b->grad_format > GB_GRAD_BF16 ||
@@ -492,14 +498,15 @@ extern "C" gb_status gb_cs_solve_batch(const gb_batch *b, int *iters_out, float 
   GB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const int sm_share = b->sm_share > 0 ? std::min(b->sm_share, sms) : std::max(1, sms / 2);
   const bool reuse = E.dev == dev && E.alg == b->alg && E.n_cap >= n_cap && E.m_cap >= m_cap && E.t_cap >= T &&
-                     E.sm_share == sm_share && (b->slots <= 0 || E.slots == b->slots) && E.gfmt == gfmt;
+                     E.sm_share == sm_share && (b->slots <= 0 || E.slots == b->slots) && E.gfmt == gfmt &&
+                     E.av_rows == b->av_rows;
   if (!reuse) {
     release(E);
     size_t free_b = 0, total_b = 0;
     GB_CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
     GB_TRY(setup_engine(E, dev, b->alg, n_cap, m_cap, T,
                         slots_for(n_cap, m_cap, free_b, std::max(T, 16), b->slots, gfmt), learned, sm_share,
-                        gfmt));
+                        gfmt, b->av_rows));
   }
   cudaStream_t s = (cudaStream_t)b->stream;
   // trial table, longest (m*n) first

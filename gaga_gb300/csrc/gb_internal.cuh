@@ -324,7 +324,8 @@ void enq_AT_mask(GbWork &w, cudaStream_t s, const float *r, float *g, float *xt,
 // batched form: the compact A^T r operand (op.gfmt) of the current trial from op.A
 void enq_split_a(GbWork &w, cudaStream_t s);
 // dense A x_S launch shape for (capacity) m and its partial buffer size in floats
-void gb_dense_av_shape(int m, int num_sms, bool share, int *ntile, int *nsplit, int *rows);
+// rows_req 128 / 256 picks the row tile (0: 256 for a whole-GPU launch, 128 on a share of the SMs)
+void gb_dense_av_shape(int m, int num_sms, bool share, int *ntile, int *nsplit, int *rows, int rows_req = 0);
 size_t gb_dense_part_floats_av(int ntile, int nsplit, int rows);
 
 // BF16 TN GEMM with FP32 accumulation (gb_gemm.cu):

@@ -1282,8 +1282,8 @@ static void launch_dct_pass(GbWork &w, cudaStream_t s, int pf, const float *vin,
 // (blocks per SM of the tile height): a grid of 1.5 waves leaves half the GPU idle in its
 // tail.  share: the launch runs on a share of the SMs beside other launches (the batched
 // form's slots), which keeps 128-row tiles and at most 16 splits.
-void gb_dense_av_shape(int m, int num_sms, bool share, int *ntile, int *nsplit, int *rows) {
-  const int R = share ? 1 : 2;
+void gb_dense_av_shape(int m, int num_sms, bool share, int *ntile, int *nsplit, int *rows, int rows_req) {
+  const int R = rows_req == 128 ? 1 : rows_req == 256 ? 2 : share ? 1 : 2;
   const int bps = R == 1 ? DvCfg<1>::BLOCKS_PER_SM : DvCfg<2>::BLOCKS_PER_SM;
   *rows = 128 * R;
   int t = (m + *rows - 1) / *rows;

@@ -263,6 +263,8 @@ typedef struct {
                                     fixed point; only the gradient directions change. */
   const unsigned char *grad_formats; /* host array of ntrials entries GB_GRAD_A24 / GB_GRAD_BF16: the
                                     operand per trial (NULL: grad_format for every trial) */
+  int av_rows;                   /* schedule: row tile of the slot graphs' A x_S kernel, 128 or 256
+                                    rows (0: 128) */
   int residual_refresh;          /* CGIHT: 0 (the default) computes y - A x at every step, as the
                                     reference does; N > 0 lets a restricted step that follows a
                                     restricted step on the same support update the residual as

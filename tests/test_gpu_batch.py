@@ -79,20 +79,21 @@ def test_batch_schedule_and_autotune(gb, tmp_path, monkeypatch):
     k = (m // 20).astype(np.int32)  # rho = 0.05: deep inside the recovery region
     tid = np.arange(len(n), dtype=np.uint32)
     ref = gb.solve_batch(n, m, k, SEED, tid, alg="NIHT", maxiter=1000)
-    for slots, share in ((4, 38), (12, 152)):
+    for slots, share, rows in ((4, 38, 0), (12, 152, 0), (8, 38, 256)):
         got = gb.solve_batch(n, m, k, SEED, tid, alg="NIHT", maxiter=1000, slots=slots, sm_share=share,
-                             resident_n=-1)
+                             resident_n=-1, av_rows=rows)
         assert got[0] == ref[0] == len(n)
     res = autotune.tune_batch(n, m, k, SEED, tid, alg="NIHT", maxiter=1000, stride=2, slots=(4, 8),
                               fractions=(0.5, 1.0), clusters=(4,))
     assert (res["slots"], res["sm_share"]) in {(c["slots"], c["sm_share"]) for c in res["candidates"]}
-    assert len(res["candidates"]) == 4 and not res["cached"]
+    # 2 slot counts x 2 shares x 1 cluster size, then the 256-row A x_S tile at the best
+    assert len(res["candidates"]) == 5 and not res["cached"] and res["av_rows"] in (128, 256)
     again = autotune.tune_batch(n, m, k, SEED, tid, alg="NIHT", maxiter=1000, stride=2, slots=(4, 8),
                                 fractions=(0.5, 1.0), clusters=(4,))
     assert again["cached"] and again["slots"] == res["slots"]
     # CGIHT with the BF16 A^T r operand tunes the resident cluster size too, under its own key
     cg = autotune.tune_batch(n, m, k, SEED, tid, alg="CGIHT", maxiter=1000, stride=2, slots=(4,), fractions=(0.5,),
-                             clusters=(4, 8), grad_format="bf16")
+                             clusters=(4, 8), grad_format="bf16", av_rows_candidates=())
     assert {c["cluster"] for c in cg["candidates"]} == {4, 8} and cg["cluster"] in (4, 8)
     assert cg["key"] != res["key"] and not cg["cached"]
 
