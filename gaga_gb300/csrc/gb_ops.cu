@@ -554,175 +554,6 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft_pass(const GbState *__restr
   }
 }
 
-// ------------------------------------------------------------------ 1024-point FFT pass
-// The same pass for L = 1024 (n1 or n2 = 1024) as a 32 x 32 Cooley-Tukey transform, one warp
-// per sequence: element e = 32 e1 + e2; lane e2 holds x[32 e1 + e2] for e1 < 32 and does a
-// 32-point DFT over e1 in registers, multiplies by exp(-+2 pi i e2 k1 / 1024), passes the
-// 32 x 32 block through padded shared memory (lane k1 then holds the values over e2), and
-// does the second 32-point DFT: lane k1 ends with X[k1 + 32 k2].  One shared round trip per
-// transform instead of ten radix-2 stages.  Loads and stores are the pass's own (Makhoul
-// reorder or frequency weighting in, twiddled transpose or inverse reorder out).
-#define F1K_SEQ 4                    // sequences per CTA (one compute warp each)
-#define F1K_THREADS 256              // all of them load and store
-#define F1K_STRIDE (1024 + 32)       // padded sequence buffer: element i at i + i / 32
-
-__device__ __forceinline__ int f1k_idx(int i) { return i + (i >> 5); }
-
-__host__ __device__ constexpr int brev5(int i) {
-  return ((i & 1) << 4) | ((i & 2) << 2) | (i & 4) | ((i & 8) >> 2) | ((i & 16) >> 4);
-}
-
-// cos and sin of 2 pi j / 32, j < 16 (the 32nd roots of unity, rounded to float)
-__device__ __forceinline__ float cos32(int j) {
-  constexpr float t[16] = {1.0f,           9.807852507e-01f, 9.238795042e-01f, 8.314695954e-01f,
-                           7.071067691e-01f, 5.555702448e-01f, 3.826834261e-01f, 1.950903237e-01f,
-                           0.0f,           -1.950903237e-01f, -3.826834261e-01f, -5.555702448e-01f,
-                           -7.071067691e-01f, -8.314695954e-01f, -9.238795042e-01f, -9.807852507e-01f};
-  return t[j];
-}
-// sin(2 pi j / 32) = cos(2 pi (8 - j) / 32) for j <= 8, cos(2 pi (j - 8) / 32) above
-__device__ __forceinline__ float sin32(int j) { return j == 0 ? 0.0f : cos32(j < 8 ? 8 - j : j - 8); }
-
-// radix-2 stage S (half = 2^(S-1)) of a 32-point DIT transform with exp(sgn 2 pi i j / 32)
-// twiddles; every index and twiddle is a compile-time constant once unrolled, so the
-// products by 1 and by +-i (46 of the 80 butterflies) become moves and sign flips
-template <int S, int INV>
-__device__ __forceinline__ void dft32_stage(float2 (&a)[32]) {
-  constexpr int half = 1 << (S - 1);
-  constexpr float sg = INV ? 1.0f : -1.0f;
-#pragma unroll
-  for (int g = 0; g < 32 / (2 * half); ++g) {
-#pragma unroll
-    for (int p = 0; p < half; ++p) {
-      const int i0 = g * 2 * half + p, i1 = i0 + half;
-      const int j = p << (5 - S);
-      const float2 u = a[i0];
-      float2 v;
-      if (j == 0) {
-        v = a[i1];
-      } else if (j == 8) {
-        v = make_float2(-sg * a[i1].y, sg * a[i1].x);  // times sg * i
-      } else {
-        v = cmul(a[i1], make_float2(cos32(j), sg * sin32(j)));
-      }
-      a[i0] = make_float2(u.x + v.x, u.y + v.y);
-      a[i1] = make_float2(u.x - v.x, u.y - v.y);
-    }
-  }
-}
-
-// 32-point DFT of a[0..31] in place, natural order in and out, exp(sgn 2 pi i jk / 32)
-template <int INV>
-__device__ __forceinline__ void dft32(float2 (&a)[32]) {
-  float2 b[32];
-#pragma unroll
-  for (int i = 0; i < 32; ++i) b[brev5(i)] = a[i];
-  dft32_stage<1, INV>(b);
-  dft32_stage<2, INV>(b);
-  dft32_stage<3, INV>(b);
-  dft32_stage<4, INV>(b);
-  dft32_stage<5, INV>(b);
-#pragma unroll
-  for (int i = 0; i < 32; ++i) a[i] = b[i];
-}
-
-template <int INV, int LOAD, int STORE>
-__global__ void __launch_bounds__(F1K_THREADS) k_fft1024(const GbState *__restrict__ st, int pf, int pass, int log1,
-                                                          int log2, const float *__restrict__ vin,
-                                                          const float2 *__restrict__ cin, float2 *__restrict__ cout,
-                                                          float *__restrict__ rout) {
-  if (!gb_pred(st, pf)) return;
-  __shared__ float2 buf[F1K_SEQ * F1K_STRIDE];
-  __shared__ float2 tw[1024];  // exp(-+2 pi i t / 1024)
-  const int L = 1024, B = F1K_SEQ;
-  const int n1 = 1 << log1, n2 = 1 << log2;
-  const int N = n1 * n2;
-  const int nseq = pass == 1 ? n2 : n1;
-  const float sgn = INV ? 1.0f : -1.0f;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int t = threadIdx.x; t < 1024; t += blockDim.x) tw[t] = cis_pi(sgn, (2.0f * t) / 1024.0f);
-  const float wn0 = sqrtf(1.0f / (float)N), wn = sqrtf(2.0f / (float)N);
-  for (int seq0 = blockIdx.x * B; seq0 < nseq; seq0 += gridDim.x * B) {
-    __syncthreads();
-    // load, natural order (the same index maps as k_fft_pass); a compile-time stride lets
-    // the loop unroll, so a thread's loads are in flight together
-#pragma unroll 8
-    for (int q = threadIdx.x; q < F1K_SEQ * 1024; q += F1K_THREADS) {
-      int b, e;
-      if (pass == 1) { b = q % B; e = q / B; }
-      else { b = q / L; e = q % L; }
-      const int sq = seq0 + b;
-      float2 val = make_float2(0.f, 0.f);
-      if (sq < nseq) {
-        if (pass == 1) {
-          const int idx = e * n2 + sq;
-          if (LOAD == LOAD_MAKHOUL) {
-            const int src = idx < N / 2 ? 2 * idx : 2 * (N - 1 - idx) + 1;
-            val = make_float2(vin[src], 0.f);
-          } else if (LOAD == LOAD_FREQ) {
-            const float xv = vin[idx];
-            if (xv != 0.0f) {
-              const float wgt = idx == 0 ? wn0 : wn;
-              const float2 c = cis_pi(1.0f, (float)idx / (float)(2 * N));
-              val = make_float2(wgt * xv * c.x, wgt * xv * c.y);
-            }
-          } else {
-            val = cin[idx];
-          }
-        } else {
-          val = cin[(size_t)sq * n2 + e];
-        }
-      }
-      buf[b * F1K_STRIDE + f1k_idx(e)] = val;
-    }
-    __syncthreads();
-    // warp w < F1K_SEQ transforms sequence w: 32 x 32
-    if (wid < F1K_SEQ) {
-      float2 *sb = buf + wid * F1K_STRIDE;
-      float2 a[32];
-#pragma unroll
-      for (int e1 = 0; e1 < 32; ++e1) a[e1] = sb[f1k_idx(32 * e1 + lane)];
-      dft32<INV>(a);
-#pragma unroll
-      for (int k1 = 1; k1 < 32; ++k1) a[k1] = cmul(a[k1], tw[(lane * k1) & 1023]);
-      __syncwarp();
-      // lane e2 writes its values over k1 to row k1 (stride 33 float2: distinct banks)
-#pragma unroll
-      for (int k1 = 0; k1 < 32; ++k1) sb[k1 * 33 + lane] = a[k1];
-      __syncwarp();
-#pragma unroll
-      for (int e2 = 0; e2 < 32; ++e2) a[e2] = sb[lane * 33 + e2];
-      dft32<INV>(a);
-      __syncwarp();
-      // X[k1 + 32 k2] back in natural order
-#pragma unroll
-      for (int k2 = 0; k2 < 32; ++k2) sb[f1k_idx(lane + 32 * k2)] = a[k2];
-    }
-    __syncthreads();
-    // store (the same index maps as k_fft_pass)
-#pragma unroll 4
-    for (int q = threadIdx.x; q < F1K_SEQ * 1024; q += F1K_THREADS) {
-      const int b = q % B, e = q / B;
-      const int sq = seq0 + b;
-      if (sq >= nseq) continue;
-      float2 val = buf[b * F1K_STRIDE + f1k_idx(e)];
-      if (pass == 1) {
-        const int prod = (int)(((long long)sq * e) & (N - 1));
-        val = cmul(val, cis_pi(sgn, (2.0f * prod) / (float)N));
-        cout[(size_t)e * n2 + sq] = val;
-      } else {
-        const int kk = sq + n1 * e;
-        if (STORE == STORE_CPLX_NAT) {
-          cout[kk] = val;
-        } else {
-          const int dst = kk < N / 2 ? 2 * kk : 2 * (N - 1 - kk) + 1;
-          rout[dst] = val.x;
-        }
-      }
-    }
-  }
-}
-
 // ------------------------------------------------------------------ half-length DCT
 // For n >= 128 the DCT runs on an M = n/2 point complex transform instead of an n-point
 // one (the input is real): the forward transform packs the Makhoul-reordered signal v as
@@ -1207,12 +1038,6 @@ static void launch_fft(GbWork &w, cudaStream_t s, int pf, int pass, const float 
   const int B = FFT_ELEMS / L;
   int blocks = (nseq + B - 1) / B;
   if (blocks > w.num_sms * 4) blocks = w.num_sms * 4;
-  if (logL == 10) {
-    int b1k = (nseq + F1K_SEQ - 1) / F1K_SEQ;
-    if (b1k > w.num_sms * 4) b1k = w.num_sms * 4;
-    k_fft1024<INV, LOAD, STORE><<<b1k, F1K_THREADS, 0, s>>>(w.st, pf, pass, op.log1, op.log2, vin, cin, cout, rout);
-    return;
-  }
   const int smem = fft_smem(logL);
   k_fft_pass<INV, LOAD, STORE><<<blocks, FFT_THREADS, smem, s>>>(w.st, pf, pass, logL, op.log1, op.log2, vin,
                                                                   cin, cout, rout);
