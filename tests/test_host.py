@@ -265,3 +265,21 @@ def test_transition_operand_policy():
     kk = np.round(rho * 500).astype(int)
     ok = (rho < 0.3).astype(int)
     assert transition.rho_star_from_verdicts(nn, mm, kk, ok) == {0.5: 0.3}
+
+
+def test_sweep_partial_round_spreads_over_the_grid():
+    """3072 independent trials = 2 rounds of the 1125-point grid + 822 points of a third,
+    which the strided order spreads over every n (not the grid's first, small-n points)."""
+    import collections
+
+    import numpy as np
+
+    from gaga_gb300 import sweep
+
+    n, m, k, tid = sweep.sweep_trials(3072)
+    per_n = collections.Counter(n.tolist())
+    assert set(per_n) == set(sweep.N_VALUES)
+    assert max(per_n.values()) - min(per_n.values()) <= 25
+    pts = collections.Counter(zip(n.tolist(), m.tolist(), k.tolist()))
+    assert len(pts) == len(sweep.grid()) and set(pts.values()) <= {2, 3}
+    assert len(set(tid.tolist())) == 3072
