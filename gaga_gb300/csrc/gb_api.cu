@@ -307,7 +307,10 @@ gb_status setup_problem(DeviceBuffers &db, GbWork &w, const gb_problem &p, cudaS
     return bad("unknown operator kind");
   }
   GB_TRY(alloc_work(db, w, op.m, op.n, op.lda, num_bins, maxiter));
-  if (op.kind == GB_OP_DENSE) GB_TRY(db.alloc(&w.part, w.part_cap, false));
+  if (op.kind == GB_OP_DENSE) {
+    GB_TRY(db.alloc(&w.part, 2 * w.part_cap, false));
+    w.part_two = 1;
+  }
   if (op.kind == GB_OP_SMV && op.n <= GB_SMV_BM_MAX_N)  // zero: the empty support of x = 0
     GB_TRY(db.alloc(&w.smv_bm, (size_t)(op.n + GB_TILE - 1) / GB_TILE * (GB_TILE / 32), true));
   if (need_y) {

@@ -355,7 +355,8 @@ gb_status setup_engine(Engine &E, int dev, int alg, int n_cap, int m_cap, int T,
     GB_TRY(A((void **)&w.tile_cnt, (size_t)((n_cap + GB_TILE - 1) / GB_TILE) * 4));
     gb_dense_av_shape(m_cap, sm_share, true, &w.av_ntile, &w.av_nsplit, &w.av_rows, av_rows);
     w.part_cap = gb_dense_part_floats_av(w.av_ntile, w.av_nsplit, w.av_rows);
-    GB_TRY(A((void **)&w.part, w.part_cap * 4));
+    GB_TRY(A((void **)&w.part, 2 * w.part_cap * 4));
+    w.part_two = 1;
     GB_TRY(A((void **)&w.av_tickets, (size_t)w.av_ntile * 4));
     if (learned) {
       w.ml_params = E.ml_params;

@@ -692,8 +692,10 @@ __device__ __forceinline__ void ctrl_phase(GbState *st, int phase, cudaGraphCond
       break;
     case C_CGIHT_STOP:
       if (live) {
+        // passes over A_S: 2 for the unrestricted step (y - A x and A p share one), 2 for the
+        // restricted one, 1 when its residual came from the recurrence
         if (st->op_kind == GB_OP_DENSE)
-          st->bytes += dense_bytes(st, 1, st->flags[F_UCG] ? 3 : st->flags[F_RESR] ? 1 : 2);
+          st->bytes += dense_bytes(st, 1, st->flags[F_RESR] ? 1 : 2);
         const bool was_rcg = st->flags[F_RCG] != 0;
         st->err = st->prev[15];
         finish_iteration(st, 749);

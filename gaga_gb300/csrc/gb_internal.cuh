@@ -163,6 +163,7 @@ struct GbWork {
   int *tile_cnt; // per-tile counts for ordered compaction
   float *part;   // dense A x_S partial tiles (av_ntile * av_nsplit * av_rows floats)
   size_t part_cap;
+  int part_two;  // part holds 2 * part_cap floats: the two-product A x_S (enq_A2) may run
   unsigned int *av_tickets;  // per row tile arrival counters
   int av_ntile, av_nsplit, av_rows;   // A x_S launch shape (row tiles of 128 or 256 rows)
   float *upd;    // l0 updates (n)
@@ -317,6 +318,8 @@ inline int argLDA(const GbWork &w) { return w.dyn ? D_LDA : w.op.lda; }
 // out = A v (v must vanish outside S for the dense operator); with y, out = y - A v;
 // with slot >= 0, st->red[slot] = ||out||^2.  Runs only while flag `pf` is set.
 void enq_A(GbWork &w, cudaStream_t s, const float *v, float *out, const float *y, int slot, int pf);
+void enq_A2(GbWork &w, cudaStream_t s, const float *v, float *out, const float *y, int slot, const float *v2,
+            float *out2, int pf);
 // g = A^T r
 void enq_AT(GbWork &w, cudaStream_t s, const float *r, float *g, int pf);
 // dense only: g = A^T r fused with xt = g on the support, ||xt||^2 and max|g|

@@ -55,14 +55,18 @@ __device__ __forceinline__ float4 ld_stream4(const float *p) {
 // warps take entries w, w+16, ... of each staged chunk.  With more than one split, each CTA
 // publishes its partial tile and the last CTA of the tile to arrive adds the partials in
 // split order (deterministic, no second kernel).
-template <int VEC, int R>
-__global__ void __launch_bounds__(DV_THREADS, DvCfg<R>::BLOCKS_PER_SM) k_dense_av(GbState *st, int pf, const float *__restrict__ A, int lda,
+// NV = 2 also forms out2_i = sum_s A[i, S[s]] v2[S[s]] from the same column loads (the
+// unrestricted CG step's A x and A p over one support): each product is summed in exactly
+// the order of its own NV = 1 launch, so the results are bit-identical to two launches.
+template <int VEC, int R, int NV>
+__global__ void __launch_bounds__(DV_THREADS, DvCfg<R>::BLOCKS_PER_SM / NV) k_dense_av(GbState *st, int pf, const float *__restrict__ A, int lda,
                                                          int m, int ntile_cap, int nsplit, const int *__restrict__ S,
-                                                         const float *__restrict__ v, const float *__restrict__ y,
-                                                         float *__restrict__ out, float *__restrict__ part,
+                                                         const float *__restrict__ v, const float *__restrict__ v2,
+                                                         const float *__restrict__ y, float *__restrict__ out,
+                                                         float *__restrict__ out2, float *__restrict__ part,
                                                          unsigned int *__restrict__ tile_tk, int slot, float *red_part,
                                                          unsigned int *tickets) {
-  constexpr int NA = 4 * R;  // accumulators per lane
+  constexpr int NA = 4 * R;  // accumulators per lane and product
   constexpr int ROWS = DvCfg<R>::ROWS;
   if (!gb_pred(st, pf)) return;
   lda = dimv(st, lda);
@@ -70,7 +74,7 @@ __global__ void __launch_bounds__(DV_THREADS, DvCfg<R>::BLOCKS_PER_SM) k_dense_a
   const int s = st->s_cnt;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   __shared__ int sj[DV_STAGE];
-  __shared__ float sv[DV_STAGE];
+  __shared__ float sv[NV][DV_STAGE];
   __shared__ float red[DV_THREADS / 32][NA][32];
   __shared__ int is_last;
   const int ntile = (m + ROWS - 1) / ROWS;
@@ -86,63 +90,81 @@ __global__ void __launch_bounds__(DV_THREADS, DvCfg<R>::BLOCKS_PER_SM) k_dense_a
     const int r0 = tile * ROWS;
     const int chunk = ((s + nsplit - 1) / nsplit + 15) & ~15;
     const int s_lo = min(s, split * chunk), s_hi = min(s, s_lo + chunk);
-    float a[NA];
+    float a[NV][NA];
 #pragma unroll
-    for (int c = 0; c < NA; ++c) a[c] = 0.0f;
+    for (int u = 0; u < NV; ++u)
+#pragma unroll
+      for (int c = 0; c < NA; ++c) a[u][c] = 0.0f;
     for (int c0 = s_lo; c0 < s_hi; c0 += DV_STAGE) {
       const int cn = min(DV_STAGE, s_hi - c0);
       __syncthreads();
       for (int c = threadIdx.x; c < cn; c += DV_THREADS) {
         const int j = S[c0 + c];
         sj[c] = j;
-        sv[c] = v[j];
+        sv[0][c] = v[j];
+        if (NV == 2) sv[NV - 1][c] = v2[j];
       }
       __syncthreads();
       if (VEC == 4) {
-#pragma unroll DvCfg<R>::UNROLL
+#pragma unroll (DvCfg<R>::UNROLL / NV)
         for (int c = warp; c < cn; c += DV_THREADS / 32) {
           const float *col = A + (size_t)sj[c] * lda + r0;
-          const float vj = sv[c];
 #pragma unroll
           for (int u = 0; u < R; ++u) {
             const int rr = (lane + 32 * u) * 4;
             if (r0 + rr < m) {
               const float4 q = ld_stream4(col + rr);
-              a[4 * u] = fmaf(q.x, vj, a[4 * u]);
-              a[4 * u + 1] = fmaf(q.y, vj, a[4 * u + 1]);
-              a[4 * u + 2] = fmaf(q.z, vj, a[4 * u + 2]);
-              a[4 * u + 3] = fmaf(q.w, vj, a[4 * u + 3]);
+#pragma unroll
+              for (int p = 0; p < NV; ++p) {
+                const float vj = sv[p][c];
+                a[p][4 * u] = fmaf(q.x, vj, a[p][4 * u]);
+                a[p][4 * u + 1] = fmaf(q.y, vj, a[p][4 * u + 1]);
+                a[p][4 * u + 2] = fmaf(q.z, vj, a[p][4 * u + 2]);
+                a[p][4 * u + 3] = fmaf(q.w, vj, a[p][4 * u + 3]);
+              }
             }
           }
         }
       } else {
-        constexpr int U1 = DvCfg<R>::UNROLL / 2;  // scalar loads: half the columns in flight
+        constexpr int U1 = DvCfg<R>::UNROLL / 2 / NV;  // scalar loads: half the columns in flight
 #pragma unroll U1
         for (int c = warp; c < cn; c += DV_THREADS / 32) {
           const float *col = A + (size_t)sj[c] * lda + r0;
-          const float vj = sv[c];
 #pragma unroll
           for (int e = 0; e < NA; ++e)
-            if (r0 + lane + 32 * e < m) a[e] = fmaf(__ldg(col + lane + 32 * e), vj, a[e]);
+            if (r0 + lane + 32 * e < m) {
+              const float q = __ldg(col + lane + 32 * e);
+#pragma unroll
+              for (int p = 0; p < NV; ++p) a[p][e] = fmaf(q, sv[p][c], a[p][e]);
+            }
         }
       }
     }
+    // cross-warp sums, one product at a time through the same shared array
+    float t[NV][NA];
 #pragma unroll
-    for (int c = 0; c < NA; ++c) red[warp][c][lane] = a[c];
-    __syncthreads();
-    float t[NA];
-    if (warp == 0) {
+    for (int p = 0; p < NV; ++p) {
+      if (p > 0) __syncthreads();
 #pragma unroll
-      for (int c = 0; c < NA; ++c) {
-        t[c] = red[0][c][lane];
+      for (int c = 0; c < NA; ++c) red[warp][c][lane] = a[p][c];
+      __syncthreads();
+      if (warp == 0) {
 #pragma unroll
-        for (int w2 = 1; w2 < DV_THREADS / 32; ++w2) t[c] += red[w2][c][lane];
+        for (int c = 0; c < NA; ++c) {
+          t[p][c] = red[0][c][lane];
+#pragma unroll
+          for (int w2 = 1; w2 < DV_THREADS / 32; ++w2) t[p][c] += red[w2][c][lane];
+        }
       }
     }
     if (nsplit > 1) {
+      // partial tile of product p at part[(((tile nsplit + split) NV + p) NA + c) 32 + lane]
       if (warp == 0) {
 #pragma unroll
-        for (int c = 0; c < NA; ++c) part[(((size_t)tile * nsplit + split) * NA + c) * 32 + lane] = t[c];
+        for (int p = 0; p < NV; ++p)
+#pragma unroll
+          for (int c = 0; c < NA; ++c)
+            part[((((size_t)tile * nsplit + split) * NV + p) * NA + c) * 32 + lane] = t[p][c];
       }
       __threadfence();
       __syncthreads();
@@ -153,12 +175,15 @@ __global__ void __launch_bounds__(DV_THREADS, DvCfg<R>::BLOCKS_PER_SM) k_dense_a
       __syncthreads();
       if (is_last && warp == 0) {
         __threadfence();
-        const float *pp = part + (size_t)tile * nsplit * NA * 32 + lane;
+        const float *pp = part + (size_t)tile * nsplit * NV * NA * 32 + lane;
 #pragma unroll
-        for (int c = 0; c < NA; ++c) t[c] = __ldcg(pp + c * 32);
-        for (int q = 1; q < nsplit; ++q) {
+        for (int p = 0; p < NV; ++p) {
 #pragma unroll
-          for (int c = 0; c < NA; ++c) t[c] += __ldcg(pp + ((size_t)q * NA + c) * 32);
+          for (int c = 0; c < NA; ++c) t[p][c] = __ldcg(pp + ((size_t)p * NA + c) * 32);
+          for (int q = 1; q < nsplit; ++q) {
+#pragma unroll
+            for (int c = 0; c < NA; ++c) t[p][c] += __ldcg(pp + (((size_t)q * NV + p) * NA + c) * 32);
+          }
         }
         if (lane == 0) tile_tk[tile] = 0u;
       }
@@ -171,9 +196,10 @@ __global__ void __launch_bounds__(DV_THREADS, DvCfg<R>::BLOCKS_PER_SM) k_dense_a
       for (int c = 0; c < NA; ++c) {
         const int i = r0 + row_of(c);
         if (i < m) {
-          const float o = y ? y[i] - t[c] : t[c];
+          const float o = y ? y[i] - t[0][c] : t[0][c];
           out[i] = o;
           acc2 = fmaf(o, o, acc2);
+          if (NV == 2) out2[i] = t[NV - 1][c];
         }
       }
     }
@@ -1132,14 +1158,26 @@ void gb_dense_av_shape(int m, int num_sms, bool share, int *ntile, int *nsplit, 
 
 size_t gb_dense_part_floats_av(int ntile, int nsplit, int rows) { return (size_t)ntile * nsplit * rows; }
 
+// out = y - A v (||out||^2 into red[slot]) and out2 = A v2 over the same support S in one
+// pass over the support columns (dense operator; w.part holds twice part_cap floats).
+void enq_A2(GbWork &w, cudaStream_t s, const float *v, float *out, const float *y, int slot, const float *v2,
+            float *out2, int pf) {
+  const GbOp &op = w.op;
+  const int grid = w.av_ntile * w.av_nsplit;
+  auto kern = op.vec4 ? (w.av_rows == 256 ? k_dense_av<4, 2, 2> : k_dense_av<4, 1, 2>)
+                      : (w.av_rows == 256 ? k_dense_av<1, 2, 2> : k_dense_av<1, 1, 2>);
+  kern<<<grid, DV_THREADS, 0, s>>>(w.st, pf, op.A, argLDA(w), argM(w), w.av_ntile, w.av_nsplit, w.S, v, v2, y, out,
+                                   out2, w.part, w.av_tickets, slot, w.red_part, w.tickets);
+}
+
 void enq_A(GbWork &w, cudaStream_t s, const float *v, float *out, const float *y, int slot, int pf) {
   const GbOp &op = w.op;
   if (op.kind == GB_OP_DENSE) {
     const int grid = w.av_ntile * w.av_nsplit;
-    auto kern = op.vec4 ? (w.av_rows == 256 ? k_dense_av<4, 2> : k_dense_av<4, 1>)
-                        : (w.av_rows == 256 ? k_dense_av<1, 2> : k_dense_av<1, 1>);
-    kern<<<grid, DV_THREADS, 0, s>>>(w.st, pf, op.A, argLDA(w), argM(w), w.av_ntile, w.av_nsplit, w.S, v, y, out,
-                                     w.part, w.av_tickets, slot, w.red_part, w.tickets);
+    auto kern = op.vec4 ? (w.av_rows == 256 ? k_dense_av<4, 2, 1> : k_dense_av<4, 1, 1>)
+                        : (w.av_rows == 256 ? k_dense_av<1, 2, 1> : k_dense_av<1, 1, 1>);
+    kern<<<grid, DV_THREADS, 0, s>>>(w.st, pf, op.A, argLDA(w), argM(w), w.av_ntile, w.av_nsplit, w.S, v, nullptr, y,
+                                     out, nullptr, w.part, w.av_tickets, slot, w.red_part, w.tickets);
   } else if (op.kind == GB_OP_DCT) {
     int l1, l2;
     if (dc_split(op.logn, &l1, &l2)) {

@@ -336,19 +336,30 @@ __device__ __forceinline__ void at_trial(int gfmt, const float *A, const unsigne
 // part (lda floats) = sum over the CTA's support entries e (ascending) of
 // A[:, c0 + sidx[e]] * v[sidx[e]].  Up to 512 row quads: one pass of the CTA, entries split
 // over P = 512 / TG thread groups whose partial vectors are then summed in group order.
-__device__ void av_own_partial(const float *A, int lda, int q4, int c0, const int *sidx, int s_own,
-                               const float *v, float *part, float4 *gscr) {
-  float4 *part4 = reinterpret_cast<float4 *>(part);
+// NV = 2 also forms part2 from v2 with the same column loads (the unrestricted CG step's
+// A x and A p), each product summed in the order of its own NV = 1 call.
+template <int NV>
+__device__ void av_own_partial_t(const float *A, int lda, int q4, int c0, const int *sidx, int s_own,
+                                 const float *v, const float *v2, float *part, float *part2, float4 *gscr) {
+  float4 *pv[2] = {reinterpret_cast<float4 *>(part), reinterpret_cast<float4 *>(part2)};
+  const float *vv[2] = {v, v2};
   const int tg = q4 >= RS_THREADS ? RS_THREADS : (q4 + 31) / 32 * 32;
   const int P = RS_THREADS / tg;
+  auto fma4 = [](float4 &acc, const float4 &l, float w) {
+    acc.x = fmaf(l.x, w, acc.x); acc.y = fmaf(l.y, w, acc.y);
+    acc.z = fmaf(l.z, w, acc.z); acc.w = fmaf(l.w, w, acc.w);
+  };
   if (P == 1) {
     // rows t, t + 512, t + 1024, t + 1536 (q4 <= 2048)
     const int t = threadIdx.x;
-    float4 acc[4] = {f4zero(), f4zero(), f4zero(), f4zero()};
+    float4 acc[NV][4];
+#pragma unroll
+    for (int p = 0; p < NV; ++p)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[p][q] = f4zero();
     int e = 0;
     for (; e + 1 < s_own; e += 2) {
       const int ca = sidx[e], cb = sidx[e + 1];
-      const float wa = v[ca], wb = v[cb];
       const float4 *aa = reinterpret_cast<const float4 *>(A + (size_t)(c0 + ca) * lda);
       const float4 *ab = reinterpret_cast<const float4 *>(A + (size_t)(c0 + cb) * lda);
       float4 la[4], lb[4];
@@ -359,70 +370,82 @@ __device__ void av_own_partial(const float *A, int lda, int q4, int c0, const in
         lb[q] = i < q4 ? __ldcg(ab + i) : f4zero();
       }
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        acc[q].x = fmaf(la[q].x, wa, acc[q].x); acc[q].y = fmaf(la[q].y, wa, acc[q].y);
-        acc[q].z = fmaf(la[q].z, wa, acc[q].z); acc[q].w = fmaf(la[q].w, wa, acc[q].w);
-        acc[q].x = fmaf(lb[q].x, wb, acc[q].x); acc[q].y = fmaf(lb[q].y, wb, acc[q].y);
-        acc[q].z = fmaf(lb[q].z, wb, acc[q].z); acc[q].w = fmaf(lb[q].w, wb, acc[q].w);
+      for (int p = 0; p < NV; ++p) {
+        const float wa = vv[p][ca], wb = vv[p][cb];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          fma4(acc[p][q], la[q], wa);
+          fma4(acc[p][q], lb[q], wb);
+        }
       }
     }
     if (e < s_own) {
       const int ca = sidx[e];
-      const float wa = v[ca];
       const float4 *aa = reinterpret_cast<const float4 *>(A + (size_t)(c0 + ca) * lda);
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const int i = t + q * RS_THREADS;
         const float4 la = i < q4 ? __ldcg(aa + i) : f4zero();
-        acc[q].x = fmaf(la.x, wa, acc[q].x); acc[q].y = fmaf(la.y, wa, acc[q].y);
-        acc[q].z = fmaf(la.z, wa, acc[q].z); acc[q].w = fmaf(la.w, wa, acc[q].w);
+#pragma unroll
+        for (int p = 0; p < NV; ++p) fma4(acc[p][q], la, vv[p][ca]);
       }
     }
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int i = t + q * RS_THREADS;
-      if (i < q4) part4[i] = acc[q];
-    }
+    for (int p = 0; p < NV; ++p)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int i = t + q * RS_THREADS;
+        if (i < q4) pv[p][i] = acc[p][q];
+      }
   } else {
     // one row quad per thread; group p takes entries p, p + P, ... four at a time
-    const int p = threadIdx.x / tg, t = threadIdx.x % tg;
-    float4 acc = f4zero();
-    if (p < P && t < q4) {
-      int e = p;
+    const int g = threadIdx.x / tg, t = threadIdx.x % tg;
+    float4 acc[NV];
+#pragma unroll
+    for (int p = 0; p < NV; ++p) acc[p] = f4zero();
+    if (g < P && t < q4) {
+      int e = g;
       for (; e + 3 * P < s_own; e += 4 * P) {
         float4 l[4];
-        float w[4];
+        int cc[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-          const int c = sidx[e + u * P];
-          w[u] = v[c];
-          l[u] = __ldcg(reinterpret_cast<const float4 *>(A + (size_t)(c0 + c) * lda) + t);
+          cc[u] = sidx[e + u * P];
+          l[u] = __ldcg(reinterpret_cast<const float4 *>(A + (size_t)(c0 + cc[u]) * lda) + t);
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          acc.x = fmaf(l[u].x, w[u], acc.x); acc.y = fmaf(l[u].y, w[u], acc.y);
-          acc.z = fmaf(l[u].z, w[u], acc.z); acc.w = fmaf(l[u].w, w[u], acc.w);
-        }
+        for (int p = 0; p < NV; ++p)
+#pragma unroll
+          for (int u = 0; u < 4; ++u) fma4(acc[p], l[u], vv[p][cc[u]]);
       }
       for (; e < s_own; e += P) {
         const int c = sidx[e];
-        const float w = v[c];
         const float4 l = __ldcg(reinterpret_cast<const float4 *>(A + (size_t)(c0 + c) * lda) + t);
-        acc.x = fmaf(l.x, w, acc.x); acc.y = fmaf(l.y, w, acc.y);
-        acc.z = fmaf(l.z, w, acc.z); acc.w = fmaf(l.w, w, acc.w);
+#pragma unroll
+        for (int p = 0; p < NV; ++p) fma4(acc[p], l, vv[p][c]);
       }
-      gscr[p * tg + t] = acc;
     }
-    __syncthreads();
-    for (int i = threadIdx.x; i < q4; i += RS_THREADS) {
-      float4 s = gscr[i];
-      for (int pp = 1; pp < P; ++pp) {
-        const float4 g = gscr[pp * tg + i];
-        s.x += g.x; s.y += g.y; s.z += g.z; s.w += g.w;
+    // group partials summed in group order, one product at a time through gscr
+#pragma unroll
+    for (int p = 0; p < NV; ++p) {
+      if (p > 0) __syncthreads();
+      if (g < P && t < q4) gscr[g * tg + t] = acc[p];
+      __syncthreads();
+      for (int i = threadIdx.x; i < q4; i += RS_THREADS) {
+        float4 s = gscr[i];
+        for (int pp = 1; pp < P; ++pp) {
+          const float4 h = gscr[pp * tg + i];
+          s.x += h.x; s.y += h.y; s.z += h.z; s.w += h.w;
+        }
+        pv[p][i] = s;
       }
-      part4[i] = s;
     }
   }
+}
+
+__device__ void av_own_partial(const float *A, int lda, int q4, int c0, const int *sidx, int s_own,
+                               const float *v, float *part, float4 *gscr) {
+  av_own_partial_t<1>(A, lda, q4, c0, sidx, s_own, v, nullptr, part, nullptr, gscr);
 }
 
 // Rows [rr0, rr1) (row quads) of the cluster sum of the CTAs' partials (rank order); with
@@ -1146,8 +1169,21 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
             }
             cl.sync();
             gather_rows(cl, C, q4, RB, rowp, r);
-          } else {
+          } else if (rcg) {
             av_rows(x, true, rowp, r, R_RES);  // r = y - A x_S
+          } else {
+            // unrestricted step: r = y - A x_S and the own rows of A grad_prev_thres from one
+            // pass over the support columns; the second partial sits in r, which the gather
+            // overwrites only after the cluster barrier that ends the reads of it
+            av_own_partial_t<2>(A, lda, q4, c0, sidx, s_own, x, gpt, part, r, gscr);
+            if (tid == 0) ipub[0] = s_own;
+            cl.sync();
+            const float s2 = reduce_rows(cl, C, part, rr0, rr1, ypart, rowp, nullptr);
+            reduce_rows(cl, C, r, rr0, rr1, nullptr, rowa, nullptr);
+            const float b = block_reduce<0>(s2, red32);
+            if (tid == 0) pub[R_RES] = b;
+            cl.sync();
+            gather_rows(cl, C, q4, RB, rowp, r);
           }
           if (tid == 0) {
             st->red[R_RES] = combine_sum(cl, C, pub, R_RES);
@@ -1200,7 +1236,7 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
               const float b = block_reduce<0>(sxt, red32);
               if (tid == 0) pub[R_XT] = b;  // combined with the dot products below
             }
-            av_rows(gpt, false, rowa, nullptr, -1);  // own rows of A grad_prev_thres
+            // (the own rows of A grad_prev_thres came with the residual's pass)
             av_rows(grad, false, rowb, nullptr, -1);  // own rows of A x_thres
             {
               const float4 *a4 = reinterpret_cast<const float4 *>(rowa);

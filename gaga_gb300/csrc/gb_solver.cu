@@ -1506,7 +1506,10 @@ void enq_body(SolvePlan &P, cudaStream_t s1, cudaGraphConditionalHandle h_outer)
     // (batched, rec_every > 0) after a restricted step on an unchanged support: r -= alpha A p
     k_lin<<<w.red_blocks, 256, 0, s1>>>(w.st, F_RESR, w.resid, w.resid, SC_NEG_CG_ALPHA, w.ru, m, nullptr, -1,
                                         R_RES, w.red_part, w.tickets);
-    enq_A(w, s1, w.x, w.ru, w.y, R_RES, F_UCG);
+    // UCG: r = y - A x and A grad_prev_thres share one pass over the support columns
+    const bool two = w.op.kind == GB_OP_DENSE && w.part_two;
+    if (two) enq_A2(w, s1, w.x, w.ru, w.y, R_RES, w.gpt, w.resid, F_UCG);
+    else enq_A(w, s1, w.x, w.ru, w.y, R_RES, F_UCG);
     enq_ctrl(w, s1, C_PUSH_RES);
     // RCG branch
     if (w.op.kind == GB_OP_DENSE) {
@@ -1527,7 +1530,7 @@ void enq_body(SolvePlan &P, cudaStream_t s1, cudaGraphConditionalHandle h_outer)
       enq_AT(w, s1, w.ru, w.grad, F_UCG);
       enq_mask(w, s1, F_UCG, w.grad, w.xt, R_XT, -1);
     }
-    enq_A(w, s1, w.gpt, w.resid, nullptr, -1, F_UCG);
+    if (!two) enq_A(w, s1, w.gpt, w.resid, nullptr, -1, F_UCG);
     enq_A(w, s1, w.xt, w.ru, nullptr, -1, F_UCG);
     k_dot2<<<w.red_blocks, 256, 0, s1>>>(w.st, F_UCG, w.resid, w.ru, R_DOT1, m, w.resid, w.resid, R_DOT2, m,
                                          w.red_part, w.tickets);
