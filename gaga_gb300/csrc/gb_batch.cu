@@ -92,13 +92,34 @@ __global__ void k_b_fetch(GbState *st, const BatchParams *bp, cudaGraphCondition
 }
 
 // A of the current trial: the element stream of k_gen_dense (gb_api.cu) keyed by seed + trial id
-__global__ void k_b_gen_A(const GbState *st, const BatchParams *bp, float *A) {
+// A, and with the trial's compact A^T r operand (st->gfmt A24 / BF16) its high parts (and low
+// bytes) rounded from the drawn values as they are written (rows m..lda-1 of the copy zero)
+__global__ void k_b_gen_A(const GbState *st, const BatchParams *bp, float *A, unsigned short *hi, unsigned char *lo) {
   if (!st->active) return;
   const int m = st->m, n = st->n, lda = st->lda;
   const uint32_t key = trial_key(bp, st);
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-  for (int j = gw; j < n; j += nw) gbgen::gen_dense_column(A + (size_t)j * lda, j, m, key, 0u, 1, lane, 32);
+  const int gfmt = hi ? st->gfmt : GB_GRAD_FP32;
+  if (gfmt == GB_GRAD_FP32) {
+    for (int j = gw; j < n; j += nw) gbgen::gen_dense_column(A + (size_t)j * lda, j, m, key, 0u, 1, lane, 32);
+    return;
+  }
+  const bool has_lo = gfmt == GB_GRAD_A24;
+  for (int j = gw; j < n; j += nw) {
+    const size_t c = (size_t)j * lda;
+    unsigned short *h = hi + c;
+    unsigned char *l = has_lo ? lo + c : nullptr;
+    gbgen::gen_dense_column_emit(A + c, j, m, key, 0u, 1, lane, 32, [&](int i, float a) {
+      const uint32_t b = round_top_bits(__float_as_uint(a), has_lo ? 8 : 16);
+      h[i] = (unsigned short)(b >> 16);
+      if (has_lo) l[i] = (unsigned char)(b >> 8);
+    });
+    for (int i = m + lane; i < lda; i += 32) {
+      h[i] = 0;
+      if (has_lo) l[i] = 0;
+    }
+  }
 }
 
 // x0 values (+-1) and support keys of createVector (GAGA/gaga/createVector.cu:207-300);
@@ -234,8 +255,9 @@ gb_status build_slot_graph(Engine &E, Slot &S) {
   GB_TRY(gb_open_while(s0, s1, h_trial));
   {
     // ---- draw the trial on the device
-    k_b_gen_A<<<w.num_sms * 8, 256, 0, s1>>>(w.st, E.d_params, const_cast<float *>(w.op.A));
-    if (E.gfmt != GB_GRAD_FP32) enq_split_a(w, s1);
+    k_b_gen_A<<<w.num_sms * 8, 256, 0, s1>>>(w.st, E.d_params, const_cast<float *>(w.op.A),
+                                             const_cast<unsigned short *>(w.op.A_hi),
+                                             const_cast<unsigned char *>(w.op.A_lo));
     k_b_gen_x<<<w.red_blocks, 256, 0, s1>>>(w.st, E.d_params, S.x0, w.xt, S.hist, w.red_part, w.tickets);
     k_b_ctrl<<<1, 32, 0, s1>>>(w.st, E.d_params, B_KEYS, 0);
     // support of x0: keys in n linear bins, the top bins holding >= k keys

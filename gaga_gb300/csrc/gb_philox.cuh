@@ -32,9 +32,11 @@ __host__ __device__ inline float u01(uint32_t x) { return ((float)(x >> 8) + 0.5
 
 // Column j of a dense Gaussian matrix (createMeasurements_gen, N(0,1)/sqrt(m)), column-major:
 // element e = j*m + i is lane e%4 of Philox block e/4 (two Box-Muller pairs per block).
-// `lane`/`nlanes` split the column's blocks over cooperating threads.
-__device__ inline void gen_dense_column(float *col, int j, int m, uint32_t key, uint32_t trial, int ens, int lane,
-                                        int nlanes) {
+// `lane`/`nlanes` split the column's blocks over cooperating threads; emit(i, a) also sees
+// every entry a written to col[i] (for copies made from registers as the column is drawn).
+template <class Emit>
+__device__ inline void gen_dense_column_emit(float *col, int j, int m, uint32_t key, uint32_t trial, int ens, int lane,
+                                             int nlanes, Emit &&emit) {
   const float scale = 1.0f / sqrtf((float)m);
   const uint64_t e0 = (uint64_t)j * (uint64_t)m, e1 = e0 + (uint64_t)m;
   for (uint64_t g = (e0 >> 2) + lane; g < ((e1 + 3) >> 2); g += nlanes) {
@@ -54,9 +56,18 @@ __device__ inline void gen_dense_column(float *col, int j, int m, uint32_t key, 
     }
     for (int t = 0; t < 4; ++t) {
       const uint64_t e = g * 4 + t;
-      if (e >= e0 && e < e1) col[e - e0] = v[t] * scale;
+      if (e >= e0 && e < e1) {
+        const float a = v[t] * scale;
+        col[e - e0] = a;
+        emit((int)(e - e0), a);
+      }
     }
   }
+}
+
+__device__ inline void gen_dense_column(float *col, int j, int m, uint32_t key, uint32_t trial, int ens, int lane,
+                                        int nlanes) {
+  gen_dense_column_emit(col, j, m, key, trial, ens, lane, nlanes, [](int, float) {});
 }
 
 // element e of a uniform stream

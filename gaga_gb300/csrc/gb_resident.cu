@@ -744,16 +744,23 @@ __global__ void __launch_bounds__(RS_THREADS, 1) k_resident(const RsParams P) {
     for (int col = wid; col < nc; col += RS_WARPS) {
       const int j = c0 + col;
       float *cp = A + (size_t)j * lda;
-      gbgen::gen_dense_column(cp, j, m, key, 0u, 1, lane, 32);
-      for (int i = m + lane; i < lda; i += 32) cp[i] = 0.0f;
-      if (gfmt_t != GB_GRAD_FP32) {
-        // the compact A^T r operand, from the column this warp just wrote
-        __syncwarp();
-        const size_t e = (size_t)j * lda;
-        for (int i = lane; i < lda; i += 32) {
-          const uint32_t b = round_top_bits(__float_as_uint(cp[i]), gfmt_t == GB_GRAD_A24 ? 8 : 16);
-          Ah[e + i] = (unsigned short)(b >> 16);
-          if (gfmt_t == GB_GRAD_A24) Al[e + i] = (unsigned char)(b >> 8);
+      if (gfmt_t == GB_GRAD_FP32) {
+        gbgen::gen_dense_column(cp, j, m, key, 0u, 1, lane, 32);
+        for (int i = m + lane; i < lda; i += 32) cp[i] = 0.0f;
+      } else {
+        // the compact A^T r operand, rounded from the drawn values as they are written
+        const bool has_lo = gfmt_t == GB_GRAD_A24;
+        unsigned short *h = Ah + (size_t)j * lda;
+        unsigned char *l = has_lo ? Al + (size_t)j * lda : nullptr;
+        gbgen::gen_dense_column_emit(cp, j, m, key, 0u, 1, lane, 32, [&](int i, float a) {
+          const uint32_t b = round_top_bits(__float_as_uint(a), has_lo ? 8 : 16);
+          h[i] = (unsigned short)(b >> 16);
+          if (has_lo) l[i] = (unsigned char)(b >> 8);
+        });
+        for (int i = m + lane; i < lda; i += 32) {
+          cp[i] = 0.0f;
+          h[i] = 0;
+          if (has_lo) l[i] = 0;
         }
       }
     }
