@@ -880,6 +880,22 @@ def bench_plain(args, first_step, verdicts_out=None):
                       "time of the 3072 + 1024 sweep" % (len(sel), len(sel2), w)}
 
 
+def shared_part_alone(args):
+    """The shared-matrix trials of one step (step --warmup) alone, in the tuned form (learned
+    start) or, with --shared-zero, from the zero start: device time of each of two calls."""
+    import gaga_gb300 as gb
+
+    lp = None if args.shared_zero else gb.learned.load_weights()
+    ks, first = shared_part(args.warmup)
+    runs = []
+    for _ in range(2):
+        ns, it, err, ok = gb.solve_shared_batch(gb.sweep.SHARED_M, gb.sweep.SHARED_N, ks, SHARED_SEED, tol_rel=TOL_REL,
+                                                maxiter=MAXITER, first_trial=first, alg=ALG, learned_params=lp)
+        runs.append(gb.shared_last_stats()[1])
+    return {"trials": int(len(ks)), "recovered": int(ns), "iterations": int(np.sum(it)), "max_iterations": int(np.max(it)),
+            "ms": runs, "start": "zero" if args.shared_zero else "learned"}
+
+
 def bench_only(args):
     import torch
 
@@ -899,6 +915,8 @@ def bench_only(args):
         out = bench_configs(cpu=not args.no_cpu, only=args.config)
     elif args.only == "resident":
         out = resident_roofline(*peaks(), max_n=args.resident_max_n, sample=args.resident_sample)
+    elif args.only == "shared":
+        out = shared_part_alone(args)
     else:
         w = args.warmup
         n, m, k, tid = wave_arrays(w)
@@ -943,7 +961,8 @@ def main():
                          "unchanged support, r - alpha A p between (0: y - A x at every step)")
     ap.add_argument("--config", default=None,
                     help="--only configs: run the configurations whose name contains this text")
-    ap.add_argument("--only", choices=["matvec", "gemm", "operators", "plain", "learned", "resident", "configs"],
+    ap.add_argument("--shared-zero", action="store_true", help="--only shared: from the zero start")
+    ap.add_argument("--only", choices=["matvec", "gemm", "operators", "plain", "learned", "resident", "configs", "shared"],
                     help="run one measurement alone and print its JSON (for profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
