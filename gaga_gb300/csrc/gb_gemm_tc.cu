@@ -247,6 +247,7 @@ struct TcArgs {
   int cb_split;
   const int *nmap, *ncount;
   int s_max;
+  int split_rows;
   GbGemmWs ws;
 };
 
@@ -271,7 +272,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   int S = 1;
   if (a.s_max > 1) {
     const int tiles = mtiles * ((cnt + TC_BN - 1) / TC_BN);
-    S = max(1, min(min(a.s_max, nkb), a.ws.num_sms / tiles));
+    S = max(1, min(min(a.s_max, nkb), a.ws.num_sms / (a.split_rows ? mtiles : tiles)));
     if (S * tiles * 2 > a.ws.part_tiles) S = 1;  // a 128 x 256 partial is two 128 x 128 units
   }
   if (sp >= S) return;
@@ -531,6 +532,7 @@ gb_status gb_gemm_tc(const GbGemm &g, cudaStream_t s) {
   a.nmap = g.nmap;
   a.ncount = g.ncount;
   a.s_max = 1;
+  a.split_rows = g.split_rows;
   if (g.ws && g.ws->part && g.ws->tickets && (g.M / TC_BM) * (g.N / TC_BN) <= g.ws->ticket_count) {
     a.ws = *g.ws;
     a.s_max = GB_GEMM_SPLIT_MAX;

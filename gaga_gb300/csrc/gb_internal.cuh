@@ -354,6 +354,8 @@ struct GbGemm {
   int cb_split;
   const int *nmap, *ncount;
   const GbGemmWs *ws;
+  int split_rows;  // tcgen05 kernel: the split-K count from the row tiles alone, so that every
+                   // 256-column block of the call is summed as a one-block call would sum it
 };
 gb_status gb_gemm(const GbGemm &g, cudaStream_t s);
 // tcgen05 + TMA kernel (gb_gemm_tc.cu): M % 128, N % 256, K % 64; and its error word

@@ -21,7 +21,7 @@
 // way, with four products per pass: the residual R and G = A^T R for every active trial,
 // then Q = A p for the direction on the support (the restricted-CG branch's new direction,
 // the unrestricted branch's previous one) and, for the trials in the unrestricted branch
-// only, Q2 = A g_S (functions.cu:1004-1220).  With the learned warm start the prologue
+// only, Q2 = A g_S (functions.cu:1004-1220); Q and Q2 are one GEMM over both trial lists.  With the learned warm start the prologue
 // starts each trial from H_k(w . A^T y) (w from the per-coordinate network, gb_mlp.cuh);
 // a trial that gives it up after 10 iterations is restarted inside the loop from the plain
 // start H_k(A^T y), its iterations added.
@@ -67,12 +67,14 @@ struct ShDev {
   const float *ml;          // CGIHT: learned warm start's network parameters (null: plain start)
   float *GP, *GPT;          // CGIHT: grad_previous and grad_prev_thres (Tp x n)
   float *G0;                // CGIHT with the learned start: A^T y, the plain restart's start
-  float *Q2;                // CGIHT: A g_S of the unrestricted-branch trials (Tp x m)
-  __nv_bfloat16 *XT2;       // its BF16 operand (Tp x kq)
+  float *Q2;                // CGIHT: A g_S of the unrestricted-branch trials (Tp x m, = Q + Tp m)
+  __nv_bfloat16 *XT2;       // its BF16 operand (Tp x kq, = XTbf + Tp kq)
   int *bins_prev;           // CGIHT: bins before this pass's binning (support evolution)
   GbState *st0;             // CGIHT with the learned start: each trial's plain initial state
   int *act_q, *act_q_cnt;   // CGIHT: trials whose pass runs the direction product
   int *act_u, *act_u_cnt;   // CGIHT: the unrestricted-branch trials among them
+  int *act_qu, *act_qu_cnt; // CGIHT: act_q, then act_u + Tp (rows of Q2 / XT2 past Q / XTbf):
+                            // Q = A p and Q2 = A g_S as one GEMM
   int *fallbacks;           // CGIHT: trials restarted from the plain start
   int *iters;
   float *err;
@@ -876,6 +878,10 @@ __global__ void __launch_bounds__(1024) k_sh_list(ShDev d, int which, int *passe
       cta_list(T, [&](int t) { return d.st[t].active != 0 && d.st[t].fell_back != 1; }, d.act_q, d.act_q_cnt);
       cta_list(T, [&](int t) { return d.st[t].active != 0 && d.st[t].fell_back != 1 && d.st[t].flags[F_UCG] != 0; },
                d.act_u, d.act_u_cnt);
+      __syncthreads();
+      const int cq = *d.act_q_cnt, cu = *d.act_u_cnt;
+      for (int i = threadIdx.x; i < cq + cu; i += blockDim.x) d.act_qu[i] = i < cq ? d.act_q[i] : d.act_u[i - cq] + d.Tp;
+      if (threadIdx.x == 0) *d.act_qu_cnt = cq + cu;
     }
   } else {
     total = cta_list(T, [&](int t) { return d.st[t].flags[F_CG] != 0; }, d.act, d.act_cnt);
@@ -1087,9 +1093,12 @@ extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *ite
   GB_TRY(buf.get(&d.Acat, (size_t)m * 3 * n));
   GB_TRY(buf.get(&d.ATcat, (size_t)n * 3 * m));
   for (float **v : {&d.X0, &d.X, &d.G}) GB_TRY(buf.get(v, (size_t)Tp * n));
-  for (float **v : {&d.Y, &d.R, &d.Q}) GB_TRY(buf.get(v, (size_t)Tp * m));
+  // CGIHT keeps Q2 and XT2 right after Q and XTbf (one GEMM forms both direction products)
+  const size_t qrows = cgiht ? 2 * (size_t)Tp : (size_t)Tp;
+  for (float **v : {&d.Y, &d.R}) GB_TRY(buf.get(v, (size_t)Tp * m));
+  GB_TRY(buf.get(&d.Q, qrows * m));
   GB_TRY(buf.get(&d.Xcat, (size_t)Tp * 3 * n));
-  GB_TRY(buf.get(&d.XTbf, (size_t)Tp * 3 * n));
+  GB_TRY(buf.get(&d.XTbf, qrows * 3 * n));
   GB_TRY(buf.get(&d.Rbf, (size_t)Tp * m));
   GB_TRY(buf.get(&d.bins, (size_t)Tp * n));
   GB_TRY(buf.get(&d.st, (size_t)Tp));
@@ -1104,13 +1113,15 @@ extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *ite
   GB_TRY(buf.get(&d.act_cnt, 1));
   if (cgiht) {
     for (float **v : {&d.GP, &d.GPT}) GB_TRY(buf.get(v, (size_t)Tp * n));
-    GB_TRY(buf.get(&d.Q2, (size_t)Tp * m));
-    GB_TRY(buf.get(&d.XT2, (size_t)Tp * 3 * n));
+    d.Q2 = d.Q + (size_t)Tp * m;
+    d.XT2 = d.XTbf + (size_t)Tp * kq;
     GB_TRY(buf.get(&d.bins_prev, (size_t)Tp * n));
     GB_TRY(buf.get(&d.act_q, Tp));
     GB_TRY(buf.get(&d.act_q_cnt, 1));
     GB_TRY(buf.get(&d.act_u, Tp));
     GB_TRY(buf.get(&d.act_u_cnt, 1));
+    GB_TRY(buf.get(&d.act_qu, 2 * (size_t)Tp));
+    GB_TRY(buf.get(&d.act_qu_cnt, 1));
     GB_TRY(buf.get(&d.fallbacks, 1));
     GB_CUDA_TRY(cudaMemsetAsync(d.fallbacks, 0, sizeof(int), s));
     GB_CUDA_TRY(cudaMemsetAsync(d.bins_prev, 0, sizeof(int) * (size_t)Tp * n, s));
@@ -1128,11 +1139,11 @@ extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *ite
   GB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   GbGemmWs ws = {};
   ws.num_sms = sms;
-  ws.part_tiles = 2 * sms;
+  ws.part_tiles = 4 * sms;  // room for the joined Q / Q2 call's split partials
   ws.ticket_count = (n / 128) * (Tp / 128);
   GB_TRY(buf.get(&ws.part, (size_t)ws.part_tiles * 128 * 128));
   GB_TRY(buf.get(&ws.tickets, ws.ticket_count));
-  ws.gather_elems = (size_t)Tp * 3 * std::max(m, n);  // widest B operand: Tp x 3n
+  ws.gather_elems = qrows * 3 * std::max(m, n);  // widest B operand: Tp x 3n (CGIHT's [p; g_S]: 2 Tp x kq)
   {
     __nv_bfloat16 *gbuf = nullptr;
     GB_TRY(buf.get(&gbuf, ws.gather_elems));
@@ -1141,9 +1152,10 @@ extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *ite
   GB_CUDA_TRY(cudaMemsetAsync(ws.tickets, 0, sizeof(unsigned) * ws.ticket_count, s));
   // Ct[Tp x M] = [Y -] A . B^T over all trials, or over the listed ones (map / count)
   auto gemm_map = [&](const void *A, const void *B, float *C, int M, int K, int lda, int ldb, const float *Y, void *Cb,
-                      int split, const int *map, const int *count, cudaStream_t st) {
+                      int split, const int *map, const int *count, cudaStream_t st, int N = 0) {
     GbGemm g = {};
-    g.A = A; g.B = B; g.Ct = C; g.M = M; g.N = Tp; g.K = K; g.lda = lda; g.ldb = ldb; g.Y = Y; g.Cb = Cb;
+    g.A = A; g.B = B; g.Ct = C; g.M = M; g.N = N > 0 ? N : Tp; g.K = K; g.lda = lda; g.ldb = ldb; g.Y = Y; g.Cb = Cb;
+    g.split_rows = g.N > Tp;  // the joined Q / Q2 call: each block split as its own call would be
     g.cb_split = split;
     if (map) {
       g.nmap = map;
@@ -1200,10 +1212,10 @@ extern "C" gb_status gb_cs_solve_shared_batch(const gb_shared_batch *b, int *ite
       k_sh_step<<<Tp, SH_THREADS, 0, c>>>(d);
     } else {
       k_sc_dir<<<Tp, SH_THREADS, 0, c>>>(d);
+      // Q = A p (act_q) and Q2 = A g_S (act_u) in one GEMM over the concatenated list: while
+      // both fit one 256-column tile, A streams once per pass instead of twice
       if (r == GB_OK)
-        r = gemm_map(d.Acat, d.XTbf, d.Q, m, kq, 3 * n, kq, nullptr, nullptr, 0, d.act_q, d.act_q_cnt, c);
-      if (r == GB_OK)
-        r = gemm_map(d.Acat, d.XT2, d.Q2, m, kq, 3 * n, kq, nullptr, nullptr, 0, d.act_u, d.act_u_cnt, c);
+        r = gemm_map(d.Acat, d.XTbf, d.Q, m, kq, 3 * n, kq, nullptr, nullptr, 0, d.act_qu, d.act_qu_cnt, c, 2 * Tp);
       k_sc_step<<<Tp, SH_THREADS, 0, c>>>(d);
     }
     return r;
