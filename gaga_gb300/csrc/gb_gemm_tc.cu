@@ -151,29 +151,29 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
   return d;
 }
 
-// Instruction descriptor, kind::f16: D FP32, A and B BF16, both K-major, N = 256, M = 128 per
-// CTA (256 for the pair)
+// Instruction descriptor, kind::f16: D FP32, A and B BF16, both K-major, M = 128 per CTA (256
+// for the pair), N = n columns (64, 128 or 256: a multiple of 16 for either M)
 template <int PAIR>
-__host__ __device__ constexpr uint32_t tc_idesc() {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TC_BN >> 3) << 17) |
+__host__ __device__ constexpr uint32_t tc_idesc(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) |
          ((uint32_t)((TC_BM << PAIR) >> 4) << 24);
 }
 
 template <int PAIR>
-__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t accumulate) {
+__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc, uint32_t accumulate) {
   if constexpr (PAIR) {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "setp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
-        "l"(da), "l"(db), "r"(tc_idesc<1>()), "r"(accumulate)
+        "l"(da), "l"(db), "r"(idesc), "r"(accumulate)
         : "memory");
   } else {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "setp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
-        "l"(da), "l"(db), "r"(tc_idesc<0>()), "r"(accumulate)
+        "l"(da), "l"(db), "r"(idesc), "r"(accumulate)
         : "memory");
   }
 }
@@ -278,6 +278,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   if (sp >= S) return;
   const int kb0 = (int)((long long)sp * nkb / S), kb1 = (int)((long long)(sp + 1) * nkb / S);
   const int nk = kb1 - kb0;
+  // MMA width: the tile's live columns rounded up to 64, 128 or 256 (a column map's few live
+  // trials do not pay for a full 256-column product); the pair's two CTAs each hold half of
+  // those columns' B rows at the start of their B buffer
+  const int live = min(TC_BN, cnt - n0);
+  const int nrt = live <= 64 ? 64 : live <= 128 ? 128 : TC_BN;
 
   uint8_t *smem = (uint8_t *)(((uintptr_t)tc_smem_raw + 1023) & ~(uintptr_t)1023);
   if (threadIdx.x == 0) {
@@ -304,7 +309,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // ---------------------------------------------------------------- TMA producer
     if (lane == 0) {
       int issued = 0;
-      const int b_row = n0 + (int)rank * Cfg::B_ROWS;  // the pair: B rows of this CTA's half
+      const int b_row = n0 + (int)rank * (nrt / 2);  // the pair: B rows of this CTA's half
       for (int it = 0; it < nk; ++it) {
         const int s = it % STAGES;
         const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
@@ -350,9 +355,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         tc_fence_after();
         const uint32_t sa = smem_u32(smem + s * Cfg::STAGE_BYTES);
         const uint64_t da = sw128_desc(sa), db = sw128_desc(sa + TC_A_BYTES);
+        const uint32_t idesc = tc_idesc<PAIR>(nrt);
 #pragma unroll
         for (int k = 0; k < TC_BK / 16; ++k)  // 16 BF16 = 32 bytes = +2 in the descriptor
-          umma<PAIR>(tmem, da + 2 * k, db + 2 * k, (it | k) != 0 ? 1u : 0u);
+          umma<PAIR>(tmem, da + 2 * k, db + 2 * k, idesc, (it | k) != 0 ? 1u : 0u);
         umma_commit<PAIR>(&empty_bar[s]);
       }
       umma_commit<PAIR>(&accum_bar);  // also on an abort: completes once every issued MMA has
@@ -371,7 +377,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (ok && S > 1) {
       // publish this split's partial tile: element (row r, column c) at c * 128 + r
       part = a.ws.part + ((size_t)(nti * S + sp) * mtiles + mt) * (TC_BM * TC_BN);
-      for (int c0 = 0; c0 < TC_BN; c0 += 32) {
+      for (int c0 = 0; c0 < nrt; c0 += 32) {
         float v[32];
         tmem_ld32(taddr + c0, v);
 #pragma unroll
@@ -386,7 +392,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       if (do_store) __threadfence();
     }
     if (do_store) {
-      for (int c0 = 0; c0 < TC_BN; c0 += 32) {
+      for (int c0 = 0; c0 < nrt; c0 += 32) {
         // the 32 columns' map entries, then their Y values, all issued before any store (the
         // stores may alias Y, so the compiler would otherwise wait out one load per column)
         int colv[32];
