@@ -11,6 +11,9 @@
 //               barriers (multicast).  Per k-block an SM receives 32 KB instead of 48 KB.
 //   single:     one CTA, tcgen05.mma.cta_group::1 (M = 128, N = 256), 128 x 64 (A) and
 //               256 x 64 (B) boxes in a 4-stage ring of 48 KB stages.
+// With a column map, a tile whose live columns number at most 64 (128) issues MMAs of
+// N = 64 (128): the pair's CTAs load B from the tile's first column plus half that width,
+// and the epilogue reads that many TMEM columns.
 // Roles in each CTA:
 //   warp 0      TMA producer: 128B-swizzled boxes into the ring, completion counted on a
 //               per-stage mbarrier (expect_tx by the issuing CTA of the MMAs)
