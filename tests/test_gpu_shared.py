@@ -215,6 +215,20 @@ def test_shared_cgiht_matches_plain(gb, gbo):
     assert np.median([abs(a - b) for a, b in both]) <= 2
 
 
+def test_shared_cgiht_two_column_blocks(gb, gbo):
+    """200 trials: the direction products of the restricted and unrestricted trials (up to
+    400 columns) span two 256-column blocks of the joined GEMM, each split as a one-block call
+    would be; verdicts against the FP32 single-trial CGIHT as above."""
+    ks = np.round(np.linspace(0.04, 0.5, 200) * 512).astype(np.int32)
+    ns, res = _shared_cgiht_vs_plain(gb, gbo, ks)
+    agree = sum(int(p == s) for p, s, _, _ in res)
+    assert 0 < ns < len(ks)
+    assert agree >= len(ks) - 4, agree
+    both = [(ip, isb) for p, s, ip, isb in res if p and s]
+    assert len(both) > 40
+    assert np.median([abs(a - b) for a, b in both]) <= 2
+
+
 def test_shared_cgiht_learned_warm_start(gb, gbo):
     """The learned warm start in the shared-matrix form: the trained network's start, the
     fallback to the plain start after 10 iterations without progress (counted), verdicts
