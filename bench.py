@@ -880,6 +880,41 @@ def bench_plain(args, first_step, verdicts_out=None):
                       "time of the 3072 + 1024 sweep" % (len(sel), len(sel2), w)}
 
 
+def size_classes(args):
+    """The independent trials of one step (step --warmup) by size class, in the tuned form
+    (learned start, the --grad-format operand) and the faithful form (zero start,
+    transition-aware operand), both with the residual recurrence: device time (best of two
+    calls) and algorithmic operator bytes per second of each class alone and of the whole
+    wave, at the tuned schedule of the bench (--slots / --sm-share / --cluster)."""
+    import gaga_gb300 as gb
+    from gaga_gb300 import transition
+
+    lp = gb.learned.load_weights()
+    n0, m0, k0, t0 = wave_arrays(args.warmup)
+    sel = [("all", n0 > 0), ("n=16384", n0 == 16384), ("n<=8192", n0 <= 8192)]
+    sel += [("n=%d" % v, n0 == v) for v in (1024, 2048, 4096, 8192)]
+    out = {"step": args.warmup, "schedule": {"slots": args.slots, "sm_share": args.sm_share, "cluster": args.cluster}}
+    for form in ("tuned", "faithful"):
+        rows = {}
+        for name, s in sel:
+            n, m, k, tid = n0[s], m0[s], k0[s], t0[s]
+            if form == "tuned":
+                kw = dict(learned_params=lp, grad_format=args.grad_format)
+            else:
+                kw = dict(grad_format="a24", grad_formats=transition.operand_formats(n, m, k))
+            best = None
+            for _ in range(2):
+                ns, it, err, ok = gb.solve_batch(n, m, k, SEED, tid, alg=ALG, tol_rel=TOL_REL, maxiter=MAXITER,
+                                                 slots=args.slots, sm_share=args.sm_share, cluster=args.cluster,
+                                                 residual_refresh=args.residual_refresh, **kw)
+                nb, ms = gb.batch_last_stats()
+                best = (ms, nb) if best is None or ms < best[0] else best
+            rows[name] = {"trials": int(len(n)), "recovered": int(ns), "iterations": int(np.sum(it)),
+                          "max_iterations": int(np.max(it)), "ms": best[0], "gbs": best[1] / best[0] / 1e6}
+        out[form] = rows
+    return out
+
+
 def shared_part_alone(args):
     """The shared-matrix trials of one step (step --warmup) alone, in the tuned form (learned
     start) or, with --shared-zero, from the zero start: device time of each of two calls."""
@@ -917,6 +952,8 @@ def bench_only(args):
         out = resident_roofline(*peaks(), max_n=args.resident_max_n, sample=args.resident_sample)
     elif args.only == "shared":
         out = shared_part_alone(args)
+    elif args.only == "classes":
+        out = size_classes(args)
     else:
         w = args.warmup
         n, m, k, tid = wave_arrays(w)
@@ -962,7 +999,11 @@ def main():
     ap.add_argument("--config", default=None,
                     help="--only configs: run the configurations whose name contains this text")
     ap.add_argument("--shared-zero", action="store_true", help="--only shared: from the zero start")
-    ap.add_argument("--only", choices=["matvec", "gemm", "operators", "plain", "learned", "resident", "configs", "shared"],
+    ap.add_argument("--slots", type=int, default=24, help="--only classes: slot graphs")
+    ap.add_argument("--sm-share", type=int, default=76, help="--only classes: SMs per slot's kernels")
+    ap.add_argument("--cluster", type=int, default=8, help="--only classes: CTAs per resident cluster")
+    ap.add_argument("--only", choices=["matvec", "gemm", "operators", "plain", "learned", "resident", "configs", "shared",
+                                       "classes"],
                     help="run one measurement alone and print its JSON (for profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
