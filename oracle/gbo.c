@@ -632,6 +632,7 @@ int gbo_solve(const gbo_op *op, const float *y, int k, const gbo_opts *o, float 
   memset(&w, 0, sizeof(w));
   w.op = op; w.m = op->m; w.n = op->n; w.k = k; w.y = y; w.x = x;
   int m = op->m, n = op->n;
+  int n_ucg = 0, n_rcg = 0; /* CGIHT's two step kinds, counted for the caller */
   w.xt = (float *)calloc((size_t)n, sizeof(float));
   w.grad = (float *)calloc((size_t)n, sizeof(float));
   w.gp = (float *)calloc((size_t)n, sizeof(float));
@@ -1076,9 +1077,11 @@ int gbo_solve(const gbo_op *op, const float *y, int k, const gbo_opts *o, float 
     int beta_to_zero = 1, supp_change = 1, k_bin_prev = 0;
     while (keep_going(&s, iter, o->maxiter)) {
       float max_change;
-      if (o->restart) max_change = rcg_support_evolution(&w, &mu, beta_to_zero, bs.k_bin);
-      else if (supp_change) max_change = unrestricted_cg(&w, &mu, beta_to_zero, bs.k_bin);
+      const int ucg = !o->restart && supp_change;
+      if (ucg) max_change = unrestricted_cg(&w, &mu, beta_to_zero, bs.k_bin);
       else max_change = rcg_support_evolution(&w, &mu, beta_to_zero, bs.k_bin);
+      n_ucg += ucg;
+      n_rcg += !ucg;
       beta_to_zero = 0;
       if (bs.min_val <= max_change) {
         max_value = gbo_max_magnitude(x, n);
@@ -1111,6 +1114,8 @@ done:
     info->iter = iter;
     info->sum = bs.sum;
     info->k_bin = bs.k_bin;
+    info->ucg_steps = n_ucg;
+    info->rcg_steps = n_rcg;
     memcpy(info->resid_prev, w.prev, sizeof(w.prev));
     /* given-data convRate (GAGA/gaga/gaga_gen.cu:733-741) */
     int temp = iter < 16 ? iter : 16;

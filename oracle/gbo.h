@@ -79,6 +79,7 @@ typedef struct {
   float conv_rate;      /* given-data convRate (GAGA/gaga/gaga_gen.cu:730-743) */
   float resid_prev[16]; /* residNorm_prev at exit */
   int k_bin;
+  int ucg_steps, rcg_steps; /* CGIHT: UnrestrictedCG / RestrictedCGwithSupportEvolution steps */
 } gbo_info;
 
 /* ---------------- random numbers and problem generation ---------------- */

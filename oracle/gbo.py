@@ -39,7 +39,7 @@ class GboOpts(C.Structure):
 
 class GboInfo(C.Structure):
     _fields_ = [("iter", C.c_int), ("sum", C.c_int), ("conv_rate", C.c_float),
-                ("resid_prev", C.c_float * 16), ("k_bin", C.c_int)]
+                ("resid_prev", C.c_float * 16), ("k_bin", C.c_int), ("ucg_steps", C.c_int), ("rcg_steps", C.c_int)]
 
 
 class GboBinState(C.Structure):

@@ -167,3 +167,24 @@ def test_oracle_sequential_decoders(gbo, alg):
     base = alg.replace("_naive", "")
     xb, resb, recb, infob = gbo.seq_decode(base, op, y, ks, 1e-6, 2000)
     assert info.iter == infob.iter and np.array_equal(rec, recb)
+
+
+def test_oracle_counts_cgiht_steps(gbo):
+    """The oracle's CGIHT reports how many of its iterations were unrestricted and restricted
+    CG steps: they add up to the iterations, the first step (restartFlag off) is unrestricted,
+    and with restartFlag on every step is restricted."""
+    import numpy as np
+
+    rng = np.random.default_rng(11)
+    m, n, k = 128, 256, 20
+    A = (rng.standard_normal((m, n)) / np.sqrt(m)).astype(np.float32)
+    x0 = np.zeros(n, np.float32)
+    x0[rng.choice(n, k, replace=False)] = rng.choice([-1.0, 1.0], k)
+    y = (A @ x0).astype(np.float32)
+    op = gbo.Op.dense(np.asfortranarray(A).ravel(order="F"), m, n)
+    tol = 1e-4 * float(np.linalg.norm(y))
+    x, info = gbo.solve("CGIHT", op, y, k, tol, maxiter=500)
+    assert info.iter > 1 and info.ucg_steps + info.rcg_steps == info.iter
+    assert info.ucg_steps >= 1
+    x, info = gbo.solve("CGIHT", op, y, k, tol, maxiter=500, restart=1)
+    assert info.ucg_steps == 0 and info.rcg_steps == info.iter
